@@ -1,0 +1,1217 @@
+/* CPU oracle for the BoomerAMG-preconditioned Krylov path.
+ *
+ * TEST INFRASTRUCTURE ONLY: a plain-C restatement of the reference library's
+ * serial CPU algorithms, used as the parity checker and as the timed CPU
+ * baseline.  The product library never links it.  Every function cites the
+ * reference file:line (paths relative to the reference project's root) whose
+ * behaviour it restates.  Integer results (strength pattern, C/F splitting,
+ * interpolation pattern, coarse-operator pattern) are meant to be identical to
+ * the reference's, and floating-point results are computed with the same
+ * operation order (build with -ffp-contract=off so no a*b+c is fused).
+ */
+#include "amg_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define C_PT   1
+#define F_PT  -1
+#define SF_PT -3
+
+static int g_threads = 1;
+
+void or_set_threads(int nthreads)
+{
+   g_threads = nthreads > 0 ? nthreads : 1;
+#ifdef _OPENMP
+   omp_set_num_threads(g_threads);
+#endif
+}
+
+static void *xmalloc(size_t n) { void *p = malloc(n ? n : 1); if (!p) { abort(); } return p; }
+static void *xcalloc(size_t n, size_t s) { void *p = calloc(n ? n : 1, s ? s : 1); if (!p) { abort(); } return p; }
+
+void or_csr_free(or_csr *A)
+{
+   if (!A) { return; }
+   free(A->i); free(A->j); free(A->v);
+   A->i = NULL; A->j = NULL; A->v = NULL;
+}
+
+void or_default_params(or_amg_params *p)
+{
+   /* defaults of hypre_BoomerAMGCreate, src/parcsr_ls/par_amg.c:162-304, with the
+    * device-path overrides of :306-313 (PMIS, l1-Jacobi) */
+   memset(p, 0, sizeof(*p));
+   p->strong_threshold = 0.25;
+   p->max_row_sum = 0.9;
+   p->trunc_factor = 0.0;
+   p->p_max_elmts = 4;
+   p->interp_type = 6;
+   p->coarsen_type = 8;
+   p->agg_num_levels = 0;
+   p->agg_interp_type = 4;
+   p->num_paths = 1;
+   p->max_levels = 25;
+   p->max_coarse_size = 9;
+   p->relax_down = 18;
+   p->relax_up = 18;
+   p->relax_coarse = 9;
+   p->num_sweeps = 1;
+   p->relax_weight = 1.0;
+   p->cheby_order = 2;
+   p->cheby_fraction = 0.3;
+   p->cheby_scale = 1;
+   p->cheby_eig_est = 10;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Park-Miller minimal standard generator, src/utilities/random.c:25-95      */
+/* ------------------------------------------------------------------------ */
+
+static int pm_next(int seed)
+{
+   /* Schrage's method with a=16807, m=2^31-1, q=127773, r=2836 (random.c:68-82) */
+   int high = seed / 127773;
+   int low = seed % 127773;
+   int test = 16807 * low - 2836 * high;
+   return test > 0 ? test : test + 2147483647;
+}
+
+static int pm_clamp_seed(int seed)
+{
+   /* hypre_SeedRand, random.c:41-54 */
+   if (seed < 1) { return 1; }
+   if (seed >= 2147483647) { return 2147483646; }
+   return seed;
+}
+
+double or_park_miller_nth(int seed, long long k)
+{
+   /* a^k * seed mod m by square-and-multiply; equals k applications of pm_next */
+   unsigned long long m = 2147483647ULL, a = 16807ULL, r = 1ULL, x = (unsigned long long) pm_clamp_seed(seed);
+   long long e = k;
+   while (e > 0) { if (e & 1) { r = (r * a) % m; } a = (a * a) % m; e >>= 1; }
+   return (double) ((r * x) % m) / (double) 2147483647;
+}
+
+void or_rand_uniform(int n, int seed, double *out)
+{
+   /* hypre_SeqVectorSetRandomValues, src/seq_mv/vector.c:615-640 */
+   int s = pm_clamp_seed(seed);
+   for (int i = 0; i < n; i++)
+   {
+      s = pm_next(s);
+      out[i] = 2.0 * ((double) s / (double) 2147483647) - 1.0;
+   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Generators                                                               */
+/* ------------------------------------------------------------------------ */
+
+int or_gen_stencil(int kind, int nx, int ny, int nz, or_csr *A)
+{
+   /* GenerateLaplacian (src/parcsr_ls/par_laplace.c:15, values src/test/ij.c:10454)
+    * and GenerateLaplacian27pt (src/parcsr_ls/par_laplace_27pt.c:15, values
+    * src/test/ij.c:11901): diagonal first, off-diagonals in ascending column order. */
+   long long n = (long long) nx * ny * nz;
+   int maxrow = kind == 27 ? 27 : 7;
+   A->nr = A->nc = (int) n;
+   A->i = xmalloc(sizeof(int) * (n + 1));
+   A->j = xmalloc(sizeof(int) * n * maxrow);
+   A->v = xmalloc(sizeof(double) * n * maxrow);
+   long long cnt = 0;
+   for (int iz = 0; iz < nz; iz++)
+      for (int iy = 0; iy < ny; iy++)
+         for (int ix = 0; ix < nx; ix++)
+         {
+            long long row = ix + (long long) nx * (iy + (long long) ny * iz);
+            A->i[row] = (int) cnt;
+            A->j[cnt] = (int) row; A->v[cnt] = kind == 27 ? 26.0 : 6.0; cnt++;
+            for (int dz = -1; dz <= 1; dz++)
+               for (int dy = -1; dy <= 1; dy++)
+                  for (int dx = -1; dx <= 1; dx++)
+                  {
+                     int m = abs(dx) + abs(dy) + abs(dz);
+                     if (m == 0 || (kind == 7 && m != 1)) { continue; }
+                     int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+                     if (jx < 0 || jy < 0 || jz < 0 || jx >= nx || jy >= ny || jz >= nz) { continue; }
+                     A->j[cnt] = jx + nx * (jy + ny * jz); A->v[cnt] = -1.0; cnt++;
+                  }
+         }
+   A->i[n] = (int) cnt;
+   return 0;
+}
+
+int or_gen_aniso2d(int n, double eps, or_csr *A)
+{
+   /* -eps*u_xx - u_yy on an n x n grid, 5-point, Dirichlet, diagonal first */
+   int N = n * n;
+   A->nr = A->nc = N;
+   A->i = xmalloc(sizeof(int) * (N + 1));
+   A->j = xmalloc(sizeof(int) * N * 5);
+   A->v = xmalloc(sizeof(double) * N * 5);
+   int cnt = 0;
+   for (int iy = 0; iy < n; iy++)
+      for (int ix = 0; ix < n; ix++)
+      {
+         int row = ix + n * iy;
+         A->i[row] = cnt;
+         A->j[cnt] = row; A->v[cnt] = 2.0 * eps + 2.0; cnt++;
+         if (iy > 0) { A->j[cnt] = row - n; A->v[cnt] = -1.0; cnt++; }
+         if (ix > 0) { A->j[cnt] = row - 1; A->v[cnt] = -eps; cnt++; }
+         if (ix < n - 1) { A->j[cnt] = row + 1; A->v[cnt] = -eps; cnt++; }
+         if (iy < n - 1) { A->j[cnt] = row + n; A->v[cnt] = -1.0; cnt++; }
+      }
+   A->i[N] = cnt;
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Strength of connection, hypre_BoomerAMGCreateSHost                        */
+/* src/parcsr_ls/par_strength.c:75-527 (num_functions == 1, offd empty)     */
+/* ------------------------------------------------------------------------ */
+
+int or_strength(const or_csr *A, double theta, double max_row_sum, or_csr *S)
+{
+   int n = A->nr;
+   int *mark = xmalloc(sizeof(int) * (size_t) (A->i[n] > 0 ? A->i[n] : 1));
+   int *cnt = xcalloc(n + 1, sizeof(int));
+   #pragma omp parallel for schedule(static)
+   for (int i = 0; i < n; i++)
+   {
+      int b = A->i[i], e = A->i[i + 1];
+      double diag = A->v[b];                      /* diagonal assumed first, :245 */
+      double row_scale = 0.0, row_sum = diag;
+      if (diag < 0)
+      {
+         for (int k = b + 1; k < e; k++) { row_scale = row_scale > A->v[k] ? row_scale : A->v[k]; row_sum += A->v[k]; }
+      }
+      else
+      {
+         for (int k = b + 1; k < e; k++) { row_scale = row_scale < A->v[k] ? row_scale : A->v[k]; row_sum += A->v[k]; }
+      }
+      int c = 0;
+      mark[b] = 0;
+      if ((fabs(row_sum) > fabs(diag) * max_row_sum) && (max_row_sum < 1.0))
+      {
+         for (int k = b + 1; k < e; k++) { mark[k] = 0; }   /* all weak, :326-340 */
+      }
+      else
+      {
+         double thr = theta * row_scale;
+         for (int k = b + 1; k < e; k++)
+         {
+            int strong = diag < 0 ? !(A->v[k] <= thr) : !(A->v[k] >= thr);
+            mark[k] = strong;
+            c += strong;
+         }
+      }
+      cnt[i + 1] = c;
+   }
+   S->nr = S->nc = n;
+   S->i = xmalloc(sizeof(int) * (n + 1));
+   S->i[0] = 0;
+   for (int i = 0; i < n; i++) { S->i[i + 1] = S->i[i] + cnt[i + 1]; }
+   S->j = xmalloc(sizeof(int) * (size_t) (S->i[n] ? S->i[n] : 1));
+   S->v = NULL;
+   #pragma omp parallel for schedule(static)
+   for (int i = 0; i < n; i++)
+   {
+      int p = S->i[i];
+      for (int k = A->i[i] + 1; k < A->i[i + 1]; k++) { if (mark[k]) { S->j[p++] = A->j[k]; } }
+   }
+   free(mark); free(cnt);
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PMIS, hypre_BoomerAMGCoarsenPMISHost src/parcsr_ls/par_coarsen.c:2094-2806 */
+/* with hypre_BoomerAMGIndepSetInit src/parcsr_ls/par_indepset.c:33-63       */
+/* ------------------------------------------------------------------------ */
+
+int or_pmis(const or_csr *S, int CF_init, int *CF)
+{
+   int n = S->nr;
+   double *measure = xcalloc(n, sizeof(double));
+   int *graph = xmalloc(sizeof(int) * (n ? n : 1));
+   int *graph2 = xmalloc(sizeof(int) * (n ? n : 1));
+   /* measures: column counts of S (:2232-2288) */
+   for (int k = 0; k < S->i[n]; k++) { measure[S->j[k]] += 1.0; }
+   /* plus one Park-Miller draw per row, seed 2747, in row order (par_indepset.c:45-60) */
+   {
+      int s = 2747;
+      for (int i = 0; i < n; i++) { s = pm_next(s); measure[i] += (double) s / (double) 2147483647; }
+   }
+   int gsize = 0;
+   for (int i = 0; i < n; i++)
+   {
+      CF[i] = 0;
+      if (S->i[i + 1] - S->i[i] == 0)
+      {
+         CF[i] = (CF_init == 3 || CF_init == 4) ? C_PT : SF_PT;    /* :2383-2400 */
+         measure[i] = 0;
+      }
+      else { graph[gsize++] = i; }
+   }
+   int iter = 0;
+   while (gsize > 0)
+   {
+      if (!CF_init || iter)
+      {
+         for (int g = 0; g < gsize; g++) { int i = graph[g]; if (measure[i] > 1) { CF[i] = 1; } }
+         for (int g = 0; g < gsize; g++)
+         {
+            int i = graph[g];
+            if (measure[i] > 1)
+            {
+               for (int k = S->i[i]; k < S->i[i + 1]; k++)
+               {
+                  int j = S->j[k];
+                  if (measure[j] > 1)
+                  {
+                     if (measure[i] > measure[j]) { CF[j] = 0; }
+                     else if (measure[j] > measure[i]) { CF[i] = 0; }
+                  }
+               }
+            }
+         }
+      }
+      iter++;
+      for (int g = 0; g < gsize; g++)   /* :2610-2662 */
+      {
+         int i = graph[g];
+         if (measure[i] < 1) { CF[i] = F_PT; }
+         if (CF[i] > 0) { CF[i] = C_PT; }
+         else
+         {
+            for (int k = S->i[i]; k < S->i[i + 1]; k++) { if (CF[S->j[k]] > 0) { CF[i] = F_PT; } }
+         }
+      }
+      int ng = 0;
+      for (int g = 0; g < gsize; g++)
+      {
+         int i = graph[g];
+         if (CF[i] != 0) { measure[i] = 0; } else { graph2[ng++] = i; }
+      }
+      int *t = graph; graph = graph2; graph2 = t;
+      gsize = ng;
+   }
+   free(measure); free(graph); free(graph2);
+   return 0;
+}
+
+int or_coarse_count(int n, const int *CF)
+{
+   /* hypre_BoomerAMGCoarseParms, src/parcsr_ls/par_coarse_parms.c:45-106 */
+   int c = 0;
+   for (int i = 0; i < n; i++) { if (CF[i] == 1) { c++; } }
+   return c;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Extended+i interpolation, hypre_BoomerAMGBuildExtPIInterpHost             */
+/* src/parcsr_ls/par_lr_interp.c:1024-1924 (one process, offd empty)        */
+/* ------------------------------------------------------------------------ */
+
+int or_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
+{
+   int n = A->nr;
+   int *f2c = xmalloc(sizeof(int) * (n ? n : 1));
+   int nc = 0;
+   for (int i = 0; i < n; i++) { f2c[i] = CF[i] >= 0 ? nc++ : -1; }   /* :1261-1266 */
+
+   /* pass 1: row sizes, with a per-row marker (:1267-1380) */
+   int *Pi = xcalloc(n + 1, sizeof(int));
+   int *marker = xmalloc(sizeof(int) * (n ? n : 1));
+   for (int i = 0; i < n; i++) { marker[i] = -1; }
+   for (int i = 0; i < n; i++)
+   {
+      int cnt = 0;
+      if (CF[i] >= 0) { cnt = 1; }
+      else if (CF[i] != SF_PT)
+      {
+         for (int k = S->i[i]; k < S->i[i + 1]; k++)
+         {
+            int i1 = S->j[k];
+            if (CF[i1] >= 0) { if (marker[i1] != i) { marker[i1] = i; cnt++; } }
+            else if (CF[i1] != SF_PT)
+            {
+               for (int kk = S->i[i1]; kk < S->i[i1 + 1]; kk++)
+               {
+                  int k1 = S->j[kk];
+                  if (CF[k1] >= 0 && marker[k1] != i) { marker[k1] = i; cnt++; }
+               }
+            }
+         }
+      }
+      Pi[i + 1] = cnt;
+   }
+   for (int i = 0; i < n; i++) { Pi[i + 1] += Pi[i]; }
+   int nnz = Pi[n];
+   int *Pj = xmalloc(sizeof(int) * (nnz ? nnz : 1));
+   double *Pv = xmalloc(sizeof(double) * (nnz ? nnz : 1));
+
+   /* pass 2: columns in first-discovery order and weights (:1500-1810).
+    * pmark[x] >= row_begin: x is a C column of this row at that position;
+    * pmark[x] == strong_f: x is a strong F neighbour of this row. */
+   int *pmark = xmalloc(sizeof(int) * (n ? n : 1));
+   for (int i = 0; i < n; i++) { pmark[i] = -1; }
+   int strong_f = -2;
+   for (int i = 0; i < n; i++)
+   {
+      int begin = Pi[i], c = begin;
+      if (CF[i] >= 0)
+      {
+         Pj[c] = f2c[i]; Pv[c] = 1.0; c++;
+      }
+      else if (CF[i] != SF_PT)
+      {
+         strong_f--;
+         for (int k = S->i[i]; k < S->i[i + 1]; k++)
+         {
+            int i1 = S->j[k];
+            if (CF[i1] >= 0)
+            {
+               if (pmark[i1] < begin) { pmark[i1] = c; Pj[c] = f2c[i1]; Pv[c] = 0.0; c++; }
+            }
+            else if (CF[i1] != SF_PT)
+            {
+               pmark[i1] = strong_f;
+               for (int kk = S->i[i1]; kk < S->i[i1 + 1]; kk++)
+               {
+                  int k1 = S->j[kk];
+                  if (CF[k1] >= 0 && pmark[k1] < begin) { pmark[k1] = c; Pj[c] = f2c[k1]; Pv[c] = 0.0; c++; }
+               }
+            }
+         }
+         int end = c;
+         double diagonal = A->v[A->i[i]];
+         for (int jj = A->i[i] + 1; jj < A->i[i + 1]; jj++)
+         {
+            int i1 = A->j[jj];
+            if (pmark[i1] >= begin) { Pv[pmark[i1]] += A->v[jj]; }
+            else if (pmark[i1] == strong_f)
+            {
+               double sum = 0.0;
+               int sgn = A->v[A->i[i1]] < 0 ? -1 : 1;
+               for (int jj1 = A->i[i1] + 1; jj1 < A->i[i1 + 1]; jj1++)
+               {
+                  int i2 = A->j[jj1];
+                  if ((pmark[i2] >= begin || i2 == i) && (sgn * A->v[jj1]) < 0) { sum += A->v[jj1]; }
+               }
+               if (sum != 0)
+               {
+                  double distribute = A->v[jj] / sum;
+                  for (int jj1 = A->i[i1] + 1; jj1 < A->i[i1 + 1]; jj1++)
+                  {
+                     int i2 = A->j[jj1];
+                     if (pmark[i2] >= begin && (sgn * A->v[jj1]) < 0) { Pv[pmark[i2]] += distribute * A->v[jj1]; }
+                     if (i2 == i && (sgn * A->v[jj1]) < 0) { diagonal += distribute * A->v[jj1]; }
+                  }
+               }
+               else { diagonal += A->v[jj]; }
+            }
+            else if (CF[i1] != SF_PT) { diagonal += A->v[jj]; }
+         }
+         if (diagonal != 0.0)
+         {
+            for (int k = begin; k < end; k++) { Pv[k] /= -diagonal; }
+         }
+      }
+      strong_f--;
+   }
+   /* SF points are reported as F points afterwards (:1896-1902) */
+   for (int i = 0; i < n; i++) { if (CF[i] == SF_PT) { CF[i] = F_PT; } }
+   P->nr = n; P->nc = nc; P->i = Pi; P->j = Pj; P->v = Pv;
+   free(f2c); free(marker); free(pmark);
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Truncation, hypre_ParCSRMatrixTruncate src/parcsr_mv/par_csr_matrix.c     */
+/* :2943-3300 (rescale = 1, infinity-norm), sorting with hypre_qsort2_abs    */
+/* src/utilities/qsort.c:452-474                                            */
+/* ------------------------------------------------------------------------ */
+
+static void swap2(int *v, double *w, int a, int b)
+{
+   int t = v[a]; v[a] = v[b]; v[b] = t;
+   double u = w[a]; w[a] = w[b]; w[b] = u;
+}
+
+static void qsort2_abs(int *v, double *w, int left, int right)
+{
+   if (left >= right) { return; }
+   swap2(v, w, left, (left + right) / 2);
+   int last = left;
+   for (int i = left + 1; i <= right; i++)
+   {
+      if (fabs(w[i]) > fabs(w[left])) { swap2(v, w, ++last, i); }
+   }
+   swap2(v, w, left, last);
+   qsort2_abs(v, w, left, last - 1);
+   qsort2_abs(v, w, last + 1, right);
+}
+
+int or_truncate(or_csr *P, double tol, int max_elmts)
+{
+   int n = P->nr;
+   if (tol <= 0.0 && max_elmts == 0) { return 0; }
+   int *Pi = P->i, *Pj = P->j;
+   double *Pv = P->v;
+   if (tol > 0)
+   {
+      /* drop |p| < tol * max|p_row|, then rescale to keep the row sum (:3038-3120) */
+      int next_open = 0, now = 0;
+      int *newi = xmalloc(sizeof(int) * (n + 1));
+      newi[0] = 0;
+      for (int i = 0; i < n; i++)
+      {
+         double row_nrm = 0;
+         for (int k = Pi[i]; k < Pi[i + 1]; k++) { row_nrm = row_nrm < fabs(Pv[k]) ? fabs(Pv[k]) : row_nrm; }
+         double drop = tol * row_nrm;
+         double row_sum = 0, scale = 0;
+         int rb = next_open;
+         for (now = Pi[i]; now < Pi[i + 1]; now++)
+         {
+            row_sum += Pv[now];
+            if (!(fabs(Pv[now]) < drop))
+            {
+               scale += Pv[now];
+               Pv[next_open] = Pv[now]; Pj[next_open] = Pj[now]; next_open++;
+            }
+         }
+         if (scale != 0. && scale != row_sum)
+         {
+            scale = row_sum / scale;
+            for (int k = rb; k < next_open; k++) { Pv[k] *= scale; }
+         }
+         newi[i + 1] = next_open;
+      }
+      memcpy(Pi, newi, sizeof(int) * (n + 1));
+      free(newi);
+   }
+   if (max_elmts > 0)
+   {
+      int mx = 0;
+      for (int i = 0; i < n; i++) { int c = Pi[i + 1] - Pi[i]; if (c > mx) { mx = c; } }
+      if (mx > max_elmts)
+      {
+         int *aj = xmalloc(sizeof(int) * mx);
+         double *av = xmalloc(sizeof(double) * mx);
+         int cntd = 0;
+         int prev_end = Pi[0];
+         for (int i = 0; i < n; i++)
+         {
+            int b = prev_end, e = Pi[i + 1];
+            prev_end = e;
+            int num = e - b;
+            Pi[i] = cntd;
+            if (max_elmts < num)
+            {
+               double row_sum = 0;
+               int c = 0;
+               for (int k = b; k < e; k++) { aj[c] = Pj[k]; av[c] = Pv[k]; row_sum += Pv[k]; c++; }
+               qsort2_abs(aj, av, 0, c - 1);
+               double scale = 0;
+               int rb = cntd;
+               for (int k = 0; k < max_elmts; k++)
+               {
+                  scale += av[k];
+                  Pj[cntd] = aj[k]; Pv[cntd] = av[k]; cntd++;
+               }
+               if (scale != 0. && scale != row_sum)
+               {
+                  scale = row_sum / scale;
+                  for (int k = rb; k < cntd; k++) { Pv[k] *= scale; }
+               }
+            }
+            else
+            {
+               for (int k = b; k < e; k++) { Pj[cntd] = Pj[k]; Pv[cntd] = Pv[k]; cntd++; }
+            }
+         }
+         Pi[n] = cntd;
+         free(aj); free(av);
+      }
+   }
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Transpose by counting sort (stable: rows of A^T list A's rows ascending),  */
+/* hypre_CSRMatrixTransposeHost src/seq_mv/csr_matop.c:1071                  */
+/* ------------------------------------------------------------------------ */
+
+int or_transpose(const or_csr *A, or_csr *AT)
+{
+   int nr = A->nr, nc = A->nc, nnz = A->i[nr];
+   AT->nr = nc; AT->nc = nr;
+   AT->i = xcalloc(nc + 1, sizeof(int));
+   AT->j = xmalloc(sizeof(int) * (nnz ? nnz : 1));
+   AT->v = A->v ? xmalloc(sizeof(double) * (nnz ? nnz : 1)) : NULL;
+   for (int k = 0; k < nnz; k++) { AT->i[A->j[k] + 1]++; }
+   for (int c = 0; c < nc; c++) { AT->i[c + 1] += AT->i[c]; }
+   int *pos = xmalloc(sizeof(int) * (nc ? nc : 1));
+   memcpy(pos, AT->i, sizeof(int) * nc);
+   for (int r = 0; r < nr; r++)
+   {
+      for (int k = A->i[r]; k < A->i[r + 1]; k++)
+      {
+         int p = pos[A->j[k]]++;
+         AT->j[p] = r;
+         if (A->v) { AT->v[p] = A->v[k]; }
+      }
+   }
+   free(pos);
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Galerkin product, hypre_BoomerAMGBuildCoarseOperatorKT                    */
+/* src/parcsr_ls/par_rap.c:30 (numeric pass :1640-1880): per coarse row ic,  */
+/* diagonal first, then RA row in discovery order, then RAP in discovery     */
+/* order over (RA entries x P rows).                                         */
+/* ------------------------------------------------------------------------ */
+
+int or_rap(const or_csr *P, const or_csr *A, or_csr *Ac)
+{
+   or_csr R;
+   or_transpose(P, &R);
+   int nc = P->nc, nf = A->nr;
+   /* pass 1: sizes */
+   int *Ci = xcalloc(nc + 1, sizeof(int));
+   int nthr = 1;
+#ifdef _OPENMP
+   nthr = g_threads;
+#endif
+   #pragma omp parallel num_threads(nthr)
+   {
+      int *pm = xmalloc(sizeof(int) * (nc ? nc : 1));
+      int *am = xmalloc(sizeof(int) * (nf ? nf : 1));
+      for (int k = 0; k < nc; k++) { pm[k] = -1; }
+      for (int k = 0; k < nf; k++) { am[k] = -1; }
+      #pragma omp for schedule(static)
+      for (int ic = 0; ic < nc; ic++)
+      {
+         int cnt = 1;
+         pm[ic] = ic;
+         for (int k1 = R.i[ic]; k1 < R.i[ic + 1]; k1++)
+         {
+            int i1 = R.j[k1];
+            for (int k2 = A->i[i1]; k2 < A->i[i1 + 1]; k2++)
+            {
+               int i2 = A->j[k2];
+               if (am[i2] != ic)
+               {
+                  am[i2] = ic;
+                  for (int k3 = P->i[i2]; k3 < P->i[i2 + 1]; k3++)
+                  {
+                     int i3 = P->j[k3];
+                     if (pm[i3] != ic) { pm[i3] = ic; cnt++; }
+                  }
+               }
+            }
+         }
+         Ci[ic + 1] = cnt;
+      }
+      free(pm); free(am);
+   }
+   for (int ic = 0; ic < nc; ic++) { Ci[ic + 1] += Ci[ic]; }
+   int nnz = Ci[nc];
+   int *Cj = xmalloc(sizeof(int) * (nnz ? nnz : 1));
+   double *Cv = xmalloc(sizeof(double) * (nnz ? nnz : 1));
+   /* pass 2: values */
+   #pragma omp parallel num_threads(nthr)
+   {
+      int *pm = xmalloc(sizeof(int) * (nc ? nc : 1));
+      int *am = xmalloc(sizeof(int) * (nf ? nf : 1));
+      int *raj = xmalloc(sizeof(int) * (nf ? nf : 1));
+      double *rav = xmalloc(sizeof(double) * (nf ? nf : 1));
+      for (int k = 0; k < nc; k++) { pm[k] = -1; }
+      for (int k = 0; k < nf; k++) { am[k] = -1; }
+      #pragma omp for schedule(static)
+      for (int ic = 0; ic < nc; ic++)
+      {
+         int begin = Ci[ic], c = begin;
+         pm[ic] = c; Cj[c] = ic; Cv[c] = 0.0; c++;
+         int nra = 0;
+         for (int k1 = R.i[ic]; k1 < R.i[ic + 1]; k1++)
+         {
+            int i1 = R.j[k1];
+            double r = R.v[k1];
+            for (int k2 = A->i[i1]; k2 < A->i[i1 + 1]; k2++)
+            {
+               int i2 = A->j[k2];
+               double a = A->v[k2];
+               /* am[i2] holds ic*? no: use a row-local check via position */
+               int m = am[i2];
+               if (m < 0 || m >= nra || raj[m] != i2) { am[i2] = nra; raj[nra] = i2; rav[nra] = r * a; nra++; }
+               else { rav[m] += r * a; }
+            }
+         }
+         for (int t = 0; t < nra; t++)
+         {
+            int i1 = raj[t];
+            double ra = rav[t];
+            for (int k3 = P->i[i1]; k3 < P->i[i1 + 1]; k3++)
+            {
+               int i2 = P->j[k3];
+               double p = P->v[k3];
+               int m = pm[i2];
+               if (m < begin) { pm[i2] = c; Cj[c] = i2; Cv[c] = ra * p; c++; }
+               else { Cv[m] += ra * p; }
+            }
+         }
+      }
+      free(pm); free(am); free(raj); free(rav);
+   }
+   Ac->nr = nc; Ac->nc = nc; Ac->i = Ci; Ac->j = Cj; Ac->v = Cv;
+   or_csr_free(&R);
+   return 0;
+}
+
+/* general product C = A*B with columns in discovery order (row-wise marker
+ * SpGEMM, the order hypre_ParMatmul's diag part produces) */
+int or_matmul(const or_csr *A, const or_csr *B, or_csr *C)
+{
+   int n = A->nr, m = B->nc;
+   int *Ci = xcalloc(n + 1, sizeof(int));
+   int *mk = xmalloc(sizeof(int) * (m ? m : 1));
+   for (int k = 0; k < m; k++) { mk[k] = -1; }
+   for (int i = 0; i < n; i++)
+   {
+      int cnt = 0;
+      for (int ka = A->i[i]; ka < A->i[i + 1]; ka++)
+      {
+         int r = A->j[ka];
+         for (int kb = B->i[r]; kb < B->i[r + 1]; kb++) { int c = B->j[kb]; if (mk[c] != i) { mk[c] = i; cnt++; } }
+      }
+      Ci[i + 1] = Ci[i] + cnt;
+   }
+   int nnz = Ci[n];
+   int *Cj = xmalloc(sizeof(int) * (nnz ? nnz : 1));
+   double *Cv = xmalloc(sizeof(double) * (nnz ? nnz : 1));
+   for (int k = 0; k < m; k++) { mk[k] = -1; }
+   for (int i = 0; i < n; i++)
+   {
+      int begin = Ci[i], c = begin;
+      for (int ka = A->i[i]; ka < A->i[i + 1]; ka++)
+      {
+         int r = A->j[ka];
+         double a = A->v[ka];
+         for (int kb = B->i[r]; kb < B->i[r + 1]; kb++)
+         {
+            int col = B->j[kb];
+            if (mk[col] < begin) { mk[col] = c; Cj[c] = col; Cv[c] = a * B->v[kb]; c++; }
+            else { Cv[mk[col]] += a * B->v[kb]; }
+         }
+      }
+   }
+   C->nr = n; C->nc = m; C->i = Ci; C->j = Cj; C->v = Cv;
+   free(mk);
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* l1 norms, hypre_ParCSRComputeL1Norms src/parcsr_ls/ams.c:517-790          */
+/* option 1: sum |a_ij| (relax 18); option 5: diagonal, 0 -> 1 (relax 7/11/12) */
+/* ------------------------------------------------------------------------ */
+
+int or_l1_norms(const or_csr *A, int option, double *l1)
+{
+   int n = A->nr;
+   #pragma omp parallel for schedule(static)
+   for (int i = 0; i < n; i++)
+   {
+      double d = 0.0, s = 0.0;
+      for (int k = A->i[i]; k < A->i[i + 1]; k++)
+      {
+         if (A->j[k] == i) { d = A->v[k]; }
+         s += fabs(A->v[k]);
+      }
+      double v;
+      if (option == 1) { v = s; }
+      else { v = d != 0.0 ? d : 1.0; }
+      if (d < 0.0) { v = -v; }   /* negative-definite rows, :747-770 */
+      l1[i] = v;
+   }
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Vectors and SpMV (hypre_CSRMatrixMatvecOutOfPlaceHost csr_matvec.c:22)    */
+/* ------------------------------------------------------------------------ */
+
+void or_matvec(double alpha, const or_csr *A, const double *x, double beta, const double *b, double *y)
+{
+   int n = A->nr;
+   #pragma omp parallel for schedule(static)
+   for (int i = 0; i < n; i++)
+   {
+      double s = 0.0;
+      for (int k = A->i[i]; k < A->i[i + 1]; k++) { s += A->v[k] * x[A->j[k]]; }
+      y[i] = alpha * s + (beta != 0.0 ? beta * b[i] : 0.0);
+   }
+}
+
+static void matvecT(const or_csr *A, const double *x, double *y)
+{
+   /* y = A^T x (restriction), hypre_CSRMatrixMatvecTHost csr_matvec.c:914 */
+   for (int c = 0; c < A->nc; c++) { y[c] = 0.0; }
+   for (int r = 0; r < A->nr; r++)
+   {
+      for (int k = A->i[r]; k < A->i[r + 1]; k++) { y[A->j[k]] += A->v[k] * x[r]; }
+   }
+}
+
+double or_dot(int n, const double *x, const double *y)
+{
+   double s = 0.0;
+   #pragma omp parallel for reduction(+ : s) schedule(static)
+   for (int i = 0; i < n; i++) { s += x[i] * y[i]; }
+   return s;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Coarsest solve: hypre_gselim (src/utilities/gselim.h) on a dense copy,    */
+/* as hypre_GaussElimSolve type 9 (src/parcsr_ls/par_gauss_elim.c:642-646)   */
+/* ------------------------------------------------------------------------ */
+
+static void gselim(double *A, double *x, int n)
+{
+   if (n == 1) { if (A[0] != 0.0) { x[0] = x[0] / A[0]; } return; }
+   for (int k = 0; k < n - 1; k++)
+   {
+      if (A[k * n + k] != 0.0)
+      {
+         double divA = 1.0 / A[k * n + k];
+         for (int j = k + 1; j < n; j++)
+         {
+            if (A[j * n + k] != 0.0)
+            {
+               double factor = A[j * n + k] * divA;
+               for (int m = k + 1; m < n; m++) { A[j * n + m] -= factor * A[k * n + m]; }
+               x[j] -= factor * x[k];
+            }
+         }
+      }
+   }
+   for (int k = n - 1; k > 0; --k)
+   {
+      if (A[k * n + k] != 0.0)
+      {
+         x[k] /= A[k * n + k];
+         for (int j = 0; j < k; j++) { if (A[j * n + k] != 0.0) { x[j] -= x[k] * A[j * n + k]; } }
+      }
+   }
+   if (A[0] != 0.0) { x[0] /= A[0]; }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Smoothers                                                                */
+/* ------------------------------------------------------------------------ */
+
+static void relax_l1_jacobi(const or_csr *A, const double *f, const double *l1, double w,
+                            double *u, double *V, int u_zero)
+{
+   /* hypre_BoomerAMGRelax7Jacobi src/parcsr_ls/par_relax.c:1178 (relax 18 calls it
+    * for relax_points == 0, :338-365): V = w(f - Au); u += V / l1 */
+   int n = A->nr;
+   if (u_zero) { for (int i = 0; i < n; i++) { V[i] = w * f[i]; } }
+   else { or_matvec(-w, A, u, w, f, V); }
+   for (int i = 0; i < n; i++) { u[i] += V[i] / l1[i]; }
+}
+
+static void relax_two_stage_gs(const or_csr *A, const double *f, double w, int inner,
+                               double *u, double *V, int u_zero)
+{
+   /* hypre_BoomerAMGRelaxTwoStageGaussSeidelHost src/parcsr_ls/par_relax.c:1506-1590 */
+   int n = A->nr;
+   if (u_zero) { for (int i = 0; i < n; i++) { V[i] = w * f[i]; } }
+   else { or_matvec(-w, A, u, w, f, V); }
+   double mult = 1.0;
+   for (int i = 0; i < n; i++) { V[i] /= A->v[A->i[i]]; u[i] += mult * V[i]; }
+   mult *= -1.0;
+   for (int k = 0; k < inner; k++)
+   {
+      for (int i = n - 1; i >= 0; i--)
+      {
+         double res = 0.0;
+         for (int jj = A->i[i]; jj < A->i[i + 1]; jj++) { if (A->j[jj] < i) { res += A->v[jj] * V[A->j[jj]]; } }
+         V[i] = res / A->v[A->i[i]];
+         u[i] += mult * V[i];
+      }
+      mult *= -1.0;
+   }
+}
+
+static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u, int u_zero)
+{
+   const or_csr *A = &H->A[lvl];
+   double w = H->prm.relax_weight;
+   if (type == 18 || type == 7)
+   {
+      relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero);
+   }
+   else if (type == 11 || type == 12)
+   {
+      relax_two_stage_gs(A, f, w, type == 11 ? 1 : 2, u, H->Vtmp, u_zero);
+   }
+   else
+   {
+      relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero);
+   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Setup driver, hypre_BoomerAMGSetup src/parcsr_ls/par_amg_setup.c:29       */
+/* (non-aggressive levels: strength -> PMIS -> ext+i + truncation -> RAP)    */
+/* ------------------------------------------------------------------------ */
+
+static void csr_copy(const or_csr *A, or_csr *B)
+{
+   int nnz = A->i[A->nr];
+   B->nr = A->nr; B->nc = A->nc;
+   B->i = xmalloc(sizeof(int) * (A->nr + 1)); memcpy(B->i, A->i, sizeof(int) * (A->nr + 1));
+   B->j = xmalloc(sizeof(int) * (nnz ? nnz : 1)); memcpy(B->j, A->j, sizeof(int) * nnz);
+   B->v = NULL;
+   if (A->v) { B->v = xmalloc(sizeof(double) * (nnz ? nnz : 1)); memcpy(B->v, A->v, sizeof(double) * nnz); }
+}
+
+int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
+{
+   memset(H, 0, sizeof(*H));
+   H->prm = *prm;
+   int maxl = prm->max_levels;
+   H->A = xcalloc(maxl, sizeof(or_csr));
+   H->P = xcalloc(maxl, sizeof(or_csr));
+   H->S = xcalloc(maxl, sizeof(or_csr));
+   H->CF = xcalloc(maxl, sizeof(int *));
+   H->l1 = xcalloc(maxl, sizeof(double *));
+   csr_copy(A0, &H->A[0]);
+   int level = 0;
+   int max_thresh = prm->max_coarse_size;
+   while (1)
+   {
+      or_csr *A = &H->A[level];
+      int n = A->nr;
+      if (level == maxl - 1 || n <= max_thresh) { break; }
+      or_csr S;
+      or_strength(A, prm->strong_threshold, prm->max_row_sum, &S);
+      int *CF = xmalloc(sizeof(int) * (n ? n : 1));
+      or_pmis(&S, 0, CF);
+      int nc = or_coarse_count(n, CF);
+      if (nc == 0 || nc == n || nc < prm->min_coarse_size)
+      {
+         or_csr_free(&S); free(CF);
+         break;
+      }
+      or_csr P;
+      or_extpi_interp(A, &S, CF, &P);
+      or_truncate(&P, prm->trunc_factor, prm->p_max_elmts);
+      or_csr Ac;
+      or_rap(&P, A, &Ac);
+      H->S[level] = S;
+      H->CF[level] = CF;
+      H->P[level] = P;
+      level++;
+      H->A[level] = Ac;
+      if (nc <= max_thresh) { break; }
+   }
+   H->num_levels = level + 1;
+   int nl = H->num_levels;
+   H->F = xcalloc(nl, sizeof(double *));
+   H->U = xcalloc(nl, sizeof(double *));
+   for (int l = 0; l < nl; l++)
+   {
+      int n = H->A[l].nr;
+      H->F[l] = xcalloc(n, sizeof(double));
+      H->U[l] = xcalloc(n, sizeof(double));
+      int type = (l == nl - 1) ? prm->relax_coarse : prm->relax_down;
+      int opt = (type == 18) ? 1 : 5;
+      H->l1[l] = xmalloc(sizeof(double) * (n ? n : 1));
+      or_l1_norms(&H->A[l], opt, H->l1[l]);
+   }
+   H->Vtmp = xcalloc(H->A[0].nr, sizeof(double));
+   H->Ztmp = xcalloc(H->A[0].nr, sizeof(double));
+   /* coarse dense matrix (hypre_GaussElimSetup par_gauss_elim.c:33) */
+   if (prm->relax_coarse == 9 || prm->relax_coarse == 99 || prm->relax_coarse == 19 || prm->relax_coarse == 98)
+   {
+      or_csr *Ac = &H->A[nl - 1];
+      int nn = Ac->nr;
+      H->coarse_n = nn;
+      H->coarse_lu = xcalloc((size_t) nn * nn, sizeof(double));
+      for (int r = 0; r < nn; r++)
+         for (int k = Ac->i[r]; k < Ac->i[r + 1]; k++) { H->coarse_lu[(size_t) r * nn + Ac->j[k]] = Ac->v[k]; }
+   }
+   return 0;
+}
+
+void or_amg_free(or_hierarchy *H)
+{
+   for (int l = 0; l < H->num_levels; l++)
+   {
+      or_csr_free(&H->A[l]);
+      if (l < H->num_levels - 1) { or_csr_free(&H->P[l]); or_csr_free(&H->S[l]); free(H->CF[l]); }
+      free(H->l1[l]); free(H->F[l]); free(H->U[l]);
+   }
+   free(H->A); free(H->P); free(H->S); free(H->CF); free(H->l1); free(H->F); free(H->U);
+   free(H->Vtmp); free(H->Ztmp); free(H->coarse_lu);
+   memset(H, 0, sizeof(*H));
+}
+
+/* ------------------------------------------------------------------------ */
+/* V(1,1) cycle, hypre_BoomerAMGCycle src/parcsr_ls/par_cycle.c:23-889       */
+/* ------------------------------------------------------------------------ */
+
+int or_amg_vcycle(or_hierarchy *H, const double *f, double *u)
+{
+   int nl = H->num_levels;
+   int n0 = H->A[0].nr;
+   memcpy(H->F[0], f, sizeof(double) * n0);
+   memcpy(H->U[0], u, sizeof(double) * n0);
+   int u0_zero = 1;
+   for (int i = 0; i < n0; i++) { if (u[i] != 0.0) { u0_zero = 0; break; } }
+   for (int l = 0; l < nl - 1; l++)
+   {
+      for (int s = 0; s < H->prm.num_sweeps; s++)
+      {
+         relax(H, l, H->prm.relax_down, H->F[l], H->U[l], (l > 0 || u0_zero) && s == 0);
+      }
+      /* residual and restriction (:739-807) */
+      or_matvec(-1.0, &H->A[l], H->U[l], 1.0, H->F[l], H->Vtmp);
+      matvecT(&H->P[l], H->Vtmp, H->F[l + 1]);
+      memset(H->U[l + 1], 0, sizeof(double) * H->A[l + 1].nr);
+   }
+   /* coarsest */
+   {
+      int l = nl - 1;
+      int nn = H->A[l].nr;
+      if (H->coarse_lu)
+      {
+         double *work = xmalloc(sizeof(double) * (size_t) nn * nn);
+         memcpy(work, H->coarse_lu, sizeof(double) * (size_t) nn * nn);
+         memcpy(H->U[l], H->F[l], sizeof(double) * nn);
+         gselim(work, H->U[l], nn);
+         free(work);
+      }
+      else
+      {
+         relax(H, l, H->prm.relax_coarse, H->F[l], H->U[l], 1);
+      }
+   }
+   for (int l = nl - 2; l >= 0; l--)
+   {
+      /* interpolation u_f += P u_c (:815-861), then post-relaxation */
+      or_matvec(1.0, &H->P[l], H->U[l + 1], 1.0, H->U[l], H->U[l]);
+      for (int s = 0; s < H->prm.num_sweeps; s++)
+      {
+         relax(H, l, H->prm.relax_up, H->F[l], H->U[l], 0);
+      }
+   }
+   memcpy(u, H->U[0], sizeof(double) * n0);
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PCG, hypre_PCGSolve src/krylov/pcg.c:313-1015 (two_norm = 1, rel_change 0, */
+/* recompute_residual 0, as the reference's ij driver configures it)         */
+/* ------------------------------------------------------------------------ */
+
+int or_pcg(const or_csr *A, or_hierarchy *H, const double *b, double *x,
+           double tol, int maxit, double *relres, int *iters)
+{
+   int n = A->nr;
+   double *r = xmalloc(sizeof(double) * n), *p = xcalloc(n, sizeof(double));
+   double *s = xcalloc(n, sizeof(double));
+   double bi_prod = or_dot(n, b, b);
+   int i = 0;
+   if (bi_prod == 0.0)
+   {
+      memcpy(x, b, sizeof(double) * n);
+      if (relres) { relres[0] = 0.0; }
+      *iters = 0;
+      free(r); free(p); free(s);
+      return 0;
+   }
+   double eps = tol * tol;
+   or_matvec(-1.0, A, x, 1.0, b, r);
+   memset(p, 0, sizeof(double) * n);
+   or_amg_vcycle(H, r, p);
+   double gamma = or_dot(n, r, p);
+   double i_prod = or_dot(n, r, r);
+   if (relres) { relres[0] = sqrt(i_prod / bi_prod); }
+   int conv = 0;
+   while (i + 1 <= maxit)
+   {
+      i++;
+      or_matvec(1.0, A, p, 0.0, NULL, s);
+      double sdotp = or_dot(n, s, p);
+      if (sdotp == 0.0) { break; }
+      double alpha = gamma / sdotp;
+      if (alpha <= 0.0) { break; }
+      double gamma_old = gamma;
+      for (int k = 0; k < n; k++) { x[k] += alpha * p[k]; }
+      for (int k = 0; k < n; k++) { r[k] += -alpha * s[k]; }
+      memset(s, 0, sizeof(double) * n);
+      or_amg_vcycle(H, r, s);
+      gamma = or_dot(n, r, s);
+      i_prod = or_dot(n, r, r);
+      if (relres) { relres[i] = sqrt(i_prod / bi_prod); }
+      if (i_prod / bi_prod < eps) { conv = 1; break; }
+      double beta = gamma / gamma_old;
+      for (int k = 0; k < n; k++) { p[k] = s[k] + beta * p[k]; }
+   }
+   *iters = i;
+   free(r); free(p); free(s);
+   return conv ? 0 : 256;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Flexible GMRES, hypre_FlexGMRESSolve src/krylov/flexgmres.c:288            */
+/* ------------------------------------------------------------------------ */
+
+int or_fgmres(const or_csr *A, or_hierarchy *H, const double *b, double *x,
+              double tol, int maxit, int kdim, double *resnorms, int *iters)
+{
+   int n = A->nr;
+   double **V = xmalloc(sizeof(double *) * (kdim + 1));
+   double **Z = xmalloc(sizeof(double *) * (kdim + 1));
+   for (int k = 0; k <= kdim; k++) { V[k] = xcalloc(n, sizeof(double)); Z[k] = xcalloc(n, sizeof(double)); }
+   double *hh = xcalloc((size_t) (kdim + 1) * kdim, sizeof(double));
+   double *c = xcalloc(kdim, sizeof(double)), *s = xcalloc(kdim, sizeof(double));
+   double *rs = xcalloc(kdim + 1, sizeof(double));
+#define HH(i, j) hh[(size_t) (i) * kdim + (j)]
+   double b_norm = sqrt(or_dot(n, b, b));
+   or_matvec(-1.0, A, x, 1.0, b, V[0]);
+   double r_norm = sqrt(or_dot(n, V[0], V[0]));
+   if (resnorms) { resnorms[0] = r_norm; }
+   double epsilon = tol * b_norm;
+   int iter = 0, conv = 0;
+   if (b_norm == 0.0 || r_norm <= epsilon) { *iters = 0; conv = 1; }
+   while (!conv && iter < maxit)
+   {
+      if (r_norm == 0.0) { conv = 1; break; }
+      double t = 1.0 / r_norm;
+      for (int k = 0; k < n; k++) { V[0][k] *= t; }
+      rs[0] = r_norm;
+      int i = 0;
+      while (i < kdim && iter < maxit)
+      {
+         i++;
+         iter++;
+         memset(Z[i - 1], 0, sizeof(double) * n);
+         or_amg_vcycle(H, V[i - 1], Z[i - 1]);
+         or_matvec(1.0, A, Z[i - 1], 0.0, NULL, V[i]);
+         /* modified Gram-Schmidt (:575-585) */
+         for (int j = 0; j < i; j++)
+         {
+            HH(j, i - 1) = or_dot(n, V[j], V[i]);
+            double h = -HH(j, i - 1);
+            for (int k = 0; k < n; k++) { V[i][k] += h * V[j][k]; }
+         }
+         t = sqrt(or_dot(n, V[i], V[i]));
+         HH(i, i - 1) = t;
+         if (t != 0.0) { t = 1.0 / t; for (int k = 0; k < n; k++) { V[i][k] *= t; } }
+         /* Givens rotations (:590-610) */
+         for (int j = 1; j < i; j++)
+         {
+            t = HH(j - 1, i - 1);
+            HH(j - 1, i - 1) = s[j - 1] * HH(j, i - 1) + c[j - 1] * t;
+            HH(j, i - 1) = -s[j - 1] * t + c[j - 1] * HH(j, i - 1);
+         }
+         t = HH(i, i - 1) * HH(i, i - 1);
+         t += HH(i - 1, i - 1) * HH(i - 1, i - 1);
+         double gamma = sqrt(t);
+         if (gamma == 0.0) { gamma = 1.0e-16; }
+         c[i - 1] = HH(i - 1, i - 1) / gamma;
+         s[i - 1] = HH(i, i - 1) / gamma;
+         rs[i] = -HH(i, i - 1) * rs[i - 1];
+         rs[i] /= gamma;
+         rs[i - 1] = c[i - 1] * rs[i - 1];
+         HH(i - 1, i - 1) = s[i - 1] * HH(i, i - 1) + c[i - 1] * HH(i - 1, i - 1);
+         r_norm = fabs(rs[i]);
+         if (resnorms) { resnorms[iter] = r_norm; }
+         if (r_norm <= epsilon) { break; }
+      }
+      /* solve the upper-triangular system and update x with the Z basis */
+      rs[i - 1] = rs[i - 1] / HH(i - 1, i - 1);
+      for (int k = i - 2; k >= 0; k--)
+      {
+         t = 0.0;
+         for (int j = k + 1; j < i; j++) { t -= HH(k, j) * rs[j]; }
+         t += rs[k];
+         rs[k] = t / HH(k, k);
+      }
+      for (int j = 0; j < i; j++) { for (int k = 0; k < n; k++) { x[k] += rs[j] * Z[j][k]; } }
+      if (r_norm <= epsilon)
+      {
+         /* true residual check */
+         or_matvec(-1.0, A, x, 1.0, b, V[0]);
+         r_norm = sqrt(or_dot(n, V[0], V[0]));
+         if (r_norm <= epsilon) { conv = 1; break; }
+      }
+      else
+      {
+         or_matvec(-1.0, A, x, 1.0, b, V[0]);
+         r_norm = sqrt(or_dot(n, V[0], V[0]));
+      }
+   }
+#undef HH
+   *iters = iter;
+   for (int k = 0; k <= kdim; k++) { free(V[k]); free(Z[k]); }
+   free(V); free(Z); free(hh); free(c); free(s); free(rs);
+   return conv ? 0 : 256;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Flat accessors for the ctypes wrapper (oracle/oracle.py)                  */
+/* ------------------------------------------------------------------------ */
+
+or_hierarchy *or_h_new(void) { return xcalloc(1, sizeof(or_hierarchy)); }
+void or_h_delete(or_hierarchy *H) { if (H) { or_amg_free(H); free(H); } }
+int or_h_num_levels(const or_hierarchy *H) { return H->num_levels; }
+
+/* which: 0 = A, 1 = P, 2 = S */
+int or_h_csr(const or_hierarchy *H, int which, int l, int *nr, int *nc, int **i, int **j, double **v)
+{
+   const or_csr *M = which == 0 ? &H->A[l] : which == 1 ? &H->P[l] : &H->S[l];
+   *nr = M->nr; *nc = M->nc; *i = M->i; *j = M->j; *v = M->v;
+   return M->i ? M->i[M->nr] : 0;
+}
+int *or_h_cf(const or_hierarchy *H, int l) { return H->CF[l]; }
+double *or_h_l1(const or_hierarchy *H, int l) { return H->l1[l]; }
+
+int or_setup_flat(int n, const int *Ai, const int *Aj, const double *Av, const or_amg_params *prm, or_hierarchy *H)
+{
+   or_csr A = { n, n, (int *) Ai, (int *) Aj, (double *) Av };
+   return or_amg_setup(&A, prm, H);
+}
+int or_pcg_flat(int n, const int *Ai, const int *Aj, const double *Av, or_hierarchy *H, const double *b, double *x,
+                double tol, int maxit, double *relres, int *iters)
+{
+   or_csr A = { n, n, (int *) Ai, (int *) Aj, (double *) Av };
+   return or_pcg(&A, H, b, x, tol, maxit, relres, iters);
+}
+int or_fgmres_flat(int n, const int *Ai, const int *Aj, const double *Av, or_hierarchy *H, const double *b, double *x,
+                   double tol, int maxit, int kdim, double *resn, int *iters)
+{
+   or_csr A = { n, n, (int *) Ai, (int *) Aj, (double *) Av };
+   return or_fgmres(&A, H, b, x, tol, maxit, kdim, resn, iters);
+}
+int or_vcycle_flat(or_hierarchy *H, const double *f, double *u) { return or_amg_vcycle(H, f, u); }
+void or_free_ptr(void *p) { free(p); }
+int or_gen_stencil_flat(int kind, int nx, int ny, int nz, int **i, int **j, double **v)
+{
+   or_csr A;
+   or_gen_stencil(kind, nx, ny, nz, &A);
+   *i = A.i; *j = A.j; *v = A.v;
+   return A.i[A.nr];
+}
