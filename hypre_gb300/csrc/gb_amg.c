@@ -1,0 +1,950 @@
+/* BoomerAMG on one GB300: parameter object, setup driver, V-cycle and the
+ * stand-alone solve, in C over the kernels of gb_setup.cu / gb_solve.cu.
+ *
+ * Reference behaviour followed:
+ *   defaults            src/parcsr_ls/par_amg.c:162-313 (device defaults: PMIS,
+ *                       l1-Jacobi, kept transpose)
+ *   setup level loop    src/parcsr_ls/par_amg_setup.c:1002-3145
+ *   coarsest solve      src/parcsr_ls/par_gauss_elim.c (dense, explicit inverse)
+ *   smoother setup      src/parcsr_ls/par_amg_setup.c:3242-3545
+ *   V-cycle             src/parcsr_ls/par_cycle.c:23-889
+ *   stand-alone solve   src/parcsr_ls/par_amg_solve.c:22-424
+ */
+#include "gb_internal.h"
+
+#include <math.h>
+
+static size_t gb_slab_bytes_c(int cap)
+{
+   /* per-warp slab of gb_device.cuh: hk[cap] hp[cap] vals/keys/slots[cap/2] */
+   return (size_t) cap * 4 * 2 + (size_t) (cap / 2) * (4 + 4 + 8);
+}
+
+static int next_pow2(long long x)
+{
+   long long p = 64;
+   while (p < x) { p <<= 1; }
+   return p > (1LL << 30) ? (1 << 30) : (int) p;
+}
+
+static void amg_defaults(gb_amg_params *p)
+{
+   memset(p, 0, sizeof(*p));
+   p->strong_threshold = 0.25;
+   p->max_row_sum = 0.9;
+   p->trunc_factor = 0.0;
+   p->p_max_elmts = 4;
+   p->interp_type = 6;
+   p->coarsen_type = 8;
+   p->agg_num_levels = 0;
+   p->agg_interp_type = 4;
+   p->num_paths = 1;
+   p->max_levels = 25;
+   p->max_coarse_size = 9;
+   p->min_coarse_size = 0;
+   p->relax_type[0] = 18; p->relax_type[1] = 18; p->relax_type[2] = 18; p->relax_type[3] = 9;
+   for (int k = 0; k < 4; k++) { p->num_sweeps[k] = 1; }
+   p->relax_weight = 1.0;
+   p->cheby_order = 2;
+   p->cheby_fraction = 0.3;
+   p->cheby_scale = 1;
+   p->cheby_eig_est = 10;
+   p->cycle_type = 1;
+   p->tol = 1.0e-6;
+   p->max_iter = 20;
+   p->cycle_prec = GB_PREC_F64;
+   p->use_graph = 1;
+}
+
+static gb_amg *amg_of(HYPRE_Solver s, int arg)
+{
+   gb_amg *a = (gb_amg *) s;
+   if (!a || a->magic != GB_MAGIC_AMG) { gb_error_in_arg(arg); return NULL; }
+   return a;
+}
+
+/* --------------------------------------------------------------------------
+ * hierarchy memory
+ * ------------------------------------------------------------------------ */
+static void level_free_vectors(gb_level *L)
+{
+   gb_dfree(L->F); gb_dfree(L->U); gb_dfree(L->U2); gb_dfree(L->V);
+   gb_dfree(L->Ff); gb_dfree(L->Uf); gb_dfree(L->U2f); gb_dfree(L->Vf);
+   L->F = L->U = L->U2 = L->V = NULL;
+   L->Ff = L->Uf = L->U2f = L->Vf = NULL;
+}
+
+static void amg_free_hierarchy(gb_amg *amg)
+{
+   if (amg->graph) { cudaGraphExecDestroy(amg->graph); amg->graph = NULL; }
+   for (int l = 0; l < amg->num_levels; l++)
+   {
+      gb_level *L = &amg->lev[l];
+      if (l > 0 && L->A) { gb_parcsr_free(L->A); }
+      if (L->P) { gb_parcsr_free(L->P); }
+      if (L->R) { gb_parcsr_free(L->R); }
+      gb_csr_free(&L->S);
+      gb_dfree(L->CF); gb_dfree(L->l1); gb_dfree(L->l1f);
+      level_free_vectors(L);
+      memset(L, 0, sizeof(*L));
+   }
+   gb_dfree(amg->coarse_inv);
+   amg->coarse_inv = NULL;
+   gb_dfree(amg->r_work);
+   amg->r_work = NULL;
+   amg->num_levels = 0;
+   amg->setup_done = 0;
+}
+
+/* --------------------------------------------------------------------------
+ * device helpers
+ * ------------------------------------------------------------------------ */
+static int read_int(const int *d)
+{
+   int h = 0;
+   cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   return h;
+}
+
+/* exclusive scan into out (n+1), returns total */
+static int scan_total(const int *in, int *out, int n)
+{
+   int *scr = (int *) gb_scratch(0, sizeof(int) * (size_t) gb_scan_scratch_ints(n > 0 ? n : 1));
+   gb_exclusive_scan(in, out, n, scr, gb_stream());
+   return read_int(out + n);
+}
+
+static int max_of(const int *d, int n)
+{
+   /* small host reduction of a device array (setup only) */
+   if (n <= 0) { return 0; }
+   int *h = (int *) malloc(sizeof(int) * (size_t) n);
+   cudaMemcpyAsync(h, d, sizeof(int) * (size_t) n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   int m = 0;
+   for (int i = 0; i < n; i++) { if (h[i] > m) { m = h[i]; } }
+   free(h);
+   return m;
+}
+
+/* number of persistent warps for slab kernels under a memory budget */
+static int slab_warps(size_t slab_bytes, int rows)
+{
+   size_t budget = (size_t) 2 << 30;   /* 2 GiB of scratch at most */
+   long long w = (long long) (budget / (slab_bytes ? slab_bytes : 1));
+   long long maxw = (long long) gb_num_sms() * 48;
+   if (w > maxw) { w = maxw; }
+   if (w > rows) { w = rows; }
+   /* launchers use 4-warp blocks: keep the count a multiple of 4 so every
+    * launched warp owns an allocated slab */
+   w = (w + 3) / 4 * 4;
+   if (w < 4) { w = 4; }
+   return (int) w;
+}
+
+static char *alloc_slabs(int cap, int nwarps)
+{
+   size_t per = (size_t) cap * 4 * 2 + (size_t) (cap / 2) * (4 + 4 + 8);
+   size_t bytes = per * (size_t) nwarps;
+   char *p = (char *) gb_dmalloc(bytes);
+   if (p) { cudaMemsetAsync(p, 0xff, bytes, gb_stream()); }
+   return p;
+}
+
+gb_parcsr *gb_transpose(gb_parcsr *M)
+{
+   gb_csr *A = &M->A;
+   gb_csr T;
+   T.nr = A->nc; T.nc = A->nr; T.nnz = A->nnz;
+   int *cnt = (int *) gb_dcalloc(sizeof(int) * (size_t) (T.nr + 1));
+   T.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (T.nr + 1));
+   T.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (T.nnz ? T.nnz : 1));
+   T.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (T.nnz ? T.nnz : 1));
+   if (!cnt || !T.i || !T.j || !T.v) { return NULL; }
+   gb_transpose_count(A->nnz, A->j, cnt, gb_stream());
+   scan_total(cnt, T.i, T.nr);
+   int *fill = (int *) gb_dmalloc(sizeof(int) * (size_t) (T.nr + 1));
+   cudaMemcpyAsync(fill, T.i, sizeof(int) * (size_t) (T.nr + 1), cudaMemcpyDeviceToDevice, gb_stream());
+   gb_transpose_fill(A->nr, T.nr, A->i, A->j, A->v, fill, T.i, T.j, T.v, gb_stream());
+   gb_dfree(fill);
+   gb_dfree(cnt);
+   return gb_parcsr_wrap(T, 1);
+}
+
+/* --------------------------------------------------------------------------
+ * one coarsening level (non-aggressive): S, CF, P, A_c
+ * returns 1 if a coarse level was produced, 0 to stop, -1 on error
+ * ------------------------------------------------------------------------ */
+static int setup_level(gb_amg *amg, int l, double *t_phase)
+{
+   gb_amg_params *prm = &amg->prm;
+   gb_level *L = &amg->lev[l];
+   gb_csr *A = &L->A->A;
+   int n = A->nr;
+   cudaStream_t s = gb_stream();
+   double t0 = gb_wtime();
+
+   /* 1. strength (par_strength.c:75) */
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_csr S;
+   memset(&S, 0, sizeof(S));
+   S.nr = S.nc = n;
+   S.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_strength_count(n, A->i, A->v, prm->strong_threshold, prm->max_row_sum, cnt, s);
+   S.nnz = scan_total(cnt, S.i, n);
+   S.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (S.nnz ? S.nnz : 1));
+   gb_strength_fill(n, A->i, A->j, A->v, prm->strong_threshold, prm->max_row_sum, S.i, S.j, s);
+   double t1 = gb_wtime();
+   t_phase[0] += t1 - t0;
+
+   /* 2. PMIS (par_coarsen.c:2094) */
+   int *CF = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
+   double *measure = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
+   int *ingraph = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
+   int *counter = (int *) gb_dmalloc(sizeof(int) * 4);
+   int *hcount = (int *) gb_hmalloc_pinned(sizeof(int) * 4);
+   int it = gb_pmis(n, S.i, S.j, 0, CF, measure, ingraph, cnt, counter, hcount, 10000, s);
+   gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter); gb_hfree_pinned(hcount);
+   if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS did not terminate"); return -1; }
+
+   /* 3. coarse points and numbering (par_coarse_parms.c:45) */
+   int *f2c = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_cpoint_flags(n, CF, cnt, s);
+   int nc = scan_total(cnt, f2c, n);
+   double t2 = gb_wtime();
+   t_phase[1] += t2 - t1;
+   if (nc == 0 || nc == n || nc < prm->min_coarse_size)
+   {
+      gb_dfree(cnt); gb_dfree(f2c); gb_dfree(CF); gb_csr_free(&S);
+      return 0;
+   }
+
+   /* 4. extended+i interpolation (par_lr_interp.c:1024) */
+   gb_extpi_ub(n, S.i, S.j, CF, cnt, s);
+   int ubmax = max_of(cnt, n);
+   int cap = next_pow2(2LL * (ubmax + 1));
+   int nw = slab_warps(gb_slab_bytes_c(cap), n);
+   char *slabs = alloc_slabs(cap, nw);
+   int *ovf = (int *) gb_dcalloc(sizeof(int) * 4);
+   gb_extpi_count(n, S.i, S.j, CF, slabs, cap, nw, cnt, ovf, s);
+   gb_csr P;
+   P.nr = n; P.nc = nc;
+   P.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   P.nnz = scan_total(cnt, P.i, n);
+   P.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P.nnz ? P.nnz : 1));
+   P.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P.nnz ? P.nnz : 1));
+   gb_extpi_fill(n, A->i, A->j, A->v, S.i, S.j, CF, f2c, P.i, P.j, P.v, slabs, cap, nw, ovf, s);
+   gb_sf_to_f(n, CF, s);
+   if (read_int(ovf)) { gb_error(HYPRE_ERROR_GENERIC, "interpolation table overflow"); return -1; }
+   gb_dfree(slabs);
+
+   /* 5. truncation (par_interp.c:2622 -> par_csr_matrix.c:2943) */
+   if (prm->trunc_factor > 0.0 || prm->p_max_elmts > 0)
+   {
+      gb_truncate_rows(n, P.i, P.j, P.v, prm->trunc_factor, prm->p_max_elmts, cnt, s);
+      int *Ni = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      int nnz2 = scan_total(cnt, Ni, n);
+      int *Nj = (int *) gb_dmalloc(sizeof(int) * (size_t) (nnz2 ? nnz2 : 1));
+      double *Nv = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz2 ? nnz2 : 1));
+      gb_compact_rows(n, P.i, P.j, P.v, Ni, Nj, Nv, s);
+      gb_csr_free(&P);
+      P.i = Ni; P.j = Nj; P.v = Nv; P.nnz = nnz2;
+   }
+   double t3 = gb_wtime();
+   t_phase[2] += t3 - t2;
+
+   /* 6. R = P^T and A_c = R A P (par_rap.c:30) */
+   gb_parcsr *Pm = gb_parcsr_wrap(P, 1);
+   gb_parcsr *Rm = gb_transpose(Pm);
+   if (!Rm) { return -1; }
+   gb_csr *R = &Rm->A;
+   int *apub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
+   int *ubra = (int *) gb_dmalloc(sizeof(int) * (size_t) nc);
+   int *ubrap = (int *) gb_dmalloc(sizeof(int) * (size_t) nc);
+   gb_rap_bounds(n, nc, R->i, R->j, A->i, A->j, P.i, apub, ubra, ubrap, s);
+   int mra = max_of(ubra, nc), mrap = max_of(ubrap, nc);
+   int cap_a = next_pow2(2LL * (mra + 1)), cap_c = next_pow2(2LL * (mrap + 1));
+   int nw2 = slab_warps(gb_slab_bytes_c(cap_a) + gb_slab_bytes_c(cap_c), nc);
+   char *sa = alloc_slabs(cap_a, nw2), *sc = alloc_slabs(cap_c, nw2);
+   gb_csr C;
+   C.nr = C.nc = nc;
+   C.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc + 1));
+   gb_rap(nc, R->i, R->j, R->v, A->i, A->j, A->v, P.i, P.j, P.v, sa, cap_a, sc, cap_c, nw2, 0, NULL, NULL, NULL,
+          cnt, ovf, s);
+   C.nnz = scan_total(cnt, C.i, nc);
+   C.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C.nnz ? C.nnz : 1));
+   C.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C.nnz ? C.nnz : 1));
+   gb_rap(nc, R->i, R->j, R->v, A->i, A->j, A->v, P.i, P.j, P.v, sa, cap_a, sc, cap_c, nw2, 1, C.i, C.j, C.v,
+          cnt, ovf, s);
+   if (read_int(ovf)) { gb_error(HYPRE_ERROR_GENERIC, "RAP table overflow"); return -1; }
+   gb_dfree(sa); gb_dfree(sc); gb_dfree(apub); gb_dfree(ubra); gb_dfree(ubrap); gb_dfree(ovf);
+   gb_dfree(cnt); gb_dfree(f2c);
+   double t4 = gb_wtime();
+   t_phase[3] += t4 - t3;
+
+   L->S = S;
+   L->CF = CF;
+   L->P = Pm;
+   L->R = Rm;
+   amg->lev[l + 1].A = gb_parcsr_wrap(C, 1);
+   amg->lev[l + 1].n = nc;
+   return 1;
+}
+
+static int relax_l1_option(int type) { return type == 18 ? 1 : 5; }
+
+int gb_amg_setup(gb_amg *amg, gb_parcsr *A0)
+{
+   amg_free_hierarchy(amg);
+   gb_amg_params *prm = &amg->prm;
+   double t_start = gb_wtime();
+   memset(amg->setup_times, 0, sizeof(amg->setup_times));
+   amg->lev[0].A = A0;
+   amg->lev[0].n = A0->A.nr;
+   int level = 0;
+   int maxl = prm->max_levels < 32 ? prm->max_levels : 32;
+   if (prm->agg_num_levels > 0)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening levels are not supported by this build");
+   }
+   while (1)
+   {
+      int n = amg->lev[level].n;
+      if (level == maxl - 1 || n <= prm->max_coarse_size) { break; }
+      int r = setup_level(amg, level, amg->setup_times);
+      if (r < 0) { amg->num_levels = level + 1; return gb_error_flag; }
+      if (r == 0) { break; }
+      level++;
+      if (amg->lev[level].n <= prm->max_coarse_size) { break; }
+   }
+   amg->num_levels = level + 1;
+   double t_sm = gb_wtime();
+   /* smoother setup: l1 norms or diagonal per level (par_amg_setup.c:3352-3496) */
+   cudaStream_t s = gb_stream();
+   for (int l = 0; l < amg->num_levels; l++)
+   {
+      gb_level *L = &amg->lev[l];
+      int n = L->n;
+      int type = (l == amg->num_levels - 1) ? prm->relax_type[3] : prm->relax_type[1];
+      L->l1 = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
+      gb_l1_norms(n, L->A->A.i, L->A->A.j, L->A->A.v, relax_l1_option(type), L->l1, s);
+      L->l1f = (float *) gb_dmalloc(sizeof(float) * (size_t) (n ? n : 1));
+      gb_d2f(n, L->l1, L->l1f, s);
+      L->relax_w = prm->level_relax_weight ? prm->level_relax_weight[l] : prm->relax_weight;
+      size_t nb = sizeof(double) * (size_t) (n ? n : 1);
+      L->F = (double *) gb_dcalloc(nb); L->U = (double *) gb_dcalloc(nb);
+      L->U2 = (double *) gb_dcalloc(nb); L->V = (double *) gb_dcalloc(nb);
+      size_t nf = sizeof(float) * (size_t) (n ? n : 1);
+      L->Ff = (float *) gb_dcalloc(nf); L->Uf = (float *) gb_dcalloc(nf);
+      L->U2f = (float *) gb_dcalloc(nf); L->Vf = (float *) gb_dcalloc(nf);
+   }
+   /* coarsest grid: dense inverse (par_gauss_elim.c:33) */
+   {
+      gb_level *L = &amg->lev[amg->num_levels - 1];
+      int t = prm->relax_type[3];
+      if ((t == 9 || t == 19 || t == 98 || t == 99 || t == 198 || t == 199) && L->n <= 4096)
+      {
+         int nn = L->n;
+         amg->coarse_n = nn;
+         amg->coarse_inv = (double *) gb_dmalloc(sizeof(double) * (size_t) nn * nn);
+         double *W = (double *) gb_dmalloc(sizeof(double) * (size_t) nn * nn);
+         gb_dense_inverse(nn, L->A->A.i, L->A->A.j, L->A->A.v, amg->coarse_inv, W, s);
+         gb_sync();
+         gb_dfree(W);
+      }
+   }
+   /* solve-phase forms of every level operator in the cycle precision */
+   for (int l = 0; l < amg->num_levels; l++)
+   {
+      gb_level *L = &amg->lev[l];
+      int vp = prm->cycle_prec == GB_PREC_F64 ? GB_PREC_F64 : GB_PREC_F32;
+      int vp0 = prm->cycle_prec == GB_PREC_F16 && l == 0 ? GB_PREC_F16 : vp;
+      gb_solve_desc(L->A, vp0);
+      if (vp0 != GB_PREC_F64) { gb_solve_desc(L->A, GB_PREC_F64); }
+      if (L->P) { gb_solve_desc(L->P, vp); gb_solve_desc(L->R, vp); }
+   }
+   gb_sync();
+   amg->r_work = (double *) gb_dmalloc(sizeof(double) * (size_t) (amg->lev[0].n ? amg->lev[0].n : 1));
+   amg->setup_times[4] = gb_wtime() - t_sm;
+   amg->setup_times[5] = gb_wtime() - t_start;
+   amg->setup_done = 1;
+   return gb_error_flag;
+}
+
+/* --------------------------------------------------------------------------
+ * V(1,1) cycle (par_cycle.c): f, u on level 0; u_zero: u is zero on entry
+ * ------------------------------------------------------------------------ */
+static void relax_d(gb_amg *amg, int l, int type, const double *f, double *u_in, double *u_out, int u_zero)
+{
+   /* l1-Jacobi (relax 18 via Relax7Jacobi par_relax.c:1178) and Jacobi (7):
+    * u_out = u_in + w (f - A u_in) ./ d ; two-stage GS (11/12, par_relax.c:1506)
+    * updates u_in in place and leaves u_out untouched. */
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   const gb_spmv_desc *A = gb_solve_desc(L->A, GB_PREC_F64);
+   double w = L->relax_w;
+   (void) type;
+   if (u_zero) { gb_scaled_div_d(L->n, w, f, L->l1, u_out, s); }
+   else { gb_spmv_d(A, u_in, u_out, 1, 0.0, 0.0, f, L->l1, w, NULL, NULL, s); }
+}
+
+static void twostage_gs_d(gb_amg *amg, int l, int inner, const double *f, double *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   const gb_spmv_desc *A = gb_solve_desc(L->A, GB_PREC_F64);
+   double w = L->relax_w;
+   double *V = L->V, *Z = L->U2;
+   /* V = w (f - A u) */
+   if (u_zero) { gb_fill_d(L->n, u, 0.0, s); gb_scaled_copy_d(L->n, w, f, V, s); }
+   else { gb_spmv_d(A, u, V, 0, -w, w, f, NULL, 0.0, NULL, NULL, s); }
+   gb_gs_first_d(L->n, L->A->A.i, L->A->A.v, V, u, s);
+   double m = -1.0;
+   for (int k = 0; k < inner; k++)
+   {
+      gb_gs_lower_d(L->n, L->A->A.i, L->A->A.j, L->A->A.v, V, Z, u, m, s);
+      double *t = V; V = Z; Z = t;
+      m = -m;
+   }
+}
+
+static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
+{
+   gb_amg_params *prm = &amg->prm;
+   cudaStream_t s = gb_stream();
+   int nl = amg->num_levels;
+   const double *F[32];
+   double *U[32];
+   F[0] = f0; U[0] = u0;
+   for (int l = 1; l < nl; l++) { F[l] = amg->lev[l].F; U[l] = amg->lev[l].U; }
+   for (int l = 0; l < nl - 1; l++)
+   {
+      gb_level *L = &amg->lev[l];
+      int type = prm->relax_type[1];
+      int uz = (l > 0) || u0_zero;
+      for (int sw = 0; sw < prm->num_sweeps[1]; sw++)
+      {
+         if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], uz && sw == 0); }
+         else
+         {
+            if (uz && sw == 0) { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
+            else
+            {
+               relax_d(amg, l, type, F[l], U[l], L->U2, 0);
+               cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+            }
+         }
+      }
+      /* residual and restriction */
+      gb_spmv_d(gb_solve_desc(L->A, GB_PREC_F64), U[l], L->V, 2, -1.0, 1.0, F[l], NULL, 0.0, NULL, NULL, s);
+      gb_spmv_d(gb_solve_desc(L->R, GB_PREC_F64), L->V, (double *) F[l + 1], 0, 1.0, 0.0, NULL, NULL, 0.0, NULL,
+                NULL, s);
+   }
+   {
+      int l = nl - 1;
+      gb_level *L = &amg->lev[l];
+      if (amg->coarse_inv) { gb_dense_apply_d(amg->coarse_n, amg->coarse_inv, F[l], U[l], s); }
+      else if (nl == 1 && !u0_zero)
+      {
+         relax_d(amg, l, prm->relax_type[3], F[l], U[l], L->U2, 0);
+         cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+      }
+      else
+      {
+         int type = prm->relax_type[3];
+         if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
+         else { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
+      }
+   }
+   for (int l = nl - 2; l >= 0; l--)
+   {
+      gb_level *L = &amg->lev[l];
+      int type = prm->relax_type[2];
+      /* u_f += P u_c written to U2, then the post-smoother writes back into U */
+      gb_spmv_d(gb_solve_desc(L->P, GB_PREC_F64), U[l + 1], L->U2, 0, 1.0, 1.0, U[l], NULL, 0.0, NULL, NULL, s);
+      for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
+      {
+         if (type == 11 || type == 12)
+         {
+            if (sw == 0) { cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
+            twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0);
+         }
+         else
+         {
+            if (sw == 0) { relax_d(amg, l, type, F[l], L->U2, U[l], 0); }
+            else
+            {
+               relax_d(amg, l, type, F[l], U[l], L->U2, 0);
+               cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+            }
+         }
+      }
+      if (prm->num_sweeps[2] == 0)
+      {
+         cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+      }
+   }
+}
+
+/* FP32 cycle (FP16 finest values when requested): f0/u0 are FP64 */
+static void relax_f(gb_amg *amg, int l, int type, const float *f, float *u_in, float *u_out, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   int vp = (amg->prm.cycle_prec == GB_PREC_F16 && l == 0) ? GB_PREC_F16 : GB_PREC_F32;
+   const gb_spmv_desc *A = gb_solve_desc(L->A, vp);
+   float w = (float) L->relax_w;
+   (void) type;
+   if (u_zero) { gb_scaled_div_f(L->n, w, f, L->l1f, u_out, s); }
+   else { gb_spmv_f(A, u_in, u_out, 1, 0.f, 0.f, f, L->l1f, w, NULL, NULL, s); }
+}
+
+static void twostage_gs_f(gb_amg *amg, int l, int inner, const float *f, float *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   int vp = (amg->prm.cycle_prec == GB_PREC_F16 && l == 0) ? GB_PREC_F16 : GB_PREC_F32;
+   const gb_spmv_desc *A = gb_solve_desc(L->A, vp);
+   float w = (float) L->relax_w;
+   float *V = L->Vf, *Z = L->U2f;
+   if (u_zero) { gb_fill_f(L->n, u, 0.f, s); gb_scaled_copy_f(L->n, w, f, V, s); }
+   else { gb_spmv_f(A, u, V, 0, -w, w, f, NULL, 0.f, NULL, NULL, s); }
+   gb_gs_first_f(L->n, L->A->A.i, A->v, vp, V, u, s);
+   float m = -1.f;
+   for (int k = 0; k < inner; k++)
+   {
+      gb_gs_lower_f(L->n, L->A->A.i, L->A->A.j, A->v, vp, V, Z, u, m, s);
+      float *t = V; V = Z; Z = t;
+      m = -m;
+   }
+}
+
+static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
+{
+   gb_amg_params *prm = &amg->prm;
+   cudaStream_t s = gb_stream();
+   int nl = amg->num_levels;
+   float *F[32], *U[32];
+   for (int l = 0; l < nl; l++) { F[l] = amg->lev[l].Ff; U[l] = amg->lev[l].Uf; }
+   gb_d2f(amg->lev[0].n, f0d, F[0], s);
+   for (int l = 0; l < nl - 1; l++)
+   {
+      gb_level *L = &amg->lev[l];
+      int type = prm->relax_type[1];
+      int vp = (prm->cycle_prec == GB_PREC_F16 && l == 0) ? GB_PREC_F16 : GB_PREC_F32;
+      for (int sw = 0; sw < prm->num_sweeps[1]; sw++)
+      {
+         if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], sw == 0); }
+         else if (sw == 0) { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
+         else
+         {
+            relax_f(amg, l, type, F[l], U[l], L->U2f, 0);
+            cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+         }
+      }
+      gb_spmv_f(gb_solve_desc(L->A, vp), U[l], L->Vf, 2, -1.f, 1.f, F[l], NULL, 0.f, NULL, NULL, s);
+      gb_spmv_f(gb_solve_desc(L->R, GB_PREC_F32), L->Vf, F[l + 1], 0, 1.f, 0.f, NULL, NULL, 0.f, NULL, NULL, s);
+   }
+   {
+      int l = nl - 1;
+      if (amg->coarse_inv) { gb_dense_apply_f(amg->coarse_n, amg->coarse_inv, F[l], U[l], s); }
+      else
+      {
+         int type = prm->relax_type[3];
+         if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
+         else { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
+      }
+   }
+   for (int l = nl - 2; l >= 0; l--)
+   {
+      gb_level *L = &amg->lev[l];
+      int type = prm->relax_type[2];
+      gb_spmv_f(gb_solve_desc(L->P, GB_PREC_F32), U[l + 1], L->U2f, 0, 1.f, 1.f, U[l], NULL, 0.f, NULL, NULL, s);
+      for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
+      {
+         if (type == 11 || type == 12)
+         {
+            if (sw == 0) { cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
+            twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0);
+         }
+         else if (sw == 0) { relax_f(amg, l, type, F[l], L->U2f, U[l], 0); }
+         else
+         {
+            relax_f(amg, l, type, F[l], U[l], L->U2f, 0);
+            cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+         }
+      }
+      if (prm->num_sweeps[2] == 0)
+      {
+         cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+      }
+   }
+   gb_f2d(amg->lev[0].n, U[0], u0d, s);
+}
+
+static long long g_graph_kernels = 0;
+
+/* One V-cycle from a zero initial guess: u = M^{-1} f.  Captured once per
+ * (f, u, precision) as a CUDA graph and replayed. */
+int gb_amg_cycle(gb_amg *amg, const double *f, double *u)
+{
+   cudaStream_t s = gb_stream();
+   int prec = amg->prm.cycle_prec;
+   if (amg->prm.use_graph)
+   {
+      if (amg->graph && (amg->graph_f != f || amg->graph_u != u || amg->graph_prec != prec))
+      {
+         cudaGraphExecDestroy(amg->graph);
+         amg->graph = NULL;
+      }
+      if (!amg->graph)
+      {
+         cudaGraph_t g;
+         long long before = 0, after = 0;
+         HYPRE_GB300_GetKernelLaunchCount(&before);
+         if (!gb_cuda_ok(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture")) { return 1; }
+         if (prec == GB_PREC_F64) { cycle_d(amg, f, u, 1); } else { cycle_f(amg, f, u); }
+         if (!gb_cuda_ok(cudaStreamEndCapture(s, &g), "capture end")) { return 1; }
+         if (!gb_cuda_ok(cudaGraphInstantiate(&amg->graph, g, 0), "graph instantiate")) { cudaGraphDestroy(g); return 1; }
+         cudaGraphDestroy(g);
+         HYPRE_GB300_GetKernelLaunchCount(&after);
+         g_graph_kernels = after - before;
+         gb_count_launch((int) -(after - before));   /* counted at replay */
+         amg->graph_f = f; amg->graph_u = u; amg->graph_prec = prec;
+      }
+      gb_cuda_ok(cudaGraphLaunch(amg->graph, s), "graph launch");
+      gb_count_launch((int) g_graph_kernels);
+      return 0;
+   }
+   if (prec == GB_PREC_F64) { cycle_d(amg, f, u, 1); } else { cycle_f(amg, f, u); }
+   return 0;
+}
+
+/* --------------------------------------------------------------------------
+ * Public API
+ * ------------------------------------------------------------------------ */
+HYPRE_Int HYPRE_BoomerAMGCreate(HYPRE_Solver *solver)
+{
+   if (!solver) { gb_error_in_arg(1); return gb_error_flag; }
+   gb_runtime_init();
+   gb_amg *a = (gb_amg *) calloc(1, sizeof(gb_amg));
+   a->magic = GB_MAGIC_AMG;
+   amg_defaults(&a->prm);
+   *solver = (HYPRE_Solver) a;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGDestroy(HYPRE_Solver solver)
+{
+   gb_amg *a = (gb_amg *) solver;
+   if (!a || a->magic != GB_MAGIC_AMG) { return gb_error_flag; }
+   amg_free_hierarchy(a);
+   free(a->prm.level_relax_weight);
+   a->magic = 0;
+   free(a);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetup(HYPRE_Solver solver, HYPRE_ParCSRMatrix A, HYPRE_ParVector b, HYPRE_ParVector x)
+{
+   (void) b; (void) x;
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (!A || A->magic != GB_MAGIC_MAT) { gb_error_in_arg(2); return gb_error_flag; }
+   return gb_amg_setup(a, A);
+}
+
+HYPRE_Int HYPRE_BoomerAMGSolve(HYPRE_Solver solver, HYPRE_ParCSRMatrix A, HYPRE_ParVector b, HYPRE_ParVector x)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (!A || A->magic != GB_MAGIC_MAT) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!b || b->magic != GB_MAGIC_VEC) { gb_error_in_arg(3); return gb_error_flag; }
+   if (!x || x->magic != GB_MAGIC_VEC) { gb_error_in_arg(4); return gb_error_flag; }
+   if (!a->setup_done) { gb_error(HYPRE_ERROR_GENERIC, "BoomerAMGSolve before Setup"); return gb_error_flag; }
+   int n = A->A.nr;
+   cudaStream_t s = gb_stream();
+   gb_amg_params *prm = &a->prm;
+   /* as a preconditioner (max_iter 1, tol 0) the caller passes x = 0 */
+   double bnorm = 0.0, rel = 0.0;
+   int check = prm->tol > 0.0;
+   if (check)
+   {
+      bnorm = sqrt(gb_dot(n, b->d, b->d));
+      if (bnorm == 0.0) { gb_fill_d(n, x->d, 0.0, s); a->num_iterations = 0; a->rel_resid = 0.0; return gb_error_flag; }
+   }
+   double *r = a->r_work;
+   double *e = a->lev[0].U2 == NULL ? NULL : NULL;
+   (void) e;
+   int iter = 0;
+   /* correction form: r = b - A x ; x += M^{-1} r (mathematically the
+    * reference's cycle on (b, x)) */
+   double *corr = (double *) gb_scratch(5, sizeof(double) * (size_t) n);
+   while (iter < prm->max_iter)
+   {
+      gb_spmv_d(gb_solve_desc(A, GB_PREC_F64), x->d, r, 2, -1.0, 1.0, b->d, NULL, 0.0, NULL, NULL, s);
+      if (check)
+      {
+         rel = sqrt(gb_dot(n, r, r)) / bnorm;
+         if (rel < prm->tol) { break; }
+      }
+      gb_amg_cycle(a, r, corr);
+      gb_axpy_d(n, 1.0, corr, x->d, s);
+      iter++;
+   }
+   if (check && iter == prm->max_iter)
+   {
+      gb_spmv_d(gb_solve_desc(A, GB_PREC_F64), x->d, r, 2, -1.0, 1.0, b->d, NULL, 0.0, NULL, NULL, s);
+      rel = sqrt(gb_dot(n, r, r)) / bnorm;
+      if (rel >= prm->tol) { gb_error(HYPRE_ERROR_CONV, NULL); }
+   }
+   a->num_iterations = iter;
+   a->rel_resid = rel;
+   return gb_error_flag;
+}
+
+/* preconditioner entry used by the Krylov drivers: x = M^{-1} b, x zero */
+int gb_amg_precond(HYPRE_Solver solver, const double *b, double *x)
+{
+   gb_amg *a = (gb_amg *) solver;
+   return gb_amg_cycle(a, b, x);
+}
+
+#define SETTER(name, field, type)                                  \
+   HYPRE_Int name(HYPRE_Solver solver, type v)                      \
+   {                                                                \
+      gb_amg *a = amg_of(solver, 1);                                \
+      if (a) { a->prm.field = v; }                                  \
+      return gb_error_flag;                                         \
+   }
+
+SETTER(HYPRE_BoomerAMGSetTol, tol, HYPRE_Real)
+SETTER(HYPRE_BoomerAMGSetMaxIter, max_iter, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetMaxCoarseSize, max_coarse_size, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetMinCoarseSize, min_coarse_size, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetStrongThreshold, strong_threshold, HYPRE_Real)
+SETTER(HYPRE_BoomerAMGSetMaxRowSum, max_row_sum, HYPRE_Real)
+SETTER(HYPRE_BoomerAMGSetAggNumLevels, agg_num_levels, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetNumPaths, num_paths, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetTruncFactor, trunc_factor, HYPRE_Real)
+SETTER(HYPRE_BoomerAMGSetPMaxElmts, p_max_elmts, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetAggInterpType, agg_interp_type, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetAggTruncFactor, agg_trunc_factor, HYPRE_Real)
+SETTER(HYPRE_BoomerAMGSetAggPMaxElmts, agg_p_max_elmts, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetAggP12MaxElmts, agg_p12_max_elmts, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetChebyOrder, cheby_order, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetChebyFraction, cheby_fraction, HYPRE_Real)
+SETTER(HYPRE_BoomerAMGSetChebyScale, cheby_scale, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetChebyVariant, cheby_variant, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetChebyEigEst, cheby_eig_est, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetPrintLevel, print_level, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetLogging, logging, HYPRE_Int)
+SETTER(HYPRE_GB300_BoomerAMGSetUseGraph, use_graph, HYPRE_Int)
+
+HYPRE_Int HYPRE_BoomerAMGSetMaxLevels(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v < 1) { gb_error_in_arg(2); return gb_error_flag; }
+   a->prm.max_levels = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetCoarsenType(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v != 8) { gb_error(HYPRE_ERROR_GENERIC, "coarsen_type: only PMIS (8) is supported"); gb_error_in_arg(2); return gb_error_flag; }
+   a->prm.coarsen_type = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetInterpType(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v != 6) { gb_error(HYPRE_ERROR_GENERIC, "interp_type: only extended+i (6) is supported"); gb_error_in_arg(2); return gb_error_flag; }
+   a->prm.interp_type = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetCycleType(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v != 1) { gb_error(HYPRE_ERROR_GENERIC, "cycle_type: only V-cycles (1) are supported"); gb_error_in_arg(2); return gb_error_flag; }
+   a->prm.cycle_type = v;
+   return gb_error_flag;
+}
+
+static int relax_supported(int t) { return t == 18 || t == 7 || t == 11 || t == 12 || t == 9 || t == 99 || t == 19 || t == 98; }
+
+HYPRE_Int HYPRE_BoomerAMGSetRelaxType(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (!relax_supported(v)) { gb_error(HYPRE_ERROR_GENERIC, "relax_type not supported"); gb_error_in_arg(2); return gb_error_flag; }
+   /* hypre_BoomerAMGSetRelaxType sets every cycle part, the coarsest to 9 only
+    * when v is not a direct solve (par_amg.c: grid_relax_type[3] = 9 default kept) */
+   a->prm.relax_type[0] = a->prm.relax_type[1] = a->prm.relax_type[2] = v;
+   a->prm.relax_type[3] = 9;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetCycleRelaxType(HYPRE_Solver solver, HYPRE_Int v, HYPRE_Int k)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (k < 0 || k > 3) { gb_error_in_arg(3); return gb_error_flag; }
+   if (!relax_supported(v)) { gb_error(HYPRE_ERROR_GENERIC, "relax_type not supported"); gb_error_in_arg(2); return gb_error_flag; }
+   a->prm.relax_type[k] = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetRelaxOrder(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v != 0) { gb_error(HYPRE_ERROR_GENERIC, "relax_order: only 0 (lexicographic) is supported"); }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetNumSweeps(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v < 0) { gb_error_in_arg(2); return gb_error_flag; }
+   a->prm.num_sweeps[0] = a->prm.num_sweeps[1] = a->prm.num_sweeps[2] = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetCycleNumSweeps(HYPRE_Solver solver, HYPRE_Int v, HYPRE_Int k)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (k < 0 || k > 3) { gb_error_in_arg(3); return gb_error_flag; }
+   a->prm.num_sweeps[k] = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetRelaxWt(HYPRE_Solver solver, HYPRE_Real v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   a->prm.relax_weight = v;
+   free(a->prm.level_relax_weight);
+   a->prm.level_relax_weight = NULL;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetLevelRelaxWt(HYPRE_Solver solver, HYPRE_Real v, HYPRE_Int level)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (level < 0 || level >= 32) { gb_error_in_arg(3); return gb_error_flag; }
+   if (!a->prm.level_relax_weight)
+   {
+      a->prm.level_relax_weight = (double *) malloc(sizeof(double) * 32);
+      for (int l = 0; l < 32; l++) { a->prm.level_relax_weight[l] = a->prm.relax_weight; }
+   }
+   a->prm.level_relax_weight[level] = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetRAP2(HYPRE_Solver solver, HYPRE_Int v) { (void) v; amg_of(solver, 1); return gb_error_flag; }
+HYPRE_Int HYPRE_BoomerAMGSetModuleRAP2(HYPRE_Solver solver, HYPRE_Int v) { (void) v; amg_of(solver, 1); return gb_error_flag; }
+HYPRE_Int HYPRE_BoomerAMGSetKeepTranspose(HYPRE_Solver solver, HYPRE_Int v) { (void) v; amg_of(solver, 1); return gb_error_flag; }
+
+HYPRE_Int HYPRE_GB300_BoomerAMGSetCyclePrecision(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v < 0 || v > 2) { gb_error_in_arg(2); return gb_error_flag; }
+   a->prm.cycle_prec = v;
+   if (a->graph) { cudaGraphExecDestroy(a->graph); a->graph = NULL; }
+   if (a->setup_done)
+   {
+      for (int l = 0; l < a->num_levels; l++)
+      {
+         gb_level *L = &a->lev[l];
+         int vp = v == GB_PREC_F64 ? GB_PREC_F64 : GB_PREC_F32;
+         gb_solve_desc(L->A, (v == GB_PREC_F16 && l == 0) ? GB_PREC_F16 : vp);
+         if (L->P) { gb_solve_desc(L->P, vp); gb_solve_desc(L->R, vp); }
+      }
+   }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGGetNumIterations(HYPRE_Solver solver, HYPRE_Int *n)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (a && n) { *n = a->num_iterations; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGGetFinalRelativeResidualNorm(HYPRE_Solver solver, HYPRE_Real *r)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (a && r) { *r = a->rel_resid; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGGetNumLevels(HYPRE_Solver solver, HYPRE_Int *n)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (a && n) { *n = a->num_levels; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_BoomerAMGGetSetupTimes(HYPRE_Solver solver, HYPRE_Real *t, HYPRE_Int n)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a || !t) { return gb_error_flag; }
+   for (int k = 0; k < n && k < 6; k++) { t[k] = a->setup_times[k]; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCSR(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int which, HYPRE_Int *nrows,
+                                           HYPRE_Int *ncols, HYPRE_Int *nnz, HYPRE_Int *rowptr, HYPRE_Int *colidx,
+                                           HYPRE_Real *values)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (level < 0 || level >= a->num_levels) { gb_error_in_arg(2); return gb_error_flag; }
+   gb_level *L = &a->lev[level];
+   gb_csr *M = NULL;
+   if (which == 0) { M = &L->A->A; }
+   else if (which == 1) { if (!L->P) { gb_error_in_arg(3); return gb_error_flag; } M = &L->P->A; }
+   else if (which == 2) { if (!L->S.i) { gb_error_in_arg(3); return gb_error_flag; } M = &L->S; }
+   else { gb_error_in_arg(3); return gb_error_flag; }
+   if (nrows) { *nrows = M->nr; }
+   if (ncols) { *ncols = M->nc; }
+   if (nnz) { *nnz = M->nnz; }
+   cudaStream_t s = gb_stream();
+   if (rowptr) { cudaMemcpyAsync(rowptr, M->i, sizeof(int) * (size_t) (M->nr + 1), cudaMemcpyDeviceToHost, s); }
+   if (colidx) { cudaMemcpyAsync(colidx, M->j, sizeof(int) * (size_t) M->nnz, cudaMemcpyDeviceToHost, s); }
+   if (values && M->v) { cudaMemcpyAsync(values, M->v, sizeof(double) * (size_t) M->nnz, cudaMemcpyDeviceToHost, s); }
+   gb_sync();
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCF(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int *cf)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (level < 0 || level >= a->num_levels - 1 || !cf) { gb_error_in_arg(2); return gb_error_flag; }
+   cudaMemcpyAsync(cf, a->lev[level].CF, sizeof(int) * (size_t) a->lev[level].n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelL1(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Real *l1)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (level < 0 || level >= a->num_levels || !l1) { gb_error_in_arg(2); return gb_error_flag; }
+   cudaMemcpyAsync(l1, a->lev[level].l1, sizeof(double) * (size_t) a->lev[level].n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   return gb_error_flag;
+}

@@ -1,0 +1,137 @@
+// Shared device helpers for the GB300 kernels: warp-ordered hash tables used
+// by the bit-exact setup kernels and launch bookkeeping.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define GB_FULL 0xffffffffu
+
+// Launch counter shared by every launcher (host side, gb_runtime.c).
+extern "C" void gb_count_launch(int n);
+#define GB_COUNT(n) gb_count_launch(n)
+
+__device__ __forceinline__ int gb_lane() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ unsigned gb_hash(int key) { return (unsigned) key * 2654435761u; }
+
+// Open-addressing table (linear probing) mapping a non-negative key to its
+// position in a per-row list kept in discovery order.  hk[] holds -1 in empty
+// slots; cap is a power of two.
+__device__ __forceinline__ int gb_tab_find(const int *hk, const int *hp, int cap, int key)
+{
+   unsigned s = gb_hash(key) & (cap - 1);
+   for (int probe = 0; probe < cap; probe++)
+   {
+      int k = hk[s];
+      if (k == key) { return hp[s]; }
+      if (k < 0) { return -1; }
+      s = (s + 1) & (cap - 1);
+   }
+   return -1;
+}
+
+// Inserts key -> pos; returns the slot used, or -1 when the table is full.
+__device__ __forceinline__ int gb_tab_insert(int *hk, int *hp, int cap, int key, int pos)
+{
+   unsigned s = gb_hash(key) & (cap - 1);
+   for (int probe = 0; probe < cap; probe++)
+   {
+      int prev = atomicCAS(&hk[s], -1, key);
+      if (prev < 0 || prev == key) { hp[s] = pos; return (int) s; }
+      s = (s + 1) & (cap - 1);
+   }
+   return -1;
+}
+
+// Warp-cooperative ordered insertion.  Every lane calls it; lanes with
+// active=true present a key.  Keys new to the table receive positions
+// count, count+1, ... in lane order of their first occurrence, i.e. the order
+// in which a sequential loop over the lanes' keys would discover them.
+// Returns the key's position (-1 for inactive lanes or overflow), sets
+// *created on the lane that created the entry, and raises *overflow when the
+// list (listcap) or the table fills up.
+__device__ __forceinline__ int gb_warp_insert(int *hk, int *hp, int cap, int *lkeys, int *lslot,
+                                              int listcap, int &count, int key, bool active,
+                                              bool *created, int *overflow)
+{
+   const int lane = gb_lane();
+   int pos = active ? gb_tab_find(hk, hp, cap, key) : -1;
+   bool need = active && pos < 0;
+   int mkey = need ? key : -(lane + 2);
+   unsigned grp = __match_any_sync(GB_FULL, mkey);
+   int leader = __ffs(grp) - 1;
+   bool lead = need && leader == lane;
+   unsigned newmask = __ballot_sync(GB_FULL, lead);
+   if (lead)
+   {
+      int p = count + __popc(newmask & ((1u << lane) - 1u));
+      int slot = p < listcap ? gb_tab_insert(hk, hp, cap, key, p) : -1;
+      if (slot >= 0) { lkeys[p] = key; lslot[p] = slot; pos = p; }
+      else { *overflow = 1; pos = -1; }
+   }
+   int lp = __shfl_sync(GB_FULL, pos, leader);
+   if (need && !lead) { pos = lp; }
+   count += __popc(newmask);
+   if (count > listcap) { count = listcap; }
+   *created = lead;
+   __syncwarp();
+   return pos;
+}
+
+// Clears the table slots used by the first n entries of a row list.  Slots are
+// recorded at insertion, so clearing in parallel cannot break probe chains.
+__device__ __forceinline__ void gb_warp_clear(int *hk, const int *lslot, int n)
+{
+   __syncwarp();
+   for (int t = gb_lane(); t < n; t += 32) { hk[lslot[t]] = -1; }
+   __syncwarp();
+}
+
+// Adds the active lanes' v to init in lane order (lowest lane first), serially,
+// so the rounding equals that of a sequential loop; result on all lanes.
+__device__ __forceinline__ double gb_warp_ordered_sum(double v, bool active, double init)
+{
+   unsigned m = __ballot_sync(GB_FULL, active);
+   double s = init;
+   while (m)
+   {
+      int l = __ffs(m) - 1;
+      m &= m - 1;
+      s += __shfl_sync(GB_FULL, v, l);
+   }
+   return s;
+}
+
+// Per-warp scratch slab for one ordered table: hash keys/positions (cap, a
+// power of two) plus a list of keys, slots and values (listcap = cap / 2).
+struct GbSlab
+{
+   int    *hk;
+   int    *hp;
+   int    *lkeys;
+   int    *lslot;
+   double *lvals;
+   int     cap;
+   int     listcap;
+};
+
+__device__ __forceinline__ GbSlab gb_slab(char *base, int cap, int warp)
+{
+   // layout per warp: hk[cap] hp[cap] lkeys[cap/2] lslot[cap/2] lvals[cap/2]
+   size_t bytes = (size_t) cap * 4 * 2 + (size_t) (cap / 2) * (4 + 4 + 8);
+   char *p = base + bytes * (size_t) warp;
+   GbSlab s;
+   s.cap = cap;
+   s.listcap = cap / 2;
+   s.hk = (int *) p; p += (size_t) cap * 4;
+   s.hp = (int *) p; p += (size_t) cap * 4;
+   s.lvals = (double *) p; p += (size_t) (cap / 2) * 8;
+   s.lkeys = (int *) p; p += (size_t) (cap / 2) * 4;
+   s.lslot = (int *) p;
+   return s;
+}
+
+static inline size_t gb_slab_bytes(int cap)
+{
+   return (size_t) cap * 4 * 2 + (size_t) (cap / 2) * (4 + 4 + 8);
+}

@@ -1,0 +1,809 @@
+/* IJ assembly interface and ParCSR / ParVector objects (one process, device
+ * data, empty off-diagonal block).
+ * Reference: src/IJ_mv/HYPRE_IJMatrix.c, IJMatrix_parcsr.c (host assembly,
+ * diagonal moved to the front of each row :2800-2990), src/IJ_mv/HYPRE_IJVector.c,
+ * src/parcsr_mv/HYPRE_parcsr_matrix.c, HYPRE_parcsr_vector.c. */
+#include "gb_internal.h"
+
+/* --------------------------------------------------------------------------
+ * ParCSR matrix
+ * ------------------------------------------------------------------------ */
+void gb_csr_free(gb_csr *A)
+{
+   gb_dfree(A->i); gb_dfree(A->j); gb_dfree(A->v);
+   A->i = NULL; A->j = NULL; A->v = NULL;
+}
+
+gb_parcsr *gb_parcsr_wrap(gb_csr A, int owns)
+{
+   gb_parcsr *M = (gb_parcsr *) calloc(1, sizeof(gb_parcsr));
+   M->magic = GB_MAGIC_MAT;
+   M->A = A;
+   M->owns = owns;
+   return M;
+}
+
+static void solveform_free(gb_solveform *f)
+{
+   gb_dfree(f->vals); gb_dfree(f->sl_ptr); gb_dfree(f->sl_w); gb_dfree(f->sl_j); gb_dfree(f->sl_v);
+   memset(f, 0, sizeof(*f));
+}
+
+void gb_parcsr_free(gb_parcsr *M)
+{
+   if (!M) { return; }
+   for (int p = 0; p < 3; p++) { solveform_free(&M->sf[p]); }
+   if (M->owns) { gb_csr_free(&M->A); }
+   gb_dfree(M->diag);
+   M->magic = 0;
+   free(M);
+}
+
+/* Lanes per row for the CSR kernel from the average row length (the
+ * reference's group-size rule, src/seq_mv/csr_spmv_device.c:302-315). */
+static int lanes_for(double avg)
+{
+   if (avg >= 64) { return 32; }
+   if (avg >= 32) { return 16; }
+   if (avg >= 16) { return 8; }
+   if (avg >= 8) { return 4; }
+   return 2;
+}
+
+const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
+{
+   gb_solveform *f = &M->sf[vprec];
+   if (f->valid) { return &f->desc; }
+   cudaStream_t s = gb_stream();
+   gb_csr *A = &M->A;
+   memset(&f->desc, 0, sizeof(f->desc));
+   f->vprec = vprec;
+   f->desc.n = A->nr;
+   f->desc.vprec = vprec;
+   f->desc.i = A->i;
+   f->desc.j = A->j;
+   double avg = A->nr ? (double) A->nnz / A->nr : 0;
+   f->desc.K = lanes_for(avg);
+   /* SELL-32 when rows are short and nearly uniform (little padding) */
+   int use_sell = 0;
+   int nsl = (A->nr + 31) / 32;
+   int *sl_w = NULL;
+   long long *sl_ptr = NULL;
+   if (A->nr >= 4096 && avg <= 40 && avg >= 4)
+   {
+      sl_w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
+      sl_ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));
+      gb_sell_build(A->nr, A->i, A->j, A->v, vprec, nsl, sl_w, sl_ptr, NULL, NULL, s, 0);
+      long long tot = 0;
+      cudaMemcpyAsync(&tot, sl_ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
+      gb_sync();
+      if ((double) tot <= 1.15 * (double) A->nnz) { use_sell = 1; }
+      else { gb_dfree(sl_w); gb_dfree(sl_ptr); sl_w = NULL; sl_ptr = NULL; }
+      if (use_sell)
+      {
+         size_t vb = vprec == GB_PREC_F64 ? 8 : vprec == GB_PREC_F32 ? 4 : 2;
+         int *sl_j = (int *) gb_dmalloc(sizeof(int) * (size_t) tot);
+         void *sl_v = gb_dmalloc(vb * (size_t) tot);
+         gb_sell_build(A->nr, A->i, A->j, A->v, vprec, nsl, sl_w, sl_ptr, sl_j, sl_v, s, 1);
+         f->sl_ptr = sl_ptr; f->sl_w = sl_w; f->sl_j = sl_j; f->sl_v = sl_v;
+         f->desc.fmt = GB_FMT_SELL;
+         f->desc.nslices = nsl;
+         f->desc.sl_ptr = sl_ptr; f->desc.sl_w = sl_w; f->desc.sl_j = sl_j; f->desc.sl_v = sl_v;
+      }
+   }
+   /* CSR values in the requested precision (the two-stage Gauss-Seidel
+    * kernels and the CSR path read them) */
+   if (vprec == GB_PREC_F64) { f->desc.v = A->v; }
+   else
+   {
+      size_t vb = vprec == GB_PREC_F32 ? 4 : 2;
+      f->vals = gb_dmalloc(vb * (size_t) (A->nnz ? A->nnz : 1));
+      gb_convert_vals(A->nnz, A->v, f->vals, vprec, s);
+      f->desc.v = f->vals;
+   }
+   if (!use_sell) { f->desc.fmt = GB_FMT_CSR; }
+   f->valid = 1;
+   return &f->desc;
+}
+
+void gb_matvec(double alpha, gb_parcsr *A, const double *x, double beta, double *y)
+{
+   const gb_spmv_desc *d = gb_solve_desc(A, GB_PREC_F64);
+   gb_spmv_d(d, x, y, 0, alpha, beta, y, NULL, 0.0, NULL, NULL, gb_stream());
+}
+
+/* --------------------------------------------------------------------------
+ * ParVector
+ * ------------------------------------------------------------------------ */
+gb_parvec *gb_parvec_new(int n)
+{
+   gb_parvec *v = (gb_parvec *) calloc(1, sizeof(gb_parvec));
+   v->magic = GB_MAGIC_VEC;
+   v->n = n;
+   v->num_vectors = 1;
+   v->d = (double *) gb_dcalloc(sizeof(double) * (size_t) (n > 0 ? n : 1));
+   v->owns = 1;
+   return v;
+}
+
+void gb_parvec_free(gb_parvec *v)
+{
+   if (!v) { return; }
+   if (v->owns) { gb_dfree(v->d); }
+   v->magic = 0;
+   free(v);
+}
+
+static int check_vec(gb_parvec *v, int arg)
+{
+   if (!v || v->magic != GB_MAGIC_VEC) { gb_error_in_arg(arg); return 0; }
+   return 1;
+}
+
+static int check_mat(gb_parcsr *A, int arg)
+{
+   if (!A || A->magic != GB_MAGIC_MAT) { gb_error_in_arg(arg); return 0; }
+   return 1;
+}
+
+HYPRE_Int HYPRE_ParVectorCreate(MPI_Comm comm, HYPRE_BigInt global_size, HYPRE_BigInt *partitioning,
+                                HYPRE_ParVector *vector)
+{
+   (void) comm; (void) partitioning;
+   if (!vector) { gb_error_in_arg(4); return gb_error_flag; }
+   if (global_size < 0) { gb_error_in_arg(2); return gb_error_flag; }
+   gb_runtime_init();
+   gb_parvec *v = (gb_parvec *) calloc(1, sizeof(gb_parvec));
+   v->magic = GB_MAGIC_VEC;
+   v->n = global_size;
+   v->num_vectors = 1;
+   *vector = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorInitialize(HYPRE_ParVector v)
+{
+   if (!check_vec(v, 1)) { return gb_error_flag; }
+   if (!v->d)
+   {
+      v->d = (double *) gb_dcalloc(sizeof(double) * (size_t) (v->n > 0 ? v->n : 1));
+      v->owns = 1;
+   }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorDestroy(HYPRE_ParVector v)
+{
+   if (v && v->magic == GB_MAGIC_VEC) { gb_parvec_free(v); }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorSetConstantValues(HYPRE_ParVector v, HYPRE_Complex value)
+{
+   if (!check_vec(v, 1)) { return gb_error_flag; }
+   gb_fill_d(v->n, v->d, value, gb_stream());
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorSetRandomValues(HYPRE_ParVector v, HYPRE_Int seed)
+{
+   /* hypre_SeqVectorSetRandomValues, src/seq_mv/vector.c:615: 2*PM-1 from the
+    * Park-Miller sequence, generated on the host as the reference does */
+   if (!check_vec(v, 1)) { return gb_error_flag; }
+   double *h = (double *) malloc(sizeof(double) * (size_t) (v->n > 0 ? v->n : 1));
+   int s = seed < 1 ? 1 : (seed >= 2147483647 ? 2147483646 : seed);
+   for (int i = 0; i < v->n; i++)
+   {
+      int high = s / 127773, low = s % 127773;
+      int test = 16807 * low - 2836 * high;
+      s = test > 0 ? test : test + 2147483647;
+      h[i] = 2.0 * ((double) s / (double) 2147483647) - 1.0;
+   }
+   cudaMemcpyAsync(v->d, h, sizeof(double) * (size_t) v->n, cudaMemcpyHostToDevice, gb_stream());
+   gb_sync();
+   free(h);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorCopy(HYPRE_ParVector x, HYPRE_ParVector y)
+{
+   if (!check_vec(x, 1) || !check_vec(y, 2)) { return gb_error_flag; }
+   if (x->n != y->n) { gb_error_in_arg(2); return gb_error_flag; }
+   cudaMemcpyAsync(y->d, x->d, sizeof(double) * (size_t) x->n, cudaMemcpyDeviceToDevice, gb_stream());
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorScale(HYPRE_Complex a, HYPRE_ParVector x)
+{
+   if (!check_vec(x, 2)) { return gb_error_flag; }
+   gb_scale_d(x->n, a, x->d, gb_stream());
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorAxpy(HYPRE_Complex a, HYPRE_ParVector x, HYPRE_ParVector y)
+{
+   if (!check_vec(x, 2) || !check_vec(y, 3)) { return gb_error_flag; }
+   gb_axpy_d(x->n, a, x->d, y->d, gb_stream());
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorInnerProd(HYPRE_ParVector x, HYPRE_ParVector y, HYPRE_Real *prod)
+{
+   if (!check_vec(x, 1) || !check_vec(y, 2)) { return gb_error_flag; }
+   if (!prod) { gb_error_in_arg(3); return gb_error_flag; }
+   *prod = gb_dot(x->n, x->d, y->d);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_ParVectorGetDevicePointer(HYPRE_ParVector v, void **dptr, HYPRE_Int *n)
+{
+   if (!check_vec(v, 1)) { return gb_error_flag; }
+   if (dptr) { *dptr = v->d; }
+   if (n) { *n = v->n; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_ParVectorCopyFromHost(HYPRE_ParVector v, const HYPRE_Real *h, HYPRE_Int n)
+{
+   if (!check_vec(v, 1)) { return gb_error_flag; }
+   if (n != v->n || !h) { gb_error_in_arg(3); return gb_error_flag; }
+   cudaMemcpyAsync(v->d, h, sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, gb_stream());
+   gb_sync();
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_ParVectorCopyToHost(HYPRE_ParVector v, HYPRE_Real *h, HYPRE_Int n)
+{
+   if (!check_vec(v, 1)) { return gb_error_flag; }
+   if (n != v->n || !h) { gb_error_in_arg(3); return gb_error_flag; }
+   cudaMemcpyAsync(h, v->d, sizeof(double) * (size_t) n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParCSRMatrixGetDims(HYPRE_ParCSRMatrix A, HYPRE_BigInt *M, HYPRE_BigInt *N)
+{
+   if (!check_mat(A, 1)) { return gb_error_flag; }
+   if (M) { *M = A->A.nr; }
+   if (N) { *N = A->A.nc; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParCSRMatrixGetLocalRange(HYPRE_ParCSRMatrix A, HYPRE_BigInt *rs, HYPRE_BigInt *re,
+                                          HYPRE_BigInt *cs, HYPRE_BigInt *ce)
+{
+   if (!check_mat(A, 1)) { return gb_error_flag; }
+   if (rs) { *rs = 0; }
+   if (re) { *re = A->A.nr - 1; }
+   if (cs) { *cs = 0; }
+   if (ce) { *ce = A->A.nc - 1; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParCSRMatrixMatvec(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,
+                                   HYPRE_Complex beta, HYPRE_ParVector y)
+{
+   if (!check_mat(A, 2) || !check_vec(x, 3) || !check_vec(y, 5)) { return gb_error_flag; }
+   if (x->n != A->A.nc || y->n != A->A.nr) { gb_error_in_arg(3); return gb_error_flag; }
+   gb_matvec(alpha, A, x->d, beta, y->d);
+   return gb_error_flag;
+}
+
+/* y = alpha*A^T x + beta*y through an explicit transpose built on demand */
+HYPRE_Int HYPRE_ParCSRMatrixMatvecT(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,
+                                    HYPRE_Complex beta, HYPRE_ParVector y)
+{
+   if (!check_mat(A, 2) || !check_vec(x, 3) || !check_vec(y, 5)) { return gb_error_flag; }
+   if (x->n != A->A.nr || y->n != A->A.nc) { gb_error_in_arg(3); return gb_error_flag; }
+   extern gb_parcsr *gb_transpose(gb_parcsr *A);
+   gb_parcsr *T = gb_transpose(A);
+   if (!T) { return gb_error_flag; }
+   gb_matvec(alpha, T, x->d, beta, y->d);
+   gb_sync();
+   gb_parcsr_free(T);
+   return gb_error_flag;
+}
+
+/* --------------------------------------------------------------------------
+ * Host CSR -> device ParCSR (diagonal moved first with shift semantics)
+ * ------------------------------------------------------------------------ */
+static gb_parcsr *upload_csr(int n, int nc, const int *I, const int *J, const double *V)
+{
+   gb_csr A;
+   A.nr = n; A.nc = nc; A.nnz = I[n];
+   A.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   A.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (A.nnz ? A.nnz : 1));
+   A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (A.nnz ? A.nnz : 1));
+   if (!A.i || !A.j || !A.v) { return NULL; }
+   cudaStream_t s = gb_stream();
+   cudaMemcpyAsync(A.i, I, sizeof(int) * (size_t) (n + 1), cudaMemcpyHostToDevice, s);
+   cudaMemcpyAsync(A.j, J, sizeof(int) * (size_t) A.nnz, cudaMemcpyHostToDevice, s);
+   cudaMemcpyAsync(A.v, V, sizeof(double) * (size_t) A.nnz, cudaMemcpyHostToDevice, s);
+   gb_sync();
+   return gb_parcsr_wrap(A, 1);
+}
+
+HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(HYPRE_Int n, const HYPRE_Int *rowptr, const HYPRE_Int *colidx,
+                                                    const HYPRE_Real *values, HYPRE_ParCSRMatrix *Aout)
+{
+   if (n < 0) { gb_error_in_arg(1); return gb_error_flag; }
+   if (!rowptr || !colidx || !values) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!Aout) { gb_error_in_arg(5); return gb_error_flag; }
+   gb_runtime_init();
+   int nnz = rowptr[n];
+   int *J = (int *) malloc(sizeof(int) * (size_t) (nnz ? nnz : 1));
+   double *V = (double *) malloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
+   for (int i = 0; i < n; i++)
+   {
+      int b = rowptr[i], e = rowptr[i + 1], c = b + 1, dpos = -1;
+      for (int k = b; k < e; k++) { if (colidx[k] == i) { dpos = k; break; } }
+      if (dpos < 0) { memcpy(J + b, colidx + b, sizeof(int) * (size_t) (e - b)); memcpy(V + b, values + b, sizeof(double) * (size_t) (e - b)); continue; }
+      J[b] = i; V[b] = values[dpos];
+      for (int k = b; k < e; k++) { if (k != dpos) { J[c] = colidx[k]; V[c] = values[k]; c++; } }
+   }
+   *Aout = upload_csr(n, n, rowptr, J, V);
+   free(J); free(V);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix A)
+{
+   if (A && A->magic == GB_MAGIC_MAT) { gb_parcsr_free(A); }
+   return gb_error_flag;
+}
+
+/* --------------------------------------------------------------------------
+ * IJ matrix: host staging rows (arena), assembled into a device ParCSR
+ * ------------------------------------------------------------------------ */
+struct hypre_IJMatrix_struct
+{
+   int        magic;
+   int        ilower, iupper, jlower, jupper;
+   int        nrows;
+   int        object_type;
+   int        initialized, assembled;
+   int        swap_diag;      /* SetDiagOffdSizes used: diagonal swapped to the front */
+   int       *row_off, *row_len, *row_cap;
+   int       *cols;
+   double    *vals;
+   long long  arena_len, arena_cap;
+   int       *hint;           /* row sizes from SetRowSizes */
+   gb_parcsr *par;
+};
+
+#define GB_MAGIC_IJM 0x494a4d31
+#define GB_MAGIC_IJV 0x494a5631
+
+static int check_ijm(HYPRE_IJMatrix m, int arg)
+{
+   if (!m || m->magic != GB_MAGIC_IJM) { gb_error_in_arg(arg); return 0; }
+   return 1;
+}
+
+HYPRE_Int HYPRE_IJMatrixCreate(MPI_Comm comm, HYPRE_BigInt ilower, HYPRE_BigInt iupper, HYPRE_BigInt jlower,
+                               HYPRE_BigInt jupper, HYPRE_IJMatrix *matrix)
+{
+   (void) comm;
+   if (!matrix) { gb_error_in_arg(6); return gb_error_flag; }
+   if (ilower > iupper + 1 || ilower < 0) { gb_error_in_arg(2); return gb_error_flag; }
+   if (jlower > jupper + 1 || jlower < 0) { gb_error_in_arg(4); return gb_error_flag; }
+   if (ilower != 0 || jlower != 0 || (iupper - ilower) != (jupper - jlower))
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "single-GPU build: the matrix must be square and start at row 0");
+      gb_error_in_arg(2);
+      return gb_error_flag;
+   }
+   gb_runtime_init();
+   struct hypre_IJMatrix_struct *m = calloc(1, sizeof(*m));
+   m->magic = GB_MAGIC_IJM;
+   m->ilower = ilower; m->iupper = iupper; m->jlower = jlower; m->jupper = jupper;
+   m->nrows = iupper - ilower + 1;
+   *matrix = m;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixSetObjectType(HYPRE_IJMatrix m, HYPRE_Int type)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (type != HYPRE_PARCSR) { gb_error_in_arg(2); return gb_error_flag; }
+   m->object_type = type;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixSetRowSizes(HYPRE_IJMatrix m, const HYPRE_Int *sizes)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!sizes) { gb_error_in_arg(2); return gb_error_flag; }
+   free(m->hint);
+   m->hint = (int *) malloc(sizeof(int) * (size_t) (m->nrows ? m->nrows : 1));
+   memcpy(m->hint, sizes, sizeof(int) * (size_t) m->nrows);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixSetDiagOffdSizes(HYPRE_IJMatrix m, const HYPRE_Int *diag_sizes, const HYPRE_Int *offd)
+{
+   (void) offd;
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!diag_sizes) { gb_error_in_arg(2); return gb_error_flag; }
+   HYPRE_IJMatrixSetRowSizes(m, diag_sizes);
+   m->swap_diag = 1;
+   return gb_error_flag;
+}
+
+static void ijm_free_stage(HYPRE_IJMatrix m)
+{
+   free(m->row_off); free(m->row_len); free(m->row_cap); free(m->cols); free(m->vals);
+   m->row_off = m->row_len = m->row_cap = NULL; m->cols = NULL; m->vals = NULL;
+   m->arena_len = m->arena_cap = 0;
+}
+
+HYPRE_Int HYPRE_IJMatrixInitialize(HYPRE_IJMatrix m)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   ijm_free_stage(m);
+   int n = m->nrows;
+   m->row_off = (int *) malloc(sizeof(int) * (size_t) (n ? n : 1));
+   m->row_len = (int *) calloc((size_t) (n ? n : 1), sizeof(int));
+   m->row_cap = (int *) malloc(sizeof(int) * (size_t) (n ? n : 1));
+   long long tot = 0;
+   for (int i = 0; i < n; i++)
+   {
+      int c = m->hint ? m->hint[i] : 8;
+      if (c < 1) { c = 1; }
+      m->row_off[i] = (int) tot;
+      m->row_cap[i] = c;
+      tot += c;
+   }
+   m->arena_cap = tot + tot / 8 + 64;
+   m->arena_len = tot;
+   m->cols = (int *) malloc(sizeof(int) * (size_t) m->arena_cap);
+   m->vals = (double *) malloc(sizeof(double) * (size_t) m->arena_cap);
+   if (!m->cols || !m->vals) { gb_error(HYPRE_ERROR_MEMORY, "IJ staging"); return gb_error_flag; }
+   m->initialized = 1;
+   m->assembled = 0;
+   if (m->par) { gb_parcsr_free(m->par); m->par = NULL; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixInitialize_v2(HYPRE_IJMatrix m, HYPRE_MemoryLocation loc)
+{
+   (void) loc;
+   return HYPRE_IJMatrixInitialize(m);
+}
+
+static int row_grow(HYPRE_IJMatrix m, int r, int need)
+{
+   int cap = m->row_cap[r];
+   if (need <= cap) { return 1; }
+   int ncap = cap * 2;
+   while (ncap < need) { ncap *= 2; }
+   if (m->arena_len + ncap > m->arena_cap)
+   {
+      long long nc = (m->arena_cap + ncap) * 2;
+      int *c2 = (int *) realloc(m->cols, sizeof(int) * (size_t) nc);
+      double *v2 = (double *) realloc(m->vals, sizeof(double) * (size_t) nc);
+      if (!c2 || !v2) { gb_error(HYPRE_ERROR_MEMORY, "IJ staging"); return 0; }
+      m->cols = c2; m->vals = v2; m->arena_cap = nc;
+   }
+   int off = (int) m->arena_len;
+   memcpy(m->cols + off, m->cols + m->row_off[r], sizeof(int) * (size_t) m->row_len[r]);
+   memcpy(m->vals + off, m->vals + m->row_off[r], sizeof(double) * (size_t) m->row_len[r]);
+   m->row_off[r] = off;
+   m->row_cap[r] = ncap;
+   m->arena_len += ncap;
+   return 1;
+}
+
+static HYPRE_Int ijm_put(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, const HYPRE_BigInt *rows,
+                         const HYPRE_BigInt *cols, const HYPRE_Complex *values, int add)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!m->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not initialized"); return gb_error_flag; }
+   if (nrows < 0) { gb_error_in_arg(2); return gb_error_flag; }
+   if (nrows == 0) { return gb_error_flag; }
+   if (!ncols) { gb_error_in_arg(3); return gb_error_flag; }
+   if (!rows) { gb_error_in_arg(4); return gb_error_flag; }
+   if (!cols) { gb_error_in_arg(5); return gb_error_flag; }
+   if (!values) { gb_error_in_arg(6); return gb_error_flag; }
+   long long k = 0;
+   for (int t = 0; t < nrows; t++)
+   {
+      int r = rows[t] - m->ilower;
+      int nc = ncols[t];
+      if (r < 0 || r >= m->nrows) { gb_error_in_arg(4); k += nc; continue; }
+      int len = m->row_len[r];
+      if (len == 0 && !add)
+      {
+         /* fresh row: append, merging repeated columns within the call */
+         if (!row_grow(m, r, nc)) { return gb_error_flag; }
+         int *rc = m->cols + m->row_off[r];
+         double *rv = m->vals + m->row_off[r];
+         int l = 0;
+         for (int q = 0; q < nc; q++, k++)
+         {
+            int c = cols[k] - m->jlower;
+            if (c < 0 || c > m->jupper - m->jlower) { gb_error_in_arg(5); continue; }
+            int found = -1;
+            if (l <= 32) { for (int z = 0; z < l; z++) { if (rc[z] == c) { found = z; break; } } }
+            else { for (int z = l - 1; z >= 0; z--) { if (rc[z] == c) { found = z; break; } } }
+            if (found >= 0) { rv[found] = values[k]; }
+            else { rc[l] = c; rv[l] = values[k]; l++; }
+         }
+         m->row_len[r] = l;
+         continue;
+      }
+      for (int q = 0; q < nc; q++, k++)
+      {
+         int c = cols[k] - m->jlower;
+         if (c < 0 || c > m->jupper - m->jlower) { gb_error_in_arg(5); continue; }
+         int *rc = m->cols + m->row_off[r];
+         int l = m->row_len[r];
+         int found = -1;
+         for (int z = 0; z < l; z++) { if (rc[z] == c) { found = z; break; } }
+         if (found >= 0)
+         {
+            double *rv = m->vals + m->row_off[r];
+            if (add) { rv[found] += values[k]; } else { rv[found] = values[k]; }
+         }
+         else
+         {
+            if (!row_grow(m, r, l + 1)) { return gb_error_flag; }
+            m->cols[m->row_off[r] + l] = c;
+            m->vals[m->row_off[r] + l] = values[k];
+            m->row_len[r] = l + 1;
+         }
+      }
+   }
+   m->assembled = 0;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixSetValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, const HYPRE_BigInt *rows,
+                                  const HYPRE_BigInt *cols, const HYPRE_Complex *values)
+{
+   return ijm_put(m, nrows, ncols, rows, cols, values, 0);
+}
+
+HYPRE_Int HYPRE_IJMatrixAddToValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, const HYPRE_BigInt *rows,
+                                    const HYPRE_BigInt *cols, const HYPRE_Complex *values)
+{
+   return ijm_put(m, nrows, ncols, rows, cols, values, 1);
+}
+
+HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!m->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not initialized"); return gb_error_flag; }
+   int n = m->nrows;
+   int *I = (int *) malloc(sizeof(int) * (size_t) (n + 1));
+   I[0] = 0;
+   for (int i = 0; i < n; i++) { I[i + 1] = I[i] + m->row_len[i]; }
+   int nnz = I[n];
+   int *J = (int *) malloc(sizeof(int) * (size_t) (nnz ? nnz : 1));
+   double *V = (double *) malloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
+   for (int i = 0; i < n; i++)
+   {
+      const int *rc = m->cols + m->row_off[i];
+      const double *rv = m->vals + m->row_off[i];
+      int l = m->row_len[i], b = I[i];
+      int dpos = -1;
+      for (int z = 0; z < l; z++) { if (rc[z] == i) { dpos = z; break; } }
+      if (dpos < 0 || dpos == 0)
+      {
+         memcpy(J + b, rc, sizeof(int) * (size_t) l);
+         memcpy(V + b, rv, sizeof(double) * (size_t) l);
+      }
+      else if (m->swap_diag)
+      {
+         /* IJMatrix_parcsr.c:2976-2990: swap the diagonal with the first entry */
+         memcpy(J + b, rc, sizeof(int) * (size_t) l);
+         memcpy(V + b, rv, sizeof(double) * (size_t) l);
+         J[b + dpos] = J[b]; V[b + dpos] = V[b];
+         J[b] = i; V[b] = rv[dpos];
+      }
+      else
+      {
+         /* IJMatrix_parcsr.c:2900-2920: diagonal first, others keep their order */
+         J[b] = i; V[b] = rv[dpos];
+         int c = b + 1;
+         for (int z = 0; z < l; z++) { if (z != dpos) { J[c] = rc[z]; V[c] = rv[z]; c++; } }
+      }
+   }
+   if (m->par) { gb_parcsr_free(m->par); }
+   m->par = upload_csr(n, m->jupper - m->jlower + 1, I, J, V);
+   free(I); free(J); free(V);
+   m->assembled = 1;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixGetValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, HYPRE_BigInt *rows,
+                                  HYPRE_BigInt *cols, HYPRE_Complex *values)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!m->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not initialized"); return gb_error_flag; }
+   long long k = 0;
+   for (int t = 0; t < nrows; t++)
+   {
+      int r = rows[t] - m->ilower;
+      for (int q = 0; q < ncols[t]; q++, k++)
+      {
+         int c = cols[k] - m->jlower;
+         double v = 0.0;
+         if (r >= 0 && r < m->nrows)
+         {
+            const int *rc = m->cols + m->row_off[r];
+            for (int z = 0; z < m->row_len[r]; z++) { if (rc[z] == c) { v = m->vals[m->row_off[r] + z]; break; } }
+         }
+         values[k] = v;
+      }
+   }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixGetLocalRange(HYPRE_IJMatrix m, HYPRE_BigInt *il, HYPRE_BigInt *iu, HYPRE_BigInt *jl,
+                                      HYPRE_BigInt *ju)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (il) { *il = m->ilower; }
+   if (iu) { *iu = m->iupper; }
+   if (jl) { *jl = m->jlower; }
+   if (ju) { *ju = m->jupper; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixGetObject(HYPRE_IJMatrix m, void **object)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!object) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!m->assembled || !m->par) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not assembled"); *object = NULL; return gb_error_flag; }
+   *object = m->par;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixDestroy(HYPRE_IJMatrix m)
+{
+   if (!m || m->magic != GB_MAGIC_IJM) { return gb_error_flag; }
+   ijm_free_stage(m);
+   free(m->hint);
+   if (m->par) { gb_parcsr_free(m->par); }
+   m->magic = 0;
+   free(m);
+   return gb_error_flag;
+}
+
+/* --------------------------------------------------------------------------
+ * IJ vector
+ * ------------------------------------------------------------------------ */
+struct hypre_IJVector_struct
+{
+   int        magic;
+   int        jlower, jupper, n;
+   int        object_type;
+   int        num_components;
+   double    *h;        /* host staging */
+   gb_parvec *par;
+   int        initialized;
+};
+
+static int check_ijv(HYPRE_IJVector v, int arg)
+{
+   if (!v || v->magic != GB_MAGIC_IJV) { gb_error_in_arg(arg); return 0; }
+   return 1;
+}
+
+HYPRE_Int HYPRE_IJVectorCreate(MPI_Comm comm, HYPRE_BigInt jlower, HYPRE_BigInt jupper, HYPRE_IJVector *vector)
+{
+   (void) comm;
+   if (!vector) { gb_error_in_arg(4); return gb_error_flag; }
+   if (jlower != 0 || jupper < jlower - 1) { gb_error_in_arg(2); return gb_error_flag; }
+   gb_runtime_init();
+   struct hypre_IJVector_struct *v = calloc(1, sizeof(*v));
+   v->magic = GB_MAGIC_IJV;
+   v->jlower = jlower; v->jupper = jupper; v->n = jupper - jlower + 1;
+   v->num_components = 1;
+   *vector = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorSetObjectType(HYPRE_IJVector v, HYPRE_Int type)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (type != HYPRE_PARCSR) { gb_error_in_arg(2); return gb_error_flag; }
+   v->object_type = type;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorSetNumComponents(HYPRE_IJVector v, HYPRE_Int nc)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (nc != 1) { gb_error(HYPRE_ERROR_GENERIC, "multi-component IJ vectors: use the batched solve entry points"); gb_error_in_arg(2); }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorInitialize(HYPRE_IJVector v)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   free(v->h);
+   v->h = (double *) calloc((size_t) (v->n ? v->n : 1), sizeof(double));
+   if (!v->par) { v->par = gb_parvec_new(v->n); }
+   else { gb_fill_d(v->n, v->par->d, 0.0, gb_stream()); }
+   v->initialized = 1;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorInitialize_v2(HYPRE_IJVector v, HYPRE_MemoryLocation loc)
+{
+   (void) loc;
+   return HYPRE_IJVectorInitialize(v);
+}
+
+static HYPRE_Int ijv_put(HYPRE_IJVector v, HYPRE_Int nvalues, const HYPRE_BigInt *idx, const HYPRE_Complex *vals,
+                         int add)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (!v->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ vector not initialized"); return gb_error_flag; }
+   if (nvalues < 0) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!vals) { gb_error_in_arg(4); return gb_error_flag; }
+   for (int k = 0; k < nvalues; k++)
+   {
+      int i = idx ? idx[k] - v->jlower : k;
+      if (i < 0 || i >= v->n) { gb_error_in_arg(3); continue; }
+      if (add) { v->h[i] += vals[k]; } else { v->h[i] = vals[k]; }
+   }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorSetValues(HYPRE_IJVector v, HYPRE_Int nvalues, const HYPRE_BigInt *idx,
+                                  const HYPRE_Complex *vals)
+{
+   return ijv_put(v, nvalues, idx, vals, 0);
+}
+
+HYPRE_Int HYPRE_IJVectorAddToValues(HYPRE_IJVector v, HYPRE_Int nvalues, const HYPRE_BigInt *idx,
+                                    const HYPRE_Complex *vals)
+{
+   return ijv_put(v, nvalues, idx, vals, 1);
+}
+
+HYPRE_Int HYPRE_IJVectorAssemble(HYPRE_IJVector v)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (!v->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ vector not initialized"); return gb_error_flag; }
+   cudaMemcpyAsync(v->par->d, v->h, sizeof(double) * (size_t) v->n, cudaMemcpyHostToDevice, gb_stream());
+   gb_sync();
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorGetValues(HYPRE_IJVector v, HYPRE_Int nvalues, const HYPRE_BigInt *idx, HYPRE_Complex *vals)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (!vals) { gb_error_in_arg(4); return gb_error_flag; }
+   /* read back the device vector (it may have been changed by a solve) */
+   cudaMemcpyAsync(v->h, v->par->d, sizeof(double) * (size_t) v->n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   for (int k = 0; k < nvalues; k++)
+   {
+      int i = idx ? idx[k] - v->jlower : k;
+      if (i < 0 || i >= v->n) { gb_error_in_arg(3); continue; }
+      vals[k] = v->h[i];
+   }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorGetObject(HYPRE_IJVector v, void **object)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (!object) { gb_error_in_arg(2); return gb_error_flag; }
+   *object = v->par;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorDestroy(HYPRE_IJVector v)
+{
+   if (!v || v->magic != GB_MAGIC_IJV) { return gb_error_flag; }
+   free(v->h);
+   if (v->par) { gb_parvec_free(v->par); }
+   v->magic = 0;
+   free(v);
+   return gb_error_flag;
+}

@@ -1,0 +1,176 @@
+/* Internal host-side structures of libHYPRE_gb300 (C). */
+#ifndef GB_INTERNAL_H
+#define GB_INTERNAL_H
+
+#include "HYPRE_gb300.h"
+#include "gb_kernels.h"
+
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* --- error flag (reference: src/utilities/error.c:13-91) ------------------ */
+extern HYPRE_Int gb_error_flag;
+extern HYPRE_Int gb_error_arg;
+void gb_error(HYPRE_Int code, const char *msg);
+void gb_error_in_arg(HYPRE_Int arg);
+int  gb_cuda_ok(cudaError_t e, const char *what);   /* records a GENERIC error on failure */
+
+/* --- runtime ------------------------------------------------------------- */
+cudaStream_t gb_stream(void);
+int   gb_runtime_init(void);
+void *gb_dmalloc(size_t bytes);              /* stream-ordered device allocation */
+void *gb_dcalloc(size_t bytes);
+void  gb_dfree(void *p);
+void *gb_hmalloc_pinned(size_t bytes);
+void  gb_hfree_pinned(void *p);
+int   gb_sync(void);                         /* stream sync + error check */
+double gb_wtime(void);
+/* scratch buffers reused across calls (grow-only, stream ordered) */
+void *gb_scratch(int slot, size_t bytes);
+double *gb_red_part(void);                   /* GB_RED_BLOCKS * 4 doubles */
+double *gb_red_out(void);                    /* 8 doubles (device) */
+double *gb_red_host(void);                   /* 8 doubles (pinned host) */
+void  gb_release_scratch(void);
+
+/* --- matrices and vectors -------------------------------------------------- */
+#define GB_MAGIC_MAT 0x4d415452
+#define GB_MAGIC_VEC 0x56454354
+#define GB_MAGIC_AMG 0x414d4731
+#define GB_MAGIC_PCG 0x50434731
+#define GB_MAGIC_GMR 0x474d5231
+#define GB_MAGIC_DS  0x44534331
+
+typedef struct
+{
+   int     nr, nc, nnz;
+   int    *i, *j;        /* device */
+   double *v;            /* device, FP64 */
+} gb_csr;
+
+/* cached solve-phase form of a matrix in one precision */
+typedef struct
+{
+   int          valid;
+   int          vprec;
+   gb_spmv_desc desc;
+   void        *vals;      /* CSR values in vprec (NULL when vprec == F64 and CSR) */
+   long long   *sl_ptr;
+   int         *sl_w;
+   int         *sl_j;
+   void        *sl_v;
+} gb_solveform;
+
+struct hypre_ParCSRMatrix_struct
+{
+   int          magic;
+   gb_csr       A;
+   int          owns;
+   gb_solveform sf[3];     /* per precision (GB_PREC_*) */
+   double      *diag;      /* device, for diagonal scaling (lazy) */
+};
+typedef struct hypre_ParCSRMatrix_struct gb_parcsr;
+
+struct hypre_ParVector_struct
+{
+   int     magic;
+   int     n;
+   int     num_vectors;
+   double *d;              /* device */
+   int     owns;
+};
+typedef struct hypre_ParVector_struct gb_parvec;
+
+gb_parcsr *gb_parcsr_wrap(gb_csr A, int owns);
+void       gb_parcsr_free(gb_parcsr *M);
+void       gb_csr_free(gb_csr *A);
+const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec);   /* builds lazily */
+gb_parvec *gb_parvec_new(int n);
+void       gb_parvec_free(gb_parvec *v);
+
+/* y = alpha*A*x + beta*y on the library stream, FP64 */
+void gb_matvec(double alpha, gb_parcsr *A, const double *x, double beta, double *y);
+double gb_dot(long long n, const double *x, const double *y);     /* synchronises */
+
+/* --- BoomerAMG ----------------------------------------------------------- */
+typedef struct
+{
+   double strong_threshold, max_row_sum, trunc_factor;
+   int    p_max_elmts, interp_type, coarsen_type;
+   int    agg_num_levels, agg_interp_type, agg_p_max_elmts, agg_p12_max_elmts, num_paths;
+   double agg_trunc_factor, agg_p12_trunc_factor;
+   int    max_levels, max_coarse_size, min_coarse_size;
+   int    relax_type[4];     /* [1] down, [2] up, [3] coarsest (reference grid_relax_type) */
+   int    num_sweeps[4];
+   double relax_weight;
+   double *level_relax_weight;   /* optional, per level */
+   int    cheby_order, cheby_scale, cheby_variant, cheby_eig_est;
+   double cheby_fraction;
+   int    cycle_type;
+   double tol;
+   int    max_iter;
+   int    print_level, logging;
+   int    cycle_prec;        /* GB_PREC_F64 / F32 / F16 (finest values) */
+   int    use_graph;
+} gb_amg_params;
+
+typedef struct
+{
+   int        n;
+   gb_parcsr *A;          /* level operator (level 0: borrowed from the caller) */
+   gb_parcsr *P;          /* interpolation to this level from level+1 (n x n_c) */
+   gb_parcsr *R;          /* P^T */
+   gb_csr     S;          /* strength pattern (kept for inspection) */
+   int       *CF;         /* device */
+   double    *l1;         /* device, FP64 */
+   float     *l1f;        /* device, FP32 copy */
+   double     relax_w;
+   /* cycle vectors (FP64 and FP32 sets) */
+   double    *F, *U, *U2, *V;
+   float     *Ff, *Uf, *U2f, *Vf;
+} gb_level;
+
+typedef struct
+{
+   int           magic;
+   gb_amg_params prm;
+   int           num_levels;
+   gb_level      lev[32];
+   double       *coarse_inv;    /* device, n_c x n_c */
+   int           coarse_n;
+   int           num_iterations;
+   double        rel_resid;
+   double        setup_times[6];
+   int           setup_done;
+   /* CUDA graph of one V-cycle for given (f, u) device pointers */
+   cudaGraphExec_t graph;
+   const void   *graph_f;
+   void         *graph_u;
+   int           graph_prec;
+   double       *r_work;        /* FP64 residual for stand-alone solve */
+} gb_amg;
+
+int gb_amg_cycle(gb_amg *amg, const double *f, double *u);   /* one V-cycle, u from zero */
+
+/* --- Krylov -------------------------------------------------------------- */
+typedef struct
+{
+   int                  magic;
+   double               tol, a_tol;
+   int                  max_iter, two_norm, rel_change, recompute_residual, k_dim;
+   int                  print_level, logging;
+   HYPRE_PtrToSolverFcn precond, precond_setup;
+   HYPRE_Solver         precond_solver;
+   int                  num_iterations;
+   double               rel_resid;
+   double              *hist;
+   int                  hist_n, hist_cap;
+   /* work vectors */
+   int                  n;
+   double              *r, *p, *s, *w;
+   double             **V, **Z;
+   int                  nV;
+} gb_krylov;
+
+#endif

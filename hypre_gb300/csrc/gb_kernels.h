@@ -1,0 +1,113 @@
+/* Launchers of the sm_103a kernels (gb_setup.cu, gb_solve.cu), called by the
+ * C host code.  All pointers are device pointers unless named h_*; every
+ * launcher enqueues on the given stream and returns immediately unless it
+ * says it synchronises. */
+#ifndef GB_KERNELS_H
+#define GB_KERNELS_H
+
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_PREC_F64 0
+#define GB_PREC_F32 1
+#define GB_PREC_F16 2
+
+#define GB_FMT_CSR 0
+#define GB_FMT_SELL 1
+
+/* blocks of every reduction kernel (fixed so sums are deterministic) */
+#define GB_RED_BLOCKS 1216
+
+/* solve-phase view of a sparse matrix */
+typedef struct
+{
+   int        n;         /* rows */
+   int        fmt;       /* GB_FMT_* */
+   int        vprec;     /* GB_PREC_* of v / sl_v */
+   int        K;         /* lanes per row (CSR) */
+   const int *i, *j;     /* CSR */
+   const void *v;        /* CSR values in vprec */
+   int        nslices;   /* SELL-32 */
+   const long long *sl_ptr;
+   const int *sl_w;
+   const int *sl_j;
+   const void *sl_v;
+} gb_spmv_desc;
+
+/* runtime */
+void gb_count_launch(int n);
+int  gb_num_sms(void);
+
+/* scan / setup */
+long long gb_scan_scratch_ints(int n);
+void gb_exclusive_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
+void gb_strength_count(int n, const int *Ai, const double *Av, double theta, double mrs, int *cnt, cudaStream_t s);
+void gb_strength_fill(int n, const int *Ai, const int *Aj, const double *Av, double theta, double mrs,
+                      const int *Si, int *Sj, cudaStream_t s);
+int  gb_pmis(int n, const int *Si, const int *Sj, int CF_init, int *CF, double *measure, int *ingraph, int *colcnt,
+             int *d_counter, int *h_counter, int max_iter, cudaStream_t s);   /* synchronises */
+void gb_cpoint_flags(int n, const int *CF, int *flag, cudaStream_t s);
+void gb_sf_to_f(int n, int *CF, cudaStream_t s);
+void gb_extpi_ub(int n, const int *Si, const int *Sj, const int *CF, int *ub, cudaStream_t s);
+void gb_extpi_count(int n, const int *Si, const int *Sj, const int *CF, char *slabs, int cap, int nwarps, int *cnt,
+                    int *overflow, cudaStream_t s);
+void gb_extpi_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj, const int *CF,
+                   const int *f2c, const int *Pi, int *Pj, double *Pv, char *slabs, int cap, int nwarps,
+                   int *overflow, cudaStream_t s);
+void gb_truncate_rows(int n, const int *Pi, int *Pj, double *Pv, double tol, int max_elmts, int *newcnt,
+                      cudaStream_t s);
+void gb_compact_rows(int n, const int *Pi, const int *Pj, const double *Pv, const int *Ni, int *Nj, double *Nv,
+                     cudaStream_t s);
+void gb_transpose_count(int nnz, const int *Aj, int *cnt, cudaStream_t s);
+void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, const double *Av, int *fill, const int *Ti,
+                       int *Tj, double *Tv, cudaStream_t s);
+void gb_rap_bounds(int nf, int nc, const int *Ri, const int *Rj, const int *Ai, const int *Aj, const int *Pi,
+                   int *apub, int *ubra, int *ubrap, cudaStream_t s);
+void gb_rap(int nc, const int *Ri, const int *Rj, const double *Rv, const int *Ai, const int *Aj, const double *Av,
+            const int *Pi, const int *Pj, const double *Pv, char *slab_a, int cap_a, char *slab_c, int cap_c,
+            int nwarps, int numeric, const int *Ci, int *Cj, double *Cv, int *cnt, int *overflow, cudaStream_t s);
+void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, double *l1, cudaStream_t s);
+void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, double *D, double *W, cudaStream_t s);
+
+/* solve phase */
+void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int mode, double alpha, double beta,
+               const double *b, const double *d, double w, const double *dotz, double *dpart, cudaStream_t st);
+void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int mode, float alpha, float beta, const float *b,
+               const float *d, float w, const float *dotz, double *dpart, cudaStream_t st);
+void gb_sell_build(int n, const int *Ai, const int *Aj, const double *Av, int vprec, int nslices, int *sl_w,
+                   long long *sl_ptr, int *sl_j, void *sl_v, cudaStream_t s, int stage);
+void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s);
+void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s);
+void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, float *v, float *u, cudaStream_t s);
+void gb_gs_lower_d(int n, const int *Ai, const int *Aj, const double *Av, const double *z, double *znew, double *u,
+                   double m, cudaStream_t s);
+void gb_gs_lower_f(int n, const int *Ai, const int *Aj, const void *Av, int vprec, const float *z, float *znew,
+                   float *u, float m, cudaStream_t s);
+
+void gb_fill_d(long long n, double *x, double v, cudaStream_t s);
+void gb_fill_f(long long n, float *x, float v, cudaStream_t s);
+void gb_scale_d(long long n, double a, double *x, cudaStream_t s);
+void gb_axpy_d(long long n, double a, const double *x, double *y, cudaStream_t s);
+void gb_xpay_d(long long n, const double *x, double a, double *y, cudaStream_t s);
+void gb_scaled_div_d(long long n, double w, const double *f, const double *d, double *u, cudaStream_t s);
+void gb_scaled_div_f(long long n, float w, const float *f, const float *d, float *u, cudaStream_t s);
+void gb_scaled_copy_d(long long n, double w, const double *f, double *v, cudaStream_t s);
+void gb_scaled_copy_f(long long n, float w, const float *f, float *v, cudaStream_t s);
+void gb_d2f(long long n, const double *a, float *b, cudaStream_t s);
+void gb_f2d(long long n, const float *a, double *b, cudaStream_t s);
+void gb_dot_d(long long n, const double *x, const double *y, double *part, double *out, cudaStream_t s);
+void gb_dot2_d(long long n, const double *x, const double *y, const double *z, double *part, double *out,
+               cudaStream_t s);
+void gb_pcg_xr_d(long long n, double a, const double *p, const double *sv, double *x, double *r, double *part,
+                 double *out, cudaStream_t s);
+void gb_final_sum(int nparts, int nsums, const double *part, double *out, cudaStream_t s);
+void gb_dense_apply_d(int n, const double *D, const double *f, double *u, cudaStream_t s);
+void gb_dense_apply_f(int n, const double *D, const float *f, float *u, cudaStream_t s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

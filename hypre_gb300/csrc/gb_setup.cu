@@ -1,0 +1,962 @@
+// AMG setup kernels for sm_103a: strength, PMIS, coarse numbering, extended+i
+// interpolation, truncation, transpose, Galerkin product (RAP), l1 norms and
+// the dense coarsest-grid inverse.
+//
+// Every integer result (strength pattern, C/F splitting, interpolation and
+// coarse-operator sparsity, column order) is identical to the reference's
+// serial CPU algorithms, and floating-point values are accumulated in the same
+// order, so the FP64 hierarchy is bit-for-bit the reference's.  This file is
+// compiled with --fmad=false: no a*b+c is fused, as in the reference's build.
+//
+// Column order matters downstream (the strength matrix keeps A's order, the
+// interpolation discovers columns in that order, truncation sorts by |value|
+// with a non-stable quicksort), so rows are built by one warp each with an
+// ordered hash table (gb_warp_insert) that assigns positions in the exact
+// discovery order of the reference's sequential loops.
+#include "gb_device.cuh"
+#include "gb_kernels.h"
+
+#include <stdio.h>
+
+#define C_PT 1
+#define F_PT -1
+#define SF_PT -3
+
+static int gb_blocks(long long n, int t) { long long b = (n + t - 1) / t; return (int) (b < 1 ? 1 : b); }
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of int32 (out[0..n], out[n] = total), three-phase.
+// ---------------------------------------------------------------------------
+#define SCAN_T 512
+#define SCAN_PER 4
+#define SCAN_TILE (SCAN_T * SCAN_PER)
+
+__global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, int *__restrict__ sums, int n)
+{
+   __shared__ int ws[SCAN_T / 32];
+   int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
+   int v[SCAN_PER];
+   int loc = 0;
+   for (int k = 0; k < SCAN_PER; k++) { int idx = base + k; v[k] = idx < n ? in[idx] : 0; loc += v[k]; }
+   // inclusive warp scan of per-thread totals
+   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   int x = loc;
+   for (int o = 1; o < 32; o <<= 1) { int y = __shfl_up_sync(GB_FULL, x, o); if (lane >= o) { x += y; } }
+   if (lane == 31) { ws[wid] = x; }
+   __syncthreads();
+   if (wid == 0)
+   {
+      int w = lane < SCAN_T / 32 ? ws[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) { int y = __shfl_up_sync(GB_FULL, w, o); if (lane >= o) { w += y; } }
+      if (lane < SCAN_T / 32) { ws[lane] = w; }
+   }
+   __syncthreads();
+   int excl = x - loc + (wid > 0 ? ws[wid - 1] : 0);
+   for (int k = 0; k < SCAN_PER; k++) { int idx = base + k; if (idx < n) { out[idx] = excl; } excl += v[k]; }
+   if (threadIdx.x == SCAN_T - 1) { sums[blockIdx.x] = excl; }
+}
+
+__global__ void k_scan_add(int *__restrict__ out, const int *__restrict__ sums_scanned, int n)
+{
+   int idx = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
+   int add = sums_scanned[blockIdx.x];
+   for (int k = 0; k < SCAN_PER; k++) { if (idx + k < n) { out[idx + k] += add; } }
+}
+
+__global__ void k_set_last(int *out, int n, const int *sums_scanned_total)
+{
+   out[n] = *sums_scanned_total;
+}
+
+// out has n+1 entries; scratch must hold gb_scan_scratch_ints(n) ints.
+extern "C" long long gb_scan_scratch_ints(int n)
+{
+   long long tot = 0;
+   long long m = n;
+   while (1)
+   {
+      long long nb = (m + SCAN_TILE - 1) / SCAN_TILE;
+      if (nb < 1) { nb = 1; }
+      tot += nb + 1;
+      if (nb == 1) { break; }
+      m = nb;
+   }
+   return 2 * tot + 16;
+}
+
+static void scan_rec(const int *in, int *out, int n, int *scratch, cudaStream_t s)
+{
+   int nb = gb_blocks(n, SCAN_TILE);
+   int *sums = scratch;            // nb+1 entries (exclusive-scanned in place below)
+   k_scan_tile<<<nb, SCAN_T, 0, s>>>(in, out, sums, n);
+   GB_COUNT(1);
+   if (nb == 1)
+   {
+      // sums[0] holds the total; out[n] = total
+      k_set_last<<<1, 1, 0, s>>>(out, n, sums);
+      GB_COUNT(1);
+      return;
+   }
+   int *sums_out = scratch + nb + 1;
+   scan_rec(sums, sums_out, nb, sums_out + nb + 1, s);
+   k_scan_add<<<nb, SCAN_T, 0, s>>>(out, sums_out, n);
+   GB_COUNT(1);
+   k_set_last<<<1, 1, 0, s>>>(out, n, sums_out + nb);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_exclusive_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s)
+{
+   if (n <= 0)
+   {
+      cudaMemsetAsync(out, 0, sizeof(int), s);
+      return;
+   }
+   scan_rec(in, out, n, scratch, s);
+}
+
+// ---------------------------------------------------------------------------
+// Strength of connection (reference: src/parcsr_ls/par_strength.c:75-527).
+// S keeps A's column order without the diagonal (the first entry of a row).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void strength_row(const int *Ai, const double *Av, int i, double theta, double mrs,
+                                             double &thr, int &all_weak, int &diag_neg)
+{
+   int b = Ai[i], e = Ai[i + 1];
+   double diag = Av[b];
+   double row_scale = 0.0, row_sum = diag;
+   if (diag < 0)
+   {
+      for (int k = b + 1; k < e; k++) { double v = Av[k]; row_scale = row_scale < v ? v : row_scale; row_sum += v; }
+   }
+   else
+   {
+      for (int k = b + 1; k < e; k++) { double v = Av[k]; row_scale = row_scale > v ? v : row_scale; row_sum += v; }
+   }
+   all_weak = (fabs(row_sum) > fabs(diag) * mrs) && (mrs < 1.0);
+   thr = theta * row_scale;
+   diag_neg = diag < 0;
+}
+
+__global__ void k_strength_count(int n, const int *__restrict__ Ai, const double *__restrict__ Av,
+                                 double theta, double mrs, int *__restrict__ cnt)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   double thr; int weak, dneg;
+   strength_row(Ai, Av, i, theta, mrs, thr, weak, dneg);
+   int c = 0;
+   if (!weak)
+   {
+      for (int k = Ai[i] + 1; k < Ai[i + 1]; k++)
+      {
+         double v = Av[k];
+         c += dneg ? !(v <= thr) : !(v >= thr);
+      }
+   }
+   cnt[i] = c;
+}
+
+__global__ void k_strength_fill(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                                const double *__restrict__ Av, double theta, double mrs,
+                                const int *__restrict__ Si, int *__restrict__ Sj)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   double thr; int weak, dneg;
+   strength_row(Ai, Av, i, theta, mrs, thr, weak, dneg);
+   if (weak) { return; }
+   int p = Si[i];
+   for (int k = Ai[i] + 1; k < Ai[i + 1]; k++)
+   {
+      double v = Av[k];
+      int strong = dneg ? !(v <= thr) : !(v >= thr);
+      if (strong) { Sj[p++] = Aj[k]; }
+   }
+}
+
+extern "C" void gb_strength_count(int n, const int *Ai, const double *Av, double theta, double mrs, int *cnt,
+                                  cudaStream_t s)
+{
+   k_strength_count<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Av, theta, mrs, cnt);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_strength_fill(int n, const int *Ai, const int *Aj, const double *Av, double theta, double mrs,
+                                 const int *Si, int *Sj, cudaStream_t s)
+{
+   k_strength_fill<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, theta, mrs, Si, Sj);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// PMIS (reference: src/parcsr_ls/par_coarsen.c:2094-2806 with the random
+// measures of src/parcsr_ls/par_indepset.c:33-63).  The reference's loops only
+// write CF=0/1/-1 in ways whose outcome does not depend on the visiting order,
+// so each phase is one data-parallel kernel.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double pm_draw(long long k)
+{
+   // k-th Park-Miller draw (k >= 1) from seed 2747: 16807^k * 2747 mod (2^31-1)
+   const unsigned long long m = 2147483647ULL;
+   unsigned long long a = 16807ULL, r = 1ULL;
+   long long e = k;
+   while (e > 0) { if (e & 1) { r = (r * a) % m; } a = (a * a) % m; e >>= 1; }
+   unsigned long long x = (r * 2747ULL) % m;
+   return (double) x / (double) 2147483647;
+}
+
+__global__ void k_colcount(int nnz, const int *__restrict__ Sj, int *__restrict__ colcnt)
+{
+   int k = blockIdx.x * blockDim.x + threadIdx.x;
+   if (k < nnz) { atomicAdd(&colcnt[Sj[k]], 1); }
+}
+
+__global__ void k_pmis_init(int n, const int *__restrict__ Si, const int *__restrict__ colcnt, int CF_init,
+                            double *__restrict__ measure, int *__restrict__ CF, int *__restrict__ ingraph)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   double m = (double) colcnt[i];
+   m += pm_draw((long long) i + 1);
+   int cf = 0, g = 1;
+   if (Si[i + 1] - Si[i] == 0)
+   {
+      cf = (CF_init == 3 || CF_init == 4) ? C_PT : SF_PT;
+      m = 0.0;
+      g = 0;
+   }
+   measure[i] = m;
+   CF[i] = cf;
+   ingraph[i] = g;
+}
+
+__global__ void k_pmis_select(int n, const int *__restrict__ ingraph, const double *__restrict__ measure,
+                              int *__restrict__ CF)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n && ingraph[i] && measure[i] > 1) { CF[i] = 1; }
+}
+
+__global__ void k_pmis_remove(int n, const int *__restrict__ ingraph, const double *__restrict__ measure,
+                              const int *__restrict__ Si, const int *__restrict__ Sj, int *CF)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n || !ingraph[i]) { return; }
+   double mi = measure[i];
+   if (!(mi > 1)) { return; }
+   for (int k = Si[i]; k < Si[i + 1]; k++)
+   {
+      int j = Sj[k];
+      double mj = measure[j];
+      if (mj > 1)
+      {
+         if (mi > mj) { CF[j] = 0; }
+         else if (mj > mi) { CF[i] = 0; }
+      }
+   }
+}
+
+__global__ void k_pmis_setcf(int n, const int *__restrict__ ingraph, const double *__restrict__ measure,
+                             const int *__restrict__ Si, const int *__restrict__ Sj, int *CF)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n || !ingraph[i]) { return; }
+   if (measure[i] < 1) { CF[i] = F_PT; }
+   if (CF[i] > 0) { CF[i] = C_PT; return; }
+   for (int k = Si[i]; k < Si[i + 1]; k++)
+   {
+      if (CF[Sj[k]] > 0) { CF[i] = F_PT; break; }
+   }
+}
+
+__global__ void k_pmis_update(int n, int *__restrict__ ingraph, double *__restrict__ measure,
+                              const int *__restrict__ CF, int *__restrict__ remaining)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   int keep = 0;
+   if (i < n && ingraph[i])
+   {
+      if (CF[i] != 0) { measure[i] = 0.0; ingraph[i] = 0; }
+      else { keep = 1; }
+   }
+   unsigned b = __ballot_sync(GB_FULL, keep);
+   if ((threadIdx.x & 31) == 0 && b) { atomicAdd(remaining, __popc(b)); }
+}
+
+extern "C" int gb_pmis(int n, const int *Si, const int *Sj, int CF_init, int *CF, double *measure, int *ingraph,
+                       int *colcnt, int *d_counter, int *h_counter, int max_iter, cudaStream_t s)
+{
+   int nnz = 0;
+   cudaMemcpyAsync(&nnz, Si + n, sizeof(int), cudaMemcpyDeviceToHost, s);
+   cudaStreamSynchronize(s);
+   cudaMemsetAsync(colcnt, 0, sizeof(int) * (size_t) (n > 0 ? n : 1), s);
+   if (nnz > 0) { k_colcount<<<gb_blocks(nnz, 256), 256, 0, s>>>(nnz, Sj, colcnt); GB_COUNT(1); }
+   int nb = gb_blocks(n, 256);
+   k_pmis_init<<<nb, 256, 0, s>>>(n, Si, colcnt, CF_init, measure, CF, ingraph);
+   GB_COUNT(1);
+   cudaMemsetAsync(d_counter, 0, sizeof(int), s);
+   // initial graph size
+   k_pmis_update<<<nb, 256, 0, s>>>(n, ingraph, measure, CF, d_counter);
+   GB_COUNT(1);
+   cudaMemcpyAsync(h_counter, d_counter, sizeof(int), cudaMemcpyDeviceToHost, s);
+   cudaStreamSynchronize(s);
+   int iter = 0;
+   while (*h_counter > 0)
+   {
+      if (iter >= max_iter) { return -1; }
+      if (!CF_init || iter)
+      {
+         k_pmis_select<<<nb, 256, 0, s>>>(n, ingraph, measure, CF);
+         k_pmis_remove<<<nb, 256, 0, s>>>(n, ingraph, measure, Si, Sj, CF);
+         GB_COUNT(2);
+      }
+      iter++;
+      k_pmis_setcf<<<nb, 256, 0, s>>>(n, ingraph, measure, Si, Sj, CF);
+      cudaMemsetAsync(d_counter, 0, sizeof(int), s);
+      k_pmis_update<<<nb, 256, 0, s>>>(n, ingraph, measure, CF, d_counter);
+      GB_COUNT(2);
+      cudaMemcpyAsync(h_counter, d_counter, sizeof(int), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+   }
+   return iter;
+}
+
+// ---------------------------------------------------------------------------
+// Coarse numbering: flags (CF >= 0) for the scan, and counting
+// ---------------------------------------------------------------------------
+__global__ void k_cflag(int n, const int *__restrict__ CF, int *__restrict__ flag)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { flag[i] = CF[i] >= 0; }
+}
+
+extern "C" void gb_cpoint_flags(int n, const int *CF, int *flag, cudaStream_t s)
+{
+   k_cflag<<<gb_blocks(n, 256), 256, 0, s>>>(n, CF, flag);
+   GB_COUNT(1);
+}
+
+__global__ void k_sf_to_f(int n, int *CF)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n && CF[i] == SF_PT) { CF[i] = F_PT; }
+}
+
+extern "C" void gb_sf_to_f(int n, int *CF, cudaStream_t s)
+{
+   k_sf_to_f<<<gb_blocks(n, 256), 256, 0, s>>>(n, CF);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Extended+i interpolation (reference: src/parcsr_ls/par_lr_interp.c:1024-1924,
+// hypre_BoomerAMGBuildExtPIInterpHost, one process).
+// ---------------------------------------------------------------------------
+
+// Upper bound of the candidate C set of each row: |S_i| + sum over strong F
+// neighbours of |S_i1| (+1).
+__global__ void k_extpi_ub(int n, const int *__restrict__ Si, const int *__restrict__ Sj, const int *__restrict__ CF,
+                           int *__restrict__ ub)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int u = 1;
+   if (CF[i] < 0 && CF[i] != SF_PT)
+   {
+      for (int k = Si[i]; k < Si[i + 1]; k++)
+      {
+         int i1 = Sj[k];
+         u += 1;
+         if (CF[i1] < 0 && CF[i1] != SF_PT) { u += Si[i1 + 1] - Si[i1]; }
+      }
+   }
+   ub[i] = u;
+}
+
+// Discovers the interpolation columns of F row i in the reference's order
+// (strong C neighbours, then strong C neighbours of strong F neighbours).
+__device__ __forceinline__ void extpi_discover(int i, const int *__restrict__ Si, const int *__restrict__ Sj,
+                                               const int *__restrict__ CF, GbSlab &T, int &count, int *overflow,
+                                               int *Pj_row, const int *f2c, double *Pv_row)
+{
+   const int lane = gb_lane();
+   for (int k = Si[i]; k < Si[i + 1]; k++)
+   {
+      int i1 = Sj[k];
+      int cf1 = CF[i1];
+      if (cf1 >= 0)
+      {
+         bool created;
+         int pos = gb_warp_insert(T.hk, T.hp, T.cap, T.lkeys, T.lslot, T.listcap, count, i1, lane == 0,
+                                  &created, overflow);
+         if (created && Pj_row && pos >= 0) { Pj_row[pos] = f2c[i1]; Pv_row[pos] = 0.0; }
+      }
+      else if (cf1 != SF_PT)
+      {
+         int b = Si[i1], e = Si[i1 + 1];
+         for (int base = b; base < e; base += 32)
+         {
+            int kk = base + lane;
+            int k1 = kk < e ? Sj[kk] : -1;
+            bool act = kk < e && CF[k1] >= 0;
+            bool created;
+            int pos = gb_warp_insert(T.hk, T.hp, T.cap, T.lkeys, T.lslot, T.listcap, count, k1, act,
+                                     &created, overflow);
+            if (created && Pj_row && pos >= 0) { Pj_row[pos] = f2c[k1]; Pv_row[pos] = 0.0; }
+         }
+      }
+   }
+}
+
+__global__ void k_extpi_count(int n, const int *__restrict__ Si, const int *__restrict__ Sj,
+                              const int *__restrict__ CF, char *slabs, int cap, int *__restrict__ cnt,
+                              int *overflow)
+{
+   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   int nwarps = (gridDim.x * blockDim.x) >> 5;
+   GbSlab T = gb_slab(slabs, cap, warp);
+   for (int i = warp; i < n; i += nwarps)
+   {
+      int cf = CF[i];
+      if (cf >= 0) { if (gb_lane() == 0) { cnt[i] = 1; } continue; }
+      if (cf == SF_PT) { if (gb_lane() == 0) { cnt[i] = 0; } continue; }
+      int count = 0;
+      extpi_discover(i, Si, Sj, CF, T, count, overflow, nullptr, nullptr, nullptr);
+      if (gb_lane() == 0) { cnt[i] = count; }
+      gb_warp_clear(T.hk, T.lslot, count);
+   }
+}
+
+__global__ void k_extpi_fill(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                             const double *__restrict__ Av, const int *__restrict__ Si,
+                             const int *__restrict__ Sj, const int *__restrict__ CF,
+                             const int *__restrict__ f2c, const int *__restrict__ Pi, int *__restrict__ Pj,
+                             double *__restrict__ Pv, char *slabs, int cap, int *overflow)
+{
+   const int lane = gb_lane();
+   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   int nwarps = (gridDim.x * blockDim.x) >> 5;
+   GbSlab T = gb_slab(slabs, cap, warp);
+   for (int i = warp; i < n; i += nwarps)
+   {
+      int cf = CF[i];
+      int begin = Pi[i];
+      if (cf >= 0)
+      {
+         if (lane == 0) { Pj[begin] = f2c[i]; Pv[begin] = 1.0; }
+         continue;
+      }
+      if (cf == SF_PT) { continue; }
+      int count = 0;
+      extpi_discover(i, Si, Sj, CF, T, count, overflow, Pj + begin, f2c, Pv + begin);
+      __syncwarp();
+      double *P = Pv + begin;
+      double diagonal = Av[Ai[i]];
+      int sp = Si[i], se = Si[i + 1];
+      for (int jj = Ai[i] + 1; jj < Ai[i + 1]; jj++)
+      {
+         int i1 = Aj[jj];
+         double a = Av[jj];
+         bool strong = (sp < se && Sj[sp] == i1);
+         if (strong) { sp++; }
+         int pos1 = gb_tab_find(T.hk, T.hp, T.cap, i1);
+         int cf1 = CF[i1];
+         if (pos1 >= 0)
+         {
+            if (lane == 0) { P[pos1] += a; }
+            __syncwarp();
+         }
+         else if (strong && cf1 < 0 && cf1 != SF_PT)
+         {
+            int b = Ai[i1], e = Ai[i1 + 1];
+            int sgn = Av[b] < 0 ? -1 : 1;
+            double sum = 0.0;
+            for (int base = b + 1; base < e; base += 32)
+            {
+               int k = base + lane;
+               bool in = k < e;
+               int i2 = in ? Aj[k] : -1;
+               double a2 = in ? Av[k] : 0.0;
+               bool cond = in && (gb_tab_find(T.hk, T.hp, T.cap, i2) >= 0 || i2 == i) && (sgn * a2) < 0;
+               sum = gb_warp_ordered_sum(a2, cond, sum);
+            }
+            if (sum != 0)
+            {
+               double distribute = a / sum;
+               for (int base = b + 1; base < e; base += 32)
+               {
+                  int k = base + lane;
+                  bool in = k < e;
+                  int i2 = in ? Aj[k] : -1;
+                  double a2 = in ? Av[k] : 0.0;
+                  int pos2 = in ? gb_tab_find(T.hk, T.hp, T.cap, i2) : -1;
+                  if (pos2 >= 0 && (sgn * a2) < 0) { P[pos2] += distribute * a2; }
+                  bool dterm = in && i2 == i && (sgn * a2) < 0;
+                  unsigned dm = __ballot_sync(GB_FULL, dterm);
+                  if (dm)
+                  {
+                     double contrib = __shfl_sync(GB_FULL, distribute * a2, __ffs(dm) - 1);
+                     diagonal += contrib;
+                  }
+               }
+               __syncwarp();
+            }
+            else { diagonal += a; }
+         }
+         else if (cf1 != SF_PT) { diagonal += a; }
+      }
+      __syncwarp();
+      if (diagonal != 0.0)
+      {
+         for (int t = lane; t < count; t += 32) { P[t] /= -diagonal; }
+      }
+      gb_warp_clear(T.hk, T.lslot, count);
+   }
+}
+
+extern "C" void gb_extpi_ub(int n, const int *Si, const int *Sj, const int *CF, int *ub, cudaStream_t s)
+{
+   k_extpi_ub<<<gb_blocks(n, 256), 256, 0, s>>>(n, Si, Sj, CF, ub);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_extpi_count(int n, const int *Si, const int *Sj, const int *CF, char *slabs, int cap, int nwarps,
+                               int *cnt, int *overflow, cudaStream_t s)
+{
+   int threads = 128;
+   int blocks = (nwarps * 32 + threads - 1) / threads;
+   k_extpi_count<<<blocks, threads, 0, s>>>(n, Si, Sj, CF, slabs, cap, cnt, overflow);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_extpi_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj,
+                              const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv, char *slabs, int cap,
+                              int nwarps, int *overflow, cudaStream_t s)
+{
+   int threads = 128;
+   int blocks = (nwarps * 32 + threads - 1) / threads;
+   k_extpi_fill<<<blocks, threads, 0, s>>>(n, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv, slabs, cap, overflow);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Truncation (reference: src/parcsr_mv/par_csr_matrix.c:2943-3300, rescale=1,
+// infinity norm; hypre_qsort2_abs src/utilities/qsort.c:452-474).
+// Works in place on each row, then the rows are compacted.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void sw2(int *v, double *w, int a, int b)
+{
+   int t = v[a]; v[a] = v[b]; v[b] = t;
+   double u = w[a]; w[a] = w[b]; w[b] = u;
+}
+
+// K&R quicksort by |w| descending (pivot (l+r)/2, strict '>'), iterative.
+// Disjoint subranges are independent, so the processing order does not change
+// the final arrangement.
+__device__ void qsort2_abs_iter(int *v, double *w, int left, int right)
+{
+   int stl[64], str[64];
+   int sp = 0;
+   stl[sp] = left; str[sp] = right; sp++;
+   while (sp > 0)
+   {
+      sp--;
+      int l = stl[sp], r = str[sp];
+      while (l < r)
+      {
+         sw2(v, w, l, (l + r) / 2);
+         int last = l;
+         for (int i = l + 1; i <= r; i++) { if (fabs(w[i]) > fabs(w[l])) { sw2(v, w, ++last, i); } }
+         sw2(v, w, l, last);
+         // ranges [l, last-1] and [last+1, r]: continue with the smaller one
+         if (last - l < r - last)
+         {
+            if (last + 1 < r) { stl[sp] = last + 1; str[sp] = r; sp++; }
+            r = last - 1;
+         }
+         else
+         {
+            if (l < last - 1) { stl[sp] = l; str[sp] = last - 1; sp++; }
+            l = last + 1;
+         }
+      }
+   }
+}
+
+__global__ void k_truncate_rows(int n, const int *__restrict__ Pi, int *__restrict__ Pj, double *__restrict__ Pv,
+                                double tol, int max_elmts, int *__restrict__ newcnt)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int b = Pi[i], e = Pi[i + 1];
+   int len = e - b;
+   if (tol > 0)
+   {
+      double row_nrm = 0;
+      for (int k = b; k < e; k++) { double a = fabs(Pv[k]); row_nrm = row_nrm < a ? a : row_nrm; }
+      double drop = tol * row_nrm;
+      double row_sum = 0, scale = 0;
+      int w = b;
+      for (int k = b; k < e; k++)
+      {
+         double v = Pv[k];
+         row_sum += v;
+         if (!(fabs(v) < drop)) { scale += v; Pv[w] = v; Pj[w] = Pj[k]; w++; }
+      }
+      if (scale != 0. && scale != row_sum)
+      {
+         scale = row_sum / scale;
+         for (int k = b; k < w; k++) { Pv[k] *= scale; }
+      }
+      len = w - b;
+   }
+   if (max_elmts > 0 && max_elmts < len)
+   {
+      double row_sum = 0;
+      for (int k = b; k < b + len; k++) { row_sum += Pv[k]; }
+      qsort2_abs_iter(Pj + b, Pv + b, 0, len - 1);
+      double scale = 0;
+      for (int k = 0; k < max_elmts; k++) { scale += Pv[b + k]; }
+      if (scale != 0. && scale != row_sum)
+      {
+         scale = row_sum / scale;
+         for (int k = 0; k < max_elmts; k++) { Pv[b + k] *= scale; }
+      }
+      len = max_elmts;
+   }
+   newcnt[i] = len;
+}
+
+__global__ void k_compact_rows(int n, const int *__restrict__ Pi, const int *__restrict__ Pj,
+                               const double *__restrict__ Pv, const int *__restrict__ Ni, int *__restrict__ Nj,
+                               double *__restrict__ Nv)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int b = Pi[i], nb = Ni[i], len = Ni[i + 1] - Ni[i];
+   for (int k = 0; k < len; k++) { Nj[nb + k] = Pj[b + k]; Nv[nb + k] = Pv[b + k]; }
+}
+
+extern "C" void gb_truncate_rows(int n, const int *Pi, int *Pj, double *Pv, double tol, int max_elmts, int *newcnt,
+                                 cudaStream_t s)
+{
+   k_truncate_rows<<<gb_blocks(n, 128), 128, 0, s>>>(n, Pi, Pj, Pv, tol, max_elmts, newcnt);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_compact_rows(int n, const int *Pi, const int *Pj, const double *Pv, const int *Ni, int *Nj,
+                                double *Nv, cudaStream_t s)
+{
+   k_compact_rows<<<gb_blocks(n, 128), 128, 0, s>>>(n, Pi, Pj, Pv, Ni, Nj, Nv);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Transpose (reference: hypre_CSRMatrixTransposeHost src/seq_mv/csr_matop.c:1071,
+// a counting sort: rows of A^T list A's rows in ascending order).  Scatter with
+// atomics, then sort each output row by row index (entries are unique).
+// ---------------------------------------------------------------------------
+__global__ void k_tr_count(int nnz, const int *__restrict__ Aj, int *__restrict__ cnt)
+{
+   int k = blockIdx.x * blockDim.x + threadIdx.x;
+   if (k < nnz) { atomicAdd(&cnt[Aj[k]], 1); }
+}
+
+__global__ void k_tr_scatter(int nr, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                             const double *__restrict__ Av, int *__restrict__ fill, int *__restrict__ Tj,
+                             double *__restrict__ Tv)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nr) { return; }
+   for (int k = Ai[r]; k < Ai[r + 1]; k++)
+   {
+      int p = atomicAdd(&fill[Aj[k]], 1);
+      Tj[p] = r;
+      if (Av) { Tv[p] = Av[k]; }
+   }
+}
+
+__global__ void k_tr_sort(int nc, const int *__restrict__ Ti, int *__restrict__ Tj, double *__restrict__ Tv)
+{
+   int c = blockIdx.x * blockDim.x + threadIdx.x;
+   if (c >= nc) { return; }
+   int b = Ti[c], e = Ti[c + 1];
+   // shell sort by row index (keys unique); values follow
+   int len = e - b;
+   for (int gap = len / 2; gap > 0; gap /= 2)
+   {
+      for (int x = b + gap; x < e; x++)
+      {
+         int kj = Tj[x];
+         double kv = Tv ? Tv[x] : 0.0;
+         int y = x;
+         while (y - gap >= b && Tj[y - gap] > kj)
+         {
+            Tj[y] = Tj[y - gap];
+            if (Tv) { Tv[y] = Tv[y - gap]; }
+            y -= gap;
+         }
+         Tj[y] = kj;
+         if (Tv) { Tv[y] = kv; }
+      }
+   }
+}
+
+extern "C" void gb_transpose_count(int nnz, const int *Aj, int *cnt, cudaStream_t s)
+{
+   if (nnz > 0) { k_tr_count<<<gb_blocks(nnz, 256), 256, 0, s>>>(nnz, Aj, cnt); GB_COUNT(1); }
+}
+
+extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, const double *Av, int *fill,
+                                  const int *Ti, int *Tj, double *Tv, cudaStream_t s)
+{
+   k_tr_scatter<<<gb_blocks(nr, 256), 256, 0, s>>>(nr, Ai, Aj, Av, fill, Tj, Tv);
+   k_tr_sort<<<gb_blocks(nc, 128), 128, 0, s>>>(nc, Ti, Tj, Tv);
+   GB_COUNT(2);
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin product A_c = R A P with R = P^T (reference:
+// hypre_BoomerAMGBuildCoarseOperatorKT src/parcsr_ls/par_rap.c:30, numeric
+// pass :1640-1880).  Per coarse row ic: the diagonal first (value 0, then
+// accumulated), RA row built in discovery order over (R row x A rows), then
+// RAP entries in discovery order over (RA entries x P rows).
+// ---------------------------------------------------------------------------
+
+// Upper bounds: apub[i] = sum_{j in A_i} |P_j| for fine rows; per coarse row
+// ubRA = sum_{i1 in R_ic} |A_i1|, ubRAP = 1 + sum_{i1 in R_ic} apub[i1].
+__global__ void k_rap_apub(int nf, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                           const int *__restrict__ Pi, int *__restrict__ apub)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= nf) { return; }
+   long long u = 0;
+   for (int k = Ai[i]; k < Ai[i + 1]; k++) { int j = Aj[k]; u += Pi[j + 1] - Pi[j]; }
+   apub[i] = (int) (u > 0x3fffffff ? 0x3fffffff : u);
+}
+
+__global__ void k_rap_ub(int nc, int nf, const int *__restrict__ Ri, const int *__restrict__ Rj,
+                         const int *__restrict__ Ai, const int *__restrict__ apub, int *__restrict__ ubra,
+                         int *__restrict__ ubrap)
+{
+   int ic = blockIdx.x * blockDim.x + threadIdx.x;
+   if (ic >= nc) { return; }
+   long long a = 0, b = 1;
+   for (int k = Ri[ic]; k < Ri[ic + 1]; k++)
+   {
+      int i1 = Rj[k];
+      a += Ai[i1 + 1] - Ai[i1];
+      b += apub[i1];
+   }
+   if (a > nf) { a = nf; }
+   if (b > nc) { b = nc; }
+   ubra[ic] = (int) a;
+   ubrap[ic] = (int) b;
+}
+
+// Builds one RAP row; numeric=false only counts.  Ta: RA table, Tc: RAP table.
+__device__ __forceinline__ int rap_row(int ic, const int *__restrict__ Ri, const int *__restrict__ Rj,
+                                       const double *__restrict__ Rv, const int *__restrict__ Ai,
+                                       const int *__restrict__ Aj, const double *__restrict__ Av,
+                                       const int *__restrict__ Pi, const int *__restrict__ Pj,
+                                       const double *__restrict__ Pv, GbSlab &Ta, GbSlab &Tc, bool numeric,
+                                       int *Cj_row, double *Cv_row, int *overflow)
+{
+   const int lane = gb_lane();
+   int nra = 0;
+   for (int k1 = Ri[ic]; k1 < Ri[ic + 1]; k1++)
+   {
+      int i1 = Rj[k1];
+      double r = numeric ? Rv[k1] : 0.0;
+      int b = Ai[i1], e = Ai[i1 + 1];
+      for (int base = b; base < e; base += 32)
+      {
+         int k2 = base + lane;
+         bool act = k2 < e;
+         int i2 = act ? Aj[k2] : -1;
+         bool created;
+         int pos = gb_warp_insert(Ta.hk, Ta.hp, Ta.cap, Ta.lkeys, Ta.lslot, Ta.listcap, nra, i2, act, &created,
+                                  overflow);
+         if (numeric && act && pos >= 0)
+         {
+            double ra = r * Av[k2];
+            if (created) { Ta.lvals[pos] = ra; }
+            else { Ta.lvals[pos] += ra; }
+         }
+         __syncwarp();
+      }
+   }
+   // RAP row: diagonal first
+   int nc_row = 0;
+   {
+      bool created;
+      int pos = gb_warp_insert(Tc.hk, Tc.hp, Tc.cap, Tc.lkeys, Tc.lslot, Tc.listcap, nc_row, ic, lane == 0,
+                               &created, overflow);
+      if (numeric && lane == 0 && pos >= 0) { Cj_row[pos] = ic; Cv_row[pos] = 0.0; }
+      __syncwarp();
+   }
+   for (int t = 0; t < nra; t++)
+   {
+      int i1 = Ta.lkeys[t];
+      double ra = numeric ? Ta.lvals[t] : 0.0;
+      int b = Pi[i1], e = Pi[i1 + 1];
+      for (int base = b; base < e; base += 32)
+      {
+         int k3 = base + lane;
+         bool act = k3 < e;
+         int i3 = act ? Pj[k3] : -1;
+         bool created;
+         int pos = gb_warp_insert(Tc.hk, Tc.hp, Tc.cap, Tc.lkeys, Tc.lslot, Tc.listcap, nc_row, i3, act, &created,
+                                  overflow);
+         if (numeric && act && pos >= 0)
+         {
+            double v = ra * Pv[k3];
+            if (created) { Cj_row[pos] = i3; Cv_row[pos] = v; }
+            else { Cv_row[pos] += v; }
+         }
+         __syncwarp();
+      }
+   }
+   gb_warp_clear(Ta.hk, Ta.lslot, nra);
+   gb_warp_clear(Tc.hk, Tc.lslot, nc_row);
+   return nc_row;
+}
+
+__global__ void k_rap(int nc, const int *__restrict__ Ri, const int *__restrict__ Rj, const double *__restrict__ Rv,
+                      const int *__restrict__ Ai, const int *__restrict__ Aj, const double *__restrict__ Av,
+                      const int *__restrict__ Pi, const int *__restrict__ Pj, const double *__restrict__ Pv,
+                      char *slab_a, int cap_a, char *slab_c, int cap_c, int numeric, const int *__restrict__ Ci,
+                      int *__restrict__ Cj, double *__restrict__ Cv, int *__restrict__ cnt, int *overflow)
+{
+   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   int nwarps = (gridDim.x * blockDim.x) >> 5;
+   GbSlab Ta = gb_slab(slab_a, cap_a, warp);
+   GbSlab Tc = gb_slab(slab_c, cap_c, warp);
+   for (int ic = warp; ic < nc; ic += nwarps)
+   {
+      int off = numeric ? Ci[ic] : 0;
+      int c = rap_row(ic, Ri, Rj, Rv, Ai, Aj, Av, Pi, Pj, Pv, Ta, Tc, numeric != 0, numeric ? Cj + off : nullptr,
+                      numeric ? Cv + off : nullptr, overflow);
+      if (!numeric && gb_lane() == 0) { cnt[ic] = c; }
+   }
+}
+
+extern "C" void gb_rap_bounds(int nf, int nc, const int *Ri, const int *Rj, const int *Ai, const int *Aj,
+                              const int *Pi, int *apub, int *ubra, int *ubrap, cudaStream_t s)
+{
+   k_rap_apub<<<gb_blocks(nf, 256), 256, 0, s>>>(nf, Ai, Aj, Pi, apub);
+   k_rap_ub<<<gb_blocks(nc, 256), 256, 0, s>>>(nc, nf, Ri, Rj, Ai, apub, ubra, ubrap);
+   GB_COUNT(2);
+}
+
+extern "C" void gb_rap(int nc, const int *Ri, const int *Rj, const double *Rv, const int *Ai, const int *Aj,
+                       const double *Av, const int *Pi, const int *Pj, const double *Pv, char *slab_a, int cap_a,
+                       char *slab_c, int cap_c, int nwarps, int numeric, const int *Ci, int *Cj, double *Cv,
+                       int *cnt, int *overflow, cudaStream_t s)
+{
+   int threads = 128;
+   int blocks = (nwarps * 32 + threads - 1) / threads;
+   k_rap<<<blocks, threads, 0, s>>>(nc, Ri, Rj, Rv, Ai, Aj, Av, Pi, Pj, Pv, slab_a, cap_a, slab_c, cap_c, numeric,
+                                    Ci, Cj, Cv, cnt, overflow);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// l1 norms (reference: hypre_ParCSRComputeL1Norms src/parcsr_ls/ams.c:517-790)
+// option 1: sum_j |a_ij|; option 5: a_ii (0 -> 1); rows with a_ii < 0 negated.
+// ---------------------------------------------------------------------------
+__global__ void k_l1(int n, const int *__restrict__ Ai, const int *__restrict__ Aj, const double *__restrict__ Av,
+                     int option, double *__restrict__ l1)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   double d = 0.0, s = 0.0;
+   for (int k = Ai[i]; k < Ai[i + 1]; k++)
+   {
+      double v = Av[k];
+      if (Aj[k] == i) { d = v; }
+      s += fabs(v);
+   }
+   double r = option == 1 ? s : (d != 0.0 ? d : 1.0);
+   if (d < 0.0) { r = -r; }
+   l1[i] = r;
+}
+
+extern "C" void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, double *l1,
+                            cudaStream_t s)
+{
+   k_l1<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, option, l1);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Coarsest grid: dense copy and inverse (Gauss-Jordan without pivoting, as the
+// reference's unpivoted elimination hypre_gselim, src/utilities/gselim.h).
+// ---------------------------------------------------------------------------
+__global__ void k_to_dense(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                           const double *__restrict__ Av, double *__restrict__ D)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   for (int j = 0; j < n; j++) { D[(size_t) i * n + j] = 0.0; }
+   for (int k = Ai[i]; k < Ai[i + 1]; k++) { D[(size_t) i * n + Aj[k]] = Av[k]; }
+}
+
+// One block; D (n x n, row major) is replaced by its inverse, W is n x n work.
+__global__ void k_gauss_jordan(int n, double *D, double *W)
+{
+   // W = I
+   for (int t = threadIdx.x; t < n * n; t += blockDim.x) { W[t] = (t / n == t % n) ? 1.0 : 0.0; }
+   __syncthreads();
+   __shared__ double piv;
+   for (int k = 0; k < n; k++)
+   {
+      if (threadIdx.x == 0) { piv = D[(size_t) k * n + k]; }
+      __syncthreads();
+      if (piv != 0.0)
+      {
+         double inv = 1.0 / piv;
+         for (int j = threadIdx.x; j < n; j += blockDim.x)
+         {
+            D[(size_t) k * n + j] *= inv;
+            W[(size_t) k * n + j] *= inv;
+         }
+         __syncthreads();
+         for (int t = threadIdx.x; t < n * n; t += blockDim.x)
+         {
+            int r = t / n, j = t % n;
+            if (r == k) { continue; }
+            double f = D[(size_t) r * n + k];
+            if (j == k) { continue; }
+            if (f != 0.0)
+            {
+               D[(size_t) r * n + j] -= f * D[(size_t) k * n + j];
+               W[(size_t) r * n + j] -= f * W[(size_t) k * n + j];
+            }
+         }
+         __syncthreads();
+         // column k: D[r][k] -= f * D[k][k] (=1) -> 0, and W column k
+         for (int r = threadIdx.x; r < n; r += blockDim.x)
+         {
+            if (r == k) { continue; }
+            double f = D[(size_t) r * n + k];
+            if (f != 0.0)
+            {
+               W[(size_t) r * n + k] -= f * W[(size_t) k * n + k];
+               D[(size_t) r * n + k] = 0.0;
+            }
+         }
+      }
+      __syncthreads();
+   }
+   for (int t = threadIdx.x; t < n * n; t += blockDim.x) { D[t] = W[t]; }
+}
+
+extern "C" void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, double *D, double *W,
+                                 cudaStream_t s)
+{
+   k_to_dense<<<gb_blocks(n, 128), 128, 0, s>>>(n, Ai, Aj, Av, D);
+   k_gauss_jordan<<<1, 1024, 0, s>>>(n, D, W);
+   GB_COUNT(2);
+}

@@ -1,0 +1,589 @@
+// Solve-phase kernels for sm_103a: SpMV in two layouts (CSR with K lanes per
+// row, and SELL-32 with one thread per row for near-uniform rows), fused
+// smoother sweeps, Krylov vector operations with deterministic two-stage
+// reductions, precision conversions and the dense coarsest-grid apply.
+//
+// All kernels are HBM-bandwidth bound.  Value and vector types are template
+// parameters: FP64 values/vectors (reference arithmetic), FP32 values/vectors
+// (mixed-precision cycle) and FP16 values with FP32 vectors and accumulation.
+#include "gb_device.cuh"
+#include "gb_kernels.h"
+
+#include <cuda_fp16.h>
+
+static int nblk(long long n, int t) { long long b = (n + t - 1) / t; return (int) (b < 1 ? 1 : b); }
+
+template <typename T> __device__ __forceinline__ float tof(T v);
+template <> __device__ __forceinline__ float tof<float>(float v) { return v; }
+template <> __device__ __forceinline__ float tof<__half>(__half v) { return __half2float(v); }
+
+template <typename VT, typename XT> struct Acc;
+template <> struct Acc<double, double>
+{
+   typedef double T;
+   static __device__ __forceinline__ double mul(double a, double x) { return a * x; }
+};
+template <> struct Acc<float, float>
+{
+   typedef float T;
+   static __device__ __forceinline__ float mul(float a, float x) { return a * x; }
+};
+template <> struct Acc<__half, float>
+{
+   typedef float T;
+   static __device__ __forceinline__ float mul(__half a, float x) { return __half2float(a) * x; }
+};
+
+// Epilogue of a row: mode 0  y = alpha*s + beta*b
+//                    mode 1  y = x_i + w*(b_i - s)/d_i   (l1 / diagonal Jacobi)
+//                    mode 2  y = (b_i - s) for residuals   (alpha=-1, beta=1 shortcut)
+template <typename XT>
+__device__ __forceinline__ XT row_epilogue(int mode, XT s, int i, XT alpha, XT beta, const XT *b, const XT *x,
+                                           const XT *d, XT w)
+{
+   if (mode == 1) { return x[i] + w * (b[i] - s) / d[i]; }
+   if (mode == 2) { return b[i] - s; }
+   XT y = alpha * s;
+   if (beta != (XT) 0) { y += beta * b[i]; }
+   return y;
+}
+
+// Block-level sum of v (fixed reduction tree: deterministic), lane 0 of warp 0
+// holds the result.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v)
+{
+   __shared__ T red[32];
+   for (int o = 16; o > 0; o >>= 1) { v += __shfl_down_sync(GB_FULL, v, o); }
+   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   __syncthreads();
+   if (lane == 0) { red[wid] = v; }
+   __syncthreads();
+   T t = 0;
+   if (wid == 0)
+   {
+      int nw = (blockDim.x + 31) >> 5;
+      t = lane < nw ? red[lane] : (T) 0;
+      for (int o = 16; o > 0; o >>= 1) { t += __shfl_down_sync(GB_FULL, t, o); }
+   }
+   return t;
+}
+
+// ---------------------------------------------------------------------------
+// CSR SpMV, K lanes per row (K in 2..32), rows distributed over the grid.
+// dotz (optional): per-block partial sums of y_i * z_i written to dpart.
+// ---------------------------------------------------------------------------
+template <int K, typename VT, typename XT>
+__global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                                                  const VT *__restrict__ Av, const XT *__restrict__ x, XT *y,
+                                                  int mode, XT alpha, XT beta, const XT *b, const XT *d, XT w,
+                                                  const XT *__restrict__ dotz, double *dpart)
+{
+   typedef typename Acc<VT, XT>::T AT;
+   const int gpw = 32 / K;                       // row groups per warp
+   const int wl = threadIdx.x & 31;
+   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+   const int lane = wl % K;
+   double dsum = 0.0;
+   for (int base = warp * gpw; base < n; base += nwarps * gpw)
+   {
+      int i = base + wl / K;
+      bool valid = i < n;
+      AT s = 0;
+      if (valid)
+      {
+         int b0 = __ldg(Ai + i), e0 = __ldg(Ai + i + 1);
+         for (int k = b0 + lane; k < e0; k += K) { s += Acc<VT, XT>::mul(__ldg(Av + k), __ldg(x + __ldg(Aj + k))); }
+      }
+      for (int o = K / 2; o > 0; o >>= 1) { s += __shfl_down_sync(GB_FULL, s, o, K); }
+      if (valid && lane == 0)
+      {
+         XT yi = row_epilogue<XT>(mode, (XT) s, i, alpha, beta, b, x, d, w);
+         y[i] = yi;
+         if (dotz) { dsum += (double) yi * (double) dotz[i]; }
+      }
+   }
+   if (dpart)
+   {
+      double t = block_sum<double>(dsum);
+      if (threadIdx.x == 0) { dpart[blockIdx.x] = t; }
+   }
+}
+
+// ---------------------------------------------------------------------------
+// SELL-32 SpMV: slice s holds rows 32s..32s+31, element k of row 32s+t at
+// sl_ptr[s] + 32k + t, so a warp's loads are fully coalesced (256 B values,
+// 128 B indices per instruction for FP64).  Padding: column 0, value 0.
+// ---------------------------------------------------------------------------
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const long long *__restrict__ sl_ptr,
+                                                   const int *__restrict__ sl_w, const int *__restrict__ Sj,
+                                                   const VT *__restrict__ Sv, const XT *__restrict__ x, XT *y,
+                                                   int mode, XT alpha, XT beta, const XT *b, const XT *d, XT w,
+                                                   const XT *__restrict__ dotz, double *dpart)
+{
+   typedef typename Acc<VT, XT>::T AT;
+   const int t = threadIdx.x & 31;
+   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+   double dsum = 0.0;
+   for (int s = warp; s < nslices; s += nwarps)
+   {
+      long long base = __ldg(sl_ptr + s) + t;
+      int width = __ldg(sl_w + s);
+      AT acc0 = 0, acc1 = 0;
+      int k = 0;
+      for (; k + 1 < width; k += 2)
+      {
+         long long p0 = base + (long long) k * 32, p1 = p0 + 32;
+         int j0 = __ldg(Sj + p0), j1 = __ldg(Sj + p1);
+         VT a0 = __ldg(Sv + p0), a1 = __ldg(Sv + p1);
+         acc0 += Acc<VT, XT>::mul(a0, __ldg(x + j0));
+         acc1 += Acc<VT, XT>::mul(a1, __ldg(x + j1));
+      }
+      if (k < width)
+      {
+         long long p0 = base + (long long) k * 32;
+         acc0 += Acc<VT, XT>::mul(__ldg(Sv + p0), __ldg(x + __ldg(Sj + p0)));
+      }
+      int i = s * 32 + t;
+      if (i < n)
+      {
+         XT yi = row_epilogue<XT>(mode, (XT) (acc0 + acc1), i, alpha, beta, b, x, d, w);
+         y[i] = yi;
+         if (dotz) { dsum += (double) yi * (double) dotz[i]; }
+      }
+   }
+   if (dpart)
+   {
+      double tt = block_sum<double>(dsum);
+      if (threadIdx.x == 0) { dpart[blockIdx.x] = tt; }
+   }
+}
+
+// SELL-32 construction: slice widths, then fill (values converted to VT).
+__global__ void k_sell_width(int n, int nslices, const int *__restrict__ Ai, int *__restrict__ w)
+{
+   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   if (s >= nslices) { return; }
+   int m = 0;
+   for (int t = 0; t < 32; t++)
+   {
+      int i = s * 32 + t;
+      if (i < n) { int l = Ai[i + 1] - Ai[i]; m = l > m ? l : m; }
+   }
+   w[s] = m;
+}
+
+__global__ void k_sell_ptr(int nslices, const int *__restrict__ w, long long *__restrict__ ptr)
+{
+   // single thread prefix (nslices is n/32; run once per matrix at setup)
+   if (blockIdx.x == 0 && threadIdx.x == 0)
+   {
+      long long p = 0;
+      for (int s = 0; s < nslices; s++) { ptr[s] = p; p += (long long) w[s] * 32; }
+      ptr[nslices] = p;
+   }
+}
+
+template <typename VT>
+__global__ void k_sell_fill(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                            const double *__restrict__ Av, const long long *__restrict__ ptr,
+                            const int *__restrict__ w, int *__restrict__ Sj, VT *__restrict__ Sv)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   int s = i >> 5, t = i & 31;
+   if (s >= nslices) { return; }
+   int width = w[s];
+   long long base = ptr[s] + t;
+   int b = 0, e = 0;
+   if (i < n) { b = Ai[i]; e = Ai[i + 1]; }
+   for (int k = 0; k < width; k++)
+   {
+      long long p = base + (long long) k * 32;
+      if (b + k < e) { Sj[p] = Aj[b + k]; Sv[p] = (VT) Av[b + k]; }
+      else { Sj[p] = i < n ? i : 0; Sv[p] = (VT) 0.0; }
+   }
+}
+
+template <typename VT>
+__global__ void k_convert_vals(long long nnz, const double *__restrict__ in, VT *__restrict__ out)
+{
+   long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (k < nnz) { out[k] = (VT) in[k]; }
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+static int g_num_sms = 0;
+static int num_sms()
+{
+   if (!g_num_sms)
+   {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+      if (g_num_sms <= 0) { g_num_sms = 148; }
+   }
+   return g_num_sms;
+}
+
+extern "C" int gb_num_sms(void) { return num_sms(); }
+
+extern "C" int gb_reduce_blocks(void) { return GB_RED_BLOCKS; }
+
+template <typename VT, typename XT>
+static void spmv_dispatch(const gb_spmv_desc *A, const XT *x, XT *y, int mode, XT alpha, XT beta, const XT *b,
+                          const XT *d, XT w, const XT *dotz, double *dpart, cudaStream_t st)
+{
+   const int T = 256;
+   if (A->fmt == GB_FMT_SELL)
+   {
+      int nsl = A->nslices;
+      int blocks = dpart ? GB_RED_BLOCKS : nblk((long long) nsl * 32, T);
+      k_spmv_sell<VT, XT><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, A->sl_j, (const VT *) A->sl_v, x, y,
+                                                 mode, alpha, beta, b, d, w, dotz, dpart);
+   }
+   else
+   {
+      int K = A->K;
+      long long threads = (long long) A->n * K;
+      int blocks = dpart ? GB_RED_BLOCKS : nblk(threads, T);
+      const VT *vals = (const VT *) A->v;
+#define LAUNCH_K(KK) k_spmv_csr<KK, VT, XT><<<blocks, T, 0, st>>>(A->n, A->i, A->j, vals, x, y, mode, alpha, beta, b, d, w, dotz, dpart)
+      switch (K)
+      {
+         case 2: LAUNCH_K(2); break;
+         case 4: LAUNCH_K(4); break;
+         case 8: LAUNCH_K(8); break;
+         case 16: LAUNCH_K(16); break;
+         default: LAUNCH_K(32); break;
+      }
+#undef LAUNCH_K
+   }
+   GB_COUNT(1);
+}
+
+extern "C" void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int mode, double alpha, double beta,
+                          const double *b, const double *d, double w, const double *dotz, double *dpart,
+                          cudaStream_t st)
+{
+   spmv_dispatch<double, double>(A, x, y, mode, alpha, beta, b, d, w, dotz, dpart, st);
+}
+
+extern "C" void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int mode, float alpha, float beta,
+                          const float *b, const float *d, float w, const float *dotz, double *dpart, cudaStream_t st)
+{
+   if (A->vprec == GB_PREC_F16)
+   {
+      spmv_dispatch<__half, float>(A, x, y, mode, alpha, beta, b, d, w, dotz, dpart, st);
+   }
+   else
+   {
+      spmv_dispatch<float, float>(A, x, y, mode, alpha, beta, b, d, w, dotz, dpart, st);
+   }
+}
+
+extern "C" void gb_sell_build(int n, const int *Ai, const int *Aj, const double *Av, int vprec, int nslices,
+                              int *sl_w, long long *sl_ptr, int *sl_j, void *sl_v, cudaStream_t s, int stage)
+{
+   // stage 0: widths + offsets (caller then reads sl_ptr[nslices] to size
+   // the arrays); stage 1: fill
+   if (stage == 0)
+   {
+      k_sell_width<<<nblk(nslices, 256), 256, 0, s>>>(n, nslices, Ai, sl_w);
+      k_sell_ptr<<<1, 1, 0, s>>>(nslices, sl_w, sl_ptr);
+      GB_COUNT(2);
+      return;
+   }
+   long long nt = (long long) nslices * 32;
+   if (vprec == GB_PREC_F64)
+   {
+      k_sell_fill<double><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, sl_j, (double *) sl_v);
+   }
+   else if (vprec == GB_PREC_F32)
+   {
+      k_sell_fill<float><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, sl_j, (float *) sl_v);
+   }
+   else
+   {
+      k_sell_fill<__half><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, sl_j, (__half *) sl_v);
+   }
+   GB_COUNT(1);
+}
+
+extern "C" void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s)
+{
+   if (nnz <= 0) { return; }
+   if (vprec == GB_PREC_F32) { k_convert_vals<float><<<nblk(nnz, 256), 256, 0, s>>>(nnz, in, (float *) out); }
+   else { k_convert_vals<__half><<<nblk(nnz, 256), 256, 0, s>>>(nnz, in, (__half *) out); }
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Two-stage Gauss-Seidel inner sweep (reference:
+// hypre_BoomerAMGRelaxTwoStageGaussSeidelHost src/parcsr_ls/par_relax.c:1506):
+// z_new_i = (sum_{j<i} a_ij z_j) / a_ii ; u_i += m * z_new_i.
+// The first entry of each row is the diagonal.
+// ---------------------------------------------------------------------------
+template <typename VT, typename XT>
+__global__ void k_gs_lower(int n, const int *__restrict__ Ai, const int *__restrict__ Aj, const VT *__restrict__ Av,
+                           const XT *__restrict__ z, XT *__restrict__ znew, XT *__restrict__ u, XT m)
+{
+   typedef typename Acc<VT, XT>::T AT;
+   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = tid >> 3, lane = tid & 7;
+   bool valid = i < n;
+   AT s = 0;
+   int b0 = 0;
+   if (valid)
+   {
+      b0 = Ai[i];
+      int e0 = Ai[i + 1];
+      for (int k = b0 + lane; k < e0; k += 8)
+      {
+         int j = Aj[k];
+         if (j < i) { s += Acc<VT, XT>::mul(Av[k], z[j]); }
+      }
+   }
+   for (int o = 4; o > 0; o >>= 1) { s += __shfl_down_sync(GB_FULL, s, o, 8); }
+   if (valid && lane == 0)
+   {
+      XT diag = (XT) Acc<VT, XT>::mul(Av[b0], (XT) 1);
+      XT zn = (XT) s / diag;
+      znew[i] = zn;
+      u[i] += m * zn;
+   }
+}
+
+template <typename VT, typename XT>
+__global__ void k_gs_first(int n, const int *__restrict__ Ai, const VT *__restrict__ Av, XT *__restrict__ v,
+                           XT *__restrict__ u)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   XT diag = (XT) Acc<VT, XT>::mul(Av[Ai[i]], (XT) 1);
+   XT z = v[i] / diag;
+   v[i] = z;
+   u[i] += z;
+}
+
+extern "C" void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s)
+{
+   k_gs_first<double, double><<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, v, u);
+   GB_COUNT(1);
+}
+extern "C" void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, float *v, float *u, cudaStream_t s)
+{
+   if (vprec == GB_PREC_F16) { k_gs_first<__half, float><<<nblk(n, 256), 256, 0, s>>>(n, Ai, (const __half *) Av, v, u); }
+   else { k_gs_first<float, float><<<nblk(n, 256), 256, 0, s>>>(n, Ai, (const float *) Av, v, u); }
+   GB_COUNT(1);
+}
+extern "C" void gb_gs_lower_d(int n, const int *Ai, const int *Aj, const double *Av, const double *z, double *znew,
+                              double *u, double m, cudaStream_t s)
+{
+   k_gs_lower<double, double><<<nblk((long long) n * 8, 256), 256, 0, s>>>(n, Ai, Aj, Av, z, znew, u, m);
+   GB_COUNT(1);
+}
+extern "C" void gb_gs_lower_f(int n, const int *Ai, const int *Aj, const void *Av, int vprec, const float *z,
+                              float *znew, float *u, float m, cudaStream_t s)
+{
+   if (vprec == GB_PREC_F16)
+   {
+      k_gs_lower<__half, float><<<nblk((long long) n * 8, 256), 256, 0, s>>>(n, Ai, Aj, (const __half *) Av, z, znew, u, m);
+   }
+   else
+   {
+      k_gs_lower<float, float><<<nblk((long long) n * 8, 256), 256, 0, s>>>(n, Ai, Aj, (const float *) Av, z, znew, u, m);
+   }
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Vector operations (FP64 unless suffixed _f)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_fill(long long n, T *x, T v)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { x[i] = v; }
+}
+template <typename T>
+__global__ void k_scale(long long n, T a, T *x)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { x[i] *= a; }
+}
+template <typename T>
+__global__ void k_axpy(long long n, T a, const T *__restrict__ x, T *__restrict__ y)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { y[i] += a * x[i]; }
+}
+template <typename T>
+__global__ void k_xpay(long long n, const T *__restrict__ x, T a, T *__restrict__ y)
+{
+   // y = x + a*y
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { y[i] = x[i] + a * y[i]; }
+}
+template <typename T>
+__global__ void k_scaled_div(long long n, T w, const T *__restrict__ f, const T *__restrict__ d, T *__restrict__ u)
+{
+   // u = w * f / d   (first Jacobi sweep from a zero guess)
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { u[i] = (w * f[i]) / d[i]; }
+}
+template <typename T>
+__global__ void k_scaled_copy(long long n, T w, const T *__restrict__ f, T *__restrict__ v)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { v[i] = w * f[i]; }
+}
+__global__ void k_d2f(long long n, const double *__restrict__ a, float *__restrict__ b)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { b[i] = (float) a[i]; }
+}
+__global__ void k_f2d(long long n, const float *__restrict__ a, double *__restrict__ b)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { b[i] = (double) a[i]; }
+}
+
+// dot products: partial sums per block over a fixed grid, then one block.
+__global__ void __launch_bounds__(256) k_dot_part(long long n, const double *__restrict__ x,
+                                                  const double *__restrict__ y, double *__restrict__ part)
+{
+   double s = 0.0;
+   for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+   {
+      s += x[i] * y[i];
+   }
+   double t = block_sum<double>(s);
+   if (threadIdx.x == 0) { part[blockIdx.x] = t; }
+}
+
+__global__ void __launch_bounds__(256) k_dot2_part(long long n, const double *__restrict__ x,
+                                                   const double *__restrict__ y, const double *__restrict__ z,
+                                                   double *__restrict__ part)
+{
+   // part[b] = sum x*y, part[nb + b] = sum x*z
+   double s = 0.0, t2 = 0.0;
+   for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+   {
+      double xi = x[i];
+      s += xi * y[i];
+      t2 += xi * z[i];
+   }
+   double a = block_sum<double>(s);
+   double c = block_sum<double>(t2);
+   if (threadIdx.x == 0) { part[blockIdx.x] = a; part[gridDim.x + blockIdx.x] = c; }
+}
+
+// x += a*p ; r -= a*s ; partial (r, r)
+__global__ void __launch_bounds__(256) k_pcg_xr(long long n, double a, const double *__restrict__ p,
+                                                const double *__restrict__ s, double *__restrict__ x,
+                                                double *__restrict__ r, double *__restrict__ part)
+{
+   double acc = 0.0;
+   for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+   {
+      x[i] += a * p[i];
+      double ri = r[i] + (-a) * s[i];
+      r[i] = ri;
+      acc += ri * ri;
+   }
+   double t = block_sum<double>(acc);
+   if (threadIdx.x == 0) { part[blockIdx.x] = t; }
+}
+
+__global__ void k_final_sum(int nparts, int nsums, const double *__restrict__ part, double *__restrict__ out)
+{
+   // one block; out[q] = sum_b part[q*nparts + b] in a fixed order
+   for (int q = 0; q < nsums; q++)
+   {
+      double s = 0.0;
+      for (int b = threadIdx.x; b < nparts; b += blockDim.x) { s += part[(size_t) q * nparts + b]; }
+      double t = block_sum<double>(s);
+      if (threadIdx.x == 0) { out[q] = t; }
+      __syncthreads();
+   }
+}
+
+extern "C" void gb_fill_d(long long n, double *x, double v, cudaStream_t s)
+{ if (n > 0) { k_fill<double><<<nblk(n, 256), 256, 0, s>>>(n, x, v); GB_COUNT(1); } }
+extern "C" void gb_fill_f(long long n, float *x, float v, cudaStream_t s)
+{ if (n > 0) { k_fill<float><<<nblk(n, 256), 256, 0, s>>>(n, x, v); GB_COUNT(1); } }
+extern "C" void gb_scale_d(long long n, double a, double *x, cudaStream_t s)
+{ if (n > 0) { k_scale<double><<<nblk(n, 256), 256, 0, s>>>(n, a, x); GB_COUNT(1); } }
+extern "C" void gb_axpy_d(long long n, double a, const double *x, double *y, cudaStream_t s)
+{ if (n > 0) { k_axpy<double><<<nblk(n, 256), 256, 0, s>>>(n, a, x, y); GB_COUNT(1); } }
+extern "C" void gb_xpay_d(long long n, const double *x, double a, double *y, cudaStream_t s)
+{ if (n > 0) { k_xpay<double><<<nblk(n, 256), 256, 0, s>>>(n, x, a, y); GB_COUNT(1); } }
+extern "C" void gb_scaled_div_d(long long n, double w, const double *f, const double *d, double *u, cudaStream_t s)
+{ if (n > 0) { k_scaled_div<double><<<nblk(n, 256), 256, 0, s>>>(n, w, f, d, u); GB_COUNT(1); } }
+extern "C" void gb_scaled_div_f(long long n, float w, const float *f, const float *d, float *u, cudaStream_t s)
+{ if (n > 0) { k_scaled_div<float><<<nblk(n, 256), 256, 0, s>>>(n, w, f, d, u); GB_COUNT(1); } }
+extern "C" void gb_scaled_copy_d(long long n, double w, const double *f, double *v, cudaStream_t s)
+{ if (n > 0) { k_scaled_copy<double><<<nblk(n, 256), 256, 0, s>>>(n, w, f, v); GB_COUNT(1); } }
+extern "C" void gb_scaled_copy_f(long long n, float w, const float *f, float *v, cudaStream_t s)
+{ if (n > 0) { k_scaled_copy<float><<<nblk(n, 256), 256, 0, s>>>(n, w, f, v); GB_COUNT(1); } }
+extern "C" void gb_d2f(long long n, const double *a, float *b, cudaStream_t s)
+{ if (n > 0) { k_d2f<<<nblk(n, 256), 256, 0, s>>>(n, a, b); GB_COUNT(1); } }
+extern "C" void gb_f2d(long long n, const float *a, double *b, cudaStream_t s)
+{ if (n > 0) { k_f2d<<<nblk(n, 256), 256, 0, s>>>(n, a, b); GB_COUNT(1); } }
+
+extern "C" void gb_dot_d(long long n, const double *x, const double *y, double *part, double *out, cudaStream_t s)
+{
+   k_dot_part<<<GB_RED_BLOCKS, 256, 0, s>>>(n, x, y, part);
+   k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
+   GB_COUNT(2);
+}
+extern "C" void gb_dot2_d(long long n, const double *x, const double *y, const double *z, double *part, double *out,
+                          cudaStream_t s)
+{
+   k_dot2_part<<<GB_RED_BLOCKS, 256, 0, s>>>(n, x, y, z, part);
+   k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 2, part, out);
+   GB_COUNT(2);
+}
+extern "C" void gb_pcg_xr_d(long long n, double a, const double *p, const double *sv, double *x, double *r,
+                            double *part, double *out, cudaStream_t s)
+{
+   k_pcg_xr<<<GB_RED_BLOCKS, 256, 0, s>>>(n, a, p, sv, x, r, part);
+   k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
+   GB_COUNT(2);
+}
+extern "C" void gb_final_sum(int nparts, int nsums, const double *part, double *out, cudaStream_t s)
+{
+   k_final_sum<<<1, 1024, 0, s>>>(nparts, nsums, part, out);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Dense coarsest-grid apply: u = Dinv * f (n small)
+// ---------------------------------------------------------------------------
+template <typename XT>
+__global__ void k_dense_apply(int n, const double *__restrict__ D, const XT *__restrict__ f, XT *__restrict__ u)
+{
+   int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+   int lane = threadIdx.x & 31;
+   if (i >= n) { return; }
+   double s = 0.0;
+   for (int j = lane; j < n; j += 32) { s += D[(size_t) i * n + j] * (double) f[j]; }
+   for (int o = 16; o > 0; o >>= 1) { s += __shfl_down_sync(GB_FULL, s, o); }
+   if (lane == 0) { u[i] = (XT) s; }
+}
+
+extern "C" void gb_dense_apply_d(int n, const double *D, const double *f, double *u, cudaStream_t s)
+{
+   k_dense_apply<double><<<nblk(n, 8), 256, 0, s>>>(n, D, f, u);
+   GB_COUNT(1);
+}
+extern "C" void gb_dense_apply_f(int n, const double *D, const float *f, float *u, cudaStream_t s)
+{
+   k_dense_apply<float><<<nblk(n, 8), 256, 0, s>>>(n, D, f, u);
+   GB_COUNT(1);
+}

@@ -1081,46 +1081,54 @@ int or_pcg(const or_csr *A, or_hierarchy *H, const double *b, double *x,
 int or_fgmres(const or_csr *A, or_hierarchy *H, const double *b, double *x,
               double tol, int maxit, int kdim, double *resnorms, int *iters)
 {
+   /* hypre_FlexGMRESSolve, src/krylov/flexgmres.c:288-800 (a_tol 0, no
+    * rel_change, min_iter 0): right preconditioning, modified Gram-Schmidt,
+    * Givens rotations, restart residual rebuilt from the Krylov basis */
    int n = A->nr;
-   double **V = xmalloc(sizeof(double *) * (kdim + 1));
-   double **Z = xmalloc(sizeof(double *) * (kdim + 1));
-   for (int k = 0; k <= kdim; k++) { V[k] = xcalloc(n, sizeof(double)); Z[k] = xcalloc(n, sizeof(double)); }
+   double **p = xmalloc(sizeof(double *) * (kdim + 1));
+   double **pre = xmalloc(sizeof(double *) * (kdim + 1));
+   for (int k = 0; k <= kdim; k++) { p[k] = xcalloc(n, sizeof(double)); pre[k] = xcalloc(n, sizeof(double)); }
+   double *r = xcalloc(n, sizeof(double)), *w = xcalloc(n, sizeof(double));
    double *hh = xcalloc((size_t) (kdim + 1) * kdim, sizeof(double));
    double *c = xcalloc(kdim, sizeof(double)), *s = xcalloc(kdim, sizeof(double));
    double *rs = xcalloc(kdim + 1, sizeof(double));
 #define HH(i, j) hh[(size_t) (i) * kdim + (j)]
+   or_matvec(-1.0, A, x, 1.0, b, p[0]);
    double b_norm = sqrt(or_dot(n, b, b));
-   or_matvec(-1.0, A, x, 1.0, b, V[0]);
-   double r_norm = sqrt(or_dot(n, V[0], V[0]));
+   double r_norm = sqrt(or_dot(n, p[0], p[0]));
    if (resnorms) { resnorms[0] = r_norm; }
-   double epsilon = tol * b_norm;
-   int iter = 0, conv = 0;
-   if (b_norm == 0.0 || r_norm <= epsilon) { *iters = 0; conv = 1; }
-   while (!conv && iter < maxit)
+   double den = b_norm > 0.0 ? b_norm : r_norm;
+   double epsilon = tol * den;
+   int iter = 0, conv = 0, i = 0;
+   while (iter < maxit)
    {
-      if (r_norm == 0.0) { conv = 1; break; }
-      double t = 1.0 / r_norm;
-      for (int k = 0; k < n; k++) { V[0][k] *= t; }
       rs[0] = r_norm;
-      int i = 0;
+      if (r_norm == 0.0) { conv = 1; break; }
+      if (r_norm <= epsilon)
+      {
+         or_matvec(-1.0, A, x, 1.0, b, r);
+         r_norm = sqrt(or_dot(n, r, r));
+         if (r_norm <= epsilon) { conv = 1; break; }
+      }
+      double t = 1.0 / r_norm;
+      for (int k = 0; k < n; k++) { p[0][k] *= t; }
+      i = 0;
       while (i < kdim && iter < maxit)
       {
          i++;
          iter++;
-         memset(Z[i - 1], 0, sizeof(double) * n);
-         or_amg_vcycle(H, V[i - 1], Z[i - 1]);
-         or_matvec(1.0, A, Z[i - 1], 0.0, NULL, V[i]);
-         /* modified Gram-Schmidt (:575-585) */
+         memset(pre[i - 1], 0, sizeof(double) * n);
+         or_amg_vcycle(H, p[i - 1], pre[i - 1]);
+         or_matvec(1.0, A, pre[i - 1], 0.0, NULL, p[i]);
          for (int j = 0; j < i; j++)
          {
-            HH(j, i - 1) = or_dot(n, V[j], V[i]);
+            HH(j, i - 1) = or_dot(n, p[j], p[i]);
             double h = -HH(j, i - 1);
-            for (int k = 0; k < n; k++) { V[i][k] += h * V[j][k]; }
+            for (int k = 0; k < n; k++) { p[i][k] += h * p[j][k]; }
          }
-         t = sqrt(or_dot(n, V[i], V[i]));
+         t = sqrt(or_dot(n, p[i], p[i]));
          HH(i, i - 1) = t;
-         if (t != 0.0) { t = 1.0 / t; for (int k = 0; k < n; k++) { V[i][k] *= t; } }
-         /* Givens rotations (:590-610) */
+         if (t != 0.0) { t = 1.0 / t; for (int k = 0; k < n; k++) { p[i][k] *= t; } }
          for (int j = 1; j < i; j++)
          {
             t = HH(j - 1, i - 1);
@@ -1141,7 +1149,6 @@ int or_fgmres(const or_csr *A, or_hierarchy *H, const double *b, double *x,
          if (resnorms) { resnorms[iter] = r_norm; }
          if (r_norm <= epsilon) { break; }
       }
-      /* solve the upper-triangular system and update x with the Z basis */
       rs[i - 1] = rs[i - 1] / HH(i - 1, i - 1);
       for (int k = i - 2; k >= 0; k--)
       {
@@ -1150,24 +1157,35 @@ int or_fgmres(const or_csr *A, or_hierarchy *H, const double *b, double *x,
          t += rs[k];
          rs[k] = t / HH(k, k);
       }
-      for (int j = 0; j < i; j++) { for (int k = 0; k < n; k++) { x[k] += rs[j] * Z[j][k]; } }
+      for (int k = 0; k < n; k++) { w[k] = pre[i - 1][k] * rs[i - 1]; }
+      for (int j = i - 2; j >= 0; j--) { for (int k = 0; k < n; k++) { w[k] += rs[j] * pre[j][k]; } }
+      for (int k = 0; k < n; k++) { x[k] += w[k]; }
       if (r_norm <= epsilon)
       {
-         /* true residual check */
-         or_matvec(-1.0, A, x, 1.0, b, V[0]);
-         r_norm = sqrt(or_dot(n, V[0], V[0]));
+         or_matvec(-1.0, A, x, 1.0, b, r);
+         r_norm = sqrt(or_dot(n, r, r));
          if (r_norm <= epsilon) { conv = 1; break; }
+         memcpy(p[0], r, sizeof(double) * n);
+         i = 0;
       }
-      else
+      for (int j = i; j > 0; j--)
       {
-         or_matvec(-1.0, A, x, 1.0, b, V[0]);
-         r_norm = sqrt(or_dot(n, V[0], V[0]));
+         rs[j - 1] = -s[j - 1] * rs[j];
+         rs[j] = c[j - 1] * rs[j];
+      }
+      if (i) { double a1 = rs[i] - 1.0; for (int k = 0; k < n; k++) { p[i][k] += a1 * p[i][k]; } }
+      for (int j = i - 1; j > 0; j--) { for (int k = 0; k < n; k++) { p[i][k] += rs[j] * p[j][k]; } }
+      if (i)
+      {
+         double a0 = rs[0] - 1.0;
+         for (int k = 0; k < n; k++) { p[0][k] += a0 * p[0][k]; }
+         for (int k = 0; k < n; k++) { p[0][k] += p[i][k]; }
       }
    }
 #undef HH
    *iters = iter;
-   for (int k = 0; k <= kdim; k++) { free(V[k]); free(Z[k]); }
-   free(V); free(Z); free(hh); free(c); free(s); free(rs);
+   for (int k = 0; k <= kdim; k++) { free(p[k]); free(pre[k]); }
+   free(p); free(pre); free(r); free(w); free(hh); free(c); free(s); free(rs);
    return conv ? 0 : 256;
 }
 
