@@ -1,0 +1,339 @@
+"""Benchmark: AMG-preconditioned Krylov setup+solve to relative residual 1e-8
+on the 3-D 27-point Laplacian, 160^3 grid (4,096,000 unknowns, 109,215,352
+nonzeros), on one GB300 through libHYPRE_gb300's C ABI.
+
+One step = BoomerAMG setup + Krylov solve from x0 = 0 on a matrix and
+right-hand side already resident in HBM (`value`, seconds, lower is better).
+`e2e` repeats the step through the public IJ interface from host buffers:
+IJ assembly of the matrix and right-hand side from pinned host memory, setup,
+solve and the read-back of x, all inside the timed region.
+
+Arms:
+  default            GPU path (FP64 setup, FP32 V-cycle inside FP64 PCG); the
+                     plain FP64 GPU path is timed alongside (`fp64_plain`)
+  --impl reference   the reference algorithm on the host cores (the CPU
+                     oracle restatement, all threads), on a bounded sample
+
+Inputs are larger than L2 (the level-0 matrix alone is 1.3 GB), so no L2
+flush is done between steps.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="laplace27_160", grid=[160, 160, 160], stencil="27-point (26, -1), Dirichlet",
+                unknowns=4096000, nnz=109215352, rhs="uniform[-1,1] Park-Miller seed 22775, unit 2-norm",
+                tol=1e-8, krylov="PCG", coarsening="PMIS theta 0.5", interp="extended+i Pmax 4",
+                smoother="l1-Jacobi V(1,1)", coarse="dense LU <= 9 rows", l2="inputs larger than L2, no flush")
+METRIC = "AMG-PCG setup+solve s to rel-res 1e-8"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=160)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-n", type=int, default=80)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, world
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    def __init__(self):
+        self.samples = []
+        self.stop = threading.Event()
+        self.t = None
+
+    def _run(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-i", "0"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 4 + k and s[4 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def gpu_arm(args):
+    import torch
+    import hypre_gb300 as gb
+    from hypre_gb300 import problems as G
+
+    rank, world = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.Stream(device=dev)
+    L = gb.lib()
+    L.HYPRE_GB300_SetStream(C.c_void_p(stream.cuda_stream))
+    L.HYPRE_Initialize()
+
+    n1 = args.n
+    I, J, V = G.laplace(27, n1, n1, n1)
+    n = len(I) - 1
+    nnz = len(J)
+    b = G.rhs(n)
+    # pinned host copies for the end-to-end arm
+    hI = torch.from_numpy(I).pin_memory()
+    hJ = torch.from_numpy(J).pin_memory()
+    hV = torch.from_numpy(V).pin_memory()
+    hb = torch.from_numpy(b).pin_memory()
+    hx = torch.zeros(n, dtype=torch.float64).pin_memory()
+
+    # resident inputs
+    A = C.c_void_p()
+    gb.check(L.HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(n, I.ctypes.data, J.ctypes.data, V.ctypes.data,
+                                                         C.byref(A)), "matrix")
+    bv = C.c_void_p(); xv = C.c_void_p()
+    L.HYPRE_ParVectorCreate(0, n, None, C.byref(bv)); L.HYPRE_ParVectorInitialize(bv)
+    L.HYPRE_ParVectorCreate(0, n, None, C.byref(xv)); L.HYPRE_ParVectorInitialize(xv)
+    L.HYPRE_GB300_ParVectorCopyFromHost(bv, b.ctypes.data, n)
+
+    def make_solver(prec):
+        amg = C.c_void_p()
+        L.HYPRE_BoomerAMGCreate(C.byref(amg))
+        L.HYPRE_BoomerAMGSetStrongThreshold(amg, 0.5)
+        L.HYPRE_BoomerAMGSetMaxRowSum(amg, 1.0)
+        L.HYPRE_BoomerAMGSetPMaxElmts(amg, 4)
+        L.HYPRE_BoomerAMGSetRelaxType(amg, 18)
+        L.HYPRE_BoomerAMGSetTol(amg, 0.0)
+        L.HYPRE_BoomerAMGSetMaxIter(amg, 1)
+        L.HYPRE_GB300_BoomerAMGSetCyclePrecision(amg, prec)
+        pcg = C.c_void_p()
+        L.HYPRE_ParCSRPCGCreate(0, C.byref(pcg))
+        L.HYPRE_PCGSetTol(pcg, 1e-8)
+        L.HYPRE_PCGSetMaxIter(pcg, 200)
+        L.HYPRE_PCGSetTwoNorm(pcg, 1)
+        L.HYPRE_PCGSetPrecond(pcg, gb.fn_ptr("HYPRE_BoomerAMGSolve"), gb.fn_ptr("HYPRE_BoomerAMGSetup"), amg)
+        return amg, pcg
+
+    def step(pcg, amg):
+        L.HYPRE_ParVectorSetConstantValues(xv, 0.0)
+        gb.check(L.HYPRE_ParCSRPCGSetup(pcg, A, bv, xv), "setup")
+        gb.check(L.HYPRE_ParCSRPCGSolve(pcg, A, bv, xv), "solve")
+
+    def timed(fn, k, w):
+        for _ in range(w):
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        return e0.elapsed_time(e1) / 1e3 / k, wall / k
+
+    def true_relres():
+        x = np.empty(n)
+        L.HYPRE_GB300_ParVectorCopyToHost(xv, x.ctypes.data, n)
+        import scipy.sparse as sp
+        M = sp.csr_matrix((V, J, I), shape=(n, n))
+        r = b - M @ x
+        return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+    out = {}
+    res = {}
+    for label, prec in (("fp64_plain", 0), ("fp32_cycle", 1)):
+        amg, pcg = make_solver(prec)
+        L.HYPRE_GB300_ResetKernelLaunchCount()
+        with ClockSampler() as cs:
+            dev_s, wall_s = timed(lambda: step(pcg, amg), args.steps, args.warmup)
+        launches = gb.kernel_launches() // max(1, args.steps + args.warmup)
+        it = C.c_int(); L.HYPRE_PCGGetNumIterations(pcg, C.byref(it))
+        t = np.zeros(6); L.HYPRE_GB300_BoomerAMGGetSetupTimes(amg, t.ctypes.data, 6)
+        nl = C.c_int(); L.HYPRE_BoomerAMGGetNumLevels(amg, C.byref(nl))
+        res[label] = dict(seconds=dev_s, wall_seconds=wall_s, iterations=it.value, levels=nl.value,
+                          setup_seconds=float(t[5]), setup_phase_seconds=[float(v) for v in t[:5]],
+                          true_relres=true_relres(), launches_per_step=launches, clocks=cs.summary())
+        if label == "fp32_cycle":
+            keep = (amg, pcg)
+        else:
+            L.HYPRE_ParCSRPCGDestroy(pcg); L.HYPRE_BoomerAMGDestroy(amg)
+
+    # ---- SpMV roofline on level 0 (FP64, CSR/SELL kernel), CUDA events on the library stream
+    reps = 20
+    yv = C.c_void_p(); L.HYPRE_ParVectorCreate(0, n, None, C.byref(yv)); L.HYPRE_ParVectorInitialize(yv)
+    for _ in range(3):
+        L.HYPRE_ParCSRMatrixMatvec(1.0, A, bv, 0.0, yv)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        L.HYPRE_ParCSRMatrixMatvec(1.0, A, bv, 0.0, yv)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    spmv_s = e0.elapsed_time(e1) / 1e3 / reps
+    spmv_bytes = nnz * 12 + (n + 1) * 4 + 8 * n + 8 * n
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = spmv_bytes / spmv_s / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get("bytes_per_launch")
+
+    # ---- end to end through the IJ interface from pinned host buffers
+    amg, pcg = keep
+    ncols = np.diff(I).astype(np.int32)
+    rows = np.arange(n, dtype=np.int32)
+
+    def e2e_step():
+        ijA = C.c_void_p()
+        L.HYPRE_IJMatrixCreate(0, 0, n - 1, 0, n - 1, C.byref(ijA))
+        L.HYPRE_IJMatrixSetObjectType(ijA, gb.HYPRE_PARCSR)
+        L.HYPRE_IJMatrixSetRowSizes(ijA, ncols.ctypes.data)
+        L.HYPRE_IJMatrixInitialize(ijA)
+        L.HYPRE_IJMatrixSetValues(ijA, n, ncols.ctypes.data, rows.ctypes.data, hJ.data_ptr(), hV.data_ptr())
+        L.HYPRE_IJMatrixAssemble(ijA)
+        pA = C.c_void_p(); L.HYPRE_IJMatrixGetObject(ijA, C.byref(pA))
+        ijb = C.c_void_p(); ijx = C.c_void_p()
+        L.HYPRE_IJVectorCreate(0, 0, n - 1, C.byref(ijb)); L.HYPRE_IJVectorSetObjectType(ijb, gb.HYPRE_PARCSR)
+        L.HYPRE_IJVectorInitialize(ijb); L.HYPRE_IJVectorSetValues(ijb, n, None, hb.data_ptr())
+        L.HYPRE_IJVectorAssemble(ijb)
+        L.HYPRE_IJVectorCreate(0, 0, n - 1, C.byref(ijx)); L.HYPRE_IJVectorSetObjectType(ijx, gb.HYPRE_PARCSR)
+        L.HYPRE_IJVectorInitialize(ijx); L.HYPRE_IJVectorAssemble(ijx)
+        pb = C.c_void_p(); px = C.c_void_p()
+        L.HYPRE_IJVectorGetObject(ijb, C.byref(pb)); L.HYPRE_IJVectorGetObject(ijx, C.byref(px))
+        gb.check(L.HYPRE_ParCSRPCGSetup(pcg, pA, pb, px), "e2e setup")
+        gb.check(L.HYPRE_ParCSRPCGSolve(pcg, pA, pb, px), "e2e solve")
+        L.HYPRE_IJVectorGetValues(ijx, n, None, hx.data_ptr())
+        L.HYPRE_IJVectorDestroy(ijx); L.HYPRE_IJVectorDestroy(ijb); L.HYPRE_IJMatrixDestroy(ijA)
+
+    e2e_dev, e2e_wall = timed(e2e_step, max(1, args.steps), 1)
+    h2d = nnz * (4 + 8) + (n + 1) * 4 + 8 * n
+    d2h = 8 * n
+
+    # ---- CPU baseline: the reference algorithm (oracle restatement) on the host cores
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.cpu_sample_n, n1)
+
+    best = res["fp32_cycle"]
+    result = {
+        "metric": METRIC, "value": best["seconds"], "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": best["seconds"] * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 setup+Krylov / f32 V-cycle",
+        "data": "synthetic (seeded generator)", "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "1 GPU"),
+        "fp64_plain": res["fp64_plain"], "fp32_cycle": best,
+        "speedup_fp32_vs_fp64_plain": res["fp64_plain"]["seconds"] / best["seconds"],
+        "e2e": {"value": e2e_wall, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "device_event_seconds": e2e_dev},
+        "gpu_launches": best["launches_per_step"],
+        "roofline": {"bound": "hbm", "kernel": "SpMV level 0 (FP64 values, int32 indices)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algorithmic_bytes": spmv_bytes, "launch_seconds": spmv_s,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "cpu_baseline": cpu,
+        "clocks": best["clocks"],
+    }
+    if rank == 0:
+        print(json.dumps(result))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(sample_n, full_n, threads=None):
+    """Times the CPU restatement of the reference algorithm (oracle) with all
+    host threads on a smaller grid of the same workload and scales the time
+    by the unknown count (the method's cost is linear in the unknowns)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from hypre_gb300 import problems as G
+    threads = threads or os.cpu_count()
+    O.set_threads(threads)
+    I, J, V = G.laplace(27, sample_n, sample_n, sample_n)
+    b = G.rhs(len(I) - 1)
+    t0 = time.perf_counter()
+    H = O.Hierarchy(I, J, V, O.default_params(max_row_sum=1.0, strong_threshold=0.5))
+    t1 = time.perf_counter()
+    x, rel, it = H.pcg(b, tol=1e-8, maxit=200)
+    t2 = time.perf_counter()
+    scale = (full_n ** 3) / (sample_n ** 3)
+    return {"value": (t2 - t0) * scale, "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"27-point {sample_n}^3 (same solver settings), setup {t1 - t0:.2f} s + solve {t2 - t1:.2f} s "
+                      f"({it} its), scaled by unknowns x{scale:.1f} to {full_n}^3"}
+
+
+def reference_arm(args):
+    rank, world = dist_info()
+    if rank != 0:
+        return
+    times = []
+    info = None
+    for _ in range(args.warmup):
+        cpu_baseline(args.cpu_sample_n, args.n)
+    for _ in range(args.steps):
+        info = cpu_baseline(args.cpu_sample_n, args.n)
+        times.append(info["value"])
+    v = float(np.mean(times))
+    info["value"] = v
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+                      "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic (seeded generator)", "config": WORKLOAD, "cpu_baseline": info,
+                      "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        gpu_arm(a)

@@ -55,6 +55,8 @@ def _declare(L):
         "HYPRE_IJVectorAddToValues": [vp, i32, vp, vp], "HYPRE_IJVectorAssemble": [vp],
         "HYPRE_IJVectorGetObject": [vp, P(vp)], "HYPRE_IJVectorGetValues": [vp, i32, vp, vp],
         "HYPRE_IJVectorDestroy": [vp],
+        "HYPRE_ParVectorCreate": [i32, i32, vp, P(vp)], "HYPRE_ParVectorInitialize": [vp],
+        "HYPRE_ParVectorDestroy": [vp],
         "HYPRE_ParVectorInnerProd": [vp, vp, P(f64)], "HYPRE_ParVectorSetConstantValues": [vp, f64],
         "HYPRE_ParVectorCopy": [vp, vp], "HYPRE_ParVectorScale": [f64, vp], "HYPRE_ParVectorAxpy": [f64, vp, vp],
         "HYPRE_ParVectorSetRandomValues": [vp, i32],

@@ -518,6 +518,29 @@ static HYPRE_Int ijm_put(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, co
          if (!row_grow(m, r, nc)) { return gb_error_flag; }
          int *rc = m->cols + m->row_off[r];
          double *rv = m->vals + m->row_off[r];
+         /* common case: columns in range and ascending after the first entry,
+          * the first not repeated later -> no duplicates, copy straight */
+         int fast = 1;
+         for (int q = 0; q < nc && fast; q++)
+         {
+            int c = cols[k + q] - m->jlower;
+            if (c < 0 || c > m->jupper - m->jlower) { fast = 0; }
+            if (q >= 2 && cols[k + q] <= cols[k + q - 1]) { fast = 0; }
+         }
+         if (fast && nc > 2)
+         {
+            int c0 = cols[k];
+            int lo = 1, hi = nc - 1;
+            while (lo <= hi) { int mid = (lo + hi) / 2; if (cols[k + mid] == c0) { fast = 0; break; } if (cols[k + mid] < c0) { lo = mid + 1; } else { hi = mid - 1; } }
+         }
+         if (fast && nc == 2 && cols[k] == cols[k + 1]) { fast = 0; }
+         if (fast)
+         {
+            for (int q = 0; q < nc; q++) { rc[q] = cols[k + q] - m->jlower; rv[q] = values[k + q]; }
+            m->row_len[r] = nc;
+            k += nc;
+            continue;
+         }
          int l = 0;
          for (int q = 0; q < nc; q++, k++)
          {
