@@ -10,6 +10,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#ifdef __cplusplus
+extern "C" {
+#endif
+
 /* --- error flag (reference: src/utilities/error.c:13-91) ------------------ */
 extern HYPRE_Int gb_error_flag;
 extern HYPRE_Int gb_error_arg;
@@ -173,4 +177,7 @@ typedef struct
    int                  nV;
 } gb_krylov;
 
+#ifdef __cplusplus
+}
+#endif
 #endif

@@ -291,6 +291,17 @@ HYPRE_Int HYPRE_GB300_GetStream(void **cuda_stream);
  * (graph replays count every kernel node). */
 HYPRE_Int HYPRE_GB300_GetKernelLaunchCount(long long *count);
 HYPRE_Int HYPRE_GB300_ResetKernelLaunchCount(void);
+/* y = alpha * A^T x + beta * y without allocating device memory: the transpose
+ * of A is built in a fixed device array of 32 MiB compiled into the library,
+ * for callers that cannot allocate (code running under CUDA-graph stream
+ * capture, or hosts whose device memory is owned by another allocator).
+ * Matrices whose transpose does not fit are rejected with HYPRE_ERROR_ARG.
+ * All calls share the array, so calls that overlap on the GPU race; the first
+ * call on a device looks the array up and should come before any capture.
+ * No counterpart in the reference (its MatvecT, HYPRE_ParCSRMatrixMatvecT
+ * above, is the allocating form). */
+HYPRE_Int HYPRE_GB300_ParCSRMatrixMatvecTNoAlloc(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,
+                                                HYPRE_Complex beta, HYPRE_ParVector y);
 /* Per-phase timings of the last setup (seconds, CUDA events):
  * [0] strength [1] coarsening [2] interpolation [3] RAP [4] smoother setup [5] total */
 HYPRE_Int HYPRE_GB300_BoomerAMGGetSetupTimes(HYPRE_Solver solver, HYPRE_Real *times, HYPRE_Int n);
