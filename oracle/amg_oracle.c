@@ -681,13 +681,18 @@ int or_rap(const or_csr *P, const or_csr *A, or_csr *Ac)
  * SpGEMM, the order hypre_ParMatmul's diag part produces) */
 int or_matmul(const or_csr *A, const or_csr *B, or_csr *C)
 {
+   /* hypre_ParMatmul, src/parcsr_mv/par_csr_matop.c:348 (one process): row-wise
+    * marker product, columns in discovery order, first contribution stored,
+    * later ones added; a square product places its diagonal first (:688-697). */
    int n = A->nr, m = B->nc;
+   int square = (n == m);
    int *Ci = xcalloc(n + 1, sizeof(int));
    int *mk = xmalloc(sizeof(int) * (m ? m : 1));
    for (int k = 0; k < m; k++) { mk[k] = -1; }
    for (int i = 0; i < n; i++)
    {
       int cnt = 0;
+      if (square) { mk[i] = i; cnt++; }
       for (int ka = A->i[i]; ka < A->i[i + 1]; ka++)
       {
          int r = A->j[ka];
@@ -702,6 +707,7 @@ int or_matmul(const or_csr *A, const or_csr *B, or_csr *C)
    for (int i = 0; i < n; i++)
    {
       int begin = Ci[i], c = begin;
+      if (square) { mk[i] = c; Cj[c] = i; Cv[c] = 0.0; c++; }
       for (int ka = A->i[i]; ka < A->i[i + 1]; ka++)
       {
          int r = A->j[ka];
@@ -716,6 +722,305 @@ int or_matmul(const or_csr *A, const or_csr *B, or_csr *C)
    }
    C->nr = n; C->nc = m; C->i = Ci; C->j = Cj; C->v = Cv;
    free(mk);
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Aggressive coarsening (agg_num_levels > 0, agg_interp_type 6)             */
+/* ------------------------------------------------------------------------ */
+
+/* Second-order strength between C points, hypre_BoomerAMGCreate2ndSHost
+ * src/parcsr_ls/par_strength.c:1795-3030 (num_paths = 1): row ic (the ic-th C
+ * point i1) holds, in discovery order, the coarse index of every C neighbour
+ * i2 of i1 in S and of every C point i3 != i1 in S_i2 for each neighbour i2.
+ * C points with an empty row are marked CF = 2 (:2701-2723). */
+int or_strength2(const or_csr *S, int *CF, int num_paths, or_csr *S2)
+{
+   (void) num_paths;
+   int n = S->nr;
+   int *f2c = xmalloc(sizeof(int) * (n ? n : 1));
+   int nc = 0;
+   for (int i = 0; i < n; i++) { f2c[i] = CF[i] > 0 ? nc++ : -1; }
+   int *c2f = xmalloc(sizeof(int) * (nc ? nc : 1));
+   for (int i = 0; i < n; i++) { if (CF[i] > 0) { c2f[f2c[i]] = i; } }
+   int *mark = xmalloc(sizeof(int) * (nc ? nc : 1));
+   for (int k = 0; k < nc; k++) { mark[k] = -1; }
+   int *Ci = xcalloc(nc + 1, sizeof(int));
+   /* pass 1: counts */
+   for (int ic = 0; ic < nc; ic++)
+   {
+      int i1 = c2f[ic], cnt = 0;
+      for (int k1 = S->i[i1]; k1 < S->i[i1 + 1]; k1++)
+      {
+         int i2 = S->j[k1];
+         if (CF[i2] > 0) { int idx = f2c[i2]; if (mark[idx] != ic) { mark[idx] = ic; cnt++; } }
+         for (int k2 = S->i[i2]; k2 < S->i[i2 + 1]; k2++)
+         {
+            int i3 = S->j[k2];
+            if (CF[i3] > 0) { int idx = f2c[i3]; if (idx != ic && mark[idx] != ic) { mark[idx] = ic; cnt++; } }
+         }
+      }
+      Ci[ic + 1] = cnt;
+   }
+   for (int ic = 0; ic < nc; ic++)
+   {
+      if (Ci[ic + 1] == 0) { CF[c2f[ic]] = 2; }
+      Ci[ic + 1] += Ci[ic];
+   }
+   int *Cj = xmalloc(sizeof(int) * (Ci[nc] ? Ci[nc] : 1));
+   for (int k = 0; k < nc; k++) { mark[k] = -1; }
+   for (int ic = 0; ic < nc; ic++)
+   {
+      int i1 = c2f[ic], c = Ci[ic];
+      for (int k1 = S->i[i1]; k1 < S->i[i1 + 1]; k1++)
+      {
+         int i2 = S->j[k1];
+         if (CF[i2] > 0) { int idx = f2c[i2]; if (mark[idx] < Ci[ic]) { mark[idx] = c; Cj[c++] = idx; } }
+         for (int k2 = S->i[i2]; k2 < S->i[i2 + 1]; k2++)
+         {
+            int i3 = S->j[k2];
+            if (CF[i3] > 0) { int idx = f2c[i3]; if (idx != ic && mark[idx] < Ci[ic]) { mark[idx] = c; Cj[c++] = idx; } }
+         }
+      }
+   }
+   S2->nr = S2->nc = nc; S2->i = Ci; S2->j = Cj; S2->v = NULL;
+   free(f2c); free(c2f); free(mark);
+   return 0;
+}
+
+/* hypre_BoomerAMGCorrectCFMarker2Host src/parcsr_ls/par_strength.c:3096:
+ * C points that the second coarsening made F become -2, the others 1. */
+void or_correct_cf2(int n, int *CF, const int *CFN)
+{
+   int cnt = 0;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] > 0) { CF[i] = CFN[cnt] == -1 ? -2 : 1; cnt++; }
+   }
+}
+
+/* Modified extended+i interpolation, hypre_BoomerAMGBuildModExtPIInterpHost
+ * src/parcsr_ls/par_mod_lr_interp.c:585-1215 with the F/C blocks of
+ * hypre_ParCSRMatrixGenerateFFFCHost src/parcsr_mv/gen_fffc.c:18-530:
+ * As_FF / As_FC are A restricted to strong connections (FF with the diagonal
+ * first), W = As_FF As_FC after the D_q, D_w, D_theta scaling, P = [I; W]. */
+int or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P)
+{
+   int n = A->nr;
+   int *f2c = xmalloc(sizeof(int) * (n ? n : 1)), *f2f = xmalloc(sizeof(int) * (n ? n : 1));
+   int nc = 0, nf = 0;
+   for (int i = 0; i < n; i++) { if (CF[i] > 0) { f2c[i] = nc++; f2f[i] = -1; } else { f2f[i] = nf++; f2c[i] = -1; } }
+   /* As_FF, As_FC */
+   int *FFi = xcalloc(nf + 1, sizeof(int)), *FCi = xcalloc(nf + 1, sizeof(int));
+   int row = 0;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] >= 0 && CF[i] > 0) { continue; }
+      if (CF[i] > 0) { continue; }
+      int ff = 0, fc = 0;
+      if (A->i[i] < A->i[i + 1] && A->j[A->i[i]] == i) { ff++; }
+      for (int k = S->i[i]; k < S->i[i + 1]; k++) { if (CF[S->j[k]] > 0) { fc++; } else { ff++; } }
+      FFi[row + 1] = FFi[row] + ff; FCi[row + 1] = FCi[row] + fc; row++;
+   }
+   int *FFj = xmalloc(sizeof(int) * (FFi[nf] ? FFi[nf] : 1)), *FCj = xmalloc(sizeof(int) * (FCi[nf] ? FCi[nf] : 1));
+   double *FFv = xmalloc(sizeof(double) * (FFi[nf] ? FFi[nf] : 1)), *FCv = xmalloc(sizeof(double) * (FCi[nf] ? FCi[nf] : 1));
+   row = 0;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] > 0) { continue; }
+      int pf = FFi[row], pc = FCi[row];
+      int jA = A->i[i];
+      if (jA < A->i[i + 1] && A->j[jA] == i) { FFj[pf] = f2f[i]; FFv[pf++] = A->v[jA]; }
+      for (int k = S->i[i]; k < S->i[i + 1]; k++)
+      {
+         jA = A->i[i];
+         if (jA < A->i[i + 1] && A->j[jA] == i) { jA++; }
+         int jS = S->j[k];
+         while (A->j[jA] != jS) { jA++; }
+         if (CF[jS] > 0) { FCj[pc] = f2c[jS]; FCv[pc++] = A->v[jA]; }
+         else { FFj[pf] = f2f[jS]; FFv[pf++] = A->v[jA]; }
+      }
+      row++;
+   }
+   double *Dq = xcalloc(nf, sizeof(double)), *Dw = xcalloc(nf, sizeof(double)), *Dt = xcalloc(nf, sizeof(double));
+   double *tmp = xmalloc(sizeof(double) * (FFi[nf] ? FFi[nf] : 1));
+   for (int r = 0; r < nf; r++) { for (int k = FCi[r]; k < FCi[r + 1]; k++) { Dq[r] += FCv[k]; } }
+   memcpy(tmp, FFv, sizeof(double) * FFi[nf]);
+   row = 0;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] >= 0) { if (CF[i] > 0) { continue; } }
+      if (CF[i] > 0) { continue; }
+      for (int k = A->i[i]; k < A->i[i + 1]; k++) { Dw[row] += A->v[k]; }
+      for (int k = FFi[row] + 1; k < FFi[row + 1]; k++) { Dw[row] -= FFv[k]; }
+      Dw[row] -= Dq[row];
+      row++;
+   }
+   for (int r = 0; r < nf; r++)
+   {
+      for (int j = FFi[r] + 1; j < FFi[r + 1]; j++)
+      {
+         int jj = FFj[j];
+         double value = Dq[jj];
+         for (int k = FFi[jj] + 1; k < FFi[jj + 1]; k++)
+         {
+            if (FFj[k] == r)
+            {
+               double value1 = tmp[k];
+               value += value1;
+               Dt[r] += FFv[j] * value1 / value;
+               break;
+            }
+         }
+         if (value != 0.0) { FFv[j] /= value; }
+      }
+      FFv[FFi[r]] = 1.0;
+   }
+   for (int r = 0; r < nf; r++)
+   {
+      double theta = Dt[r] + Dw[r];
+      if (theta != 0.0)
+      {
+         theta = -1.0 / theta;
+         for (int j = FFi[r]; j < FFi[r + 1]; j++) { FFv[j] *= theta; }
+      }
+   }
+   or_csr FF = { nf, nf, FFi, FFj, FFv }, FC = { nf, nc, FCi, FCj, FCv }, W;
+   or_matmul(&FF, &FC, &W);
+   /* P = [I; W] in fine order */
+   int *Pi = xcalloc(n + 1, sizeof(int));
+   row = 0;
+   for (int i = 0; i < n; i++)
+   {
+      int len = CF[i] > 0 ? 1 : W.i[row + 1] - W.i[row];
+      if (CF[i] <= 0) { row++; }
+      Pi[i + 1] = Pi[i] + len;
+   }
+   int *Pj = xmalloc(sizeof(int) * (Pi[n] ? Pi[n] : 1));
+   double *Pv = xmalloc(sizeof(double) * (Pi[n] ? Pi[n] : 1));
+   row = 0;
+   for (int i = 0; i < n; i++)
+   {
+      int c = Pi[i];
+      if (CF[i] > 0) { Pj[c] = f2c[i]; Pv[c] = 1.0; }
+      else
+      {
+         for (int k = W.i[row]; k < W.i[row + 1]; k++) { Pj[c] = W.j[k]; Pv[c] = W.v[k]; c++; }
+         row++;
+      }
+   }
+   P->nr = n; P->nc = nc; P->i = Pi; P->j = Pj; P->v = Pv;
+   or_csr_free(&FF); or_csr_free(&FC); or_csr_free(&W);
+   free(f2c); free(f2f); free(Dq); free(Dw); free(Dt); free(tmp);
+   return 0;
+}
+
+/* Partial extended+i interpolation, hypre_BoomerAMGBuildPartialExtPIInterp
+ * src/parcsr_ls/partial.c:16-720: extended+i weights (as
+ * or_extpi_interp) for the rows of the old C points only (CF == 1 identity,
+ * CF == -2 interpolated); rows numbered by old coarse index, columns by new.
+ * Afterwards CF values below -1 become -1 (:700). */
+int or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
+{
+   int n = A->nr;
+   int *f2c = xmalloc(sizeof(int) * (n ? n : 1));
+   int nco = 0, nc = 0;
+   for (int i = 0; i < n; i++) { f2c[i] = -1; if (CF[i] == 1) { f2c[i] = nc++; nco++; } else if (CF[i] == -2) { nco++; } }
+   int *oc2f = xmalloc(sizeof(int) * (nco ? nco : 1));
+   nco = 0;
+   for (int i = 0; i < n; i++) { if (CF[i] == 1 || CF[i] == -2) { oc2f[nco++] = i; } }
+   int *Pi = xcalloc(nco + 1, sizeof(int));
+   int *marker = xmalloc(sizeof(int) * (n ? n : 1));
+   for (int i = 0; i < n; i++) { marker[i] = -1; }
+   for (int ii = 0; ii < nco; ii++)
+   {
+      int i = oc2f[ii], cnt = 0;
+      if (CF[i] > 0) { cnt = 1; }
+      else if (CF[i] == -2)
+      {
+         for (int k = S->i[i]; k < S->i[i + 1]; k++)
+         {
+            int i1 = S->j[k];
+            if (CF[i1] > 0) { if (marker[i1] != i) { marker[i1] = i; cnt++; } }
+            else if (CF[i1] != SF_PT)
+            {
+               for (int kk = S->i[i1]; kk < S->i[i1 + 1]; kk++)
+               {
+                  int k1 = S->j[kk];
+                  if (CF[k1] > 0 && marker[k1] != i) { marker[k1] = i; cnt++; }
+               }
+            }
+         }
+      }
+      Pi[ii + 1] = Pi[ii] + cnt;
+   }
+   int nnz = Pi[nco];
+   int *Pj = xmalloc(sizeof(int) * (nnz ? nnz : 1));
+   double *Pv = xmalloc(sizeof(double) * (nnz ? nnz : 1));
+   int *pmark = xmalloc(sizeof(int) * (n ? n : 1));
+   for (int i = 0; i < n; i++) { pmark[i] = -1; }
+   int strong_f = -2;
+   for (int ii = 0; ii < nco; ii++)
+   {
+      int i = oc2f[ii];
+      int begin = Pi[ii], c = begin;
+      if (CF[i] > 0) { Pj[c] = f2c[i]; Pv[c] = 1.0; c++; }
+      else if (CF[i] == -2)
+      {
+         strong_f--;
+         for (int k = S->i[i]; k < S->i[i + 1]; k++)
+         {
+            int i1 = S->j[k];
+            if (CF[i1] >= 0)
+            {
+               if (pmark[i1] < begin) { pmark[i1] = c; Pj[c] = f2c[i1]; Pv[c] = 0.0; c++; }
+            }
+            else if (CF[i1] != SF_PT)
+            {
+               pmark[i1] = strong_f;
+               for (int kk = S->i[i1]; kk < S->i[i1 + 1]; kk++)
+               {
+                  int k1 = S->j[kk];
+                  if (CF[k1] >= 0 && pmark[k1] < begin) { pmark[k1] = c; Pj[c] = f2c[k1]; Pv[c] = 0.0; c++; }
+               }
+            }
+         }
+         int end = c;
+         double diagonal = A->v[A->i[i]];
+         for (int jj = A->i[i] + 1; jj < A->i[i + 1]; jj++)
+         {
+            int i1 = A->j[jj];
+            if (pmark[i1] >= begin) { Pv[pmark[i1]] += A->v[jj]; }
+            else if (pmark[i1] == strong_f)
+            {
+               double sum = 0.0;
+               int sgn = A->v[A->i[i1]] < 0 ? -1 : 1;
+               for (int jj1 = A->i[i1] + 1; jj1 < A->i[i1 + 1]; jj1++)
+               {
+                  int i2 = A->j[jj1];
+                  if ((pmark[i2] >= begin || i2 == i) && (sgn * A->v[jj1]) < 0) { sum += A->v[jj1]; }
+               }
+               if (sum != 0)
+               {
+                  double distribute = A->v[jj] / sum;
+                  for (int jj1 = A->i[i1] + 1; jj1 < A->i[i1 + 1]; jj1++)
+                  {
+                     int i2 = A->j[jj1];
+                     if (pmark[i2] >= begin && (sgn * A->v[jj1]) < 0) { Pv[pmark[i2]] += distribute * A->v[jj1]; }
+                     if (i2 == i && (sgn * A->v[jj1]) < 0) { diagonal += distribute * A->v[jj1]; }
+                  }
+               }
+               else { diagonal += A->v[jj]; }
+            }
+            else if (CF[i1] != SF_PT) { diagonal += A->v[jj]; }
+         }
+         if (diagonal != 0.0) { for (int k = begin; k < end; k++) { Pv[k] /= -diagonal; } }
+      }
+      strong_f--;
+   }
+   for (int i = 0; i < n; i++) { if (CF[i] < -1) { CF[i] = -1; } }
+   P->nr = nco; P->nc = nc; P->i = Pi; P->j = Pj; P->v = Pv;
+   free(f2c); free(oc2f); free(marker); free(pmark);
    return 0;
 }
 
@@ -907,15 +1212,37 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
       or_strength(A, prm->strong_threshold, prm->max_row_sum, &S);
       int *CF = xmalloc(sizeof(int) * (n ? n : 1));
       or_pmis(&S, 0, CF);
-      int nc = or_coarse_count(n, CF);
-      if (nc == 0 || nc == n || nc < prm->min_coarse_size)
-      {
-         or_csr_free(&S); free(CF);
-         break;
-      }
       or_csr P;
-      or_extpi_interp(A, &S, CF, &P);
-      or_truncate(&P, prm->trunc_factor, prm->p_max_elmts);
+      int nc;
+      if (level < prm->agg_num_levels)
+      {
+         /* par_amg_setup.c:1311-1358 and :1778-1915 (agg_interp_type 6) */
+         or_csr S2;
+         or_strength2(&S, CF, prm->num_paths, &S2);
+         int *CFN = xmalloc(sizeof(int) * (S2.nr ? S2.nr : 1));
+         or_pmis(&S2, 3, CFN);
+         or_csr P1, P2;
+         or_mod_extpi_interp(A, &S, CF, &P1);
+         or_truncate(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
+         or_correct_cf2(n, CF, CFN);
+         or_partial_extpi_interp(A, &S, CF, &P2);
+         or_truncate(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
+         or_matmul(&P1, &P2, &P);
+         or_truncate(&P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
+         nc = P.nc;
+         or_csr_free(&S2); or_csr_free(&P1); or_csr_free(&P2); free(CFN);
+      }
+      else
+      {
+         nc = or_coarse_count(n, CF);
+         if (nc == 0 || nc == n || nc < prm->min_coarse_size)
+         {
+            or_csr_free(&S); free(CF);
+            break;
+         }
+         or_extpi_interp(A, &S, CF, &P);
+         or_truncate(&P, prm->trunc_factor, prm->p_max_elmts);
+      }
       or_csr Ac;
       or_rap(&P, A, &Ac);
       H->S[level] = S;

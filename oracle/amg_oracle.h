@@ -91,10 +91,10 @@ int    or_transpose(const or_csr *A, or_csr *AT);
 int    or_rap(const or_csr *P, const or_csr *A, or_csr *Ac);
 int    or_l1_norms(const or_csr *A, int option, double *l1);
 int    or_matmul(const or_csr *A, const or_csr *B, or_csr *C);
-int    or_strength2(const or_csr *S, const int *CF, int num_paths, or_csr *S2);
+int    or_strength2(const or_csr *S, int *CF, int num_paths, or_csr *S2);
+void   or_correct_cf2(int n, int *CF, const int *CFN);
 int    or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P);
-int    or_partial_extpi_interp(const or_csr *A, const or_csr *S, const int *CF,
-                               const int *CF_coarse_of_fine, or_csr *P);
+int    or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
 
 /* hierarchy */
 int    or_amg_setup(const or_csr *A, const or_amg_params *prm, or_hierarchy *H);
