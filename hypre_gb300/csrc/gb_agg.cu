@@ -1,0 +1,374 @@
+// Aggressive-coarsening kernels for sm_103a (agg_interp_type 6): second-order
+// strength between C points, C/F marker corrections, the F/C blocks of A and
+// the scalings of the modified extended+i interpolation, and the assembly of
+// P1 = [I; W].  Results are identical to the reference's serial loops
+// (compiled with --fmad=false like the other setup kernels).
+#include "gb_device.cuh"
+#include "gb_kernels.h"
+
+#define C_PT 1
+#define F_PT -1
+#define SF_PT -3
+
+static int gb_blocks2(long long n, int t) { long long b = (n + t - 1) / t; return (int) (b < 1 ? 1 : b); }
+
+__global__ void k_flag_pos(int n, const int *__restrict__ CF, int *__restrict__ flag)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { flag[i] = CF[i] > 0; }
+}
+__global__ void k_flag_eq(int n, const int *__restrict__ CF, int v, int *__restrict__ flag)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { flag[i] = CF[i] == v; }
+}
+__global__ void k_flag_nonpos(int n, const int *__restrict__ CF, int *__restrict__ flag)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { flag[i] = CF[i] <= 0; }
+}
+// inverse of a scanned flag: list[scan[i]] = i where flag[i]
+__global__ void k_scatter_list(int n, const int *__restrict__ flag, const int *__restrict__ scan, int *__restrict__ list)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n && flag[i]) { list[scan[i]] = i; }
+}
+
+extern "C" void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s)
+{
+   // kind 0: CF > 0 ; 1: CF == v ; 2: CF <= 0
+   if (kind == 0) { k_flag_pos<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, flag); }
+   else if (kind == 1) { k_flag_eq<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, v, flag); }
+   else { k_flag_nonpos<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, flag); }
+   GB_COUNT(1);
+}
+
+extern "C" void gb_scatter_list(int n, const int *flag, const int *scan, int *list, cudaStream_t s)
+{
+   k_scatter_list<<<gb_blocks2(n, 256), 256, 0, s>>>(n, flag, scan, list);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Second-order strength (reference: hypre_BoomerAMGCreate2ndSHost
+// src/parcsr_ls/par_strength.c:1795-3030, num_paths = 1).  Row ic is the
+// ic-th C point i1; its columns are, in discovery order, the coarse indices of
+// C neighbours i2 of i1 in S and of C points i3 != i1 in S_i2 for every
+// neighbour i2.  Shared-memory tables, global tables for overflowing rows.
+// ---------------------------------------------------------------------------
+template <bool GLOBAL, bool FILL>
+__global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f, const int *__restrict__ f2c,
+                                            const int *__restrict__ Si, const int *__restrict__ Sj,
+                                            const int *__restrict__ CF, int *__restrict__ cnt,
+                                            const int *__restrict__ S2i, int *__restrict__ S2j, int *ovf_list,
+                                            int *ovf_n, int *gtab, int gcap, int *err)
+{
+   extern __shared__ int sh[];
+   const int lane = gb_lane();
+   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   int nwarps = (gridDim.x * blockDim.x) >> 5;
+   GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
+                    : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
+   if (!GLOBAL) { gb_tab_init(T); }
+   int total = GLOBAL ? *ovf_n : nc;
+   for (int t = warp; t < total; t += nwarps)
+   {
+      int ic = GLOBAL ? ovf_list[t] : t;
+      int off = 0;
+      if (FILL)
+      {
+         off = S2i[ic];
+         if (!GLOBAL && S2i[ic + 1] - off > T.listcap) { continue; }
+      }
+      int i1 = c2f[ic];
+      int count = 0, ovf = 0;
+      bool created;
+      for (int k1 = Si[i1]; k1 < Si[i1 + 1] && !ovf; k1++)
+      {
+         int i2 = Sj[k1];
+         if (CF[i2] > 0)
+         {
+            int idx = f2c[i2];
+            int pos = gb_winsert(T, count, idx, lane == 0, created, ovf);
+            if (FILL && created && pos >= 0) { S2j[off + pos] = idx; }
+            __syncwarp();
+         }
+         int b = Si[i2], e = Si[i2 + 1];
+         for (int base = b; base < e && !ovf; base += 32)
+         {
+            int k2 = base + lane;
+            bool act = false;
+            int idx = -1;
+            if (k2 < e)
+            {
+               int i3 = Sj[k2];
+               if (CF[i3] > 0) { idx = f2c[i3]; act = idx != ic; }
+            }
+            int pos = gb_winsert(T, count, idx, act, created, ovf);
+            if (FILL && created && pos >= 0) { S2j[off + pos] = idx; }
+            __syncwarp();
+         }
+      }
+      if (lane == 0)
+      {
+         if (!ovf) { if (!FILL) { cnt[ic] = count; } }
+         else if (!GLOBAL && !FILL) { ovf_list[atomicAdd(ovf_n, 1)] = ic; cnt[ic] = 0; }
+         else { atomicExch(err, 1); }
+      }
+      gb_tab_clear(T, count);
+   }
+}
+
+static int smem_blocks(int nrows)
+{
+   int dev = 0, sms = 148;
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   long long want = (nrows + GB_SMEM_WARPS - 1) / GB_SMEM_WARPS;
+   long long maxb = (long long) sms * 4;
+   return (int) (want < maxb ? (want < 1 ? 1 : want) : maxb);
+}
+
+extern "C" void gb_strength2(int nc, const int *c2f, const int *f2c, const int *Si, const int *Sj, const int *CF,
+                             int *cnt, const int *S2i, int *S2j, int *ovf_list, int *ovf_n, int *gtab, int gcap,
+                             int gwarps, int *err, int fill, int tier, cudaStream_t s)
+{
+   if (tier == 0)
+   {
+      int blocks = smem_blocks(nc);
+      if (!fill) { k_s2<false, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
+      else { k_s2<false, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
+   }
+   else
+   {
+      int blocks = (gwarps + 3) / 4;
+      if (!fill) { k_s2<true, false><<<blocks, 128, 0, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, gtab, gcap, err); }
+      else { k_s2<true, true><<<blocks, 128, 0, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, gtab, gcap, err); }
+   }
+   GB_COUNT(1);
+}
+
+// upper bound of an S2 row: |S_i1| + sum |S_i2|
+__global__ void k_s2_ub(int nc, const int *__restrict__ c2f, const int *__restrict__ Si, const int *__restrict__ Sj,
+                        int *__restrict__ ub)
+{
+   int ic = blockIdx.x * blockDim.x + threadIdx.x;
+   if (ic >= nc) { return; }
+   int i1 = c2f[ic];
+   long long u = 0;
+   for (int k = Si[i1]; k < Si[i1 + 1]; k++) { int i2 = Sj[k]; u += 1 + Si[i2 + 1] - Si[i2]; }
+   ub[ic] = (int) (u > nc ? nc : u);
+}
+
+extern "C" void gb_strength2_ub(int nc, const int *c2f, const int *Si, const int *Sj, int *ub, cudaStream_t s)
+{
+   k_s2_ub<<<gb_blocks2(nc, 256), 256, 0, s>>>(nc, c2f, Si, Sj, ub);
+   GB_COUNT(1);
+}
+
+// C points whose S2 row is empty become CF = 2 (par_strength.c:2701-2723)
+__global__ void k_mark_isolated(int nc, const int *__restrict__ c2f, const int *__restrict__ cnt, int *CF)
+{
+   int ic = blockIdx.x * blockDim.x + threadIdx.x;
+   if (ic < nc && cnt[ic] == 0) { CF[c2f[ic]] = 2; }
+}
+
+extern "C" void gb_mark_isolated(int nc, const int *c2f, const int *cnt, int *CF, cudaStream_t s)
+{
+   k_mark_isolated<<<gb_blocks2(nc, 256), 256, 0, s>>>(nc, c2f, cnt, CF);
+   GB_COUNT(1);
+}
+
+// hypre_BoomerAMGCorrectCFMarker2Host (par_strength.c:3096): C points made F
+// by the second coarsening become -2, the others 1.
+__global__ void k_correct_cf2(int n, const int *__restrict__ f2c, const int *__restrict__ CFN, int *CF)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n && CF[i] > 0) { CF[i] = CFN[f2c[i]] == -1 ? -2 : 1; }
+}
+
+extern "C" void gb_correct_cf2(int n, const int *f2c, const int *CFN, int *CF, cudaStream_t s)
+{
+   k_correct_cf2<<<gb_blocks2(n, 256), 256, 0, s>>>(n, f2c, CFN, CF);
+   GB_COUNT(1);
+}
+
+// CF < -1 -> -1 (partial.c:700)
+__global__ void k_cf_clamp(int n, int *CF)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n && CF[i] < -1) { CF[i] = -1; }
+}
+
+extern "C" void gb_cf_clamp(int n, int *CF, cudaStream_t s)
+{
+   k_cf_clamp<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// F/C blocks of A on strong connections (hypre_ParCSRMatrixGenerateFFFCHost
+// src/parcsr_mv/gen_fffc.c:18-530): for F row r (fine point i = fl[r]):
+// FF = [a_ii, strong F neighbours], FC = strong C neighbours, in S's order.
+// ---------------------------------------------------------------------------
+__global__ void k_fffc_count(int nf, const int *__restrict__ fl, const int *__restrict__ Ai,
+                             const int *__restrict__ Aj, const int *__restrict__ Si, const int *__restrict__ Sj,
+                             const int *__restrict__ CF, int *__restrict__ cff, int *__restrict__ cfc)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   int i = fl[r];
+   int ff = 0, fc = 0;
+   if (Ai[i] < Ai[i + 1] && Aj[Ai[i]] == i) { ff++; }
+   for (int k = Si[i]; k < Si[i + 1]; k++) { if (CF[Sj[k]] > 0) { fc++; } else { ff++; } }
+   cff[r] = ff;
+   cfc[r] = fc;
+}
+
+__global__ void k_fffc_fill(int nf, const int *__restrict__ fl, const int *__restrict__ Ai,
+                            const int *__restrict__ Aj, const double *__restrict__ Av, const int *__restrict__ Si,
+                            const int *__restrict__ Sj, const int *__restrict__ CF, const int *__restrict__ f2c,
+                            const int *__restrict__ f2f, const int *__restrict__ FFi, int *__restrict__ FFj,
+                            double *__restrict__ FFv, const int *__restrict__ FCi, int *__restrict__ FCj,
+                            double *__restrict__ FCv)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   int i = fl[r];
+   int pf = FFi[r], pc = FCi[r];
+   int a0 = Ai[i], a1 = Ai[i + 1];
+   int hasdiag = (a0 < a1 && Aj[a0] == i);
+   if (hasdiag) { FFj[pf] = f2f[i]; FFv[pf++] = Av[a0]; }
+   for (int k = Si[i]; k < Si[i + 1]; k++)
+   {
+      int jS = Sj[k];
+      int jA = a0 + hasdiag;
+      while (Aj[jA] != jS) { jA++; }
+      if (CF[jS] > 0) { FCj[pc] = f2c[jS]; FCv[pc++] = Av[jA]; }
+      else { FFj[pf] = f2f[jS]; FFv[pf++] = Av[jA]; }
+   }
+}
+
+extern "C" void gb_fffc_count(int nf, const int *fl, const int *Ai, const int *Aj, const int *Si, const int *Sj,
+                              const int *CF, int *cff, int *cfc, cudaStream_t s)
+{
+   k_fffc_count<<<gb_blocks2(nf, 256), 256, 0, s>>>(nf, fl, Ai, Aj, Si, Sj, CF, cff, cfc);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_fffc_fill(int nf, const int *fl, const int *Ai, const int *Aj, const double *Av, const int *Si,
+                             const int *Sj, const int *CF, const int *f2c, const int *f2f, const int *FFi, int *FFj,
+                             double *FFv, const int *FCi, int *FCj, double *FCv, cudaStream_t s)
+{
+   k_fffc_fill<<<gb_blocks2(nf, 128), 128, 0, s>>>(nf, fl, Ai, Aj, Av, Si, Sj, CF, f2c, f2f, FFi, FFj, FFv, FCi,
+                                                   FCj, FCv);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Scalings of the modified extended+i interpolation
+// (hypre_BoomerAMGBuildModExtPIInterpHost src/parcsr_ls/par_mod_lr_interp.c
+// :690-905, one function): D_q (FC row sums), D_w (A row sum minus the strong
+// F and C parts), D_theta, the division of FF's off-diagonals and the final
+// row scaling -1/(D_theta + D_w).
+// ---------------------------------------------------------------------------
+__global__ void k_mod_dq_dw(int nf, const int *__restrict__ fl, const int *__restrict__ Ai,
+                            const double *__restrict__ Av, const int *__restrict__ FFi,
+                            const double *__restrict__ FFv, const int *__restrict__ FCi,
+                            const double *__restrict__ FCv, double *__restrict__ Dq, double *__restrict__ Dw)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   double q = 0.0;
+   for (int k = FCi[r]; k < FCi[r + 1]; k++) { q += FCv[k]; }
+   int i = fl[r];
+   double w = 0.0;
+   for (int k = Ai[i]; k < Ai[i + 1]; k++) { w += Av[k]; }
+   for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { w -= FFv[k]; }
+   w -= q;
+   Dq[r] = q;
+   Dw[r] = w;
+}
+
+__global__ void k_mod_theta(int nf, const int *__restrict__ FFi, const int *__restrict__ FFj,
+                            double *__restrict__ FFv, const double *__restrict__ tmp, const double *__restrict__ Dq,
+                            const double *__restrict__ Dw)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   double dt = 0.0;
+   for (int j = FFi[r] + 1; j < FFi[r + 1]; j++)
+   {
+      int jj = FFj[j];
+      double value = Dq[jj];
+      for (int k = FFi[jj] + 1; k < FFi[jj + 1]; k++)
+      {
+         if (FFj[k] == r)
+         {
+            double value1 = tmp[k];
+            value += value1;
+            dt += FFv[j] * value1 / value;
+            break;
+         }
+      }
+      if (value != 0.0) { FFv[j] /= value; }
+   }
+   FFv[FFi[r]] = 1.0;
+   double theta = dt + Dw[r];
+   if (theta != 0.0)
+   {
+      theta = -1.0 / theta;
+      for (int j = FFi[r]; j < FFi[r + 1]; j++) { FFv[j] *= theta; }
+   }
+}
+
+extern "C" void gb_mod_extpi_scale(int nf, const int *fl, const int *Ai, const double *Av, const int *FFi,
+                                   const int *FFj, double *FFv, const int *FCi, const double *FCv, double *tmp,
+                                   double *Dq, double *Dw, cudaStream_t s)
+{
+   int nnzff = 0;
+   cudaMemcpyAsync(&nnzff, FFi + nf, sizeof(int), cudaMemcpyDeviceToHost, s);
+   cudaStreamSynchronize(s);
+   cudaMemcpyAsync(tmp, FFv, sizeof(double) * (size_t) nnzff, cudaMemcpyDeviceToDevice, s);
+   k_mod_dq_dw<<<gb_blocks2(nf, 256), 256, 0, s>>>(nf, fl, Ai, Av, FFi, FFv, FCi, FCv, Dq, Dw);
+   k_mod_theta<<<gb_blocks2(nf, 128), 128, 0, s>>>(nf, FFi, FFj, FFv, tmp, Dq, Dw);
+   GB_COUNT(2);
+}
+
+// P1 = [I; W] in fine order: C points get (f2c[i], 1), F points W's row f2f[i]
+__global__ void k_p1_len(int n, const int *__restrict__ CF, const int *__restrict__ f2f, const int *__restrict__ Wi,
+                         int *__restrict__ len)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   if (CF[i] > 0) { len[i] = 1; }
+   else { int r = f2f[i]; len[i] = Wi[r + 1] - Wi[r]; }
+}
+
+__global__ void k_p1_fill(int n, const int *__restrict__ CF, const int *__restrict__ f2c, const int *__restrict__ f2f,
+                          const int *__restrict__ Wi, const int *__restrict__ Wj, const double *__restrict__ Wv,
+                          const int *__restrict__ Pi, int *__restrict__ Pj, double *__restrict__ Pv)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int c = Pi[i];
+   if (CF[i] > 0) { Pj[c] = f2c[i]; Pv[c] = 1.0; }
+   else
+   {
+      int r = f2f[i];
+      for (int k = Wi[r]; k < Wi[r + 1]; k++) { Pj[c] = Wj[k]; Pv[c] = Wv[k]; c++; }
+   }
+}
+
+extern "C" void gb_p1_len(int n, const int *CF, const int *f2f, const int *Wi, int *len, cudaStream_t s)
+{
+   k_p1_len<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, f2f, Wi, len);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_p1_fill(int n, const int *CF, const int *f2c, const int *f2f, const int *Wi, const int *Wj,
+                           const double *Wv, const int *Pi, int *Pj, double *Pv, cudaStream_t s)
+{
+   k_p1_fill<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, f2c, f2f, Wi, Wj, Wv, Pi, Pj, Pv);
+   GB_COUNT(1);
+}

@@ -173,7 +173,273 @@ gb_parcsr *gb_transpose(gb_parcsr *M)
 }
 
 /* --------------------------------------------------------------------------
- * one coarsening level (non-aggressive): S, CF, P, A_c
+ * Tiered drivers: shared-memory tables first, overflowing rows again with
+ * global tables sized from the rows' upper bounds.
+ * ------------------------------------------------------------------------ */
+typedef struct
+{
+   int *ovf_list, *ovf_n, *err;
+   int  h_ovf;
+   int *gtab;
+   int  gcap, gwarps;
+} gb_tier;
+
+static void tier_begin(gb_tier *t, int nrows)
+{
+   memset(t, 0, sizeof(*t));
+   t->ovf_list = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows > 0 ? nrows : 1));
+   t->ovf_n = (int *) gb_dcalloc(sizeof(int) * 2);
+   t->err = (int *) gb_dcalloc(sizeof(int) * 2);
+}
+
+/* after the symbolic shared-memory pass: read the overflow count and, if
+ * needed, size the global tables from ub (device, nub entries) */
+static void tier_global(gb_tier *t, const int *ub, int nub)
+{
+   t->h_ovf = read_int(t->ovf_n);
+   if (t->h_ovf <= 0) { return; }
+   int m = max_of(ub, nub);
+   t->gcap = next_pow2(2LL * (m + 1));
+   size_t per = (size_t) 12 * (size_t) t->gcap;
+   t->gwarps = slab_warps(per, t->h_ovf);
+   t->gtab = (int *) gb_dmalloc(per * (size_t) t->gwarps);
+   if (t->gtab) { cudaMemsetAsync(t->gtab, 0xff, per * (size_t) t->gwarps, gb_stream()); }
+}
+
+static int tier_end(gb_tier *t)
+{
+   int e = read_int(t->err);
+   gb_dfree(t->ovf_list); gb_dfree(t->ovf_n); gb_dfree(t->err); gb_dfree(t->gtab);
+   return e;
+}
+
+/* C = A B with hypre_ParMatmul's column order (square: diagonal first) */
+static int spgemm_host(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
+{
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_tier t;
+   tier_begin(&t, n);
+   gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, 0, 0,
+             t.err, 0, 0, s);
+   int *ub = NULL;
+   if (read_int(t.ovf_n) > 0)
+   {
+      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+      gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+   }
+   tier_global(&t, ub, n);
+   if (t.h_ovf > 0)
+   {
+      gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, t.gtab,
+                t.gcap, t.gwarps, t.err, 0, 1, s);
+   }
+   C->nr = n; C->nc = B->nc;
+   C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   C->nnz = scan_total(cnt, C->i, n);
+   C->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C->nnz ? C->nnz : 1));
+   C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
+   gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL, 0, 0,
+             t.err, 1, 0, s);
+   if (t.h_ovf > 0)
+   {
+      gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, t.gtab,
+                t.gcap, t.gwarps, t.err, 1, 1, s);
+   }
+   int e = tier_end(&t);
+   gb_dfree(ub); gb_dfree(cnt);
+   if (e) { gb_error(HYPRE_ERROR_GENERIC, "sparse product table overflow"); return -1; }
+   return 0;
+}
+
+/* extended+i rows for fine points rows[r] (all points when rows == NULL) */
+static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int *f2c, int nrows, const int *rows,
+                      int ncols, gb_csr *P)
+{
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
+   gb_tier t;
+   tier_begin(&t, nrows);
+   gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 0, s);
+   int *ub = NULL;
+   if (read_int(t.ovf_n) > 0)
+   {
+      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+      gb_extpi_ub(n, S->i, S->j, CF, ub, s);
+   }
+   tier_global(&t, ub, n);
+   if (t.h_ovf > 0)
+   {
+      gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps, t.err, 1, s);
+   }
+   P->nr = nrows; P->nc = ncols;
+   P->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
+   P->nnz = scan_total(cnt, P->i, nrows);
+   P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
+   P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
+   gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, t.ovf_list, t.ovf_n, NULL, 0,
+                 0, t.err, 0, s);
+   if (t.h_ovf > 0)
+   {
+      gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, t.ovf_list, t.ovf_n,
+                    t.gtab, t.gcap, t.gwarps, t.err, 1, s);
+   }
+   int e = tier_end(&t);
+   gb_dfree(ub); gb_dfree(cnt);
+   if (e) { gb_error(HYPRE_ERROR_GENERIC, "interpolation table overflow"); return -1; }
+   return 0;
+}
+
+/* truncation by tolerance / max elements (par_csr_matrix.c:2943) in place */
+static void truncate_host(gb_csr *P, double tol, int max_elmts)
+{
+   if (!(tol > 0.0 || max_elmts > 0)) { return; }
+   cudaStream_t s = gb_stream();
+   int n = P->nr;
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_truncate_rows(n, P->i, P->j, P->v, tol, max_elmts, cnt, s);
+   int *Ni = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int nnz2 = scan_total(cnt, Ni, n);
+   int *Nj = (int *) gb_dmalloc(sizeof(int) * (size_t) (nnz2 ? nnz2 : 1));
+   double *Nv = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz2 ? nnz2 : 1));
+   gb_compact_rows(n, P->i, P->j, P->v, Ni, Nj, Nv, s);
+   gb_dfree(P->i); gb_dfree(P->j); gb_dfree(P->v);
+   P->i = Ni; P->j = Nj; P->v = Nv; P->nnz = nnz2;
+   gb_dfree(cnt);
+}
+
+/* scanned flag numbering: out[i] = number of flagged points before i; list (optional) */
+static int number_points(int n, const int *CF, int kind, int v, int *out, int **list)
+{
+   cudaStream_t s = gb_stream();
+   int *flag = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_flags(n, CF, kind, v, flag, s);
+   int tot = scan_total(flag, out, n);
+   if (list)
+   {
+      *list = (int *) gb_dmalloc(sizeof(int) * (size_t) (tot > 0 ? tot : 1));
+      gb_scatter_list(n, flag, out, *list, s);
+   }
+   gb_dfree(flag);
+   return tot;
+}
+
+/* aggressive level (par_amg_setup.c:1311-1358, :1778-1915, agg_interp_type 6):
+ * second-order strength, PMIS on it, P = P1 P2 with P1 modified extended+i
+ * and P2 partial extended+i.  Returns the number of coarse points. */
+static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb_csr *P)
+{
+   gb_amg_params *prm = &amg->prm;
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   /* first-pass C numbering and list */
+   int *f2c1 = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *c2f1 = NULL;
+   int nc1 = number_points(n, CF, 0, 0, f2c1, &c2f1);
+   /* S2 (par_strength.c:1795) */
+   gb_csr S2;
+   memset(&S2, 0, sizeof(S2));
+   S2.nr = S2.nc = nc1;
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 + 1));
+   gb_tier t;
+   tier_begin(&t, nc1);
+   gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, NULL, NULL, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 0, 0, s);
+   int *ub = NULL;
+   if (read_int(t.ovf_n) > 0)
+   {
+      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 > 0 ? nc1 : 1));
+      gb_strength2_ub(nc1, c2f1, S->i, S->j, ub, s);
+   }
+   tier_global(&t, ub, nc1);
+   if (t.h_ovf > 0)
+   {
+      gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, NULL, NULL, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
+                   t.err, 0, 1, s);
+   }
+   gb_mark_isolated(nc1, c2f1, cnt, CF, s);
+   S2.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 + 1));
+   S2.nnz = scan_total(cnt, S2.i, nc1);
+   S2.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (S2.nnz ? S2.nnz : 1));
+   gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, S2.i, S2.j, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 1, 0, s);
+   if (t.h_ovf > 0)
+   {
+      gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, S2.i, S2.j, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
+                   t.err, 1, 1, s);
+   }
+   if (tier_end(&t)) { gb_error(HYPRE_ERROR_GENERIC, "second-order strength overflow"); return -1; }
+   gb_dfree(ub);
+   /* PMIS on S2 with CF_init 3 */
+   int *CFN = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 ? nc1 : 1));
+   {
+      double *measure = (double *) gb_dmalloc(sizeof(double) * (size_t) (nc1 ? nc1 : 1));
+      int *ingraph = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 ? nc1 : 1));
+      int *counter = (int *) gb_dmalloc(sizeof(int) * 4);
+      int *hcount = (int *) gb_hmalloc_pinned(sizeof(int) * 4);
+      int it = gb_pmis(nc1, S2.i, S2.j, 3, CFN, measure, ingraph, cnt, counter, hcount, 10000, s);
+      gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter); gb_hfree_pinned(hcount);
+      if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS on S2 did not terminate"); return -1; }
+   }
+   gb_csr_free(&S2);
+   /* P1: modified extended+i (par_mod_lr_interp.c:585) */
+   int *f2f = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *fl = NULL;
+   int nf = number_points(n, CF, 2, 0, f2f, &fl);
+   gb_csr FF, FC;
+   FF.nr = FF.nc = nf; FC.nr = nf; FC.nc = nc1;
+   int *cff = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   int *cfc = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   gb_fffc_count(nf, fl, A->i, A->j, S->i, S->j, CF, cff, cfc, s);
+   FF.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   FC.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   FF.nnz = scan_total(cff, FF.i, nf);
+   FC.nnz = scan_total(cfc, FC.i, nf);
+   FF.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FF.nnz ? FF.nnz : 1));
+   FF.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
+   FC.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FC.nnz ? FC.nnz : 1));
+   FC.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FC.nnz ? FC.nnz : 1));
+   gb_fffc_fill(nf, fl, A->i, A->j, A->v, S->i, S->j, CF, f2c1, f2f, FF.i, FF.j, FF.v, FC.i, FC.j, FC.v, s);
+   {
+      double *tmp = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
+      double *Dq = (double *) gb_dmalloc(sizeof(double) * (size_t) (nf ? nf : 1));
+      double *Dw = (double *) gb_dmalloc(sizeof(double) * (size_t) (nf ? nf : 1));
+      gb_mod_extpi_scale(nf, fl, A->i, A->v, FF.i, FF.j, FF.v, FC.i, FC.v, tmp, Dq, Dw, s);
+      gb_dfree(tmp); gb_dfree(Dq); gb_dfree(Dw);
+   }
+   gb_csr W;
+   if (spgemm_host(&FF, &FC, nf == nc1, &W)) { return -1; }
+   gb_csr_free(&FF); gb_csr_free(&FC);
+   gb_csr P1;
+   P1.nr = n; P1.nc = nc1;
+   int *len = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_p1_len(n, CF, f2f, W.i, len, s);
+   P1.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   P1.nnz = scan_total(len, P1.i, n);
+   P1.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P1.nnz ? P1.nnz : 1));
+   P1.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P1.nnz ? P1.nnz : 1));
+   gb_p1_fill(n, CF, f2c1, f2f, W.i, W.j, W.v, P1.i, P1.j, P1.v, s);
+   gb_csr_free(&W);
+   truncate_host(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
+   /* CF correction (par_strength.c:3096) and P2: partial extended+i over the
+    * old C points (partial.c:16) */
+   gb_correct_cf2(n, f2c1, CFN, CF, s);
+   int *f2c2 = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int nc2 = number_points(n, CF, 1, 1, f2c2, NULL);
+   gb_csr P2;
+   if (extpi_host(A, S, CF, f2c2, nc1, c2f1, nc2, &P2)) { return -1; }
+   gb_cf_clamp(n, CF, s);
+   truncate_host(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
+   if (spgemm_host(&P1, &P2, n == nc2, P)) { return -1; }
+   truncate_host(P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
+   gb_csr_free(&P1); gb_csr_free(&P2);
+   gb_dfree(f2c1); gb_dfree(c2f1); gb_dfree(f2f); gb_dfree(fl); gb_dfree(f2c2); gb_dfree(cnt); gb_dfree(CFN);
+   gb_dfree(cff); gb_dfree(cfc); gb_dfree(len);
+   return nc2;
+}
+
+/* --------------------------------------------------------------------------
+ * one coarsening level: S, CF, P, A_c
  * returns 1 if a coarse level was produced, 0 to stop, -1 on error
  * ------------------------------------------------------------------------ */
 static int setup_level(gb_amg *amg, int l, double *t_phase)
@@ -200,86 +466,54 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
 
    /* 2. PMIS (par_coarsen.c:2094) */
    int *CF = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
-   double *measure = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
-   int *ingraph = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
-   int *counter = (int *) gb_dmalloc(sizeof(int) * 4);
-   int *hcount = (int *) gb_hmalloc_pinned(sizeof(int) * 4);
-   int it = gb_pmis(n, S.i, S.j, 0, CF, measure, ingraph, cnt, counter, hcount, 10000, s);
-   gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter); gb_hfree_pinned(hcount);
-   if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS did not terminate"); return -1; }
-
-   /* 3. coarse points and numbering (par_coarse_parms.c:45) */
-   int *f2c = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   gb_cpoint_flags(n, CF, cnt, s);
-   int nc = scan_total(cnt, f2c, n);
+   {
+      double *measure = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
+      int *ingraph = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
+      int *counter = (int *) gb_dmalloc(sizeof(int) * 4);
+      int *hcount = (int *) gb_hmalloc_pinned(sizeof(int) * 4);
+      int it = gb_pmis(n, S.i, S.j, 0, CF, measure, ingraph, cnt, counter, hcount, 10000, s);
+      gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter); gb_hfree_pinned(hcount);
+      if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS did not terminate"); return -1; }
+   }
    double t2 = gb_wtime();
    t_phase[1] += t2 - t1;
-   if (nc == 0 || nc == n || nc < prm->min_coarse_size)
-   {
-      gb_dfree(cnt); gb_dfree(f2c); gb_dfree(CF); gb_csr_free(&S);
-      return 0;
-   }
 
-   /* 4. extended+i interpolation (par_lr_interp.c:1024) */
-   gb_extpi_ub(n, S.i, S.j, CF, cnt, s);
-   int ubmax = max_of(cnt, n);
-   int cap = next_pow2(2LL * (ubmax + 1));
-   int nw = slab_warps(gb_slab_bytes_c(cap), n);
-   char *slabs = alloc_slabs(cap, nw);
-   int *ovf = (int *) gb_dcalloc(sizeof(int) * 4);
-   gb_extpi_count(n, S.i, S.j, CF, slabs, cap, nw, cnt, ovf, s);
    gb_csr P;
-   P.nr = n; P.nc = nc;
-   P.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   P.nnz = scan_total(cnt, P.i, n);
-   P.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P.nnz ? P.nnz : 1));
-   P.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P.nnz ? P.nnz : 1));
-   gb_extpi_fill(n, A->i, A->j, A->v, S.i, S.j, CF, f2c, P.i, P.j, P.v, slabs, cap, nw, ovf, s);
-   gb_sf_to_f(n, CF, s);
-   if (read_int(ovf)) { gb_error(HYPRE_ERROR_GENERIC, "interpolation table overflow"); return -1; }
-   gb_dfree(slabs);
-
-   /* 5. truncation (par_interp.c:2622 -> par_csr_matrix.c:2943) */
-   if (prm->trunc_factor > 0.0 || prm->p_max_elmts > 0)
+   int nc;
+   if (l < prm->agg_num_levels)
    {
-      gb_truncate_rows(n, P.i, P.j, P.v, prm->trunc_factor, prm->p_max_elmts, cnt, s);
-      int *Ni = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-      int nnz2 = scan_total(cnt, Ni, n);
-      int *Nj = (int *) gb_dmalloc(sizeof(int) * (size_t) (nnz2 ? nnz2 : 1));
-      double *Nv = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz2 ? nnz2 : 1));
-      gb_compact_rows(n, P.i, P.j, P.v, Ni, Nj, Nv, s);
-      gb_csr_free(&P);
-      P.i = Ni; P.j = Nj; P.v = Nv; P.nnz = nnz2;
+      nc = agg_interp(amg, A, &S, CF, &P);
+      if (nc < 0) { return -1; }
+   }
+   else
+   {
+      /* 3. coarse points and numbering (par_coarse_parms.c:45) */
+      int *f2c = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      gb_cpoint_flags(n, CF, cnt, s);
+      nc = scan_total(cnt, f2c, n);
+      if (nc == 0 || nc == n || nc < prm->min_coarse_size)
+      {
+         gb_dfree(cnt); gb_dfree(f2c); gb_dfree(CF); gb_csr_free(&S);
+         return 0;
+      }
+      /* 4. extended+i interpolation (par_lr_interp.c:1024) and truncation */
+      if (extpi_host(A, &S, CF, f2c, n, NULL, nc, &P)) { return -1; }
+      gb_sf_to_f(n, CF, s);
+      truncate_host(&P, prm->trunc_factor, prm->p_max_elmts);
+      gb_dfree(f2c);
    }
    double t3 = gb_wtime();
    t_phase[2] += t3 - t2;
 
-   /* 6. R = P^T and A_c = R A P (par_rap.c:30) */
+   /* 5. R = P^T and A_c = (R A) P (par_rap.c:30) */
    gb_parcsr *Pm = gb_parcsr_wrap(P, 1);
    gb_parcsr *Rm = gb_transpose(Pm);
    if (!Rm) { return -1; }
-   gb_csr *R = &Rm->A;
-   int *apub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
-   int *ubra = (int *) gb_dmalloc(sizeof(int) * (size_t) nc);
-   int *ubrap = (int *) gb_dmalloc(sizeof(int) * (size_t) nc);
-   gb_rap_bounds(n, nc, R->i, R->j, A->i, A->j, P.i, apub, ubra, ubrap, s);
-   int mra = max_of(ubra, nc), mrap = max_of(ubrap, nc);
-   int cap_a = next_pow2(2LL * (mra + 1)), cap_c = next_pow2(2LL * (mrap + 1));
-   int nw2 = slab_warps(gb_slab_bytes_c(cap_a) + gb_slab_bytes_c(cap_c), nc);
-   char *sa = alloc_slabs(cap_a, nw2), *sc = alloc_slabs(cap_c, nw2);
-   gb_csr C;
-   C.nr = C.nc = nc;
-   C.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc + 1));
-   gb_rap(nc, R->i, R->j, R->v, A->i, A->j, A->v, P.i, P.j, P.v, sa, cap_a, sc, cap_c, nw2, 0, NULL, NULL, NULL,
-          cnt, ovf, s);
-   C.nnz = scan_total(cnt, C.i, nc);
-   C.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C.nnz ? C.nnz : 1));
-   C.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C.nnz ? C.nnz : 1));
-   gb_rap(nc, R->i, R->j, R->v, A->i, A->j, A->v, P.i, P.j, P.v, sa, cap_a, sc, cap_c, nw2, 1, C.i, C.j, C.v,
-          cnt, ovf, s);
-   if (read_int(ovf)) { gb_error(HYPRE_ERROR_GENERIC, "RAP table overflow"); return -1; }
-   gb_dfree(sa); gb_dfree(sc); gb_dfree(apub); gb_dfree(ubra); gb_dfree(ubrap); gb_dfree(ovf);
-   gb_dfree(cnt); gb_dfree(f2c);
+   gb_csr RA, C;
+   if (spgemm_host(&Rm->A, A, 0, &RA)) { return -1; }
+   if (spgemm_host(&RA, &P, 1, &C)) { return -1; }
+   gb_csr_free(&RA);
+   gb_dfree(cnt);
    double t4 = gb_wtime();
    t_phase[3] += t4 - t3;
 
@@ -304,9 +538,10 @@ int gb_amg_setup(gb_amg *amg, gb_parcsr *A0)
    amg->lev[0].n = A0->A.nr;
    int level = 0;
    int maxl = prm->max_levels < 32 ? prm->max_levels : 32;
-   if (prm->agg_num_levels > 0)
+   if (prm->agg_num_levels > 0 && prm->agg_interp_type != 6)
    {
-      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening levels are not supported by this build");
+      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening: only agg_interp_type 6 is supported");
+      return gb_error_flag;
    }
    while (1)
    {

@@ -135,3 +135,79 @@ static inline size_t gb_slab_bytes(int cap)
 {
    return (size_t) cap * 4 * 2 + (size_t) (cap / 2) * (4 + 4 + 8);
 }
+
+// ---------------------------------------------------------------------------
+// Table used by the tiered setup kernels: the hash (key -> position) and the
+// row's key list (for clearing), without values -- values are accumulated in
+// the output arrays at row_offset + position.  Layout: hk[cap] hp[cap]
+// lkeys[cap/2] lslot[cap/2]  (12 * cap bytes).
+// ---------------------------------------------------------------------------
+struct GbTab
+{
+   int *hk, *hp, *lkeys, *lslot;
+   int  cap, listcap;
+};
+
+__device__ __forceinline__ GbTab gb_tab_at(int *base, int cap)
+{
+   GbTab t;
+   t.cap = cap;
+   t.listcap = cap / 2;
+   t.hk = base;
+   t.hp = base + cap;
+   t.lkeys = base + 2 * cap;
+   t.lslot = base + 2 * cap + cap / 2;
+   return t;
+}
+
+#define GB_TAB_INTS(cap) (3 * (cap))
+
+// Fills the hash keys of a table with -1 (warp-cooperative).
+__device__ __forceinline__ void gb_tab_init(GbTab &t)
+{
+   for (int k = gb_lane(); k < t.cap; k += 32) { t.hk[k] = -1; }
+   __syncwarp();
+}
+
+// Ordered insertion as gb_warp_insert; ovf becomes 1 on every lane when the
+// table or the list fills up.
+__device__ __forceinline__ int gb_winsert(GbTab &t, int &count, int key, bool active, bool &created, int &ovf)
+{
+   const int lane = gb_lane();
+   int pos = active ? gb_tab_find(t.hk, t.hp, t.cap, key) : -1;
+   bool need = active && pos < 0;
+   int mkey = need ? key : -(lane + 2);
+   unsigned grp = __match_any_sync(GB_FULL, mkey);
+   int leader = __ffs(grp) - 1;
+   bool lead = need && leader == lane;
+   unsigned newmask = __ballot_sync(GB_FULL, lead);
+   bool bad = false;
+   if (lead)
+   {
+      int p = count + __popc(newmask & ((1u << lane) - 1u));
+      int slot = p < t.listcap ? gb_tab_insert(t.hk, t.hp, t.cap, key, p) : -1;
+      if (slot >= 0) { t.lkeys[p] = key; t.lslot[p] = slot; pos = p; }
+      else { bad = true; pos = -1; }
+   }
+   int lp = __shfl_sync(GB_FULL, pos, leader);
+   if (need && !lead) { pos = lp; }
+   count += __popc(newmask);
+   if (count > t.listcap) { count = t.listcap; }
+   if (__any_sync(GB_FULL, bad)) { ovf = 1; }
+   created = lead;
+   __syncwarp();
+   return pos;
+}
+
+__device__ __forceinline__ void gb_tab_clear(GbTab &t, int n)
+{
+   __syncwarp();
+   if (n > t.listcap) { n = t.listcap; }
+   for (int k = gb_lane(); k < n; k += 32) { t.hk[t.lslot[k]] = -1; }
+   __syncwarp();
+}
+
+// shared-memory tier: 1024-slot table (512 list entries) per warp, 4 warps
+#define GB_SMEM_CAP 1024
+#define GB_SMEM_WARPS 4
+#define GB_SMEM_BYTES (GB_SMEM_WARPS * GB_TAB_INTS(GB_SMEM_CAP) * 4)

@@ -52,11 +52,12 @@ int  gb_pmis(int n, const int *Si, const int *Sj, int CF_init, int *CF, double *
 void gb_cpoint_flags(int n, const int *CF, int *flag, cudaStream_t s);
 void gb_sf_to_f(int n, int *CF, cudaStream_t s);
 void gb_extpi_ub(int n, const int *Si, const int *Sj, const int *CF, int *ub, cudaStream_t s);
-void gb_extpi_count(int n, const int *Si, const int *Sj, const int *CF, char *slabs, int cap, int nwarps, int *cnt,
-                    int *overflow, cudaStream_t s);
-void gb_extpi_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj, const int *CF,
-                   const int *f2c, const int *Pi, int *Pj, double *Pv, char *slabs, int cap, int nwarps,
-                   int *overflow, cudaStream_t s);
+void gb_extpi_count(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF, int *cnt,
+                    int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int tier, cudaStream_t s);
+void gb_extpi_fill(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av, const int *Si,
+                   const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv,
+                   const int *ovf_list, const int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int tier,
+                   cudaStream_t s);
 void gb_truncate_rows(int n, const int *Pi, int *Pj, double *Pv, double tol, int max_elmts, int *newcnt,
                       cudaStream_t s);
 void gb_compact_rows(int n, const int *Pi, const int *Pj, const double *Pv, const int *Ni, int *Nj, double *Nv,
@@ -64,11 +65,32 @@ void gb_compact_rows(int n, const int *Pi, const int *Pj, const double *Pv, cons
 void gb_transpose_count(int nnz, const int *Aj, int *cnt, cudaStream_t s);
 void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, const double *Av, int *fill, const int *Ti,
                        int *Tj, double *Tv, cudaStream_t s);
-void gb_rap_bounds(int nf, int nc, const int *Ri, const int *Rj, const int *Ai, const int *Aj, const int *Pi,
-                   int *apub, int *ubra, int *ubrap, cudaStream_t s);
-void gb_rap(int nc, const int *Ri, const int *Rj, const double *Rv, const int *Ai, const int *Aj, const double *Av,
-            const int *Pi, const int *Pj, const double *Pv, char *slab_a, int cap_a, char *slab_c, int cap_c,
-            int nwarps, int numeric, const int *Ci, int *Cj, double *Cv, int *cnt, int *overflow, cudaStream_t s);
+void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int *ub,
+                  cudaStream_t s);
+void gb_spgemm(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi, const int *Bj,
+               const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list, int *ovf_n, int *gtab,
+               int gcap, int gwarps, int *err, int phase, int tier, cudaStream_t s);
+/* aggressive coarsening (gb_agg.cu) */
+void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);
+void gb_scatter_list(int n, const int *flag, const int *scan, int *list, cudaStream_t s);
+void gb_strength2(int nc, const int *c2f, const int *f2c, const int *Si, const int *Sj, const int *CF, int *cnt,
+                  const int *S2i, int *S2j, int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err,
+                  int fill, int tier, cudaStream_t s);
+void gb_strength2_ub(int nc, const int *c2f, const int *Si, const int *Sj, int *ub, cudaStream_t s);
+void gb_mark_isolated(int nc, const int *c2f, const int *cnt, int *CF, cudaStream_t s);
+void gb_correct_cf2(int n, const int *f2c, const int *CFN, int *CF, cudaStream_t s);
+void gb_cf_clamp(int n, int *CF, cudaStream_t s);
+void gb_fffc_count(int nf, const int *fl, const int *Ai, const int *Aj, const int *Si, const int *Sj, const int *CF,
+                   int *cff, int *cfc, cudaStream_t s);
+void gb_fffc_fill(int nf, const int *fl, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj,
+                  const int *CF, const int *f2c, const int *f2f, const int *FFi, int *FFj, double *FFv,
+                  const int *FCi, int *FCj, double *FCv, cudaStream_t s);
+void gb_mod_extpi_scale(int nf, const int *fl, const int *Ai, const double *Av, const int *FFi, const int *FFj,
+                        double *FFv, const int *FCi, const double *FCv, double *tmp, double *Dq, double *Dw,
+                        cudaStream_t s);
+void gb_p1_len(int n, const int *CF, const int *f2f, const int *Wi, int *len, cudaStream_t s);
+void gb_p1_fill(int n, const int *CF, const int *f2c, const int *f2f, const int *Wi, const int *Wj, const double *Wv,
+                const int *Pi, int *Pj, double *Pv, cudaStream_t s);
 void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, double *l1, cudaStream_t s);
 void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, double *D, double *W, cudaStream_t s);
 

@@ -351,7 +351,14 @@ extern "C" void gb_sf_to_f(int n, int *CF, cudaStream_t s)
 
 // ---------------------------------------------------------------------------
 // Extended+i interpolation (reference: src/parcsr_ls/par_lr_interp.c:1024-1924,
-// hypre_BoomerAMGBuildExtPIInterpHost, one process).
+// hypre_BoomerAMGBuildExtPIInterpHost, one process) and its partial form for
+// aggressive coarsening (src/parcsr_ls/partial.c:16-720), which builds the same
+// rows for a listed subset of points (the old C points) numbered by list
+// position.
+//
+// Tiers: every row is first built with a 1024-slot table in shared memory;
+// rows whose candidate set does not fit are listed and rebuilt by a second
+// launch with tables in global memory.
 // ---------------------------------------------------------------------------
 
 // Upper bound of the candidate C set of each row: |S_i| + sum over strong F
@@ -377,80 +384,108 @@ __global__ void k_extpi_ub(int n, const int *__restrict__ Si, const int *__restr
 // Discovers the interpolation columns of F row i in the reference's order
 // (strong C neighbours, then strong C neighbours of strong F neighbours).
 __device__ __forceinline__ void extpi_discover(int i, const int *__restrict__ Si, const int *__restrict__ Sj,
-                                               const int *__restrict__ CF, GbSlab &T, int &count, int *overflow,
+                                               const int *__restrict__ CF, GbTab &T, int &count, int &ovf,
                                                int *Pj_row, const int *f2c, double *Pv_row)
 {
    const int lane = gb_lane();
-   for (int k = Si[i]; k < Si[i + 1]; k++)
+   for (int k = Si[i]; k < Si[i + 1] && !ovf; k++)
    {
       int i1 = Sj[k];
       int cf1 = CF[i1];
       if (cf1 >= 0)
       {
          bool created;
-         int pos = gb_warp_insert(T.hk, T.hp, T.cap, T.lkeys, T.lslot, T.listcap, count, i1, lane == 0,
-                                  &created, overflow);
+         int pos = gb_winsert(T, count, i1, lane == 0, created, ovf);
          if (created && Pj_row && pos >= 0) { Pj_row[pos] = f2c[i1]; Pv_row[pos] = 0.0; }
       }
       else if (cf1 != SF_PT)
       {
          int b = Si[i1], e = Si[i1 + 1];
-         for (int base = b; base < e; base += 32)
+         for (int base = b; base < e && !ovf; base += 32)
          {
             int kk = base + lane;
             int k1 = kk < e ? Sj[kk] : -1;
             bool act = kk < e && CF[k1] >= 0;
             bool created;
-            int pos = gb_warp_insert(T.hk, T.hp, T.cap, T.lkeys, T.lslot, T.listcap, count, k1, act,
-                                     &created, overflow);
+            int pos = gb_winsert(T, count, k1, act, created, ovf);
             if (created && Pj_row && pos >= 0) { Pj_row[pos] = f2c[k1]; Pv_row[pos] = 0.0; }
          }
       }
    }
+   __syncwarp();
 }
 
-__global__ void k_extpi_count(int n, const int *__restrict__ Si, const int *__restrict__ Sj,
-                              const int *__restrict__ CF, char *slabs, int cap, int *__restrict__ cnt,
-                              int *overflow)
+// Row r of the output is point i = rows ? rows[r] : r.
+// GLOBAL == false: shared-memory tables, all rows; rows that overflow are
+// appended to ovf_list.  GLOBAL == true: global tables, rows from ovf_list.
+template <bool GLOBAL>
+__global__ void __launch_bounds__(128) k_extpi_count(int nrows, const int *__restrict__ rows,
+                                                     const int *__restrict__ Si, const int *__restrict__ Sj,
+                                                     const int *__restrict__ CF, int *__restrict__ cnt,
+                                                     int *ovf_list, int *ovf_n, int *gtab, int gcap, int *err)
 {
-   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-   int nwarps = (gridDim.x * blockDim.x) >> 5;
-   GbSlab T = gb_slab(slabs, cap, warp);
-   for (int i = warp; i < n; i += nwarps)
-   {
-      int cf = CF[i];
-      if (cf >= 0) { if (gb_lane() == 0) { cnt[i] = 1; } continue; }
-      if (cf == SF_PT) { if (gb_lane() == 0) { cnt[i] = 0; } continue; }
-      int count = 0;
-      extpi_discover(i, Si, Sj, CF, T, count, overflow, nullptr, nullptr, nullptr);
-      if (gb_lane() == 0) { cnt[i] = count; }
-      gb_warp_clear(T.hk, T.lslot, count);
-   }
-}
-
-__global__ void k_extpi_fill(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
-                             const double *__restrict__ Av, const int *__restrict__ Si,
-                             const int *__restrict__ Sj, const int *__restrict__ CF,
-                             const int *__restrict__ f2c, const int *__restrict__ Pi, int *__restrict__ Pj,
-                             double *__restrict__ Pv, char *slabs, int cap, int *overflow)
-{
+   extern __shared__ int sh[];
    const int lane = gb_lane();
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;
-   GbSlab T = gb_slab(slabs, cap, warp);
-   for (int i = warp; i < n; i += nwarps)
+   GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
+                    : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
+   if (!GLOBAL) { gb_tab_init(T); }
+   int total = GLOBAL ? *ovf_n : nrows;
+   for (int t = warp; t < total; t += nwarps)
    {
+      int r = GLOBAL ? ovf_list[t] : t;
+      int i = rows ? rows[r] : r;
       int cf = CF[i];
-      int begin = Pi[i];
+      if (cf >= 0) { if (lane == 0) { cnt[r] = 1; } continue; }
+      if (cf == SF_PT) { if (lane == 0) { cnt[r] = 0; } continue; }
+      int count = 0, ovf = 0;
+      extpi_discover(i, Si, Sj, CF, T, count, ovf, nullptr, nullptr, nullptr);
+      if (lane == 0)
+      {
+         if (!ovf) { cnt[r] = count; }
+         else if (!GLOBAL) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         else { atomicExch(err, 1); }
+      }
+      gb_tab_clear(T, count);
+   }
+}
+
+template <bool GLOBAL>
+__global__ void __launch_bounds__(128) k_extpi_fill(int nrows, const int *__restrict__ rows,
+                                                    const int *__restrict__ Ai, const int *__restrict__ Aj,
+                                                    const double *__restrict__ Av, const int *__restrict__ Si,
+                                                    const int *__restrict__ Sj, const int *__restrict__ CF,
+                                                    const int *__restrict__ f2c, const int *__restrict__ Pi,
+                                                    int *__restrict__ Pj, double *__restrict__ Pv,
+                                                    const int *ovf_list, const int *ovf_n, int *gtab, int gcap,
+                                                    int *err)
+{
+   extern __shared__ int sh[];
+   const int lane = gb_lane();
+   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   int nwarps = (gridDim.x * blockDim.x) >> 5;
+   GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
+                    : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
+   if (!GLOBAL) { gb_tab_init(T); }
+   int total = GLOBAL ? *ovf_n : nrows;
+   for (int t = warp; t < total; t += nwarps)
+   {
+      int r = GLOBAL ? ovf_list[t] : t;
+      int i = rows ? rows[r] : r;
+      int cf = CF[i];
+      int begin = Pi[r];
+      int len = Pi[r + 1] - begin;
       if (cf >= 0)
       {
          if (lane == 0) { Pj[begin] = f2c[i]; Pv[begin] = 1.0; }
          continue;
       }
       if (cf == SF_PT) { continue; }
-      int count = 0;
-      extpi_discover(i, Si, Sj, CF, T, count, overflow, Pj + begin, f2c, Pv + begin);
-      __syncwarp();
+      if (!GLOBAL && len > T.listcap) { continue; }   // rebuilt by the global tier
+      int count = 0, ovf = 0;
+      extpi_discover(i, Si, Sj, CF, T, count, ovf, Pj + begin, f2c, Pv + begin);
+      if (ovf) { if (lane == 0) { atomicExch(err, 1); } gb_tab_clear(T, count); continue; }
       double *P = Pv + begin;
       double diagonal = Av[Ai[i]];
       int sp = Si[i], se = Si[i + 1];
@@ -470,7 +505,7 @@ __global__ void k_extpi_fill(int n, const int *__restrict__ Ai, const int *__res
          else if (strong && cf1 < 0 && cf1 != SF_PT)
          {
             int b = Ai[i1], e = Ai[i1 + 1];
-            int sgn = Av[b] < 0 ? -1 : 1;
+            int neg = Av[b] < 0;          // sgn = -1 when the neighbour's diagonal is negative
             double sum = 0.0;
             for (int base = b + 1; base < e; base += 32)
             {
@@ -478,7 +513,8 @@ __global__ void k_extpi_fill(int n, const int *__restrict__ Ai, const int *__res
                bool in = k < e;
                int i2 = in ? Aj[k] : -1;
                double a2 = in ? Av[k] : 0.0;
-               bool cond = in && (gb_tab_find(T.hk, T.hp, T.cap, i2) >= 0 || i2 == i) && (sgn * a2) < 0;
+               bool sgnneg = neg ? (a2 > 0) : (a2 < 0);    // sgn * a2 < 0
+               bool cond = in && sgnneg && (i2 == i || gb_tab_find(T.hk, T.hp, T.cap, i2) >= 0);
                sum = gb_warp_ordered_sum(a2, cond, sum);
             }
             if (sum != 0)
@@ -490,9 +526,10 @@ __global__ void k_extpi_fill(int n, const int *__restrict__ Ai, const int *__res
                   bool in = k < e;
                   int i2 = in ? Aj[k] : -1;
                   double a2 = in ? Av[k] : 0.0;
-                  int pos2 = in ? gb_tab_find(T.hk, T.hp, T.cap, i2) : -1;
-                  if (pos2 >= 0 && (sgn * a2) < 0) { P[pos2] += distribute * a2; }
-                  bool dterm = in && i2 == i && (sgn * a2) < 0;
+                  bool sgnneg = neg ? (a2 > 0) : (a2 < 0);
+                  int pos2 = (in && sgnneg) ? gb_tab_find(T.hk, T.hp, T.cap, i2) : -1;
+                  if (pos2 >= 0) { P[pos2] += distribute * a2; }
+                  bool dterm = in && i2 == i && sgnneg;
                   unsigned dm = __ballot_sync(GB_FULL, dterm);
                   if (dm)
                   {
@@ -509,9 +546,9 @@ __global__ void k_extpi_fill(int n, const int *__restrict__ Ai, const int *__res
       __syncwarp();
       if (diagonal != 0.0)
       {
-         for (int t = lane; t < count; t += 32) { P[t] /= -diagonal; }
+         for (int t2 = lane; t2 < count; t2 += 32) { P[t2] /= -diagonal; }
       }
-      gb_warp_clear(T.hk, T.lslot, count);
+      gb_tab_clear(T, count);
    }
 }
 
@@ -521,22 +558,50 @@ extern "C" void gb_extpi_ub(int n, const int *Si, const int *Sj, const int *CF, 
    GB_COUNT(1);
 }
 
-extern "C" void gb_extpi_count(int n, const int *Si, const int *Sj, const int *CF, char *slabs, int cap, int nwarps,
-                               int *cnt, int *overflow, cudaStream_t s)
+static int gb_smem_blocks(int nrows)
 {
-   int threads = 128;
-   int blocks = (nwarps * 32 + threads - 1) / threads;
-   k_extpi_count<<<blocks, threads, 0, s>>>(n, Si, Sj, CF, slabs, cap, cnt, overflow);
+   int dev = 0, sms = 148;
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   long long want = (nrows + GB_SMEM_WARPS - 1) / GB_SMEM_WARPS;
+   long long maxb = (long long) sms * 4;
+   return (int) (want < maxb ? (want < 1 ? 1 : want) : maxb);
+}
+
+// tier: 0 shared-memory pass over all rows; 1 global pass over the overflow list
+extern "C" void gb_extpi_count(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF, int *cnt,
+                               int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int tier,
+                               cudaStream_t s)
+{
+   if (tier == 0)
+   {
+      k_extpi_count<false><<<gb_smem_blocks(nrows), 128, GB_SMEM_BYTES, s>>>(nrows, rows, Si, Sj, CF, cnt, ovf_list,
+                                                                            ovf_n, nullptr, 0, err);
+   }
+   else
+   {
+      k_extpi_count<true><<<(gwarps + 3) / 4, 128, 0, s>>>(nrows, rows, Si, Sj, CF, cnt, ovf_list, ovf_n, gtab, gcap,
+                                                           err);
+   }
    GB_COUNT(1);
 }
 
-extern "C" void gb_extpi_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj,
-                              const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv, char *slabs, int cap,
-                              int nwarps, int *overflow, cudaStream_t s)
+extern "C" void gb_extpi_fill(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av,
+                              const int *Si, const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj,
+                              double *Pv, const int *ovf_list, const int *ovf_n, int *gtab, int gcap, int gwarps,
+                              int *err, int tier, cudaStream_t s)
 {
-   int threads = 128;
-   int blocks = (nwarps * 32 + threads - 1) / threads;
-   k_extpi_fill<<<blocks, threads, 0, s>>>(n, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv, slabs, cap, overflow);
+   if (tier == 0)
+   {
+      k_extpi_fill<false><<<gb_smem_blocks(nrows), 128, GB_SMEM_BYTES, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c,
+                                                                           Pi, Pj, Pv, ovf_list, ovf_n, nullptr, 0,
+                                                                           err);
+   }
+   else
+   {
+      k_extpi_fill<true><<<(gwarps + 3) / 4, 128, 0, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv,
+                                                          ovf_list, ovf_n, gtab, gcap, err);
+   }
    GB_COUNT(1);
 }
 
@@ -717,148 +782,135 @@ extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, 
 }
 
 // ---------------------------------------------------------------------------
-// Galerkin product A_c = R A P with R = P^T (reference:
-// hypre_BoomerAMGBuildCoarseOperatorKT src/parcsr_ls/par_rap.c:30, numeric
-// pass :1640-1880).  Per coarse row ic: the diagonal first (value 0, then
-// accumulated), RA row built in discovery order over (R row x A rows), then
-// RAP entries in discovery order over (RA entries x P rows).
+// Ordered sparse product C = A B (reference: hypre_ParMatmul
+// src/parcsr_mv/par_csr_matop.c:348, one process): row i lists columns in
+// the order a loop over A's row and then B's rows first meets them; the first
+// contribution is stored, later ones added; a square product starts each row
+// with its diagonal (value 0, then accumulated).  The Galerkin product of
+// hypre_BoomerAMGBuildCoarseOperatorKT (src/parcsr_ls/par_rap.c:30) is the
+// same two products: RA = P^T A (rectangular), then A_c = RA P (square), so
+// it is computed with this kernel twice.
+// Tiers as for the interpolation: shared-memory tables first, overflowing rows
+// rebuilt with global tables.
 // ---------------------------------------------------------------------------
-
-// Upper bounds: apub[i] = sum_{j in A_i} |P_j| for fine rows; per coarse row
-// ubRA = sum_{i1 in R_ic} |A_i1|, ubRAP = 1 + sum_{i1 in R_ic} apub[i1].
-__global__ void k_rap_apub(int nf, const int *__restrict__ Ai, const int *__restrict__ Aj,
-                           const int *__restrict__ Pi, int *__restrict__ apub)
+template <bool GLOBAL, bool NUMERIC>
+__global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, const int *__restrict__ Ai,
+                                                const int *__restrict__ Aj, const double *__restrict__ Av,
+                                                const int *__restrict__ Bi, const int *__restrict__ Bj,
+                                                const double *__restrict__ Bv, int *__restrict__ cnt,
+                                                const int *__restrict__ Ci, int *__restrict__ Cj,
+                                                double *__restrict__ Cv, int *ovf_list, int *ovf_n, int *gtab,
+                                                int gcap, int *err)
 {
-   int i = blockIdx.x * blockDim.x + threadIdx.x;
-   if (i >= nf) { return; }
-   long long u = 0;
-   for (int k = Ai[i]; k < Ai[i + 1]; k++) { int j = Aj[k]; u += Pi[j + 1] - Pi[j]; }
-   apub[i] = (int) (u > 0x3fffffff ? 0x3fffffff : u);
-}
-
-__global__ void k_rap_ub(int nc, int nf, const int *__restrict__ Ri, const int *__restrict__ Rj,
-                         const int *__restrict__ Ai, const int *__restrict__ apub, int *__restrict__ ubra,
-                         int *__restrict__ ubrap)
-{
-   int ic = blockIdx.x * blockDim.x + threadIdx.x;
-   if (ic >= nc) { return; }
-   long long a = 0, b = 1;
-   for (int k = Ri[ic]; k < Ri[ic + 1]; k++)
-   {
-      int i1 = Rj[k];
-      a += Ai[i1 + 1] - Ai[i1];
-      b += apub[i1];
-   }
-   if (a > nf) { a = nf; }
-   if (b > nc) { b = nc; }
-   ubra[ic] = (int) a;
-   ubrap[ic] = (int) b;
-}
-
-// Builds one RAP row; numeric=false only counts.  Ta: RA table, Tc: RAP table.
-__device__ __forceinline__ int rap_row(int ic, const int *__restrict__ Ri, const int *__restrict__ Rj,
-                                       const double *__restrict__ Rv, const int *__restrict__ Ai,
-                                       const int *__restrict__ Aj, const double *__restrict__ Av,
-                                       const int *__restrict__ Pi, const int *__restrict__ Pj,
-                                       const double *__restrict__ Pv, GbSlab &Ta, GbSlab &Tc, bool numeric,
-                                       int *Cj_row, double *Cv_row, int *overflow)
-{
+   extern __shared__ int sh[];
    const int lane = gb_lane();
-   int nra = 0;
-   for (int k1 = Ri[ic]; k1 < Ri[ic + 1]; k1++)
-   {
-      int i1 = Rj[k1];
-      double r = numeric ? Rv[k1] : 0.0;
-      int b = Ai[i1], e = Ai[i1 + 1];
-      for (int base = b; base < e; base += 32)
-      {
-         int k2 = base + lane;
-         bool act = k2 < e;
-         int i2 = act ? Aj[k2] : -1;
-         bool created;
-         int pos = gb_warp_insert(Ta.hk, Ta.hp, Ta.cap, Ta.lkeys, Ta.lslot, Ta.listcap, nra, i2, act, &created,
-                                  overflow);
-         if (numeric && act && pos >= 0)
-         {
-            double ra = r * Av[k2];
-            if (created) { Ta.lvals[pos] = ra; }
-            else { Ta.lvals[pos] += ra; }
-         }
-         __syncwarp();
-      }
-   }
-   // RAP row: diagonal first
-   int nc_row = 0;
-   {
-      bool created;
-      int pos = gb_warp_insert(Tc.hk, Tc.hp, Tc.cap, Tc.lkeys, Tc.lslot, Tc.listcap, nc_row, ic, lane == 0,
-                               &created, overflow);
-      if (numeric && lane == 0 && pos >= 0) { Cj_row[pos] = ic; Cv_row[pos] = 0.0; }
-      __syncwarp();
-   }
-   for (int t = 0; t < nra; t++)
-   {
-      int i1 = Ta.lkeys[t];
-      double ra = numeric ? Ta.lvals[t] : 0.0;
-      int b = Pi[i1], e = Pi[i1 + 1];
-      for (int base = b; base < e; base += 32)
-      {
-         int k3 = base + lane;
-         bool act = k3 < e;
-         int i3 = act ? Pj[k3] : -1;
-         bool created;
-         int pos = gb_warp_insert(Tc.hk, Tc.hp, Tc.cap, Tc.lkeys, Tc.lslot, Tc.listcap, nc_row, i3, act, &created,
-                                  overflow);
-         if (numeric && act && pos >= 0)
-         {
-            double v = ra * Pv[k3];
-            if (created) { Cj_row[pos] = i3; Cv_row[pos] = v; }
-            else { Cv_row[pos] += v; }
-         }
-         __syncwarp();
-      }
-   }
-   gb_warp_clear(Ta.hk, Ta.lslot, nra);
-   gb_warp_clear(Tc.hk, Tc.lslot, nc_row);
-   return nc_row;
-}
-
-__global__ void k_rap(int nc, const int *__restrict__ Ri, const int *__restrict__ Rj, const double *__restrict__ Rv,
-                      const int *__restrict__ Ai, const int *__restrict__ Aj, const double *__restrict__ Av,
-                      const int *__restrict__ Pi, const int *__restrict__ Pj, const double *__restrict__ Pv,
-                      char *slab_a, int cap_a, char *slab_c, int cap_c, int numeric, const int *__restrict__ Ci,
-                      int *__restrict__ Cj, double *__restrict__ Cv, int *__restrict__ cnt, int *overflow)
-{
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;
-   GbSlab Ta = gb_slab(slab_a, cap_a, warp);
-   GbSlab Tc = gb_slab(slab_c, cap_c, warp);
-   for (int ic = warp; ic < nc; ic += nwarps)
+   GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
+                    : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
+   if (!GLOBAL) { gb_tab_init(T); }
+   int total = GLOBAL ? *ovf_n : nrows;
+   for (int t = warp; t < total; t += nwarps)
    {
-      int off = numeric ? Ci[ic] : 0;
-      int c = rap_row(ic, Ri, Rj, Rv, Ai, Aj, Av, Pi, Pj, Pv, Ta, Tc, numeric != 0, numeric ? Cj + off : nullptr,
-                      numeric ? Cv + off : nullptr, overflow);
-      if (!numeric && gb_lane() == 0) { cnt[ic] = c; }
+      int r = GLOBAL ? ovf_list[t] : t;
+      int off = 0;
+      if (NUMERIC)
+      {
+         off = Ci[r];
+         if (!GLOBAL && Ci[r + 1] - off > T.listcap) { continue; }
+      }
+      int count = 0, ovf = 0;
+      bool created;
+      if (square)
+      {
+         int pos = gb_winsert(T, count, r, lane == 0, created, ovf);
+         if (NUMERIC && lane == 0 && pos >= 0) { Cj[off + pos] = r; Cv[off + pos] = 0.0; }
+         __syncwarp();
+      }
+      for (int ka = Ai[r]; ka < Ai[r + 1] && !ovf; ka++)
+      {
+         int k = Aj[ka];
+         double a = NUMERIC ? Av[ka] : 0.0;
+         int b = Bi[k], e = Bi[k + 1];
+         for (int base = b; base < e && !ovf; base += 32)
+         {
+            int kb = base + lane;
+            bool act = kb < e;
+            int col = act ? Bj[kb] : -1;
+            int pos = gb_winsert(T, count, col, act, created, ovf);
+            if (NUMERIC && act && pos >= 0)
+            {
+               double v = a * Bv[kb];
+               if (created) { Cj[off + pos] = col; Cv[off + pos] = v; }
+               else { Cv[off + pos] += v; }
+            }
+            __syncwarp();
+         }
+      }
+      if (lane == 0)
+      {
+         if (!ovf) { if (!NUMERIC) { cnt[r] = count; } }
+         else if (!GLOBAL && !NUMERIC) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         else { atomicExch(err, 1); }
+      }
+      gb_tab_clear(T, count);
    }
 }
 
-extern "C" void gb_rap_bounds(int nf, int nc, const int *Ri, const int *Rj, const int *Ai, const int *Aj,
-                              const int *Pi, int *apub, int *ubra, int *ubrap, cudaStream_t s)
+// Upper bound of each product row's length: sum over A's row of B row lengths
+// (+1 when square), capped by B's column count.
+__global__ void k_spgemm_ub(int nrows, int ncols, int square, const int *__restrict__ Ai,
+                            const int *__restrict__ Aj, const int *__restrict__ Bi, int *__restrict__ ub)
 {
-   k_rap_apub<<<gb_blocks(nf, 256), 256, 0, s>>>(nf, Ai, Aj, Pi, apub);
-   k_rap_ub<<<gb_blocks(nc, 256), 256, 0, s>>>(nc, nf, Ri, Rj, Ai, apub, ubra, ubrap);
-   GB_COUNT(2);
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nrows) { return; }
+   long long u = square ? 1 : 0;
+   for (int ka = Ai[r]; ka < Ai[r + 1]; ka++) { int k = Aj[ka]; u += Bi[k + 1] - Bi[k]; }
+   if (u > ncols) { u = ncols; }
+   ub[r] = (int) u;
 }
 
-extern "C" void gb_rap(int nc, const int *Ri, const int *Rj, const double *Rv, const int *Ai, const int *Aj,
-                       const double *Av, const int *Pi, const int *Pj, const double *Pv, char *slab_a, int cap_a,
-                       char *slab_c, int cap_c, int nwarps, int numeric, const int *Ci, int *Cj, double *Cv,
-                       int *cnt, int *overflow, cudaStream_t s)
+extern "C" void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int *ub,
+                             cudaStream_t s)
 {
-   int threads = 128;
-   int blocks = (nwarps * 32 + threads - 1) / threads;
-   k_rap<<<blocks, threads, 0, s>>>(nc, Ri, Rj, Rv, Ai, Aj, Av, Pi, Pj, Pv, slab_a, cap_a, slab_c, cap_c, numeric,
-                                    Ci, Cj, Cv, cnt, overflow);
+   k_spgemm_ub<<<gb_blocks(nrows, 256), 256, 0, s>>>(nrows, ncols, square, Ai, Aj, Bi, ub);
+   GB_COUNT(1);
+}
+
+// phase: 0 symbolic, 1 numeric; tier: 0 shared memory (all rows), 1 global (overflow list)
+extern "C" void gb_spgemm(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi,
+                          const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv,
+                          int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int phase, int tier,
+                          cudaStream_t s)
+{
+   if (tier == 0)
+   {
+      int blocks = gb_smem_blocks(nrows);
+      if (phase == 0)
+      {
+         k_spgemm<false, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
+                                                                   Cj, Cv, ovf_list, ovf_n, nullptr, 0, err);
+      }
+      else
+      {
+         k_spgemm<false, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
+                                                                  Cj, Cv, ovf_list, ovf_n, nullptr, 0, err);
+      }
+   }
+   else
+   {
+      int blocks = (gwarps + 3) / 4;
+      if (phase == 0)
+      {
+         k_spgemm<true, false><<<blocks, 128, 0, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
+                                                      ovf_list, ovf_n, gtab, gcap, err);
+      }
+      else
+      {
+         k_spgemm<true, true><<<blocks, 128, 0, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
+                                                     ovf_list, ovf_n, gtab, gcap, err);
+      }
+   }
    GB_COUNT(1);
 }
 

@@ -15,7 +15,8 @@ RTOL_HIST = 1e-10
 def _setup_both(gb, O, I, J, V, **prm):
     oprm = dict(max_row_sum=prm.get("MaxRowSum", 0.9), max_coarse_size=prm.get("MaxCoarseSize", 9),
                 strong_threshold=prm.get("StrongThreshold", 0.25), p_max_elmts=prm.get("PMaxElmts", 4),
-                trunc_factor=prm.get("TruncFactor", 0.0))
+                trunc_factor=prm.get("TruncFactor", 0.0), agg_num_levels=prm.get("AggNumLevels", 0),
+                agg_interp_type=prm.get("AggInterpType", 4))
     if "RelaxType" in prm:
         oprm.update(relax_down=prm["RelaxType"], relax_up=prm["RelaxType"])
     H = O.Hierarchy(I, J, V, O.default_params(**oprm))
@@ -56,6 +57,40 @@ def test_hierarchy_bitexact(gb, oracle_mod, kind, nx, th, mcs):
     I, J, V = O.stencil(kind, nx, nx, nx)
     H, A, amg, bv, xv = _setup_both(gb, O, I, J, V, MaxRowSum=1.0, StrongThreshold=th, MaxCoarseSize=mcs)
     _compare_hierarchy(H, amg)
+
+
+@pytest.mark.parametrize("kind,nx,th,agg", [(27, 20, 0.5, 1), (7, 24, 0.25, 1), (7, 30, 0.25, 2), (27, 12, 0.5, 1)])
+def test_hierarchy_aggressive_bitexact(gb, oracle_mod, kind, nx, th, agg):
+    """Aggressive coarsening (second-order strength, PMIS on it, modified and
+    partial extended+i, P1 P2) on the first levels."""
+    O = oracle_mod
+    I, J, V = O.stencil(kind, nx, nx, nx)
+    H, A, amg, bv, xv = _setup_both(gb, O, I, J, V, MaxRowSum=1.0, StrongThreshold=th, AggNumLevels=agg,
+                                    AggInterpType=6)
+    _compare_hierarchy(H, amg)
+
+
+def test_aggressive_fgmres_two_stage_gs(gb, oracle_mod):
+    """Miniature of the 160^3 configuration: aggressive first level, PMIS 0.5,
+    two-stage Gauss-Seidel, FlexGMRES(30)."""
+    O = oracle_mod
+    I, J, V = O.stencil(27, 24, 24, 24)
+    n = len(I) - 1
+    b = O.rhs_normalised(n)
+    prm = O.default_params(max_row_sum=1.0, strong_threshold=0.5, agg_num_levels=1, agg_interp_type=6,
+                           relax_down=11, relax_up=11)
+    H = O.Hierarchy(I, J, V, prm)
+    _, res_o, it_o = H.fgmres(b, tol=1e-8, maxit=100, kdim=30)
+    A = gb.IJMatrix(I, J, V)
+    bv, xv = gb.IJVector(n, b), gb.IJVector(n, np.zeros(n))
+    amg = gb.BoomerAMG(MaxRowSum=1.0, StrongThreshold=0.5, AggNumLevels=1, AggInterpType=6, RelaxType=11,
+                       Tol=0.0, MaxIter=1)
+    k = gb.Krylov("fgmres", tol=1e-8, maxit=100, kdim=30, amg=amg)
+    k.setup(A, bv, xv)
+    k.solve(A, bv, xv)
+    assert abs(k.iterations() - it_o) <= 1
+    m = min(len(res_o), len(k.history()))
+    np.testing.assert_allclose(k.history()[:m], res_o[:m] / np.linalg.norm(b), rtol=1e-9, atol=0)
 
 
 def test_hierarchy_fv_diffusion(gb, oracle_mod):
