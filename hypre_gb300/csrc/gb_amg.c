@@ -221,8 +221,13 @@ static int spgemm_host(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
    int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    gb_tier t;
    tier_begin(&t, n);
-   gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, 0, 0,
-             t.err, 0, 0, s);
+   /* lane-group width from B's longest row */
+   gb_rowlen_max(B->nr, B->i, t.err + 1, s);
+   int maxb = read_int(t.err + 1);
+   int W = 0;
+   if (maxb <= 32) { W = 1; while (W < maxb) { W <<= 1; } }
+   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, 0,
+             0, t.err, 0, 0, s);
    int *ub = NULL;
    if (read_int(t.ovf_n) > 0)
    {
@@ -232,20 +237,20 @@ static int spgemm_host(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
    tier_global(&t, ub, n);
    if (t.h_ovf > 0)
    {
-      gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, t.gtab,
-                t.gcap, t.gwarps, t.err, 0, 1, s);
+      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n,
+                t.gtab, t.gcap, t.gwarps, t.err, 0, 1, s);
    }
    C->nr = n; C->nc = B->nc;
    C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    C->nnz = scan_total(cnt, C->i, n);
    C->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C->nnz ? C->nnz : 1));
    C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
-   gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL, 0, 0,
-             t.err, 1, 0, s);
+   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL, 0,
+             0, t.err, 1, 0, s);
    if (t.h_ovf > 0)
    {
-      gb_spgemm(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, t.gtab,
-                t.gcap, t.gwarps, t.err, 1, 1, s);
+      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
+                t.gtab, t.gcap, t.gwarps, t.err, 1, 1, s);
    }
    int e = tier_end(&t);
    gb_dfree(ub); gb_dfree(cnt);
@@ -253,41 +258,55 @@ static int spgemm_host(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
    return 0;
 }
 
-/* extended+i rows for fine points rows[r] (all points when rows == NULL) */
+/* extended+i rows for fine points rows[r] (all points when rows == NULL).
+ * Tier 0: one thread per row (rows with <= 64 candidates); tier 1: one warp
+ * per row with shared-memory tables; tier 2: global-memory tables. */
 static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int *f2c, int nrows, const int *rows,
                       int ncols, gb_csr *P)
 {
    cudaStream_t s = gb_stream();
    int n = A->nr;
    int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
+   int *l1 = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows > 0 ? nrows : 1));
+   int *n1 = (int *) gb_dcalloc(sizeof(int) * 2);
    gb_tier t;
    tier_begin(&t, nrows);
-   gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 0, s);
+   gb_extpi_count_t(nrows, rows, S->i, S->j, CF, f2c, cnt, l1, n1, s);
+   int h1 = read_int(n1);
    int *ub = NULL;
-   if (read_int(t.ovf_n) > 0)
+   if (h1 > 0)
    {
-      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
-      gb_extpi_ub(n, S->i, S->j, CF, ub, s);
-   }
-   tier_global(&t, ub, n);
-   if (t.h_ovf > 0)
-   {
-      gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps, t.err, 1, s);
+      gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, l1, n1, h1, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 1, s);
+      if (read_int(t.ovf_n) > 0)
+      {
+         ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+         gb_extpi_ub(n, S->i, S->j, CF, ub, s);
+      }
+      tier_global(&t, ub, n);
+      if (t.h_ovf > 0)
+      {
+         gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, t.ovf_list, t.ovf_n, t.h_ovf, NULL, NULL, t.gtab, t.gcap,
+                        t.gwarps, t.err, 2, s);
+      }
    }
    P->nr = nrows; P->nc = ncols;
    P->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
    P->nnz = scan_total(cnt, P->i, nrows);
    P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
    P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
-   gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, t.ovf_list, t.ovf_n, NULL, 0,
-                 0, t.err, 0, s);
-   if (t.h_ovf > 0)
+   gb_extpi_fill_t(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, s);
+   if (h1 > 0)
    {
-      gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, t.ovf_list, t.ovf_n,
-                    t.gtab, t.gcap, t.gwarps, t.err, 1, s);
+      gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, l1, n1, h1, NULL, 0, 0,
+                    t.err, 1, s);
+      if (t.h_ovf > 0)
+      {
+         gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, t.ovf_list, t.ovf_n,
+                       t.h_ovf, t.gtab, t.gcap, t.gwarps, t.err, 2, s);
+      }
    }
    int e = tier_end(&t);
-   gb_dfree(ub); gb_dfree(cnt);
+   gb_dfree(ub); gb_dfree(cnt); gb_dfree(l1); gb_dfree(n1);
    if (e) { gb_error(HYPRE_ERROR_GENERIC, "interpolation table overflow"); return -1; }
    return 0;
 }

@@ -53,11 +53,17 @@ void gb_cpoint_flags(int n, const int *CF, int *flag, cudaStream_t s);
 void gb_sf_to_f(int n, int *CF, cudaStream_t s);
 void gb_extpi_ub(int n, const int *Si, const int *Sj, const int *CF, int *ub, cudaStream_t s);
 void gb_extpi_count(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF, int *cnt,
-                    int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int tier, cudaStream_t s);
+                    const int *in_list, const int *in_n, int n_hint, int *out_list, int *out_n, int *gtab, int gcap,
+                    int gwarps, int *err, int tier, cudaStream_t s);
 void gb_extpi_fill(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av, const int *Si,
                    const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv,
-                   const int *ovf_list, const int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int tier,
-                   cudaStream_t s);
+                   const int *in_list, const int *in_n, int n_hint, int *gtab, int gcap, int gwarps, int *err,
+                   int tier, cudaStream_t s);
+void gb_extpi_count_t(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF, const int *f2c,
+                      int *cnt, int *ovf_list, int *ovf_n, cudaStream_t s);
+void gb_extpi_fill_t(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av, const int *Si,
+                     const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv,
+                     cudaStream_t s);
 void gb_truncate_rows(int n, const int *Pi, int *Pj, double *Pv, double tol, int max_elmts, int *newcnt,
                       cudaStream_t s);
 void gb_compact_rows(int n, const int *Pi, const int *Pj, const double *Pv, const int *Ni, int *Nj, double *Nv,
@@ -67,9 +73,10 @@ void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, const doubl
                        int *Tj, double *Tv, cudaStream_t s);
 void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int *ub,
                   cudaStream_t s);
-void gb_spgemm(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi, const int *Bj,
-               const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list, int *ovf_n, int *gtab,
-               int gcap, int gwarps, int *err, int phase, int tier, cudaStream_t s);
+void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av, const int *Bi,
+               const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list,
+               int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int phase, int tier, cudaStream_t s);
+void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 /* aggressive coarsening (gb_agg.cu) */
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);
 void gb_scatter_list(int n, const int *flag, const int *scan, int *list, cudaStream_t s);

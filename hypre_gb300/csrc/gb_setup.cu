@@ -422,7 +422,8 @@ template <bool GLOBAL>
 __global__ void __launch_bounds__(128) k_extpi_count(int nrows, const int *__restrict__ rows,
                                                      const int *__restrict__ Si, const int *__restrict__ Sj,
                                                      const int *__restrict__ CF, int *__restrict__ cnt,
-                                                     int *ovf_list, int *ovf_n, int *gtab, int gcap, int *err)
+                                                     const int *in_list, const int *in_n, int *ovf_list, int *ovf_n,
+                                                     int *gtab, int gcap, int *err)
 {
    extern __shared__ int sh[];
    const int lane = gb_lane();
@@ -431,10 +432,10 @@ __global__ void __launch_bounds__(128) k_extpi_count(int nrows, const int *__res
    GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
                     : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
    if (!GLOBAL) { gb_tab_init(T); }
-   int total = GLOBAL ? *ovf_n : nrows;
+   int total = *in_n;
    for (int t = warp; t < total; t += nwarps)
    {
-      int r = GLOBAL ? ovf_list[t] : t;
+      int r = in_list[t];
       int i = rows ? rows[r] : r;
       int cf = CF[i];
       if (cf >= 0) { if (lane == 0) { cnt[r] = 1; } continue; }
@@ -458,7 +459,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill(int nrows, const int *__rest
                                                     const int *__restrict__ Sj, const int *__restrict__ CF,
                                                     const int *__restrict__ f2c, const int *__restrict__ Pi,
                                                     int *__restrict__ Pj, double *__restrict__ Pv,
-                                                    const int *ovf_list, const int *ovf_n, int *gtab, int gcap,
+                                                    const int *in_list, const int *in_n, int *gtab, int gcap,
                                                     int *err)
 {
    extern __shared__ int sh[];
@@ -468,10 +469,10 @@ __global__ void __launch_bounds__(128) k_extpi_fill(int nrows, const int *__rest
    GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
                     : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
    if (!GLOBAL) { gb_tab_init(T); }
-   int total = GLOBAL ? *ovf_n : nrows;
+   int total = *in_n;
    for (int t = warp; t < total; t += nwarps)
    {
-      int r = GLOBAL ? ovf_list[t] : t;
+      int r = in_list[t];
       int i = rows ? rows[r] : r;
       int cf = CF[i];
       int begin = Pi[r];
@@ -568,40 +569,201 @@ static int gb_smem_blocks(int nrows)
    return (int) (want < maxb ? (want < 1 ? 1 : want) : maxb);
 }
 
-// tier: 0 shared-memory pass over all rows; 1 global pass over the overflow list
+// tier 1: shared-memory tables, rows in_list -> overflow to out_list;
+// tier 2: global tables, rows in_list.  (Tier 0 is the thread-per-row kernel.)
 extern "C" void gb_extpi_count(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF, int *cnt,
-                               int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int tier,
-                               cudaStream_t s)
+                               const int *in_list, const int *in_n, int n_hint, int *out_list, int *out_n, int *gtab,
+                               int gcap, int gwarps, int *err, int tier, cudaStream_t s)
 {
-   if (tier == 0)
+   if (tier == 1)
    {
-      k_extpi_count<false><<<gb_smem_blocks(nrows), 128, GB_SMEM_BYTES, s>>>(nrows, rows, Si, Sj, CF, cnt, ovf_list,
-                                                                            ovf_n, nullptr, 0, err);
+      k_extpi_count<false><<<gb_smem_blocks(n_hint), 128, GB_SMEM_BYTES, s>>>(nrows, rows, Si, Sj, CF, cnt, in_list,
+                                                                             in_n, out_list, out_n, nullptr, 0, err);
    }
    else
    {
-      k_extpi_count<true><<<(gwarps + 3) / 4, 128, 0, s>>>(nrows, rows, Si, Sj, CF, cnt, ovf_list, ovf_n, gtab, gcap,
-                                                           err);
+      k_extpi_count<true><<<(gwarps + 3) / 4, 128, 0, s>>>(nrows, rows, Si, Sj, CF, cnt, in_list, in_n, out_list,
+                                                           out_n, gtab, gcap, err);
    }
    GB_COUNT(1);
 }
 
 extern "C" void gb_extpi_fill(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av,
                               const int *Si, const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj,
-                              double *Pv, const int *ovf_list, const int *ovf_n, int *gtab, int gcap, int gwarps,
-                              int *err, int tier, cudaStream_t s)
+                              double *Pv, const int *in_list, const int *in_n, int n_hint, int *gtab, int gcap,
+                              int gwarps, int *err, int tier, cudaStream_t s)
 {
-   if (tier == 0)
+   if (tier == 1)
    {
-      k_extpi_fill<false><<<gb_smem_blocks(nrows), 128, GB_SMEM_BYTES, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c,
-                                                                           Pi, Pj, Pv, ovf_list, ovf_n, nullptr, 0,
-                                                                           err);
+      k_extpi_fill<false><<<gb_smem_blocks(n_hint), 128, GB_SMEM_BYTES, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c,
+                                                                            Pi, Pj, Pv, in_list, in_n, nullptr, 0,
+                                                                            err);
    }
    else
    {
       k_extpi_fill<true><<<(gwarps + 3) / 4, 128, 0, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv,
-                                                          ovf_list, ovf_n, gtab, gcap, err);
+                                                          in_list, in_n, gtab, gcap, err);
    }
+   GB_COUNT(1);
+}
+
+
+// ---------------------------------------------------------------------------
+// Thread-per-row extended+i (rows with at most GB_TPR_MAX candidates): each
+// thread runs the reference's sequential loops for its row, so the FP64
+// additions of 32 rows proceed in parallel on a warp instead of one serial
+// chain per warp.  Membership of a fine point in the row's column set is a
+// search of the row's coarse columns (only C points can be members).
+// Rows with more candidates are listed for the warp-per-row kernels.
+// ---------------------------------------------------------------------------
+#define GB_TPR_MAX 64
+
+// sign tests on the bit pattern (integer ops; x < 0 and x > 0 as IEEE compares,
+// false for zeros and NaN)
+__device__ __forceinline__ bool gb_lt0(double x)
+{
+   long long b = __double_as_longlong(x);
+   return b < 0 && (b & 0x7fffffffffffffffLL) != 0 && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool gb_gt0(double x)
+{
+   long long b = __double_as_longlong(x);
+   return b > 0 && b <= 0x7ff0000000000000LL;
+}
+
+__device__ __forceinline__ int tpr_find(const int *cols, int len, int c)
+{
+   for (int k = 0; k < len; k++) { if (cols[k] == c) { return k; } }
+   return -1;
+}
+
+// counts (or fills, when Pj != NULL) the candidate columns of row i in
+// discovery order into cols[] (coarse indices); returns -1 beyond GB_TPR_MAX
+__device__ int tpr_discover(int i, const int *__restrict__ Si, const int *__restrict__ Sj, const int *__restrict__ CF,
+                            const int *__restrict__ f2c, int *cols)
+{
+   int len = 0;
+   for (int k = Si[i]; k < Si[i + 1]; k++)
+   {
+      int i1 = Sj[k];
+      int cf1 = CF[i1];
+      if (cf1 >= 0)
+      {
+         int c = f2c[i1];
+         if (tpr_find(cols, len, c) < 0) { if (len == GB_TPR_MAX) { return -1; } cols[len++] = c; }
+      }
+      else if (cf1 != SF_PT)
+      {
+         for (int kk = Si[i1]; kk < Si[i1 + 1]; kk++)
+         {
+            int k1 = Sj[kk];
+            if (CF[k1] >= 0)
+            {
+               int c = f2c[k1];
+               if (tpr_find(cols, len, c) < 0) { if (len == GB_TPR_MAX) { return -1; } cols[len++] = c; }
+            }
+         }
+      }
+   }
+   return len;
+}
+
+__global__ void __launch_bounds__(128) k_extpi_count_t(int nrows, const int *__restrict__ rows,
+                                                       const int *__restrict__ Si, const int *__restrict__ Sj,
+                                                       const int *__restrict__ CF, const int *__restrict__ f2c,
+                                                       int *__restrict__ cnt, int *ovf_list, int *ovf_n)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nrows) { return; }
+   int i = rows ? rows[r] : r;
+   int cf = CF[i];
+   if (cf >= 0) { cnt[r] = 1; return; }
+   if (cf == SF_PT) { cnt[r] = 0; return; }
+   int cols[GB_TPR_MAX];
+   int len = tpr_discover(i, Si, Sj, CF, f2c, cols);
+   if (len < 0) { cnt[r] = 0; ovf_list[atomicAdd(ovf_n, 1)] = r; }
+   else { cnt[r] = len; }
+}
+
+__global__ void __launch_bounds__(128) k_extpi_fill_t(int nrows, const int *__restrict__ rows,
+                                                      const int *__restrict__ Ai, const int *__restrict__ Aj,
+                                                      const double *__restrict__ Av, const int *__restrict__ Si,
+                                                      const int *__restrict__ Sj, const int *__restrict__ CF,
+                                                      const int *__restrict__ f2c, const int *__restrict__ Pi,
+                                                      int *__restrict__ Pj, double *__restrict__ Pv)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nrows) { return; }
+   int i = rows ? rows[r] : r;
+   int cf = CF[i];
+   int begin = Pi[r];
+   int len = Pi[r + 1] - begin;
+   if (cf >= 0) { Pj[begin] = f2c[i]; Pv[begin] = 1.0; return; }
+   if (cf == SF_PT || len > GB_TPR_MAX) { return; }
+   int cols[GB_TPR_MAX];
+   int l2 = tpr_discover(i, Si, Sj, CF, f2c, cols);
+   (void) l2;
+   double *P = Pv + begin;
+   for (int k = 0; k < len; k++) { Pj[begin + k] = cols[k]; P[k] = 0.0; }
+   double diagonal = Av[Ai[i]];
+   int sp = Si[i], se = Si[i + 1];
+   for (int jj = Ai[i] + 1; jj < Ai[i + 1]; jj++)
+   {
+      int i1 = Aj[jj];
+      double a = Av[jj];
+      bool strong = (sp < se && Sj[sp] == i1);
+      if (strong) { sp++; }
+      int cf1 = CF[i1];
+      int pos1 = cf1 >= 0 ? tpr_find(cols, len, f2c[i1]) : -1;
+      if (pos1 >= 0) { P[pos1] += a; }
+      else if (strong && cf1 < 0 && cf1 != SF_PT)
+      {
+         int b = Ai[i1], e = Ai[i1 + 1];
+         bool neg = gb_lt0(Av[b]);
+         double sum = 0.0;
+         for (int k = b + 1; k < e; k++)
+         {
+            int i2 = Aj[k];
+            double a2 = Av[k];
+            bool sg = neg ? gb_gt0(a2) : gb_lt0(a2);
+            if (sg && (i2 == i || (CF[i2] >= 0 && tpr_find(cols, len, f2c[i2]) >= 0))) { sum += a2; }
+         }
+         if (sum != 0)
+         {
+            double distribute = a / sum;
+            for (int k = b + 1; k < e; k++)
+            {
+               int i2 = Aj[k];
+               double a2 = Av[k];
+               bool sg = neg ? gb_gt0(a2) : gb_lt0(a2);
+               if (!sg) { continue; }
+               int p2 = CF[i2] >= 0 ? tpr_find(cols, len, f2c[i2]) : -1;
+               if (p2 >= 0) { P[p2] += distribute * a2; }
+               if (i2 == i) { diagonal += distribute * a2; }
+            }
+         }
+         else { diagonal += a; }
+      }
+      else if (cf1 != SF_PT) { diagonal += a; }
+   }
+   if (diagonal != 0.0)
+   {
+      for (int k = 0; k < len; k++) { P[k] /= -diagonal; }
+   }
+}
+
+extern "C" void gb_extpi_count_t(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF,
+                                 const int *f2c, int *cnt, int *ovf_list, int *ovf_n, cudaStream_t s)
+{
+   k_extpi_count_t<<<gb_blocks(nrows, 128), 128, 0, s>>>(nrows, rows, Si, Sj, CF, f2c, cnt, ovf_list, ovf_n);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_extpi_fill_t(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av,
+                                const int *Si, const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj,
+                                double *Pv, cudaStream_t s)
+{
+   k_extpi_fill_t<<<gb_blocks(nrows, 128), 128, 0, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv);
    GB_COUNT(1);
 }
 
@@ -790,11 +952,18 @@ extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, 
 // hypre_BoomerAMGBuildCoarseOperatorKT (src/parcsr_ls/par_rap.c:30) is the
 // same two products: RA = P^T A (rectangular), then A_c = RA P (square), so
 // it is computed with this kernel twice.
-// Tiers as for the interpolation: shared-memory tables first, overflowing rows
-// rebuilt with global tables.
+//
+// One warp per row.  When B's rows are short (at most W <= 32 entries, W a
+// power of two) each warp step covers 32/W consecutive entries of A's row,
+// lane groups of W lanes each reading one B row; keys repeated within a step
+// are merged in lane order (the sequential order), the group leader adding
+// the other members' products one by one.  Longer B rows are walked one A
+// entry at a time in chunks of 32.
+// Tiers: shared-memory tables first, overflowing rows rebuilt with global
+// tables.
 // ---------------------------------------------------------------------------
 template <bool GLOBAL, bool NUMERIC>
-__global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, const int *__restrict__ Ai,
+__global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, const int *__restrict__ Ai,
                                                 const int *__restrict__ Aj, const double *__restrict__ Av,
                                                 const int *__restrict__ Bi, const int *__restrict__ Bj,
                                                 const double *__restrict__ Bv, int *__restrict__ cnt,
@@ -803,13 +972,16 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, const int
                                                 int gcap, int *err)
 {
    extern __shared__ int sh[];
+   __shared__ double stage_all[128];
    const int lane = gb_lane();
+   double *stage = stage_all + (threadIdx.x & ~31);
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;
    GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
                     : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
    if (!GLOBAL) { gb_tab_init(T); }
    int total = GLOBAL ? *ovf_n : nrows;
+   const int per = W > 0 ? 32 / W : 1;
    for (int t = warp; t < total; t += nwarps)
    {
       int r = GLOBAL ? ovf_list[t] : t;
@@ -827,15 +999,65 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, const int
          if (NUMERIC && lane == 0 && pos >= 0) { Cj[off + pos] = r; Cv[off + pos] = 0.0; }
          __syncwarp();
       }
-      for (int ka = Ai[r]; ka < Ai[r + 1] && !ovf; ka++)
+      const int ka0 = Ai[r], ka1 = Ai[r + 1];
+      for (int base = ka0; base < ka1 && !ovf; base += per)
       {
-         int k = Aj[ka];
-         double a = NUMERIC ? Av[ka] : 0.0;
-         int b = Bi[k], e = Bi[k + 1];
-         for (int base = b; base < e && !ovf; base += 32)
+         int kstart = 0, kend = 0;
+         int e = base + (W > 0 ? lane / W : 0);
+         double a = 0.0;
+         if (W > 0)
          {
-            int kb = base + lane;
-            bool act = kb < e;
+            // batched: lane group of W lanes per A entry
+            bool act = false;
+            int col = -1;
+            double v = 0.0;
+            if (e < ka1)
+            {
+               int k = Aj[e];
+               int kb = Bi[k] + (lane % W);
+               if (kb < Bi[k + 1])
+               {
+                  act = true;
+                  col = Bj[kb];
+                  if (NUMERIC) { v = Av[e] * Bv[kb]; }
+               }
+            }
+            int pos = gb_winsert(T, count, col, act, created, ovf);
+            if (NUMERIC)
+            {
+               stage[lane] = v;
+               __syncwarp();
+               unsigned grp = __match_any_sync(GB_FULL, (act && pos >= 0) ? pos : -(lane + 2));
+               int leader = __ffs(grp) - 1;
+               if (act && pos >= 0 && lane == leader)
+               {
+                  double x;
+                  if (created) { Cj[off + pos] = col; x = v; }
+                  else { x = Cv[off + pos] + v; }
+                  unsigned rest = grp & (grp - 1u);
+                  while (rest)
+                  {
+                     int m = __ffs(rest) - 1;
+                     rest &= rest - 1u;
+                     x += stage[m];
+                  }
+                  Cv[off + pos] = x;
+               }
+               __syncwarp();
+            }
+            continue;
+         }
+         // long B rows: one A entry, chunks of 32
+         {
+            int k = Aj[base];
+            if (NUMERIC) { a = Av[base]; }
+            kstart = Bi[k];
+            kend = Bi[k + 1];
+         }
+         for (int cb = kstart; cb < kend && !ovf; cb += 32)
+         {
+            int kb = cb + lane;
+            bool act = kb < kend;
             int col = act ? Bj[kb] : -1;
             int pos = gb_winsert(T, count, col, act, created, ovf);
             if (NUMERIC && act && pos >= 0)
@@ -870,6 +1092,20 @@ __global__ void k_spgemm_ub(int nrows, int ncols, int square, const int *__restr
    ub[r] = (int) u;
 }
 
+__global__ void k_rowlen_max(int n, const int *__restrict__ Bi, int *__restrict__ out)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   int l = r < n ? Bi[r + 1] - Bi[r] : 0;
+   for (int o = 16; o > 0; o >>= 1) { int y = __shfl_down_sync(GB_FULL, l, o); l = y > l ? y : l; }
+   if ((threadIdx.x & 31) == 0) { atomicMax(out, l); }
+}
+
+extern "C" void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s)
+{
+   cudaMemsetAsync(out, 0, sizeof(int), s);
+   if (n > 0) { k_rowlen_max<<<gb_blocks(n, 256), 256, 0, s>>>(n, Bi, out); GB_COUNT(1); }
+}
+
 extern "C" void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int *ub,
                              cudaStream_t s)
 {
@@ -877,23 +1113,33 @@ extern "C" void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, co
    GB_COUNT(1);
 }
 
-// phase: 0 symbolic, 1 numeric; tier: 0 shared memory (all rows), 1 global (overflow list)
-extern "C" void gb_spgemm(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi,
-                          const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv,
-                          int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int phase, int tier,
-                          cudaStream_t s)
+// phase: 0 symbolic, 1 numeric; tier: 0 shared memory (all rows), 1 global (overflow list).
+// W: lane-group width for B rows of at most W entries (power of two <= 32), 0 for long rows.
+extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av,
+                          const int *Bi, const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj,
+                          double *Cv, int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int phase,
+                          int tier, cudaStream_t s)
 {
+   static int attr_done = 0;
+   if (!attr_done)
+   {
+      /* 48 KB of tables plus the static staging array exceed the default
+       * dynamic shared-memory limit: opt in once */
+      cudaFuncSetAttribute(k_spgemm<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
+      cudaFuncSetAttribute(k_spgemm<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
+      attr_done = 1;
+   }
    if (tier == 0)
    {
       int blocks = gb_smem_blocks(nrows);
       if (phase == 0)
       {
-         k_spgemm<false, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
+         k_spgemm<false, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
                                                                    Cj, Cv, ovf_list, ovf_n, nullptr, 0, err);
       }
       else
       {
-         k_spgemm<false, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
+         k_spgemm<false, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
                                                                   Cj, Cv, ovf_list, ovf_n, nullptr, 0, err);
       }
    }
@@ -902,12 +1148,12 @@ extern "C" void gb_spgemm(int nrows, int square, const int *Ai, const int *Aj, c
       int blocks = (gwarps + 3) / 4;
       if (phase == 0)
       {
-         k_spgemm<true, false><<<blocks, 128, 0, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
+         k_spgemm<true, false><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
                                                       ovf_list, ovf_n, gtab, gcap, err);
       }
       else
       {
-         k_spgemm<true, true><<<blocks, 128, 0, s>>>(nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
+         k_spgemm<true, true><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
                                                      ovf_list, ovf_n, gtab, gcap, err);
       }
    }

@@ -40,3 +40,10 @@ def test_library_has_no_torch_or_oracle_dependency():
 def test_build_targets_sm_103a_only():
     from hypre_gb300 import build
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+@pytest.mark.skipif(not _lib_built(), reason="library not built")
+def test_no_unresolved_internal_symbols():
+    out = subprocess.run(["nm", "-D", "--undefined-only", gb.LIB_PATH], capture_output=True, text=True).stdout
+    bad = [l for l in out.splitlines() if " gb_" in l or " HYPRE_" in l]
+    assert not bad, bad
