@@ -239,13 +239,17 @@ __global__ void k_fffc_fill(int nf, const int *__restrict__ fl, const int *__res
    int a0 = Ai[i], a1 = Ai[i + 1];
    int hasdiag = (a0 < a1 && Aj[a0] == i);
    if (hasdiag) { FFj[pf] = f2f[i]; FFv[pf++] = Av[a0]; }
+   /* S_i is A_i's off-diagonal columns filtered in order, so the matching
+    * A position only moves forward (the reference rescans from the start
+    * for every S entry and finds the same position) */
+   int jA = a0 + hasdiag;
    for (int k = Si[i]; k < Si[i + 1]; k++)
    {
       int jS = Sj[k];
-      int jA = a0 + hasdiag;
       while (Aj[jA] != jS) { jA++; }
       if (CF[jS] > 0) { FCj[pc] = f2c[jS]; FCv[pc++] = Av[jA]; }
       else { FFj[pf] = f2f[jS]; FFv[pf++] = Av[jA]; }
+      jA++;
    }
 }
 

@@ -271,8 +271,19 @@ static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int
    int *n1 = (int *) gb_dcalloc(sizeof(int) * 2);
    gb_tier t;
    tier_begin(&t, nrows);
-   gb_extpi_count_t(nrows, rows, S->i, S->j, CF, f2c, cnt, l1, n1, s);
-   int h1 = read_int(n1);
+   /* thread-per-row only pays off on large levels (many rows, short rows) */
+   int use_thread = nrows >= 65536;
+   int h1;
+   if (use_thread)
+   {
+      gb_extpi_count_t(nrows, rows, S->i, S->j, CF, f2c, cnt, l1, n1, s);
+      h1 = read_int(n1);
+   }
+   else
+   {
+      gb_iota(nrows, l1, n1, s);
+      h1 = nrows;
+   }
    int *ub = NULL;
    if (h1 > 0)
    {
@@ -294,7 +305,7 @@ static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int
    P->nnz = scan_total(cnt, P->i, nrows);
    P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
    P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
-   gb_extpi_fill_t(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, s);
+   if (use_thread) { gb_extpi_fill_t(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, s); }
    if (h1 > 0)
    {
       gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, l1, n1, h1, NULL, 0, 0,
@@ -779,7 +790,7 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
    gb_amg_params *prm = &amg->prm;
    cudaStream_t s = gb_stream();
    int nl = amg->num_levels;
-   float *F[32], *U[32];
+   float *F[32] = {0}, *U[32] = {0};
    for (int l = 0; l < nl; l++) { F[l] = amg->lev[l].Ff; U[l] = amg->lev[l].Uf; }
    gb_d2f(amg->lev[0].n, f0d, F[0], s);
    for (int l = 0; l < nl - 1; l++)

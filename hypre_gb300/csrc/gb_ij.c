@@ -69,7 +69,7 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
    int nsl = (A->nr + 31) / 32;
    int *sl_w = NULL;
    long long *sl_ptr = NULL;
-   if (A->nr >= 4096 && avg <= 40 && avg >= 4)
+   if (A->nr >= 4096 && avg <= 40 && avg >= 4 && nsl <= 1024 * 1024)
    {
       sl_w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
       sl_ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));

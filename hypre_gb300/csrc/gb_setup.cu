@@ -752,6 +752,19 @@ __global__ void __launch_bounds__(128) k_extpi_fill_t(int nrows, const int *__re
    }
 }
 
+__global__ void k_iota(int n, int *__restrict__ out, int *__restrict__ count)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { out[i] = i; }
+   if (i == 0) { *count = n; }
+}
+
+extern "C" void gb_iota(int n, int *out, int *count, cudaStream_t s)
+{
+   k_iota<<<gb_blocks(n, 256), 256, 0, s>>>(n, out, count);
+   GB_COUNT(1);
+}
+
 extern "C" void gb_extpi_count_t(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF,
                                  const int *f2c, int *cnt, int *ovf_list, int *ovf_n, cudaStream_t s)
 {
@@ -904,13 +917,16 @@ __global__ void k_tr_scatter(int nr, const int *__restrict__ Ai, const int *__re
    }
 }
 
-__global__ void k_tr_sort(int nc, const int *__restrict__ Ti, int *__restrict__ Tj, double *__restrict__ Tv)
+__global__ void k_tr_sort(int nc, const int *__restrict__ Ti, int *__restrict__ Tj, double *__restrict__ Tv,
+                          int minlen)
 {
+   // shell sort of one row by a thread (rows of at least minlen entries
+   // are left to the block sort)
    int c = blockIdx.x * blockDim.x + threadIdx.x;
    if (c >= nc) { return; }
    int b = Ti[c], e = Ti[c + 1];
-   // shell sort by row index (keys unique); values follow
    int len = e - b;
+   if (len >= minlen && len <= 2048) { return; }
    for (int gap = len / 2; gap > 0; gap /= 2)
    {
       for (int x = b + gap; x < e; x++)
@@ -930,6 +946,55 @@ __global__ void k_tr_sort(int nc, const int *__restrict__ Ti, int *__restrict__ 
    }
 }
 
+// bitonic sort of one row (minlen <= len <= 2048) by a 256-thread block
+__global__ void __launch_bounds__(256) k_tr_sort_block(int nc, const int *__restrict__ Ti, int *__restrict__ Tj,
+                                                      double *__restrict__ Tv, int minlen)
+{
+   __shared__ int key[2048];
+   __shared__ double val[2048];
+   for (int c = blockIdx.x; c < nc; c += gridDim.x)
+   {
+      int b = Ti[c], e = Ti[c + 1];
+      int len = e - b;
+      if (len < minlen || len > 2048) { continue; }
+      int m = 1;
+      while (m < len) { m <<= 1; }
+      for (int t = threadIdx.x; t < m; t += blockDim.x)
+      {
+         key[t] = t < len ? Tj[b + t] : 0x7fffffff;
+         val[t] = (t < len && Tv) ? Tv[b + t] : 0.0;
+      }
+      __syncthreads();
+      for (int k = 2; k <= m; k <<= 1)
+      {
+         for (int j = k >> 1; j > 0; j >>= 1)
+         {
+            for (int t = threadIdx.x; t < m; t += blockDim.x)
+            {
+               int p = t ^ j;
+               if (p > t)
+               {
+                  bool up = (t & k) == 0;
+                  int a = key[t], bb = key[p];
+                  if ((a > bb) == up)
+                  {
+                     key[t] = bb; key[p] = a;
+                     double tv = val[t]; val[t] = val[p]; val[p] = tv;
+                  }
+               }
+            }
+            __syncthreads();
+         }
+      }
+      for (int t = threadIdx.x; t < len; t += blockDim.x)
+      {
+         Tj[b + t] = key[t];
+         if (Tv) { Tv[b + t] = val[t]; }
+      }
+      __syncthreads();
+   }
+}
+
 extern "C" void gb_transpose_count(int nnz, const int *Aj, int *cnt, cudaStream_t s)
 {
    if (nnz > 0) { k_tr_count<<<gb_blocks(nnz, 256), 256, 0, s>>>(nnz, Aj, cnt); GB_COUNT(1); }
@@ -939,8 +1004,11 @@ extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, 
                                   const int *Ti, int *Tj, double *Tv, cudaStream_t s)
 {
    k_tr_scatter<<<gb_blocks(nr, 256), 256, 0, s>>>(nr, Ai, Aj, Av, fill, Tj, Tv);
-   k_tr_sort<<<gb_blocks(nc, 128), 128, 0, s>>>(nc, Ti, Tj, Tv);
-   GB_COUNT(2);
+   const int minlen = 64;
+   k_tr_sort<<<gb_blocks(nc, 128), 128, 0, s>>>(nc, Ti, Tj, Tv, minlen);
+   int nb = nc < 4096 ? (nc > 0 ? nc : 1) : 4096;
+   k_tr_sort_block<<<nb, 256, 0, s>>>(nc, Ti, Tj, Tv, minlen);
+   GB_COUNT(3);
 }
 
 // ---------------------------------------------------------------------------

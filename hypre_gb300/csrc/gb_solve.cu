@@ -176,15 +176,43 @@ __global__ void k_sell_width(int n, int nslices, const int *__restrict__ Ai, int
    w[s] = m;
 }
 
-__global__ void k_sell_ptr(int nslices, const int *__restrict__ w, long long *__restrict__ ptr)
+// slice offsets: block-level scans of width*32 (int64), then block offsets
+__global__ void k_sell_ptr_blocks(int nslices, const int *__restrict__ w, long long *__restrict__ ptr,
+                                  long long *__restrict__ bsum)
 {
-   // single thread prefix (nslices is n/32; run once per matrix at setup)
-   if (blockIdx.x == 0 && threadIdx.x == 0)
+   __shared__ long long ws[32];
+   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   long long v = s < nslices ? (long long) w[s] * 32 : 0;
+   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   long long x = v;
+   for (int o = 1; o < 32; o <<= 1) { long long y = __shfl_up_sync(GB_FULL, x, o); if (lane >= o) { x += y; } }
+   if (lane == 31) { ws[wid] = x; }
+   __syncthreads();
+   if (wid == 0)
    {
-      long long p = 0;
-      for (int s = 0; s < nslices; s++) { ptr[s] = p; p += (long long) w[s] * 32; }
-      ptr[nslices] = p;
+      long long t = lane < (int) (blockDim.x >> 5) ? ws[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) { long long y = __shfl_up_sync(GB_FULL, t, o); if (lane >= o) { t += y; } }
+      ws[lane] = t;
    }
+   __syncthreads();
+   long long excl = x - v + (wid > 0 ? ws[wid - 1] : 0);
+   if (s < nslices) { ptr[s] = excl; }
+   if (threadIdx.x == blockDim.x - 1) { bsum[blockIdx.x] = excl + v; }
+}
+
+__global__ void k_sell_ptr_fix(int nslices, long long *__restrict__ ptr, const long long *__restrict__ bsum,
+                               int nblocks)
+{
+   // one block: exclusive scan of the block sums (nblocks small), then add
+   __shared__ long long off[1024];
+   if (threadIdx.x == 0)
+   {
+      long long a = 0;
+      for (int b = 0; b < nblocks; b++) { off[b] = a; a += bsum[b]; }
+      ptr[nslices] = a;
+   }
+   __syncthreads();
+   for (int s = threadIdx.x; s < nslices; s += blockDim.x) { ptr[s] += off[s / 1024]; }
 }
 
 template <typename VT>
@@ -294,8 +322,13 @@ extern "C" void gb_sell_build(int n, const int *Ai, const int *Aj, const double 
    if (stage == 0)
    {
       k_sell_width<<<nblk(nslices, 256), 256, 0, s>>>(n, nslices, Ai, sl_w);
-      k_sell_ptr<<<1, 1, 0, s>>>(nslices, sl_w, sl_ptr);
-      GB_COUNT(2);
+      int nb = nblk(nslices, 1024);
+      long long *bsum = NULL;
+      cudaMallocAsync((void **) &bsum, sizeof(long long) * (size_t) nb, s);
+      k_sell_ptr_blocks<<<nb, 1024, 0, s>>>(nslices, sl_w, sl_ptr, bsum);
+      k_sell_ptr_fix<<<1, 1024, 0, s>>>(nslices, sl_ptr, bsum, nb);
+      cudaFreeAsync(bsum, s);
+      GB_COUNT(3);
       return;
    }
    long long nt = (long long) nslices * 32;
