@@ -75,6 +75,7 @@ def _declare(L):
         "HYPRE_FlexGMRESGetFinalRelativeResidualNorm": [vp, P(f64)],
         "HYPRE_GB300_BoomerAMGGetLevelCSR": [vp, i32, i32, P(i32), P(i32), P(i32), vp, vp, vp],
         "HYPRE_GB300_BoomerAMGGetLevelCF": [vp, i32, vp], "HYPRE_GB300_BoomerAMGGetLevelL1": [vp, i32, vp],
+        "HYPRE_GB300_BoomerAMGGetLevelCheby": [vp, i32, vp, vp, vp],
         "HYPRE_GB300_KrylovGetResidualHistory": [vp, i32, vp, P(i32)],
         "HYPRE_GB300_ParVectorGetDevicePointer": [vp, P(vp), P(i32)],
         "HYPRE_GB300_ParVectorCopyFromHost": [vp, vp, i32], "HYPRE_GB300_ParVectorCopyToHost": [vp, vp, i32],
@@ -249,6 +250,15 @@ class BoomerAMG:
         out = np.empty(n, np.float64)
         lib().HYPRE_GB300_BoomerAMGGetLevelL1(self.h, level, out.ctypes.data)
         return out
+
+    def level_cheby(self, level, n, order):
+        """(coefficients, (max_eig, min_eig), D^{-1/2}) of a level's Chebyshev smoother."""
+        order = min(max(order, 1), 4)
+        c = np.zeros(order)
+        e = np.zeros(2)
+        ds = np.empty(n, np.float64)
+        check(lib().HYPRE_GB300_BoomerAMGGetLevelCheby(self.h, level, c.ctypes.data, e.ctypes.data, ds.ctypes.data))
+        return c, (float(e[0]), float(e[1])), ds
 
     def setup_times(self):
         t = np.zeros(6)

@@ -70,8 +70,11 @@ static void level_free_vectors(gb_level *L)
 {
    gb_dfree(L->F); gb_dfree(L->U); gb_dfree(L->U2); gb_dfree(L->V);
    gb_dfree(L->Ff); gb_dfree(L->Uf); gb_dfree(L->U2f); gb_dfree(L->Vf);
+   gb_dfree(L->cheb_ds); gb_dfree(L->cheb_dsf); gb_dfree(L->W); gb_dfree(L->Wf);
    L->F = L->U = L->U2 = L->V = NULL;
    L->Ff = L->Uf = L->U2f = L->Vf = NULL;
+   L->cheb_ds = L->W = NULL;
+   L->cheb_dsf = L->Wf = NULL;
 }
 
 static void amg_free_hierarchy(gb_amg *amg)
@@ -558,6 +561,257 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
 
 static int relax_l1_option(int type) { return type == 18 ? 1 : 5; }
 
+/* --------------------------------------------------------------------------
+ * Chebyshev smoother setup
+ * ------------------------------------------------------------------------ */
+static double pythag(double a, double b)
+{
+   /* sqrt(a^2 + b^2) by the overflow-free iteration of Moler and Morrison
+    * (IBM J. Res. Dev. 27, 1983) */
+   double aa = fabs(a), ab = fabs(b);
+   double p = aa > ab ? aa : ab;
+   if (p == 0.0) { return p; }
+   double q = (aa < ab ? aa : ab) / p;
+   double r = q * q;
+   for (;;)
+   {
+      double t = r + 4.0;
+      if (t == 4.0) { break; }
+      double sr = r / t;
+      double u = sr * 2.0 + 1.0;
+      p = u * p;
+      double v = sr / u;
+      r = v * v * r;
+   }
+   return p;
+}
+
+/* Eigenvalues (ascending, in d) of the symmetric tridiagonal matrix with
+ * diagonal d[0..n-1] and sub-diagonal e[1..n-1], by the implicit QL method
+ * TQL1 (Bowdler, Martin, Reinsch, Wilkinson, Numer. Math. 11, 1968), which the
+ * reference calls as hypre_LINPACKcgtql1 (src/parcsr_ls/par_relax_more.c:507).
+ * Returns nonzero if an eigenvalue needs more than 30 QL steps. */
+static int eig_tridiag(int n, double *d, double *e)
+{
+   if (n <= 1) { return 0; }
+   for (int i = 1; i < n; i++) { e[i - 1] = e[i]; }
+   e[n - 1] = 0.0;
+   double f = 0.0, tst1 = 0.0;
+   for (int l = 0; l < n; l++)
+   {
+      double h = fabs(d[l]) + fabs(e[l]);
+      if (tst1 < h) { tst1 = h; }
+      int m = l;
+      while (tst1 + fabs(e[m]) != tst1) { m++; }
+      if (m > l)
+      {
+         int steps = 0;
+         do
+         {
+            if (steps == 30) { return l + 1; }
+            steps++;
+            double g = d[l];
+            double p = (d[l + 1] - g) / (e[l] * 2.0);
+            double r = pythag(p, 1.0);
+            double sg = p < 0.0 ? -1.0 : 1.0;
+            d[l] = e[l] / (p + sg * r);
+            d[l + 1] = e[l] * (p + sg * r);
+            double dl1 = d[l + 1];
+            h = g - d[l];
+            for (int i = l + 2; i < n; i++) { d[i] -= h; }
+            f += h;
+            p = d[m];
+            double c = 1.0, c2 = 1.0, c3 = 0.0, sn = 0.0, s2 = 0.0;
+            double el1 = e[l + 1];
+            for (int i = m - 1; i >= l; i--)
+            {
+               c3 = c2;
+               c2 = c;
+               s2 = sn;
+               g = c * e[i];
+               h = c * p;
+               r = pythag(p, e[i]);
+               e[i + 1] = sn * r;
+               sn = e[i] / r;
+               c = p / r;
+               p = c * d[i] - sn * g;
+               d[i + 1] = h + sn * (c * g + sn * d[i]);
+            }
+            p = -sn * s2 * c3 * el1 * e[l] / dl1;
+            e[l] = sn * p;
+            d[l] = c * p;
+         } while (tst1 + fabs(e[l]) > tst1);
+      }
+      double p = d[l] + f;
+      int i = l;
+      while (i > 0 && p < d[i - 1]) { d[i] = d[i - 1]; i--; }
+      d[i] = p;
+   }
+   return 0;
+}
+
+/* Extreme eigenvalue estimates of D^{-1/2} A D^{-1/2} (or A without scaling):
+ * max_iter CG steps from the seed-1 random vector, Lanczos tridiagonal from
+ * the CG coefficients (hypre_ParCSRMaxEigEstimateCGHost,
+ * src/parcsr_ls/par_relax_more.c:203).  ds must already hold the scaling. */
+static void cheby_eig_estimate(gb_level *L, int scale, int max_iter, double *max_eig, double *min_eig)
+{
+   int n = L->n;
+   cudaStream_t s = gb_stream();
+   if (n < max_iter) { max_iter = n; }
+   const gb_spmv_desc *A = gb_solve_desc(L->A, GB_PREC_F64);
+   size_t nb = sizeof(double) * (size_t) (n ? n : 1);
+   double *r = (double *) gb_dmalloc(nb), *p = (double *) gb_dcalloc(nb);
+   double *sv = (double *) gb_dmalloc(nb), *u = (double *) gb_dmalloc(nb);
+   double td[34], te[34];
+   memset(td, 0, sizeof(td));
+   memset(te, 0, sizeof(te));
+   gb_rand_uniform(n, 1, r, s);
+   double gamma = 0.0, gamma_old, beta = 1.0;   /* <r, p> with p = 0 */
+   int it = 0;
+   while (it < max_iter)
+   {
+      cudaMemcpyAsync(sv, r, nb, cudaMemcpyDeviceToDevice, s);
+      gamma_old = gamma;
+      gamma = gb_dot(n, r, sv);
+      if (gamma < 2.220446049250313e-16) { break; }
+      if (it == 0) { beta = 1.0; cudaMemcpyAsync(p, sv, nb, cudaMemcpyDeviceToDevice, s); }
+      else
+      {
+         beta = gamma / gamma_old;
+         gb_xpay_d(n, sv, beta, p, s);
+      }
+      if (scale)
+      {
+         gb_vmul_d(n, L->cheb_ds, p, u, s);
+         gb_spmv_d(A, u, sv, GB_EPI_AXPBY, 1.0, 0.0, NULL, NULL, 0.0, NULL, NULL, s);
+         gb_vmul_d(n, L->cheb_ds, sv, sv, s);
+      }
+      else { gb_spmv_d(A, p, sv, GB_EPI_AXPBY, 1.0, 0.0, NULL, NULL, 0.0, NULL, NULL, s); }
+      double sdotp = gb_dot(n, sv, p);
+      double alpha = gamma / sdotp;
+      double ainv = 1.0 / alpha;
+      td[it + 1] = ainv;
+      td[it] *= beta;
+      td[it] += ainv;
+      te[it + 1] = ainv;
+      te[it] *= sqrt(beta);
+      gb_axpy_d(n, -alpha, sv, r, s);
+      it++;
+   }
+   gb_sync();
+   gb_dfree(r); gb_dfree(p); gb_dfree(sv); gb_dfree(u);
+   eig_tridiag(it, td, te);
+   *max_eig = it > 0 ? td[it - 1] : 0.0;
+   *min_eig = td[0];
+}
+
+/* Coefficients of s(t) with u <- u + s(A) r, 1 - t s(t) the Chebyshev residual
+ * polynomial of the given order on [lower, upper] (hypre_ParCSRRelax_Cheby_Setup,
+ * src/parcsr_ls/par_cheby_setup.c): upper = 1.1 max_eig, lower = min_eig +
+ * fraction (upper - min_eig); variant 1 is the reference's modified form. */
+static void cheby_coefs(double max_eig, double min_eig, double fraction, int order, int variant, double *c)
+{
+   int co = order - 1;
+   double upper, lower;
+   if (max_eig <= 0.0)
+   {
+      upper = min_eig * 1.1;
+      lower = max_eig - (max_eig - upper) * fraction;
+   }
+   else
+   {
+      upper = max_eig * 1.1;
+      lower = (upper - min_eig) * fraction + min_eig;
+   }
+   double th = (upper + lower) / 2, de = (upper - lower) / 2, den;
+   for (int k = 0; k < 5; k++) { c[k] = 0.0; }
+   if (co == 0) { c[0] = fabs(th) > 0.0 ? 1.0 / th : 0.0; return; }
+   if (variant == 1)
+   {
+      if (co == 1)
+      {
+         den = th * th + de * th;
+         if (fabs(den) > 0.0) { c[0] = (de + 2 * th) / den; c[1] = -1.0 / den; }
+      }
+      else if (co == 2)
+      {
+         den = 2 * de * th * th - de * de * th - pow(de, 3) + 2 * pow(th, 3);
+         if (fabs(den) > 0.0)
+         {
+            c[0] = (4 * de * th - pow(de, 2) + 6 * pow(th, 2)) / den;
+            c[1] = -(2 * de + 6 * th) / den;
+            c[2] = 2 / den;
+         }
+      }
+      else
+      {
+         den = -4 * de * pow(th, 3) + 3 * pow(de, 2) * pow(th, 2) + 3 * pow(de, 3) * th - 4 * pow(th, 4);
+         if (fabs(den) > 0.0)
+         {
+            c[0] = (6 * pow(de, 2) * th - 12 * de * pow(th, 2) + 3 * pow(de, 3) - 16 * pow(th, 3)) / den;
+            c[1] = (12 * de * th - 3 * pow(de, 2) + 24 * pow(th, 2)) / den;
+            c[2] = -(4 * de + 16 * th) / den;
+            c[3] = 4 / den;
+         }
+      }
+      return;
+   }
+   if (co == 1)
+   {
+      den = de * de - 2 * th * th;
+      if (fabs(den) > 0.0) { c[0] = -4 * th / den; c[1] = 2 / den; }
+   }
+   else if (co == 2)
+   {
+      den = 3 * (de * de) * th - 4 * (th * th * th);
+      if (fabs(den) > 0.0)
+      {
+         c[0] = (3 * de * de - 12 * th * th) / den;
+         c[1] = 12 * th / den;
+         c[2] = -4 / den;
+      }
+   }
+   else
+   {
+      den = pow(de, 4) - 8 * ((de * th) * (de * th)) + pow(th, 4) * 8;
+      if (fabs(den) > 0.0)
+      {
+         c[0] = (32 * pow(th, 3) - 16 * de * de * th) / den;
+         c[1] = (8 * de * de - 48 * th * th) / den;
+         c[2] = 32 * th / den;
+         c[3] = -8 / den;
+      }
+   }
+}
+
+static void cheby_level_setup(gb_amg *amg, int l)
+{
+   gb_amg_params *prm = &amg->prm;
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   int n = L->n;
+   int order = prm->cheby_order > 4 ? 4 : (prm->cheby_order < 1 ? 1 : prm->cheby_order);
+   L->cheb_order = order;
+   size_t nb = sizeof(double) * (size_t) (n ? n : 1), nf = sizeof(float) * (size_t) (n ? n : 1);
+   L->cheb_ds = (double *) gb_dmalloc(nb);
+   L->cheb_dsf = (float *) gb_dmalloc(nf);
+   L->W = (double *) gb_dcalloc(nb);
+   L->Wf = (float *) gb_dcalloc(nf);
+   if (prm->cheby_scale) { gb_diag_inv_sqrt(n, L->A->A.i, L->A->A.j, L->A->A.v, L->cheb_ds, s); }
+   else { gb_fill_d(n, L->cheb_ds, 1.0, s); }
+   gb_d2f(n, L->cheb_ds, L->cheb_dsf, s);
+   double mx = 0.0, mn = 0.0;
+   if (prm->cheby_eig_est > 0)
+   {
+      int it = prm->cheby_eig_est < 32 ? prm->cheby_eig_est : 32;
+      cheby_eig_estimate(L, prm->cheby_scale, it, &mx, &mn);
+   }
+   L->cheb_eig[0] = mx;
+   L->cheb_eig[1] = mn;
+   cheby_coefs(mx, mn, prm->cheby_fraction, order, prm->cheby_variant, L->cheb_c);
+}
+
 int gb_amg_setup(gb_amg *amg, gb_parcsr *A0)
 {
    amg_free_hierarchy(amg);
@@ -629,6 +883,15 @@ int gb_amg_setup(gb_amg *amg, gb_parcsr *A0)
       if (vp0 != GB_PREC_F64) { gb_solve_desc(L->A, GB_PREC_F64); }
       if (L->P) { gb_solve_desc(L->P, vp); gb_solve_desc(L->R, vp); }
    }
+   /* Chebyshev data on the levels that relax with it (par_amg_setup.c:3496-3536) */
+   for (int l = 0; l < amg->num_levels; l++)
+   {
+      if (prm->relax_type[1] == 16 || prm->relax_type[2] == 16 ||
+          (prm->relax_type[3] == 16 && l == amg->num_levels - 1))
+      {
+         cheby_level_setup(amg, l);
+      }
+   }
    gb_sync();
    amg->r_work = (double *) gb_dmalloc(sizeof(double) * (size_t) (amg->lev[0].n ? amg->lev[0].n : 1));
    amg->setup_times[4] = gb_wtime() - t_sm;
@@ -674,6 +937,51 @@ static void twostage_gs_d(gb_amg *amg, int l, int inner, const double *f, double
    }
 }
 
+/* Chebyshev smoother, in place on u (hypre_ParCSRRelax_Cheby_SolveHost,
+ * src/parcsr_ls/par_cheby_solve.c:194): r = D^{-1/2}(f - Au), then the
+ * polynomial by Horner steps, each one SpMV with a fused epilogue. */
+static void cheby_d(gb_amg *amg, int l, const double *f, double *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   const gb_spmv_desc *A = gb_solve_desc(L->A, GB_PREC_F64);
+   int co = L->cheb_order - 1;
+   const double *c = L->cheb_c, *ds = L->cheb_ds;
+   double *r = L->V, *q = L->U2, *q2 = L->W;
+   if (u_zero) { gb_fill_d(L->n, u, 0.0, s); gb_vmul_d(L->n, ds, f, r, s); }
+   else { gb_spmv_d(A, u, r, GB_EPI_CHEB_RES, 0.0, 0.0, f, ds, 0.0, NULL, NULL, s); }
+   if (co == 0) { gb_cheb_order1_d(L->n, c[0], r, ds, u, s); return; }
+   gb_cheb_start_d(L->n, c[co], r, ds, q, s);
+   for (int k = co - 1; k >= 1; k--)
+   {
+      gb_spmv_d(A, q, q2, GB_EPI_CHEB_STEP, c[k], 0.0, r, ds, 0.0, NULL, NULL, s);
+      double *t = q; q = q2; q2 = t;
+   }
+   gb_spmv_d(A, q, u, GB_EPI_CHEB_LAST, c[0], 0.0, r, ds, 0.0, NULL, NULL, s);
+}
+
+static void cheby_f(gb_amg *amg, int l, const float *f, float *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   int vp = (amg->prm.cycle_prec == GB_PREC_F16 && l == 0) ? GB_PREC_F16 : GB_PREC_F32;
+   const gb_spmv_desc *A = gb_solve_desc(L->A, vp);
+   int co = L->cheb_order - 1;
+   const double *c = L->cheb_c;
+   const float *ds = L->cheb_dsf;
+   float *r = L->Vf, *q = L->U2f, *q2 = L->Wf;
+   if (u_zero) { gb_fill_f(L->n, u, 0.0f, s); gb_vmul_f(L->n, ds, f, r, s); }
+   else { gb_spmv_f(A, u, r, GB_EPI_CHEB_RES, 0.0f, 0.0f, f, ds, 0.0f, NULL, NULL, s); }
+   if (co == 0) { gb_cheb_order1_f(L->n, (float) c[0], r, ds, u, s); return; }
+   gb_cheb_start_f(L->n, (float) c[co], r, ds, q, s);
+   for (int k = co - 1; k >= 1; k--)
+   {
+      gb_spmv_f(A, q, q2, GB_EPI_CHEB_STEP, (float) c[k], 0.0f, r, ds, 0.0f, NULL, NULL, s);
+      float *t = q; q = q2; q2 = t;
+   }
+   gb_spmv_f(A, q, u, GB_EPI_CHEB_LAST, (float) c[0], 0.0f, r, ds, 0.0f, NULL, NULL, s);
+}
+
 static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
 {
    gb_amg_params *prm = &amg->prm;
@@ -691,6 +999,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       for (int sw = 0; sw < prm->num_sweeps[1]; sw++)
       {
          if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], uz && sw == 0); }
+         else if (type == 16) { cheby_d(amg, l, F[l], U[l], uz && sw == 0); }
          else
          {
             if (uz && sw == 0) { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
@@ -710,6 +1019,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       int l = nl - 1;
       gb_level *L = &amg->lev[l];
       if (amg->coarse_inv) { gb_dense_apply_d(amg->coarse_n, amg->coarse_inv, F[l], U[l], s); }
+      else if (nl == 1 && !u0_zero && prm->relax_type[3] == 16) { cheby_d(amg, l, F[l], U[l], 0); }
       else if (nl == 1 && !u0_zero)
       {
          relax_d(amg, l, prm->relax_type[3], F[l], U[l], L->U2, 0);
@@ -719,6 +1029,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       {
          int type = prm->relax_type[3];
          if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
+         else if (type == 16) { cheby_d(amg, l, F[l], U[l], 1); }
          else { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
       }
    }
@@ -730,10 +1041,11 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       gb_spmv_d(gb_solve_desc(L->P, GB_PREC_F64), U[l + 1], L->U2, 0, 1.0, 1.0, U[l], NULL, 0.0, NULL, NULL, s);
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
-         if (type == 11 || type == 12)
+         if (type == 11 || type == 12 || type == 16)
          {
             if (sw == 0) { cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
-            twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0);
+            if (type == 16) { cheby_d(amg, l, F[l], U[l], 0); }
+            else { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0); }
          }
          else
          {
@@ -801,6 +1113,7 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
       for (int sw = 0; sw < prm->num_sweeps[1]; sw++)
       {
          if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], sw == 0); }
+         else if (type == 16) { cheby_f(amg, l, F[l], U[l], sw == 0); }
          else if (sw == 0) { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
          else
          {
@@ -818,6 +1131,7 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
       {
          int type = prm->relax_type[3];
          if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
+         else if (type == 16) { cheby_f(amg, l, F[l], U[l], 1); }
          else { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
       }
    }
@@ -828,10 +1142,11 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
       gb_spmv_f(gb_solve_desc(L->P, GB_PREC_F32), U[l + 1], L->U2f, 0, 1.f, 1.f, U[l], NULL, 0.f, NULL, NULL, s);
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
-         if (type == 11 || type == 12)
+         if (type == 11 || type == 12 || type == 16)
          {
             if (sw == 0) { cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
-            twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0);
+            if (type == 16) { cheby_f(amg, l, F[l], U[l], 0); }
+            else { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0); }
          }
          else if (sw == 0) { relax_f(amg, l, type, F[l], L->U2f, U[l], 0); }
          else
@@ -1043,7 +1358,10 @@ HYPRE_Int HYPRE_BoomerAMGSetCycleType(HYPRE_Solver solver, HYPRE_Int v)
    return gb_error_flag;
 }
 
-static int relax_supported(int t) { return t == 18 || t == 7 || t == 11 || t == 12 || t == 9 || t == 99 || t == 19 || t == 98; }
+static int relax_supported(int t)
+{
+   return t == 18 || t == 7 || t == 11 || t == 12 || t == 16 || t == 9 || t == 99 || t == 19 || t == 98;
+}
 
 HYPRE_Int HYPRE_BoomerAMGSetRelaxType(HYPRE_Solver solver, HYPRE_Int v)
 {
@@ -1201,6 +1519,24 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCF(HYPRE_Solver solver, HYPRE_Int level, 
    if (level < 0 || level >= a->num_levels - 1 || !cf) { gb_error_in_arg(2); return gb_error_flag; }
    cudaMemcpyAsync(cf, a->lev[level].CF, sizeof(int) * (size_t) a->lev[level].n, cudaMemcpyDeviceToHost, gb_stream());
    gb_sync();
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCheby(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Real *coefs,
+                                             HYPRE_Real *eig, HYPRE_Real *ds)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (level < 0 || level >= a->num_levels) { gb_error_in_arg(2); return gb_error_flag; }
+   gb_level *L = &a->lev[level];
+   if (!L->cheb_ds) { gb_error(HYPRE_ERROR_GENERIC, "level has no Chebyshev smoother data"); return gb_error_flag; }
+   if (coefs) { for (int k = 0; k < L->cheb_order; k++) { coefs[k] = L->cheb_c[k]; } }
+   if (eig) { eig[0] = L->cheb_eig[0]; eig[1] = L->cheb_eig[1]; }
+   if (ds)
+   {
+      cudaMemcpyAsync(ds, L->cheb_ds, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToHost, gb_stream());
+      gb_sync();
+   }
    return gb_error_flag;
 }
 

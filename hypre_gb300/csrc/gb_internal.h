@@ -133,6 +133,13 @@ typedef struct
    /* cycle vectors (FP64 and FP32 sets) */
    double    *F, *U, *U2, *V;
    float     *Ff, *Uf, *U2f, *Vf;
+   /* Chebyshev smoother (relax 16): coefficients of s(t), eigenvalue
+    * estimates, D^{-1/2} (ones without scaling) and a second work vector */
+   int        cheb_order;
+   double     cheb_c[5];
+   double     cheb_eig[2];
+   double    *cheb_ds, *W;
+   float     *cheb_dsf, *Wf;
 } gb_level;
 
 typedef struct

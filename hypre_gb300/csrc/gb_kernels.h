@@ -11,6 +11,14 @@
 extern "C" {
 #endif
 
+/* SpMV epilogue modes: y = alpha*Ax + beta*b (0), Jacobi (1), residual b - Ax (2),
+ * Chebyshev: d.*(b - Ax) (3), d.*(alpha*b + d.*Ax) (4), y + d.*(alpha*b + d.*Ax) (5) */
+#define GB_EPI_AXPBY 0
+#define GB_EPI_JACOBI 1
+#define GB_EPI_RESID 2
+#define GB_EPI_CHEB_RES 3
+#define GB_EPI_CHEB_STEP 4
+#define GB_EPI_CHEB_LAST 5
 #define GB_PREC_F64 0
 #define GB_PREC_F32 1
 #define GB_PREC_F16 2
@@ -116,6 +124,15 @@ void gb_gs_lower_d(int n, const int *Ai, const int *Aj, const double *Av, const 
                    double m, cudaStream_t s);
 void gb_gs_lower_f(int n, const int *Ai, const int *Aj, const void *Av, int vprec, const float *z, float *znew,
                    float *u, float m, cudaStream_t s);
+
+void gb_rand_uniform(int n, int seed, double *v, cudaStream_t s);
+void gb_diag_inv_sqrt(int n, const int *Ai, const int *Aj, const double *Av, double *ds, cudaStream_t s);
+void gb_cheb_start_d(long long n, double c, const double *r, const double *d, double *q, cudaStream_t s);
+void gb_cheb_start_f(long long n, float c, const float *r, const float *d, float *q, cudaStream_t s);
+void gb_cheb_order1_d(long long n, double c, const double *r, const double *d, double *u, cudaStream_t s);
+void gb_cheb_order1_f(long long n, float c, const float *r, const float *d, float *u, cudaStream_t s);
+void gb_vmul_d(long long n, const double *a, const double *b, double *c, cudaStream_t s);
+void gb_vmul_f(long long n, const float *a, const float *b, float *c, cudaStream_t s);
 
 void gb_fill_d(long long n, double *x, double v, cudaStream_t s);
 void gb_fill_f(long long n, float *x, float v, cudaStream_t s);

@@ -206,6 +206,52 @@ __device__ __forceinline__ double pm_draw(long long k)
    return (double) x / (double) 2147483647;
 }
 
+// v[i] = 2 * (i+1)-th Park-Miller draw from seed - 1 (hypre_SeqVectorSetRandomValues,
+// src/seq_mv/vector.c), each element computed independently by jump-ahead
+__global__ void k_rand_uniform(int n, unsigned long long seed, double *__restrict__ v)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   const unsigned long long m = 2147483647ULL;
+   unsigned long long a = 16807ULL, r = 1ULL;
+   long long e = (long long) i + 1;
+   while (e > 0) { if (e & 1) { r = (r * a) % m; } a = (a * a) % m; e >>= 1; }
+   unsigned long long x = (r * seed) % m;
+   v[i] = 2.0 * ((double) x / (double) 2147483647) - 1.0;
+}
+
+extern "C" void gb_rand_uniform(int n, int seed, double *v, cudaStream_t s)
+{
+   // seeds are clamped to [1, 2^31 - 2] as hypre_SeedRand does
+   long long sd = seed < 1 ? 1 : (seed >= 2147483647 ? 2147483646 : seed);
+   if (n > 0) { k_rand_uniform<<<gb_blocks(n, 256), 256, 0, s>>>(n, (unsigned long long) sd, v); GB_COUNT(1); }
+}
+
+// ds[i] = 1/sqrt(|a_ii|) for the first entry of row i in column i, 0 when
+// there is none or it is zero (hypre_CSRMatrixExtractDiagonal type 4,
+// src/seq_mv/csr_matop.c)
+__global__ void k_diag_inv_sqrt(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                                const double *__restrict__ Av, double *__restrict__ ds)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   double d = 0.0;
+   for (int k = Ai[i]; k < Ai[i + 1]; k++)
+   {
+      if (Aj[k] == i)
+      {
+         if (Av[k] != 0.0) { d = 1.0 / sqrt(fabs(Av[k])); }
+         break;
+      }
+   }
+   ds[i] = d;
+}
+
+extern "C" void gb_diag_inv_sqrt(int n, const int *Ai, const int *Aj, const double *Av, double *ds, cudaStream_t s)
+{
+   if (n > 0) { k_diag_inv_sqrt<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, ds); GB_COUNT(1); }
+}
+
 __global__ void k_colcount(int nnz, const int *__restrict__ Sj, int *__restrict__ colcnt)
 {
    int k = blockIdx.x * blockDim.x + threadIdx.x;

@@ -39,13 +39,17 @@ template <> struct Acc<__half, float>
 //                    mode 2  y = (b_i - s) for residuals   (alpha=-1, beta=1 shortcut)
 template <typename XT>
 __device__ __forceinline__ XT row_epilogue(int mode, XT s, int i, XT alpha, XT beta, const XT *b, const XT *x,
-                                           const XT *d, XT w)
+                                           const XT *d, XT w, const XT *y)
 {
    if (mode == 1) { return x[i] + w * (b[i] - s) / d[i]; }
    if (mode == 2) { return b[i] - s; }
-   XT y = alpha * s;
-   if (beta != (XT) 0) { y += beta * b[i]; }
-   return y;
+   // Chebyshev steps (d = D^{-1/2}, b = scaled residual r, alpha = coefficient)
+   if (mode == 3) { return d[i] * (b[i] - s); }
+   if (mode == 4) { return d[i] * (alpha * b[i] + d[i] * s); }
+   if (mode == 5) { return y[i] + d[i] * (alpha * b[i] + d[i] * s); }
+   XT r = alpha * s;
+   if (beta != (XT) 0) { r += beta * b[i]; }
+   return r;
 }
 
 // Block-level sum of v (fixed reduction tree: deterministic), lane 0 of warp 0
@@ -99,7 +103,7 @@ __global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__
       for (int o = K / 2; o > 0; o >>= 1) { s += __shfl_down_sync(GB_FULL, s, o, K); }
       if (valid && lane == 0)
       {
-         XT yi = row_epilogue<XT>(mode, (XT) s, i, alpha, beta, b, x, d, w);
+         XT yi = row_epilogue<XT>(mode, (XT) s, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
@@ -150,7 +154,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
       int i = s * 32 + t;
       if (i < n)
       {
-         XT yi = row_epilogue<XT>(mode, (XT) (acc0 + acc1), i, alpha, beta, b, x, d, w);
+         XT yi = row_epilogue<XT>(mode, (XT) (acc0 + acc1), i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
@@ -568,6 +572,41 @@ extern "C" void gb_d2f(long long n, const double *a, float *b, cudaStream_t s)
 { if (n > 0) { k_d2f<<<nblk(n, 256), 256, 0, s>>>(n, a, b); GB_COUNT(1); } }
 extern "C" void gb_f2d(long long n, const float *a, double *b, cudaStream_t s)
 { if (n > 0) { k_f2d<<<nblk(n, 256), 256, 0, s>>>(n, a, b); GB_COUNT(1); } }
+
+// Chebyshev smoother vector steps (d = D^{-1/2}):
+//   start:   q = d .* (c * r)          (u stays as the original iterate)
+//   order 1: u = u + d .* (c * r)
+template <typename T>
+__global__ void k_cheb_start(long long n, T c, const T *__restrict__ r, const T *__restrict__ d, T *__restrict__ q)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { q[i] = d[i] * (r[i] * c); }
+}
+template <typename T>
+__global__ void k_cheb_order1(long long n, T c, const T *__restrict__ r, const T *__restrict__ d, T *__restrict__ u)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { u[i] = u[i] + d[i] * (r[i] * c); }
+}
+template <typename T>
+__global__ void k_vmul(long long n, const T *__restrict__ a, const T *__restrict__ b, T *c)
+{
+   long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { c[i] = a[i] * b[i]; }
+}
+
+extern "C" void gb_cheb_start_d(long long n, double c, const double *r, const double *d, double *q, cudaStream_t s)
+{ if (n > 0) { k_cheb_start<double><<<nblk(n, 256), 256, 0, s>>>(n, c, r, d, q); GB_COUNT(1); } }
+extern "C" void gb_cheb_start_f(long long n, float c, const float *r, const float *d, float *q, cudaStream_t s)
+{ if (n > 0) { k_cheb_start<float><<<nblk(n, 256), 256, 0, s>>>(n, c, r, d, q); GB_COUNT(1); } }
+extern "C" void gb_cheb_order1_d(long long n, double c, const double *r, const double *d, double *u, cudaStream_t s)
+{ if (n > 0) { k_cheb_order1<double><<<nblk(n, 256), 256, 0, s>>>(n, c, r, d, u); GB_COUNT(1); } }
+extern "C" void gb_cheb_order1_f(long long n, float c, const float *r, const float *d, float *u, cudaStream_t s)
+{ if (n > 0) { k_cheb_order1<float><<<nblk(n, 256), 256, 0, s>>>(n, c, r, d, u); GB_COUNT(1); } }
+extern "C" void gb_vmul_d(long long n, const double *a, const double *b, double *c, cudaStream_t s)
+{ if (n > 0) { k_vmul<double><<<nblk(n, 256), 256, 0, s>>>(n, a, b, c); GB_COUNT(1); } }
+extern "C" void gb_vmul_f(long long n, const float *a, const float *b, float *c, cudaStream_t s)
+{ if (n > 0) { k_vmul<float><<<nblk(n, 256), 256, 0, s>>>(n, a, b, c); GB_COUNT(1); } }
 
 extern "C" void gb_dot_d(long long n, const double *x, const double *y, double *part, double *out, cudaStream_t s)
 {

@@ -270,6 +270,11 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCSR(HYPRE_Solver solver, HYPRE_Int level,
                                            HYPRE_Int *rowptr, HYPRE_Int *colidx, HYPRE_Real *values);
 HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCF(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int *cf_marker);
 HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelL1(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Real *l1);
+/* Chebyshev smoother data of a level (relax type 16): the ChebyOrder
+ * coefficients of s(t) in u <- u + s(A) r, eig[0..1] = max/min eigenvalue
+ * estimates, ds = D^{-1/2} (n values); any pointer may be NULL. */
+HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCheby(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Real *coefs,
+                                             HYPRE_Real *eig, HYPRE_Real *ds);
 /* Relative residual history of the last Krylov solve (entries 0..iters). */
 HYPRE_Int HYPRE_GB300_KrylovGetResidualHistory(HYPRE_Solver solver, HYPRE_Int maxn, HYPRE_Real *relres,
                                                HYPRE_Int *n);

@@ -1157,10 +1157,307 @@ static void relax_two_stage_gs(const or_csr *A, const double *f, double w, int i
    }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Chebyshev smoother (relax 16)                                             */
+/* ------------------------------------------------------------------------ */
+
+static double pythag(double a, double b)
+{
+   /* sqrt(a^2 + b^2) without overflow: the iteration of Moler and Morrison
+    * (IBM J. Res. Dev. 27, 1983) as used by EISPACK's PYTHAG */
+   double aa = fabs(a), ab = fabs(b);
+   double p = aa > ab ? aa : ab;
+   if (p == 0.0) { return p; }
+   double q = (aa < ab ? aa : ab) / p;
+   double r = q * q;
+   for (;;)
+   {
+      double t = r + 4.0;
+      if (t == 4.0) { break; }
+      double sr = r / t;
+      double u = sr * 2.0 + 1.0;
+      p = u * p;
+      double v = sr / u;
+      r = v * v * r;
+   }
+   return p;
+}
+
+int or_eig_tridiag(int n, double *d, double *e)
+{
+   /* Eigenvalues (ascending, in d) of the symmetric tridiagonal matrix with
+    * diagonal d[0..n-1] and sub-diagonal e[1..n-1] (e[0] unused), by the
+    * implicit QL method TQL1 of Bowdler, Martin, Reinsch and Wilkinson
+    * (Numer. Math. 11, 293-306, 1968), as the reference calls it through
+    * hypre_LINPACKcgtql1 (src/parcsr_ls/par_relax_more.c:507).  Returns the
+    * 1-based index of an eigenvalue that did not converge in 30 steps, else 0. */
+   if (n <= 1) { return 0; }
+   for (int i = 1; i < n; i++) { e[i - 1] = e[i]; }
+   e[n - 1] = 0.0;
+   double f = 0.0, tst1 = 0.0;
+   for (int l = 0; l < n; l++)
+   {
+      double h = fabs(d[l]) + fabs(e[l]);
+      if (tst1 < h) { tst1 = h; }
+      int m = l;
+      while (tst1 + fabs(e[m]) != tst1) { m++; }   /* e[n-1] == 0 ends the search */
+      if (m > l)
+      {
+         int steps = 0;
+         do
+         {
+            if (steps == 30) { return l + 1; }
+            steps++;
+            /* Wilkinson-type shift from the leading 2x2 block */
+            double g = d[l];
+            double p = (d[l + 1] - g) / (e[l] * 2.0);
+            double r = pythag(p, 1.0);
+            double sg = p < 0.0 ? -1.0 : 1.0;
+            d[l] = e[l] / (p + sg * r);
+            d[l + 1] = e[l] * (p + sg * r);
+            double dl1 = d[l + 1];
+            h = g - d[l];
+            for (int i = l + 2; i < n; i++) { d[i] -= h; }
+            f += h;
+            /* QL sweep from m-1 up to l */
+            p = d[m];
+            double c = 1.0, c2 = 1.0, c3 = 0.0, sn = 0.0, s2 = 0.0;
+            double el1 = e[l + 1];
+            for (int i = m - 1; i >= l; i--)
+            {
+               c3 = c2;
+               c2 = c;
+               s2 = sn;
+               g = c * e[i];
+               h = c * p;
+               r = pythag(p, e[i]);
+               e[i + 1] = sn * r;
+               sn = e[i] / r;
+               c = p / r;
+               p = c * d[i] - sn * g;
+               d[i + 1] = h + sn * (c * g + sn * d[i]);
+            }
+            p = -sn * s2 * c3 * el1 * e[l] / dl1;
+            e[l] = sn * p;
+            d[l] = c * p;
+         } while (tst1 + fabs(e[l]) > tst1);
+      }
+      /* place d[l] + f among the already ordered d[0..l-1] */
+      double p = d[l] + f;
+      int i = l;
+      while (i > 0 && p < d[i - 1]) { d[i] = d[i - 1]; i--; }
+      d[i] = p;
+   }
+   return 0;
+}
+
+static void diag_inv_sqrt(const or_csr *A, double *ds)
+{
+   /* hypre_CSRMatrixExtractDiagonal type 4 (src/seq_mv/csr_matop.c:2100-2150):
+    * 1/sqrt(|a_ii|) of the first entry in row i whose column is i, else 0 */
+   for (int i = 0; i < A->nr; i++)
+   {
+      double di = 0.0;
+      for (int k = A->i[i]; k < A->i[i + 1]; k++)
+      {
+         if (A->j[k] == i)
+         {
+            if (A->v[k] != 0.0) { di = 1.0 / sqrt(fabs(A->v[k])); }
+            break;
+         }
+      }
+      ds[i] = di;
+   }
+}
+
+int or_max_eig_cg(const or_csr *A, int scale, int max_iter, double *max_eig, double *min_eig)
+{
+   /* hypre_ParCSRMaxEigEstimateCGHost src/parcsr_ls/par_relax_more.c:203-390:
+    * max_iter steps of CG on D^{-1/2} A D^{-1/2} (or A) from a random start
+    * (seed 1); the Lanczos tridiagonal built from the CG coefficients gives the
+    * extreme eigenvalue estimates. */
+   int n = A->nr;
+   if (n < max_iter) { max_iter = n; }
+   double *r = xmalloc(sizeof(double) * (n ? n : 1)), *p = xcalloc(n, sizeof(double));
+   double *sv = xcalloc(n, sizeof(double)), *ds = xmalloc(sizeof(double) * (n ? n : 1));
+   double *u = xcalloc(n, sizeof(double));
+   double *td = xcalloc(max_iter + 1, sizeof(double)), *te = xcalloc(max_iter + 1, sizeof(double));
+   or_rand_uniform(n, 1, r);
+   if (scale) { diag_inv_sqrt(A, ds); }
+   else { for (int i = 0; i < n; i++) { ds[i] = 1.0; } }
+   double gamma = or_dot(n, r, p), gamma_old, beta = 1.0;
+   int it = 0;
+   while (it < max_iter)
+   {
+      memcpy(sv, r, sizeof(double) * n);
+      gamma_old = gamma;
+      gamma = or_dot(n, r, sv);
+      if (gamma < 2.220446049250313e-16) { break; }
+      if (it == 0) { beta = 1.0; memcpy(p, sv, sizeof(double) * n); }
+      else
+      {
+         beta = gamma / gamma_old;
+         for (int i = 0; i < n; i++) { p[i] = sv[i] + beta * p[i]; }
+      }
+      if (scale)
+      {
+         for (int i = 0; i < n; i++) { u[i] = ds[i] * p[i]; }
+         or_matvec(1.0, A, u, 0.0, NULL, sv);
+         for (int i = 0; i < n; i++) { sv[i] = ds[i] * sv[i]; }
+      }
+      else { or_matvec(1.0, A, p, 0.0, NULL, sv); }
+      double sdotp = or_dot(n, sv, p);
+      double alpha = gamma / sdotp;
+      double ainv = 1.0 / alpha;
+      td[it + 1] = ainv;
+      td[it] *= beta;
+      td[it] += ainv;
+      te[it + 1] = ainv;
+      te[it] *= sqrt(beta);
+      for (int i = 0; i < n; i++) { r[i] += -alpha * sv[i]; }
+      it++;
+   }
+   or_eig_tridiag(it, td, te);
+   *max_eig = it > 0 ? td[it - 1] : 0.0;
+   *min_eig = td[0];
+   free(r); free(p); free(sv); free(ds); free(u); free(td); free(te);
+   return 0;
+}
+
+int or_cheby_setup(const or_csr *A, double max_eig, double min_eig, double fraction, int order,
+                   int scale, int variant, double *coefs, double *ds)
+{
+   /* hypre_ParCSRRelax_Cheby_Setup src/parcsr_ls/par_cheby_setup.c: the
+    * coefficients of s(t), u <- u + s(A) r, where 1 - t s(t) is the Chebyshev
+    * residual polynomial of the given order on [lower, upper] (upper = 1.1 *
+    * max_eig, lower = min_eig + fraction * (upper - min_eig)); ds = D^{-1/2} */
+   if (order > 4) { order = 4; }
+   if (order < 1) { order = 1; }
+   int co = order - 1;
+   double upper, lower;
+   if (max_eig <= 0.0)
+   {
+      upper = min_eig * 1.1;
+      lower = max_eig - (max_eig - upper) * fraction;
+   }
+   else
+   {
+      upper = max_eig * 1.1;
+      lower = (upper - min_eig) * fraction + min_eig;
+   }
+   double th = (upper + lower) / 2, de = (upper - lower) / 2, den;
+   for (int k = 0; k <= co; k++) { coefs[k] = 0.0; }
+   if (variant == 1)
+   {
+      if (co == 0) { coefs[0] = fabs(th) > 0.0 ? 1.0 / th : 0.0; }
+      else if (co == 1)
+      {
+         den = th * th + de * th;
+         if (fabs(den) > 0.0) { coefs[0] = (de + 2 * th) / den; coefs[1] = -1.0 / den; }
+      }
+      else if (co == 2)
+      {
+         den = 2 * de * th * th - de * de * th - pow(de, 3) + 2 * pow(th, 3);
+         if (fabs(den) > 0.0)
+         {
+            coefs[0] = (4 * de * th - pow(de, 2) + 6 * pow(th, 2)) / den;
+            coefs[1] = -(2 * de + 6 * th) / den;
+            coefs[2] = 2 / den;
+         }
+      }
+      else
+      {
+         den = -4 * de * pow(th, 3) + 3 * pow(de, 2) * pow(th, 2) + 3 * pow(de, 3) * th - 4 * pow(th, 4);
+         if (fabs(den) > 0.0)
+         {
+            coefs[0] = (6 * pow(de, 2) * th - 12 * de * pow(th, 2) + 3 * pow(de, 3) - 16 * pow(th, 3)) / den;
+            coefs[1] = (12 * de * th - 3 * pow(de, 2) + 24 * pow(th, 2)) / den;
+            coefs[2] = -(4 * de + 16 * th) / den;
+            coefs[3] = 4 / den;
+         }
+      }
+   }
+   else
+   {
+      if (co == 0) { coefs[0] = fabs(th) > 0.0 ? 1.0 / th : 0.0; }
+      else if (co == 1)
+      {
+         den = de * de - 2 * th * th;
+         if (fabs(den) > 0.0) { coefs[0] = -4 * th / den; coefs[1] = 2 / den; }
+      }
+      else if (co == 2)
+      {
+         den = 3 * (de * de) * th - 4 * (th * th * th);
+         if (fabs(den) > 0.0)
+         {
+            coefs[0] = (3 * de * de - 12 * th * th) / den;
+            coefs[1] = 12 * th / den;
+            coefs[2] = -4 / den;
+         }
+      }
+      else
+      {
+         den = pow(de, 4) - 8 * ((de * th) * (de * th)) + pow(th, 4) * 8;
+         if (fabs(den) > 0.0)
+         {
+            coefs[0] = (32 * pow(th, 3) - 16 * de * de * th) / den;
+            coefs[1] = (8 * de * de - 48 * th * th) / den;
+            coefs[2] = 32 * th / den;
+            coefs[3] = -8 / den;
+         }
+      }
+   }
+   if (scale) { diag_inv_sqrt(A, ds); }
+   else { for (int i = 0; i < A->nr; i++) { ds[i] = 1.0; } }
+   return 0;
+}
+
+static void relax_cheby(const or_csr *A, const double *f, const double *ds, const double *coefs, int order,
+                        int scale, double *u, double *r, double *o, double *v, double *tmp)
+{
+   /* hypre_ParCSRRelax_Cheby_SolveHost src/parcsr_ls/par_cheby_solve.c:194-330 */
+   int n = A->nr;
+   if (order > 4) { order = 4; }
+   if (order < 1) { order = 1; }
+   int co = order - 1;
+   if (!scale)
+   {
+      or_matvec(-1.0, A, u, 1.0, f, r);
+      for (int i = 0; i < n; i++) { o[i] = u[i]; u[i] = r[i] * coefs[co]; }
+      for (int k = co - 1; k >= 0; k--)
+      {
+         or_matvec(1.0, A, u, 0.0, NULL, v);
+         for (int i = 0; i < n; i++) { u[i] = coefs[k] * r[i] + v[i]; }
+      }
+      for (int i = 0; i < n; i++) { u[i] = o[i] + u[i]; }
+      return;
+   }
+   or_matvec(-1.0, A, u, 0.0, NULL, tmp);
+   for (int i = 0; i < n; i++) { r[i] = ds[i] * (f[i] + tmp[i]); }
+   for (int i = 0; i < n; i++) { o[i] = u[i]; u[i] = r[i] * coefs[co]; }
+   for (int k = co - 1; k >= 0; k--)
+   {
+      for (int i = 0; i < n; i++) { tmp[i] = ds[i] * u[i]; }
+      or_matvec(1.0, A, tmp, 0.0, NULL, v);
+      for (int i = 0; i < n; i++) { u[i] = coefs[k] * r[i] + ds[i] * v[i]; }
+   }
+   for (int i = 0; i < n; i++) { u[i] = o[i] + ds[i] * u[i]; }
+}
+
 static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u, int u_zero)
 {
    const or_csr *A = &H->A[lvl];
    double w = H->prm.relax_weight;
+   if (type == 16)
+   {
+      int n = A->nr;
+      double *r = xmalloc(sizeof(double) * (n ? n : 1)), *o = xmalloc(sizeof(double) * (n ? n : 1));
+      double *tmp = xmalloc(sizeof(double) * (n ? n : 1));
+      relax_cheby(A, f, H->cheby_ds[lvl], H->cheby_coefs[lvl], H->prm.cheby_order, H->prm.cheby_scale, u, r, o,
+                  H->Vtmp, tmp);
+      free(r); free(o); free(tmp);
+      return;
+   }
    if (type == 18 || type == 7)
    {
       relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero);
@@ -1268,6 +1565,24 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
    }
    H->Vtmp = xcalloc(H->A[0].nr, sizeof(double));
    H->Ztmp = xcalloc(H->A[0].nr, sizeof(double));
+   /* Chebyshev data per level (par_amg_setup.c:3496-3536) */
+   H->cheby_coefs = xcalloc(nl, sizeof(double *));
+   H->cheby_ds = xcalloc(nl, sizeof(double *));
+   H->cheby_eig = xcalloc(2 * nl, sizeof(double));
+   for (int l = 0; l < nl; l++)
+   {
+      if (prm->relax_down == 16 || prm->relax_up == 16 || (prm->relax_coarse == 16 && l == nl - 1))
+      {
+         double mx = 0.0, mn = 0.0;
+         if (prm->cheby_eig_est > 0) { or_max_eig_cg(&H->A[l], prm->cheby_scale, prm->cheby_eig_est, &mx, &mn); }
+         H->cheby_eig[2 * l] = mx;
+         H->cheby_eig[2 * l + 1] = mn;
+         H->cheby_coefs[l] = xcalloc(5, sizeof(double));
+         H->cheby_ds[l] = xmalloc(sizeof(double) * (H->A[l].nr ? H->A[l].nr : 1));
+         or_cheby_setup(&H->A[l], mx, mn, prm->cheby_fraction, prm->cheby_order, prm->cheby_scale,
+                        prm->cheby_variant, H->cheby_coefs[l], H->cheby_ds[l]);
+      }
+   }
    /* coarse dense matrix (hypre_GaussElimSetup par_gauss_elim.c:33) */
    if (prm->relax_coarse == 9 || prm->relax_coarse == 99 || prm->relax_coarse == 19 || prm->relax_coarse == 98)
    {
@@ -1289,6 +1604,11 @@ void or_amg_free(or_hierarchy *H)
       if (l < H->num_levels - 1) { or_csr_free(&H->P[l]); or_csr_free(&H->S[l]); free(H->CF[l]); }
       free(H->l1[l]); free(H->F[l]); free(H->U[l]);
    }
+   if (H->cheby_coefs)
+   {
+      for (int l = 0; l < H->num_levels; l++) { free(H->cheby_coefs[l]); free(H->cheby_ds[l]); }
+   }
+   free(H->cheby_coefs); free(H->cheby_ds); free(H->cheby_eig);
    free(H->A); free(H->P); free(H->S); free(H->CF); free(H->l1); free(H->F); free(H->U);
    free(H->Vtmp); free(H->Ztmp); free(H->coarse_lu);
    memset(H, 0, sizeof(*H));
@@ -1533,6 +1853,9 @@ int or_h_csr(const or_hierarchy *H, int which, int l, int *nr, int *nc, int **i,
 }
 int *or_h_cf(const or_hierarchy *H, int l) { return H->CF[l]; }
 double *or_h_l1(const or_hierarchy *H, int l) { return H->l1[l]; }
+double *or_h_cheby_coefs(const or_hierarchy *H, int l) { return H->cheby_coefs ? H->cheby_coefs[l] : NULL; }
+double *or_h_cheby_ds(const or_hierarchy *H, int l) { return H->cheby_ds ? H->cheby_ds[l] : NULL; }
+double *or_h_cheby_eig(const or_hierarchy *H) { return H->cheby_eig; }
 
 int or_setup_flat(int n, const int *Ai, const int *Aj, const double *Av, const or_amg_params *prm, or_hierarchy *H)
 {

@@ -63,7 +63,8 @@ typedef struct
    int    **CF;           /* num_levels-1 */
    double **l1;           /* num_levels (l1 norms or diagonal, per the smoother) */
    double **cheby_coefs;  /* num_levels, order+1 coefficients */
-   double **cheby_ds;     /* num_levels, D^{-1/2} scaling */
+   double **cheby_ds;     /* num_levels, D^{-1/2} scaling (ones when cheby_scale is 0) */
+   double  *cheby_eig;    /* 2 per level: max, min eigenvalue estimates */
    double  *coarse_lu;    /* dense n_c x n_c row-major copy of the coarsest matrix */
    int      coarse_n;
    or_amg_params prm;
@@ -95,6 +96,10 @@ int    or_strength2(const or_csr *S, int *CF, int num_paths, or_csr *S2);
 void   or_correct_cf2(int n, int *CF, const int *CFN);
 int    or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P);
 int    or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
+int    or_eig_tridiag(int n, double *d, double *e);
+int    or_max_eig_cg(const or_csr *A, int scale, int max_iter, double *max_eig, double *min_eig);
+int    or_cheby_setup(const or_csr *A, double max_eig, double min_eig, double fraction, int order,
+                      int scale, int variant, double *coefs, double *ds);
 
 /* hierarchy */
 int    or_amg_setup(const or_csr *A, const or_amg_params *prm, or_hierarchy *H);

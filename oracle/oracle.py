@@ -50,6 +50,14 @@ def lib():
         L.or_h_cf.restype = P(C.c_int)
         L.or_h_l1.argtypes = [C.c_void_p, C.c_int]
         L.or_h_l1.restype = P(C.c_double)
+        for nm in ("or_h_cheby_coefs", "or_h_cheby_ds"):
+            getattr(L, nm).argtypes = [C.c_void_p, C.c_int]
+            getattr(L, nm).restype = P(C.c_double)
+        L.or_h_cheby_eig.argtypes = [C.c_void_p]
+        L.or_h_cheby_eig.restype = P(C.c_double)
+        L.or_eig_tridiag.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+        L.or_max_eig_cg.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                    P(C.c_double), P(C.c_double)]
         L.or_setup_flat.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, P(Params), C.c_void_p]
         L.or_pcg_flat.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_double, C.c_int, C.c_void_p, P(C.c_int)]
@@ -147,6 +155,19 @@ class Hierarchy:
         n = self.csr("A", level)[0].shape[0] - 1
         return np.ctypeslib.as_array(lib().or_h_l1(self.h, level), (n,)).copy()
 
+    def cheby(self, level, order):
+        """(coefficients, (max_eig, min_eig), D^{-1/2} scaling) of a level, or None."""
+        L = lib()
+        pc = L.or_h_cheby_coefs(self.h, level)
+        if not pc:
+            return None
+        n = self.csr("A", level)[0].shape[0] - 1
+        order = min(max(order, 1), 4)
+        coefs = np.ctypeslib.as_array(pc, (order,)).copy()
+        ds = np.ctypeslib.as_array(L.or_h_cheby_ds(self.h, level), (n,)).copy()
+        eig = np.ctypeslib.as_array(L.or_h_cheby_eig(self.h), (2 * self.num_levels,))
+        return coefs, (float(eig[2 * level]), float(eig[2 * level + 1])), ds
+
     def pcg(self, b, tol=1e-8, maxit=100):
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = np.zeros(self.n)
@@ -170,6 +191,16 @@ class Hierarchy:
         u = np.zeros(self.n)
         lib().or_vcycle_flat(self.h, f.ctypes.data, u.ctypes.data)
         return u
+
+
+def eig_tridiag(d, e):
+    """Eigenvalues (ascending) of the symmetric tridiagonal (d, e[1:]) by TQL1."""
+    d = np.ascontiguousarray(d, dtype=np.float64).copy()
+    e = np.ascontiguousarray(e, dtype=np.float64).copy()
+    err = lib().or_eig_tridiag(len(d), d.ctypes.data, e.ctypes.data)
+    if err:
+        raise RuntimeError("tridiagonal QL did not converge")
+    return d
 
 
 def read_records(path):

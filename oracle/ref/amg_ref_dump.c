@@ -366,6 +366,24 @@ int main(int argc, char **argv)
             hypre_ParCSRMatrixDestroy(S);
          }
       }
+      /* Chebyshev smoother data (relax 16): eigenvalue estimates, coefficients, D^{-1/2} */
+      HYPRE_Real **coefs = hypre_ParAMGDataChebyCoefs(amg_data);
+      if (coefs && coefs[l])
+      {
+         char nm[32];
+         int ord = cheby_order < 1 ? 1 : (cheby_order > 4 ? 4 : cheby_order);
+         snprintf(nm, 32, "CHEB_COEF%d", l);
+         rec(nm, 1, ord, coefs[l]);
+         double eig[2] = {hypre_ParAMGDataMaxEigEst(amg_data)[l], hypre_ParAMGDataMinEigEst(amg_data)[l]};
+         snprintf(nm, 32, "CHEB_EIG%d", l);
+         rec(nm, 1, 2, eig);
+         hypre_Vector **ds = hypre_ParAMGDataChebyDS(amg_data);
+         if (ds && ds[l] && hypre_VectorData(ds[l]))
+         {
+            snprintf(nm, 32, "CHEB_DS%d", l);
+            rec(nm, 1, lev_rows[l], hypre_VectorData(ds[l]));
+         }
+      }
       hypre_Vector **l1 = hypre_ParAMGDataL1Norms(amg_data);
       if (l1 && l1[l])
       {

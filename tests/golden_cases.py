@@ -1,0 +1,110 @@
+"""Golden fixtures written by tests/golden/make_golden.py from the reference
+library (compiled from its own sources) and the checks that compare a
+hierarchy -- the oracle's or the GPU's -- against them."""
+import glob
+import hashlib
+import json
+import os
+
+import numpy as np
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def case_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+
+
+def load(name):
+    d = dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+    d["case"] = json.loads(str(d["case"]))
+    return d
+
+
+def oracle_params(c):
+    """or_amg_params keyword arguments of a golden case."""
+    p = dict(strong_threshold=c["th"], max_row_sum=c["mxrs"], p_max_elmts=c["Pmx"],
+             trunc_factor=c.get("tr", 0.0), agg_num_levels=c.get("agg_nl", 0),
+             agg_interp_type=c.get("agg_interp", 4), relax_down=c["rlx"], relax_up=c["rlx"], relax_coarse=9,
+             max_coarse_size=c["coarse_th"])
+    if "cheby_order" in c:
+        p["cheby_order"] = c["cheby_order"]
+    return p
+
+
+def amg_params(c):
+    """HYPRE_BoomerAMGSet* values of a golden case."""
+    p = dict(StrongThreshold=c["th"], MaxRowSum=c["mxrs"], PMaxElmts=c["Pmx"], TruncFactor=c.get("tr", 0.0),
+             AggNumLevels=c.get("agg_nl", 0), RelaxType=c["rlx"], MaxCoarseSize=c["coarse_th"])
+    if c.get("agg_nl", 0):
+        p["AggInterpType"] = c.get("agg_interp", 4)
+    if "cheby_order" in c:
+        p["ChebyOrder"] = c["cheby_order"]
+    return p
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def check_array(g, key, a, rtol=0.0):
+    """a against the golden record key: exact for integers; floats exact when
+    rtol is 0, else to rtol relative (checksums and a seeded sample for the
+    large cases)."""
+    a = np.asarray(a)
+    if key in g:
+        ref = g[key]
+        assert a.shape == ref.shape, f"{key}: {a.shape} vs {ref.shape}"
+        if ref.dtype == np.int32 or rtol == 0.0:
+            assert np.array_equal(a, ref), f"{key} differs"
+        else:
+            np.testing.assert_allclose(a, ref, rtol=rtol, atol=0, err_msg=key)
+        return
+    if ("sha256:" + key) in g:
+        assert len(a) == int(g["len:" + key]), f"{key} length"
+        assert _digest(a.astype(np.int32)) == str(g["sha256:" + key]), f"{key} digest"
+        return
+    if ("sum:" + key) in g:
+        idx = g["sample_idx:" + key]
+        if rtol == 0.0:
+            assert np.array_equal(a[idx], g["sample:" + key]), f"{key} sample"
+        else:
+            np.testing.assert_allclose(a[idx], g["sample:" + key], rtol=rtol, atol=0, err_msg=key)
+        np.testing.assert_allclose(np.sum(np.abs(a)), float(g["abssum:" + key]), rtol=max(rtol, 1e-13), atol=0,
+                                   err_msg=key + " abs checksum")
+        return
+    raise KeyError(key)
+
+
+def has(g, key):
+    return key in g or ("sha256:" + key) in g or ("sum:" + key) in g
+
+
+def check_hierarchy(g, num_levels, csr, cf, l1, cheby=None, value_rtol=0.0, cheby_rtol=0.0):
+    """Compares a hierarchy given by accessor functions with the golden case:
+    csr(which, level) -> (I, J, V), cf(level), l1(level), cheby(level, order) ->
+    (coefs, (max_eig, min_eig), ds)."""
+    c = g["case"]
+    assert num_levels == int(g["nlev"][0]), "number of levels"
+    for l in range(num_levels):
+        I, J, V = csr("A", l)
+        check_array(g, f"A{l}_i", I)
+        check_array(g, f"A{l}_j", J)
+        check_array(g, f"A{l}_v", V, value_rtol)
+        if has(g, f"L1_{l}"):
+            check_array(g, f"L1_{l}", l1(l), value_rtol)
+        if l < num_levels - 1:
+            I, J, V = csr("P", l)
+            check_array(g, f"P{l}_i", I)
+            check_array(g, f"P{l}_j", J)
+            check_array(g, f"P{l}_v", V, value_rtol)
+            check_array(g, f"CF{l}", cf(l))
+            if has(g, f"S{l}_i"):
+                I, J, _ = csr("S", l)
+                check_array(g, f"S{l}_i", I)
+                check_array(g, f"S{l}_j", J)
+        if cheby is not None and has(g, f"CHEB_COEF{l}"):
+            co, eig, ds = cheby(l, c["cheby_order"])
+            check_array(g, f"CHEB_DS{l}", ds)
+            check_array(g, f"CHEB_EIG{l}", np.array(eig), cheby_rtol)
+            check_array(g, f"CHEB_COEF{l}", co, cheby_rtol * 10)
