@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--n", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=80)
+    ap.add_argument("--spmv-only", action="store_true",
+                    help="only the level-0 FP64 SpMV loop of the roofline measurement (for profiling)")
     return ap.parse_args()
 
 
@@ -143,6 +145,14 @@ def gpu_arm(args):
     L.HYPRE_ParVectorCreate(0, n, None, C.byref(bv)); L.HYPRE_ParVectorInitialize(bv)
     L.HYPRE_ParVectorCreate(0, n, None, C.byref(xv)); L.HYPRE_ParVectorInitialize(xv)
     L.HYPRE_GB300_ParVectorCopyFromHost(bv, b.ctypes.data, n)
+
+    if args.spmv_only:
+        yv = C.c_void_p(); L.HYPRE_ParVectorCreate(0, n, None, C.byref(yv)); L.HYPRE_ParVectorInitialize(yv)
+        for _ in range(args.warmup + args.steps):
+            gb.check(L.HYPRE_ParCSRMatrixMatvec(1.0, A, bv, 0.0, yv), "matvec")
+        torch.cuda.synchronize()
+        print(json.dumps({"spmv_only": True, "launches": args.warmup + args.steps}))
+        return
 
     def make_solver(prec):
         amg = C.c_void_p()
