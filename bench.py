@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--cpu-sample-n", type=int, default=80)
     ap.add_argument("--spmv-only", action="store_true",
                     help="only the level-0 FP64 SpMV loop of the roofline measurement (for profiling)")
+    ap.add_argument("--workload", default="laplace27_160",
+                    choices=["laplace27_160", "batch512", "multi64", "learned128", "fv256"],
+                    help="laplace27_160: the headline line; the others measure the batched, multi-RHS, "
+                         "learned-parameter and mixed-precision FV configurations")
     return ap.parse_args()
 
 
@@ -350,9 +354,186 @@ def reference_arm(args):
                       "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+# ---------------------------------------------------------------------------
+# further configurations (one JSON line each, not part of the default run)
+# ---------------------------------------------------------------------------
+def _timed_steps(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts)), ts
+
+
+def _line(metric, value, unit, args, config, dtype, extra):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": value * 1e3 if unit == "s" else None, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded generator)",
+           "config": config}
+    out.update(extra)
+    print(json.dumps(out))
+
+
+def suite_arm(args):
+    import torch
+    import hypre_gb300 as gb
+    from hypre_gb300 import problems as G
+    L = gb.lib()
+    L.HYPRE_Initialize()
+    csr = lambda I, J, V: __import__("scipy.sparse", fromlist=["csr_matrix"]).csr_matrix(
+        (V, J, I), shape=(len(I) - 1, len(I) - 1))
+    if args.workload == "batch512":
+        I, J, V, off, ns, eps = G.aniso2d_batch(512, seed=11)
+        n = len(I) - 1
+        A = gb.IJMatrix(I, J, V)
+        b = G.rhs(n, normalise=False)
+        bv, xv = gb.IJVector(n, b), gb.IJVector(n, np.zeros(n))
+        amg = gb.BoomerAMG(StrongThreshold=0.25, RelaxType=18, Tol=0.0, MaxIter=1)
+        bp = gb.BatchedPCG(amg, tol=1e-8, maxit=200, prec=1)
+        bp.setup(A, off)
+        bp.solve(bv, xv)      # autotunes the kernel shape
+
+        def step():
+            bp.setup(A, off)
+            xv.set(np.zeros(n))
+            L.HYPRE_GB300_ResetKernelLaunchCount()
+            bp.solve(bv, xv)
+
+        t, _ = _timed_steps(step, args.steps, args.warmup)
+        ts, _ = _timed_steps(lambda: bp.solve(bv, xv), args.steps, 1)
+        r = b - csr(I, J, V) @ xv.values()
+        worst = max(np.linalg.norm(r[off[s]:off[s + 1]]) / np.linalg.norm(b[off[s]:off[s + 1]]) for s in range(512))
+        _line("batched AMG-PCG setup+solve s, 512 systems to rel-res 1e-8", t, "s", args,
+              {"workload": "aniso2d_batch512", "systems": 512, "n_range": [16, 128], "eps": "log-uniform [1e-3, 1]",
+               "unknowns": n, "nnz": len(J), "cycle": "FP32 V-cycle, l1-Jacobi, inside FP64 PCG"},
+              "f64 Krylov / f32 V-cycle",
+              {"solve_seconds": ts, "setup_seconds": t - ts, "iterations_max": int(bp.iterations().max()),
+               "iterations_mean": float(bp.iterations().mean()), "worst_true_relres": float(worst),
+               "kernel_shape": list(bp.shape()), "tuning_ms": bp.tuning_times().tolist(),
+               "gpu_launches_solve": 1})
+    elif args.workload == "multi64":
+        n1, nv = args.n, 64
+        I, J, V = G.laplace(27, n1, n1, n1)
+        n = len(I) - 1
+        B = np.random.default_rng(22775).uniform(-1.0, 1.0, (n, nv))
+        A = gb.IJMatrix(I, J, V)
+        amg = gb.BoomerAMG(MaxRowSum=1.0, StrongThreshold=0.5, AggNumLevels=1, AggInterpType=6, RelaxType=18,
+                           Tol=0.0, MaxIter=1)
+        amg.set("CyclePrecision", 1)
+        k = gb.Krylov("pcg", tol=1e-8, maxit=200, amg=amg)
+        b1, x1 = gb.IJVector(n, B[:, 0]), gb.IJVector(n, np.zeros(n))
+        k.setup(A, b1, x1)
+        Bm, Xm = gb.MultiVector(B), gb.MultiVector(np.zeros((n, nv)))
+
+        def multi():
+            Xm.set(np.zeros((n, nv)))
+            L.HYPRE_ParCSRPCGSolve(k.h, A.par, Bm.par, Xm.par)
+
+        t_multi, _ = _timed_steps(multi, args.steps, args.warmup)
+        its, rel, _ = gb.multi_results(k, nv, 200)
+
+        def single():
+            x1.set(np.zeros(n))
+            k.solve(A, b1, x1)
+
+        t_single, _ = _timed_steps(single, args.steps, args.warmup)
+        R = B - csr(I, J, V) @ Xm.values()
+        worst = float(np.max(np.linalg.norm(R, axis=0) / np.linalg.norm(B, axis=0)))
+        _line("AMG-PCG solve s for 64 right-hand sides to rel-res 1e-8", t_multi, "s", args,
+              {"workload": f"laplace27_{n1}_64rhs", "unknowns": n, "nnz": len(J), "rhs": nv,
+               "amg": "aggressive level 0, PMIS 0.5, l1-Jacobi, FP32 SpMM V-cycle"},
+              "f64 Krylov / f32 V-cycle",
+              {"single_rhs_solve_seconds": t_single, "sequential_64_estimate_seconds": 64 * t_single,
+               "speedup_vs_sequential": 64 * t_single / t_multi, "iterations_max": int(its.max()),
+               "worst_true_relres": worst})
+    elif args.workload == "fv256":
+        n1 = args.n if args.n != 160 else 256
+        I, J, V = G.fv_diffusion(n1, seed=0)
+        n = len(I) - 1
+        b = G.rhs(n)
+        A = gb.IJMatrix(I, J, V)
+        res = {}
+        for label, prec in (("fp64", 0), ("fp32", 1), ("fp16_finest", 2)):
+            amg = gb.BoomerAMG(StrongThreshold=0.25, RelaxType=18, Tol=0.0, MaxIter=1)
+            amg.set("CyclePrecision", prec)
+            k = gb.Krylov("fgmres", tol=1e-8, maxit=300, kdim=30, amg=amg)
+            bv, xv = gb.IJVector(n, b), gb.IJVector(n, np.zeros(n))
+
+            def step():
+                xv.set(np.zeros(n))
+                k.setup(A, bv, xv)
+                k.solve(A, bv, xv)
+
+            t, _ = _timed_steps(step, args.steps, args.warmup)
+            r = b - csr(I, J, V) @ xv.values()
+            res[label] = {"seconds": t, "iterations": k.iterations(),
+                          "true_relres": float(np.linalg.norm(r) / np.linalg.norm(b))}
+        _line("AMG-FGMRES(30) setup+solve s to rel-res 1e-8, FV diffusion", res["fp32"]["seconds"], "s", args,
+              {"workload": f"fv_diffusion_{n1}", "unknowns": n, "nnz": len(J),
+               "coefficients": "log-normal sigma 2, 8^3 blocks x 10^+-4, harmonic faces"},
+              "f64 Krylov / f32 V-cycle", {"variants": res})
+    elif args.workload == "learned128":
+        from hypre_gb300 import learned
+        t0 = time.perf_counter()
+        I, J, V, off, eps, ang = learned.make_problems(2000, n=10, seed=7)
+        cost, its, labels, shape = learned.sweep_labels(I, J, V, off)
+        t_sweep = time.perf_counter() - t0
+        A = gb.IJMatrix(I, J, V)
+        X = learned.features(A)
+        T = torch.tensor(learned.row_targets(off, labels), device="cuda")
+        t0 = time.perf_counter()
+        params, hist = learned.train(X, T, steps=400, lr=3e-3)
+        t_train = time.perf_counter() - t0
+        solver = learned.LearnedSolver(params, judge_iters=4)
+        rng = np.random.default_rng(123)
+        rows = []
+        for q in range(4):
+            e = float(np.exp(rng.uniform(np.log(1e-4), 0.0)))
+            a = rng.uniform(0, 2 * np.pi, 3)
+            I2, J2, V2 = G.rotated_aniso3d(args.n if args.n != 160 else 128, e, a)
+            n = len(I2) - 1
+            A2 = gb.IJMatrix(I2, J2, V2)
+            b = G.rhs(n)
+            bv, xv = gb.IJVector(n, b), gb.IJVector(n, np.zeros(n))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = solver.solve(A2, bv, xv, key=None)
+            torch.cuda.synchronize()
+            t_l = time.perf_counter() - t0
+            amg = gb.BoomerAMG(StrongThreshold=0.25, RelaxType=18, Tol=0.0, MaxIter=1)
+            amg.set("CyclePrecision", 1)
+            k = gb.Krylov("pcg", tol=1e-8, maxit=300, amg=amg)
+            xv.set(np.zeros(n))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            k.setup(A2, bv, xv)
+            k.solve(A2, bv, xv)
+            torch.cuda.synchronize()
+            t_d = time.perf_counter() - t0
+            rows.append({"eps": e, "learned_seconds_with_judge": t_l, "default_seconds": t_d,
+                         "learned_iterations": out["iterations"], "default_iterations": k.iterations(),
+                         "used": out["used"], "theta": out["theta"], "weights": out["weights"],
+                         "factor_learned": out["factor_learned"], "factor_default": out["factor_default"]})
+        _line("AMG-PCG s to rel-res 1e-8 with learned parameters, rotated anisotropic 128^3",
+              float(np.mean([r["learned_seconds_with_judge"] for r in rows])), "s", args,
+              {"workload": "rotated_aniso_128", "training_problems": 2000, "training_grid": "10^3 7-point",
+               "sweep": {"theta": list(learned.THETAS), "weight": list(learned.WEIGHTS)}},
+              "bf16 MLP / f64 Krylov / f32 V-cycle",
+              {"default_seconds_mean": float(np.mean([r["default_seconds"] for r in rows])),
+               "sweep_seconds": t_sweep, "train_seconds": t_train, "final_loss": hist[-1][1], "problems": rows})
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         reference_arm(a)
+    elif a.workload != "laplace27_160":
+        suite_arm(a)
     else:
         gpu_arm(a)

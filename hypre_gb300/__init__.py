@@ -85,6 +85,27 @@ def _declare(L):
         "HYPRE_GB300_GetKernelLaunchCount": [P(C.c_longlong)], "HYPRE_GB300_ResetKernelLaunchCount": [],
         "HYPRE_GB300_BoomerAMGGetSetupTimes": [vp, vp, i32],
         "HYPRE_GB300_BoomerAMGSetCyclePrecision": [vp, i32], "HYPRE_GB300_BoomerAMGSetUseGraph": [vp, i32],
+        "HYPRE_GB300_BatchedPCGCreate": [P(vp)], "HYPRE_GB300_BatchedPCGDestroy": [vp],
+        "HYPRE_GB300_BatchedPCGSetTol": [vp, f64], "HYPRE_GB300_BatchedPCGSetMaxIter": [vp, i32],
+        "HYPRE_GB300_BatchedPCGSetCyclePrecision": [vp, i32],
+        "HYPRE_GB300_BatchedPCGSetKernelShape": [vp, i32, i32], "HYPRE_GB300_BatchedPCGSetAutotune": [vp, i32],
+        "HYPRE_GB300_BatchedPCGGetKernelShape": [vp, P(i32), P(i32)],
+        "HYPRE_GB300_BatchedPCGGetTuningTimes": [vp, vp],
+        "HYPRE_GB300_BatchedPCGSetup": [vp, vp, vp, i32, vp], "HYPRE_GB300_BatchedPCGSolve": [vp, vp, vp],
+        "HYPRE_GB300_BatchedPCGGetNumIterations": [vp, vp],
+        "HYPRE_GB300_BatchedPCGGetFinalRelativeResidualNorms": [vp, vp],
+        "HYPRE_GB300_BatchedPCGGetResidualHistory": [vp, i32, i32, vp, P(i32)],
+        "HYPRE_GB300_BatchedPCGGetLevelOffsets": [vp, i32, vp],
+        "HYPRE_GB300_BatchedPCGGetOperatorComplexities": [vp, vp],
+        "HYPRE_GB300_ParVectorCreateMulti": [i32, i32, P(vp)],
+        "HYPRE_GB300_KrylovGetMultiNumIterations": [vp, vp],
+        "HYPRE_GB300_KrylovGetMultiFinalRelativeResidualNorms": [vp, vp],
+        "HYPRE_GB300_KrylovGetMultiResidualHistory": [vp, i32, i32, vp, P(i32)],
+        "HYPRE_GB300_MLPNumParams": [P(i32)], "HYPRE_GB300_BoomerAMGSetLearnedModel": [vp, vp],
+        "HYPRE_GB300_BoomerAMGGetLearnedParams": [vp, P(f64), vp, i32],
+        "HYPRE_GB300_MLPRowFeatures": [vp, vp], "HYPRE_GB300_MLPForward": [i32, vp, vp, vp],
+        "HYPRE_GB300_MLPGradient": [i32, vp, vp, vp, vp, vp],
+        "HYPRE_GB300_MLPAdamStep": [vp, vp, vp, vp, f64, i32],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -342,3 +363,112 @@ def kernel_launches():
     c = C.c_longlong()
     lib().HYPRE_GB300_GetKernelLaunchCount(C.byref(c))
     return c.value
+
+
+class BatchedPCG:
+    """HYPRE_GB300_BatchedPCG*: independent systems (diagonal blocks of one
+    matrix) solved by FP64 PCG with a BoomerAMG V-cycle, one persistent launch."""
+
+    def __init__(self, amg, tol=1e-8, maxit=100, prec=1, shape=None):
+        L = lib()
+        self.amg = amg
+        self.h = C.c_void_p()
+        check(L.HYPRE_GB300_BatchedPCGCreate(C.byref(self.h)), "BatchedPCGCreate")
+        L.HYPRE_GB300_BatchedPCGSetTol(self.h, tol)
+        L.HYPRE_GB300_BatchedPCGSetMaxIter(self.h, maxit)
+        L.HYPRE_GB300_BatchedPCGSetCyclePrecision(self.h, prec)
+        self.maxit = maxit
+        if shape is not None:
+            check(L.HYPRE_GB300_BatchedPCGSetKernelShape(self.h, shape[0], shape[1]), "shape")
+
+    def setup(self, A, offsets):
+        self.off = np.ascontiguousarray(offsets, np.int32)
+        self.nsys = len(self.off) - 1
+        check(lib().HYPRE_GB300_BatchedPCGSetup(self.h, self.amg.h, A.par, self.nsys, self.off.ctypes.data),
+              "BatchedPCGSetup")
+
+    def solve(self, b, x):
+        return lib().HYPRE_GB300_BatchedPCGSolve(self.h, b.par, x.par)
+
+    def iterations(self):
+        out = np.zeros(self.nsys, np.int32)
+        lib().HYPRE_GB300_BatchedPCGGetNumIterations(self.h, out.ctypes.data)
+        return out
+
+    def relres(self):
+        out = np.zeros(self.nsys)
+        lib().HYPRE_GB300_BatchedPCGGetFinalRelativeResidualNorms(self.h, out.ctypes.data)
+        return out
+
+    def history(self, s):
+        out = np.zeros(self.maxit + 1)
+        n = C.c_int()
+        lib().HYPRE_GB300_BatchedPCGGetResidualHistory(self.h, s, self.maxit + 1, out.ctypes.data, C.byref(n))
+        return out[: n.value]
+
+    def level_offsets(self, level):
+        out = np.zeros(self.nsys + 1, np.int32)
+        check(lib().HYPRE_GB300_BatchedPCGGetLevelOffsets(self.h, level, out.ctypes.data), "offsets")
+        return out
+
+    def complexities(self):
+        out = np.zeros(self.nsys)
+        check(lib().HYPRE_GB300_BatchedPCGGetOperatorComplexities(self.h, out.ctypes.data), "complexities")
+        return out
+
+    def shape(self):
+        a, b = C.c_int(), C.c_int()
+        lib().HYPRE_GB300_BatchedPCGGetKernelShape(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def tuning_times(self):
+        out = np.zeros(12)
+        lib().HYPRE_GB300_BatchedPCGGetTuningTimes(self.h, out.ctypes.data)
+        return out.reshape(4, 3)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().HYPRE_GB300_BatchedPCGDestroy(self.h)
+            self.h = None
+
+
+class MultiVector:
+    """HYPRE_GB300_ParVectorCreateMulti: n x nv values, interleaved by row."""
+
+    def __init__(self, values):
+        values = np.ascontiguousarray(values, np.float64)
+        self.n, self.nv = values.shape
+        self.par = C.c_void_p()
+        check(lib().HYPRE_GB300_ParVectorCreateMulti(self.n, self.nv, C.byref(self.par)), "CreateMulti")
+        self.set(values)
+
+    def set(self, values):
+        v = np.ascontiguousarray(values, np.float64)
+        check(lib().HYPRE_GB300_ParVectorCopyFromHost(self.par, v.ctypes.data, self.n * self.nv), "copy")
+
+    def values(self):
+        out = np.empty((self.n, self.nv))
+        check(lib().HYPRE_GB300_ParVectorCopyToHost(self.par, out.ctypes.data, self.n * self.nv), "copy")
+        return out
+
+    def __del__(self):
+        if getattr(self, "par", None):
+            lib().HYPRE_ParVectorDestroy(self.par)
+            self.par = None
+
+
+def multi_results(krylov, nv, maxit):
+    """Per-column iterations, final relative residuals and histories of a
+    multi-vector PCG solve."""
+    L = lib()
+    its = np.zeros(nv, np.int32)
+    rel = np.zeros(nv)
+    L.HYPRE_GB300_KrylovGetMultiNumIterations(krylov.h, its.ctypes.data)
+    L.HYPRE_GB300_KrylovGetMultiFinalRelativeResidualNorms(krylov.h, rel.ctypes.data)
+    hist = []
+    for c in range(nv):
+        h = np.zeros(maxit + 1)
+        m = C.c_int()
+        L.HYPRE_GB300_KrylovGetMultiResidualHistory(krylov.h, c, maxit + 1, h.ctypes.data, C.byref(m))
+        hist.append(h[: m.value])
+    return its, rel, hist

@@ -80,6 +80,7 @@ static void level_free_vectors(gb_level *L)
 static void amg_free_hierarchy(gb_amg *amg)
 {
    if (amg->graph) { cudaGraphExecDestroy(amg->graph); amg->graph = NULL; }
+   gb_multi_free(amg);
    for (int l = 0; l < amg->num_levels; l++)
    {
       gb_level *L = &amg->lev[l];
@@ -812,11 +813,29 @@ static void cheby_level_setup(gb_amg *amg, int l)
    cheby_coefs(mx, mn, prm->cheby_fraction, order, prm->cheby_variant, L->cheb_c);
 }
 
+static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0);
+
+/* With a learned model the strength threshold of this setup is the model's
+ * prediction from the finest level's rows; the user's value is kept. */
 int gb_amg_setup(gb_amg *amg, gb_parcsr *A0)
+{
+   double user_theta = amg->prm.strong_threshold;
+   if (amg->mlp_params)
+   {
+      amg_free_hierarchy(amg);
+      if (gb_learn_theta(amg, A0, &amg->prm.strong_threshold)) { return gb_error_flag; }
+   }
+   int r = amg_setup_inner(amg, A0);
+   amg->prm.strong_threshold = user_theta;
+   return r;
+}
+
+static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
 {
    amg_free_hierarchy(amg);
    gb_amg_params *prm = &amg->prm;
    double t_start = gb_wtime();
+
    memset(amg->setup_times, 0, sizeof(amg->setup_times));
    amg->lev[0].A = A0;
    amg->lev[0].n = A0->A.nr;
@@ -883,6 +902,7 @@ int gb_amg_setup(gb_amg *amg, gb_parcsr *A0)
       if (vp0 != GB_PREC_F64) { gb_solve_desc(L->A, GB_PREC_F64); }
       if (L->P) { gb_solve_desc(L->P, vp); gb_solve_desc(L->R, vp); }
    }
+   if (amg->mlp_params && gb_learn_weights(amg)) { return gb_error_flag; }
    /* Chebyshev data on the levels that relax with it (par_amg_setup.c:3496-3536) */
    for (int l = 0; l < amg->num_levels; l++)
    {
@@ -1220,6 +1240,7 @@ HYPRE_Int HYPRE_BoomerAMGDestroy(HYPRE_Solver solver)
    gb_amg *a = (gb_amg *) solver;
    if (!a || a->magic != GB_MAGIC_AMG) { return gb_error_flag; }
    amg_free_hierarchy(a);
+   gb_dfree(a->mlp_params);
    free(a->prm.level_relax_weight);
    a->magic = 0;
    free(a);

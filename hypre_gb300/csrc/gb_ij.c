@@ -246,7 +246,7 @@ HYPRE_Int HYPRE_GB300_ParVectorGetDevicePointer(HYPRE_ParVector v, void **dptr, 
 HYPRE_Int HYPRE_GB300_ParVectorCopyFromHost(HYPRE_ParVector v, const HYPRE_Real *h, HYPRE_Int n)
 {
    if (!check_vec(v, 1)) { return gb_error_flag; }
-   if (n != v->n || !h) { gb_error_in_arg(3); return gb_error_flag; }
+   if ((long long) n != (long long) v->n * v->num_vectors || !h) { gb_error_in_arg(3); return gb_error_flag; }
    cudaMemcpyAsync(v->d, h, sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, gb_stream());
    gb_sync();
    return gb_error_flag;
@@ -255,7 +255,7 @@ HYPRE_Int HYPRE_GB300_ParVectorCopyFromHost(HYPRE_ParVector v, const HYPRE_Real 
 HYPRE_Int HYPRE_GB300_ParVectorCopyToHost(HYPRE_ParVector v, HYPRE_Real *h, HYPRE_Int n)
 {
    if (!check_vec(v, 1)) { return gb_error_flag; }
-   if (n != v->n || !h) { gb_error_in_arg(3); return gb_error_flag; }
+   if ((long long) n != (long long) v->n * v->num_vectors || !h) { gb_error_in_arg(3); return gb_error_flag; }
    cudaMemcpyAsync(h, v->d, sizeof(double) * (size_t) n, cudaMemcpyDeviceToHost, gb_stream());
    gb_sync();
    return gb_error_flag;

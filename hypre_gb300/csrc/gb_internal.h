@@ -45,6 +45,7 @@ void  gb_release_scratch(void);
 #define GB_MAGIC_PCG 0x50434731
 #define GB_MAGIC_GMR 0x474d5231
 #define GB_MAGIC_DS  0x44534331
+#define GB_MAGIC_BAT 0x42415431
 
 typedef struct
 {
@@ -160,9 +161,19 @@ typedef struct
    void         *graph_u;
    int           graph_prec;
    double       *r_work;        /* FP64 residual for stand-alone solve */
+   /* learned parameters: MLP weights (device FP32) and what they predicted */
+   float        *mlp_params;
+   double        learned_theta;
+   double        learned_w[32];
+   void         *multi_ws;      /* multi-vector cycle work space (gb_multi.c) */
 } gb_amg;
 
 int gb_amg_cycle(gb_amg *amg, const double *f, double *u);   /* one V-cycle, u from zero */
+int gb_amg_setup(gb_amg *amg, gb_parcsr *A0);
+/* learned parameters (gb_learn.c): strength threshold from the finest level's
+ * rows before coarsening, smoother weight per level after the hierarchy */
+int gb_learn_theta(gb_amg *amg, gb_parcsr *A0, double *theta);
+int gb_learn_weights(gb_amg *amg);
 
 /* --- Krylov -------------------------------------------------------------- */
 typedef struct
@@ -182,7 +193,17 @@ typedef struct
    double              *r, *p, *s, *w;
    double             **V, **Z;
    int                  nV;
+   /* multi-vector PCG (gb_multi.c); last_multi: the last solve had multi-vectors */
+   int                  last_multi;
+   int                  m_nv, m_n;
+   double              *m_r, *m_p, *m_s, *m_dev;
+   int                 *m_iters;
+   double              *m_relres, *m_hist;
 } gb_krylov;
+
+void gb_multi_free(gb_amg *amg);
+void gb_krylov_multi_free(gb_krylov *k);
+int  gb_pcg_multi(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x);
 
 #ifdef __cplusplus
 }

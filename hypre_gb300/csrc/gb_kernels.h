@@ -135,6 +135,28 @@ void gb_vmul_d(long long n, const double *a, const double *b, double *c, cudaStr
 void gb_vmul_f(long long n, const float *a, const float *b, float *c, cudaStream_t s);
 
 void gb_fill_d(long long n, double *x, double v, cudaStream_t s);
+/* batched persistent AMG-PCG (gb_batch.cu) */
+void gb_check_blockdiag(int n, const int *Ai, const int *Aj, const int *off, int nsys, int *bad, cudaStream_t s);
+void gb_batch_pcg(const void *lev_dev, int nlev, int nsys, int sweeps_down, int sweeps_up, const int *Ai,
+                  const int *Aj, const double *Av, const int *order, int *counter, const double *b, double *x,
+                  double *r, double *p, double *sv, const double *Dinv, int nc, double tol, int maxit, int *iters,
+                  double *relres, double *hist, int prec, int lpr, int grid, int block, cudaStream_t s);
+size_t gb_blevel_size(void);
+/* learned parameters (gb_mlp.cu) */
+int gb_mlp_nparam(void);
+int gb_mlp_nbw(void);
+int gb_mlp_grid(void);
+void gb_mlp_pack(const float *P, void *W, cudaStream_t s);
+void gb_mlp_forward(long long N, const void *X, const void *W, const float *P, float *out, cudaStream_t s);
+int gb_mlp_grad(long long N, const void *X, const float *T, const void *W, const float *P, float *part,
+                float *loss_part, float *grad, float *loss, cudaStream_t s);
+void gb_mlp_adam(float *P, const float *grad, float *m, float *v, float lr, float b1, float b2, float eps, int step,
+                 cudaStream_t s);
+void gb_row_features(int n, const int *Ai, const int *Aj, const double *Av, void *X, cudaStream_t s);
+void gb_mean2(long long N, const float *out, double *res, cudaStream_t s);
+void gb_blevel_set(void *host_array, int l, int n, const int *Ai, const int *Aj, const void *Av, const int *Pi,
+                   const int *Pj, const void *Pv, const int *Ri, const int *Rj, const void *Rv, const void *l1,
+                   void *F, void *U, void *V, const int *off, double w);
 void gb_fill_f(long long n, float *x, float v, cudaStream_t s);
 void gb_scale_d(long long n, double a, double *x, cudaStream_t s);
 void gb_axpy_d(long long n, double a, const double *x, double *y, cudaStream_t s);

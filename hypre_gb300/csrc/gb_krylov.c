@@ -19,6 +19,7 @@ static gb_krylov *kry_of(HYPRE_Solver s, int arg)
 
 static void kry_free_work(gb_krylov *k)
 {
+   gb_krylov_multi_free(k);
    gb_dfree(k->r); gb_dfree(k->p); gb_dfree(k->s); gb_dfree(k->w);
    k->r = k->p = k->s = k->w = NULL;
    for (int i = 0; i < k->nV; i++) { gb_dfree(k->V[i]); gb_dfree(k->Z[i]); }
@@ -375,6 +376,14 @@ static HYPRE_Int kry_solve(HYPRE_Solver solver, HYPRE_Matrix A, HYPRE_Vector b, 
    if (!M || M->magic != GB_MAGIC_MAT) { gb_error_in_arg(2); return gb_error_flag; }
    if (!bv || bv->magic != GB_MAGIC_VEC || bv->n != M->A.nr) { gb_error_in_arg(3); return gb_error_flag; }
    if (!xv || xv->magic != GB_MAGIC_VEC || xv->n != M->A.nr) { gb_error_in_arg(4); return gb_error_flag; }
+   k->last_multi = bv->num_vectors > 1 || xv->num_vectors > 1;
+   if (k->last_multi)
+   {
+      if (k->magic == GB_MAGIC_PCG) { return gb_pcg_multi(k, M, bv, xv); }
+      gb_error(HYPRE_ERROR_GENERIC, "multi-vector right-hand sides: PCG only");
+      gb_error_in_arg(3);
+      return gb_error_flag;
+   }
    if (k->magic == GB_MAGIC_PCG) { return pcg_solve(k, M, bv, xv); }
    return fgmres_solve(k, M, bv, xv);
 }

@@ -1,0 +1,525 @@
+// Learned AMG parameters: a per-row MLP over local stencil features
+// (16 -> 64 -> 64 -> 2, ReLU) that predicts the strength threshold and the
+// smoother weight.  BF16 operands on the tensor cores (mma.sync m16n8k16,
+// FP32 accumulation), FP32 master weights and Adam; no reference counterpart.
+//
+// Each warp owns a tile of 16 rows.  Forward: H1 = relu(X W1^T + b1),
+// H2 = relu(H1 W2^T + b2), O = H2 W3^T + b3, activations rounded to BF16 where
+// they feed the next product.  Training (mean squared error against per-row
+// targets): dO = (O - T) / N, dH2 = (dO W3) .* [H2 > 0], dH1 = (dH2 W2) .* [H1 > 0],
+// dW = dZ^T A summed over rows -- every product on the tensor cores.  The
+// weight gradients are accumulated per warp in shared memory, reduced per CTA
+// in a fixed order and then over a fixed grid, so training is deterministic.
+#include <cuda_bf16.h>
+#include "gb_device.cuh"
+#include "gb_internal.h"
+
+#define MLP_IN 16
+#define MLP_H 64
+#define MLP_OUT 2
+#define MLP_OUTP 8   // output width padded to one n8 tile
+// packed FP32 parameter layout
+#define OFF_W1 0
+#define OFF_B1 (OFF_W1 + MLP_H * MLP_IN)
+#define OFF_W2 (OFF_B1 + MLP_H)
+#define OFF_B2 (OFF_W2 + MLP_H * MLP_H)
+#define OFF_W3 (OFF_B2 + MLP_H)
+#define OFF_B3 (OFF_W3 + MLP_OUT * MLP_H)
+#define MLP_NPARAM (OFF_B3 + MLP_OUT)
+// BF16 weight copies: W1 [64][16], W2 [64][64], W3 padded [8][64]
+#define BW_W1 0
+#define BW_W2 (BW_W1 + MLP_H * MLP_IN)
+#define BW_W3 (BW_W2 + MLP_H * MLP_H)
+#define MLP_NBW (BW_W3 + MLP_OUTP * MLP_H)
+
+#define MLP_WARPS 4
+#define MLP_GRID 152
+
+typedef __nv_bfloat16 bf16;
+
+namespace
+{
+
+__device__ __forceinline__ unsigned pack2(bf16 lo, bf16 hi)
+{
+   unsigned short a = __bfloat16_as_ushort(lo), b = __bfloat16_as_ushort(hi);
+   return (unsigned) a | ((unsigned) b << 16);
+}
+
+__device__ __forceinline__ void mma16816(float *c, const unsigned *a, const unsigned *b)
+{
+   asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Fragment loaders for m16n8k16 (g = lane / 4, t = lane % 4):
+//   A 16x16: {A[g][2t..2t+1]}, {A[g+8][2t..]}, {A[g][2t+8..]}, {A[g+8][2t+8..]}
+//   B 16x8 : {B[2t..2t+1][g]}, {B[2t+8..2t+9][g]}
+//   C 16x8 : c0,c1 = C[g][2t..2t+1], c2,c3 = C[g+8][2t..2t+1]
+// The accessor get(r, c) returns the element (bf16) of the logical matrix.
+template <typename Get>
+__device__ __forceinline__ void load_a(unsigned *a, Get get)
+{
+   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+   a[0] = pack2(get(g, 2 * t), get(g, 2 * t + 1));
+   a[1] = pack2(get(g + 8, 2 * t), get(g + 8, 2 * t + 1));
+   a[2] = pack2(get(g, 2 * t + 8), get(g, 2 * t + 9));
+   a[3] = pack2(get(g + 8, 2 * t + 8), get(g + 8, 2 * t + 9));
+}
+
+template <typename Get>
+__device__ __forceinline__ void load_b(unsigned *b, Get get)
+{
+   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+   b[0] = pack2(get(2 * t, g), get(2 * t + 1, g));
+   b[1] = pack2(get(2 * t + 8, g), get(2 * t + 9, g));
+}
+
+// per-warp shared tiles (BF16)
+struct WarpTiles
+{
+   bf16 X[16][MLP_IN];
+   bf16 H1[16][MLP_H];
+   bf16 H2[16][MLP_H];
+   bf16 dO[16][MLP_OUTP];
+   bf16 dH2[16][MLP_H];
+   bf16 dH1[16][MLP_H];
+};
+
+// Forward of one 16-row tile: fills H1, H2 (BF16) and returns the outputs in
+// C-fragment form o[4] (columns 2t, 2t+1 of rows g and g+8).
+__device__ __forceinline__ void forward_tile(WarpTiles &T, const bf16 *__restrict__ W, const float *__restrict__ P,
+                                             float *o)
+{
+   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+   const bf16 *W1 = W + BW_W1, *W2 = W + BW_W2, *W3 = W + BW_W3;
+   // layer 1: X (16x16) W1^T
+   unsigned a[4];
+   load_a(a, [&](int r, int c) { return T.X[r][c]; });
+   for (int nt = 0; nt < MLP_H / 8; nt++)
+   {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      unsigned b[2];
+      load_b(b, [&](int k, int n) { return W1[(nt * 8 + n) * MLP_IN + k]; });
+      mma16816(c, a, b);
+      int n0 = nt * 8 + 2 * t;
+      float b0 = P[OFF_B1 + n0], b1 = P[OFF_B1 + n0 + 1];
+      T.H1[g][n0] = __float2bfloat16_rn(fmaxf(c[0] + b0, 0.f));
+      T.H1[g][n0 + 1] = __float2bfloat16_rn(fmaxf(c[1] + b1, 0.f));
+      T.H1[g + 8][n0] = __float2bfloat16_rn(fmaxf(c[2] + b0, 0.f));
+      T.H1[g + 8][n0 + 1] = __float2bfloat16_rn(fmaxf(c[3] + b1, 0.f));
+   }
+   __syncwarp();
+   // layer 2: H1 (16x64) W2^T
+   for (int nt = 0; nt < MLP_H / 8; nt++)
+   {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int kt = 0; kt < MLP_H / 16; kt++)
+      {
+         load_a(a, [&](int r, int cc) { return T.H1[r][kt * 16 + cc]; });
+         unsigned b[2];
+         load_b(b, [&](int k, int n) { return W2[(nt * 8 + n) * MLP_H + kt * 16 + k]; });
+         mma16816(c, a, b);
+      }
+      int n0 = nt * 8 + 2 * t;
+      float b0 = P[OFF_B2 + n0], b1 = P[OFF_B2 + n0 + 1];
+      T.H2[g][n0] = __float2bfloat16_rn(fmaxf(c[0] + b0, 0.f));
+      T.H2[g][n0 + 1] = __float2bfloat16_rn(fmaxf(c[1] + b1, 0.f));
+      T.H2[g + 8][n0] = __float2bfloat16_rn(fmaxf(c[2] + b0, 0.f));
+      T.H2[g + 8][n0 + 1] = __float2bfloat16_rn(fmaxf(c[3] + b1, 0.f));
+   }
+   __syncwarp();
+   // layer 3: H2 (16x64) W3^T (8 padded outputs)
+   o[0] = o[1] = o[2] = o[3] = 0.f;
+   for (int kt = 0; kt < MLP_H / 16; kt++)
+   {
+      load_a(a, [&](int r, int cc) { return T.H2[r][kt * 16 + cc]; });
+      unsigned b[2];
+      load_b(b, [&](int k, int n) { return W3[n * MLP_H + kt * 16 + k]; });
+      mma16816(o, a, b);
+   }
+   if (t == 0)
+   {
+      o[0] += P[OFF_B3];
+      o[1] += P[OFF_B3 + 1];
+      o[2] += P[OFF_B3];
+      o[3] += P[OFF_B3 + 1];
+   }
+}
+
+__device__ __forceinline__ void load_x_tile(WarpTiles &T, const bf16 *__restrict__ X, long long row0, long long N)
+{
+   const int lane = threadIdx.x & 31;
+   for (int e = lane; e < 16 * MLP_IN; e += 32)
+   {
+      int r = e / MLP_IN, c = e % MLP_IN;
+      long long row = row0 + r;
+      T.X[r][c] = row < N ? X[row * MLP_IN + c] : __float2bfloat16_rn(0.f);
+   }
+   __syncwarp();
+}
+
+} // namespace
+
+// Inference: out[row][0..1] = MLP(X[row]).
+__global__ void __launch_bounds__(32 * MLP_WARPS) k_mlp_forward(long long N, const bf16 *__restrict__ X,
+                                                                const bf16 *__restrict__ W,
+                                                                const float *__restrict__ P, float *__restrict__ out)
+{
+   __shared__ WarpTiles tiles[MLP_WARPS];
+   WarpTiles &T = tiles[threadIdx.x >> 5];
+   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+   const long long ntiles = (N + 15) / 16;
+   const long long wid = (long long) blockIdx.x * MLP_WARPS + (threadIdx.x >> 5);
+   const long long nw = (long long) gridDim.x * MLP_WARPS;
+   for (long long tile = wid; tile < ntiles; tile += nw)
+   {
+      long long row0 = tile * 16;
+      load_x_tile(T, X, row0, N);
+      float o[4];
+      forward_tile(T, W, P, o);
+      if (t == 0)
+      {
+         if (row0 + g < N) { out[(row0 + g) * 2] = o[0]; out[(row0 + g) * 2 + 1] = o[1]; }
+         if (row0 + g + 8 < N) { out[(row0 + g + 8) * 2] = o[2]; out[(row0 + g + 8) * 2 + 1] = o[3]; }
+      }
+      __syncwarp();
+   }
+}
+
+// Training gradients of the mean squared error over N rows.  Writes one
+// partial gradient (MLP_NPARAM floats) and one partial loss per CTA.
+__global__ void __launch_bounds__(32 * MLP_WARPS) k_mlp_grad(long long N, const bf16 *__restrict__ X,
+                                                             const float *__restrict__ Tg,
+                                                             const bf16 *__restrict__ W,
+                                                             const float *__restrict__ P, float inv_n,
+                                                             float *__restrict__ part, float *__restrict__ loss_part)
+{
+   extern __shared__ float smem[];
+   // per-warp gradient accumulators, then tiles
+   float *acc = smem + (threadIdx.x >> 5) * MLP_NPARAM;
+   WarpTiles *tiles = (WarpTiles *) (smem + MLP_WARPS * MLP_NPARAM);
+   WarpTiles &T = tiles[threadIdx.x >> 5];
+   __shared__ float lsum[MLP_WARPS];
+   const int lane = threadIdx.x & 31;
+   const int g = lane >> 2, t = lane & 3;
+   for (int e = lane; e < MLP_NPARAM; e += 32) { acc[e] = 0.f; }
+   float loss = 0.f;
+   const bf16 *W2 = W + BW_W2, *W3 = W + BW_W3;
+   const long long ntiles = (N + 15) / 16;
+   const long long wid = (long long) blockIdx.x * MLP_WARPS + (threadIdx.x >> 5);
+   const long long nw = (long long) gridDim.x * MLP_WARPS;
+   __syncwarp();
+   for (long long tile = wid; tile < ntiles; tile += nw)
+   {
+      long long row0 = tile * 16;
+      load_x_tile(T, X, row0, N);
+      float o[4];
+      forward_tile(T, W, P, o);
+      // dO (BF16), loss
+      for (int e = lane; e < 16 * MLP_OUTP; e += 32) { T.dO[e / MLP_OUTP][e % MLP_OUTP] = __float2bfloat16_rn(0.f); }
+      __syncwarp();
+      if (t == 0)
+      {
+         for (int h = 0; h < 2; h++)
+         {
+            long long row = row0 + g + 8 * h;
+            if (row < N)
+            {
+               float d0 = o[2 * h] - Tg[row * 2], d1 = o[2 * h + 1] - Tg[row * 2 + 1];
+               loss += d0 * d0 + d1 * d1;
+               T.dO[g + 8 * h][0] = __float2bfloat16_rn(d0 * inv_n);
+               T.dO[g + 8 * h][1] = __float2bfloat16_rn(d1 * inv_n);
+            }
+         }
+      }
+      __syncwarp();
+      unsigned a[4], b[2];
+      // dH2 = (dO W3) .* [H2 > 0]; K = 8 outputs padded to 16
+      load_a(a, [&](int r, int c) { return c < MLP_OUTP ? T.dO[r][c] : __float2bfloat16_rn(0.f); });
+      for (int nt = 0; nt < MLP_H / 8; nt++)
+      {
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+         load_b(b, [&](int k, int n) { return k < MLP_OUTP ? W3[k * MLP_H + nt * 8 + n] : __float2bfloat16_rn(0.f); });
+         mma16816(c, a, b);
+         int n0 = nt * 8 + 2 * t;
+         for (int q = 0; q < 4; q++)
+         {
+            int r = g + 8 * (q >> 1), cc = n0 + (q & 1);
+            float v = __bfloat162float(T.H2[r][cc]) > 0.f ? c[q] : 0.f;
+            T.dH2[r][cc] = __float2bfloat16_rn(v);
+         }
+      }
+      __syncwarp();
+      // dH1 = (dH2 W2) .* [H1 > 0]
+      for (int nt = 0; nt < MLP_H / 8; nt++)
+      {
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+         for (int kt = 0; kt < MLP_H / 16; kt++)
+         {
+            load_a(a, [&](int r, int cc) { return T.dH2[r][kt * 16 + cc]; });
+            load_b(b, [&](int k, int n) { return W2[(kt * 16 + k) * MLP_H + nt * 8 + n]; });
+            mma16816(c, a, b);
+         }
+         int n0 = nt * 8 + 2 * t;
+         for (int q = 0; q < 4; q++)
+         {
+            int r = g + 8 * (q >> 1), cc = n0 + (q & 1);
+            float v = __bfloat162float(T.H1[r][cc]) > 0.f ? c[q] : 0.f;
+            T.dH1[r][cc] = __float2bfloat16_rn(v);
+         }
+      }
+      __syncwarp();
+      // weight gradients, K = the 16 rows of the tile
+      // dW3[j][k] = sum_r dO[r][j] H2[r][k]   (M = 8 outputs padded to 16)
+      load_a(a, [&](int m, int k) { return m < MLP_OUTP ? T.dO[k][m] : __float2bfloat16_rn(0.f); });
+      for (int nt = 0; nt < MLP_H / 8; nt++)
+      {
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+         load_b(b, [&](int k, int n) { return T.H2[k][nt * 8 + n]; });
+         mma16816(c, a, b);
+         if (g < MLP_OUT)
+         {
+            acc[OFF_W3 + g * MLP_H + nt * 8 + 2 * t] += c[0];
+            acc[OFF_W3 + g * MLP_H + nt * 8 + 2 * t + 1] += c[1];
+         }
+      }
+      // dW2[n][k] = sum_r dH2[r][n] H1[r][k]
+      for (int mt = 0; mt < MLP_H / 16; mt++)
+      {
+         load_a(a, [&](int m, int k) { return T.dH2[k][mt * 16 + m]; });
+         for (int nt = 0; nt < MLP_H / 8; nt++)
+         {
+            float c[4] = {0.f, 0.f, 0.f, 0.f};
+            load_b(b, [&](int k, int n) { return T.H1[k][nt * 8 + n]; });
+            mma16816(c, a, b);
+            int r0 = mt * 16 + g, c0 = nt * 8 + 2 * t;
+            acc[OFF_W2 + r0 * MLP_H + c0] += c[0];
+            acc[OFF_W2 + r0 * MLP_H + c0 + 1] += c[1];
+            acc[OFF_W2 + (r0 + 8) * MLP_H + c0] += c[2];
+            acc[OFF_W2 + (r0 + 8) * MLP_H + c0 + 1] += c[3];
+         }
+      }
+      // dW1[n][k] = sum_r dH1[r][n] X[r][k]
+      for (int mt = 0; mt < MLP_H / 16; mt++)
+      {
+         load_a(a, [&](int m, int k) { return T.dH1[k][mt * 16 + m]; });
+         for (int nt = 0; nt < MLP_IN / 8; nt++)
+         {
+            float c[4] = {0.f, 0.f, 0.f, 0.f};
+            load_b(b, [&](int k, int n) { return T.X[k][nt * 8 + n]; });
+            mma16816(c, a, b);
+            int r0 = mt * 16 + g, c0 = nt * 8 + 2 * t;
+            acc[OFF_W1 + r0 * MLP_IN + c0] += c[0];
+            acc[OFF_W1 + r0 * MLP_IN + c0 + 1] += c[1];
+            acc[OFF_W1 + (r0 + 8) * MLP_IN + c0] += c[2];
+            acc[OFF_W1 + (r0 + 8) * MLP_IN + c0 + 1] += c[3];
+         }
+      }
+      // bias gradients: column sums over the tile's rows
+      for (int c = lane; c < MLP_H; c += 32)
+      {
+         float s1 = 0.f, s2 = 0.f;
+         for (int r = 0; r < 16; r++) { s1 += __bfloat162float(T.dH1[r][c]); s2 += __bfloat162float(T.dH2[r][c]); }
+         acc[OFF_B1 + c] += s1;
+         acc[OFF_B2 + c] += s2;
+      }
+      if (lane < MLP_OUT)
+      {
+         float s3 = 0.f;
+         for (int r = 0; r < 16; r++) { s3 += __bfloat162float(T.dO[r][lane]); }
+         acc[OFF_B3 + lane] += s3;
+      }
+      __syncwarp();
+   }
+   for (int o = 16; o > 0; o >>= 1) { loss += __shfl_down_sync(GB_FULL, loss, o); }
+   if (lane == 0) { lsum[threadIdx.x >> 5] = loss; }
+   __syncthreads();
+   // CTA partial: warps summed in a fixed order
+   for (int e = threadIdx.x; e < MLP_NPARAM; e += blockDim.x)
+   {
+      float s = 0.f;
+      for (int w = 0; w < MLP_WARPS; w++) { s += smem[w * MLP_NPARAM + e]; }
+      part[(size_t) blockIdx.x * MLP_NPARAM + e] = s;
+   }
+   if (threadIdx.x == 0)
+   {
+      float s = 0.f;
+      for (int w = 0; w < MLP_WARPS; w++) { s += lsum[w]; }
+      loss_part[blockIdx.x] = s;
+   }
+}
+
+// grad[e] = sum over CTAs of part[b][e] (fixed order); loss = sum / (2N)
+__global__ void k_mlp_reduce(int nb, const float *__restrict__ part, const float *__restrict__ loss_part,
+                             float inv_2n, float *__restrict__ grad, float *__restrict__ loss)
+{
+   int e = blockIdx.x * blockDim.x + threadIdx.x;
+   if (e < MLP_NPARAM)
+   {
+      float s = 0.f;
+      for (int b = 0; b < nb; b++) { s += part[(size_t) b * MLP_NPARAM + e]; }
+      grad[e] = s;
+   }
+   if (e == 0)
+   {
+      float s = 0.f;
+      for (int b = 0; b < nb; b++) { s += loss_part[b]; }
+      *loss = s * inv_2n;
+   }
+}
+
+// FP32 master parameters -> BF16 weight copies (W3 padded to 8 rows)
+__global__ void k_mlp_pack(const float *__restrict__ P, bf16 *__restrict__ W)
+{
+   int e = blockIdx.x * blockDim.x + threadIdx.x;
+   if (e < MLP_H * MLP_IN) { W[BW_W1 + e] = __float2bfloat16_rn(P[OFF_W1 + e]); }
+   if (e < MLP_H * MLP_H) { W[BW_W2 + e] = __float2bfloat16_rn(P[OFF_W2 + e]); }
+   if (e < MLP_OUTP * MLP_H)
+   {
+      int r = e / MLP_H;
+      W[BW_W3 + e] = __float2bfloat16_rn(r < MLP_OUT ? P[OFF_W3 + e] : 0.f);
+   }
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters
+__global__ void k_mlp_adam(float *__restrict__ P, const float *__restrict__ grad, float *__restrict__ m,
+                           float *__restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+   int e = blockIdx.x * blockDim.x + threadIdx.x;
+   if (e >= MLP_NPARAM) { return; }
+   float gr = grad[e];
+   float mm = b1 * m[e] + (1.f - b1) * gr;
+   float vv = b2 * v[e] + (1.f - b2) * gr * gr;
+   m[e] = mm;
+   v[e] = vv;
+   P[e] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+}
+
+// Per-row stencil features of a CSR matrix whose rows start with the
+// diagonal: with d = a_ii and c_j = -a_ij / d for the off-diagonal entries,
+//   0 nnz / 27            1 sum c_j              2 sum |c_j|
+//   3 max c_j             4 min c_j              5-13 fraction of entries with
+//   c_j >= tau * max c_j for tau = 0.1, 0.2, ..., 0.9
+//   14 sum of positive off-diagonals / d          15 fraction of positive off-diagonals
+__global__ void k_row_features(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                               const double *__restrict__ Av, bf16 *__restrict__ X)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int b = Ai[i], e = Ai[i + 1];
+   double d = e > b ? Av[b] : 1.0;
+   if (!(d > 0.0) && !(d < 0.0)) { d = 1.0; }
+   double sum = 0.0, asum = 0.0, mx = -1e300, mn = 1e300, pos = 0.0;
+   int npos = 0, m = e - b - 1;
+   for (int k = b + 1; k < e; k++)
+   {
+      double c = -Av[k] / d;
+      sum += c;
+      asum += fabs(c);
+      mx = c > mx ? c : mx;
+      mn = c < mn ? c : mn;
+      if (Av[k] > 0.0) { pos += Av[k] / fabs(d); npos++; }
+   }
+   if (m <= 0) { mx = 0.0; mn = 0.0; }
+   float f[MLP_IN];
+   f[0] = (float) (e - b) / 27.f;
+   f[1] = (float) sum;
+   f[2] = (float) asum;
+   f[3] = (float) mx;
+   f[4] = (float) mn;
+   for (int q = 0; q < 9; q++)
+   {
+      double tau = 0.1 * (q + 1);
+      int cnt = 0;
+      if (mx > 0.0)
+      {
+         for (int k = b + 1; k < e; k++) { cnt += (-Av[k] / d) >= tau * mx; }
+      }
+      f[5 + q] = m > 0 ? (float) cnt / (float) m : 0.f;
+   }
+   f[14] = (float) pos;
+   f[15] = m > 0 ? (float) npos / (float) m : 0.f;
+   for (int q = 0; q < MLP_IN; q++) { X[(size_t) i * MLP_IN + q] = __float2bfloat16_rn(f[q]); }
+}
+
+// column means of out (N x 2) into res[0..1], fixed-order two-level sum
+__global__ void k_mean2(long long N, const float *__restrict__ out, double *__restrict__ res)
+{
+   __shared__ double s0[256], s1[256];
+   double a = 0.0, c = 0.0;
+   for (long long r = threadIdx.x; r < N; r += blockDim.x) { a += out[r * 2]; c += out[r * 2 + 1]; }
+   s0[threadIdx.x] = a;
+   s1[threadIdx.x] = c;
+   __syncthreads();
+   if (threadIdx.x == 0)
+   {
+      double x = 0.0, y = 0.0;
+      for (int t = 0; t < (int) blockDim.x; t++) { x += s0[t]; y += s1[t]; }
+      res[0] = N > 0 ? x / (double) N : 0.0;
+      res[1] = N > 0 ? y / (double) N : 0.0;
+   }
+}
+
+static size_t grad_smem_bytes(void) { return sizeof(float) * MLP_WARPS * MLP_NPARAM + sizeof(WarpTiles) * MLP_WARPS; }
+
+extern "C" int gb_mlp_nparam(void) { return MLP_NPARAM; }
+extern "C" int gb_mlp_nbw(void) { return MLP_NBW; }
+extern "C" int gb_mlp_grid(void) { return MLP_GRID; }
+
+extern "C" void gb_mlp_pack(const float *P, void *W, cudaStream_t s)
+{
+   k_mlp_pack<<<(MLP_H * MLP_H + 255) / 256, 256, 0, s>>>(P, (bf16 *) W);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_mlp_forward(long long N, const void *X, const void *W, const float *P, float *out, cudaStream_t s)
+{
+   long long tiles = (N + 15) / 16;
+   long long blocks = (tiles + MLP_WARPS - 1) / MLP_WARPS;
+   int grid = (int) (blocks < 152 * 16 ? (blocks > 0 ? blocks : 1) : 152 * 16);
+   k_mlp_forward<<<grid, 32 * MLP_WARPS, 0, s>>>(N, (const bf16 *) X, (const bf16 *) W, P, out);
+   GB_COUNT(1);
+}
+
+extern "C" int gb_mlp_grad(long long N, const void *X, const float *T, const void *W, const float *P, float *part,
+                           float *loss_part, float *grad, float *loss, cudaStream_t s)
+{
+   static int attr_done = 0;
+   size_t sm = grad_smem_bytes();
+   if (!attr_done)
+   {
+      if (cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm) != cudaSuccess)
+      {
+         return 1;
+      }
+      attr_done = 1;
+   }
+   float inv_n = N > 0 ? 1.f / (float) N : 0.f;
+   k_mlp_grad<<<MLP_GRID, 32 * MLP_WARPS, sm, s>>>(N, (const bf16 *) X, T, (const bf16 *) W, P, inv_n, part,
+                                                    loss_part);
+   k_mlp_reduce<<<(MLP_NPARAM + 255) / 256, 256, 0, s>>>(MLP_GRID, part, loss_part, 0.5f * inv_n, grad, loss);
+   GB_COUNT(2);
+   return 0;
+}
+
+extern "C" void gb_mlp_adam(float *P, const float *grad, float *m, float *v, float lr, float b1, float b2, float eps,
+                            int step, cudaStream_t s)
+{
+   float c1 = 1.f - powf(b1, (float) step), c2 = 1.f - powf(b2, (float) step);
+   k_mlp_adam<<<(MLP_NPARAM + 255) / 256, 256, 0, s>>>(P, grad, m, v, lr, b1, b2, eps, c1, c2);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_row_features(int n, const int *Ai, const int *Aj, const double *Av, void *X, cudaStream_t s)
+{
+   if (n > 0) { k_row_features<<<(n + 255) / 256, 256, 0, s>>>(n, Ai, Aj, Av, (bf16 *) X); GB_COUNT(1); }
+}
+
+extern "C" void gb_mean2(long long N, const float *out, double *res, cudaStream_t s)
+{
+   k_mean2<<<1, 256, 0, s>>>(N, out, res);
+   GB_COUNT(1);
+}

@@ -183,3 +183,27 @@ def rhs(n, seed=22775, normalise=True):
         s = float(np.add.reduce(b * b)) if n > 100000 else sum((b * b).tolist())
         b = b * (1.0 / np.sqrt(s))
     return b
+
+
+def aniso2d_batch(num, nmin=16, nmax=128, eps_lo=1e-3, eps_hi=1.0, seed=0):
+    """Block-diagonal matrix of `num` independent 2-D anisotropic 5-point
+    problems (-eps d_xx - d_yy on n x n grids), n uniform in [nmin, nmax],
+    eps log-uniform in [eps_lo, eps_hi]; returns (I, J, V, offsets, sizes, eps)."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(nmin, nmax + 1, size=num)
+    eps = np.exp(rng.uniform(np.log(eps_lo), np.log(eps_hi), size=num))
+    Is, Js, Vs = [], [], []
+    off = np.zeros(num + 1, np.int64)
+    nnz_off = 0
+    for k in range(num):
+        I, J, V = aniso2d(int(ns[k]), float(eps[k]))
+        N = len(I) - 1
+        Is.append(I[:-1].astype(np.int64) + nnz_off)
+        Js.append(J.astype(np.int64) + off[k])
+        Vs.append(V)
+        off[k + 1] = off[k] + N
+        nnz_off += len(J)
+    I = np.concatenate(Is + [np.array([nnz_off])]).astype(np.int32)
+    J = np.concatenate(Js).astype(np.int32)
+    V = np.concatenate(Vs)
+    return I, J, V, off.astype(np.int32), ns, eps

@@ -255,6 +255,71 @@ HYPRE_Int HYPRE_ParCSRFlexGMRESSetPrecond(HYPRE_Solver solver, HYPRE_PtrToParSol
 HYPRE_Int HYPRE_ParCSRFlexGMRESGetNumIterations(HYPRE_Solver solver, HYPRE_Int *num_iterations); /* :3495 */
 HYPRE_Int HYPRE_ParCSRFlexGMRESGetFinalRelativeResidualNorm(HYPRE_Solver solver, HYPRE_Real *norm); /* :3498 */
 
+/* --- Batched AMG-PCG (no counterpart in the reference) ---------------------
+ * Many independent systems given as the diagonal blocks of one matrix A
+ * (system s owns rows system_offsets[s] .. system_offsets[s+1]-1; entries
+ * outside the blocks are rejected).  Setup runs HYPRE_BoomerAMGSetup's
+ * algorithm once on A with the given BoomerAMG solver's parameters (relax
+ * type 18 or 7, direct coarsest solve, no aggressive levels); Solve runs an
+ * FP64 PCG per system (two-norm stopping test, tolerance per system) with the
+ * V-cycle in FP64 or FP32, all systems in one persistent kernel launch.  The
+ * kernel shape (lanes per row 1/2/4/8, block 128/256/512) is autotuned on the
+ * first Solve unless set explicitly.  Errors: HYPRE_ERROR_CONV when a system
+ * does not reach the tolerance. */
+HYPRE_Int HYPRE_GB300_BatchedPCGCreate(HYPRE_Solver *solver);
+HYPRE_Int HYPRE_GB300_BatchedPCGDestroy(HYPRE_Solver solver);
+HYPRE_Int HYPRE_GB300_BatchedPCGSetTol(HYPRE_Solver solver, HYPRE_Real tol);
+HYPRE_Int HYPRE_GB300_BatchedPCGSetMaxIter(HYPRE_Solver solver, HYPRE_Int max_iter);
+HYPRE_Int HYPRE_GB300_BatchedPCGSetCyclePrecision(HYPRE_Solver solver, HYPRE_Int precision); /* 0 FP64, 1 FP32 */
+HYPRE_Int HYPRE_GB300_BatchedPCGSetKernelShape(HYPRE_Solver solver, HYPRE_Int lanes_per_row, HYPRE_Int block);
+HYPRE_Int HYPRE_GB300_BatchedPCGSetAutotune(HYPRE_Solver solver, HYPRE_Int autotune);
+HYPRE_Int HYPRE_GB300_BatchedPCGGetKernelShape(HYPRE_Solver solver, HYPRE_Int *lanes_per_row, HYPRE_Int *block);
+HYPRE_Int HYPRE_GB300_BatchedPCGGetTuningTimes(HYPRE_Solver solver, HYPRE_Real *ms); /* 4 x 3 */
+HYPRE_Int HYPRE_GB300_BatchedPCGSetup(HYPRE_Solver solver, HYPRE_Solver amg, HYPRE_ParCSRMatrix A,
+                                      HYPRE_Int num_systems, const HYPRE_Int *system_offsets);
+HYPRE_Int HYPRE_GB300_BatchedPCGSolve(HYPRE_Solver solver, HYPRE_ParVector b, HYPRE_ParVector x);
+HYPRE_Int HYPRE_GB300_BatchedPCGGetNumIterations(HYPRE_Solver solver, HYPRE_Int *iterations);
+HYPRE_Int HYPRE_GB300_BatchedPCGGetFinalRelativeResidualNorms(HYPRE_Solver solver, HYPRE_Real *relres);
+HYPRE_Int HYPRE_GB300_BatchedPCGGetResidualHistory(HYPRE_Solver solver, HYPRE_Int system, HYPRE_Int maxn,
+                                                   HYPRE_Real *relres, HYPRE_Int *n);
+HYPRE_Int HYPRE_GB300_BatchedPCGGetLevelOffsets(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int *offsets);
+/* per system: sum over levels of its nonzeros divided by its level-0 nonzeros */
+HYPRE_Int HYPRE_GB300_BatchedPCGGetOperatorComplexities(HYPRE_Solver solver, HYPRE_Real *opc);
+
+/* --- Multiple right-hand sides (extends the reference's PCG column-wise) ----
+ * A multi-vector of num_vectors <= 64 columns, stored interleaved (entry
+ * (i, c) at i * num_vectors + c); CopyFromHost/CopyToHost take
+ * n * num_vectors values.  HYPRE_ParCSRPCGSolve on multi-vectors runs one
+ * PCG per column (own scalars, stopping test and history) with every
+ * product and the BoomerAMG V-cycle (relax 18 or 7, FP64 or FP32 cycle)
+ * applied to all columns in one pass. */
+HYPRE_Int HYPRE_GB300_ParVectorCreateMulti(HYPRE_BigInt n, HYPRE_Int num_vectors, HYPRE_ParVector *vector);
+HYPRE_Int HYPRE_GB300_KrylovGetMultiNumIterations(HYPRE_Solver solver, HYPRE_Int *iterations);
+HYPRE_Int HYPRE_GB300_KrylovGetMultiFinalRelativeResidualNorms(HYPRE_Solver solver, HYPRE_Real *relres);
+HYPRE_Int HYPRE_GB300_KrylovGetMultiResidualHistory(HYPRE_Solver solver, HYPRE_Int column, HYPRE_Int maxn,
+                                                    HYPRE_Real *relres, HYPRE_Int *n);
+
+/* --- Learned parameters (no counterpart in the reference) ------------------
+ * A per-row MLP (16 stencil features -> 64 -> 64 -> 2, ReLU, BF16 tensor-core
+ * products with FP32 accumulation) predicts (strength threshold, smoother
+ * weight) for each row.  With a model set, BoomerAMG setup uses the mean
+ * predicted threshold over the finest level's rows (clamped to [0.1, 0.9]) and
+ * sets each level's relaxation weight to the mean predicted weight over its
+ * rows (clamped to [0.3, 1.5]); NULL removes the model.  params: the
+ * HYPRE_GB300_MLPNumParams() FP32 values W1[64][16] b1[64] W2[64][64] b2[64]
+ * W3[2][64] b3[2].  The training primitives take device pointers:
+ * features n x 16 BF16, targets and out n x 2 FP32, params/grad/m/v FP32. */
+HYPRE_Int HYPRE_GB300_MLPNumParams(HYPRE_Int *n);
+HYPRE_Int HYPRE_GB300_BoomerAMGSetLearnedModel(HYPRE_Solver solver, const HYPRE_Real *params);
+HYPRE_Int HYPRE_GB300_BoomerAMGGetLearnedParams(HYPRE_Solver solver, HYPRE_Real *theta, HYPRE_Real *weights,
+                                                HYPRE_Int max_levels);
+HYPRE_Int HYPRE_GB300_MLPRowFeatures(HYPRE_ParCSRMatrix A, void *features);
+HYPRE_Int HYPRE_GB300_MLPForward(HYPRE_BigInt n, const void *features, const float *params, float *out);
+HYPRE_Int HYPRE_GB300_MLPGradient(HYPRE_BigInt n, const void *features, const float *targets,
+                                  const float *params, float *grad, float *loss);
+HYPRE_Int HYPRE_GB300_MLPAdamStep(float *params, const float *grad, float *m, float *v, HYPRE_Real lr,
+                                  HYPRE_Int step);
+
 /* --- GB300 extensions (no counterpart in the reference) ------------------- */
 /* Precision of the AMG V-cycle (hierarchy values, smoothers, level SpMVs);
  * setup and the outer Krylov method stay in FP64.

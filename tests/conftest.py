@@ -25,3 +25,12 @@ def gb():
     import hypre_gb300
     hypre_gb300.lib().HYPRE_Initialize()
     return hypre_gb300
+
+
+@pytest.fixture(autouse=True)
+def _clear_error_flag(request):
+    """Each test starts with a clear sticky error flag (as a fresh process would)."""
+    if "gb" in request.fixturenames:
+        import hypre_gb300
+        hypre_gb300.lib().HYPRE_ClearAllErrors()
+    yield

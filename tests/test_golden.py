@@ -67,3 +67,23 @@ def test_tridiagonal_eigenvalues(O):
         e = np.concatenate([[0.0], rng.uniform(-1, 1, n - 1)])
         T = np.diag(d) + np.diag(e[1:], 1) + np.diag(e[1:], -1)
         np.testing.assert_allclose(O.eig_tridiag(d, e), np.linalg.eigvalsh(T), rtol=1e-13, atol=1e-14)
+
+
+def test_mlp_reference_gradient_finite_differences():
+    """The CPU reference of the learned-parameter MLP (exact FP64 mode) against
+    central finite differences of its own loss."""
+    import mlp_ref
+    rng = np.random.default_rng(0)
+    X = rng.uniform(-1, 1, (40, 16))
+    T = rng.uniform(0, 1, (40, 2))
+    p = mlp_ref.init_params(1)
+    p[-2:] = [0.3, 0.8]
+    _, g = mlp_ref.gradient(X, T, p, rounding=False)
+    idx = rng.choice(len(p), 60, replace=False)
+    for k in idx:
+        h = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h
+        pm[k] -= h
+        fd = (mlp_ref.gradient(X, T, pp, rounding=False)[0] - mlp_ref.gradient(X, T, pm, rounding=False)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 + 1e-5 * abs(g[k]), (k, fd, g[k])
