@@ -218,7 +218,36 @@ static int tier_end(gb_tier *t)
 }
 
 /* C = A B with hypre_ParMatmul's column order (square: diagonal first) */
+/* algorithmic bytes and device time of the sparse products of the current
+ * setup (CUDA events on the library stream around each product) */
+static double g_sg_bytes, g_sg_seconds;
+static int g_sg_calls;
+static cudaEvent_t g_sg_ev[2];
+
+static double csr_bytes(const gb_csr *M) { return 12.0 * (double) M->nnz + 4.0 * ((double) M->nr + 1.0); }
+
+static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_csr *C);
+
 static int spgemm_host(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
+{
+   cudaStream_t s = gb_stream();
+   if (!g_sg_ev[0]) { cudaEventCreate(&g_sg_ev[0]); cudaEventCreate(&g_sg_ev[1]); }
+   cudaEventRecord(g_sg_ev[0], s);
+   int r = spgemm_host_inner(A, B, square, C);
+   cudaEventRecord(g_sg_ev[1], s);
+   cudaEventSynchronize(g_sg_ev[1]);
+   float ms = 0.f;
+   cudaEventElapsedTime(&ms, g_sg_ev[0], g_sg_ev[1]);
+   if (r == 0)
+   {
+      g_sg_bytes += csr_bytes(A) + csr_bytes(B) + csr_bytes(C);
+      g_sg_seconds += ms * 1e-3;
+      g_sg_calls++;
+   }
+   return r;
+}
+
+static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
 {
    cudaStream_t s = gb_stream();
    int n = A->nr;
@@ -835,6 +864,8 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    amg_free_hierarchy(amg);
    gb_amg_params *prm = &amg->prm;
    double t_start = gb_wtime();
+   g_sg_bytes = g_sg_seconds = 0.0;
+   g_sg_calls = 0;
 
    memset(amg->setup_times, 0, sizeof(amg->setup_times));
    amg->lev[0].A = A0;
@@ -915,6 +946,9 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    gb_sync();
    amg->r_work = (double *) gb_dmalloc(sizeof(double) * (size_t) (amg->lev[0].n ? amg->lev[0].n : 1));
    amg->setup_times[4] = gb_wtime() - t_sm;
+   amg->spgemm_bytes = g_sg_bytes;
+   amg->spgemm_seconds = g_sg_seconds;
+   amg->spgemm_calls = g_sg_calls;
    amg->setup_times[5] = gb_wtime() - t_start;
    amg->setup_done = 1;
    return gb_error_flag;
@@ -1540,6 +1574,17 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCF(HYPRE_Solver solver, HYPRE_Int level, 
    if (level < 0 || level >= a->num_levels - 1 || !cf) { gb_error_in_arg(2); return gb_error_flag; }
    cudaMemcpyAsync(cf, a->lev[level].CF, sizeof(int) * (size_t) a->lev[level].n, cudaMemcpyDeviceToHost, gb_stream());
    gb_sync();
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_GB300_BoomerAMGGetSpGEMMStats(HYPRE_Solver solver, HYPRE_Real *bytes, HYPRE_Real *seconds,
+                                              HYPRE_Int *calls)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (bytes) { *bytes = a->spgemm_bytes; }
+   if (seconds) { *seconds = a->spgemm_seconds; }
+   if (calls) { *calls = a->spgemm_calls; }
    return gb_error_flag;
 }
 

@@ -166,6 +166,8 @@ typedef struct
    double        learned_theta;
    double        learned_w[32];
    void         *multi_ws;      /* multi-vector cycle work space (gb_multi.c) */
+   double        spgemm_bytes, spgemm_seconds;   /* sparse products of the last setup */
+   int           spgemm_calls;
 } gb_amg;
 
 int gb_amg_cycle(gb_amg *amg, const double *f, double *u);   /* one V-cycle, u from zero */

@@ -335,6 +335,12 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCSR(HYPRE_Solver solver, HYPRE_Int level,
                                            HYPRE_Int *rowptr, HYPRE_Int *colidx, HYPRE_Real *values);
 HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCF(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int *cf_marker);
 HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelL1(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Real *l1);
+/* Sparse matrix products of the last setup (the Galerkin products and the
+ * aggressive level's products): algorithmic bytes (inputs read once, output
+ * written once, 12 bytes per nonzero + 4 per row pointer), device seconds
+ * (CUDA events on the library stream around each product) and their count. */
+HYPRE_Int HYPRE_GB300_BoomerAMGGetSpGEMMStats(HYPRE_Solver solver, HYPRE_Real *bytes, HYPRE_Real *seconds,
+                                              HYPRE_Int *calls);
 /* Chebyshev smoother data of a level (relax type 16): the ChebyOrder
  * coefficients of s(t) in u <- u + s(A) r, eig[0..1] = max/min eigenvalue
  * estimates, ds = D^{-1/2} (n values); any pointer may be NULL. */
