@@ -198,9 +198,9 @@ static void tier_begin(gb_tier *t, int nrows)
 
 /* after the symbolic shared-memory pass: read the overflow count and, if
  * needed, size the global tables from ub (device, nub entries) */
-static void tier_global(gb_tier *t, const int *ub, int nub)
+static void tier_global_n(gb_tier *t, const int *ub, int nub, int count)
 {
-   t->h_ovf = read_int(t->ovf_n);
+   t->h_ovf = count;
    if (t->h_ovf <= 0) { return; }
    int m = max_of(ub, nub);
    t->gcap = next_pow2(2LL * (m + 1));
@@ -209,6 +209,8 @@ static void tier_global(gb_tier *t, const int *ub, int nub)
    t->gtab = (int *) gb_dmalloc(per * (size_t) t->gwarps);
    if (t->gtab) { cudaMemsetAsync(t->gtab, 0xff, per * (size_t) t->gwarps, gb_stream()); }
 }
+
+static void tier_global(gb_tier *t, const int *ub, int nub) { tier_global_n(t, ub, nub, read_int(t->ovf_n)); }
 
 static int tier_end(gb_tier *t)
 {
@@ -254,39 +256,54 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    gb_tier t;
    tier_begin(&t, n);
+   int *list2 = NULL, *n2 = (int *) gb_dcalloc(sizeof(int) * 2);
    /* lane-group width from B's longest row */
    gb_rowlen_max(B->nr, B->i, t.err + 1, s);
    int maxb = read_int(t.err + 1);
    int W = 0;
    if (maxb <= 32) { W = 1; while (W < maxb) { W <<= 1; } }
-   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, 0,
-             0, t.err, 0, 0, s);
+   /* symbolic: small shared tables, then large shared tables for the rows
+    * that did not fit, then global tables for the rest */
+   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, NULL,
+             n, NULL, 0, 0, t.err, 0, 0, s);
+   int h1 = read_int(t.ovf_n), h2 = 0;
+   if (h1 > 0)
+   {
+      list2 = (int *) gb_dmalloc(sizeof(int) * (size_t) h1);
+      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, list2,
+                n2, h1, NULL, 0, 0, t.err, 0, 1, s);
+      h2 = read_int(n2);
+   }
    int *ub = NULL;
-   if (read_int(t.ovf_n) > 0)
+   if (h2 > 0)
    {
       ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
       gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
-   }
-   tier_global(&t, ub, n);
-   if (t.h_ovf > 0)
-   {
-      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n,
-                t.gtab, t.gcap, t.gwarps, t.err, 0, 1, s);
+      /* global tables for the rows of the second list */
+      tier_global_n(&t, ub, n, h2);
+      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, list2, n2, NULL, NULL, h2,
+                t.gtab, t.gcap, t.gwarps, t.err, 0, 2, s);
    }
    C->nr = n; C->nc = B->nc;
    C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    C->nnz = scan_total(cnt, C->i, n);
    C->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C->nnz ? C->nnz : 1));
    C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
-   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL, 0,
-             0, t.err, 1, 0, s);
-   if (t.h_ovf > 0)
+   /* numeric: the same three tiers (each skips rows longer than its tables) */
+   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL, NULL,
+             n, NULL, 0, 0, t.err, 1, 0, s);
+   if (h1 > 0)
    {
-      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
-                t.gtab, t.gcap, t.gwarps, t.err, 1, 1, s);
+      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL,
+                NULL, h1, NULL, 0, 0, t.err, 1, 1, s);
+   }
+   if (h2 > 0)
+   {
+      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, list2, n2, NULL, NULL, h2,
+                t.gtab, t.gcap, t.gwarps, t.err, 1, 2, s);
    }
    int e = tier_end(&t);
-   gb_dfree(ub); gb_dfree(cnt);
+   gb_dfree(ub); gb_dfree(cnt); gb_dfree(list2); gb_dfree(n2);
    if (e) { gb_error(HYPRE_ERROR_GENERIC, "sparse product table overflow"); return -1; }
    return 0;
 }

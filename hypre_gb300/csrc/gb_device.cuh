@@ -211,3 +211,97 @@ __device__ __forceinline__ void gb_tab_clear(GbTab &t, int n)
 #define GB_SMEM_CAP 1024
 #define GB_SMEM_WARPS 4
 #define GB_SMEM_BYTES (GB_SMEM_WARPS * GB_TAB_INTS(GB_SMEM_CAP) * 4)
+
+// ---------------------------------------------------------------------------
+// Compact table for long rows in shared memory: keys (int) and positions
+// (16 bit) only, 6 bytes per slot, so more warps fit on an SM.  Without the
+// key list the table is cleared by sweeping all slots.  listcap bounds the
+// load factor (3/4 of the slots).
+// ---------------------------------------------------------------------------
+struct GbTabC
+{
+   int *hk;
+   unsigned short *hp;
+   int cap, listcap;
+};
+
+#define GB_TABC_BYTES(cap) ((cap) * 6)
+
+__device__ __forceinline__ GbTabC gb_tabc_at(char *base, int cap)
+{
+   GbTabC t;
+   t.cap = cap;
+   t.listcap = cap / 4 * 3;
+   t.hk = (int *) base;
+   t.hp = (unsigned short *) (base + (size_t) cap * 4);
+   return t;
+}
+
+__device__ __forceinline__ void gb_tab_init(GbTabC &t)
+{
+   for (int k = gb_lane(); k < t.cap; k += 32) { t.hk[k] = -1; }
+   __syncwarp();
+}
+
+__device__ __forceinline__ int gb_tabc_find(const GbTabC &t, int key)
+{
+   unsigned s = gb_hash(key) & (t.cap - 1);
+   for (int probe = 0; probe < t.cap; probe++)
+   {
+      int k = t.hk[s];
+      if (k == key) { return t.hp[s]; }
+      if (k < 0) { return -1; }
+      s = (s + 1) & (t.cap - 1);
+   }
+   return -1;
+}
+
+__device__ __forceinline__ int gb_tabc_insert(GbTabC &t, int key, int pos)
+{
+   unsigned s = gb_hash(key) & (t.cap - 1);
+   for (int probe = 0; probe < t.cap; probe++)
+   {
+      int prev = atomicCAS(&t.hk[s], -1, key);
+      if (prev < 0 || prev == key) { t.hp[s] = (unsigned short) pos; return (int) s; }
+      s = (s + 1) & (t.cap - 1);
+   }
+   return -1;
+}
+
+// Ordered insertion with the semantics of gb_winsert (positions in the order
+// of first discovery, lanes in order within a step).
+__device__ __forceinline__ int gb_winsert(GbTabC &t, int &count, int key, bool active, bool &created, int &ovf)
+{
+   const int lane = gb_lane();
+   int pos = active ? gb_tabc_find(t, key) : -1;
+   bool need = active && pos < 0;
+   int mkey = need ? key : -(lane + 2);
+   unsigned grp = __match_any_sync(GB_FULL, mkey);
+   int leader = __ffs(grp) - 1;
+   bool lead = need && leader == lane;
+   unsigned newmask = __ballot_sync(GB_FULL, lead);
+   bool bad = false;
+   if (lead)
+   {
+      int p = count + __popc(newmask & ((1u << lane) - 1u));
+      int slot = p < t.listcap ? gb_tabc_insert(t, key, p) : -1;
+      if (slot >= 0) { pos = p; }
+      else { bad = true; pos = -1; }
+   }
+   int lp = __shfl_sync(GB_FULL, pos, leader);
+   if (need && !lead) { pos = lp; }
+   count += __popc(newmask);
+   if (count > t.listcap) { count = t.listcap; }
+   if (__any_sync(GB_FULL, bad)) { ovf = 1; }
+   created = lead;
+   __syncwarp();
+   return pos;
+}
+
+__device__ __forceinline__ void gb_tab_clear(GbTabC &t, int n)
+{
+   (void) n;
+   __syncwarp();
+   for (int k = gb_lane(); k < t.cap; k += 32) { t.hk[k] = -1; }
+   __syncwarp();
+}

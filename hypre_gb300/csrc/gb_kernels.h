@@ -82,9 +82,13 @@ void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, const doubl
                        int *Tj, double *Tv, cudaStream_t s);
 void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int *ub,
                   cudaStream_t s);
+/* ordered sparse product, tier 0 (small shared tables, all rows), 1 (large
+ * shared tables, rows in ovf_list, overflow to out_list) or 2 (global tables,
+ * rows in ovf_list); phase 0 symbolic, 1 numeric */
 void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av, const int *Bi,
                const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list,
-               int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int phase, int tier, cudaStream_t s);
+               int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab, int gcap, int gwarps, int *err,
+               int phase, int tier, cudaStream_t s);
 void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 /* aggressive coarsening (gb_agg.cu) */
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);

@@ -1076,14 +1076,38 @@ extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, 
 // Tiers: shared-memory tables first, overflowing rows rebuilt with global
 // tables.
 // ---------------------------------------------------------------------------
-template <bool GLOBAL, bool NUMERIC>
+// Tiers of the ordered sparse product, by the row's number of distinct
+// output columns: MODE 0 every row, 1024-slot tables in shared memory (4 warps
+// per block); MODE 1 the rows MODE 0 could not hold (list in ovf_list),
+// compact 2048-slot tables in shared memory (rows up to 1536 columns, 4 warps
+// per block, 12 KB per warp); MODE 2 the
+// rows MODE 1 could not hold (list in ovf_list), tables in global memory.
+// The symbolic pass of MODE 0 / MODE 1 appends the rows it cannot hold to
+// ovf_list / out_list; the numeric pass of MODE 0 / 1 skips rows longer than
+// its list capacity.
+#define GB_BIG_CAP 2048
+#define GB_BIG_WARPS 4
+#define GB_BIG_BYTES (GB_BIG_WARPS * GB_TABC_BYTES(GB_BIG_CAP))
+
+template <int MODE> struct SpgemmTab { typedef GbTab type; };
+template <> struct SpgemmTab<1> { typedef GbTabC type; };
+
+template <int MODE>
+__device__ __forceinline__ typename SpgemmTab<MODE>::type spgemm_tab(int *sh, int *gtab, int gcap, int warp)
+{
+   if constexpr (MODE == 1) { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TABC_BYTES(GB_BIG_CAP), GB_BIG_CAP); }
+   else if constexpr (MODE == 2) { return gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap); }
+   else { return gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP); }
+}
+
+template <int MODE, bool NUMERIC>
 __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, const int *__restrict__ Ai,
                                                 const int *__restrict__ Aj, const double *__restrict__ Av,
                                                 const int *__restrict__ Bi, const int *__restrict__ Bj,
                                                 const double *__restrict__ Bv, int *__restrict__ cnt,
                                                 const int *__restrict__ Ci, int *__restrict__ Cj,
-                                                double *__restrict__ Cv, int *ovf_list, int *ovf_n, int *gtab,
-                                                int gcap, int *err)
+                                                double *__restrict__ Cv, int *ovf_list, int *ovf_n, int *out_list,
+                                                int *out_n, int *gtab, int gcap, int *err)
 {
    extern __shared__ int sh[];
    __shared__ double stage_all[128];
@@ -1091,19 +1115,18 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
    double *stage = stage_all + (threadIdx.x & ~31);
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;
-   GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
-                    : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
-   if (!GLOBAL) { gb_tab_init(T); }
-   int total = GLOBAL ? *ovf_n : nrows;
+   typename SpgemmTab<MODE>::type T = spgemm_tab<MODE>(sh, gtab, gcap, warp);
+   if (MODE != 2) { gb_tab_init(T); }
+   int total = MODE ? *ovf_n : nrows;
    const int per = W > 0 ? 32 / W : 1;
    for (int t = warp; t < total; t += nwarps)
    {
-      int r = GLOBAL ? ovf_list[t] : t;
+      int r = MODE ? ovf_list[t] : t;
       int off = 0;
       if (NUMERIC)
       {
          off = Ci[r];
-         if (!GLOBAL && Ci[r + 1] - off > T.listcap) { continue; }
+         if (MODE != 2 && Ci[r + 1] - off > T.listcap) { continue; }
       }
       int count = 0, ovf = 0;
       bool created;
@@ -1186,7 +1209,8 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
       if (lane == 0)
       {
          if (!ovf) { if (!NUMERIC) { cnt[r] = count; } }
-         else if (!GLOBAL && !NUMERIC) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         else if (MODE == 0 && !NUMERIC) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         else if (MODE == 1 && !NUMERIC) { out_list[atomicAdd(out_n, 1)] = r; cnt[r] = 0; }
          else { atomicExch(err, 1); }
       }
       gb_tab_clear(T, count);
@@ -1231,16 +1255,18 @@ extern "C" void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, co
 // W: lane-group width for B rows of at most W entries (power of two <= 32), 0 for long rows.
 extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av,
                           const int *Bi, const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj,
-                          double *Cv, int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err, int phase,
-                          int tier, cudaStream_t s)
+                          double *Cv, int *ovf_list, int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab,
+                          int gcap, int gwarps, int *err, int phase, int tier, cudaStream_t s)
 {
    static int attr_done = 0;
    if (!attr_done)
    {
-      /* 48 KB of tables plus the static staging array exceed the default
-       * dynamic shared-memory limit: opt in once */
-      cudaFuncSetAttribute(k_spgemm<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
-      cudaFuncSetAttribute(k_spgemm<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
+      /* the tables plus the static staging array exceed the default dynamic
+       * shared-memory limit: opt in once */
+      cudaFuncSetAttribute(k_spgemm<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
+      cudaFuncSetAttribute(k_spgemm<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
+      cudaFuncSetAttribute(k_spgemm<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_BIG_BYTES);
+      cudaFuncSetAttribute(k_spgemm<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_BIG_BYTES);
       attr_done = 1;
    }
    if (tier == 0)
@@ -1248,13 +1274,32 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
       int blocks = gb_smem_blocks(nrows);
       if (phase == 0)
       {
-         k_spgemm<false, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
-                                                                   Cj, Cv, ovf_list, ovf_n, nullptr, 0, err);
+         k_spgemm<0, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
+                                                               Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err);
       }
       else
       {
-         k_spgemm<false, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
-                                                                  Cj, Cv, ovf_list, ovf_n, nullptr, 0, err);
+         k_spgemm<0, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
+                                                              Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err);
+      }
+   }
+   else if (tier == 1)
+   {
+      /* persistent: four blocks of four warps per SM, grid-stride over the list */
+      long long want = ((long long) nlist + GB_BIG_WARPS - 1) / GB_BIG_WARPS;
+      int blocks = (int) (want < 152 * 4 ? (want > 0 ? want : 1) : 152 * 4);
+      int threads = 32 * GB_BIG_WARPS;
+      if (phase == 0)
+      {
+         k_spgemm<1, false><<<blocks, threads, GB_BIG_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
+                                                                  Cj, Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0,
+                                                                  err);
+      }
+      else
+      {
+         k_spgemm<1, true><<<blocks, threads, GB_BIG_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
+                                                                 Cj, Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0,
+                                                                 err);
       }
    }
    else
@@ -1262,13 +1307,13 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
       int blocks = (gwarps + 3) / 4;
       if (phase == 0)
       {
-         k_spgemm<true, false><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
-                                                      ovf_list, ovf_n, gtab, gcap, err);
+         k_spgemm<2, false><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
+                                                   ovf_list, ovf_n, out_list, out_n, gtab, gcap, err);
       }
       else
       {
-         k_spgemm<true, true><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
-                                                     ovf_list, ovf_n, gtab, gcap, err);
+         k_spgemm<2, true><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
+                                                  ovf_list, ovf_n, out_list, out_n, gtab, gcap, err);
       }
    }
    GB_COUNT(1);
