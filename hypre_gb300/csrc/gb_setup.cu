@@ -1118,7 +1118,7 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
    typename SpgemmTab<MODE>::type T = spgemm_tab<MODE>(sh, gtab, gcap, warp);
    if (MODE != 2) { gb_tab_init(T); }
    int total = MODE ? *ovf_n : nrows;
-   const int per = W > 0 ? 32 / W : 1;
+   (void) W;
    for (int t = warp; t < total; t += nwarps)
    {
       int r = MODE ? ovf_list[t] : t;
@@ -1136,74 +1136,83 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
          if (NUMERIC && lane == 0 && pos >= 0) { Cj[off + pos] = r; Cv[off + pos] = 0.0; }
          __syncwarp();
       }
-      const int ka0 = Ai[r], ka1 = Ai[r + 1];
-      for (int base = ka0; base < ka1 && !ovf; base += per)
+      // The row's products a_rk b_kc in sequential order (A entries in
+      // order, each B row in order), 32 per step: lane l takes the l-th
+      // product after the cursor (entry ka, offset off0 into its B row).
+      int ka = Ai[r];
+      const int ka1 = Ai[r + 1];
+      int off0 = 0;
+      while (ka < ka1 && !ovf)
       {
-         int kstart = 0, kend = 0;
-         int e = base + (W > 0 ? lane / W : 0);
-         double a = 0.0;
-         if (W > 0)
+         // lane i describes entry ka + i: remaining products and first B index
+         const int e = ka + lane;
+         int len = 0, kb0 = 0;
+         if (e < ka1)
          {
-            // batched: lane group of W lanes per A entry
-            bool act = false;
-            int col = -1;
-            double v = 0.0;
-            if (e < ka1)
-            {
-               int k = Aj[e];
-               int kb = Bi[k] + (lane % W);
-               if (kb < Bi[k + 1])
-               {
-                  act = true;
-                  col = Bj[kb];
-                  if (NUMERIC) { v = Av[e] * Bv[kb]; }
-               }
-            }
-            int pos = gb_winsert(T, count, col, act, created, ovf);
-            if (NUMERIC)
-            {
-               stage[lane] = v;
-               __syncwarp();
-               unsigned grp = __match_any_sync(GB_FULL, (act && pos >= 0) ? pos : -(lane + 2));
-               int leader = __ffs(grp) - 1;
-               if (act && pos >= 0 && lane == leader)
-               {
-                  double x;
-                  if (created) { Cj[off + pos] = col; x = v; }
-                  else { x = Cv[off + pos] + v; }
-                  unsigned rest = grp & (grp - 1u);
-                  while (rest)
-                  {
-                     int m = __ffs(rest) - 1;
-                     rest &= rest - 1u;
-                     x += stage[m];
-                  }
-                  Cv[off + pos] = x;
-               }
-               __syncwarp();
-            }
-            continue;
+            const int k = Aj[e];
+            kb0 = Bi[k];
+            len = Bi[k + 1] - kb0;
+            if (lane == 0) { kb0 += off0; len -= off0; }
          }
-         // long B rows: one A entry, chunks of 32
+         int pre = len;   // inclusive prefix over lanes
+         for (int o = 1; o < 32; o <<= 1)
          {
-            int k = Aj[base];
-            if (NUMERIC) { a = Av[base]; }
-            kstart = Bi[k];
-            kend = Bi[k + 1];
+            int y = __shfl_up_sync(GB_FULL, pre, o);
+            if (lane >= o) { pre += y; }
          }
-         for (int cb = kstart; cb < kend && !ovf; cb += 32)
+         const int total = __shfl_sync(GB_FULL, pre, 31);
+         // entry j of lane's product l = lane: smallest j with pre_j > l
+         int lo = 0, hi = 31;
+         for (int it = 0; it < 5; it++)
          {
-            int kb = cb + lane;
-            bool act = kb < kend;
-            int col = act ? Bj[kb] : -1;
-            int pos = gb_winsert(T, count, col, act, created, ovf);
-            if (NUMERIC && act && pos >= 0)
+            int mid = (lo + hi) >> 1;
+            int pm = __shfl_sync(GB_FULL, pre, mid);
+            if (pm > lane) { hi = mid; } else { lo = mid + 1; }
+         }
+         const int j = lo;
+         const int prej = __shfl_sync(GB_FULL, pre, j > 0 ? j - 1 : 0);
+         const int kbj = __shfl_sync(GB_FULL, kb0, j);
+         const bool act = lane < total;
+         int col = -1;
+         double v = 0.0;
+         if (act)
+         {
+            const int kb = kbj + (lane - (j > 0 ? prej : 0));
+            col = Bj[kb];
+            if (NUMERIC) { v = Av[ka + j] * Bv[kb]; }
+         }
+         int pos = gb_winsert(T, count, col, act, created, ovf);
+         if (NUMERIC)
+         {
+            stage[lane] = v;
+            __syncwarp();
+            unsigned grp = __match_any_sync(GB_FULL, (act && pos >= 0) ? pos : -(lane + 2));
+            int leader = __ffs(grp) - 1;
+            if (act && pos >= 0 && lane == leader)
             {
-               double v = a * Bv[kb];
-               if (created) { Cj[off + pos] = col; Cv[off + pos] = v; }
-               else { Cv[off + pos] += v; }
+               double x;
+               if (created) { Cj[off + pos] = col; x = v; }
+               else { x = Cv[off + pos] + v; }
+               unsigned rest = grp & (grp - 1u);
+               while (rest)
+               {
+                  int m = __ffs(rest) - 1;
+                  rest &= rest - 1u;
+                  x += stage[m];
+               }
+               Cv[off + pos] = x;
             }
             __syncwarp();
+         }
+         // advance the cursor past the consumed products
+         const int consumed = total < 32 ? total : 32;
+         const int nfull = __popc(__ballot_sync(GB_FULL, pre <= consumed));
+         if (nfull == 0) { off0 += consumed; }
+         else
+         {
+            const int pn = __shfl_sync(GB_FULL, pre, nfull - 1);
+            off0 = nfull < 32 ? consumed - pn : 0;
+            ka += nfull;
          }
       }
       if (lane == 0)
