@@ -257,32 +257,29 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    gb_tier t;
    tier_begin(&t, n);
    int *list2 = NULL, *n2 = (int *) gb_dcalloc(sizeof(int) * 2);
-   /* lane-group width from B's longest row */
-   gb_rowlen_max(B->nr, B->i, t.err + 1, s);
-   int maxb = read_int(t.err + 1);
-   int W = 0;
-   if (maxb <= 32) { W = 1; while (W < maxb) { W <<= 1; } }
-   /* symbolic: small shared tables, then large shared tables for the rows
+   const int W = 0;   /* products are flattened 32 per step; no lane groups */
+   /* upper bound of each row's length (products, capped by B's columns):
+    * rows that cannot fit the small tables skip the first tier */
+   int *ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+   gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+   /* symbolic: small shared tables, then compact shared tables for the rows
     * that did not fit, then global tables for the rest */
    gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, NULL,
-             n, NULL, 0, 0, t.err, 0, 0, s);
+             n, NULL, 0, 0, t.err, ub, 0, 0, s);
    int h1 = read_int(t.ovf_n), h2 = 0;
    if (h1 > 0)
    {
       list2 = (int *) gb_dmalloc(sizeof(int) * (size_t) h1);
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, list2,
-                n2, h1, NULL, 0, 0, t.err, 0, 1, s);
+                n2, h1, NULL, 0, 0, t.err, NULL, 0, 1, s);
       h2 = read_int(n2);
    }
-   int *ub = NULL;
    if (h2 > 0)
    {
-      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
-      gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
       /* global tables for the rows of the second list */
       tier_global_n(&t, ub, n, h2);
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, list2, n2, NULL, NULL, h2,
-                t.gtab, t.gcap, t.gwarps, t.err, 0, 2, s);
+                t.gtab, t.gcap, t.gwarps, t.err, NULL, 0, 2, s);
    }
    C->nr = n; C->nc = B->nc;
    C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
@@ -291,16 +288,16 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
    /* numeric: the same three tiers (each skips rows longer than its tables) */
    gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL, NULL,
-             n, NULL, 0, 0, t.err, 1, 0, s);
+             n, NULL, 0, 0, t.err, NULL, 1, 0, s);
    if (h1 > 0)
    {
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL,
-                NULL, h1, NULL, 0, 0, t.err, 1, 1, s);
+                NULL, h1, NULL, 0, 0, t.err, NULL, 1, 1, s);
    }
    if (h2 > 0)
    {
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, list2, n2, NULL, NULL, h2,
-                t.gtab, t.gcap, t.gwarps, t.err, 1, 2, s);
+                t.gtab, t.gcap, t.gwarps, t.err, NULL, 1, 2, s);
    }
    int e = tier_end(&t);
    gb_dfree(ub); gb_dfree(cnt); gb_dfree(list2); gb_dfree(n2);
@@ -1158,7 +1155,7 @@ static void twostage_gs_f(gb_amg *amg, int l, int inner, const float *f, float *
    float *V = L->Vf, *Z = L->U2f;
    if (u_zero) { gb_fill_f(L->n, u, 0.f, s); gb_scaled_copy_f(L->n, w, f, V, s); }
    else { gb_spmv_f(A, u, V, 0, -w, w, f, NULL, 0.f, NULL, NULL, s); }
-   gb_gs_first_f(L->n, L->A->A.i, A->v, vp, V, u, s);
+   gb_gs_first_f(L->n, L->A->A.i, A->v, vp, A->rs, V, u, s);
    float m = -1.f;
    for (int k = 0; k < inner; k++)
    {

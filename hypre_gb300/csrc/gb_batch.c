@@ -31,6 +31,8 @@ typedef struct
    double  *relres_h, *hist_h;
    double  *r, *p, *s;
    double  *opc;          /* per-system operator complexity (host) */
+   double  *dinv;         /* coarsest level: inverse of each system's block (device) */
+   long long *doff_d;
    int      sms;
    float    tune_ms[4][3];
 } gb_batch;
@@ -63,6 +65,9 @@ static void batch_free_setup(gb_batch *b)
    b->r = b->p = b->s = NULL;
    free(b->opc);
    b->opc = NULL;
+   gb_dfree(b->dinv); gb_dfree(b->doff_d);
+   b->dinv = NULL;
+   b->doff_d = NULL;
    b->nlev = 0;
 }
 
@@ -239,7 +244,8 @@ HYPRE_Int HYPRE_GB300_BatchedPCGSetup(HYPRE_Solver solver, HYPRE_Solver amg_solv
    /* one BoomerAMG setup for the whole block-diagonal matrix */
    if (gb_amg_setup(amg, A)) { batch_free_setup(b); return gb_error_flag; }
    int nl = amg->num_levels;
-   if (!amg->coarse_inv)
+   int ct = prm->relax_type[3];
+   if (!(ct == 9 || ct == 19 || ct == 98 || ct == 99))
    {
       gb_error(HYPRE_ERROR_GENERIC, "batched PCG: the coarsest level needs a direct solve (relax 9/19/98/99)");
       batch_free_setup(b);
@@ -272,6 +278,36 @@ HYPRE_Int HYPRE_GB300_BatchedPCGSetup(HYPRE_Solver solver, HYPRE_Solver amg_solv
       b->off_h[l + 1] = o;
       b->off_d[l + 1] = (int *) gb_dmalloc(ob);
       cudaMemcpyAsync(b->off_d[l + 1], o, ob, cudaMemcpyHostToDevice, st);
+   }
+   /* coarsest level: the inverse of each system's diagonal block */
+   {
+      const int *oc = b->off_h[nl - 1];
+      long long *doff = (long long *) malloc(sizeof(long long) * (size_t) (num_systems + 1));
+      doff[0] = 0;
+      int mmax = 0;
+      for (int s = 0; s < num_systems; s++)
+      {
+         long long m = oc[s + 1] - oc[s];
+         if (m > mmax) { mmax = (int) m; }
+         doff[s + 1] = doff[s] + m * m;
+      }
+      if (mmax > 2048)
+      {
+         free(doff);
+         gb_error(HYPRE_ERROR_GENERIC, "batched PCG: a system's coarsest block exceeds 2048 rows");
+         batch_free_setup(b);
+         return gb_error_flag;
+      }
+      size_t tot = sizeof(double) * (size_t) (doff[num_systems] > 0 ? doff[num_systems] : 1);
+      b->dinv = (double *) gb_dmalloc(tot);
+      double *W = (double *) gb_dmalloc(tot);
+      b->doff_d = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (num_systems + 1));
+      cudaMemcpyAsync(b->doff_d, doff, sizeof(long long) * (size_t) (num_systems + 1), cudaMemcpyHostToDevice, st);
+      gb_csr *Ac = &amg->lev[nl - 1].A->A;
+      gb_block_inverse(num_systems, b->off_d[nl - 1], Ac->i, Ac->j, Ac->v, b->doff_d, b->dinv, W, st);
+      gb_sync();
+      gb_dfree(W);
+      free(doff);
    }
    /* per-system operator complexity: sum over levels of the system's nonzeros / level-0 nonzeros */
    b->opc = (double *) calloc((size_t) num_systems, sizeof(double));
@@ -367,7 +403,7 @@ static void launch(gb_batch *b, const double *bd, double *xd, int lpr, int block
    if (grid > b->nsys) { grid = b->nsys; }
    gb_batch_pcg(b->lev_d[b->prec == GB_PREC_F64 ? 0 : 1], b->nlev, b->nsys, amg->prm.num_sweeps[1],
                 amg->prm.num_sweeps[2], b->A->A.i, b->A->A.j, b->A->A.v, b->order_d, b->counter_d, bd, xd, b->r,
-                b->p, b->s, amg->coarse_inv, amg->coarse_n, b->tol, b->maxit, b->iters_d, b->relres_d, b->hist_d,
+                b->p, b->s, b->dinv, b->doff_d, b->tol, b->maxit, b->iters_d, b->relres_d, b->hist_d,
                 b->prec, lpr, grid, block, gb_stream());
 }
 

@@ -42,8 +42,8 @@ typedef struct
    int *counter;
    const double *b;
    double *x, *r, *p, *s;
-   const double *Dinv;       // coarsest level, dense inverse (nc x nc)
-   int nc;
+   const double *Dinv;       // coarsest level: inverse of each system's block
+   const long long *doff;    // its offset in Dinv (block s is m x m, m its coarsest rows)
    double tol;
    int maxit;
    int *iters;
@@ -152,7 +152,8 @@ __device__ void vcycle(const gb_batch_args &A, int sys, const double *r0, double
       for (int i = a + threadIdx.x; i < b; i += blockDim.x)
       {
          double s = 0.0;
-         for (int j = a; j < b; j++) { s += A.Dinv[(size_t) i * A.nc + j] * (double) F[j]; }
+         const double *Ds = A.Dinv + A.doff[sys] + (size_t) (i - a) * (b - a);
+         for (int j = a; j < b; j++) { s += Ds[j - a] * (double) F[j]; }
          U[i] = (CT) s;
       }
       __syncthreads();
@@ -310,7 +311,7 @@ extern "C" void gb_check_blockdiag(int n, const int *Ai, const int *Aj, const in
 extern "C" void gb_batch_pcg(const void *lev_dev, int nlev, int nsys, int sweeps_down, int sweeps_up,
                              const int *Ai, const int *Aj, const double *Av, const int *order, int *counter,
                              const double *b, double *x, double *r, double *p, double *sv, const double *Dinv,
-                             int nc, double tol, int maxit, int *iters, double *relres, double *hist, int prec,
+                             const long long *doff, double tol, int maxit, int *iters, double *relres, double *hist, int prec,
                              int lpr, int grid, int block, cudaStream_t s)
 {
    gb_batch_args A;
@@ -322,7 +323,7 @@ extern "C" void gb_batch_pcg(const void *lev_dev, int nlev, int nsys, int sweeps
    A.Ai = Ai; A.Aj = Aj; A.Av = Av;
    A.order = order; A.counter = counter;
    A.b = b; A.x = x; A.r = r; A.p = p; A.s = sv;
-   A.Dinv = Dinv; A.nc = nc;
+   A.Dinv = Dinv; A.doff = doff;
    A.tol = tol; A.maxit = maxit;
    A.iters = iters; A.relres = relres; A.hist = hist;
    cudaMemsetAsync(counter, 0, sizeof(int), s);

@@ -26,6 +26,7 @@ gb_parcsr *gb_parcsr_wrap(gb_csr A, int owns)
 static void solveform_free(gb_solveform *f)
 {
    gb_dfree(f->vals); gb_dfree(f->sl_ptr); gb_dfree(f->sl_w); gb_dfree(f->sl_j); gb_dfree(f->sl_v);
+   gb_dfree(f->rs);
    memset(f, 0, sizeof(*f));
 }
 
@@ -64,6 +65,18 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
    f->desc.j = A->j;
    double avg = A->nr ? (double) A->nnz / A->nr : 0;
    f->desc.K = lanes_for(avg);
+   /* FP16 forms hold row-scaled values a_ij / a_ii (unit diagonal) with the
+    * diagonal kept in FP32, so coefficients of any magnitude stay in range */
+   const double *vsrc = A->v;
+   double *scaled = NULL;
+   if (vprec == GB_PREC_F16)
+   {
+      scaled = (double *) gb_dmalloc(sizeof(double) * (size_t) (A->nnz ? A->nnz : 1));
+      f->rs = (float *) gb_dmalloc(sizeof(float) * (size_t) (A->nr ? A->nr : 1));
+      gb_row_scaled_vals(A->nr, A->i, A->v, scaled, f->rs, s);
+      vsrc = scaled;
+      f->desc.rs = f->rs;
+   }
    /* SELL-32 when rows are short and nearly uniform (little padding) */
    int use_sell = 0;
    int nsl = (A->nr + 31) / 32;
@@ -73,7 +86,7 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
    {
       sl_w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
       sl_ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));
-      gb_sell_build(A->nr, A->i, A->j, A->v, vprec, nsl, sl_w, sl_ptr, NULL, NULL, s, 0);
+      gb_sell_build(A->nr, A->i, A->j, vsrc, vprec, nsl, sl_w, sl_ptr, NULL, NULL, s, 0);
       long long tot = 0;
       cudaMemcpyAsync(&tot, sl_ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
       gb_sync();
@@ -84,7 +97,7 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
          size_t vb = vprec == GB_PREC_F64 ? 8 : vprec == GB_PREC_F32 ? 4 : 2;
          int *sl_j = (int *) gb_dmalloc(sizeof(int) * (size_t) tot);
          void *sl_v = gb_dmalloc(vb * (size_t) tot);
-         gb_sell_build(A->nr, A->i, A->j, A->v, vprec, nsl, sl_w, sl_ptr, sl_j, sl_v, s, 1);
+         gb_sell_build(A->nr, A->i, A->j, vsrc, vprec, nsl, sl_w, sl_ptr, sl_j, sl_v, s, 1);
          f->sl_ptr = sl_ptr; f->sl_w = sl_w; f->sl_j = sl_j; f->sl_v = sl_v;
          f->desc.fmt = GB_FMT_SELL;
          f->desc.nslices = nsl;
@@ -98,9 +111,10 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
    {
       size_t vb = vprec == GB_PREC_F32 ? 4 : 2;
       f->vals = gb_dmalloc(vb * (size_t) (A->nnz ? A->nnz : 1));
-      gb_convert_vals(A->nnz, A->v, f->vals, vprec, s);
+      gb_convert_vals(A->nnz, vsrc, f->vals, vprec, s);
       f->desc.v = f->vals;
    }
+   if (scaled) { gb_sync(); gb_dfree(scaled); }
    if (!use_sell) { f->desc.fmt = GB_FMT_CSR; }
    f->valid = 1;
    return &f->desc;

@@ -65,6 +65,7 @@ typedef struct
    int         *sl_w;
    int         *sl_j;
    void        *sl_v;
+   float       *rs;        /* FP16 form: row scales a_ii */
 } gb_solveform;
 
 struct hypre_ParCSRMatrix_struct

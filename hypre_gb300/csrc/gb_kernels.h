@@ -43,6 +43,7 @@ typedef struct
    const int *sl_w;
    const int *sl_j;
    const void *sl_v;
+   const float *rs;      /* FP16 forms: values are a_ij / a_ii, rs[i] = a_ii (NULL otherwise) */
 } gb_spmv_desc;
 
 /* runtime */
@@ -82,13 +83,14 @@ void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, const doubl
                        int *Tj, double *Tv, cudaStream_t s);
 void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int *ub,
                   cudaStream_t s);
-/* ordered sparse product, tier 0 (small shared tables, all rows), 1 (large
+/* ordered sparse product, tier 0 (small shared tables, all rows; with ub,
+ * rows whose upper bound exceeds the table go straight to the list), 1 (large
  * shared tables, rows in ovf_list, overflow to out_list) or 2 (global tables,
  * rows in ovf_list); phase 0 symbolic, 1 numeric */
 void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av, const int *Bi,
                const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list,
                int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab, int gcap, int gwarps, int *err,
-               int phase, int tier, cudaStream_t s);
+               const int *ub, int phase, int tier, cudaStream_t s);
 void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 /* aggressive coarsening (gb_agg.cu) */
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);
@@ -112,6 +114,8 @@ void gb_p1_len(int n, const int *CF, const int *f2f, const int *Wi, int *len, cu
 void gb_p1_fill(int n, const int *CF, const int *f2c, const int *f2f, const int *Wi, const int *Wj, const double *Wv,
                 const int *Pi, int *Pj, double *Pv, cudaStream_t s);
 void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, double *l1, cudaStream_t s);
+void gb_block_inverse(int nsys, const int *off, const int *Ai, const int *Aj, const double *Av,
+                      const long long *doff, double *D, double *W, cudaStream_t s);
 void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, double *D, double *W, cudaStream_t s);
 
 /* solve phase */
@@ -122,8 +126,10 @@ void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int mode, float 
 void gb_sell_build(int n, const int *Ai, const int *Aj, const double *Av, int vprec, int nslices, int *sl_w,
                    long long *sl_ptr, int *sl_j, void *sl_v, cudaStream_t s, int stage);
 void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s);
+void gb_row_scaled_vals(int n, const int *Ai, const double *Av, double *out, float *rs, cudaStream_t s);
 void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s);
-void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, float *v, float *u, cudaStream_t s);
+void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, const float *rs, float *v, float *u,
+                   cudaStream_t s);
 void gb_gs_lower_d(int n, const int *Ai, const int *Aj, const double *Av, const double *z, double *znew, double *u,
                    double m, cudaStream_t s);
 void gb_gs_lower_f(int n, const int *Ai, const int *Aj, const void *Av, int vprec, const float *z, float *znew,
@@ -143,7 +149,8 @@ void gb_fill_d(long long n, double *x, double v, cudaStream_t s);
 void gb_check_blockdiag(int n, const int *Ai, const int *Aj, const int *off, int nsys, int *bad, cudaStream_t s);
 void gb_batch_pcg(const void *lev_dev, int nlev, int nsys, int sweeps_down, int sweeps_up, const int *Ai,
                   const int *Aj, const double *Av, const int *order, int *counter, const double *b, double *x,
-                  double *r, double *p, double *sv, const double *Dinv, int nc, double tol, int maxit, int *iters,
+                  double *r, double *p, double *sv, const double *Dinv, const long long *doff, double tol, int maxit,
+                  int *iters,
                   double *relres, double *hist, int prec, int lpr, int grid, int block, cudaStream_t s);
 size_t gb_blevel_size(void);
 /* learned parameters (gb_mlp.cu) */

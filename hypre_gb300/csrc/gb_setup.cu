@@ -1107,7 +1107,7 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
                                                 const double *__restrict__ Bv, int *__restrict__ cnt,
                                                 const int *__restrict__ Ci, int *__restrict__ Cj,
                                                 double *__restrict__ Cv, int *ovf_list, int *ovf_n, int *out_list,
-                                                int *out_n, int *gtab, int gcap, int *err)
+                                                int *out_n, int *gtab, int gcap, int *err, const int *__restrict__ ub)
 {
    extern __shared__ int sh[];
    __shared__ double stage_all[128];
@@ -1123,6 +1123,13 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
    {
       int r = MODE ? ovf_list[t] : t;
       int off = 0;
+      if (MODE == 0 && !NUMERIC && ub && ub[r] > 16 * T.listcap)
+      {
+         // far more products than the table holds (at most 16 per distinct
+         // column on average would be needed to fit): straight to the next tier
+         if (lane == 0) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         continue;
+      }
       if (NUMERIC)
       {
          off = Ci[r];
@@ -1265,7 +1272,7 @@ extern "C" void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, co
 extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av,
                           const int *Bi, const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj,
                           double *Cv, int *ovf_list, int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab,
-                          int gcap, int gwarps, int *err, int phase, int tier, cudaStream_t s)
+                          int gcap, int gwarps, int *err, const int *ub, int phase, int tier, cudaStream_t s)
 {
    static int attr_done = 0;
    if (!attr_done)
@@ -1284,12 +1291,12 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
       if (phase == 0)
       {
          k_spgemm<0, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
-                                                               Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err);
+                                                               Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
       }
       else
       {
          k_spgemm<0, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
-                                                              Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err);
+                                                              Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
       }
    }
    else if (tier == 1)
@@ -1302,13 +1309,13 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
       {
          k_spgemm<1, false><<<blocks, threads, GB_BIG_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
                                                                   Cj, Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0,
-                                                                  err);
+                                                                  err, ub);
       }
       else
       {
          k_spgemm<1, true><<<blocks, threads, GB_BIG_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
                                                                  Cj, Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0,
-                                                                 err);
+                                                                 err, ub);
       }
    }
    else
@@ -1317,12 +1324,12 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
       if (phase == 0)
       {
          k_spgemm<2, false><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
-                                                   ovf_list, ovf_n, out_list, out_n, gtab, gcap, err);
+                                                   ovf_list, ovf_n, out_list, out_n, gtab, gcap, err, ub);
       }
       else
       {
          k_spgemm<2, true><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
-                                                  ovf_list, ovf_n, out_list, out_n, gtab, gcap, err);
+                                                  ovf_list, ovf_n, out_list, out_n, gtab, gcap, err, ub);
       }
    }
    GB_COUNT(1);
@@ -1370,7 +1377,9 @@ __global__ void k_to_dense(int n, const int *__restrict__ Ai, const int *__restr
 }
 
 // One block; D (n x n, row major) is replaced by its inverse, W is n x n work.
-__global__ void k_gauss_jordan(int n, double *D, double *W)
+// Gauss-Jordan inverse of the n x n row-major D by one thread block (W: n x n
+// work); D is replaced by its inverse.
+__device__ void gj_block(int n, double *D, double *W)
 {
    // W = I
    for (int t = threadIdx.x; t < n * n; t += blockDim.x) { W[t] = (t / n == t % n) ? 1.0 : 0.0; }
@@ -1417,6 +1426,42 @@ __global__ void k_gauss_jordan(int n, double *D, double *W)
       __syncthreads();
    }
    for (int t = threadIdx.x; t < n * n; t += blockDim.x) { D[t] = W[t]; }
+   __syncthreads();
+}
+
+__global__ void k_gauss_jordan(int n, double *D, double *W) { gj_block(n, D, W); }
+
+// Inverse of each diagonal block rows off[s]..off[s+1]-1 of a block-diagonal
+// CSR matrix (one thread block per system), stored at D + doff[s] (m x m).
+__global__ void k_block_inverse(int nsys, const int *__restrict__ off, const int *__restrict__ Ai,
+                                const int *__restrict__ Aj, const double *__restrict__ Av,
+                                const long long *__restrict__ doff, double *D, double *W)
+{
+   for (int sys = blockIdx.x; sys < nsys; sys += gridDim.x)
+   {
+      const int a = off[sys], m = off[sys + 1] - a;
+      double *Ds = D + doff[sys], *Ws = W + doff[sys];
+      for (int t = threadIdx.x; t < m * m; t += blockDim.x) { Ds[t] = 0.0; }
+      __syncthreads();
+      for (int r = threadIdx.x; r < m; r += blockDim.x)
+      {
+         for (int k = Ai[a + r]; k < Ai[a + r + 1]; k++)
+         {
+            int c = Aj[k] - a;
+            if (c >= 0 && c < m) { Ds[(size_t) r * m + c] = Av[k]; }
+         }
+      }
+      __syncthreads();
+      if (m > 0) { gj_block(m, Ds, Ws); }
+   }
+}
+
+extern "C" void gb_block_inverse(int nsys, const int *off, const int *Ai, const int *Aj, const double *Av,
+                                 const long long *doff, double *D, double *W, cudaStream_t s)
+{
+   int grid = nsys < 152 * 8 ? (nsys > 0 ? nsys : 1) : 152 * 8;
+   k_block_inverse<<<grid, 256, 0, s>>>(nsys, off, Ai, Aj, Av, doff, D, W);
+   GB_COUNT(1);
 }
 
 extern "C" void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, double *D, double *W,

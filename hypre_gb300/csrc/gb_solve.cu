@@ -81,7 +81,8 @@ template <int K, typename VT, typename XT>
 __global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
                                                   const VT *__restrict__ Av, const XT *__restrict__ x, XT *y,
                                                   int mode, XT alpha, XT beta, const XT *b, const XT *d, XT w,
-                                                  const XT *__restrict__ dotz, double *dpart)
+                                                  const XT *__restrict__ dotz, double *dpart,
+                                                  const float *__restrict__ rs)
 {
    typedef typename Acc<VT, XT>::T AT;
    const int gpw = 32 / K;                       // row groups per warp
@@ -103,7 +104,9 @@ __global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__
       for (int o = K / 2; o > 0; o >>= 1) { s += __shfl_down_sync(GB_FULL, s, o, K); }
       if (valid && lane == 0)
       {
-         XT yi = row_epilogue<XT>(mode, (XT) s, i, alpha, beta, b, x, d, w, y);
+         XT si = (XT) s;
+         if (rs) { si *= (XT) rs[i]; }
+         XT yi = row_epilogue<XT>(mode, si, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
@@ -125,7 +128,8 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
                                                    const int *__restrict__ sl_w, const int *__restrict__ Sj,
                                                    const VT *__restrict__ Sv, const XT *__restrict__ x, XT *y,
                                                    int mode, XT alpha, XT beta, const XT *b, const XT *d, XT w,
-                                                   const XT *__restrict__ dotz, double *dpart)
+                                                   const XT *__restrict__ dotz, double *dpart,
+                                                   const float *__restrict__ rs)
 {
    typedef typename Acc<VT, XT>::T AT;
    const int t = threadIdx.x & 31;
@@ -154,7 +158,9 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
       int i = s * 32 + t;
       if (i < n)
       {
-         XT yi = row_epilogue<XT>(mode, (XT) (acc0 + acc1), i, alpha, beta, b, x, d, w, y);
+         XT si = (XT) (acc0 + acc1);
+         if (rs) { si *= (XT) rs[i]; }
+         XT yi = row_epilogue<XT>(mode, si, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
@@ -276,7 +282,7 @@ static void spmv_dispatch(const gb_spmv_desc *A, const XT *x, XT *y, int mode, X
       int nsl = A->nslices;
       int blocks = dpart ? GB_RED_BLOCKS : nblk((long long) nsl * 32, T);
       k_spmv_sell<VT, XT><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, A->sl_j, (const VT *) A->sl_v, x, y,
-                                                 mode, alpha, beta, b, d, w, dotz, dpart);
+                                                 mode, alpha, beta, b, d, w, dotz, dpart, A->rs);
    }
    else
    {
@@ -284,7 +290,7 @@ static void spmv_dispatch(const gb_spmv_desc *A, const XT *x, XT *y, int mode, X
       long long threads = (long long) A->n * K;
       int blocks = dpart ? GB_RED_BLOCKS : nblk(threads, T);
       const VT *vals = (const VT *) A->v;
-#define LAUNCH_K(KK) k_spmv_csr<KK, VT, XT><<<blocks, T, 0, st>>>(A->n, A->i, A->j, vals, x, y, mode, alpha, beta, b, d, w, dotz, dpart)
+#define LAUNCH_K(KK) k_spmv_csr<KK, VT, XT><<<blocks, T, 0, st>>>(A->n, A->i, A->j, vals, x, y, mode, alpha, beta, b, d, w, dotz, dpart, A->rs)
       switch (K)
       {
          case 2: LAUNCH_K(2); break;
@@ -351,6 +357,25 @@ extern "C" void gb_sell_build(int n, const int *Ai, const int *Aj, const double 
    GB_COUNT(1);
 }
 
+// out = a_ij / a_ii row by row (the diagonal is each row's first entry),
+// rs[i] = a_ii: the FP16 forms store these so their range stays near 1
+__global__ void k_row_scaled(int n, const int *__restrict__ Ai, const double *__restrict__ Av,
+                             double *__restrict__ out, float *__restrict__ rs)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int b = Ai[i], e = Ai[i + 1];
+   double d = e > b ? Av[b] : 1.0;
+   if (d == 0.0) { d = 1.0; }
+   rs[i] = (float) d;
+   for (int k = b; k < e; k++) { out[k] = Av[k] / d; }
+}
+
+extern "C" void gb_row_scaled_vals(int n, const int *Ai, const double *Av, double *out, float *rs, cudaStream_t s)
+{
+   if (n > 0) { k_row_scaled<<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, out, rs); GB_COUNT(1); }
+}
+
 extern "C" void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s)
 {
    if (nnz <= 0) { return; }
@@ -397,11 +422,12 @@ __global__ void k_gs_lower(int n, const int *__restrict__ Ai, const int *__restr
 
 template <typename VT, typename XT>
 __global__ void k_gs_first(int n, const int *__restrict__ Ai, const VT *__restrict__ Av, XT *__restrict__ v,
-                           XT *__restrict__ u)
+                           XT *__restrict__ u, const float *__restrict__ rs)
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i >= n) { return; }
-   XT diag = (XT) Acc<VT, XT>::mul(Av[Ai[i]], (XT) 1);
+   // row-scaled FP16 values have a unit diagonal: the diagonal is rs[i]
+   XT diag = rs ? (XT) rs[i] : (XT) Acc<VT, XT>::mul(Av[Ai[i]], (XT) 1);
    XT z = v[i] / diag;
    v[i] = z;
    u[i] += z;
@@ -409,13 +435,17 @@ __global__ void k_gs_first(int n, const int *__restrict__ Ai, const VT *__restri
 
 extern "C" void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s)
 {
-   k_gs_first<double, double><<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, v, u);
+   k_gs_first<double, double><<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, v, u, nullptr);
    GB_COUNT(1);
 }
-extern "C" void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, float *v, float *u, cudaStream_t s)
+extern "C" void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, const float *rs, float *v, float *u,
+                              cudaStream_t s)
 {
-   if (vprec == GB_PREC_F16) { k_gs_first<__half, float><<<nblk(n, 256), 256, 0, s>>>(n, Ai, (const __half *) Av, v, u); }
-   else { k_gs_first<float, float><<<nblk(n, 256), 256, 0, s>>>(n, Ai, (const float *) Av, v, u); }
+   if (vprec == GB_PREC_F16)
+   {
+      k_gs_first<__half, float><<<nblk(n, 256), 256, 0, s>>>(n, Ai, (const __half *) Av, v, u, rs);
+   }
+   else { k_gs_first<float, float><<<nblk(n, 256), 256, 0, s>>>(n, Ai, (const float *) Av, v, u, nullptr); }
    GB_COUNT(1);
 }
 extern "C" void gb_gs_lower_d(int n, const int *Ai, const int *Aj, const double *Av, const double *z, double *znew,
