@@ -258,14 +258,13 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    tier_begin(&t, n);
    int *list2 = NULL, *n2 = (int *) gb_dcalloc(sizeof(int) * 2);
    const int W = 0;   /* products are flattened 32 per step; no lane groups */
-   /* upper bound of each row's length (products, capped by B's columns):
-    * rows that cannot fit the small tables skip the first tier */
-   int *ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
-   gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+   int *ub = NULL;
    /* symbolic: small shared tables, then compact shared tables for the rows
-    * that did not fit, then global tables for the rest */
+    * that did not fit, then global tables for the rest.  (Routing rows by an
+    * upper bound of their length was measured slower: the product count is a
+    * poor bound for rows of RA*P, which then leave the fast tier.) */
    gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, NULL,
-             n, NULL, 0, 0, t.err, ub, 0, 0, s);
+             n, NULL, 0, 0, t.err, NULL, 0, 0, s);
    int h1 = read_int(t.ovf_n), h2 = 0;
    if (h1 > 0)
    {
@@ -276,7 +275,9 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    }
    if (h2 > 0)
    {
-      /* global tables for the rows of the second list */
+      /* global tables for the rows of the second list, sized from upper bounds */
+      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+      gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
       tier_global_n(&t, ub, n, h2);
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, list2, n2, NULL, NULL, h2,
                 t.gtab, t.gcap, t.gwarps, t.err, NULL, 0, 2, s);

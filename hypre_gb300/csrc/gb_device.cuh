@@ -305,3 +305,60 @@ __device__ __forceinline__ void gb_tab_clear(GbTabC &t, int n)
    for (int k = gb_lane(); k < t.cap; k += 32) { t.hk[k] = -1; }
    __syncwarp();
 }
+
+// ---------------------------------------------------------------------------
+// Counting insertion for symbolic passes: only the number of distinct keys
+// matters, so each active lane inserts its key directly (one probe sequence
+// with atomicCAS) and the new keys are counted with a ballot; no discovery
+// order, no positions.  The slots of new keys are recorded in the key list
+// (GbTab) so the table can be cleared entry by entry.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int gb_tab_claim(int *hk, int cap, int key, bool &isnew)
+{
+   unsigned s = gb_hash(key) & (cap - 1);
+   for (int probe = 0; probe < cap; probe++)
+   {
+      int prev = atomicCAS(&hk[s], -1, key);
+      if (prev < 0) { isnew = true; return (int) s; }
+      if (prev == key) { isnew = false; return (int) s; }
+      s = (s + 1) & (cap - 1);
+   }
+   isnew = false;
+   return -1;
+}
+
+__device__ __forceinline__ void gb_wcount(GbTab &t, int &count, int key, bool active, int &ovf)
+{
+   const int lane = gb_lane();
+   bool isnew = false, bad = false;
+   int slot = -1;
+   if (active)
+   {
+      slot = gb_tab_claim(t.hk, t.cap, key, isnew);
+      if (slot < 0) { bad = true; }
+   }
+   unsigned m = __ballot_sync(GB_FULL, isnew);
+   if (isnew)
+   {
+      int p = count + __popc(m & ((1u << lane) - 1u));
+      if (p < t.listcap) { t.lslot[p] = slot; }
+      else { bad = true; }
+   }
+   count += __popc(m);
+   if (count > t.listcap) { count = t.listcap; bad = true; }
+   if (__any_sync(GB_FULL, bad)) { ovf = 1; }
+   __syncwarp();
+}
+
+__device__ __forceinline__ void gb_wcount(GbTabC &t, int &count, int key, bool active, int &ovf)
+{
+   bool isnew = false, bad = false;
+   if (active)
+   {
+      if (gb_tab_claim(t.hk, t.cap, key, isnew) < 0) { bad = true; }
+   }
+   count += __popc(__ballot_sync(GB_FULL, isnew));
+   if (count > t.listcap) { count = t.listcap; bad = true; }
+   if (__any_sync(GB_FULL, bad)) { ovf = 1; }
+   __syncwarp();
+}

@@ -1188,9 +1188,13 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
             col = Bj[kb];
             if (NUMERIC) { v = Av[ka + j] * Bv[kb]; }
          }
-         int pos = gb_winsert(T, count, col, act, created, ovf);
-         if (NUMERIC)
+         if (!NUMERIC)
          {
+            gb_wcount(T, count, col, act, ovf);
+         }
+         else
+         {
+            int pos = gb_winsert(T, count, col, act, created, ovf);
             stage[lane] = v;
             __syncwarp();
             unsigned grp = __match_any_sync(GB_FULL, (act && pos >= 0) ? pos : -(lane + 2));
