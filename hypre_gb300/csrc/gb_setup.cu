@@ -1077,8 +1077,8 @@ extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, 
 // tables.
 // ---------------------------------------------------------------------------
 // Tiers of the ordered sparse product, by the row's number of distinct
-// output columns: MODE 0 every row, 1024-slot tables in shared memory (4 warps
-// per block); MODE 1 the rows MODE 0 could not hold (list in ovf_list),
+// output columns: MODE 0 every row, compact 1024-slot tables in shared memory
+// (rows up to 768 columns, 4 warps per block, 6 KB per warp); MODE 1 the rows MODE 0 could not hold (list in ovf_list),
 // compact 2048-slot tables in shared memory (rows up to 1536 columns, 4 warps
 // per block, 12 KB per warp); MODE 2 the
 // rows MODE 1 could not hold (list in ovf_list), tables in global memory.
@@ -1089,15 +1089,18 @@ extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, 
 #define GB_BIG_WARPS 4
 #define GB_BIG_BYTES (GB_BIG_WARPS * GB_TABC_BYTES(GB_BIG_CAP))
 
-template <int MODE> struct SpgemmTab { typedef GbTab type; };
-template <> struct SpgemmTab<1> { typedef GbTabC type; };
+// tier 0: compact 1024-slot tables (6 KB per warp, rows up to 768 columns)
+#define GB_SMALL_BYTES (GB_SMEM_WARPS * GB_TABC_BYTES(GB_SMEM_CAP))
+
+template <int MODE> struct SpgemmTab { typedef GbTabC type; };
+template <> struct SpgemmTab<2> { typedef GbTab type; };
 
 template <int MODE>
 __device__ __forceinline__ typename SpgemmTab<MODE>::type spgemm_tab(int *sh, int *gtab, int gcap, int warp)
 {
    if constexpr (MODE == 1) { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TABC_BYTES(GB_BIG_CAP), GB_BIG_CAP); }
    else if constexpr (MODE == 2) { return gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap); }
-   else { return gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP); }
+   else { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TABC_BYTES(GB_SMEM_CAP), GB_SMEM_CAP); }
 }
 
 template <int MODE, bool NUMERIC>
@@ -1283,23 +1286,25 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
    {
       /* the tables plus the static staging array exceed the default dynamic
        * shared-memory limit: opt in once */
-      cudaFuncSetAttribute(k_spgemm<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
-      cudaFuncSetAttribute(k_spgemm<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM_BYTES);
+      cudaFuncSetAttribute(k_spgemm<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMALL_BYTES);
+      cudaFuncSetAttribute(k_spgemm<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMALL_BYTES);
       cudaFuncSetAttribute(k_spgemm<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_BIG_BYTES);
       cudaFuncSetAttribute(k_spgemm<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_BIG_BYTES);
       attr_done = 1;
    }
    if (tier == 0)
    {
-      int blocks = gb_smem_blocks(nrows);
+      /* eight blocks of four warps per SM (24 KB of tables each) */
+      long long want = ((long long) nrows + GB_SMEM_WARPS - 1) / GB_SMEM_WARPS;
+      int blocks = (int) (want < 152 * 8 ? (want > 0 ? want : 1) : 152 * 8);
       if (phase == 0)
       {
-         k_spgemm<0, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
+         k_spgemm<0, false><<<blocks, 128, GB_SMALL_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
                                                                Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
       }
       else
       {
-         k_spgemm<0, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
+         k_spgemm<0, true><<<blocks, 128, GB_SMALL_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
                                                               Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
       }
    }
