@@ -1148,22 +1148,22 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
       }
       // The row's products a_rk b_kc in sequential order (A entries in
       // order, each B row in order), 32 per step: lane l takes the l-th
-      // product after the cursor (entry ka, offset off0 into its B row).
+      // product after the cursor (entry ka, from its first unused B entry).
       int ka = Ai[r];
       const int ka1 = Ai[r + 1];
-      int off0 = 0;
+      // window: lane i holds entry ka + i -- its remaining products (len),
+      // next B index (kb0) and A value; refilled only as entries are used up
+      int len = 0, kb0 = 0;
+      double av = 0.0;
+      if (ka + lane < ka1)
+      {
+         const int k = Aj[ka + lane];
+         kb0 = Bi[k];
+         len = Bi[k + 1] - kb0;
+         if (NUMERIC) { av = Av[ka + lane]; }
+      }
       while (ka < ka1 && !ovf)
       {
-         // lane i describes entry ka + i: remaining products and first B index
-         const int e = ka + lane;
-         int len = 0, kb0 = 0;
-         if (e < ka1)
-         {
-            const int k = Aj[e];
-            kb0 = Bi[k];
-            len = Bi[k + 1] - kb0;
-            if (lane == 0) { kb0 += off0; len -= off0; }
-         }
          int pre = len;   // inclusive prefix over lanes
          for (int o = 1; o < 32; o <<= 1)
          {
@@ -1182,6 +1182,7 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
          const int j = lo;
          const int prej = __shfl_sync(GB_FULL, pre, j > 0 ? j - 1 : 0);
          const int kbj = __shfl_sync(GB_FULL, kb0, j);
+         const double avj = NUMERIC ? __shfl_sync(GB_FULL, av, j) : 0.0;
          const bool act = lane < total;
          int col = -1;
          double v = 0.0;
@@ -1189,7 +1190,7 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
          {
             const int kb = kbj + (lane - (j > 0 ? prej : 0));
             col = Bj[kb];
-            if (NUMERIC) { v = Av[ka + j] * Bv[kb]; }
+            if (NUMERIC) { v = avj * Bv[kb]; }
          }
          if (!NUMERIC)
          {
@@ -1218,15 +1219,36 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
             }
             __syncwarp();
          }
-         // advance the cursor past the consumed products
+         // advance past the consumed products: drop the nfull used-up
+         // entries, shift the window down and load the entries that enter it
          const int consumed = total < 32 ? total : 32;
          const int nfull = __popc(__ballot_sync(GB_FULL, pre <= consumed));
-         if (nfull == 0) { off0 += consumed; }
+         if (nfull == 0)
+         {
+            if (lane == 0) { kb0 += consumed; len -= consumed; }
+         }
          else
          {
-            const int pn = __shfl_sync(GB_FULL, pre, nfull - 1);
-            off0 = nfull < 32 ? consumed - pn : 0;
+            const int used = consumed - __shfl_sync(GB_FULL, pre, nfull - 1);   // of entry ka + nfull
             ka += nfull;
+            if (nfull < 32)
+            {
+               len = __shfl_down_sync(GB_FULL, len, nfull);
+               kb0 = __shfl_down_sync(GB_FULL, kb0, nfull);
+               if (NUMERIC) { av = __shfl_down_sync(GB_FULL, av, nfull); }
+            }
+            if (lane >= 32 - nfull)
+            {
+               len = 0;
+               if (ka + lane < ka1)
+               {
+                  const int k = Aj[ka + lane];
+                  kb0 = Bi[k];
+                  len = Bi[k + 1] - kb0;
+                  if (NUMERIC) { av = Av[ka + lane]; }
+               }
+            }
+            if (lane == 0) { kb0 += used; len -= used; }
          }
       }
       if (lane == 0)
