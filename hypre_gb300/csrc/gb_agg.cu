@@ -89,8 +89,12 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
          if (CF[i2] > 0)
          {
             int idx = f2c[i2];
-            int pos = gb_winsert(T, count, idx, lane == 0, created, ovf);
-            if (FILL && created && pos >= 0) { S2j[off + pos] = idx; }
+            if (FILL)
+            {
+               int pos = gb_winsert(T, count, idx, lane == 0, created, ovf);
+               if (created && pos >= 0) { S2j[off + pos] = idx; }
+            }
+            else { gb_wcount(T, count, idx, lane == 0, ovf); }
             __syncwarp();
          }
          int b = Si[i2], e = Si[i2 + 1];
@@ -104,8 +108,12 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
                int i3 = Sj[k2];
                if (CF[i3] > 0) { idx = f2c[i3]; act = idx != ic; }
             }
-            int pos = gb_winsert(T, count, idx, act, created, ovf);
-            if (FILL && created && pos >= 0) { S2j[off + pos] = idx; }
+            if (FILL)
+            {
+               int pos = gb_winsert(T, count, idx, act, created, ovf);
+               if (created && pos >= 0) { S2j[off + pos] = idx; }
+            }
+            else { gb_wcount(T, count, idx, act, ovf); }
             __syncwarp();
          }
       }

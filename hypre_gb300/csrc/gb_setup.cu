@@ -440,9 +440,13 @@ __device__ __forceinline__ void extpi_discover(int i, const int *__restrict__ Si
       int cf1 = CF[i1];
       if (cf1 >= 0)
       {
-         bool created;
-         int pos = gb_winsert(T, count, i1, lane == 0, created, ovf);
-         if (created && Pj_row && pos >= 0) { Pj_row[pos] = f2c[i1]; Pv_row[pos] = 0.0; }
+         if (Pj_row)
+         {
+            bool created;
+            int pos = gb_winsert(T, count, i1, lane == 0, created, ovf);
+            if (created && pos >= 0) { Pj_row[pos] = f2c[i1]; Pv_row[pos] = 0.0; }
+         }
+         else { gb_wcount(T, count, i1, lane == 0, ovf); }
       }
       else if (cf1 != SF_PT)
       {
@@ -452,9 +456,13 @@ __device__ __forceinline__ void extpi_discover(int i, const int *__restrict__ Si
             int kk = base + lane;
             int k1 = kk < e ? Sj[kk] : -1;
             bool act = kk < e && CF[k1] >= 0;
-            bool created;
-            int pos = gb_winsert(T, count, k1, act, created, ovf);
-            if (created && Pj_row && pos >= 0) { Pj_row[pos] = f2c[k1]; Pv_row[pos] = 0.0; }
+            if (Pj_row)
+            {
+               bool created;
+               int pos = gb_winsert(T, count, k1, act, created, ovf);
+               if (created && pos >= 0) { Pj_row[pos] = f2c[k1]; Pv_row[pos] = 0.0; }
+            }
+            else { gb_wcount(T, count, k1, act, ovf); }
          }
       }
    }
