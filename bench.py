@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--arms", default="fp64_plain,fp32_cycle",
+    ap.add_argument("--arms", default="fp64_plain,fp32_cycle,fp16_finest",
                     help="comma-separated arms to time (profiling runs use fp32_cycle alone)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end IJ arm (profiling runs)")
     ap.add_argument("--cpu-sample-n", type=int, default=80)
@@ -213,7 +213,7 @@ def gpu_arm(args):
 
     out = {}
     res = {}
-    arms = [a for a in (("fp64_plain", 0), ("fp32_cycle", 1)) if a[0] in args.arms.split(",")]
+    arms = [a for a in (("fp64_plain", 0), ("fp32_cycle", 1), ("fp16_finest", 2)) if a[0] in args.arms.split(",")]
     if not any(a[0] == "fp32_cycle" for a in arms):
         arms.append(("fp32_cycle", 1))
     for label, prec in arms:
@@ -235,6 +235,12 @@ def gpu_arm(args):
             keep = (amg, pcg)
         else:
             L.HYPRE_ParCSRFlexGMRESDestroy(pcg); L.HYPRE_BoomerAMGDestroy(amg)
+    # the reported mixed-precision path: the faster of the FP32 cycle and the
+    # FP16-finest cycle, provided it reached the tolerance in FP64
+    mixed = "fp32_cycle"
+    if "fp16_finest" in res and res["fp16_finest"]["true_relres"] <= 1.0e-8 and \
+            res["fp16_finest"]["seconds"] < res["fp32_cycle"]["seconds"]:
+        mixed = "fp16_finest"
 
     # ---- SpMV roofline on level 0 (FP64, CSR/SELL kernel), CUDA events on the library stream
     reps = 20
@@ -300,14 +306,16 @@ def gpu_arm(args):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.cpu_sample_n, n1)
 
-    best = res["fp32_cycle"]
+    best = res[mixed]
     result = {
         "metric": METRIC, "value": best["seconds"], "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": best["seconds"] * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64 setup+Krylov / f32 V-cycle",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 setup+Krylov / " + ("f32 V-cycle" if mixed == "fp32_cycle" else "f32 V-cycle, f16 finest values"),
         "data": "synthetic (seeded generator)", "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "1 GPU"),
-        "fp64_plain": res.get("fp64_plain"), "fp32_cycle": best,
-        "speedup_fp32_vs_fp64_plain": res["fp64_plain"]["seconds"] / best["seconds"] if "fp64_plain" in res else None,
+        "fp64_plain": res.get("fp64_plain"), "fp32_cycle": res["fp32_cycle"], "fp16_finest": res.get("fp16_finest"),
+        "value_arm": mixed,
+        "speedup_mixed_vs_fp64_plain": res["fp64_plain"]["seconds"] / best["seconds"] if "fp64_plain" in res else None,
         "e2e": {"value": e2e_wall, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "device_event_seconds": e2e_dev},
         "gpu_launches": best["launches_per_step"],
