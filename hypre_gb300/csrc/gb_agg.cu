@@ -67,8 +67,7 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
    const int lane = gb_lane();
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;
-   GbTab T = GLOBAL ? gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap)
-                    : gb_tab_at(sh + (threadIdx.x >> 5) * GB_TAB_INTS(GB_SMEM_CAP), GB_SMEM_CAP);
+   auto T = gb_tier_tab<GLOBAL>(sh, gtab, gcap, warp);
    if (!GLOBAL) { gb_tab_init(T); }
    int total = GLOBAL ? *ovf_n : nc;
    for (int t = warp; t < total; t += nwarps)
@@ -85,19 +84,11 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
       bool created;
       for (int k1 = Si[i1]; k1 < Si[i1 + 1] && !ovf; k1++)
       {
+         /* item 0 is i2 itself, items 1.. are S_i2's entries: one warp step
+          * covers i2 and up to 31 of its neighbours in discovery order
+          * (S has no diagonal, so f2c[i2] != ic) */
          int i2 = Sj[k1];
-         if (CF[i2] > 0)
-         {
-            int idx = f2c[i2];
-            if (FILL)
-            {
-               int pos = gb_winsert(T, count, idx, lane == 0, created, ovf);
-               if (created && pos >= 0) { S2j[off + pos] = idx; }
-            }
-            else { gb_wcount(T, count, idx, lane == 0, ovf); }
-            __syncwarp();
-         }
-         int b = Si[i2], e = Si[i2 + 1];
+         int b = Si[i2] - 1, e = Si[i2 + 1];
          for (int base = b; base < e && !ovf; base += 32)
          {
             int k2 = base + lane;
@@ -105,7 +96,7 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
             int idx = -1;
             if (k2 < e)
             {
-               int i3 = Sj[k2];
+               int i3 = (k2 == b) ? i2 : Sj[k2];
                if (CF[i3] > 0) { idx = f2c[i3]; act = idx != ic; }
             }
             if (FILL)
@@ -133,7 +124,7 @@ static int smem_blocks(int nrows)
    cudaGetDevice(&dev);
    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
    long long want = (nrows + GB_SMEM_WARPS - 1) / GB_SMEM_WARPS;
-   long long maxb = (long long) sms * 4;
+   long long maxb = (long long) sms * 8;
    return (int) (want < maxb ? (want < 1 ? 1 : want) : maxb);
 }
 
@@ -144,8 +135,8 @@ extern "C" void gb_strength2(int nc, const int *c2f, const int *f2c, const int *
    if (tier == 0)
    {
       int blocks = smem_blocks(nc);
-      if (!fill) { k_s2<false, false><<<blocks, 128, GB_SMEM_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
-      else { k_s2<false, true><<<blocks, 128, GB_SMEM_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
+      if (!fill) { k_s2<false, false><<<blocks, 128, GB_SMEMC_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
+      else { k_s2<false, true><<<blocks, 128, GB_SMEMC_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
    }
    else
    {
@@ -240,24 +231,38 @@ __global__ void k_fffc_fill(int nf, const int *__restrict__ fl, const int *__res
                             double *__restrict__ FFv, const int *__restrict__ FCi, int *__restrict__ FCj,
                             double *__restrict__ FCv)
 {
-   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   /* one warp per F row.  S_i is A_i's off-diagonal columns filtered in
+    * order (the reference looks each S entry up in A_i), and A_i's columns
+    * are distinct, so an A entry is strong iff its column occurs among the
+    * next 32 unmatched S entries; ballot prefixes keep the A order, which
+    * is the S order of the sequential fill */
+   int r = (int) ((blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5);
+   int lane = threadIdx.x & 31;
    if (r >= nf) { return; }
    int i = fl[r];
    int pf = FFi[r], pc = FCi[r];
    int a0 = Ai[i], a1 = Ai[i + 1];
    int hasdiag = (a0 < a1 && Aj[a0] == i);
-   if (hasdiag) { FFj[pf] = f2f[i]; FFv[pf++] = Av[a0]; }
-   /* S_i is A_i's off-diagonal columns filtered in order, so the matching
-    * A position only moves forward (the reference rescans from the start
-    * for every S entry and finds the same position) */
-   int jA = a0 + hasdiag;
-   for (int k = Si[i]; k < Si[i + 1]; k++)
+   if (hasdiag && lane == 0) { FFj[pf] = f2f[i]; FFv[pf] = Av[a0]; }
+   pf += hasdiag;
+   int s0 = Si[i], s1 = Si[i + 1];
+   unsigned lt = (1u << lane) - 1u;
+   for (int base = a0 + hasdiag; base < a1 && s0 < s1; base += 32)
    {
-      int jS = Sj[k];
-      while (Aj[jA] != jS) { jA++; }
-      if (CF[jS] > 0) { FCj[pc] = f2c[jS]; FCv[pc++] = Av[jA]; }
-      else { FFj[pf] = f2f[jS]; FFv[pf++] = Av[jA]; }
-      jA++;
+      int p = base + lane;
+      int c = (p < a1) ? Aj[p] : -1;
+      int ns = min(32, s1 - s0);
+      int sj = (lane < ns) ? Sj[s0 + lane] : -2;
+      bool in = false;
+      for (int t = 0; t < ns; t++) { in |= (c == __shfl_sync(0xffffffffu, sj, t)); }
+      bool isc = in && CF[c] > 0;
+      bool isf = in && !isc;
+      unsigned bc = __ballot_sync(0xffffffffu, isc), bf = __ballot_sync(0xffffffffu, isf);
+      if (isc) { int q = pc + __popc(bc & lt); FCj[q] = f2c[c]; FCv[q] = Av[p]; }
+      if (isf) { int q = pf + __popc(bf & lt); FFj[q] = f2f[c]; FFv[q] = Av[p]; }
+      pc += __popc(bc);
+      pf += __popc(bf);
+      s0 += __popc(bc | bf);
    }
 }
 
@@ -272,7 +277,7 @@ extern "C" void gb_fffc_fill(int nf, const int *fl, const int *Ai, const int *Aj
                              const int *Sj, const int *CF, const int *f2c, const int *f2f, const int *FFi, int *FFj,
                              double *FFv, const int *FCi, int *FCj, double *FCv, cudaStream_t s)
 {
-   k_fffc_fill<<<gb_blocks2(nf, 128), 128, 0, s>>>(nf, fl, Ai, Aj, Av, Si, Sj, CF, f2c, f2f, FFi, FFj, FFv, FCi,
+   k_fffc_fill<<<gb_blocks2((long long) nf * 32, 256), 256, 0, s>>>(nf, fl, Ai, Aj, Av, Si, Sj, CF, f2c, f2f, FFi, FFj, FFv, FCi,
                                                    FCj, FCv);
    GB_COUNT(1);
 }

@@ -320,7 +320,7 @@ static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int
    gb_tier t;
    tier_begin(&t, nrows);
    /* thread-per-row only pays off on large levels (many rows, short rows) */
-   int use_thread = nrows >= 65536;
+   int use_thread = nrows >= 65536 && ncols < (1 << 25);
    int h1;
    if (use_thread)
    {

@@ -306,6 +306,21 @@ __device__ __forceinline__ void gb_tab_clear(GbTabC &t, int n)
    __syncwarp();
 }
 
+// Table of a warp in a two-tier kernel: a compact 1024-slot shared-memory
+// table (GB_SMEMC_BYTES per block of GB_SMEM_WARPS warps), or a full table in
+// global memory for the rows that overflow it.
+#define GB_SMEMC_BYTES (GB_SMEM_WARPS * GB_TABC_BYTES(GB_SMEM_CAP))
+
+template <bool GLOBAL> struct GbTierTab { typedef GbTabC type; };
+template <> struct GbTierTab<true> { typedef GbTab type; };
+
+template <bool GLOBAL>
+__device__ __forceinline__ typename GbTierTab<GLOBAL>::type gb_tier_tab(int *sh, int *gtab, int gcap, int warp)
+{
+   if constexpr (GLOBAL) { return gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap); }
+   else { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TABC_BYTES(GB_SMEM_CAP), GB_SMEM_CAP); }
+}
+
 // ---------------------------------------------------------------------------
 // Counting insertion for symbolic passes: only the number of distinct keys
 // matters, so each active lane inserts its key directly (one probe sequence

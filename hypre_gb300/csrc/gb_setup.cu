@@ -685,16 +685,45 @@ __device__ __forceinline__ bool gb_gt0(double x)
    return b > 0 && b <= 0x7ff0000000000000LL;
 }
 
-__device__ __forceinline__ int tpr_find(const int *cols, int len, int c)
+/* The row's coarse columns are kept as a sorted set of packed keys
+ * (coarse index << 6 | position in discovery order), so a membership test is
+ * a binary search; coarse indices stay below 2^25 (checked by the host). */
+__device__ __forceinline__ int tpr_lower(const int *sk, int len, int c)
 {
-   for (int k = 0; k < len; k++) { if (cols[k] == c) { return k; } }
-   return -1;
+   int lo = 0, hi = len;
+   while (lo < hi)
+   {
+      int mid = (lo + hi) >> 1;
+      if ((sk[mid] >> 6) < c) { lo = mid + 1; }
+      else { hi = mid; }
+   }
+   return lo;
 }
 
-// counts (or fills, when Pj != NULL) the candidate columns of row i in
-// discovery order into cols[] (coarse indices); returns -1 beyond GB_TPR_MAX
+__device__ __forceinline__ int tpr_find(const int *sk, int len, int c)
+{
+   int lo = tpr_lower(sk, len, c);
+   return (lo < len && (sk[lo] >> 6) == c) ? (sk[lo] & 63) : -1;
+}
+
+// adds coarse column c (new columns take the next position; Pj, when given,
+// receives the columns in discovery order); false beyond GB_TPR_MAX
+__device__ __forceinline__ bool tpr_add(int *sk, int &len, int c, int *Pj)
+{
+   int lo = tpr_lower(sk, len, c);
+   if (lo < len && (sk[lo] >> 6) == c) { return true; }
+   if (len == GB_TPR_MAX) { return false; }
+   for (int q = len; q > lo; q--) { sk[q] = sk[q - 1]; }
+   sk[lo] = (c << 6) | len;
+   if (Pj) { Pj[len] = c; }
+   len++;
+   return true;
+}
+
+// counts (or fills Pj, when given) the candidate columns of row i in
+// discovery order; returns -1 beyond GB_TPR_MAX
 __device__ int tpr_discover(int i, const int *__restrict__ Si, const int *__restrict__ Sj, const int *__restrict__ CF,
-                            const int *__restrict__ f2c, int *cols)
+                            const int *__restrict__ f2c, int *sk, int *Pj)
 {
    int len = 0;
    for (int k = Si[i]; k < Si[i + 1]; k++)
@@ -703,19 +732,14 @@ __device__ int tpr_discover(int i, const int *__restrict__ Si, const int *__rest
       int cf1 = CF[i1];
       if (cf1 >= 0)
       {
-         int c = f2c[i1];
-         if (tpr_find(cols, len, c) < 0) { if (len == GB_TPR_MAX) { return -1; } cols[len++] = c; }
+         if (!tpr_add(sk, len, f2c[i1], Pj)) { return -1; }
       }
       else if (cf1 != SF_PT)
       {
          for (int kk = Si[i1]; kk < Si[i1 + 1]; kk++)
          {
             int k1 = Sj[kk];
-            if (CF[k1] >= 0)
-            {
-               int c = f2c[k1];
-               if (tpr_find(cols, len, c) < 0) { if (len == GB_TPR_MAX) { return -1; } cols[len++] = c; }
-            }
+            if (CF[k1] >= 0 && !tpr_add(sk, len, f2c[k1], Pj)) { return -1; }
          }
       }
    }
@@ -733,8 +757,8 @@ __global__ void __launch_bounds__(128) k_extpi_count_t(int nrows, const int *__r
    int cf = CF[i];
    if (cf >= 0) { cnt[r] = 1; return; }
    if (cf == SF_PT) { cnt[r] = 0; return; }
-   int cols[GB_TPR_MAX];
-   int len = tpr_discover(i, Si, Sj, CF, f2c, cols);
+   int sk[GB_TPR_MAX];
+   int len = tpr_discover(i, Si, Sj, CF, f2c, sk, nullptr);
    if (len < 0) { cnt[r] = 0; ovf_list[atomicAdd(ovf_n, 1)] = r; }
    else { cnt[r] = len; }
 }
@@ -754,11 +778,11 @@ __global__ void __launch_bounds__(128) k_extpi_fill_t(int nrows, const int *__re
    int len = Pi[r + 1] - begin;
    if (cf >= 0) { Pj[begin] = f2c[i]; Pv[begin] = 1.0; return; }
    if (cf == SF_PT || len > GB_TPR_MAX) { return; }
-   int cols[GB_TPR_MAX];
-   int l2 = tpr_discover(i, Si, Sj, CF, f2c, cols);
+   int sk[GB_TPR_MAX];
+   int l2 = tpr_discover(i, Si, Sj, CF, f2c, sk, Pj + begin);
    (void) l2;
    double *P = Pv + begin;
-   for (int k = 0; k < len; k++) { Pj[begin + k] = cols[k]; P[k] = 0.0; }
+   for (int k = 0; k < len; k++) { P[k] = 0.0; }
    double diagonal = Av[Ai[i]];
    int sp = Si[i], se = Si[i + 1];
    for (int jj = Ai[i] + 1; jj < Ai[i + 1]; jj++)
@@ -768,7 +792,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill_t(int nrows, const int *__re
       bool strong = (sp < se && Sj[sp] == i1);
       if (strong) { sp++; }
       int cf1 = CF[i1];
-      int pos1 = cf1 >= 0 ? tpr_find(cols, len, f2c[i1]) : -1;
+      int pos1 = cf1 >= 0 ? tpr_find(sk, len, f2c[i1]) : -1;
       if (pos1 >= 0) { P[pos1] += a; }
       else if (strong && cf1 < 0 && cf1 != SF_PT)
       {
@@ -780,7 +804,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill_t(int nrows, const int *__re
             int i2 = Aj[k];
             double a2 = Av[k];
             bool sg = neg ? gb_gt0(a2) : gb_lt0(a2);
-            if (sg && (i2 == i || (CF[i2] >= 0 && tpr_find(cols, len, f2c[i2]) >= 0))) { sum += a2; }
+            if (sg && (i2 == i || (CF[i2] >= 0 && tpr_find(sk, len, f2c[i2]) >= 0))) { sum += a2; }
          }
          if (sum != 0)
          {
@@ -791,7 +815,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill_t(int nrows, const int *__re
                double a2 = Av[k];
                bool sg = neg ? gb_gt0(a2) : gb_lt0(a2);
                if (!sg) { continue; }
-               int p2 = CF[i2] >= 0 ? tpr_find(cols, len, f2c[i2]) : -1;
+               int p2 = CF[i2] >= 0 ? tpr_find(sk, len, f2c[i2]) : -1;
                if (p2 >= 0) { P[p2] += distribute * a2; }
                if (i2 == i) { diagonal += distribute * a2; }
             }
