@@ -259,25 +259,55 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    int *list2 = NULL, *n2 = (int *) gb_dcalloc(sizeof(int) * 2);
    const int W = 0;   /* products are flattened 32 per step; no lane groups */
    int *ub = NULL;
+   /* B rows of a dozen entries or more: one B-row chunk per warp step
+    * (gb_spgemm_rc); short B rows: products flattened 32 per step */
+   const int rowchunk = B->nr > 0 && (long long) B->nnz >= 12LL * (long long) B->nr;
+   if (rowchunk)
+   {
+      /* rows with far more products than a 1024-slot table holds skip
+       * tier 0 (they are the long rows of R*A) */
+      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+      gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+   }
    /* symbolic: small shared tables, then compact shared tables for the rows
-    * that did not fit, then global tables for the rest.  (Routing rows by an
-    * upper bound of their length was measured slower: the product count is a
-    * poor bound for rows of RA*P, which then leave the fast tier.) */
-   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL, NULL,
-             n, NULL, 0, 0, t.err, NULL, 0, 0, s);
+    * that did not fit, then global tables for the rest.  (Routing rows of
+    * the flattened kernel by an upper bound of their length was measured
+    * slower: the product count is a poor bound for rows of RA*P, which then
+    * leave the fast tier.) */
+   if (rowchunk)
+   {
+      gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL,
+                   NULL, n, t.err, ub, 0, 0, s);
+   }
+   else
+   {
+      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL,
+                NULL, n, NULL, 0, 0, t.err, NULL, 0, 0, s);
+   }
    int h1 = read_int(t.ovf_n), h2 = 0;
    if (h1 > 0)
    {
       list2 = (int *) gb_dmalloc(sizeof(int) * (size_t) h1);
-      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, list2,
-                n2, h1, NULL, 0, 0, t.err, NULL, 0, 1, s);
+      if (rowchunk)
+      {
+         gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n,
+                      list2, n2, h1, t.err, NULL, 0, 1, s);
+      }
+      else
+      {
+         gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n,
+                   list2, n2, h1, NULL, 0, 0, t.err, NULL, 0, 1, s);
+      }
       h2 = read_int(n2);
    }
    if (h2 > 0)
    {
       /* global tables for the rows of the second list, sized from upper bounds */
-      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
-      gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+      if (!ub)
+      {
+         ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+         gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+      }
       tier_global_n(&t, ub, n, h2);
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, list2, n2, NULL, NULL, h2,
                 t.gtab, t.gcap, t.gwarps, t.err, NULL, 0, 2, s);
@@ -288,12 +318,25 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    C->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C->nnz ? C->nnz : 1));
    C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
    /* numeric: the same three tiers (each skips rows longer than its tables) */
-   gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL, NULL,
-             n, NULL, 0, 0, t.err, NULL, 1, 0, s);
-   if (h1 > 0)
+   if (rowchunk)
+   {
+      gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL,
+                   NULL, n, t.err, NULL, 1, 0, s);
+      if (h1 > 0)
+      {
+         gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
+                      NULL, NULL, h1, t.err, NULL, 1, 1, s);
+      }
+   }
+   else
    {
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL,
-                NULL, h1, NULL, 0, 0, t.err, NULL, 1, 1, s);
+                NULL, n, NULL, 0, 0, t.err, NULL, 1, 0, s);
+      if (h1 > 0)
+      {
+         gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
+                   NULL, NULL, h1, NULL, 0, 0, t.err, NULL, 1, 1, s);
+      }
    }
    if (h2 > 0)
    {

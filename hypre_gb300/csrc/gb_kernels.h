@@ -91,6 +91,10 @@ void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const
                const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list,
                int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab, int gcap, int gwarps, int *err,
                const int *ub, int phase, int tier, cudaStream_t s);
+void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi, const int *Bj,
+                  const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list, int *ovf_n,
+                  int *out_list, int *out_n, int nlist, int *err, const int *ub, int phase, int tier,
+                  cudaStream_t s);
 void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 /* aggressive coarsening (gb_agg.cu) */
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);

@@ -1399,6 +1399,217 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
 }
 
 // ---------------------------------------------------------------------------
+// Row-chunk products for B operands with long rows (R*A: A's rows hold tens
+// of entries).  A warp step takes one chunk of up to 32 entries of one B
+// row; the columns of a B row are distinct, so no two lanes of a step share
+// a column and the ordered insertion needs neither lane grouping nor a
+// product prefix: new columns take positions in lane order (= product
+// order), and each column receives at most one term per step, added in
+// product order -- the same positions and sums as the flattened kernel.
+// The numeric pass accumulates in shared memory (vals[pos]) and writes the
+// row once.  Chunk c+1's B entries and the next window of 32 A entries are
+// loaded while chunk c is inserted.
+// MODE 0: 1024-slot tables for all rows; MODE 1: 2048-slot tables for the
+// rows listed by MODE 0's symbolic pass.
+// ---------------------------------------------------------------------------
+template <int MODE, bool NUMERIC> struct RcCfg
+{
+   static constexpr int CAP = MODE ? GB_BIG_CAP : GB_SMEM_CAP;
+   static constexpr int LCAP = CAP / 4 * 3;
+   static constexpr int WBYTES = GB_TABC_BYTES(CAP) + (NUMERIC ? LCAP * 8 : 0);
+   static constexpr int WARPS = 4;
+   static constexpr int BYTES = WARPS * WBYTES;
+};
+
+template <int MODE, bool NUMERIC>
+__global__ void __launch_bounds__(128) k_spgemm_rc(int nrows, int square, const int *__restrict__ Ai,
+                                                   const int *__restrict__ Aj, const double *__restrict__ Av,
+                                                   const int *__restrict__ Bi, const int *__restrict__ Bj,
+                                                   const double *__restrict__ Bv, int *__restrict__ cnt,
+                                                   const int *__restrict__ Ci, int *__restrict__ Cj,
+                                                   double *__restrict__ Cv, int *ovf_list, int *ovf_n,
+                                                   int *out_list, int *out_n, int *err, const int *__restrict__ ub)
+{
+   typedef RcCfg<MODE, NUMERIC> K;
+   extern __shared__ __align__(16) unsigned char shrc[];
+   const int lane = gb_lane();
+   const unsigned lt = (1u << lane) - 1u;
+   unsigned char *mine = shrc + (size_t) (threadIdx.x >> 5) * K::WBYTES;
+   GbTabC T = gb_tabc_at((char *) mine, K::CAP);
+   double *vals = (double *) (mine + GB_TABC_BYTES(K::CAP));
+   gb_tab_init(T);
+   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+   const int total = MODE ? *ovf_n : nrows;
+   for (int t = warp; t < total; t += nwarps)
+   {
+      const int r = MODE ? ovf_list[t] : t;
+      if (MODE == 0 && !NUMERIC && ub && ub[r] > 16 * K::LCAP)
+      {
+         // far more products than the table holds: straight to the next tier
+         if (lane == 0) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         continue;
+      }
+      int off = 0;
+      if (NUMERIC)
+      {
+         off = Ci[r];
+         const int len = Ci[r + 1] - off;
+         if (len > K::LCAP) { continue; }
+         if (MODE == 1 && len <= RcCfg<0, true>::LCAP) { continue; }   // done by MODE 0
+      }
+      int count = 0, ovf = 0;
+      if (square)
+      {
+         if (lane == 0)
+         {
+            gb_tabc_insert(T, r, 0);
+            if (NUMERIC) { vals[0] = 0.0; Cj[off] = r; }
+         }
+         count = 1;
+         __syncwarp();
+      }
+      const int ka1 = Ai[r + 1];
+      int wb = Ai[r];
+      // window registers: lane l holds entry wb + l (cur) and wb + 32 + l (nxt)
+      int cb0 = 0, cb1 = 0, nb0 = 0, nb1 = 0;
+      double ca = 0.0, na = 0.0;
+      {
+         const int e = wb + lane;
+         if (e < ka1) { const int k = Aj[e]; cb0 = Bi[k]; cb1 = Bi[k + 1]; if (NUMERIC) { ca = Av[e]; } }
+         const int e2 = e + 32;
+         if (e2 < ka1) { const int k = Aj[e2]; nb0 = Bi[k]; nb1 = Bi[k + 1]; if (NUMERIC) { na = Av[e2]; } }
+      }
+      int q = 0;
+      int base = __shfl_sync(GB_FULL, cb0, 0), end = __shfl_sync(GB_FULL, cb1, 0);
+      double aq = NUMERIC ? __shfl_sync(GB_FULL, ca, 0) : 0.0;
+      int col = -1;
+      double bv = 0.0;
+      {
+         const int kb = base + lane;
+         if (kb < end) { col = Bj[kb]; if (NUMERIC) { bv = Bv[kb]; } }
+      }
+      while (wb + q < ka1 && !ovf)
+      {
+         // descriptor and loads of the next chunk
+         int nbase = base + 32, nend = end, nq = q;
+         double naq = aq;
+         if (nbase >= nend)
+         {
+            nq = q + 1;
+            if (nq < 32)
+            {
+               nbase = __shfl_sync(GB_FULL, cb0, nq);
+               nend = __shfl_sync(GB_FULL, cb1, nq);
+               if (NUMERIC) { naq = __shfl_sync(GB_FULL, ca, nq); }
+            }
+            else
+            {
+               nbase = __shfl_sync(GB_FULL, nb0, 0);
+               nend = __shfl_sync(GB_FULL, nb1, 0);
+               if (NUMERIC) { naq = __shfl_sync(GB_FULL, na, 0); }
+            }
+         }
+         int ncol = -1;
+         double nbv = 0.0;
+         {
+            const int kb = nbase + lane;
+            if (kb < nend) { ncol = Bj[kb]; if (NUMERIC) { nbv = Bv[kb]; } }
+         }
+         // insert the current chunk
+         const bool act = col >= 0;
+         if (!NUMERIC) { gb_wcount(T, count, col, act, ovf); }
+         else
+         {
+            const double v = aq * bv;
+            int pos = act ? gb_tabc_find(T, col) : -1;
+            const bool need = act && pos < 0;
+            const unsigned nm = __ballot_sync(GB_FULL, need);
+            bool bad = false;
+            if (need)
+            {
+               const int p = count + __popc(nm & lt);
+               if (p < K::LCAP && gb_tabc_insert(T, col, p) >= 0) { vals[p] = v; Cj[off + p] = col; }
+               else { bad = true; }
+            }
+            else if (act) { vals[pos] += v; }
+            count += __popc(nm);
+            if (__any_sync(GB_FULL, bad)) { ovf = 1; }
+            __syncwarp();
+         }
+         // advance
+         base = nbase; end = nend; aq = naq; col = ncol; bv = nbv;
+         if (nq == 32)
+         {
+            q = 0;
+            wb += 32;
+            cb0 = nb0; cb1 = nb1; ca = na;
+            nb0 = nb1 = 0; na = 0.0;
+            const int e2 = wb + 32 + lane;
+            if (e2 < ka1) { const int k = Aj[e2]; nb0 = Bi[k]; nb1 = Bi[k + 1]; if (NUMERIC) { na = Av[e2]; } }
+         }
+         else { q = nq; }
+      }
+      if (NUMERIC && !ovf)
+      {
+         for (int p = lane; p < count; p += 32) { Cv[off + p] = vals[p]; }
+      }
+      if (lane == 0)
+      {
+         if (!ovf) { if (!NUMERIC) { cnt[r] = count; } }
+         else if (MODE == 0 && !NUMERIC) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         else if (MODE == 1 && !NUMERIC) { out_list[atomicAdd(out_n, 1)] = r; cnt[r] = 0; }
+         else { atomicExch(err, 1); }
+      }
+      gb_tab_clear(T, count);
+   }
+}
+
+// phase: 0 symbolic, 1 numeric; tier 0 (all rows) or 1 (listed rows)
+extern "C" void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi,
+                             const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv,
+                             int *ovf_list, int *ovf_n, int *out_list, int *out_n, int nlist, int *err,
+                             const int *ub, int phase, int tier, cudaStream_t s)
+{
+   static int attr_done = 0;
+   if (!attr_done)
+   {
+      cudaFuncSetAttribute(k_spgemm_rc<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RcCfg<0, false>::BYTES);
+      cudaFuncSetAttribute(k_spgemm_rc<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RcCfg<0, true>::BYTES);
+      cudaFuncSetAttribute(k_spgemm_rc<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RcCfg<1, false>::BYTES);
+      cudaFuncSetAttribute(k_spgemm_rc<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RcCfg<1, true>::BYTES);
+      attr_done = 1;
+   }
+   int dev = 0, sms = 152;
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   const long long rows = tier == 0 ? nrows : nlist;
+   const long long want = (rows + 3) / 4;
+   /* resident blocks per SM from the shared memory each one takes (about
+    * 227 KB usable per SM) */
+   int bytes = tier == 0 ? (phase ? RcCfg<0, true>::BYTES : RcCfg<0, false>::BYTES)
+                         : (phase ? RcCfg<1, true>::BYTES : RcCfg<1, false>::BYTES);
+   int per_sm = (227 * 1024) / (bytes + 1024);
+   if (per_sm < 1) { per_sm = 1; }
+   if (per_sm > 16) { per_sm = 16; }
+   const long long maxb = (long long) sms * per_sm;
+   const int blocks = (int) (want < maxb ? (want > 0 ? want : 1) : maxb);
+#define GB_RC_ARGS nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv, ovf_list, ovf_n, out_list, out_n, err, ub
+   if (tier == 0)
+   {
+      if (phase == 0) { k_spgemm_rc<0, false><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+      else { k_spgemm_rc<0, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+   }
+   else
+   {
+      if (phase == 0) { k_spgemm_rc<1, false><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+      else { k_spgemm_rc<1, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+   }
+#undef GB_RC_ARGS
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
 // l1 norms (reference: hypre_ParCSRComputeL1Norms src/parcsr_ls/ams.c:517-790)
 // option 1: sum_j |a_ij|; option 5: a_ii (0 -> 1); rows with a_ii < 0 negated.
 // ---------------------------------------------------------------------------
