@@ -312,7 +312,10 @@ def gpu_arm(args):
         "warmup": args.warmup, "ms_per_step": best["seconds"] * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 setup+Krylov / " + ("f32 V-cycle" if mixed == "fp32_cycle" else "f32 V-cycle, f16 finest values"),
-        "data": "synthetic (seeded generator)", "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "1 GPU"),
+        "data": "synthetic (seeded generator)",
+        "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "1 GPU",
+                       **({} if n1 == 160 else {"workload": f"laplace27_{n1}", "grid": [n1, n1, n1],
+                                                 "unknowns": n, "nnz": nnz})),
         "fp64_plain": res.get("fp64_plain"), "fp32_cycle": res["fp32_cycle"], "fp16_finest": res.get("fp16_finest"),
         "value_arm": mixed,
         "speedup_mixed_vs_fp64_plain": res["fp64_plain"]["seconds"] / best["seconds"] if "fp64_plain" in res else None,

@@ -74,6 +74,9 @@ def _declare(L):
         "HYPRE_FlexGMRESSetPrecond": [vp, vp, vp, vp], "HYPRE_FlexGMRESGetNumIterations": [vp, P(i32)],
         "HYPRE_FlexGMRESGetFinalRelativeResidualNorm": [vp, P(f64)],
         "HYPRE_GB300_BoomerAMGGetLevelCSR": [vp, i32, i32, P(i32), P(i32), P(i32), vp, vp, vp],
+        "HYPRE_GB300_ParCSRMatrixCopyToHostCSR": [vp, P(i32), P(i32), vp, vp, vp],
+        "HYPRE_ParCSRMatrixGetRow": [vp, i32, P(i32), P(P(i32)), P(P(f64))],
+        "HYPRE_ParCSRMatrixRestoreRow": [vp, i32, P(i32), P(P(i32)), P(P(f64))],
         "HYPRE_GB300_BoomerAMGGetLevelCF": [vp, i32, vp], "HYPRE_GB300_BoomerAMGGetLevelL1": [vp, i32, vp],
         "HYPRE_GB300_BoomerAMGGetLevelCheby": [vp, i32, vp, vp, vp],
         "HYPRE_GB300_KrylovGetResidualHistory": [vp, i32, vp, P(i32)],
@@ -162,6 +165,19 @@ def check(code, what=""):
 # ---------------------------------------------------------------------------
 # Thin object wrappers (same calls a C user makes)
 # ---------------------------------------------------------------------------
+def parcsr_to_host(par):
+    """A ParCSR matrix's local CSR arrays copied to host memory."""
+    L = lib()
+    nr, nnz = C.c_int(), C.c_int()
+    check(L.HYPRE_GB300_ParCSRMatrixCopyToHostCSR(par, C.byref(nr), C.byref(nnz), None, None, None), "CopyToHostCSR")
+    I = np.empty(nr.value + 1, np.int32)
+    J = np.empty(max(nnz.value, 1), np.int32)
+    V = np.empty(max(nnz.value, 1), np.float64)
+    check(L.HYPRE_GB300_ParCSRMatrixCopyToHostCSR(par, None, None, I.ctypes.data, J.ctypes.data, V.ctypes.data),
+          "CopyToHostCSR")
+    return I, J[:nnz.value], V[:nnz.value]
+
+
 class IJMatrix:
     """HYPRE_IJMatrix assembled from host CSR arrays, one SetValues call per
     row (the diagonal is moved to the front of each row at assembly)."""
@@ -188,6 +204,10 @@ class IJMatrix:
         check(L.HYPRE_IJMatrixAssemble(self.h), "IJMatrixAssemble")
         self.par = C.c_void_p()
         L.HYPRE_IJMatrixGetObject(self.h, C.byref(self.par))
+
+    def csr(self):
+        """The assembled matrix as host CSR arrays (I, J, V)."""
+        return parcsr_to_host(self.par)
 
     def destroy(self):
         if self.h:

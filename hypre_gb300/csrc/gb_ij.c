@@ -36,6 +36,7 @@ void gb_parcsr_free(gb_parcsr *M)
    for (int p = 0; p < 3; p++) { solveform_free(&M->sf[p]); }
    if (M->owns) { gb_csr_free(&M->A); }
    gb_dfree(M->diag);
+   free(M->row_cols); free(M->row_vals);
    M->magic = 0;
    free(M);
 }
@@ -360,6 +361,70 @@ HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(HYPRE_Int n, const HYPRE_Int
    return gb_error_flag;
 }
 
+/* One row of the matrix in host memory (reference: HYPRE_ParCSRMatrixGetRow,
+ * src/parcsr_mv/HYPRE_parcsr_matrix.c / par_csr_matrix.c hypre_ParCSRMatrixGetRow):
+ * global column indices, diagonal first; one row may be active at a time and
+ * RestoreRow releases it. */
+HYPRE_Int HYPRE_ParCSRMatrixGetRow(HYPRE_ParCSRMatrix A, HYPRE_BigInt row, HYPRE_Int *size, HYPRE_BigInt **col_ind,
+                                   HYPRE_Complex **values)
+{
+   if (!check_mat(A, 1)) { return gb_error_flag; }
+   if (row < 0 || row >= A->A.nr) { gb_error_in_arg(2); return gb_error_flag; }
+   if (A->row_active) { gb_error(HYPRE_ERROR_GENERIC, "a row is already active"); return gb_error_flag; }
+   int be[2];
+   cudaMemcpyAsync(be, A->A.i + row, sizeof(int) * 2, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   int l = be[1] - be[0];
+   if (l > A->row_cap)
+   {
+      free(A->row_cols); free(A->row_vals);
+      A->row_cols = (int *) malloc(sizeof(int) * (size_t) l);
+      A->row_vals = (double *) malloc(sizeof(double) * (size_t) l);
+      A->row_cap = (A->row_cols && A->row_vals) ? l : 0;
+      if (!A->row_cap) { gb_error(HYPRE_ERROR_MEMORY, "GetRow"); return gb_error_flag; }
+   }
+   if (l > 0)
+   {
+      if (col_ind) { cudaMemcpyAsync(A->row_cols, A->A.j + be[0], sizeof(int) * (size_t) l, cudaMemcpyDeviceToHost, gb_stream()); }
+      if (values) { cudaMemcpyAsync(A->row_vals, A->A.v + be[0], sizeof(double) * (size_t) l, cudaMemcpyDeviceToHost, gb_stream()); }
+      gb_sync();
+   }
+   A->row_active = 1;
+   if (size) { *size = l; }
+   if (col_ind) { *col_ind = A->row_cols; }
+   if (values) { *values = A->row_vals; }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParCSRMatrixRestoreRow(HYPRE_ParCSRMatrix A, HYPRE_BigInt row, HYPRE_Int *size,
+                                       HYPRE_BigInt **col_ind, HYPRE_Complex **values)
+{
+   (void) row;
+   if (!check_mat(A, 1)) { return gb_error_flag; }
+   if (!A->row_active) { gb_error_in_arg(1); return gb_error_flag; }
+   A->row_active = 0;
+   if (size) { *size = 0; }
+   if (col_ind) { *col_ind = NULL; }
+   if (values) { *values = NULL; }
+   return gb_error_flag;
+}
+
+/* The whole local CSR (row pointers n+1, columns and values nnz; any of the
+ * arrays may be NULL) copied to host memory. */
+HYPRE_Int HYPRE_GB300_ParCSRMatrixCopyToHostCSR(HYPRE_ParCSRMatrix A, HYPRE_Int *nrows, HYPRE_Int *nnz,
+                                               HYPRE_Int *rowptr, HYPRE_Int *colidx, HYPRE_Real *values)
+{
+   if (!check_mat(A, 1)) { return gb_error_flag; }
+   if (nrows) { *nrows = A->A.nr; }
+   if (nnz) { *nnz = A->A.nnz; }
+   cudaStream_t s = gb_stream();
+   if (rowptr) { cudaMemcpyAsync(rowptr, A->A.i, sizeof(int) * (size_t) (A->A.nr + 1), cudaMemcpyDeviceToHost, s); }
+   if (colidx) { cudaMemcpyAsync(colidx, A->A.j, sizeof(int) * (size_t) A->A.nnz, cudaMemcpyDeviceToHost, s); }
+   if (values && A->A.v) { cudaMemcpyAsync(values, A->A.v, sizeof(double) * (size_t) A->A.nnz, cudaMemcpyDeviceToHost, s); }
+   gb_sync();
+   return gb_error_flag;
+}
+
 HYPRE_Int HYPRE_GB300_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix A)
 {
    if (A && A->magic == GB_MAGIC_MAT) { gb_parcsr_free(A); }
@@ -383,9 +448,22 @@ struct hypre_IJMatrix_struct
    long long  arena_len, arena_cap;
    int       *hint;           /* row sizes from SetRowSizes */
    gb_parcsr *par;
+   /* device staging: rows put by large SetValues calls are copied straight
+    * to the device (row_state 2, entries at dev_off[r]); the others live in
+    * the host arena (row_state 0/1) */
+   unsigned char *row_state;
+   long long *dev_off;
+   int       *st_cols;
+   double    *st_vals;
+   long long  st_len, st_cap;
 };
 
 #define GB_MAGIC_IJM 0x494a4d31
+#define GB_IJ_ROW_DEVICE 2
+#define GB_IJ_ROW_PENDING 3
+/* puts with fewer entries stay on the host (one copy per call would cost
+ * more than the staging) */
+#define GB_IJ_DEVICE_MIN 65536
 #define GB_MAGIC_IJV 0x494a5631
 
 static int check_ijm(HYPRE_IJMatrix m, int arg)
@@ -449,6 +527,11 @@ static void ijm_free_stage(HYPRE_IJMatrix m)
    free(m->row_off); free(m->row_len); free(m->row_cap); free(m->cols); free(m->vals);
    m->row_off = m->row_len = m->row_cap = NULL; m->cols = NULL; m->vals = NULL;
    m->arena_len = m->arena_cap = 0;
+   free(m->row_state); free(m->dev_off);
+   m->row_state = NULL; m->dev_off = NULL;
+   gb_dfree(m->st_cols); gb_dfree(m->st_vals);
+   m->st_cols = NULL; m->st_vals = NULL;
+   m->st_len = m->st_cap = 0;
 }
 
 HYPRE_Int HYPRE_IJMatrixInitialize(HYPRE_IJMatrix m)
@@ -472,7 +555,13 @@ HYPRE_Int HYPRE_IJMatrixInitialize(HYPRE_IJMatrix m)
    m->arena_len = tot;
    m->cols = (int *) malloc(sizeof(int) * (size_t) m->arena_cap);
    m->vals = (double *) malloc(sizeof(double) * (size_t) m->arena_cap);
-   if (!m->cols || !m->vals) { gb_error(HYPRE_ERROR_MEMORY, "IJ staging"); return gb_error_flag; }
+   m->row_state = (unsigned char *) calloc((size_t) (n ? n : 1), 1);
+   m->dev_off = (long long *) malloc(sizeof(long long) * (size_t) (n ? n : 1));
+   if (!m->cols || !m->vals || !m->row_state || !m->dev_off)
+   {
+      gb_error(HYPRE_ERROR_MEMORY, "IJ staging");
+      return gb_error_flag;
+   }
    m->initialized = 1;
    m->assembled = 0;
    if (m->par) { gb_parcsr_free(m->par); m->par = NULL; }
@@ -508,6 +597,115 @@ static int row_grow(HYPRE_IJMatrix m, int r, int need)
    return 1;
 }
 
+static int ij_read_int(const int *d)
+{
+   int h = 0;
+   cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   return h;
+}
+
+/* grows the device staging to hold need entries (stream-ordered copies);
+ * 0 when the device memory is not available */
+static int ijm_staging_reserve(HYPRE_IJMatrix m, long long need)
+{
+   if (need <= m->st_cap) { return 1; }
+   long long cap = m->st_cap * 2;
+   if (cap < need) { cap = need; }
+   int *c = (int *) gb_dmalloc(sizeof(int) * (size_t) cap);
+   double *v = (double *) gb_dmalloc(sizeof(double) * (size_t) cap);
+   if (!c || !v) { gb_dfree(c); gb_dfree(v); return 0; }
+   if (m->st_len > 0)
+   {
+      cudaMemcpyAsync(c, m->st_cols, sizeof(int) * (size_t) m->st_len, cudaMemcpyDeviceToDevice, gb_stream());
+      cudaMemcpyAsync(v, m->st_vals, sizeof(double) * (size_t) m->st_len, cudaMemcpyDeviceToDevice, gb_stream());
+   }
+   gb_dfree(m->st_cols); gb_dfree(m->st_vals);
+   m->st_cols = c; m->st_vals = v; m->st_cap = cap;
+   return 1;
+}
+
+/* Moves every device-staged row into the host arena (before a put that the
+ * host path must handle touches one of them, or a GetValues). */
+static int ijm_migrate(HYPRE_IJMatrix m)
+{
+   if (m->st_len == 0) { return 1; }
+   int *hc = (int *) malloc(sizeof(int) * (size_t) m->st_len);
+   double *hv = (double *) malloc(sizeof(double) * (size_t) m->st_len);
+   if (!hc || !hv) { free(hc); free(hv); gb_error(HYPRE_ERROR_MEMORY, "IJ staging"); return 0; }
+   cudaMemcpyAsync(hc, m->st_cols, sizeof(int) * (size_t) m->st_len, cudaMemcpyDeviceToHost, gb_stream());
+   cudaMemcpyAsync(hv, m->st_vals, sizeof(double) * (size_t) m->st_len, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   for (int r = 0; r < m->nrows; r++)
+   {
+      if (m->row_state[r] != GB_IJ_ROW_DEVICE) { continue; }
+      int len = m->row_len[r];
+      m->row_len[r] = 0;
+      if (!row_grow(m, r, len)) { free(hc); free(hv); return 0; }
+      memcpy(m->cols + m->row_off[r], hc + m->dev_off[r], sizeof(int) * (size_t) len);
+      memcpy(m->vals + m->row_off[r], hv + m->dev_off[r], sizeof(double) * (size_t) len);
+      m->row_len[r] = len;
+      m->row_state[r] = 0;
+   }
+   free(hc); free(hv);
+   m->st_len = 0;
+   return 1;
+}
+
+/* SetValues of new rows with many entries: copied from the caller's buffers
+ * to the device staging and checked there (columns in range, none repeated
+ * within a row).  Returns 1 when the put was taken, 0 when the host path must
+ * run it (small put, repeated or already-set rows, failed check); nothing is
+ * changed in that case. */
+static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const int *rows, const int *cols,
+                          const double *values)
+{
+   long long tot = 0;
+   for (int t = 0; t < nrows; t++)
+   {
+      if (ncols[t] < 0) { return 0; }
+      tot += ncols[t];
+   }
+   if (tot < GB_IJ_DEVICE_MIN || tot > 0x7fffffffLL) { return 0; }
+   int t = 0, ok = 1;
+   for (; t < nrows; t++)
+   {
+      int r = rows[t] - m->ilower;
+      if (r < 0 || r >= m->nrows || m->row_state[r] != 0 || m->row_len[r] != 0) { ok = 0; break; }
+      m->row_state[r] = GB_IJ_ROW_PENDING;
+   }
+   for (int u = 0; u < t; u++) { m->row_state[rows[u] - m->ilower] = 0; }
+   if (!ok) { return 0; }
+   int *hstart = (int *) malloc(sizeof(int) * (size_t) (nrows + 1));
+   int *dstart = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
+   int *flags = (int *) gb_dcalloc(sizeof(int));
+   if (!hstart || !dstart || !flags || !ijm_staging_reserve(m, m->st_len + tot))
+   {
+      free(hstart); gb_dfree(dstart); gb_dfree(flags);
+      return 0;
+   }
+   hstart[0] = 0;
+   for (int u = 0; u < nrows; u++) { hstart[u + 1] = hstart[u] + ncols[u]; }
+   cudaStream_t s = gb_stream();
+   cudaMemcpyAsync(m->st_cols + m->st_len, cols, sizeof(int) * (size_t) tot, cudaMemcpyHostToDevice, s);
+   cudaMemcpyAsync(m->st_vals + m->st_len, values, sizeof(double) * (size_t) tot, cudaMemcpyHostToDevice, s);
+   cudaMemcpyAsync(dstart, hstart, sizeof(int) * (size_t) (nrows + 1), cudaMemcpyHostToDevice, s);
+   gb_ij_check(nrows, dstart, m->st_cols + m->st_len, m->jupper - m->jlower + 1, flags, s);
+   int f = ij_read_int(flags);   /* also the point after which the caller's buffers are free */
+   gb_dfree(dstart); gb_dfree(flags);
+   if (f != 0) { free(hstart); return 0; }
+   for (int u = 0; u < nrows; u++)
+   {
+      int r = rows[u] - m->ilower;
+      m->dev_off[r] = m->st_len + hstart[u];
+      m->row_len[r] = ncols[u];
+      m->row_state[r] = GB_IJ_ROW_DEVICE;
+   }
+   m->st_len += tot;
+   free(hstart);
+   return 1;
+}
+
 static HYPRE_Int ijm_put(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, const HYPRE_BigInt *rows,
                          const HYPRE_BigInt *cols, const HYPRE_Complex *values, int add)
 {
@@ -519,6 +717,25 @@ static HYPRE_Int ijm_put(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, co
    if (!rows) { gb_error_in_arg(4); return gb_error_flag; }
    if (!cols) { gb_error_in_arg(5); return gb_error_flag; }
    if (!values) { gb_error_in_arg(6); return gb_error_flag; }
+   if (!add && ijm_put_device(m, nrows, ncols, rows, cols, values))
+   {
+      m->assembled = 0;
+      return gb_error_flag;
+   }
+   if (m->st_len > 0)
+   {
+      /* the host path edits rows in the arena: bring staged rows back first
+       * when this put touches one */
+      for (int t = 0; t < nrows; t++)
+      {
+         int r = rows[t] - m->ilower;
+         if (r >= 0 && r < m->nrows && m->row_state[r] == GB_IJ_ROW_DEVICE)
+         {
+            if (!ijm_migrate(m)) { return gb_error_flag; }
+            break;
+         }
+      }
+   }
    long long k = 0;
    for (int t = 0; t < nrows; t++)
    {
@@ -612,43 +829,66 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
    if (!check_ijm(m, 1)) { return gb_error_flag; }
    if (!m->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not initialized"); return gb_error_flag; }
    int n = m->nrows;
+   cudaStream_t s = gb_stream();
+   /* row pointers; host-arena rows are packed behind the device-staged ones
+    * (their offsets point past st_len into a temporary upload) */
    int *I = (int *) malloc(sizeof(int) * (size_t) (n + 1));
+   long long *off = (long long *) malloc(sizeof(long long) * (size_t) (n ? n : 1));
+   if (!I || !off) { free(I); free(off); gb_error(HYPRE_ERROR_MEMORY, "IJ assembly"); return gb_error_flag; }
    I[0] = 0;
-   for (int i = 0; i < n; i++) { I[i + 1] = I[i] + m->row_len[i]; }
-   int nnz = I[n];
-   int *J = (int *) malloc(sizeof(int) * (size_t) (nnz ? nnz : 1));
-   double *V = (double *) malloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
+   long long nhost = 0;
    for (int i = 0; i < n; i++)
    {
-      const int *rc = m->cols + m->row_off[i];
-      const double *rv = m->vals + m->row_off[i];
-      int l = m->row_len[i], b = I[i];
-      int dpos = -1;
-      for (int z = 0; z < l; z++) { if (rc[z] == i) { dpos = z; break; } }
-      if (dpos < 0 || dpos == 0)
-      {
-         memcpy(J + b, rc, sizeof(int) * (size_t) l);
-         memcpy(V + b, rv, sizeof(double) * (size_t) l);
-      }
-      else if (m->swap_diag)
-      {
-         /* IJMatrix_parcsr.c:2976-2990: swap the diagonal with the first entry */
-         memcpy(J + b, rc, sizeof(int) * (size_t) l);
-         memcpy(V + b, rv, sizeof(double) * (size_t) l);
-         J[b + dpos] = J[b]; V[b + dpos] = V[b];
-         J[b] = i; V[b] = rv[dpos];
-      }
-      else
-      {
-         /* IJMatrix_parcsr.c:2900-2920: diagonal first, others keep their order */
-         J[b] = i; V[b] = rv[dpos];
-         int c = b + 1;
-         for (int z = 0; z < l; z++) { if (z != dpos) { J[c] = rc[z]; V[c] = rv[z]; c++; } }
-      }
+      int l = m->row_len[i];
+      I[i + 1] = I[i] + l;
+      if (m->row_state[i] == GB_IJ_ROW_DEVICE) { off[i] = m->dev_off[i]; }
+      else { off[i] = m->st_len + nhost; nhost += l; }
    }
+   int nnz = I[n];
+   long long need = m->st_len + nhost;
+   if (!ijm_staging_reserve(m, need > 0 ? need : 1))
+   {
+      free(I); free(off);
+      gb_error(HYPRE_ERROR_MEMORY, "IJ device staging");
+      return gb_error_flag;
+   }
+   int *hc = NULL;
+   double *hv = NULL;
+   if (nhost > 0)
+   {
+      hc = (int *) malloc(sizeof(int) * (size_t) nhost);
+      hv = (double *) malloc(sizeof(double) * (size_t) nhost);
+      if (!hc || !hv) { free(I); free(off); free(hc); free(hv); gb_error(HYPRE_ERROR_MEMORY, "IJ assembly"); return gb_error_flag; }
+      for (int i = 0; i < n; i++)
+      {
+         if (m->row_state[i] == GB_IJ_ROW_DEVICE || m->row_len[i] == 0) { continue; }
+         long long o = off[i] - m->st_len;
+         memcpy(hc + o, m->cols + m->row_off[i], sizeof(int) * (size_t) m->row_len[i]);
+         memcpy(hv + o, m->vals + m->row_off[i], sizeof(double) * (size_t) m->row_len[i]);
+      }
+      cudaMemcpyAsync(m->st_cols + m->st_len, hc, sizeof(int) * (size_t) nhost, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(m->st_vals + m->st_len, hv, sizeof(double) * (size_t) nhost, cudaMemcpyHostToDevice, s);
+   }
+   gb_csr A;
+   A.nr = n; A.nc = m->jupper - m->jlower + 1; A.nnz = nnz;
+   A.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   A.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (nnz ? nnz : 1));
+   A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
+   long long *doff = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (n ? n : 1));
+   if (!A.i || !A.j || !A.v || !doff)
+   {
+      free(I); free(off); free(hc); free(hv);
+      gb_dfree(A.i); gb_dfree(A.j); gb_dfree(A.v); gb_dfree(doff);
+      return gb_error_flag;
+   }
+   cudaMemcpyAsync(A.i, I, sizeof(int) * (size_t) (n + 1), cudaMemcpyHostToDevice, s);
+   cudaMemcpyAsync(doff, off, sizeof(long long) * (size_t) (n ? n : 1), cudaMemcpyHostToDevice, s);
+   gb_ij_gather(n, doff, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
+   gb_sync();   /* the host buffers above are read by the copies */
+   gb_dfree(doff);
+   free(I); free(off); free(hc); free(hv);
    if (m->par) { gb_parcsr_free(m->par); }
-   m->par = upload_csr(n, m->jupper - m->jlower + 1, I, J, V);
-   free(I); free(J); free(V);
+   m->par = gb_parcsr_wrap(A, 1);
    m->assembled = 1;
    return gb_error_flag;
 }
@@ -658,6 +898,7 @@ HYPRE_Int HYPRE_IJMatrixGetValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *
 {
    if (!check_ijm(m, 1)) { return gb_error_flag; }
    if (!m->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not initialized"); return gb_error_flag; }
+   if (!ijm_migrate(m)) { return gb_error_flag; }
    long long k = 0;
    for (int t = 0; t < nrows; t++)
    {

@@ -75,6 +75,10 @@ struct hypre_ParCSRMatrix_struct
    int          owns;
    gb_solveform sf[3];     /* per precision (GB_PREC_*) */
    double      *diag;      /* device, for diagonal scaling (lazy) */
+   int          row_active;          /* GetRow .. RestoreRow */
+   int         *row_cols;            /* host copy of the active row */
+   double      *row_vals;
+   int          row_cap;
 };
 typedef struct hypre_ParCSRMatrix_struct gb_parcsr;
 

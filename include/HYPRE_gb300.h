@@ -129,6 +129,11 @@ HYPRE_Int HYPRE_ParCSRMatrixGetDims(HYPRE_ParCSRMatrix matrix, HYPRE_BigInt *M, 
 HYPRE_Int HYPRE_ParCSRMatrixGetLocalRange(HYPRE_ParCSRMatrix matrix, HYPRE_BigInt *row_start,
                                           HYPRE_BigInt *row_end, HYPRE_BigInt *col_start,
                                           HYPRE_BigInt *col_end);          /* :123 */
+/* one row in host memory, diagonal first; one active row at a time */
+HYPRE_Int HYPRE_ParCSRMatrixGetRow(HYPRE_ParCSRMatrix matrix, HYPRE_BigInt row, HYPRE_Int *size,
+                                   HYPRE_BigInt **col_ind, HYPRE_Complex **values);   /* :130 */
+HYPRE_Int HYPRE_ParCSRMatrixRestoreRow(HYPRE_ParCSRMatrix matrix, HYPRE_BigInt row, HYPRE_Int *size,
+                                       HYPRE_BigInt **col_ind, HYPRE_Complex **values); /* :137 */
 HYPRE_Int HYPRE_ParCSRMatrixMatvec(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,
                                    HYPRE_Complex beta, HYPRE_ParVector y); /* :285 */
 HYPRE_Int HYPRE_ParCSRMatrixMatvecT(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,
@@ -360,6 +365,10 @@ HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(HYPRE_Int n, const HYPRE_Int
                                                     const HYPRE_Int *colidx, const HYPRE_Real *values,
                                                     HYPRE_ParCSRMatrix *A);
 HYPRE_Int HYPRE_GB300_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix A);
+/* The local CSR arrays copied to host memory (any array may be NULL).  No
+ * counterpart in the reference (whose matrices are host-addressable). */
+HYPRE_Int HYPRE_GB300_ParCSRMatrixCopyToHostCSR(HYPRE_ParCSRMatrix A, HYPRE_Int *nrows, HYPRE_Int *nnz,
+                                               HYPRE_Int *rowptr, HYPRE_Int *colidx, HYPRE_Real *values);
 /* Stream used for every kernel (default: a library-owned non-blocking stream). */
 HYPRE_Int HYPRE_GB300_SetStream(void *cuda_stream);
 HYPRE_Int HYPRE_GB300_GetStream(void **cuda_stream);

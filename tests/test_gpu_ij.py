@@ -1,0 +1,195 @@
+"""IJ matrix assembly: the device path (one large SetValues call, copied to
+the device and gathered there) and the host path (many small calls) give the
+same CSR as the reference's rules (IJMatrix_parcsr.c): repeated columns of a
+fresh row merged at their first position with the last value, AddToValues
+adding to existing entries and appending new ones, and the diagonal moved to
+the front of each row by shifting the entries before it, or by swapping it
+with the first entry after SetDiagOffdSizes."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def random_rows(n, seed, maxlen=80, dup_rows=()):
+    rng = np.random.default_rng(seed)
+    rows = []
+    for r in range(n):
+        l = int(rng.integers(0, maxlen + 1))
+        cols = rng.choice(n, size=min(l, n), replace=False)
+        if l > 0 and rng.random() < 0.8 and r not in cols:
+            cols[rng.integers(0, len(cols))] = r
+        cols = list(int(c) for c in cols)
+        if r in dup_rows and len(cols) > 2:
+            cols.append(cols[1])
+        vals = list(rng.standard_normal(len(cols)))
+        rows.append((cols, vals))
+    return rows
+
+
+def expected_csr(rows, swap=False, adds=()):
+    out = []
+    for r, (cols, vals) in enumerate(rows):
+        ec, ev = [], []
+        for c, v in zip(cols, vals):
+            if c in ec:
+                ev[ec.index(c)] = v
+            else:
+                ec.append(c)
+                ev.append(v)
+        out.append([ec, ev])
+    for r, cols, vals in adds:
+        ec, ev = out[r]
+        for c, v in zip(cols, vals):
+            if c in ec:
+                ev[ec.index(c)] += v
+            else:
+                ec.append(c)
+                ev.append(v)
+    I, J, V = [0], [], []
+    for r, (ec, ev) in enumerate(out):
+        ec, ev = list(ec), list(ev)
+        if r in ec:
+            d = ec.index(r)
+            if d > 0:
+                if swap:
+                    ec[0], ec[d] = ec[d], ec[0]
+                    ev[0], ev[d] = ev[d], ev[0]
+                else:
+                    ec.insert(0, ec.pop(d))
+                    ev.insert(0, ev.pop(d))
+        J += ec
+        V += ev
+        I.append(len(J))
+    return np.array(I, np.int32), np.array(J, np.int32), np.array(V, np.float64)
+
+
+def assemble(gb, rows, bulk, swap=False, adds=(), extra=None, strict=True):
+    L = gb.lib()
+    n = len(rows)
+    h = C.c_void_p()
+    gb.check(L.HYPRE_IJMatrixCreate(0, 0, n - 1, 0, n - 1, C.byref(h)), "create")
+    L.HYPRE_IJMatrixSetObjectType(h, gb.HYPRE_PARCSR)
+    sizes = np.array([max(len(c), 1) for c, _ in rows], np.int32)
+    if swap:
+        L.HYPRE_IJMatrixSetDiagOffdSizes(h, sizes.ctypes.data, None)
+    else:
+        L.HYPRE_IJMatrixSetRowSizes(h, sizes.ctypes.data)
+    L.HYPRE_IJMatrixInitialize(h)
+    if bulk:
+        nc = np.array([len(c) for c, _ in rows], np.int32)
+        ri = np.arange(n, dtype=np.int32)
+        J = np.array([c for cs, _ in rows for c in cs], np.int32)
+        V = np.array([v for _, vs in rows for v in vs], np.float64)
+        L.HYPRE_IJMatrixSetValues(h, n, nc.ctypes.data, ri.ctypes.data, J.ctypes.data, V.ctypes.data)
+    else:
+        for r, (cs, vs) in enumerate(rows):
+            nc = np.array([len(cs)], np.int32)
+            ri = np.array([r], np.int32)
+            J = np.array(cs, np.int32)
+            V = np.array(vs, np.float64)
+            L.HYPRE_IJMatrixSetValues(h, 1, nc.ctypes.data, ri.ctypes.data, J.ctypes.data, V.ctypes.data)
+    for r, cs, vs in adds:
+        nc = np.array([len(cs)], np.int32)
+        ri = np.array([r], np.int32)
+        J = np.array(cs, np.int32)
+        V = np.array(vs, np.float64)
+        L.HYPRE_IJMatrixAddToValues(h, 1, nc.ctypes.data, ri.ctypes.data, J.ctypes.data, V.ctypes.data)
+    if extra is not None:
+        extra(L, h)
+    code = L.HYPRE_IJMatrixAssemble(h)
+    if strict:
+        gb.check(code, "assemble")
+    par = C.c_void_p()
+    L.HYPRE_IJMatrixGetObject(h, C.byref(par))
+    if not strict:
+        L.HYPRE_IJMatrixDestroy(h)
+        return None
+    out = gb.parcsr_to_host(par)
+    L.HYPRE_IJMatrixDestroy(h)
+    return out
+
+
+def same(a, b):
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("swap", [False, True])
+def test_bulk_and_per_row_puts_match_reference_rules(gb, swap):
+    rows = random_rows(6000, seed=5)
+    exp = expected_csr(rows, swap=swap)
+    assert len(exp[1]) >= 65536          # large enough for the device path
+    same(assemble(gb, rows, bulk=True, swap=swap), exp)
+    same(assemble(gb, rows, bulk=False, swap=swap), exp)
+    assert gb.lib().HYPRE_GetError() == 0
+
+
+def test_repeated_columns_in_a_large_put_are_merged(gb):
+    rows = random_rows(5000, seed=6, dup_rows=(7, 1234, 4999))
+    exp = expected_csr(rows)
+    same(assemble(gb, rows, bulk=True), exp)
+    assert gb.lib().HYPRE_GetError() == 0
+
+
+def test_add_to_values_after_a_large_put(gb):
+    rows = random_rows(5000, seed=7)
+    rng = np.random.default_rng(8)
+    adds = []
+    for r in (3, 77, 2500, 4998):
+        cs = list(rows[r][0][:2]) + [int(c) for c in rng.choice(5000, 2, replace=False) if c not in rows[r][0]]
+        adds.append((r, cs, list(rng.standard_normal(len(cs)))))
+    exp = expected_csr(rows, adds=adds)
+    same(assemble(gb, rows, bulk=True, adds=adds), exp)
+    same(assemble(gb, rows, bulk=False, adds=adds), exp)
+
+
+def test_get_values_after_a_large_put(gb):
+    rows = random_rows(4000, seed=9)
+    got = {}
+
+    def read(L, h):
+        for r in (0, 11, 1999, 3999):
+            cs = rows[r][0]
+            if not cs:
+                continue
+            nc = np.array([len(cs)], np.int32)
+            ri = np.array([r], np.int32)
+            J = np.array(cs, np.int32)
+            V = np.zeros(len(cs))
+            L.HYPRE_IJMatrixGetValues(h, 1, nc.ctypes.data, ri.ctypes.data, J.ctypes.data, V.ctypes.data)
+            got[r] = V
+
+    assemble(gb, rows, bulk=True, extra=read)
+    for r, V in got.items():
+        np.testing.assert_array_equal(V, np.array(rows[r][1]))
+    assert gb.lib().HYPRE_GetError() == 0
+
+
+def test_out_of_range_column_in_a_large_put_is_an_argument_error(gb):
+    rows = random_rows(3000, seed=10)
+    rows[100][0].append(3000)            # one past the last column
+    rows[100][1].append(1.0)
+    assemble(gb, rows, bulk=True, strict=False)
+    assert gb.lib().HYPRE_GetError() & 4        # HYPRE_ERROR_ARG
+    gb.lib().HYPRE_ClearAllErrors()
+
+
+def test_get_row(gb):
+    rows = random_rows(3000, seed=11)
+    I, J, V = expected_csr(rows)
+    A = gb.IJMatrix(I, J, V)
+    L = gb.lib()
+    for r in (0, 5, 2999):
+        size = C.c_int()
+        pc = C.POINTER(C.c_int)()
+        pv = C.POINTER(C.c_double)()
+        gb.check(L.HYPRE_ParCSRMatrixGetRow(A.par, r, C.byref(size), C.byref(pc), C.byref(pv)), "GetRow")
+        got_c = np.ctypeslib.as_array(pc, (size.value,)).copy() if size.value else np.zeros(0, np.int32)
+        got_v = np.ctypeslib.as_array(pv, (size.value,)).copy() if size.value else np.zeros(0)
+        L.HYPRE_ParCSRMatrixRestoreRow(A.par, r, C.byref(size), C.byref(pc), C.byref(pv))
+        np.testing.assert_array_equal(got_c, J[I[r]:I[r + 1]])
+        np.testing.assert_array_equal(got_v, V[I[r]:I[r + 1]])
+    A.destroy()
