@@ -306,6 +306,21 @@ __device__ __forceinline__ void gb_tab_clear(GbTabC &t, int n)
    __syncwarp();
 }
 
+// Find / insert on either table type (insert records the slot in GbTab's key
+// list so the table can be cleared entry by entry); insert returns false
+// when the table is full.
+__device__ __forceinline__ int gb_tfind(GbTab &t, int key) { return gb_tab_find(t.hk, t.hp, t.cap, key); }
+__device__ __forceinline__ int gb_tfind(GbTabC &t, int key) { return gb_tabc_find(t, key); }
+__device__ __forceinline__ bool gb_tinsert(GbTab &t, int key, int p)
+{
+   int slot = gb_tab_insert(t.hk, t.hp, t.cap, key, p);
+   if (slot < 0) { return false; }
+   t.lkeys[p] = key;
+   t.lslot[p] = slot;
+   return true;
+}
+__device__ __forceinline__ bool gb_tinsert(GbTabC &t, int key, int p) { return gb_tabc_insert(t, key, p) >= 0; }
+
 // Table of a warp in a two-tier kernel: a compact 1024-slot shared-memory
 // table (GB_SMEMC_BYTES per block of GB_SMEM_WARPS warps), or a full table in
 // global memory for the rows that overflow it.

@@ -660,32 +660,42 @@ static int ijm_migrate(HYPRE_IJMatrix m)
 static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const int *rows, const int *cols,
                           const double *values)
 {
+   if (nrows <= 0) { return 0; }
+   int *hstart = (int *) malloc(sizeof(int) * (size_t) (nrows + 1));
+   if (!hstart) { return 0; }
+   /* one pass: row offsets within the put, and every row valid, new and
+    * not repeated in this put (marked pending; unmarked on failure) */
    long long tot = 0;
-   for (int t = 0; t < nrows; t++)
-   {
-      if (ncols[t] < 0) { return 0; }
-      tot += ncols[t];
-   }
-   if (tot < GB_IJ_DEVICE_MIN || tot > 0x7fffffffLL) { return 0; }
    int t = 0, ok = 1;
+   hstart[0] = 0;
    for (; t < nrows; t++)
    {
       int r = rows[t] - m->ilower;
-      if (r < 0 || r >= m->nrows || m->row_state[r] != 0 || m->row_len[r] != 0) { ok = 0; break; }
+      int nc = ncols[t];
+      if (nc < 0 || r < 0 || r >= m->nrows || m->row_state[r] != 0 || m->row_len[r] != 0 || tot + nc > 0x7fffffffLL)
+      {
+         ok = 0;
+         break;
+      }
       m->row_state[r] = GB_IJ_ROW_PENDING;
+      tot += nc;
+      hstart[t + 1] = (int) tot;
    }
-   for (int u = 0; u < t; u++) { m->row_state[rows[u] - m->ilower] = 0; }
-   if (!ok) { return 0; }
-   int *hstart = (int *) malloc(sizeof(int) * (size_t) (nrows + 1));
+   if (ok && tot < GB_IJ_DEVICE_MIN) { ok = 0; }
+   if (!ok)
+   {
+      for (int u = 0; u < t; u++) { m->row_state[rows[u] - m->ilower] = 0; }
+      free(hstart);
+      return 0;
+   }
    int *dstart = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
    int *flags = (int *) gb_dcalloc(sizeof(int));
-   if (!hstart || !dstart || !flags || !ijm_staging_reserve(m, m->st_len + tot))
+   if (!dstart || !flags || !ijm_staging_reserve(m, m->st_len + tot))
    {
+      for (int u = 0; u < nrows; u++) { m->row_state[rows[u] - m->ilower] = 0; }
       free(hstart); gb_dfree(dstart); gb_dfree(flags);
       return 0;
    }
-   hstart[0] = 0;
-   for (int u = 0; u < nrows; u++) { hstart[u + 1] = hstart[u] + ncols[u]; }
    cudaStream_t s = gb_stream();
    cudaMemcpyAsync(m->st_cols + m->st_len, cols, sizeof(int) * (size_t) tot, cudaMemcpyHostToDevice, s);
    cudaMemcpyAsync(m->st_vals + m->st_len, values, sizeof(double) * (size_t) tot, cudaMemcpyHostToDevice, s);
@@ -693,7 +703,12 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
    gb_ij_check(nrows, dstart, m->st_cols + m->st_len, m->jupper - m->jlower + 1, flags, s);
    int f = ij_read_int(flags);   /* also the point after which the caller's buffers are free */
    gb_dfree(dstart); gb_dfree(flags);
-   if (f != 0) { free(hstart); return 0; }
+   if (f != 0)
+   {
+      for (int u = 0; u < nrows; u++) { m->row_state[rows[u] - m->ilower] = 0; }
+      free(hstart);
+      return 0;
+   }
    for (int u = 0; u < nrows; u++)
    {
       int r = rows[u] - m->ilower;
@@ -958,7 +973,9 @@ struct hypre_IJVector_struct
    int        jlower, jupper, n;
    int        object_type;
    int        num_components;
-   double    *h;        /* host staging */
+   double    *h;        /* host mirror for partial puts */
+   int        h_valid;  /* h holds the vector's values (plus pending puts) */
+   int        h_dirty;  /* h has puts not yet on the device */
    gb_parvec *par;
    int        initialized;
 };
@@ -1001,10 +1018,10 @@ HYPRE_Int HYPRE_IJVectorSetNumComponents(HYPRE_IJVector v, HYPRE_Int nc)
 HYPRE_Int HYPRE_IJVectorInitialize(HYPRE_IJVector v)
 {
    if (!check_ijv(v, 1)) { return gb_error_flag; }
-   free(v->h);
-   v->h = (double *) calloc((size_t) (v->n ? v->n : 1), sizeof(double));
    if (!v->par) { v->par = gb_parvec_new(v->n); }
-   else { gb_fill_d(v->n, v->par->d, 0.0, gb_stream()); }
+   if (v->par) { gb_fill_d(v->n, v->par->d, 0.0, gb_stream()); }
+   v->h_valid = 0;
+   v->h_dirty = 0;
    v->initialized = 1;
    return gb_error_flag;
 }
@@ -1015,6 +1032,22 @@ HYPRE_Int HYPRE_IJVectorInitialize_v2(HYPRE_IJVector v, HYPRE_MemoryLocation loc
    return HYPRE_IJVectorInitialize(v);
 }
 
+/* host mirror = the device vector's current values */
+static int ijv_mirror(HYPRE_IJVector v)
+{
+   if (v->h_valid) { return 1; }
+   if (!v->h) { v->h = (double *) malloc(sizeof(double) * (size_t) (v->n ? v->n : 1)); }
+   if (!v->h) { gb_error(HYPRE_ERROR_MEMORY, "IJ vector"); return 0; }
+   cudaMemcpyAsync(v->h, v->par->d, sizeof(double) * (size_t) v->n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   v->h_valid = 1;
+   return 1;
+}
+
+/* Puts write the vector's values (as the reference's, which go straight into
+ * the ParVector's data).  A put of all n values in order is copied from the
+ * caller's buffer to the device; other puts edit the host mirror, which
+ * Assemble uploads. */
 static HYPRE_Int ijv_put(HYPRE_IJVector v, HYPRE_Int nvalues, const HYPRE_BigInt *idx, const HYPRE_Complex *vals,
                          int add)
 {
@@ -1022,12 +1055,22 @@ static HYPRE_Int ijv_put(HYPRE_IJVector v, HYPRE_Int nvalues, const HYPRE_BigInt
    if (!v->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ vector not initialized"); return gb_error_flag; }
    if (nvalues < 0) { gb_error_in_arg(2); return gb_error_flag; }
    if (!vals) { gb_error_in_arg(4); return gb_error_flag; }
+   if (!add && !idx && nvalues == v->n)
+   {
+      cudaMemcpyAsync(v->par->d, vals, sizeof(double) * (size_t) v->n, cudaMemcpyHostToDevice, gb_stream());
+      gb_sync();
+      v->h_valid = 0;
+      v->h_dirty = 0;
+      return gb_error_flag;
+   }
+   if (!ijv_mirror(v)) { return gb_error_flag; }
    for (int k = 0; k < nvalues; k++)
    {
       int i = idx ? idx[k] - v->jlower : k;
       if (i < 0 || i >= v->n) { gb_error_in_arg(3); continue; }
       if (add) { v->h[i] += vals[k]; } else { v->h[i] = vals[k]; }
    }
+   v->h_dirty = 1;
    return gb_error_flag;
 }
 
@@ -1047,8 +1090,14 @@ HYPRE_Int HYPRE_IJVectorAssemble(HYPRE_IJVector v)
 {
    if (!check_ijv(v, 1)) { return gb_error_flag; }
    if (!v->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ vector not initialized"); return gb_error_flag; }
-   cudaMemcpyAsync(v->par->d, v->h, sizeof(double) * (size_t) v->n, cudaMemcpyHostToDevice, gb_stream());
-   gb_sync();
+   if (v->h_dirty)
+   {
+      cudaMemcpyAsync(v->par->d, v->h, sizeof(double) * (size_t) v->n, cudaMemcpyHostToDevice, gb_stream());
+      gb_sync();
+      v->h_dirty = 0;
+   }
+   /* solves change the device vector from here on */
+   v->h_valid = 0;
    return gb_error_flag;
 }
 
@@ -1056,9 +1105,16 @@ HYPRE_Int HYPRE_IJVectorGetValues(HYPRE_IJVector v, HYPRE_Int nvalues, const HYP
 {
    if (!check_ijv(v, 1)) { return gb_error_flag; }
    if (!vals) { gb_error_in_arg(4); return gb_error_flag; }
-   /* read back the device vector (it may have been changed by a solve) */
-   cudaMemcpyAsync(v->h, v->par->d, sizeof(double) * (size_t) v->n, cudaMemcpyDeviceToHost, gb_stream());
-   gb_sync();
+   if (!v->initialized || !v->par) { gb_error(HYPRE_ERROR_GENERIC, "IJ vector not initialized"); return gb_error_flag; }
+   if (!v->h_dirty && !idx && nvalues == v->n)
+   {
+      /* the device vector (it may have been changed by a solve) */
+      cudaMemcpyAsync(vals, v->par->d, sizeof(double) * (size_t) v->n, cudaMemcpyDeviceToHost, gb_stream());
+      gb_sync();
+      return gb_error_flag;
+   }
+   if (!v->h_dirty) { v->h_valid = 0; }
+   if (!ijv_mirror(v)) { return gb_error_flag; }
    for (int k = 0; k < nvalues; k++)
    {
       int i = idx ? idx[k] - v->jlower : k;

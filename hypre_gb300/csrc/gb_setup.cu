@@ -1136,7 +1136,7 @@ __device__ __forceinline__ typename SpgemmTab<MODE>::type spgemm_tab(int *sh, in
 }
 
 template <int MODE, bool NUMERIC>
-__global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, const int *__restrict__ Ai,
+__global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W, const int *__restrict__ Ai,
                                                 const int *__restrict__ Aj, const double *__restrict__ Av,
                                                 const int *__restrict__ Bi, const int *__restrict__ Bj,
                                                 const double *__restrict__ Bv, int *__restrict__ cnt,
@@ -1194,15 +1194,16 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
          len = Bi[k + 1] - kb0;
          if (NUMERIC) { av = Av[ka + lane]; }
       }
-      while (ka < ka1 && !ovf)
-      {
-         int pre = len;   // inclusive prefix over lanes
+      // maps lane l to its product in the window (inclusive prefix pre over
+      // the entries' remaining lengths) and loads its column and B value
+      auto map_step = [&](int &pre, int &total, int &col, double &bval, double &aval) {
+         pre = len;
          for (int o = 1; o < 32; o <<= 1)
          {
             int y = __shfl_up_sync(GB_FULL, pre, o);
             if (lane >= o) { pre += y; }
          }
-         const int total = __shfl_sync(GB_FULL, pre, 31);
+         total = __shfl_sync(GB_FULL, pre, 31);
          // entry j of lane's product l = lane: smallest j with pre_j > l
          int lo = 0, hi = 31;
          for (int it = 0; it < 5; it++)
@@ -1214,45 +1215,19 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
          const int j = lo;
          const int prej = __shfl_sync(GB_FULL, pre, j > 0 ? j - 1 : 0);
          const int kbj = __shfl_sync(GB_FULL, kb0, j);
-         const double avj = NUMERIC ? __shfl_sync(GB_FULL, av, j) : 0.0;
-         const bool act = lane < total;
-         int col = -1;
-         double v = 0.0;
-         if (act)
+         aval = NUMERIC ? __shfl_sync(GB_FULL, av, j) : 0.0;
+         col = -1;
+         bval = 0.0;
+         if (lane < total)
          {
             const int kb = kbj + (lane - (j > 0 ? prej : 0));
             col = Bj[kb];
-            if (NUMERIC) { v = avj * Bv[kb]; }
+            if (NUMERIC) { bval = Bv[kb]; }
          }
-         if (!NUMERIC)
-         {
-            gb_wcount(T, count, col, act, ovf);
-         }
-         else
-         {
-            int pos = gb_winsert(T, count, col, act, created, ovf);
-            stage[lane] = v;
-            __syncwarp();
-            unsigned grp = __match_any_sync(GB_FULL, (act && pos >= 0) ? pos : -(lane + 2));
-            int leader = __ffs(grp) - 1;
-            if (act && pos >= 0 && lane == leader)
-            {
-               double x;
-               if (created) { Cj[off + pos] = col; x = v; }
-               else { x = Cv[off + pos] + v; }
-               unsigned rest = grp & (grp - 1u);
-               while (rest)
-               {
-                  int m = __ffs(rest) - 1;
-                  rest &= rest - 1u;
-                  x += stage[m];
-               }
-               Cv[off + pos] = x;
-            }
-            __syncwarp();
-         }
-         // advance past the consumed products: drop the nfull used-up
-         // entries, shift the window down and load the entries that enter it
+      };
+      // drops the products of the step just mapped: the nfull used-up
+      // entries leave, the window shifts down and loads the entries that enter
+      auto advance = [&](int pre, int total) {
          const int consumed = total < 32 ? total : 32;
          const int nfull = __popc(__ballot_sync(GB_FULL, pre <= consumed));
          if (nfull == 0)
@@ -1281,6 +1256,62 @@ __global__ void __launch_bounds__(128) k_spgemm(int nrows, int square, int W, co
                }
             }
             if (lane == 0) { kb0 += used; len -= used; }
+         }
+      };
+      int pre = 0, total = 0, col = -1;
+      double bval = 0.0, aval = 0.0;
+      if (ka < ka1) { map_step(pre, total, col, bval, aval); }
+      while (ka < ka1 && !ovf)
+      {
+         const bool act = lane < total;
+         const int ccol = col;
+         const double v = aval * bval;
+         // map and load the next step before inserting this one
+         advance(pre, total);
+         if (ka < ka1) { map_step(pre, total, col, bval, aval); }
+         if (!NUMERIC)
+         {
+            gb_wcount(T, count, ccol, act, ovf);
+         }
+         else
+         {
+            // lanes with the same column form a group; its first lane finds
+            // or inserts the column (new columns numbered in lane order, the
+            // order of first discovery) and adds the group's terms in lane
+            // order to the row's value
+            const unsigned grp = __match_any_sync(GB_FULL, act ? ccol : -(lane + 2));
+            const int leader = __ffs(grp) - 1;
+            const bool lead = act && lane == leader;
+            int pos = lead ? gb_tfind(T, ccol) : -1;
+            const bool need = lead && pos < 0;
+            const unsigned nm = __ballot_sync(GB_FULL, need);
+            bool bad = false, created = false;
+            if (need)
+            {
+               const int p = count + __popc(nm & ((1u << lane) - 1u));
+               if (p < T.listcap && gb_tinsert(T, ccol, p)) { pos = p; created = true; }
+               else { bad = true; }
+            }
+            count += __popc(nm);
+            if (count > T.listcap) { count = T.listcap; }
+            if (__any_sync(GB_FULL, bad)) { ovf = 1; }
+            stage[lane] = v;
+            __syncwarp();
+            if (lead && pos >= 0)
+            {
+               double x;
+               if (created) { Cj[off + pos] = ccol; x = v; }
+               else { x = Cv[off + pos] + v; }
+               unsigned rest = grp & (grp - 1u);
+               while (rest)
+               {
+                  int m = __ffs(rest) - 1;
+                  rest &= rest - 1u;
+                  x += stage[m];
+               }
+               Cv[off + pos] = x;
+            }
+            __syncwarp();
          }
       }
       if (lane == 0)

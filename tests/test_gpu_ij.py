@@ -193,3 +193,46 @@ def test_get_row(gb):
         np.testing.assert_array_equal(got_c, J[I[r]:I[r + 1]])
         np.testing.assert_array_equal(got_v, V[I[r]:I[r + 1]])
     A.destroy()
+
+
+def test_ij_vector_puts_and_gets(gb):
+    L = gb.lib()
+    n = 10000
+    rng = np.random.default_rng(12)
+    a = rng.standard_normal(n)
+    v = C.c_void_p()
+    L.HYPRE_IJVectorCreate(0, 0, n - 1, C.byref(v))
+    L.HYPRE_IJVectorSetObjectType(v, gb.HYPRE_PARCSR)
+    L.HYPRE_IJVectorInitialize(v)
+    L.HYPRE_IJVectorSetValues(v, n, None, a.ctypes.data)          # all values, in order
+    L.HYPRE_IJVectorAssemble(v)
+    out = np.zeros(n)
+    L.HYPRE_IJVectorGetValues(v, n, None, out.ctypes.data)
+    np.testing.assert_array_equal(out, a)
+    # indexed puts and adds act on the current values
+    idx = np.array([5, 17, 9999, 17], np.int32)
+    add = np.array([1.0, 2.0, 3.0, 4.0])
+    L.HYPRE_IJVectorAddToValues(v, 4, idx.ctypes.data, add.ctypes.data)
+    exp = a.copy()
+    for i, x in zip(idx, add):
+        exp[i] += x
+    got = np.zeros(3)
+    gi = np.array([17, 5, 9999], np.int32)
+    L.HYPRE_IJVectorGetValues(v, 3, gi.ctypes.data, got.ctypes.data)    # pending puts are visible
+    np.testing.assert_array_equal(got, exp[gi])
+    L.HYPRE_IJVectorAssemble(v)
+    L.HYPRE_IJVectorGetValues(v, n, None, out.ctypes.data)
+    np.testing.assert_array_equal(out, exp)
+    # the device vector changed by the library (scaled through the ParVector)
+    par = C.c_void_p()
+    L.HYPRE_IJVectorGetObject(v, C.byref(par))
+    L.HYPRE_ParVectorScale(2.0, par)
+    one = np.array([3.0])
+    L.HYPRE_IJVectorSetValues(v, 1, np.array([0], np.int32).ctypes.data, one.ctypes.data)
+    L.HYPRE_IJVectorAssemble(v)
+    L.HYPRE_IJVectorGetValues(v, n, None, out.ctypes.data)
+    exp = 2.0 * exp
+    exp[0] = 3.0
+    np.testing.assert_array_equal(out, exp)
+    assert L.HYPRE_GetError() == 0
+    L.HYPRE_IJVectorDestroy(v)
