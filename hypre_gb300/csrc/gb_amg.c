@@ -119,6 +119,22 @@ static int scan_total(const int *in, int *out, int n)
    return read_int(out + n);
 }
 
+/* Rewrites a list of distinct rows of 0..n-1 in increasing order (flags,
+ * scan, scatter): the warps of the next tier then work on neighbouring rows
+ * at the same time, whose B rows share the L2. */
+static void sort_row_list(int *list, int nlist, int n)
+{
+   if (nlist <= 1) { return; }
+   cudaStream_t s = gb_stream();
+   int *flag = (int *) gb_dcalloc(sizeof(int) * (size_t) (n + 1));
+   int *pos = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   if (!flag || !pos) { gb_dfree(flag); gb_dfree(pos); return; }
+   gb_list_flags(nlist, list, flag, s);
+   scan_total(flag, pos, n);
+   gb_scatter_list(n, flag, pos, list, s);
+   gb_dfree(flag); gb_dfree(pos);
+}
+
 static int max_of(const int *d, int n)
 {
    /* small host reduction of a device array (setup only) */
@@ -287,6 +303,7 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    int h1 = read_int(t.ovf_n), h2 = 0;
    if (h1 > 0)
    {
+      sort_row_list(t.ovf_list, h1, n);
       list2 = (int *) gb_dmalloc(sizeof(int) * (size_t) h1);
       if (rowchunk)
       {

@@ -12,14 +12,22 @@ extern "C" void gb_count_launch(int n);
 
 __device__ __forceinline__ int gb_lane() { return threadIdx.x & 31; }
 
-__device__ __forceinline__ unsigned gb_hash(int key) { return (unsigned) key * 2654435761u; }
+// Home slot of a key in a table of cap (a power of two) slots: the top
+// log2(cap) bits of the multiplicative (Fibonacci) hash.  The low bits of the
+// product would only permute key mod cap, and the columns of a row from a
+// structured grid differ by multiples of the row and plane strides, so they
+// would share low bits and build long probe chains.
+__device__ __forceinline__ unsigned gb_slot(int key, int cap)
+{
+   return cap > 1 ? ((unsigned) key * 2654435761u) >> (__clz(cap) + 1) : 0u;
+}
 
 // Open-addressing table (linear probing) mapping a non-negative key to its
 // position in a per-row list kept in discovery order.  hk[] holds -1 in empty
 // slots; cap is a power of two.
 __device__ __forceinline__ int gb_tab_find(const int *hk, const int *hp, int cap, int key)
 {
-   unsigned s = gb_hash(key) & (cap - 1);
+   unsigned s = gb_slot(key, cap);
    for (int probe = 0; probe < cap; probe++)
    {
       int k = hk[s];
@@ -33,7 +41,7 @@ __device__ __forceinline__ int gb_tab_find(const int *hk, const int *hp, int cap
 // Inserts key -> pos; returns the slot used, or -1 when the table is full.
 __device__ __forceinline__ int gb_tab_insert(int *hk, int *hp, int cap, int key, int pos)
 {
-   unsigned s = gb_hash(key) & (cap - 1);
+   unsigned s = gb_slot(key, cap);
    for (int probe = 0; probe < cap; probe++)
    {
       int prev = atomicCAS(&hk[s], -1, key);
@@ -245,7 +253,7 @@ __device__ __forceinline__ void gb_tab_init(GbTabC &t)
 
 __device__ __forceinline__ int gb_tabc_find(const GbTabC &t, int key)
 {
-   unsigned s = gb_hash(key) & (t.cap - 1);
+   unsigned s = gb_slot(key, t.cap);
    for (int probe = 0; probe < t.cap; probe++)
    {
       int k = t.hk[s];
@@ -258,7 +266,7 @@ __device__ __forceinline__ int gb_tabc_find(const GbTabC &t, int key)
 
 __device__ __forceinline__ int gb_tabc_insert(GbTabC &t, int key, int pos)
 {
-   unsigned s = gb_hash(key) & (t.cap - 1);
+   unsigned s = gb_slot(key, t.cap);
    for (int probe = 0; probe < t.cap; probe++)
    {
       int prev = atomicCAS(&t.hk[s], -1, key);
@@ -345,7 +353,7 @@ __device__ __forceinline__ typename GbTierTab<GLOBAL>::type gb_tier_tab(int *sh,
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int gb_tab_claim(int *hk, int cap, int key, bool &isnew)
 {
-   unsigned s = gb_hash(key) & (cap - 1);
+   unsigned s = gb_slot(key, cap);
    for (int probe = 0; probe < cap; probe++)
    {
       int prev = atomicCAS(&hk[s], -1, key);
