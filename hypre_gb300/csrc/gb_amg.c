@@ -273,7 +273,7 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    gb_tier t;
    tier_begin(&t, n);
    int *list2 = NULL, *n2 = (int *) gb_dcalloc(sizeof(int) * 2);
-   const int W = 0;   /* products are flattened 32 per step; no lane groups */
+   const int W = 0;   /* no rows skipped by the tier-0 numeric pass */
    int *ub = NULL;
    /* B rows of a dozen entries or more: one B-row chunk per warp step
     * (gb_spgemm_rc); short B rows: products flattened 32 per step */
@@ -347,8 +347,20 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    }
    else
    {
-      gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL,
-                NULL, n, NULL, 0, 0, t.err, NULL, 1, 0, s);
+      /* many products per row (RA*P): rows of at most 192 columns accumulate
+       * in shared memory (tier 3), the longer ones in tier 0; few products
+       * per row (FF*FC, P1*P2): tier 0 alone, where the fixed cost per row
+       * is lower */
+      const double prods = ((double) A->nnz / (A->nr > 0 ? A->nr : 1)) * ((double) B->nnz / (B->nr > 0 ? B->nr : 1));
+      int skip = 0;
+      if (prods >= 512.0)
+      {
+         gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
+                   NULL, NULL, n, NULL, 0, 0, t.err, NULL, 1, 3, s);
+         skip = GB_SPGEMM_TINY_COLS;
+      }
+      gb_spgemm(n, square, skip, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
+                NULL, NULL, n, NULL, 0, 0, t.err, NULL, 1, 0, s);
       if (h1 > 0)
       {
          gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,

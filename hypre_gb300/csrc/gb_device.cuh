@@ -12,19 +12,22 @@ extern "C" void gb_count_launch(int n);
 
 __device__ __forceinline__ int gb_lane() { return threadIdx.x & 31; }
 
-// Home slot of a key in a table of cap (a power of two) slots: the top
-// log2(cap) bits of the multiplicative (Fibonacci) hash.  The low bits of the
-// product would only permute key mod cap, and the columns of a row from a
-// structured grid differ by multiples of the row and plane strides, so they
-// would share low bits and build long probe chains.
+// Home slot of a key in a table of cap slots: the multiplicative (Fibonacci)
+// hash scaled to [0, cap) by its high bits (for a power of two, the top
+// log2(cap) bits).  The low bits of the product would only permute key mod
+// cap, and the columns of a row from a structured grid differ by multiples of
+// the row and plane strides, so they would share low bits and build long
+// probe chains.  Any cap works (probing wraps explicitly).
 __device__ __forceinline__ unsigned gb_slot(int key, int cap)
 {
-   return cap > 1 ? ((unsigned) key * 2654435761u) >> (__clz(cap) + 1) : 0u;
+   return __umulhi((unsigned) key * 2654435761u, (unsigned) cap);
 }
+
+__device__ __forceinline__ unsigned gb_next_slot(unsigned s, int cap) { return s + 1 == (unsigned) cap ? 0u : s + 1; }
 
 // Open-addressing table (linear probing) mapping a non-negative key to its
 // position in a per-row list kept in discovery order.  hk[] holds -1 in empty
-// slots; cap is a power of two.
+// slots.
 __device__ __forceinline__ int gb_tab_find(const int *hk, const int *hp, int cap, int key)
 {
    unsigned s = gb_slot(key, cap);
@@ -33,7 +36,7 @@ __device__ __forceinline__ int gb_tab_find(const int *hk, const int *hp, int cap
       int k = hk[s];
       if (k == key) { return hp[s]; }
       if (k < 0) { return -1; }
-      s = (s + 1) & (cap - 1);
+      s = gb_next_slot(s, cap);
    }
    return -1;
 }
@@ -46,7 +49,7 @@ __device__ __forceinline__ int gb_tab_insert(int *hk, int *hp, int cap, int key,
    {
       int prev = atomicCAS(&hk[s], -1, key);
       if (prev < 0 || prev == key) { hp[s] = pos; return (int) s; }
-      s = (s + 1) & (cap - 1);
+      s = gb_next_slot(s, cap);
    }
    return -1;
 }
@@ -259,7 +262,7 @@ __device__ __forceinline__ int gb_tabc_find(const GbTabC &t, int key)
       int k = t.hk[s];
       if (k == key) { return t.hp[s]; }
       if (k < 0) { return -1; }
-      s = (s + 1) & (t.cap - 1);
+      s = gb_next_slot(s, t.cap);
    }
    return -1;
 }
@@ -271,7 +274,7 @@ __device__ __forceinline__ int gb_tabc_insert(GbTabC &t, int key, int pos)
    {
       int prev = atomicCAS(&t.hk[s], -1, key);
       if (prev < 0 || prev == key) { t.hp[s] = (unsigned short) pos; return (int) s; }
-      s = (s + 1) & (t.cap - 1);
+      s = gb_next_slot(s, t.cap);
    }
    return -1;
 }
@@ -359,7 +362,7 @@ __device__ __forceinline__ int gb_tab_claim(int *hk, int cap, int key, bool &isn
       int prev = atomicCAS(&hk[s], -1, key);
       if (prev < 0) { isnew = true; return (int) s; }
       if (prev == key) { isnew = false; return (int) s; }
-      s = (s + 1) & (cap - 1);
+      s = gb_next_slot(s, cap);
    }
    isnew = false;
    return -1;

@@ -87,6 +87,7 @@ void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj
  * rows whose upper bound exceeds the table go straight to the list), 1 (large
  * shared tables, rows in ovf_list, overflow to out_list) or 2 (global tables,
  * rows in ovf_list); phase 0 symbolic, 1 numeric */
+#define GB_SPGEMM_TINY_COLS 192   /* list capacity of numeric tier 3 */
 void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av, const int *Bi,
                const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list,
                int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab, int gcap, int gwarps, int *err,

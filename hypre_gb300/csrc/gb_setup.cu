@@ -1124,6 +1124,14 @@ extern "C" void gb_transpose_fill(int nr, int nc, const int *Ai, const int *Aj, 
 // tier 0: compact 1024-slot tables (6 KB per warp, rows up to 768 columns)
 #define GB_SMALL_BYTES (GB_SMEM_WARPS * GB_TABC_BYTES(GB_SMEM_CAP))
 
+// numeric tier 3: rows of at most 192 columns, 256-slot compact tables with
+// the row's FP64 values in shared memory beside them (3 KB per warp)
+#define GB_TINY_CAP 256
+#define GB_TINY_LCAP (GB_TINY_CAP / 4 * 3)
+#define GB_TINY_WBYTES (GB_TABC_BYTES(GB_TINY_CAP) + GB_TINY_LCAP * 8)
+#define GB_TINY_BYTES (GB_SMEM_WARPS * GB_TINY_WBYTES)
+static_assert(GB_TINY_LCAP == GB_SPGEMM_TINY_COLS, "tier-3 capacity known to the host");
+
 template <int MODE> struct SpgemmTab { typedef GbTabC type; };
 template <> struct SpgemmTab<2> { typedef GbTab type; };
 
@@ -1132,6 +1140,7 @@ __device__ __forceinline__ typename SpgemmTab<MODE>::type spgemm_tab(int *sh, in
 {
    if constexpr (MODE == 1) { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TABC_BYTES(GB_BIG_CAP), GB_BIG_CAP); }
    else if constexpr (MODE == 2) { return gb_tab_at(gtab + (size_t) warp * GB_TAB_INTS(gcap), gcap); }
+   else if constexpr (MODE == 3) { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TINY_WBYTES, GB_TINY_CAP); }
    else { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TABC_BYTES(GB_SMEM_CAP), GB_SMEM_CAP); }
 }
 
@@ -1152,11 +1161,15 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
    int nwarps = (gridDim.x * blockDim.x) >> 5;
    typename SpgemmTab<MODE>::type T = spgemm_tab<MODE>(sh, gtab, gcap, warp);
    if (MODE != 2) { gb_tab_init(T); }
-   int total = MODE ? *ovf_n : nrows;
-   (void) W;
+   // tier 3 keeps the row's values in shared memory behind its table
+   double *vals = MODE == 3 ? (double *) ((char *) sh + (threadIdx.x >> 5) * GB_TINY_WBYTES +
+                                          GB_TABC_BYTES(GB_TINY_CAP))
+                            : nullptr;
+   constexpr bool LISTED = MODE == 1 || MODE == 2;
+   int total = LISTED ? *ovf_n : nrows;
    for (int t = warp; t < total; t += nwarps)
    {
-      int r = MODE ? ovf_list[t] : t;
+      int r = LISTED ? ovf_list[t] : t;
       int off = 0;
       if (MODE == 0 && !NUMERIC && ub && ub[r] > 16 * T.listcap)
       {
@@ -1168,14 +1181,22 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
       if (NUMERIC)
       {
          off = Ci[r];
-         if (MODE != 2 && Ci[r + 1] - off > T.listcap) { continue; }
+         const int len = Ci[r + 1] - off;
+         if (MODE != 2 && len > T.listcap) { continue; }
+         // W > 0: rows of at most W columns were done by tier 3
+         if (MODE == 0 && W > 0 && len <= W) { continue; }
       }
       int count = 0, ovf = 0;
       bool created;
       if (square)
       {
          int pos = gb_winsert(T, count, r, lane == 0, created, ovf);
-         if (NUMERIC && lane == 0 && pos >= 0) { Cj[off + pos] = r; Cv[off + pos] = 0.0; }
+         if (NUMERIC && lane == 0 && pos >= 0)
+         {
+            Cj[off + pos] = r;
+            if (MODE == 3) { vals[pos] = 0.0; }
+            else { Cv[off + pos] = 0.0; }
+         }
          __syncwarp();
       }
       // The row's products a_rk b_kc in sequential order (A entries in
@@ -1301,7 +1322,7 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
             {
                double x;
                if (created) { Cj[off + pos] = ccol; x = v; }
-               else { x = Cv[off + pos] + v; }
+               else { x = (MODE == 3 ? vals[pos] : Cv[off + pos]) + v; }
                unsigned rest = grp & (grp - 1u);
                while (rest)
                {
@@ -1309,10 +1330,16 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
                   rest &= rest - 1u;
                   x += stage[m];
                }
-               Cv[off + pos] = x;
+               if (MODE == 3) { vals[pos] = x; }
+               else { Cv[off + pos] = x; }
             }
             __syncwarp();
          }
+      }
+      if (MODE == 3 && NUMERIC && !ovf)
+      {
+         for (int p = lane; p < count; p += 32) { Cv[off + p] = vals[p]; }
+         __syncwarp();
       }
       if (lane == 0)
       {
@@ -1359,8 +1386,10 @@ extern "C" void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, co
    GB_COUNT(1);
 }
 
-// phase: 0 symbolic, 1 numeric; tier: 0 shared memory (all rows), 1 global (overflow list).
-// W: lane-group width for B rows of at most W entries (power of two <= 32), 0 for long rows.
+// phase: 0 symbolic, 1 numeric; tier: 0 shared memory (all rows), 1 large shared tables
+// (overflow list), 2 global tables (second list), 3 numeric rows of at most GB_TINY_LCAP
+// columns with values in shared memory.  W (numeric tier 0): rows of at most W columns
+// are skipped (done by tier 3); 0 skips none.
 extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av,
                           const int *Bi, const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj,
                           double *Cv, int *ovf_list, int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab,
@@ -1392,6 +1421,14 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
          k_spgemm<0, true><<<blocks, 128, GB_SMALL_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
                                                               Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
       }
+   }
+   else if (tier == 3)
+   {
+      /* numeric only: 3 KB tables per warp, twelve blocks per SM (registers) */
+      long long want = ((long long) nrows + GB_SMEM_WARPS - 1) / GB_SMEM_WARPS;
+      int blocks = (int) (want < 152 * 12 ? (want > 0 ? want : 1) : 152 * 12);
+      k_spgemm<3, true><<<blocks, 128, GB_TINY_BYTES, s>>>(nrows, square, 0, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
+                                                           ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
    }
    else if (tier == 1)
    {
