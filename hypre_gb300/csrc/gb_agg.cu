@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
                                             const int *__restrict__ S2i, int *__restrict__ S2j, int *ovf_list,
                                             int *ovf_n, int *gtab, int gcap, int *err)
 {
-   extern __shared__ int sh[];
+   extern __shared__ __align__(16) int sh[];
    const int lane = gb_lane();
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;

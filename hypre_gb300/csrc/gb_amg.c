@@ -1019,6 +1019,15 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
       gb_solve_desc(L->A, vp0);
       if (vp0 != GB_PREC_F64) { gb_solve_desc(L->A, GB_PREC_F64); }
       if (L->P) { gb_solve_desc(L->P, vp); gb_solve_desc(L->R, vp); }
+      /* lower-part forms for two-stage Gauss-Seidel (built here, outside any
+       * graph capture of the cycle) */
+      int ts = 0;
+      for (int k = 1; k <= 2; k++) { ts |= prm->relax_type[k] == 11 || prm->relax_type[k] == 12; }
+      if (ts && l < amg->num_levels - 1)
+      {
+         const void *dg = NULL;
+         gb_lower_desc(L->A, vp0, &dg);
+      }
    }
    if (amg->mlp_params && gb_learn_weights(amg)) { return gb_error_flag; }
    /* Chebyshev data on the levels that relax with it (par_amg_setup.c:3496-3536) */
@@ -1068,11 +1077,17 @@ static void twostage_gs_d(gb_amg *amg, int l, int inner, const double *f, double
    /* V = w (f - A u) */
    if (u_zero) { gb_fill_d(L->n, u, 0.0, s); gb_scaled_copy_d(L->n, w, f, V, s); }
    else { gb_spmv_d(A, u, V, 0, -w, w, f, NULL, 0.0, NULL, NULL, s); }
-   gb_gs_first_d(L->n, L->A->A.i, L->A->A.v, V, u, s);
+   /* large levels: the strictly lower part as SELL-32 with the diagonal in
+    * a contiguous array (coalesced, half the bytes of the whole rows) */
+   const void *diag = NULL;
+   const gb_spmv_desc *Lo = gb_lower_desc(L->A, GB_PREC_F64, &diag);
+   if (Lo) { gb_gs_first_diag_d(L->n, (const double *) diag, V, u, s); }
+   else { gb_gs_first_d(L->n, L->A->A.i, L->A->A.v, V, u, s); }
    double m = -1.0;
    for (int k = 0; k < inner; k++)
    {
-      gb_gs_lower_d(L->n, L->A->A.i, L->A->A.j, L->A->A.v, V, Z, u, m, s);
+      if (Lo) { gb_spmv_d(Lo, V, Z, GB_EPI_GS, m, 0.0, u, (const double *) diag, 0.0, NULL, NULL, s); }
+      else { gb_gs_lower_d(L->n, L->A->A.i, L->A->A.j, L->A->A.v, V, Z, u, m, s); }
       double *t = V; V = Z; Z = t;
       m = -m;
    }
@@ -1228,11 +1243,18 @@ static void twostage_gs_f(gb_amg *amg, int l, int inner, const float *f, float *
    float *V = L->Vf, *Z = L->U2f;
    if (u_zero) { gb_fill_f(L->n, u, 0.f, s); gb_scaled_copy_f(L->n, w, f, V, s); }
    else { gb_spmv_f(A, u, V, 0, -w, w, f, NULL, 0.f, NULL, NULL, s); }
-   gb_gs_first_f(L->n, L->A->A.i, A->v, vp, A->rs, V, u, s);
+   /* large levels: strictly lower part as SELL-32 (see twostage_gs_d); the
+    * FP16 form has a unit diagonal in its values and a_ii in rs */
+   const void *diag = NULL;
+   const gb_spmv_desc *Lo = gb_lower_desc(L->A, vp, &diag);
+   const float *d1 = vp == GB_PREC_F16 ? A->rs : (const float *) diag;
+   if (Lo) { gb_gs_first_diag_f(L->n, d1, V, u, s); }
+   else { gb_gs_first_f(L->n, L->A->A.i, A->v, vp, A->rs, V, u, s); }
    float m = -1.f;
    for (int k = 0; k < inner; k++)
    {
-      gb_gs_lower_f(L->n, L->A->A.i, L->A->A.j, A->v, vp, V, Z, u, m, s);
+      if (Lo) { gb_spmv_f(Lo, V, Z, GB_EPI_GS, m, 0.f, u, (const float *) diag, 0.f, NULL, NULL, s); }
+      else { gb_gs_lower_f(L->n, L->A->A.i, L->A->A.j, A->v, vp, V, Z, u, m, s); }
       float *t = V; V = Z; Z = t;
       m = -m;
    }

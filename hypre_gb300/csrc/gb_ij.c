@@ -27,6 +27,7 @@ static void solveform_free(gb_solveform *f)
 {
    gb_dfree(f->vals); gb_dfree(f->sl_ptr); gb_dfree(f->sl_w); gb_dfree(f->sl_j); gb_dfree(f->sl_v);
    gb_dfree(f->rs);
+   gb_dfree(f->lo_diag); gb_dfree(f->lo_sl_ptr); gb_dfree(f->lo_sl_w); gb_dfree(f->lo_sl_j); gb_dfree(f->lo_sl_v);
    memset(f, 0, sizeof(*f));
 }
 
@@ -119,6 +120,70 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
    if (!use_sell) { f->desc.fmt = GB_FMT_CSR; }
    f->valid = 1;
    return &f->desc;
+}
+
+const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag)
+{
+   gb_solveform *f = &M->sf[vprec];
+   if (!f->valid) { gb_solve_desc(M, vprec); }
+   if (f->lo_valid) { *diag = f->lo_diag; return f->lo_valid > 0 ? &f->lo : NULL; }
+   gb_csr *A = &M->A;
+   double avg = A->nr ? (double) A->nnz / A->nr : 0;
+   int nsl = (A->nr + 31) / 32;
+   if (A->nr < 65536 || avg > 40 || nsl > 1024 * 1024) { f->lo_valid = -1; *diag = NULL; return NULL; }
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   /* the values of this precision's form in FP64: row-scaled for FP16 */
+   const double *vsrc = A->v;
+   double *scaled = NULL;
+   if (vprec == GB_PREC_F16)
+   {
+      scaled = (double *) gb_dmalloc(sizeof(double) * (size_t) (A->nnz ? A->nnz : 1));
+      float *rs_tmp = (float *) gb_dmalloc(sizeof(float) * (size_t) n);
+      gb_row_scaled_vals(n, A->i, A->v, scaled, rs_tmp, s);
+      gb_dfree(rs_tmp);
+      vsrc = scaled;
+   }
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *Li = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *scr = (int *) gb_dmalloc(sizeof(int) * (size_t) gb_scan_scratch_ints(n));
+   gb_lower_count(n, A->i, A->j, cnt, s);
+   gb_exclusive_scan(cnt, Li, n, scr, s);
+   int lnnz = 0;
+   cudaMemcpyAsync(&lnnz, Li + n, sizeof(int), cudaMemcpyDeviceToHost, s);
+   gb_sync();
+   int *Lj = (int *) gb_dmalloc(sizeof(int) * (size_t) (lnnz ? lnnz : 1));
+   double *Lv = (double *) gb_dmalloc(sizeof(double) * (size_t) (lnnz ? lnnz : 1));
+   gb_lower_fill(n, A->i, A->j, vsrc, Li, Lj, Lv, s);
+   /* SELL-32 of the lower part */
+   f->lo_sl_w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
+   f->lo_sl_ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));
+   gb_sell_build(n, Li, Lj, Lv, vprec, nsl, f->lo_sl_w, f->lo_sl_ptr, NULL, NULL, s, 0);
+   long long tot = 0;
+   cudaMemcpyAsync(&tot, f->lo_sl_ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
+   gb_sync();
+   size_t vb = vprec == GB_PREC_F64 ? 8 : vprec == GB_PREC_F32 ? 4 : 2;
+   f->lo_sl_j = (int *) gb_dmalloc(sizeof(int) * (size_t) (tot ? tot : 1));
+   f->lo_sl_v = gb_dmalloc(vb * (size_t) (tot ? tot : 1));
+   gb_sell_build(n, Li, Lj, Lv, vprec, nsl, f->lo_sl_w, f->lo_sl_ptr, f->lo_sl_j, f->lo_sl_v, s, 1);
+   /* the diagonal in the vector precision (FP16 forms: unit diagonal) */
+   if (vprec != GB_PREC_F16)
+   {
+      f->lo_diag = gb_dmalloc((vprec == GB_PREC_F64 ? 8 : 4) * (size_t) n);
+      gb_diag_vals(n, A->i, A->v, vprec, f->lo_diag, s);
+   }
+   gb_sync();
+   gb_dfree(cnt); gb_dfree(Li); gb_dfree(scr); gb_dfree(Lj); gb_dfree(Lv); gb_dfree(scaled);
+   memset(&f->lo, 0, sizeof(f->lo));
+   f->lo.n = n;
+   f->lo.vprec = vprec;
+   f->lo.fmt = GB_FMT_SELL;
+   f->lo.nslices = nsl;
+   f->lo.sl_ptr = f->lo_sl_ptr; f->lo.sl_w = f->lo_sl_w; f->lo.sl_j = f->lo_sl_j; f->lo.sl_v = f->lo_sl_v;
+   f->lo.K = 8;
+   f->lo_valid = 1;
+   *diag = f->lo_diag;
+   return &f->lo;
 }
 
 void gb_matvec(double alpha, gb_parcsr *A, const double *x, double beta, double *y)

@@ -66,6 +66,16 @@ typedef struct
    int         *sl_j;
    void        *sl_v;
    float       *rs;        /* FP16 form: row scales a_ii */
+   /* strictly lower part as SELL-32 and the diagonal (in the vector
+    * precision; none for the unit-diagonal FP16 form), for two-stage
+    * Gauss-Seidel sweeps on large levels; lo_valid 1 built, -1 not used */
+   int          lo_valid;
+   gb_spmv_desc lo;
+   void        *lo_diag;
+   long long   *lo_sl_ptr;
+   int         *lo_sl_w;
+   int         *lo_sl_j;
+   void        *lo_sl_v;
 } gb_solveform;
 
 struct hypre_ParCSRMatrix_struct
@@ -96,6 +106,9 @@ gb_parcsr *gb_parcsr_wrap(gb_csr A, int owns);
 void       gb_parcsr_free(gb_parcsr *M);
 void       gb_csr_free(gb_csr *A);
 const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec);   /* builds lazily */
+/* strictly lower part of a large matrix for two-stage Gauss-Seidel (NULL for
+ * small or wide-row matrices: the CSR kernel is used there); builds lazily */
+const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag);
 gb_parvec *gb_parvec_new(int n);
 void       gb_parvec_free(gb_parvec *v);
 

@@ -19,6 +19,7 @@ extern "C" {
 #define GB_EPI_CHEB_RES 3
 #define GB_EPI_CHEB_STEP 4
 #define GB_EPI_CHEB_LAST 5
+#define GB_EPI_GS 6            /* y = s / d_i (s when d is NULL), b_i += alpha * y_i */
 #define GB_PREC_F64 0
 #define GB_PREC_F32 1
 #define GB_PREC_F16 2
@@ -140,6 +141,14 @@ void gb_row_scaled_vals(int n, const int *Ai, const double *Av, double *out, flo
 void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s);
 void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, const float *rs, float *v, float *u,
                    cudaStream_t s);
+/* strictly lower part (j < i) of a CSR matrix, diagonal entries, and the
+ * first stage of the two-stage Gauss-Seidel sweep with a diagonal array */
+void gb_lower_count(int n, const int *Ai, const int *Aj, int *cnt, cudaStream_t s);
+void gb_lower_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Li, int *Lj, double *Lv,
+                   cudaStream_t s);
+void gb_diag_vals(int n, const int *Ai, const double *Av, int vprec, void *out, cudaStream_t s);
+void gb_gs_first_diag_d(int n, const double *diag, double *v, double *u, cudaStream_t s);
+void gb_gs_first_diag_f(int n, const float *diag, float *v, float *u, cudaStream_t s);
 void gb_gs_lower_d(int n, const int *Ai, const int *Aj, const double *Av, const double *z, double *znew, double *u,
                    double m, cudaStream_t s);
 void gb_gs_lower_f(int n, const int *Ai, const int *Aj, const void *Av, int vprec, const float *z, float *znew,

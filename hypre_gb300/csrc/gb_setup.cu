@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(128) k_extpi_count(int nrows, const int *__res
                                                      const int *in_list, const int *in_n, int *ovf_list, int *ovf_n,
                                                      int *gtab, int gcap, int *err)
 {
-   extern __shared__ int sh[];
+   extern __shared__ __align__(16) int sh[];
    const int lane = gb_lane();
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill(int nrows, const int *__rest
                                                     const int *in_list, const int *in_n, int *gtab, int gcap,
                                                     int *err)
 {
-   extern __shared__ int sh[];
+   extern __shared__ __align__(16) int sh[];
    const int lane = gb_lane();
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -1153,7 +1153,7 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
                                                 double *__restrict__ Cv, int *ovf_list, int *ovf_n, int *out_list,
                                                 int *out_n, int *gtab, int gcap, int *err, const int *__restrict__ ub)
 {
-   extern __shared__ int sh[];
+   extern __shared__ __align__(16) int sh[];
    __shared__ double stage_all[128];
    const int lane = gb_lane();
    double *stage = stage_all + (threadIdx.x & ~31);
@@ -1490,7 +1490,7 @@ template <int MODE, bool NUMERIC> struct RcCfg
 };
 
 template <int MODE, bool NUMERIC>
-__global__ void __launch_bounds__(128) k_spgemm_rc(int nrows, int square, const int *__restrict__ Ai,
+__global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, const int *__restrict__ Ai,
                                                    const int *__restrict__ Aj, const double *__restrict__ Av,
                                                    const int *__restrict__ Bi, const int *__restrict__ Bj,
                                                    const double *__restrict__ Bv, int *__restrict__ cnt,

@@ -37,6 +37,7 @@ template <> struct Acc<__half, float>
 // Epilogue of a row: mode 0  y = alpha*s + beta*b
 //                    mode 1  y = x_i + w*(b_i - s)/d_i   (l1 / diagonal Jacobi)
 //                    mode 2  y = (b_i - s) for residuals   (alpha=-1, beta=1 shortcut)
+//                    mode 6  y = s/d_i, and b_i += alpha*y (two-stage Gauss-Seidel)
 template <typename XT>
 __device__ __forceinline__ XT row_epilogue(int mode, XT s, int i, XT alpha, XT beta, const XT *b, const XT *x,
                                            const XT *d, XT w, const XT *y)
@@ -47,6 +48,9 @@ __device__ __forceinline__ XT row_epilogue(int mode, XT s, int i, XT alpha, XT b
    if (mode == 3) { return d[i] * (b[i] - s); }
    if (mode == 4) { return d[i] * (alpha * b[i] + d[i] * s); }
    if (mode == 5) { return y[i] + d[i] * (alpha * b[i] + d[i] * s); }
+   // two-stage Gauss-Seidel inner sweep over the strictly lower part: the
+   // kernel also adds alpha * y_i to b_i
+   if (mode == 6) { return d ? s / d[i] : s; }
    XT r = alpha * s;
    if (beta != (XT) 0) { r += beta * b[i]; }
    return r;
@@ -108,6 +112,7 @@ __global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__
          if (rs) { si *= (XT) rs[i]; }
          XT yi = row_epilogue<XT>(mode, si, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
+         if (mode == GB_EPI_GS) { const_cast<XT *>(b)[i] += alpha * yi; }
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
    }
@@ -162,6 +167,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
          if (rs) { si *= (XT) rs[i]; }
          XT yi = row_epilogue<XT>(mode, si, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
+         if (mode == GB_EPI_GS) { const_cast<XT *>(b)[i] += alpha * yi; }
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
    }
@@ -431,6 +437,79 @@ __global__ void k_gs_first(int n, const int *__restrict__ Ai, const VT *__restri
    XT z = v[i] / diag;
    v[i] = z;
    u[i] += z;
+}
+
+// strictly lower part of each row (columns j < i, in row order)
+__global__ void k_lower_count(int n, const int *__restrict__ Ai, const int *__restrict__ Aj, int *__restrict__ cnt)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int c = 0;
+   for (int k = Ai[i]; k < Ai[i + 1]; k++) { c += Aj[k] < i; }
+   cnt[i] = c;
+}
+
+__global__ void k_lower_fill(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                             const double *__restrict__ Av, const int *__restrict__ Li, int *__restrict__ Lj,
+                             double *__restrict__ Lv)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int p = Li[i];
+   for (int k = Ai[i]; k < Ai[i + 1]; k++)
+   {
+      if (Aj[k] < i) { Lj[p] = Aj[k]; Lv[p] = Av[k]; p++; }
+   }
+}
+
+// a_ii (the first entry of row i; 1 for an empty row) in the given precision
+template <typename T>
+__global__ void k_diag_vals(int n, const int *__restrict__ Ai, const double *__restrict__ Av, T *__restrict__ out)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int b = Ai[i];
+   out[i] = (T) (Ai[i + 1] > b ? Av[b] : 1.0);
+}
+
+// first stage with a contiguous diagonal: z = v/d; v = z; u += z
+template <typename XT>
+__global__ void k_gs_first_diag(int n, const XT *__restrict__ diag, XT *__restrict__ v, XT *__restrict__ u)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   XT z = v[i] / diag[i];
+   v[i] = z;
+   u[i] += z;
+}
+
+extern "C" void gb_lower_count(int n, const int *Ai, const int *Aj, int *cnt, cudaStream_t s)
+{
+   if (n > 0) { k_lower_count<<<nblk(n, 256), 256, 0, s>>>(n, Ai, Aj, cnt); GB_COUNT(1); }
+}
+
+extern "C" void gb_lower_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Li, int *Lj,
+                              double *Lv, cudaStream_t s)
+{
+   if (n > 0) { k_lower_fill<<<nblk(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, Li, Lj, Lv); GB_COUNT(1); }
+}
+
+extern "C" void gb_diag_vals(int n, const int *Ai, const double *Av, int vprec, void *out, cudaStream_t s)
+{
+   if (n <= 0) { return; }
+   if (vprec == GB_PREC_F64) { k_diag_vals<double><<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, (double *) out); }
+   else { k_diag_vals<float><<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, (float *) out); }
+   GB_COUNT(1);
+}
+
+extern "C" void gb_gs_first_diag_d(int n, const double *diag, double *v, double *u, cudaStream_t s)
+{
+   if (n > 0) { k_gs_first_diag<double><<<nblk(n, 256), 256, 0, s>>>(n, diag, v, u); GB_COUNT(1); }
+}
+
+extern "C" void gb_gs_first_diag_f(int n, const float *diag, float *v, float *u, cudaStream_t s)
+{
+   if (n > 0) { k_gs_first_diag<float><<<nblk(n, 256), 256, 0, s>>>(n, diag, v, u); GB_COUNT(1); }
 }
 
 extern "C" void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s)
