@@ -115,6 +115,7 @@ void       gb_parvec_free(gb_parvec *v);
 /* y = alpha*A*x + beta*y on the library stream, FP64 */
 void gb_matvec(double alpha, gb_parcsr *A, const double *x, double beta, double *y);
 double gb_dot(long long n, const double *x, const double *y);     /* synchronises */
+double gb_axpy_dot(long long n, double a, const double *x, double *y, const double *z);   /* y += a x; (z, y) */
 
 /* --- BoomerAMG ----------------------------------------------------------- */
 typedef struct

@@ -231,13 +231,15 @@ static int fgmres_solve(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
          gb_parvec pin = wrap_vec(p[i - 1], n), zout = wrap_vec(pre[i - 1], n);
          apply_precond(k, A, &pin, &zout);
          gb_spmv_d(Ad, pre[i - 1], p[i], 0, 1.0, 0.0, NULL, NULL, 0.0, NULL, NULL, st);
+         /* modified Gram-Schmidt; each update of p[i] is fused with the
+          * next inner product (with p[j+1], or p[i]'s own norm at the end) */
+         double hj = gb_dot(n, p[0], p[i]);
          for (int j = 0; j < i; j++)
          {
-            double hj = gb_dot(n, p[j], p[i]);
             HH(j, i - 1) = hj;
-            gb_axpy_d(n, -hj, p[j], p[i], st);
+            hj = gb_axpy_dot(n, -hj, p[j], p[i], j + 1 < i ? p[j + 1] : p[i]);
          }
-         double t = sqrt(gb_dot(n, p[i], p[i]));
+         double t = sqrt(hj);
          HH(i, i - 1) = t;
          if (t != 0.0) { gb_scale_d(n, 1.0 / t, p[i], st); }
          for (int j = 1; j < i; j++)

@@ -112,7 +112,6 @@ __global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__
          if (rs) { si *= (XT) rs[i]; }
          XT yi = row_epilogue<XT>(mode, si, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
-         if (mode == GB_EPI_GS) { const_cast<XT *>(b)[i] += alpha * yi; }
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
    }
@@ -128,7 +127,8 @@ __global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__
 // sl_ptr[s] + 32k + t, so a warp's loads are fully coalesced (256 B values,
 // 128 B indices per instruction for FP64).  Padding: column 0, value 0.
 // ---------------------------------------------------------------------------
-template <typename VT, typename XT>
+// GS: the two-stage Gauss-Seidel epilogue (mode 6), which also updates b
+template <typename VT, typename XT, bool GS>
 __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const long long *__restrict__ sl_ptr,
                                                    const int *__restrict__ sl_w, const int *__restrict__ Sj,
                                                    const VT *__restrict__ Sv, const XT *__restrict__ x, XT *y,
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
          if (rs) { si *= (XT) rs[i]; }
          XT yi = row_epilogue<XT>(mode, si, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
-         if (mode == GB_EPI_GS) { const_cast<XT *>(b)[i] += alpha * yi; }
+         if (GS) { const_cast<XT *>(b)[i] += alpha * yi; }
          if (dotz) { dsum += (double) yi * (double) dotz[i]; }
       }
    }
@@ -287,8 +287,17 @@ static void spmv_dispatch(const gb_spmv_desc *A, const XT *x, XT *y, int mode, X
    {
       int nsl = A->nslices;
       int blocks = dpart ? GB_RED_BLOCKS : nblk((long long) nsl * 32, T);
-      k_spmv_sell<VT, XT><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, A->sl_j, (const VT *) A->sl_v, x, y,
-                                                 mode, alpha, beta, b, d, w, dotz, dpart, A->rs);
+      if (mode == GB_EPI_GS)
+      {
+         k_spmv_sell<VT, XT, true><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, A->sl_j, (const VT *) A->sl_v,
+                                                        x, y, mode, alpha, beta, b, d, w, dotz, dpart, A->rs);
+      }
+      else
+      {
+         k_spmv_sell<VT, XT, false><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, A->sl_j,
+                                                         (const VT *) A->sl_v, x, y, mode, alpha, beta, b, d, w, dotz,
+                                                         dpart, A->rs);
+      }
    }
    else
    {
@@ -612,6 +621,23 @@ __global__ void __launch_bounds__(256) k_dot_part(long long n, const double *__r
    if (threadIdx.x == 0) { part[blockIdx.x] = t; }
 }
 
+// y += a*x, then partial sums of z . y (z may be y): one pass for a
+// modified Gram-Schmidt step and the next inner product, with the grid,
+// loop order and reduction of k_dot_part (identical sums)
+__global__ void __launch_bounds__(256) k_axpy_dot_part(long long n, double a, const double *__restrict__ x, double *y,
+                                                       const double *z, double *__restrict__ part)
+{
+   double s = 0.0;
+   for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+   {
+      double yi = y[i] + a * x[i];
+      y[i] = yi;
+      s += z[i] * yi;
+   }
+   double t = block_sum<double>(s);
+   if (threadIdx.x == 0) { part[blockIdx.x] = t; }
+}
+
 __global__ void __launch_bounds__(256) k_dot2_part(long long n, const double *__restrict__ x,
                                                    const double *__restrict__ y, const double *__restrict__ z,
                                                    double *__restrict__ part)
@@ -720,6 +746,13 @@ extern "C" void gb_vmul_f(long long n, const float *a, const float *b, float *c,
 extern "C" void gb_dot_d(long long n, const double *x, const double *y, double *part, double *out, cudaStream_t s)
 {
    k_dot_part<<<GB_RED_BLOCKS, 256, 0, s>>>(n, x, y, part);
+   k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
+   GB_COUNT(2);
+}
+extern "C" void gb_axpy_dot_d(long long n, double a, const double *x, double *y, const double *z, double *part,
+                              double *out, cudaStream_t s)
+{
+   k_axpy_dot_part<<<GB_RED_BLOCKS, 256, 0, s>>>(n, a, x, y, z, part);
    k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
    GB_COUNT(2);
 }
