@@ -2,14 +2,17 @@
 on the 3-D 27-point Laplacian, 160^3 grid (4,096,000 unknowns, 109,215,352
 nonzeros), on one GB300 through libHYPRE_gb300's C ABI.
 
-One step = BoomerAMG setup + Krylov solve from x0 = 0 on a matrix and
-right-hand side already resident in HBM (`value`, seconds, lower is better).
+One step = the library matrix built from CSR arrays already resident in HBM
+(a device copy with the diagonal first; every solve-phase form of it is then
+derived inside the step), BoomerAMG setup and Krylov solve from x0 = 0
+(`value`, seconds, lower is better).
 `e2e` repeats the step through the public IJ interface from host buffers:
 IJ assembly of the matrix and right-hand side from pinned host memory, setup,
 solve and the read-back of x, all inside the timed region.
 
 Arms:
-  default            GPU path (FP64 setup, FP32 V-cycle inside FP64 PCG); the
+  default            GPU path (FP64 setup, FP32 or FP16-finest V-cycle inside
+                     FP64 FlexGMRES; `value` is the faster of the two); the
                      plain FP64 GPU path is timed alongside (`fp64_plain`)
   --impl reference   the reference algorithm on the host cores (the CPU
                      oracle restatement, all threads), on a bounded sample
@@ -181,10 +184,27 @@ def gpu_arm(args):
         L.HYPRE_FlexGMRESSetPrecond(kry, gb.fn_ptr("HYPRE_BoomerAMGSolve"), gb.fn_ptr("HYPRE_BoomerAMGSetup"), amg)
         return amg, kry
 
+    # device-resident CSR inputs: every timed step builds its matrix from them
+    # (a device copy with the diagonal first), so the setup derives every
+    # solve-phase form of the finest level inside the timed region
+    dI = torch.from_numpy(I).to(dev)
+    dJ = torch.from_numpy(J).to(dev)
+    dV = torch.from_numpy(V).to(dev)
+    torch.cuda.synchronize()
+    step_mats = {}
+
     def step(kry, amg):
+        Ak = C.c_void_p()
+        gb.check(L.HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(n, dI.data_ptr(), dJ.data_ptr(), dV.data_ptr(),
+                                                               C.byref(Ak)), "matrix")
         L.HYPRE_ParVectorSetConstantValues(xv, 0.0)
-        gb.check(L.HYPRE_ParCSRFlexGMRESSetup(kry, A, bv, xv), "setup")
-        gb.check(L.HYPRE_ParCSRFlexGMRESSolve(kry, A, bv, xv), "solve")
+        gb.check(L.HYPRE_ParCSRFlexGMRESSetup(kry, Ak, bv, xv), "setup")
+        gb.check(L.HYPRE_ParCSRFlexGMRESSolve(kry, Ak, bv, xv), "solve")
+        # the previous step's matrix: its hierarchy was freed by this setup
+        old = step_mats.get(kry.value)
+        if old is not None:
+            L.HYPRE_GB300_ParCSRMatrixDestroy(old)
+        step_mats[kry.value] = Ak
 
     def timed(fn, k, w):
         for _ in range(w):
@@ -236,6 +256,9 @@ def gpu_arm(args):
             solvers[label] = (amg, pcg)
         else:
             L.HYPRE_ParCSRFlexGMRESDestroy(pcg); L.HYPRE_BoomerAMGDestroy(amg)
+            m_o = step_mats.pop(pcg.value, None)
+            if m_o is not None:
+                L.HYPRE_GB300_ParCSRMatrixDestroy(m_o)
     # the reported mixed-precision path: the faster of the FP32 cycle and the
     # FP16-finest cycle, provided it reached the tolerance in FP64; the
     # end-to-end step below runs the same solver
@@ -246,6 +269,9 @@ def gpu_arm(args):
     keep = solvers.pop(mixed)
     for amg_o, pcg_o in solvers.values():
         L.HYPRE_ParCSRFlexGMRESDestroy(pcg_o); L.HYPRE_BoomerAMGDestroy(amg_o)
+        m_o = step_mats.pop(pcg_o.value, None)
+        if m_o is not None:
+            L.HYPRE_GB300_ParCSRMatrixDestroy(m_o)
 
     # ---- SpMV roofline on level 0 (FP64, CSR/SELL kernel), CUDA events on the library stream
     reps = 20
@@ -303,6 +329,11 @@ def gpu_arm(args):
         L.HYPRE_IJVectorDestroy(ijx); L.HYPRE_IJVectorDestroy(ijb); L.HYPRE_IJMatrixDestroy(ijA)
 
     e2e_dev, e2e_wall = (None, None) if args.no_e2e else timed(e2e_step, max(1, args.steps), 1)
+    if not args.no_e2e:
+        # the e2e setups released the kept solver's last resident-step hierarchy
+        m_k = step_mats.pop(keep[1].value, None)
+        if m_k is not None:
+            L.HYPRE_GB300_ParCSRMatrixDestroy(m_k)
     h2d = nnz * (4 + 8) + (n + 1) * 4 + 8 * n
     d2h = 8 * n
 
@@ -435,11 +466,20 @@ def suite_arm(args):
         bp.setup(A, off)
         bp.solve(bv, xv)      # autotunes the kernel shape
 
+        dI, dJ, dV = (torch.from_numpy(a).cuda() for a in (I, J, V))
+        mats = []
+
         def step():
-            bp.setup(A, off)
+            # the matrix built from device-resident CSR in every step, so the
+            # setup derives its solve-phase forms inside the step
+            Ak = gb.DeviceMatrix(dI, dJ, dV)
+            bp.setup(Ak, off)
             xv.set(np.zeros(n))
             L.HYPRE_GB300_ResetKernelLaunchCount()
             bp.solve(bv, xv)
+            if mats:
+                mats.pop().destroy()
+            mats.append(Ak)
 
         t, _ = _timed_steps(step, args.steps, args.warmup)
 
@@ -506,10 +546,17 @@ def suite_arm(args):
             k = gb.Krylov("fgmres", tol=1e-8, maxit=300, kdim=30, amg=amg)
             bv, xv = gb.IJVector(n, b), gb.IJVector(n, np.zeros(n))
 
+            dI, dJ, dV = (torch.from_numpy(a).cuda() for a in (I, J, V))
+            mats = []
+
             def step():
+                Ak = gb.DeviceMatrix(dI, dJ, dV)
                 xv.set(np.zeros(n))
-                k.setup(A, bv, xv)
-                k.solve(A, bv, xv)
+                k.setup(Ak, bv, xv)
+                k.solve(Ak, bv, xv)
+                if mats:
+                    mats.pop().destroy()
+                mats.append(Ak)
 
             t, _ = _timed_steps(step, args.steps, args.warmup)
             r = b - csr(I, J, V) @ xv.values()

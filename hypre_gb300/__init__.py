@@ -75,6 +75,7 @@ def _declare(L):
         "HYPRE_FlexGMRESGetFinalRelativeResidualNorm": [vp, P(f64)],
         "HYPRE_GB300_BoomerAMGGetLevelCSR": [vp, i32, i32, P(i32), P(i32), P(i32), vp, vp, vp],
         "HYPRE_GB300_ParCSRMatrixCopyToHostCSR": [vp, P(i32), P(i32), vp, vp, vp],
+        "HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR": [i32, vp, vp, vp, P(vp)],
         "HYPRE_ParCSRMatrixGetRow": [vp, i32, P(i32), P(P(i32)), P(P(f64))],
         "HYPRE_ParCSRMatrixRestoreRow": [vp, i32, P(i32), P(P(i32)), P(P(f64))],
         "HYPRE_GB300_BoomerAMGGetLevelCF": [vp, i32, vp], "HYPRE_GB300_BoomerAMGGetLevelL1": [vp, i32, vp],
@@ -213,6 +214,28 @@ class IJMatrix:
         if self.h:
             lib().HYPRE_IJMatrixDestroy(self.h)
             self.h = None
+
+
+class DeviceMatrix:
+    """ParCSR matrix built by the library from CSR arrays in device memory
+    (objects with ``data_ptr()``, e.g. CUDA tensors; int32 row pointers and
+    columns, float64 values).  The arrays are copied; the diagonal is moved to
+    the front of each row."""
+
+    def __init__(self, dI, dJ, dV):
+        L = lib()
+        self.n = int(dI.numel()) - 1
+        self.par = C.c_void_p()
+        check(L.HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(self.n, dI.data_ptr(), dJ.data_ptr(), dV.data_ptr(),
+                                                            C.byref(self.par)), "CreateFromDeviceCSR")
+
+    def csr(self):
+        return parcsr_to_host(self.par)
+
+    def destroy(self):
+        if self.par:
+            lib().HYPRE_GB300_ParCSRMatrixDestroy(self.par)
+            self.par = None
 
 
 class IJVector:

@@ -490,6 +490,32 @@ HYPRE_Int HYPRE_GB300_ParCSRMatrixCopyToHostCSR(HYPRE_ParCSRMatrix A, HYPRE_Int 
    return gb_error_flag;
 }
 
+/* A ParCSR matrix from CSR arrays in device memory (copied; the diagonal is
+ * moved to the front of each row, shifting the entries before it, as for
+ * host arrays). */
+HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(HYPRE_Int n, const HYPRE_Int *rowptr, const HYPRE_Int *colidx,
+                                                     const HYPRE_Real *values, HYPRE_ParCSRMatrix *Aout)
+{
+   if (n < 0) { gb_error_in_arg(1); return gb_error_flag; }
+   if (!rowptr || !colidx || !values) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!Aout) { gb_error_in_arg(5); return gb_error_flag; }
+   gb_runtime_init();
+   cudaStream_t s = gb_stream();
+   int nnz = 0;
+   cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int), cudaMemcpyDeviceToHost, s);
+   if (gb_sync()) { return gb_error_flag; }
+   gb_csr A;
+   A.nr = n; A.nc = n; A.nnz = nnz;
+   A.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   A.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (nnz ? nnz : 1));
+   A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
+   if (!A.i || !A.j || !A.v) { gb_dfree(A.i); gb_dfree(A.j); gb_dfree(A.v); *Aout = NULL; return gb_error_flag; }
+   cudaMemcpyAsync(A.i, rowptr, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToDevice, s);
+   gb_ij_gather(n, NULL, A.i, colidx, values, 0, A.j, A.v, s);
+   *Aout = gb_parcsr_wrap(A, 1);
+   return gb_error_flag;
+}
+
 HYPRE_Int HYPRE_GB300_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix A)
 {
    if (A && A->magic == GB_MAGIC_MAT) { gb_parcsr_free(A); }
@@ -521,6 +547,7 @@ struct hypre_IJMatrix_struct
    int       *st_cols;
    double    *st_vals;
    long long  st_len, st_cap;
+   int       *st_rowptr;      /* device: set when one put holds every row in order */
 };
 
 #define GB_MAGIC_IJM 0x494a4d31
@@ -594,8 +621,8 @@ static void ijm_free_stage(HYPRE_IJMatrix m)
    m->arena_len = m->arena_cap = 0;
    free(m->row_state); free(m->dev_off);
    m->row_state = NULL; m->dev_off = NULL;
-   gb_dfree(m->st_cols); gb_dfree(m->st_vals);
-   m->st_cols = NULL; m->st_vals = NULL;
+   gb_dfree(m->st_cols); gb_dfree(m->st_vals); gb_dfree(m->st_rowptr);
+   m->st_cols = NULL; m->st_vals = NULL; m->st_rowptr = NULL;
    m->st_len = m->st_cap = 0;
 }
 
@@ -714,6 +741,8 @@ static int ijm_migrate(HYPRE_IJMatrix m)
    }
    free(hc); free(hv);
    m->st_len = 0;
+   gb_dfree(m->st_rowptr);
+   m->st_rowptr = NULL;
    return 1;
 }
 
@@ -726,51 +755,55 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
                           const double *values)
 {
    if (nrows <= 0) { return 0; }
-   int *hstart = (int *) malloc(sizeof(int) * (size_t) (nrows + 1));
-   if (!hstart) { return 0; }
-   /* one pass: row offsets within the put, and every row valid, new and
-    * not repeated in this put (marked pending; unmarked on failure) */
+   /* sizes first, so the copies of the caller's buffers start before the row
+    * checks (they overlap when the buffers are pinned) */
    long long tot = 0;
-   int t = 0, ok = 1;
+   for (int t = 0; t < nrows; t++)
+   {
+      if (ncols[t] < 0) { return 0; }
+      tot += ncols[t];
+   }
+   if (tot < GB_IJ_DEVICE_MIN || tot > 0x7fffffffLL) { return 0; }
+   int *hstart = (int *) malloc(sizeof(int) * (size_t) (nrows + 1));
+   if (!hstart || !ijm_staging_reserve(m, m->st_len + tot)) { free(hstart); return 0; }
+   cudaStream_t s = gb_stream();
+   cudaMemcpyAsync(m->st_cols + m->st_len, cols, sizeof(int) * (size_t) tot, cudaMemcpyHostToDevice, s);
+   cudaMemcpyAsync(m->st_vals + m->st_len, values, sizeof(double) * (size_t) tot, cudaMemcpyHostToDevice, s);
+   /* row offsets within the put; every row valid, new and not repeated in
+    * this put (marked pending, unmarked on failure); whether the put is the
+    * whole matrix in row order (its offsets are then the CSR row pointers) */
+   int t = 0, ok = 1, inorder = m->st_len == 0 && nrows == m->nrows;
+   long long acc = 0;
    hstart[0] = 0;
    for (; t < nrows; t++)
    {
       int r = rows[t] - m->ilower;
-      int nc = ncols[t];
-      if (nc < 0 || r < 0 || r >= m->nrows || m->row_state[r] != 0 || m->row_len[r] != 0 || tot + nc > 0x7fffffffLL)
-      {
-         ok = 0;
-         break;
-      }
+      if (r < 0 || r >= m->nrows || m->row_state[r] != 0 || m->row_len[r] != 0) { ok = 0; break; }
       m->row_state[r] = GB_IJ_ROW_PENDING;
-      tot += nc;
-      hstart[t + 1] = (int) tot;
+      inorder &= r == t;
+      acc += ncols[t];
+      hstart[t + 1] = (int) acc;
    }
-   if (ok && tot < GB_IJ_DEVICE_MIN) { ok = 0; }
-   if (!ok)
+   int *dstart = NULL, *flags = NULL;
+   if (ok)
    {
-      for (int u = 0; u < t; u++) { m->row_state[rows[u] - m->ilower] = 0; }
-      free(hstart);
-      return 0;
+      dstart = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
+      flags = (int *) gb_dcalloc(sizeof(int));
+      ok = dstart && flags;
    }
-   int *dstart = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
-   int *flags = (int *) gb_dcalloc(sizeof(int));
-   if (!dstart || !flags || !ijm_staging_reserve(m, m->st_len + tot))
+   int f = 1;
+   if (ok)
    {
-      for (int u = 0; u < nrows; u++) { m->row_state[rows[u] - m->ilower] = 0; }
-      free(hstart); gb_dfree(dstart); gb_dfree(flags);
-      return 0;
+      cudaMemcpyAsync(dstart, hstart, sizeof(int) * (size_t) (nrows + 1), cudaMemcpyHostToDevice, s);
+      gb_ij_check(nrows, dstart, m->st_cols + m->st_len, m->jupper - m->jlower + 1, flags, s);
+      f = ij_read_int(flags);   /* also the point after which the caller's buffers are free */
    }
-   cudaStream_t s = gb_stream();
-   cudaMemcpyAsync(m->st_cols + m->st_len, cols, sizeof(int) * (size_t) tot, cudaMemcpyHostToDevice, s);
-   cudaMemcpyAsync(m->st_vals + m->st_len, values, sizeof(double) * (size_t) tot, cudaMemcpyHostToDevice, s);
-   cudaMemcpyAsync(dstart, hstart, sizeof(int) * (size_t) (nrows + 1), cudaMemcpyHostToDevice, s);
-   gb_ij_check(nrows, dstart, m->st_cols + m->st_len, m->jupper - m->jlower + 1, flags, s);
-   int f = ij_read_int(flags);   /* also the point after which the caller's buffers are free */
-   gb_dfree(dstart); gb_dfree(flags);
+   else { gb_sync(); }          /* the copies read the caller's buffers */
+   gb_dfree(flags);
    if (f != 0)
    {
-      for (int u = 0; u < nrows; u++) { m->row_state[rows[u] - m->ilower] = 0; }
+      for (int u = 0; u < (ok ? nrows : t); u++) { m->row_state[rows[u] - m->ilower] = 0; }
+      gb_dfree(dstart);
       free(hstart);
       return 0;
    }
@@ -782,6 +815,8 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
       m->row_state[r] = GB_IJ_ROW_DEVICE;
    }
    m->st_len += tot;
+   if (inorder) { m->st_rowptr = dstart; }
+   else { gb_dfree(dstart); }
    free(hstart);
    return 1;
 }
@@ -910,6 +945,24 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
    if (!m->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not initialized"); return gb_error_flag; }
    int n = m->nrows;
    cudaStream_t s = gb_stream();
+   if (m->st_rowptr)
+   {
+      /* one device put of every row in order: its offsets are the row
+       * pointers and the staged rows are gathered in place order */
+      int nnz = (int) m->st_len;
+      gb_csr A;
+      A.nr = n; A.nc = m->jupper - m->jlower + 1; A.nnz = nnz;
+      A.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      A.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (nnz ? nnz : 1));
+      A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
+      if (!A.i || !A.j || !A.v) { gb_dfree(A.i); gb_dfree(A.j); gb_dfree(A.v); return gb_error_flag; }
+      cudaMemcpyAsync(A.i, m->st_rowptr, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToDevice, s);
+      gb_ij_gather(n, NULL, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
+      if (m->par) { gb_parcsr_free(m->par); }
+      m->par = gb_parcsr_wrap(A, 1);
+      m->assembled = 1;
+      return gb_error_flag;
+   }
    /* row pointers; host-arena rows are packed behind the device-staged ones
     * (their offsets point past st_len into a temporary upload) */
    int *I = (int *) malloc(sizeof(int) * (size_t) (n + 1));

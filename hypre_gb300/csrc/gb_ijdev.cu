@@ -62,8 +62,9 @@ extern "C" void gb_ij_check(int nrows, const int *start, const int *cols, int nc
    GB_COUNT(1);
 }
 
-// one warp per row r: staged entries off[r] .. off[r]+len (len = I[r+1]-I[r])
-// -> J, V at I[r], diagonal first (shift, or swap when swap_diag)
+// one warp per row r: staged entries off[r] .. off[r]+len (len = I[r+1]-I[r];
+// off NULL: the staging is in row order, off[r] = I[r]) -> J, V at I[r],
+// diagonal first (shift, or swap when swap_diag)
 __global__ void k_ij_gather(int n, const long long *__restrict__ off, const int *__restrict__ I,
                             const int *__restrict__ scols, const double *__restrict__ svals, int swap_diag,
                             int *__restrict__ J, double *__restrict__ V)
@@ -72,7 +73,7 @@ __global__ void k_ij_gather(int n, const long long *__restrict__ off, const int 
    const int lane = threadIdx.x & 31;
    if (r >= n) { return; }
    const int d = I[r], l = I[r + 1] - d;
-   const long long o = off[r];
+   const long long o = off ? off[r] : (long long) d;
    // first position of the diagonal
    int dpos = -1;
    for (int c = 0; c < l && dpos < 0; c += 32)

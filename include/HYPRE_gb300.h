@@ -364,6 +364,11 @@ HYPRE_Int HYPRE_GB300_ParVectorCopyToHost(HYPRE_ParVector v, HYPRE_Real *h, HYPR
 HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(HYPRE_Int n, const HYPRE_Int *rowptr,
                                                     const HYPRE_Int *colidx, const HYPRE_Real *values,
                                                     HYPRE_ParCSRMatrix *A);
+/* The same from CSR arrays in device memory (copied by the library; the
+ * caller keeps its arrays). */
+HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(HYPRE_Int n, const HYPRE_Int *rowptr,
+                                                      const HYPRE_Int *colidx, const HYPRE_Real *values,
+                                                      HYPRE_ParCSRMatrix *A);
 HYPRE_Int HYPRE_GB300_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix A);
 /* The local CSR arrays copied to host memory (any array may be NULL).  No
  * counterpart in the reference (whose matrices are host-addressable). */

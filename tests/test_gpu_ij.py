@@ -236,3 +236,55 @@ def test_ij_vector_puts_and_gets(gb):
     np.testing.assert_array_equal(out, exp)
     assert L.HYPRE_GetError() == 0
     L.HYPRE_IJVectorDestroy(v)
+
+
+def test_two_large_puts_in_permuted_row_order(gb):
+    # rows staged on the device by two puts, not in row order: the general
+    # assembly (per-row offsets) instead of the single in-order put's
+    rows = random_rows(8000, seed=13)
+    exp = expected_csr(rows)
+    L = gb.lib()
+    n = len(rows)
+    h = C.c_void_p()
+    L.HYPRE_IJMatrixCreate(0, 0, n - 1, 0, n - 1, C.byref(h))
+    L.HYPRE_IJMatrixSetObjectType(h, gb.HYPRE_PARCSR)
+    L.HYPRE_IJMatrixInitialize(h)
+    perm = np.random.default_rng(14).permutation(n).astype(np.int32)
+    for part in (perm[: n // 2], perm[n // 2:]):
+        nc = np.array([len(rows[r][0]) for r in part], np.int32)
+        J = np.array([c for r in part for c in rows[r][0]], np.int32)
+        V = np.array([v for r in part for v in rows[r][1]], np.float64)
+        assert len(J) >= 65536
+        L.HYPRE_IJMatrixSetValues(h, len(part), nc.ctypes.data, part.ctypes.data, J.ctypes.data, V.ctypes.data)
+    gb.check(L.HYPRE_IJMatrixAssemble(h), "assemble")
+    par = C.c_void_p()
+    L.HYPRE_IJMatrixGetObject(h, C.byref(par))
+    same(gb.parcsr_to_host(par), exp)
+    L.HYPRE_IJMatrixDestroy(h)
+    assert L.HYPRE_GetError() == 0
+
+
+def test_matrix_from_device_csr_matches_host_csr(gb):
+    torch = pytest.importorskip("torch")
+    rows = random_rows(3000, seed=15)
+    I = np.zeros(len(rows) + 1, np.int32)
+    I[1:] = np.cumsum([len(c) for c, _ in rows])
+    J = np.array([c for cs, _ in rows for c in cs], np.int32)
+    V = np.array([v for _, vs in rows for v in vs], np.float64)
+    L = gb.lib()
+    n = len(rows)
+    Ah = C.c_void_p()
+    gb.check(L.HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(n, I.ctypes.data, J.ctypes.data, V.ctypes.data,
+                                                         C.byref(Ah)), "host csr")
+    dI = torch.from_numpy(I).cuda()
+    dJ = torch.from_numpy(J).cuda()
+    dV = torch.from_numpy(V).cuda()
+    torch.cuda.synchronize()
+    Ad = C.c_void_p()
+    gb.check(L.HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(n, dI.data_ptr(), dJ.data_ptr(), dV.data_ptr(),
+                                                           C.byref(Ad)), "device csr")
+    same(gb.parcsr_to_host(Ad), gb.parcsr_to_host(Ah))
+    # the diagonal moved first with the entries before it shifted
+    same(gb.parcsr_to_host(Ad), expected_csr(rows))
+    L.HYPRE_GB300_ParCSRMatrixDestroy(Ad)
+    L.HYPRE_GB300_ParCSRMatrixDestroy(Ah)
