@@ -25,16 +25,23 @@ gb_parcsr *gb_parcsr_wrap(gb_csr A, int owns)
 
 static void solveform_free(gb_solveform *f)
 {
-   gb_dfree(f->vals); gb_dfree(f->sl_ptr); gb_dfree(f->sl_w); gb_dfree(f->sl_j); gb_dfree(f->sl_v);
-   gb_dfree(f->rs);
-   gb_dfree(f->lo_diag); gb_dfree(f->lo_sl_ptr); gb_dfree(f->lo_sl_w); gb_dfree(f->lo_sl_j); gb_dfree(f->lo_sl_v);
+   gb_dfree(f->vals); gb_dfree(f->sl_v); gb_dfree(f->rs);
+   gb_dfree(f->lo_diag); gb_dfree(f->lo_sl_v);
    memset(f, 0, sizeof(*f));
+}
+
+static void sellstruct_free(gb_sellstruct *S)
+{
+   gb_dfree(S->w); gb_dfree(S->ptr); gb_dfree(S->j);
+   memset(S, 0, sizeof(*S));
 }
 
 void gb_parcsr_free(gb_parcsr *M)
 {
    if (!M) { return; }
    for (int p = 0; p < 3; p++) { solveform_free(&M->sf[p]); }
+   sellstruct_free(&M->sell);
+   sellstruct_free(&M->lsell);
    if (M->owns) { gb_csr_free(&M->A); }
    gb_dfree(M->diag);
    free(M->row_cols); free(M->row_vals);
@@ -53,6 +60,38 @@ static int lanes_for(double avg)
    return 2;
 }
 
+/* SELL-32 structure of M's rows (lower = 0: used when rows are short and
+ * near uniform, n >= 4096, 4 <= nnz/row <= 40, padding <= 15%) or of their
+ * strictly lower parts (lower = 1: levels of >= 65,536 rows); built once and
+ * shared by the forms of every precision.  1 when usable. */
+static int sell_struct(gb_parcsr *M, int lower)
+{
+   gb_sellstruct *S = lower ? &M->lsell : &M->sell;
+   if (S->state) { return S->state > 0; }
+   gb_csr *A = &M->A;
+   double avg = A->nr ? (double) A->nnz / A->nr : 0;
+   int nsl = (A->nr + 31) / 32;
+   int ok = lower ? (A->nr >= 65536 && avg <= 40 && nsl <= 1024 * 1024)
+                  : (A->nr >= 4096 && avg <= 40 && avg >= 4 && nsl <= 1024 * 1024);
+   if (!ok) { S->state = -1; return 0; }
+   cudaStream_t s = gb_stream();
+   S->nslices = nsl;
+   S->w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
+   S->ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));
+   if (!S->w || !S->ptr) { sellstruct_free(S); S->state = -1; return 0; }
+   gb_sell_struct(A->nr, A->i, A->j, lower, nsl, S->w, S->ptr, NULL, s, 0);
+   cudaMemcpyAsync(&S->tot, S->ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
+   gb_sync();
+   if (!lower && (double) S->tot > 1.15 * (double) A->nnz) { sellstruct_free(S); S->state = -1; return 0; }
+   S->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (S->tot ? S->tot : 1));
+   if (!S->j) { sellstruct_free(S); S->state = -1; return 0; }
+   gb_sell_struct(A->nr, A->i, A->j, lower, nsl, S->w, S->ptr, S->j, s, 1);
+   S->state = 1;
+   return 1;
+}
+
+static size_t vbytes(int vprec) { return vprec == GB_PREC_F64 ? 8 : vprec == GB_PREC_F32 ? 4 : 2; }
+
 const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
 {
    gb_solveform *f = &M->sf[vprec];
@@ -69,55 +108,32 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
    f->desc.K = lanes_for(avg);
    /* FP16 forms hold row-scaled values a_ij / a_ii (unit diagonal) with the
     * diagonal kept in FP32, so coefficients of any magnitude stay in range */
-   const double *vsrc = A->v;
-   double *scaled = NULL;
-   if (vprec == GB_PREC_F16)
-   {
-      scaled = (double *) gb_dmalloc(sizeof(double) * (size_t) (A->nnz ? A->nnz : 1));
-      f->rs = (float *) gb_dmalloc(sizeof(float) * (size_t) (A->nr ? A->nr : 1));
-      gb_row_scaled_vals(A->nr, A->i, A->v, scaled, f->rs, s);
-      vsrc = scaled;
-      f->desc.rs = f->rs;
-   }
-   /* SELL-32 when rows are short and nearly uniform (little padding) */
-   int use_sell = 0;
-   int nsl = (A->nr + 31) / 32;
-   int *sl_w = NULL;
-   long long *sl_ptr = NULL;
-   if (A->nr >= 4096 && avg <= 40 && avg >= 4 && nsl <= 1024 * 1024)
-   {
-      sl_w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
-      sl_ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));
-      gb_sell_build(A->nr, A->i, A->j, vsrc, vprec, nsl, sl_w, sl_ptr, NULL, NULL, s, 0);
-      long long tot = 0;
-      cudaMemcpyAsync(&tot, sl_ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
-      gb_sync();
-      if ((double) tot <= 1.15 * (double) A->nnz) { use_sell = 1; }
-      else { gb_dfree(sl_w); gb_dfree(sl_ptr); sl_w = NULL; sl_ptr = NULL; }
-      if (use_sell)
-      {
-         size_t vb = vprec == GB_PREC_F64 ? 8 : vprec == GB_PREC_F32 ? 4 : 2;
-         int *sl_j = (int *) gb_dmalloc(sizeof(int) * (size_t) tot);
-         void *sl_v = gb_dmalloc(vb * (size_t) tot);
-         gb_sell_build(A->nr, A->i, A->j, vsrc, vprec, nsl, sl_w, sl_ptr, sl_j, sl_v, s, 1);
-         f->sl_ptr = sl_ptr; f->sl_w = sl_w; f->sl_j = sl_j; f->sl_v = sl_v;
-         f->desc.fmt = GB_FMT_SELL;
-         f->desc.nslices = nsl;
-         f->desc.sl_ptr = sl_ptr; f->desc.sl_w = sl_w; f->desc.sl_j = sl_j; f->desc.sl_v = sl_v;
-      }
-   }
-   /* CSR values in the requested precision (the two-stage Gauss-Seidel
-    * kernels and the CSR path read them) */
+   const int scaled = vprec == GB_PREC_F16;
+   /* CSR values in the requested precision (the CSR SpMV and the small-level
+    * Gauss-Seidel kernels read them; FP16: also the row scales) */
    if (vprec == GB_PREC_F64) { f->desc.v = A->v; }
    else
    {
-      size_t vb = vprec == GB_PREC_F32 ? 4 : 2;
-      f->vals = gb_dmalloc(vb * (size_t) (A->nnz ? A->nnz : 1));
-      gb_convert_vals(A->nnz, vsrc, f->vals, vprec, s);
+      f->vals = gb_dmalloc(vbytes(vprec) * (size_t) (A->nnz ? A->nnz : 1));
+      if (scaled)
+      {
+         f->rs = (float *) gb_dmalloc(sizeof(float) * (size_t) (A->nr ? A->nr : 1));
+         gb_row_scaled_half(A->nr, A->i, A->v, f->vals, f->rs, s);
+         f->desc.rs = f->rs;
+      }
+      else { gb_convert_vals(A->nnz, A->v, f->vals, vprec, s); }
       f->desc.v = f->vals;
    }
-   if (scaled) { gb_sync(); gb_dfree(scaled); }
-   if (!use_sell) { f->desc.fmt = GB_FMT_CSR; }
+   /* SELL-32 values on the shared structure */
+   f->desc.fmt = GB_FMT_CSR;
+   if (sell_struct(M, 0))
+   {
+      f->sl_v = gb_dmalloc(vbytes(vprec) * (size_t) (M->sell.tot ? M->sell.tot : 1));
+      gb_sell_vals(A->nr, A->i, A->j, A->v, 0, scaled, vprec, M->sell.nslices, M->sell.w, M->sell.ptr, f->sl_v, s);
+      f->desc.fmt = GB_FMT_SELL;
+      f->desc.nslices = M->sell.nslices;
+      f->desc.sl_ptr = M->sell.ptr; f->desc.sl_w = M->sell.w; f->desc.sl_j = M->sell.j; f->desc.sl_v = f->sl_v;
+   }
    f->valid = 1;
    return &f->desc;
 }
@@ -127,59 +143,25 @@ const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag)
    gb_solveform *f = &M->sf[vprec];
    if (!f->valid) { gb_solve_desc(M, vprec); }
    if (f->lo_valid) { *diag = f->lo_diag; return f->lo_valid > 0 ? &f->lo : NULL; }
-   gb_csr *A = &M->A;
-   double avg = A->nr ? (double) A->nnz / A->nr : 0;
-   int nsl = (A->nr + 31) / 32;
-   if (A->nr < 65536 || avg > 40 || nsl > 1024 * 1024) { f->lo_valid = -1; *diag = NULL; return NULL; }
+   if (!sell_struct(M, 1)) { f->lo_valid = -1; *diag = NULL; return NULL; }
    cudaStream_t s = gb_stream();
+   gb_csr *A = &M->A;
    int n = A->nr;
-   /* the values of this precision's form in FP64: row-scaled for FP16 */
-   const double *vsrc = A->v;
-   double *scaled = NULL;
-   if (vprec == GB_PREC_F16)
-   {
-      scaled = (double *) gb_dmalloc(sizeof(double) * (size_t) (A->nnz ? A->nnz : 1));
-      float *rs_tmp = (float *) gb_dmalloc(sizeof(float) * (size_t) n);
-      gb_row_scaled_vals(n, A->i, A->v, scaled, rs_tmp, s);
-      gb_dfree(rs_tmp);
-      vsrc = scaled;
-   }
-   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   int *Li = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   int *scr = (int *) gb_dmalloc(sizeof(int) * (size_t) gb_scan_scratch_ints(n));
-   gb_lower_count(n, A->i, A->j, cnt, s);
-   gb_exclusive_scan(cnt, Li, n, scr, s);
-   int lnnz = 0;
-   cudaMemcpyAsync(&lnnz, Li + n, sizeof(int), cudaMemcpyDeviceToHost, s);
-   gb_sync();
-   int *Lj = (int *) gb_dmalloc(sizeof(int) * (size_t) (lnnz ? lnnz : 1));
-   double *Lv = (double *) gb_dmalloc(sizeof(double) * (size_t) (lnnz ? lnnz : 1));
-   gb_lower_fill(n, A->i, A->j, vsrc, Li, Lj, Lv, s);
-   /* SELL-32 of the lower part */
-   f->lo_sl_w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
-   f->lo_sl_ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));
-   gb_sell_build(n, Li, Lj, Lv, vprec, nsl, f->lo_sl_w, f->lo_sl_ptr, NULL, NULL, s, 0);
-   long long tot = 0;
-   cudaMemcpyAsync(&tot, f->lo_sl_ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
-   gb_sync();
-   size_t vb = vprec == GB_PREC_F64 ? 8 : vprec == GB_PREC_F32 ? 4 : 2;
-   f->lo_sl_j = (int *) gb_dmalloc(sizeof(int) * (size_t) (tot ? tot : 1));
-   f->lo_sl_v = gb_dmalloc(vb * (size_t) (tot ? tot : 1));
-   gb_sell_build(n, Li, Lj, Lv, vprec, nsl, f->lo_sl_w, f->lo_sl_ptr, f->lo_sl_j, f->lo_sl_v, s, 1);
+   f->lo_sl_v = gb_dmalloc(vbytes(vprec) * (size_t) (M->lsell.tot ? M->lsell.tot : 1));
+   gb_sell_vals(n, A->i, A->j, A->v, 1, vprec == GB_PREC_F16, vprec, M->lsell.nslices, M->lsell.w, M->lsell.ptr,
+                f->lo_sl_v, s);
    /* the diagonal in the vector precision (FP16 forms: unit diagonal) */
    if (vprec != GB_PREC_F16)
    {
       f->lo_diag = gb_dmalloc((vprec == GB_PREC_F64 ? 8 : 4) * (size_t) n);
       gb_diag_vals(n, A->i, A->v, vprec, f->lo_diag, s);
    }
-   gb_sync();
-   gb_dfree(cnt); gb_dfree(Li); gb_dfree(scr); gb_dfree(Lj); gb_dfree(Lv); gb_dfree(scaled);
    memset(&f->lo, 0, sizeof(f->lo));
    f->lo.n = n;
    f->lo.vprec = vprec;
    f->lo.fmt = GB_FMT_SELL;
-   f->lo.nslices = nsl;
-   f->lo.sl_ptr = f->lo_sl_ptr; f->lo.sl_w = f->lo_sl_w; f->lo.sl_j = f->lo_sl_j; f->lo.sl_v = f->lo_sl_v;
+   f->lo.nslices = M->lsell.nslices;
+   f->lo.sl_ptr = M->lsell.ptr; f->lo.sl_w = M->lsell.w; f->lo.sl_j = M->lsell.j; f->lo.sl_v = f->lo_sl_v;
    f->lo.K = 8;
    f->lo_valid = 1;
    *diag = f->lo_diag;

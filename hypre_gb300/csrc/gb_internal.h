@@ -54,17 +54,27 @@ typedef struct
    double *v;            /* device, FP64 */
 } gb_csr;
 
+/* SELL-32 structure of a matrix (whole rows, or their strictly lower parts):
+ * slice widths and offsets and column indices, shared by the solve forms of
+ * every precision; state 1 built, -1 not used, 0 not tried */
+typedef struct
+{
+   int        state;
+   int        nslices;
+   long long  tot;
+   int       *w;
+   long long *ptr;
+   int       *j;
+} gb_sellstruct;
+
 /* cached solve-phase form of a matrix in one precision */
 typedef struct
 {
    int          valid;
    int          vprec;
    gb_spmv_desc desc;
-   void        *vals;      /* CSR values in vprec (NULL when vprec == F64 and CSR) */
-   long long   *sl_ptr;
-   int         *sl_w;
-   int         *sl_j;
-   void        *sl_v;
+   void        *vals;      /* CSR values in vprec (NULL when vprec == F64) */
+   void        *sl_v;      /* SELL values in vprec */
    float       *rs;        /* FP16 form: row scales a_ii */
    /* strictly lower part as SELL-32 and the diagonal (in the vector
     * precision; none for the unit-diagonal FP16 form), for two-stage
@@ -72,9 +82,6 @@ typedef struct
    int          lo_valid;
    gb_spmv_desc lo;
    void        *lo_diag;
-   long long   *lo_sl_ptr;
-   int         *lo_sl_w;
-   int         *lo_sl_j;
    void        *lo_sl_v;
 } gb_solveform;
 
@@ -84,6 +91,8 @@ struct hypre_ParCSRMatrix_struct
    gb_csr       A;
    int          owns;
    gb_solveform sf[3];     /* per precision (GB_PREC_*) */
+   gb_sellstruct sell;     /* SELL-32 structure of the rows */
+   gb_sellstruct lsell;    /* ... of the strictly lower parts */
    double      *diag;      /* device, for diagonal scaling (lazy) */
    int          row_active;          /* GetRow .. RestoreRow */
    int         *row_cols;            /* host copy of the active row */

@@ -134,18 +134,17 @@ void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int mode, doub
                const double *b, const double *d, double w, const double *dotz, double *dpart, cudaStream_t st);
 void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int mode, float alpha, float beta, const float *b,
                const float *d, float w, const float *dotz, double *dpart, cudaStream_t st);
-void gb_sell_build(int n, const int *Ai, const int *Aj, const double *Av, int vprec, int nslices, int *sl_w,
-                   long long *sl_ptr, int *sl_j, void *sl_v, cudaStream_t s, int stage);
+void gb_sell_struct(int n, const int *Ai, const int *Aj, int lower, int nslices, int *sl_w, long long *sl_ptr,
+                    int *sl_j, cudaStream_t s, int stage);
+void gb_sell_vals(int n, const int *Ai, const int *Aj, const double *Av, int lower, int scaled, int vprec, int nslices,
+                  const int *sl_w, const long long *sl_ptr, void *sl_v, cudaStream_t s);
 void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s);
-void gb_row_scaled_vals(int n, const int *Ai, const double *Av, double *out, float *rs, cudaStream_t s);
+void gb_row_scaled_half(int n, const int *Ai, const double *Av, void *out, float *rs, cudaStream_t s);
 void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s);
 void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, const float *rs, float *v, float *u,
                    cudaStream_t s);
-/* strictly lower part (j < i) of a CSR matrix, diagonal entries, and the
- * first stage of the two-stage Gauss-Seidel sweep with a diagonal array */
-void gb_lower_count(int n, const int *Ai, const int *Aj, int *cnt, cudaStream_t s);
-void gb_lower_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Li, int *Lj, double *Lv,
-                   cudaStream_t s);
+/* diagonal entries, and the first stage of the two-stage Gauss-Seidel sweep
+ * with a diagonal array */
 void gb_diag_vals(int n, const int *Ai, const double *Av, int vprec, void *out, cudaStream_t s);
 void gb_gs_first_diag_d(int n, const double *diag, double *v, double *u, cudaStream_t s);
 void gb_gs_first_diag_f(int n, const float *diag, float *v, float *u, cudaStream_t s);

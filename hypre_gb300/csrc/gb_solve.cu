@@ -178,18 +178,25 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
    }
 }
 
-// SELL-32 construction: slice widths, then fill (values converted to VT).
-__global__ void k_sell_width(int n, int nslices, const int *__restrict__ Ai, int *__restrict__ w)
+// SELL-32 construction: slice widths (the longest row of each slice of 32
+// rows; lower: only the entries j < i), offsets, then column indices and
+// values (values converted to VT, optionally divided by the row's first
+// entry for the row-scaled FP16 forms).  One warp per slice, one lane per row.
+__global__ void k_sell_width(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj, int lower,
+                             int *__restrict__ w)
 {
-   int s = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const int s = i >> 5;
    if (s >= nslices) { return; }
-   int m = 0;
-   for (int t = 0; t < 32; t++)
+   int l = 0;
+   if (i < n)
    {
-      int i = s * 32 + t;
-      if (i < n) { int l = Ai[i + 1] - Ai[i]; m = l > m ? l : m; }
+      const int b = Ai[i], e = Ai[i + 1];
+      if (!lower) { l = e - b; }
+      else { for (int k = b; k < e; k++) { l += Aj[k] < i; } }
    }
-   w[s] = m;
+   for (int o = 16; o > 0; o >>= 1) { l = max(l, __shfl_xor_sync(GB_FULL, l, o)); }
+   if ((i & 31) == 0) { w[s] = l; }
 }
 
 // slice offsets: block-level scans of width*32 (int64), then block offsets
@@ -231,24 +238,58 @@ __global__ void k_sell_ptr_fix(int nslices, long long *__restrict__ ptr, const l
    for (int s = threadIdx.x; s < nslices; s += blockDim.x) { ptr[s] += off[s / 1024]; }
 }
 
-template <typename VT>
-__global__ void k_sell_fill(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj,
-                            const double *__restrict__ Av, const long long *__restrict__ ptr,
-                            const int *__restrict__ w, int *__restrict__ Sj, VT *__restrict__ Sv)
+__global__ void k_sell_fill_j(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                              const long long *__restrict__ ptr, const int *__restrict__ w, int lower,
+                              int *__restrict__ Sj)
 {
-   int i = blockIdx.x * blockDim.x + threadIdx.x;
-   int s = i >> 5, t = i & 31;
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const int s = i >> 5;
    if (s >= nslices) { return; }
-   int width = w[s];
-   long long base = ptr[s] + t;
-   int b = 0, e = 0;
-   if (i < n) { b = Ai[i]; e = Ai[i + 1]; }
-   for (int k = 0; k < width; k++)
+   const int width = w[s];
+   const long long base = ptr[s] + (i & 31);
+   int k = 0;
+   if (i < n)
    {
-      long long p = base + (long long) k * 32;
-      if (b + k < e) { Sj[p] = Aj[b + k]; Sv[p] = (VT) Av[b + k]; }
-      else { Sj[p] = i < n ? i : 0; Sv[p] = (VT) 0.0; }
+      for (int q = Ai[i]; q < Ai[i + 1]; q++)
+      {
+         const int j = Aj[q];
+         if (!lower || j < i) { Sj[base + (long long) k * 32] = j; k++; }
+      }
    }
+   // padding: the row's own index (a valid column) with value 0
+   for (; k < width; k++) { Sj[base + (long long) k * 32] = i < n ? i : 0; }
+}
+
+template <typename VT>
+__global__ void k_sell_fill_v(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                              const double *__restrict__ Av, const long long *__restrict__ ptr,
+                              const int *__restrict__ w, int lower, int scaled, VT *__restrict__ Sv)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const int s = i >> 5;
+   if (s >= nslices) { return; }
+   const int width = w[s];
+   const long long base = ptr[s] + (i & 31);
+   int k = 0;
+   if (i < n)
+   {
+      const int b = Ai[i], e = Ai[i + 1];
+      double d = 1.0;
+      if (scaled)
+      {
+         d = e > b ? Av[b] : 1.0;
+         if (d == 0.0) { d = 1.0; }
+      }
+      for (int q = b; q < e; q++)
+      {
+         if (!lower || Aj[q] < i)
+         {
+            Sv[base + (long long) k * 32] = (VT) (scaled ? Av[q] / d : Av[q]);
+            k++;
+         }
+      }
+   }
+   for (; k < width; k++) { Sv[base + (long long) k * 32] = (VT) 0.0; }
 }
 
 template <typename VT>
@@ -339,14 +380,15 @@ extern "C" void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int m
    }
 }
 
-extern "C" void gb_sell_build(int n, const int *Ai, const int *Aj, const double *Av, int vprec, int nslices,
-                              int *sl_w, long long *sl_ptr, int *sl_j, void *sl_v, cudaStream_t s, int stage)
+extern "C" void gb_sell_struct(int n, const int *Ai, const int *Aj, int lower, int nslices, int *sl_w,
+                               long long *sl_ptr, int *sl_j, cudaStream_t s, int stage)
 {
    // stage 0: widths + offsets (caller then reads sl_ptr[nslices] to size
-   // the arrays); stage 1: fill
+   // the arrays); stage 1: column indices
+   const long long nt = (long long) nslices * 32;
    if (stage == 0)
    {
-      k_sell_width<<<nblk(nslices, 256), 256, 0, s>>>(n, nslices, Ai, sl_w);
+      k_sell_width<<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, lower, sl_w);
       int nb = nblk(nslices, 1024);
       long long *bsum = NULL;
       cudaMallocAsync((void **) &bsum, sizeof(long long) * (size_t) nb, s);
@@ -356,26 +398,37 @@ extern "C" void gb_sell_build(int n, const int *Ai, const int *Aj, const double 
       GB_COUNT(3);
       return;
    }
-   long long nt = (long long) nslices * 32;
+   k_sell_fill_j<<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, sl_ptr, sl_w, lower, sl_j);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_sell_vals(int n, const int *Ai, const int *Aj, const double *Av, int lower, int scaled, int vprec,
+                             int nslices, const int *sl_w, const long long *sl_ptr, void *sl_v, cudaStream_t s)
+{
+   const long long nt = (long long) nslices * 32;
    if (vprec == GB_PREC_F64)
    {
-      k_sell_fill<double><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, sl_j, (double *) sl_v);
+      k_sell_fill_v<double><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, lower, scaled,
+                                                          (double *) sl_v);
    }
    else if (vprec == GB_PREC_F32)
    {
-      k_sell_fill<float><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, sl_j, (float *) sl_v);
+      k_sell_fill_v<float><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, lower, scaled,
+                                                         (float *) sl_v);
    }
    else
    {
-      k_sell_fill<__half><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, sl_j, (__half *) sl_v);
+      k_sell_fill_v<__half><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, Av, sl_ptr, sl_w, lower, scaled,
+                                                          (__half *) sl_v);
    }
    GB_COUNT(1);
 }
 
-// out = a_ij / a_ii row by row (the diagonal is each row's first entry),
-// rs[i] = a_ii: the FP16 forms store these so their range stays near 1
-__global__ void k_row_scaled(int n, const int *__restrict__ Ai, const double *__restrict__ Av,
-                             double *__restrict__ out, float *__restrict__ rs)
+// FP16 CSR values a_ij / a_ii row by row (the diagonal is each row's first
+// entry; 1 for an empty row or a zero diagonal) and rs[i] = a_ii: the FP16
+// forms store these so their range stays near 1
+__global__ void k_row_scaled_half(int n, const int *__restrict__ Ai, const double *__restrict__ Av,
+                                  __half *__restrict__ out, float *__restrict__ rs)
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i >= n) { return; }
@@ -383,12 +436,12 @@ __global__ void k_row_scaled(int n, const int *__restrict__ Ai, const double *__
    double d = e > b ? Av[b] : 1.0;
    if (d == 0.0) { d = 1.0; }
    rs[i] = (float) d;
-   for (int k = b; k < e; k++) { out[k] = Av[k] / d; }
+   for (int k = b; k < e; k++) { out[k] = (__half) (Av[k] / d); }
 }
 
-extern "C" void gb_row_scaled_vals(int n, const int *Ai, const double *Av, double *out, float *rs, cudaStream_t s)
+extern "C" void gb_row_scaled_half(int n, const int *Ai, const double *Av, void *out, float *rs, cudaStream_t s)
 {
-   if (n > 0) { k_row_scaled<<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, out, rs); GB_COUNT(1); }
+   if (n > 0) { k_row_scaled_half<<<nblk(n, 256), 256, 0, s>>>(n, Ai, Av, (__half *) out, rs); GB_COUNT(1); }
 }
 
 extern "C" void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s)
@@ -448,29 +501,6 @@ __global__ void k_gs_first(int n, const int *__restrict__ Ai, const VT *__restri
    u[i] += z;
 }
 
-// strictly lower part of each row (columns j < i, in row order)
-__global__ void k_lower_count(int n, const int *__restrict__ Ai, const int *__restrict__ Aj, int *__restrict__ cnt)
-{
-   int i = blockIdx.x * blockDim.x + threadIdx.x;
-   if (i >= n) { return; }
-   int c = 0;
-   for (int k = Ai[i]; k < Ai[i + 1]; k++) { c += Aj[k] < i; }
-   cnt[i] = c;
-}
-
-__global__ void k_lower_fill(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
-                             const double *__restrict__ Av, const int *__restrict__ Li, int *__restrict__ Lj,
-                             double *__restrict__ Lv)
-{
-   int i = blockIdx.x * blockDim.x + threadIdx.x;
-   if (i >= n) { return; }
-   int p = Li[i];
-   for (int k = Ai[i]; k < Ai[i + 1]; k++)
-   {
-      if (Aj[k] < i) { Lj[p] = Aj[k]; Lv[p] = Av[k]; p++; }
-   }
-}
-
 // a_ii (the first entry of row i; 1 for an empty row) in the given precision
 template <typename T>
 __global__ void k_diag_vals(int n, const int *__restrict__ Ai, const double *__restrict__ Av, T *__restrict__ out)
@@ -490,17 +520,6 @@ __global__ void k_gs_first_diag(int n, const XT *__restrict__ diag, XT *__restri
    XT z = v[i] / diag[i];
    v[i] = z;
    u[i] += z;
-}
-
-extern "C" void gb_lower_count(int n, const int *Ai, const int *Aj, int *cnt, cudaStream_t s)
-{
-   if (n > 0) { k_lower_count<<<nblk(n, 256), 256, 0, s>>>(n, Ai, Aj, cnt); GB_COUNT(1); }
-}
-
-extern "C" void gb_lower_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Li, int *Lj,
-                              double *Lv, cudaStream_t s)
-{
-   if (n > 0) { k_lower_fill<<<nblk(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, Li, Lj, Lv); GB_COUNT(1); }
 }
 
 extern "C" void gb_diag_vals(int n, const int *Ai, const double *Av, int vprec, void *out, cudaStream_t s)
