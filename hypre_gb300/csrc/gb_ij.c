@@ -530,6 +530,7 @@ struct hypre_IJMatrix_struct
    double    *st_vals;
    long long  st_len, st_cap;
    int       *st_rowptr;      /* device: set when one put holds every row in order */
+   int       *st_hstart;      /* host copy of those offsets until per-row state exists */
 };
 
 #define GB_MAGIC_IJM 0x494a4d31
@@ -605,17 +606,29 @@ static void ijm_free_stage(HYPRE_IJMatrix m)
    m->row_state = NULL; m->dev_off = NULL;
    gb_dfree(m->st_cols); gb_dfree(m->st_vals); gb_dfree(m->st_rowptr);
    m->st_cols = NULL; m->st_vals = NULL; m->st_rowptr = NULL;
+   free(m->st_hstart);
+   m->st_hstart = NULL;
    m->st_len = m->st_cap = 0;
 }
 
-HYPRE_Int HYPRE_IJMatrixInitialize(HYPRE_IJMatrix m)
+/* Per-row host state (arena slots sized from SetRowSizes, row lengths, where
+ * each row lives), allocated on first use: a single in-order put of every
+ * row never needs it.  Rows of such a put are recorded here when it is
+ * first needed. */
+static int ijm_host_ready(HYPRE_IJMatrix m)
 {
-   if (!check_ijm(m, 1)) { return gb_error_flag; }
-   ijm_free_stage(m);
+   if (m->row_len) { return 1; }
    int n = m->nrows;
    m->row_off = (int *) malloc(sizeof(int) * (size_t) (n ? n : 1));
    m->row_len = (int *) calloc((size_t) (n ? n : 1), sizeof(int));
    m->row_cap = (int *) malloc(sizeof(int) * (size_t) (n ? n : 1));
+   m->row_state = (unsigned char *) calloc((size_t) (n ? n : 1), 1);
+   m->dev_off = (long long *) malloc(sizeof(long long) * (size_t) (n ? n : 1));
+   if (!m->row_off || !m->row_len || !m->row_cap || !m->row_state || !m->dev_off)
+   {
+      gb_error(HYPRE_ERROR_MEMORY, "IJ staging");
+      return 0;
+   }
    long long tot = 0;
    for (int i = 0; i < n; i++)
    {
@@ -629,13 +642,25 @@ HYPRE_Int HYPRE_IJMatrixInitialize(HYPRE_IJMatrix m)
    m->arena_len = tot;
    m->cols = (int *) malloc(sizeof(int) * (size_t) m->arena_cap);
    m->vals = (double *) malloc(sizeof(double) * (size_t) m->arena_cap);
-   m->row_state = (unsigned char *) calloc((size_t) (n ? n : 1), 1);
-   m->dev_off = (long long *) malloc(sizeof(long long) * (size_t) (n ? n : 1));
-   if (!m->cols || !m->vals || !m->row_state || !m->dev_off)
+   if (!m->cols || !m->vals) { gb_error(HYPRE_ERROR_MEMORY, "IJ staging"); return 0; }
+   if (m->st_hstart)
    {
-      gb_error(HYPRE_ERROR_MEMORY, "IJ staging");
-      return gb_error_flag;
+      for (int r = 0; r < n; r++)
+      {
+         m->dev_off[r] = m->st_hstart[r];
+         m->row_len[r] = m->st_hstart[r + 1] - m->st_hstart[r];
+         m->row_state[r] = GB_IJ_ROW_DEVICE;
+      }
+      free(m->st_hstart);
+      m->st_hstart = NULL;
    }
+   return 1;
+}
+
+HYPRE_Int HYPRE_IJMatrixInitialize(HYPRE_IJMatrix m)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   ijm_free_stage(m);
    m->initialized = 1;
    m->assembled = 0;
    if (m->par) { gb_parcsr_free(m->par); m->par = NULL; }
@@ -704,6 +729,7 @@ static int ijm_staging_reserve(HYPRE_IJMatrix m, long long need)
 static int ijm_migrate(HYPRE_IJMatrix m)
 {
    if (m->st_len == 0) { return 1; }
+   if (!ijm_host_ready(m)) { return 0; }
    int *hc = (int *) malloc(sizeof(int) * (size_t) m->st_len);
    double *hv = (double *) malloc(sizeof(double) * (size_t) m->st_len);
    if (!hc || !hv) { free(hc); free(hv); gb_error(HYPRE_ERROR_MEMORY, "IJ staging"); return 0; }
@@ -751,6 +777,40 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
    cudaStream_t s = gb_stream();
    cudaMemcpyAsync(m->st_cols + m->st_len, cols, sizeof(int) * (size_t) tot, cudaMemcpyHostToDevice, s);
    cudaMemcpyAsync(m->st_vals + m->st_len, values, sizeof(double) * (size_t) tot, cudaMemcpyHostToDevice, s);
+   if (!m->row_len && m->st_len == 0 && nrows == m->nrows)
+   {
+      /* no row holds data yet: a put of every row in order needs no per-row
+       * host state (its offsets are the CSR row pointers) */
+      int inorder = 1;
+      long long acc = 0;
+      hstart[0] = 0;
+      for (int t = 0; t < nrows; t++)
+      {
+         inorder &= rows[t] - m->ilower == t;
+         acc += ncols[t];
+         hstart[t + 1] = (int) acc;
+      }
+      if (inorder)
+      {
+         int *dstart = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
+         int *flags = (int *) gb_dcalloc(sizeof(int));
+         int f = 1;
+         if (dstart && flags)
+         {
+            cudaMemcpyAsync(dstart, hstart, sizeof(int) * (size_t) (nrows + 1), cudaMemcpyHostToDevice, s);
+            gb_ij_check(nrows, dstart, m->st_cols, m->jupper - m->jlower + 1, flags, s);
+            f = ij_read_int(flags);   /* also the point after which the caller's buffers are free */
+         }
+         else { gb_sync(); }
+         gb_dfree(flags);
+         if (f != 0) { gb_dfree(dstart); free(hstart); return 0; }
+         m->st_len = tot;
+         m->st_rowptr = dstart;
+         m->st_hstart = hstart;
+         return 1;
+      }
+   }
+   if (!ijm_host_ready(m)) { gb_sync(); free(hstart); return 0; }
    /* row offsets within the put; every row valid, new and not repeated in
     * this put (marked pending, unmarked on failure); whether the put is the
     * whole matrix in row order (its offsets are then the CSR row pointers) */
@@ -819,6 +879,7 @@ static HYPRE_Int ijm_put(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, co
       m->assembled = 0;
       return gb_error_flag;
    }
+   if (!ijm_host_ready(m)) { return gb_error_flag; }
    if (m->st_len > 0)
    {
       /* the host path edits rows in the arena: bring staged rows back first
@@ -945,6 +1006,7 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
       m->assembled = 1;
       return gb_error_flag;
    }
+   if (!ijm_host_ready(m)) { return gb_error_flag; }
    /* row pointers; host-arena rows are packed behind the device-staged ones
     * (their offsets point past st_len into a temporary upload) */
    int *I = (int *) malloc(sizeof(int) * (size_t) (n + 1));
@@ -1013,7 +1075,7 @@ HYPRE_Int HYPRE_IJMatrixGetValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *
 {
    if (!check_ijm(m, 1)) { return gb_error_flag; }
    if (!m->initialized) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not initialized"); return gb_error_flag; }
-   if (!ijm_migrate(m)) { return gb_error_flag; }
+   if (!ijm_host_ready(m) || !ijm_migrate(m)) { return gb_error_flag; }
    long long k = 0;
    for (int t = 0; t < nrows; t++)
    {
