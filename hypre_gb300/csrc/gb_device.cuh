@@ -248,9 +248,12 @@ __device__ __forceinline__ GbTabC gb_tabc_at(char *base, int cap)
    return t;
 }
 
+// (compact tables start on 16-byte boundaries and hold a multiple of four
+// slots: they are reset with 16-byte stores)
 __device__ __forceinline__ void gb_tab_init(GbTabC &t)
 {
-   for (int k = gb_lane(); k < t.cap; k += 32) { t.hk[k] = -1; }
+   const int4 e = make_int4(-1, -1, -1, -1);
+   for (int k = 4 * gb_lane(); k < t.cap; k += 128) { *reinterpret_cast<int4 *>(t.hk + k) = e; }
    __syncwarp();
 }
 
@@ -313,7 +316,8 @@ __device__ __forceinline__ void gb_tab_clear(GbTabC &t, int n)
 {
    (void) n;
    __syncwarp();
-   for (int k = gb_lane(); k < t.cap; k += 32) { t.hk[k] = -1; }
+   const int4 e = make_int4(-1, -1, -1, -1);
+   for (int k = 4 * gb_lane(); k < t.cap; k += 128) { *reinterpret_cast<int4 *>(t.hk + k) = e; }
    __syncwarp();
 }
 

@@ -1320,18 +1320,35 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
             __syncwarp();
             if (lead && pos >= 0)
             {
-               double x;
-               if (created) { Cj[off + pos] = ccol; x = v; }
-               else { x = (MODE == 3 ? vals[pos] : Cv[off + pos]) + v; }
                unsigned rest = grp & (grp - 1u);
-               while (rest)
+               if (MODE == 3)
                {
-                  int m = __ffs(rest) - 1;
-                  rest &= rest - 1u;
-                  x += stage[m];
+                  double x;
+                  if (created) { Cj[off + pos] = ccol; x = v; }
+                  else { x = vals[pos] + v; }
+                  while (rest)
+                  {
+                     int m = __ffs(rest) - 1;
+                     rest &= rest - 1u;
+                     x += stage[m];
+                  }
+                  vals[pos] = x;
                }
-               if (MODE == 3) { vals[pos] = x; }
-               else { Cv[off + pos] = x; }
+               else
+               {
+                  // the first term stored (new column) or added, then the
+                  // group's other terms in lane order: fire-and-forget adds
+                  // from one thread to one address apply in issue order, and
+                  // __syncwarp orders them after the previous steps' adds
+                  if (created) { Cj[off + pos] = ccol; Cv[off + pos] = v; }
+                  else { atomicAdd(Cv + off + pos, v); }
+                  while (rest)
+                  {
+                     int m = __ffs(rest) - 1;
+                     rest &= rest - 1u;
+                     atomicAdd(Cv + off + pos, stage[m]);
+                  }
+               }
             }
             __syncwarp();
          }
@@ -1474,9 +1491,12 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
 // product prefix: new columns take positions in lane order (= product
 // order), and each column receives at most one term per step, added in
 // product order -- the same positions and sums as the flattened kernel.
-// The numeric pass accumulates in shared memory (vals[pos]) and writes the
-// row once.  Chunk c+1's B entries and the next window of 32 A entries are
-// loaded while chunk c is inserted.
+// The numeric pass stores a new column's first term and adds later terms
+// with fire-and-forget FP64 atomics: a column gets at most one term per step
+// and __syncwarp orders one step's memory operations before the next's, so
+// the adds to each output entry happen in product order (the sequential sum)
+// and no warp waits on them.  Chunk c+1's B entries and the next window of 32
+// A entries are loaded while chunk c is inserted.
 // MODE 0: 1024-slot tables for all rows; MODE 1: 2048-slot tables for the
 // rows listed by MODE 0's symbolic pass.
 // ---------------------------------------------------------------------------
@@ -1484,7 +1504,7 @@ template <int MODE, bool NUMERIC> struct RcCfg
 {
    static constexpr int CAP = MODE ? GB_BIG_CAP : GB_SMEM_CAP;
    static constexpr int LCAP = CAP / 4 * 3;
-   static constexpr int WBYTES = GB_TABC_BYTES(CAP) + (NUMERIC ? LCAP * 8 : 0);
+   static constexpr int WBYTES = GB_TABC_BYTES(CAP);
    static constexpr int WARPS = 4;
    static constexpr int BYTES = WARPS * WBYTES;
 };
@@ -1504,7 +1524,6 @@ __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, con
    const unsigned lt = (1u << lane) - 1u;
    unsigned char *mine = shrc + (size_t) (threadIdx.x >> 5) * K::WBYTES;
    GbTabC T = gb_tabc_at((char *) mine, K::CAP);
-   double *vals = (double *) (mine + GB_TABC_BYTES(K::CAP));
    gb_tab_init(T);
    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
    const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -1532,7 +1551,7 @@ __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, con
          if (lane == 0)
          {
             gb_tabc_insert(T, r, 0);
-            if (NUMERIC) { vals[0] = 0.0; Cj[off] = r; }
+            if (NUMERIC) { Cv[off] = 0.0; Cj[off] = r; }
          }
          count = 1;
          __syncwarp();
@@ -1597,10 +1616,10 @@ __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, con
             if (need)
             {
                const int p = count + __popc(nm & lt);
-               if (p < K::LCAP && gb_tabc_insert(T, col, p) >= 0) { vals[p] = v; Cj[off + p] = col; }
+               if (p < K::LCAP && gb_tabc_insert(T, col, p) >= 0) { Cv[off + p] = v; Cj[off + p] = col; }
                else { bad = true; }
             }
-            else if (act) { vals[pos] += v; }
+            else if (act) { atomicAdd(Cv + off + pos, v); }
             count += __popc(nm);
             if (__any_sync(GB_FULL, bad)) { ovf = 1; }
             __syncwarp();
@@ -1617,10 +1636,6 @@ __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, con
             if (e2 < ka1) { const int k = Aj[e2]; nb0 = Bi[k]; nb1 = Bi[k + 1]; if (NUMERIC) { na = Av[e2]; } }
          }
          else { q = nq; }
-      }
-      if (NUMERIC && !ovf)
-      {
-         for (int p = lane; p < count; p += 32) { Cv[off + p] = vals[p]; }
       }
       if (lane == 0)
       {
