@@ -265,9 +265,110 @@ static int spgemm_host(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
    return r;
 }
 
+/* Sparse product with one counting-and-filling pass per shared-memory tier
+ * (gb_spgemm / gb_spgemm_rc phase 2): each row goes to a temporary area
+ * sized by its product count (capped by the tier-0 table; rows that may
+ * overflow it get a tier-1 area), the row counts are scanned into C's row
+ * pointers and a gather moves the rows into place.  Rows beyond tier 1 take
+ * the global-table tier's two passes.  Returns -2 when the temporary areas
+ * would exceed 2^31 entries (the caller runs the two-pass driver). */
+#define GB_SPGEMM_LCAP0 768
+#define GB_SPGEMM_LCAP1 1536
+static int spgemm_fused(const gb_csr *A, const gb_csr *B, int square, gb_csr *C, int rowchunk)
+{
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   int *ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+   int *cap = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *over = (int *) gb_dcalloc(sizeof(int) * 2);
+   unsigned long long *sum = (unsigned long long *) gb_dcalloc(sizeof(unsigned long long));
+   if (!ub || !cap || !over || !sum) { gb_dfree(ub); gb_dfree(cap); gb_dfree(over); gb_dfree(sum); return -1; }
+   gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+   gb_spgemm_cap(n, ub, GB_SPGEMM_LCAP0, cap, sum, over, s);
+   unsigned long long hsum = 0;
+   cudaMemcpyAsync(&hsum, sum, sizeof(hsum), cudaMemcpyDeviceToHost, s);
+   int hover = read_int(over);
+   gb_dfree(sum); gb_dfree(over);
+   long long tot = (long long) hsum + (long long) hover * GB_SPGEMM_LCAP1;
+   if (tot > 0x7fffff00LL) { gb_dfree(ub); gb_dfree(cap); return -2; }
+   int *tofs = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *tj = (int *) gb_dmalloc(sizeof(int) * (size_t) (tot > 0 ? tot : 1));
+   double *tv = (double *) gb_dmalloc(sizeof(double) * (size_t) (tot > 0 ? tot : 1));
+   int *src = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *list2 = NULL, *n2 = (int *) gb_dcalloc(sizeof(int) * 2);
+   if (!tofs || !tj || !tv || !src || !cnt || !n2)
+   {
+      gb_dfree(ub); gb_dfree(cap); gb_dfree(tofs); gb_dfree(tj); gb_dfree(tv); gb_dfree(src); gb_dfree(cnt);
+      gb_dfree(n2);
+      return -1;
+   }
+   scan_total(cap, tofs, n);
+   gb_dfree(cap);
+   gb_tier t;
+   tier_begin(&t, n);
+   /* tier 0 over every row: areas at tofs[r] */
+   if (rowchunk)
+   {
+      gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, tofs, tj, tv, t.ovf_list, t.ovf_n, NULL,
+                   NULL, n, t.err, ub, src, 0, 2, 0, s);
+   }
+   else
+   {
+      gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, tofs, tj, tv, t.ovf_list, t.ovf_n, NULL,
+                NULL, n, NULL, 0, 0, t.err, ub, src, 0, 2, 0, s);
+   }
+   int h1 = read_int(t.ovf_n), h2 = 0;
+   if (h1 > 0)
+   {
+      /* tier 1 over the rows that did not fit, in row order: areas of 1536
+       * entries after the tier-0 ones */
+      sort_row_list(t.ovf_list, h1, n);
+      list2 = (int *) gb_dmalloc(sizeof(int) * (size_t) h1);
+      if (rowchunk)
+      {
+         gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, tj, tv, t.ovf_list, t.ovf_n, list2,
+                      n2, h1, t.err, NULL, src, (int) hsum, 2, 1, s);
+      }
+      else
+      {
+         gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, tj, tv, t.ovf_list, t.ovf_n, list2,
+                   n2, h1, NULL, 0, 0, t.err, NULL, src, (int) hsum, 2, 1, s);
+      }
+      h2 = read_int(n2);
+   }
+   if (h2 > 0)
+   {
+      tier_global_n(&t, ub, n, h2);
+      gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, list2, n2, NULL, NULL, h2,
+                t.gtab, t.gcap, t.gwarps, t.err, NULL, NULL, 0, 0, 2, s);
+   }
+   C->nr = n; C->nc = B->nc;
+   C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   C->nnz = scan_total(cnt, C->i, n);
+   C->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C->nnz ? C->nnz : 1));
+   C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
+   gb_spgemm_gather(n, C->i, src, tj, tv, C->j, C->v, s);
+   if (h2 > 0)
+   {
+      gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, list2, n2, NULL, NULL, h2,
+                t.gtab, t.gcap, t.gwarps, t.err, NULL, NULL, 0, 1, 2, s);
+   }
+   int e = tier_end(&t);
+   gb_dfree(ub); gb_dfree(tofs); gb_dfree(tj); gb_dfree(tv); gb_dfree(src); gb_dfree(cnt); gb_dfree(list2);
+   gb_dfree(n2);
+   if (e) { gb_error(HYPRE_ERROR_GENERIC, "sparse product table overflow"); return -1; }
+   return 0;
+}
+
 static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
 {
    cudaStream_t s = gb_stream();
+   {
+      const int rc = B->nr > 0 && (long long) B->nnz >= 12LL * (long long) B->nr;
+      int f = spgemm_fused(A, B, square, C, rc);
+      if (f != -2) { return f; }
+   }
    int n = A->nr;
    int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    gb_tier t;
@@ -293,12 +394,12 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    if (rowchunk)
    {
       gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL,
-                   NULL, n, t.err, ub, 0, 0, s);
+                   NULL, n, t.err, ub, NULL, 0, 0, 0, s);
    }
    else
    {
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL,
-                NULL, n, NULL, 0, 0, t.err, NULL, 0, 0, s);
+                NULL, n, NULL, 0, 0, t.err, NULL, NULL, 0, 0, 0, s);
    }
    int h1 = read_int(t.ovf_n), h2 = 0;
    if (h1 > 0)
@@ -308,12 +409,12 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
       if (rowchunk)
       {
          gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n,
-                      list2, n2, h1, t.err, NULL, 0, 1, s);
+                      list2, n2, h1, t.err, NULL, NULL, 0, 0, 1, s);
       }
       else
       {
          gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n,
-                   list2, n2, h1, NULL, 0, 0, t.err, NULL, 0, 1, s);
+                   list2, n2, h1, NULL, 0, 0, t.err, NULL, NULL, 0, 0, 1, s);
       }
       h2 = read_int(n2);
    }
@@ -327,7 +428,7 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
       }
       tier_global_n(&t, ub, n, h2);
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, list2, n2, NULL, NULL, h2,
-                t.gtab, t.gcap, t.gwarps, t.err, NULL, 0, 2, s);
+                t.gtab, t.gcap, t.gwarps, t.err, NULL, NULL, 0, 0, 2, s);
    }
    C->nr = n; C->nc = B->nc;
    C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
@@ -338,11 +439,11 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    if (rowchunk)
    {
       gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL,
-                   NULL, n, t.err, NULL, 1, 0, s);
+                   NULL, n, t.err, NULL, NULL, 0, 1, 0, s);
       if (h1 > 0)
       {
          gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
-                      NULL, NULL, h1, t.err, NULL, 1, 1, s);
+                      NULL, NULL, h1, t.err, NULL, NULL, 0, 1, 1, s);
       }
    }
    else
@@ -356,21 +457,21 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
       if (prods >= 512.0)
       {
          gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
-                   NULL, NULL, n, NULL, 0, 0, t.err, NULL, 1, 3, s);
+                   NULL, NULL, n, NULL, 0, 0, t.err, NULL, NULL, 0, 1, 3, s);
          skip = GB_SPGEMM_TINY_COLS;
       }
       gb_spgemm(n, square, skip, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
-                NULL, NULL, n, NULL, 0, 0, t.err, NULL, 1, 0, s);
+                NULL, NULL, n, NULL, 0, 0, t.err, NULL, NULL, 0, 1, 0, s);
       if (h1 > 0)
       {
          gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n,
-                   NULL, NULL, h1, NULL, 0, 0, t.err, NULL, 1, 1, s);
+                   NULL, NULL, h1, NULL, 0, 0, t.err, NULL, NULL, 0, 1, 1, s);
       }
    }
    if (h2 > 0)
    {
       gb_spgemm(n, square, W, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, list2, n2, NULL, NULL, h2,
-                t.gtab, t.gcap, t.gwarps, t.err, NULL, 1, 2, s);
+                t.gtab, t.gcap, t.gwarps, t.err, NULL, NULL, 0, 1, 2, s);
    }
    int e = tier_end(&t);
    gb_dfree(ub); gb_dfree(cnt); gb_dfree(list2); gb_dfree(n2);

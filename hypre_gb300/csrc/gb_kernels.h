@@ -92,11 +92,17 @@ void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, const int *Aj
 void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av, const int *Bi,
                const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list,
                int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab, int gcap, int gwarps, int *err,
-               const int *ub, int phase, int tier, cudaStream_t s);
+               const int *ub, int *src, int fbase, int phase, int tier, cudaStream_t s);
+/* phase 2 (tiers 0 and 1): count and fill in one pass into temporary areas
+ * (tier 0 at Ci[r], tier 1 at fbase + t * 1536), cnt[r] and src[r] set;
+ * gb_spgemm_cap sizes the areas, gb_spgemm_gather moves rows into place */
+void gb_spgemm_cap(int n, const int *ub, int lcap0, int *cap, unsigned long long *sum, int *over, cudaStream_t s);
+void gb_spgemm_gather(int n, const int *Ci, const int *src, const int *tj, const double *tv, int *Cj, double *Cv,
+                      cudaStream_t s);
 void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi, const int *Bj,
                   const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list, int *ovf_n,
-                  int *out_list, int *out_n, int nlist, int *err, const int *ub, int phase, int tier,
-                  cudaStream_t s);
+                  int *out_list, int *out_n, int nlist, int *err, const int *ub, int *src, int fbase, int phase,
+                  int tier, cudaStream_t s);
 /* IJ matrix device assembly (gb_ijdev.cu) */
 void gb_ij_check(int nrows, const int *start, const int *cols, int ncol, int *flags, cudaStream_t s);
 void gb_ij_gather(int n, const long long *off, const int *I, const int *scols, const double *svals, int swap_diag,

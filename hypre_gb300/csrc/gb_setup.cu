@@ -1144,15 +1144,23 @@ __device__ __forceinline__ typename SpgemmTab<MODE>::type spgemm_tab(int *sh, in
    else { return gb_tabc_at((char *) sh + (threadIdx.x >> 5) * GB_TABC_BYTES(GB_SMEM_CAP), GB_SMEM_CAP); }
 }
 
-template <int MODE, bool NUMERIC>
+// FUSED (numeric tiers 0 and 1): one pass instead of count + fill.  Each row
+// is written to a temporary area -- at Ci[r] for tier 0 (sized by the row's
+// product count, capped by the table), at fbase + t * listcap for the t-th
+// listed row of tier 1 -- and its column count and area offset go to cnt[r]
+// and src[r]; rows that overflow are listed for the next tier as in the
+// symbolic pass (src[r] = -1).  A gather then moves the rows into place.
+template <int MODE, bool NUMERIC, bool FUSED = false>
 __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W, const int *__restrict__ Ai,
                                                 const int *__restrict__ Aj, const double *__restrict__ Av,
                                                 const int *__restrict__ Bi, const int *__restrict__ Bj,
                                                 const double *__restrict__ Bv, int *__restrict__ cnt,
                                                 const int *__restrict__ Ci, int *__restrict__ Cj,
                                                 double *__restrict__ Cv, int *ovf_list, int *ovf_n, int *out_list,
-                                                int *out_n, int *gtab, int gcap, int *err, const int *__restrict__ ub)
+                                                int *out_n, int *gtab, int gcap, int *err, const int *__restrict__ ub,
+                                                int *__restrict__ src, int fbase)
 {
+   constexpr bool COUNTING = !NUMERIC || FUSED;
    extern __shared__ __align__(16) int sh[];
    __shared__ double stage_all[128];
    const int lane = gb_lane();
@@ -1171,14 +1179,20 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
    {
       int r = LISTED ? ovf_list[t] : t;
       int off = 0;
-      if (MODE == 0 && !NUMERIC && ub && ub[r] > 16 * T.listcap)
+      if (MODE == 0 && COUNTING && ub && ub[r] > 16 * T.listcap)
       {
          // far more products than the table holds (at most 16 per distinct
          // column on average would be needed to fit): straight to the next tier
-         if (lane == 0) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         if (lane == 0)
+         {
+            ovf_list[atomicAdd(ovf_n, 1)] = r;
+            cnt[r] = 0;
+            if (FUSED) { src[r] = -1; }
+         }
          continue;
       }
-      if (NUMERIC)
+      if (FUSED) { off = MODE == 0 ? Ci[r] : fbase + t * T.listcap; }
+      else if (NUMERIC)
       {
          off = Ci[r];
          const int len = Ci[r + 1] - off;
@@ -1360,9 +1374,23 @@ __global__ void __launch_bounds__(128, 8) k_spgemm(int nrows, int square, int W,
       }
       if (lane == 0)
       {
-         if (!ovf) { if (!NUMERIC) { cnt[r] = count; } }
-         else if (MODE == 0 && !NUMERIC) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
-         else if (MODE == 1 && !NUMERIC) { out_list[atomicAdd(out_n, 1)] = r; cnt[r] = 0; }
+         if (!ovf)
+         {
+            if (COUNTING) { cnt[r] = count; }
+            if (FUSED) { src[r] = off; }
+         }
+         else if (MODE == 0 && COUNTING)
+         {
+            ovf_list[atomicAdd(ovf_n, 1)] = r;
+            cnt[r] = 0;
+            if (FUSED) { src[r] = -1; }
+         }
+         else if (MODE == 1 && COUNTING)
+         {
+            out_list[atomicAdd(out_n, 1)] = r;
+            cnt[r] = 0;
+            if (FUSED) { src[r] = -1; }
+         }
          else { atomicExch(err, 1); }
       }
       gb_tab_clear(T, count);
@@ -1410,7 +1438,8 @@ extern "C" void gb_spgemm_ub(int nrows, int ncols, int square, const int *Ai, co
 extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const double *Av,
                           const int *Bi, const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj,
                           double *Cv, int *ovf_list, int *ovf_n, int *out_list, int *out_n, int nlist, int *gtab,
-                          int gcap, int gwarps, int *err, const int *ub, int phase, int tier, cudaStream_t s)
+                          int gcap, int gwarps, int *err, const int *ub, int *src, int fbase, int phase, int tier,
+                          cudaStream_t s)
 {
    static int attr_done = 0;
    if (!attr_done)
@@ -1419,33 +1448,29 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
        * shared-memory limit: opt in once */
       cudaFuncSetAttribute(k_spgemm<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMALL_BYTES);
       cudaFuncSetAttribute(k_spgemm<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMALL_BYTES);
+      cudaFuncSetAttribute(k_spgemm<0, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMALL_BYTES);
       cudaFuncSetAttribute(k_spgemm<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_BIG_BYTES);
       cudaFuncSetAttribute(k_spgemm<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_BIG_BYTES);
+      cudaFuncSetAttribute(k_spgemm<1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_BIG_BYTES);
       attr_done = 1;
    }
+#define GB_SG_ARGS(gt, gc) nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv, ovf_list, ovf_n, out_list, \
+                           out_n, gt, gc, err, ub, src, fbase
    if (tier == 0)
    {
       /* eight blocks of four warps per SM (24 KB of tables each) */
       long long want = ((long long) nrows + GB_SMEM_WARPS - 1) / GB_SMEM_WARPS;
       int blocks = (int) (want < 152 * 8 ? (want > 0 ? want : 1) : 152 * 8);
-      if (phase == 0)
-      {
-         k_spgemm<0, false><<<blocks, 128, GB_SMALL_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
-                                                               Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
-      }
-      else
-      {
-         k_spgemm<0, true><<<blocks, 128, GB_SMALL_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj,
-                                                              Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
-      }
+      if (phase == 0) { k_spgemm<0, false><<<blocks, 128, GB_SMALL_BYTES, s>>>(GB_SG_ARGS(nullptr, 0)); }
+      else if (phase == 1) { k_spgemm<0, true><<<blocks, 128, GB_SMALL_BYTES, s>>>(GB_SG_ARGS(nullptr, 0)); }
+      else { k_spgemm<0, true, true><<<blocks, 128, GB_SMALL_BYTES, s>>>(GB_SG_ARGS(nullptr, 0)); }
    }
    else if (tier == 3)
    {
       /* numeric only: 3 KB tables per warp, twelve blocks per SM (registers) */
       long long want = ((long long) nrows + GB_SMEM_WARPS - 1) / GB_SMEM_WARPS;
       int blocks = (int) (want < 152 * 12 ? (want > 0 ? want : 1) : 152 * 12);
-      k_spgemm<3, true><<<blocks, 128, GB_TINY_BYTES, s>>>(nrows, square, 0, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
-                                                           ovf_list, ovf_n, out_list, out_n, nullptr, 0, err, ub);
+      k_spgemm<3, true><<<blocks, 128, GB_TINY_BYTES, s>>>(GB_SG_ARGS(nullptr, 0));
    }
    else if (tier == 1)
    {
@@ -1453,34 +1478,80 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
       long long want = ((long long) nlist + GB_BIG_WARPS - 1) / GB_BIG_WARPS;
       int blocks = (int) (want < 152 * 4 ? (want > 0 ? want : 1) : 152 * 4);
       int threads = 32 * GB_BIG_WARPS;
-      if (phase == 0)
-      {
-         k_spgemm<1, false><<<blocks, threads, GB_BIG_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
-                                                                  Cj, Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0,
-                                                                  err, ub);
-      }
-      else
-      {
-         k_spgemm<1, true><<<blocks, threads, GB_BIG_BYTES, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci,
-                                                                 Cj, Cv, ovf_list, ovf_n, out_list, out_n, nullptr, 0,
-                                                                 err, ub);
-      }
+      if (phase == 0) { k_spgemm<1, false><<<blocks, threads, GB_BIG_BYTES, s>>>(GB_SG_ARGS(nullptr, 0)); }
+      else if (phase == 1) { k_spgemm<1, true><<<blocks, threads, GB_BIG_BYTES, s>>>(GB_SG_ARGS(nullptr, 0)); }
+      else { k_spgemm<1, true, true><<<blocks, threads, GB_BIG_BYTES, s>>>(GB_SG_ARGS(nullptr, 0)); }
    }
    else
    {
       int blocks = (gwarps + 3) / 4;
-      if (phase == 0)
-      {
-         k_spgemm<2, false><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
-                                                   ovf_list, ovf_n, out_list, out_n, gtab, gcap, err, ub);
-      }
-      else
-      {
-         k_spgemm<2, true><<<blocks, 128, 0, s>>>(nrows, square, W, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv,
-                                                  ovf_list, ovf_n, out_list, out_n, gtab, gcap, err, ub);
-      }
+      if (phase == 0) { k_spgemm<2, false><<<blocks, 128, 0, s>>>(GB_SG_ARGS(gtab, gcap)); }
+      else { k_spgemm<2, true><<<blocks, 128, 0, s>>>(GB_SG_ARGS(gtab, gcap)); }
    }
+#undef GB_SG_ARGS
    GB_COUNT(1);
+}
+
+// temporary areas of the fused products: cap[r] = min(ub[r], lcap0); *sum
+// accumulates the capped sizes, *over counts the rows whose bound exceeds lcap0
+__global__ void k_spgemm_cap(int n, const int *__restrict__ ub, int lcap0, int *__restrict__ cap,
+                             unsigned long long *sum, int *over)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   unsigned long long c = 0;
+   int o = 0;
+   if (r < n)
+   {
+      const int u = ub[r];
+      c = (unsigned long long) (u < lcap0 ? u : lcap0);
+      o = u > lcap0;
+      cap[r] = (int) c;
+   }
+   for (int d = 16; d > 0; d >>= 1)
+   {
+      c += __shfl_down_sync(GB_FULL, c, d);
+      o += __shfl_down_sync(GB_FULL, o, d);
+   }
+   if ((threadIdx.x & 31) == 0)
+   {
+      if (c) { atomicAdd(sum, c); }
+      if (o) { atomicAdd(over, o); }
+   }
+}
+
+extern "C" void gb_spgemm_cap(int n, const int *ub, int lcap0, int *cap, unsigned long long *sum, int *over,
+                              cudaStream_t s)
+{
+   if (n > 0) { k_spgemm_cap<<<gb_blocks(n, 256), 256, 0, s>>>(n, ub, lcap0, cap, sum, over); GB_COUNT(1); }
+}
+
+// one warp per row: the row's cnt entries from its temporary area src[r]
+// (rows with src[r] < 0 were filled in place by the global-table tier)
+__global__ void k_spgemm_gather(int n, const int *__restrict__ Ci, const int *__restrict__ src,
+                                const int *__restrict__ tj, const double *__restrict__ tv, int *__restrict__ Cj,
+                                double *__restrict__ Cv)
+{
+   const int r = (int) ((blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5);
+   const int lane = threadIdx.x & 31;
+   if (r >= n) { return; }
+   const int o = src[r];
+   if (o < 0) { return; }
+   const int d = Ci[r], l = Ci[r + 1] - d;
+   for (int q = lane; q < l; q += 32)
+   {
+      Cj[d + q] = tj[o + q];
+      Cv[d + q] = tv[o + q];
+   }
+}
+
+extern "C" void gb_spgemm_gather(int n, const int *Ci, const int *src, const int *tj, const double *tv, int *Cj,
+                                 double *Cv, cudaStream_t s)
+{
+   if (n > 0)
+   {
+      k_spgemm_gather<<<gb_blocks((long long) n * 32, 256), 256, 0, s>>>(n, Ci, src, tj, tv, Cj, Cv);
+      GB_COUNT(1);
+   }
 }
 
 // ---------------------------------------------------------------------------
@@ -1509,15 +1580,18 @@ template <int MODE, bool NUMERIC> struct RcCfg
    static constexpr int BYTES = WARPS * WBYTES;
 };
 
-template <int MODE, bool NUMERIC>
+// FUSED: one pass into a temporary area, as for k_spgemm
+template <int MODE, bool NUMERIC, bool FUSED = false>
 __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, const int *__restrict__ Ai,
                                                    const int *__restrict__ Aj, const double *__restrict__ Av,
                                                    const int *__restrict__ Bi, const int *__restrict__ Bj,
                                                    const double *__restrict__ Bv, int *__restrict__ cnt,
                                                    const int *__restrict__ Ci, int *__restrict__ Cj,
                                                    double *__restrict__ Cv, int *ovf_list, int *ovf_n,
-                                                   int *out_list, int *out_n, int *err, const int *__restrict__ ub)
+                                                   int *out_list, int *out_n, int *err, const int *__restrict__ ub,
+                                                   int *__restrict__ src, int fbase)
 {
+   constexpr bool COUNTING = !NUMERIC || FUSED;
    typedef RcCfg<MODE, NUMERIC> K;
    extern __shared__ __align__(16) unsigned char shrc[];
    const int lane = gb_lane();
@@ -1531,14 +1605,20 @@ __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, con
    for (int t = warp; t < total; t += nwarps)
    {
       const int r = MODE ? ovf_list[t] : t;
-      if (MODE == 0 && !NUMERIC && ub && ub[r] > 16 * K::LCAP)
+      if (MODE == 0 && COUNTING && ub && ub[r] > 16 * K::LCAP)
       {
          // far more products than the table holds: straight to the next tier
-         if (lane == 0) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
+         if (lane == 0)
+         {
+            ovf_list[atomicAdd(ovf_n, 1)] = r;
+            cnt[r] = 0;
+            if (FUSED) { src[r] = -1; }
+         }
          continue;
       }
       int off = 0;
-      if (NUMERIC)
+      if (FUSED) { off = MODE == 0 ? Ci[r] : fbase + t * K::LCAP; }
+      else if (NUMERIC)
       {
          off = Ci[r];
          const int len = Ci[r + 1] - off;
@@ -1639,9 +1719,23 @@ __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, con
       }
       if (lane == 0)
       {
-         if (!ovf) { if (!NUMERIC) { cnt[r] = count; } }
-         else if (MODE == 0 && !NUMERIC) { ovf_list[atomicAdd(ovf_n, 1)] = r; cnt[r] = 0; }
-         else if (MODE == 1 && !NUMERIC) { out_list[atomicAdd(out_n, 1)] = r; cnt[r] = 0; }
+         if (!ovf)
+         {
+            if (COUNTING) { cnt[r] = count; }
+            if (FUSED) { src[r] = off; }
+         }
+         else if (MODE == 0 && COUNTING)
+         {
+            ovf_list[atomicAdd(ovf_n, 1)] = r;
+            cnt[r] = 0;
+            if (FUSED) { src[r] = -1; }
+         }
+         else if (MODE == 1 && COUNTING)
+         {
+            out_list[atomicAdd(out_n, 1)] = r;
+            cnt[r] = 0;
+            if (FUSED) { src[r] = -1; }
+         }
          else { atomicExch(err, 1); }
       }
       gb_tab_clear(T, count);
@@ -1652,7 +1746,7 @@ __global__ void __launch_bounds__(128, 8) k_spgemm_rc(int nrows, int square, con
 extern "C" void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi,
                              const int *Bj, const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv,
                              int *ovf_list, int *ovf_n, int *out_list, int *out_n, int nlist, int *err,
-                             const int *ub, int phase, int tier, cudaStream_t s)
+                             const int *ub, int *src, int fbase, int phase, int tier, cudaStream_t s)
 {
    static int attr_done = 0;
    if (!attr_done)
@@ -1661,6 +1755,10 @@ extern "C" void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj
       cudaFuncSetAttribute(k_spgemm_rc<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RcCfg<0, true>::BYTES);
       cudaFuncSetAttribute(k_spgemm_rc<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RcCfg<1, false>::BYTES);
       cudaFuncSetAttribute(k_spgemm_rc<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RcCfg<1, true>::BYTES);
+      cudaFuncSetAttribute(k_spgemm_rc<0, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           RcCfg<0, true>::BYTES);
+      cudaFuncSetAttribute(k_spgemm_rc<1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           RcCfg<1, true>::BYTES);
       attr_done = 1;
    }
    int dev = 0, sms = 152;
@@ -1677,16 +1775,19 @@ extern "C" void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj
    if (per_sm > 16) { per_sm = 16; }
    const long long maxb = (long long) sms * per_sm;
    const int blocks = (int) (want < maxb ? (want > 0 ? want : 1) : maxb);
-#define GB_RC_ARGS nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv, ovf_list, ovf_n, out_list, out_n, err, ub
+#define GB_RC_ARGS nrows, square, Ai, Aj, Av, Bi, Bj, Bv, cnt, Ci, Cj, Cv, ovf_list, ovf_n, out_list, out_n, err, ub, \
+                   src, fbase
    if (tier == 0)
    {
       if (phase == 0) { k_spgemm_rc<0, false><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
-      else { k_spgemm_rc<0, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+      else if (phase == 1) { k_spgemm_rc<0, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+      else { k_spgemm_rc<0, true, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
    }
    else
    {
       if (phase == 0) { k_spgemm_rc<1, false><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
-      else { k_spgemm_rc<1, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+      else if (phase == 1) { k_spgemm_rc<1, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
+      else { k_spgemm_rc<1, true, true><<<blocks, 128, bytes, s>>>(GB_RC_ARGS); }
    }
 #undef GB_RC_ARGS
    GB_COUNT(1);
