@@ -70,13 +70,18 @@ extern "C" void gb_scatter_list(int n, const int *flag, const int *scan, int *li
 // C neighbours i2 of i1 in S and of C points i3 != i1 in S_i2 for every
 // neighbour i2.  Shared-memory tables, global tables for overflowing rows.
 // ---------------------------------------------------------------------------
-template <bool GLOBAL, bool FILL>
+// FUSED (shared-memory tier): count and fill in one pass, each row into a
+// temporary area at S2i[ic] (sized by its upper bound, capped by the table);
+// the count goes to cnt[ic] and the area to src[ic] (-1 for rows listed for
+// the global tier), and a gather then moves the rows into place.
+template <bool GLOBAL, bool FILL, bool FUSED = false>
 __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f, const int *__restrict__ f2c,
                                             const int *__restrict__ Si, const int *__restrict__ Sj,
                                             const int *__restrict__ CF, int *__restrict__ cnt,
                                             const int *__restrict__ S2i, int *__restrict__ S2j, int *ovf_list,
-                                            int *ovf_n, int *gtab, int gcap, int *err)
+                                            int *ovf_n, int *gtab, int gcap, int *err, int *__restrict__ src)
 {
+   constexpr bool COUNTING = !FILL || FUSED;
    extern __shared__ __align__(16) int sh[];
    const int lane = gb_lane();
    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -88,7 +93,8 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
    {
       int ic = GLOBAL ? ovf_list[t] : t;
       int off = 0;
-      if (FILL)
+      if (FUSED) { off = S2i[ic]; }
+      else if (FILL)
       {
          off = S2i[ic];
          if (!GLOBAL && S2i[ic + 1] - off > T.listcap) { continue; }
@@ -124,8 +130,17 @@ __global__ void __launch_bounds__(128) k_s2(int nc, const int *__restrict__ c2f,
       }
       if (lane == 0)
       {
-         if (!ovf) { if (!FILL) { cnt[ic] = count; } }
-         else if (!GLOBAL && !FILL) { ovf_list[atomicAdd(ovf_n, 1)] = ic; cnt[ic] = 0; }
+         if (!ovf)
+         {
+            if (COUNTING) { cnt[ic] = count; }
+            if (FUSED) { src[ic] = off; }
+         }
+         else if (!GLOBAL && COUNTING)
+         {
+            ovf_list[atomicAdd(ovf_n, 1)] = ic;
+            cnt[ic] = 0;
+            if (FUSED) { src[ic] = -1; }
+         }
          else { atomicExch(err, 1); }
       }
       gb_tab_clear(T, count);
@@ -142,23 +157,48 @@ static int smem_blocks(int nrows)
    return (int) (want < maxb ? (want < 1 ? 1 : want) : maxb);
 }
 
+// fill: 0 count, 1 fill (at S2i), 2 count and fill into temporary areas
+// (tier 0 only; src receives each row's area)
 extern "C" void gb_strength2(int nc, const int *c2f, const int *f2c, const int *Si, const int *Sj, const int *CF,
                              int *cnt, const int *S2i, int *S2j, int *ovf_list, int *ovf_n, int *gtab, int gcap,
-                             int gwarps, int *err, int fill, int tier, cudaStream_t s)
+                             int gwarps, int *err, int *src, int fill, int tier, cudaStream_t s)
 {
+#define GB_S2_ARGS(gt, gc) nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, gt, gc, err, src
    if (tier == 0)
    {
       int blocks = smem_blocks(nc);
-      if (!fill) { k_s2<false, false><<<blocks, 128, GB_SMEMC_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
-      else { k_s2<false, true><<<blocks, 128, GB_SMEMC_BYTES, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, nullptr, 0, err); }
+      if (fill == 0) { k_s2<false, false><<<blocks, 128, GB_SMEMC_BYTES, s>>>(GB_S2_ARGS(nullptr, 0)); }
+      else if (fill == 1) { k_s2<false, true><<<blocks, 128, GB_SMEMC_BYTES, s>>>(GB_S2_ARGS(nullptr, 0)); }
+      else { k_s2<false, true, true><<<blocks, 128, GB_SMEMC_BYTES, s>>>(GB_S2_ARGS(nullptr, 0)); }
    }
    else
    {
       int blocks = (gwarps + 3) / 4;
-      if (!fill) { k_s2<true, false><<<blocks, 128, 0, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, gtab, gcap, err); }
-      else { k_s2<true, true><<<blocks, 128, 0, s>>>(nc, c2f, f2c, Si, Sj, CF, cnt, S2i, S2j, ovf_list, ovf_n, gtab, gcap, err); }
+      if (!fill) { k_s2<true, false><<<blocks, 128, 0, s>>>(GB_S2_ARGS(gtab, gcap)); }
+      else { k_s2<true, true><<<blocks, 128, 0, s>>>(GB_S2_ARGS(gtab, gcap)); }
    }
+#undef GB_S2_ARGS
    GB_COUNT(1);
+}
+
+// cap[r] = min(ub[r], lcap); *sum accumulates the capped sizes
+__global__ void k_cap_sum(int n, const int *__restrict__ ub, int lcap, int *__restrict__ cap, unsigned long long *sum)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   unsigned long long c = 0;
+   if (r < n)
+   {
+      const int u = ub[r];
+      c = (unsigned long long) (u < lcap ? u : lcap);
+      cap[r] = (int) c;
+   }
+   for (int d = 16; d > 0; d >>= 1) { c += __shfl_down_sync(0xffffffffu, c, d); }
+   if ((threadIdx.x & 31) == 0 && c) { atomicAdd(sum, c); }
+}
+
+extern "C" void gb_cap_sum(int n, const int *ub, int lcap, int *cap, unsigned long long *sum, cudaStream_t s)
+{
+   if (n > 0) { k_cap_sum<<<gb_blocks2(n, 256), 256, 0, s>>>(n, ub, lcap, cap, sum); GB_COUNT(1); }
 }
 
 // upper bound of an S2 row: |S_i1| + sum |S_i2|

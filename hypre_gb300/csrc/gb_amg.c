@@ -283,8 +283,7 @@ static int spgemm_fused(const gb_csr *A, const gb_csr *B, int square, gb_csr *C,
    int *over = (int *) gb_dcalloc(sizeof(int) * 2);
    unsigned long long *sum = (unsigned long long *) gb_dcalloc(sizeof(unsigned long long));
    if (!ub || !cap || !over || !sum) { gb_dfree(ub); gb_dfree(cap); gb_dfree(over); gb_dfree(sum); return -1; }
-   gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
-   gb_spgemm_cap(n, ub, GB_SPGEMM_LCAP0, cap, sum, over, s);
+   gb_spgemm_cap(n, B->nc, square, A->i, A->j, B->i, GB_SPGEMM_LCAP0, ub, cap, sum, over, s);
    unsigned long long hsum = 0;
    cudaMemcpyAsync(&hsum, sum, sizeof(hsum), cudaMemcpyDeviceToHost, s);
    int hover = read_int(over);
@@ -596,29 +595,43 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 + 1));
    gb_tier t;
    tier_begin(&t, nc1);
-   gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, NULL, NULL, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 0, 0, s);
-   int *ub = NULL;
-   if (read_int(t.ovf_n) > 0)
-   {
-      ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 > 0 ? nc1 : 1));
-      gb_strength2_ub(nc1, c2f1, S->i, S->j, ub, s);
-   }
+   /* count and fill in one pass into temporary areas sized by each row's
+    * upper bound (capped by the shared-memory table), then the rows that did
+    * not fit with global tables (count, then fill in place) */
+   int *ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 > 0 ? nc1 : 1));
+   int *cap = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 + 1));
+   unsigned long long *dsum = (unsigned long long *) gb_dcalloc(sizeof(unsigned long long));
+   gb_strength2_ub(nc1, c2f1, S->i, S->j, ub, s);
+   gb_cap_sum(nc1, ub, GB_SPGEMM_LCAP0, cap, dsum, s);
+   unsigned long long hsum = 0;
+   cudaMemcpyAsync(&hsum, dsum, sizeof(hsum), cudaMemcpyDeviceToHost, s);
+   gb_sync();
+   gb_dfree(dsum);
+   if (hsum > 0x7fffff00ULL) { gb_error(HYPRE_ERROR_MEMORY, "second-order strength: temporary areas"); return -1; }
+   int *tofs = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 + 1));
+   scan_total(cap, tofs, nc1);
+   gb_dfree(cap);
+   int *tj = (int *) gb_dmalloc(sizeof(int) * (size_t) (hsum > 0 ? hsum : 1));
+   int *src = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 > 0 ? nc1 : 1));
+   gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, tofs, tj, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, src, 2, 0,
+                s);
    tier_global(&t, ub, nc1);
    if (t.h_ovf > 0)
    {
       gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, NULL, NULL, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
-                   t.err, 0, 1, s);
+                   t.err, NULL, 0, 1, s);
    }
    gb_mark_isolated(nc1, c2f1, cnt, CF, s);
    S2.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 + 1));
    S2.nnz = scan_total(cnt, S2.i, nc1);
    S2.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (S2.nnz ? S2.nnz : 1));
-   gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, S2.i, S2.j, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 1, 0, s);
+   gb_spgemm_gather(nc1, S2.i, src, tj, NULL, S2.j, NULL, s);
    if (t.h_ovf > 0)
    {
       gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, S2.i, S2.j, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
-                   t.err, 1, 1, s);
+                   t.err, NULL, 1, 1, s);
    }
+   gb_dfree(tofs); gb_dfree(tj); gb_dfree(src);
    if (tier_end(&t)) { gb_error(HYPRE_ERROR_GENERIC, "second-order strength overflow"); return -1; }
    gb_dfree(ub);
    /* PMIS on S2 with CF_init 3 */

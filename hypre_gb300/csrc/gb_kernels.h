@@ -96,7 +96,8 @@ void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const
 /* phase 2 (tiers 0 and 1): count and fill in one pass into temporary areas
  * (tier 0 at Ci[r], tier 1 at fbase + t * 1536), cnt[r] and src[r] set;
  * gb_spgemm_cap sizes the areas, gb_spgemm_gather moves rows into place */
-void gb_spgemm_cap(int n, const int *ub, int lcap0, int *cap, unsigned long long *sum, int *over, cudaStream_t s);
+void gb_spgemm_cap(int n, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int lcap0, int *ub,
+                   int *cap, unsigned long long *sum, int *over, cudaStream_t s);
 void gb_spgemm_gather(int n, const int *Ci, const int *src, const int *tj, const double *tv, int *Cj, double *Cv,
                       cudaStream_t s);
 void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi, const int *Bj,
@@ -114,7 +115,8 @@ void gb_list_flags(int nlist, const int *list, int *flag, cudaStream_t s);
 void gb_scatter_list(int n, const int *flag, const int *scan, int *list, cudaStream_t s);
 void gb_strength2(int nc, const int *c2f, const int *f2c, const int *Si, const int *Sj, const int *CF, int *cnt,
                   const int *S2i, int *S2j, int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err,
-                  int fill, int tier, cudaStream_t s);
+                  int *src, int fill, int tier, cudaStream_t s);
+void gb_cap_sum(int n, const int *ub, int lcap, int *cap, unsigned long long *sum, cudaStream_t s);
 void gb_strength2_ub(int nc, const int *c2f, const int *Si, const int *Sj, int *ub, cudaStream_t s);
 void gb_mark_isolated(int nc, const int *c2f, const int *cnt, int *CF, cudaStream_t s);
 void gb_correct_cf2(int n, const int *f2c, const int *CFN, int *CF, cudaStream_t s);

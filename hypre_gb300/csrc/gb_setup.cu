@@ -1492,9 +1492,11 @@ extern "C" void gb_spgemm(int nrows, int square, int W, const int *Ai, const int
    GB_COUNT(1);
 }
 
-// temporary areas of the fused products: cap[r] = min(ub[r], lcap0); *sum
-// accumulates the capped sizes, *over counts the rows whose bound exceeds lcap0
-__global__ void k_spgemm_cap(int n, const int *__restrict__ ub, int lcap0, int *__restrict__ cap,
+// temporary areas of the fused products: ub[r] = the row's product count
+// (as k_spgemm_ub), cap[r] = min(ub[r], lcap0); *sum accumulates the capped
+// sizes, *over counts the rows whose bound exceeds lcap0
+__global__ void k_spgemm_cap(int n, int ncols, int square, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                             const int *__restrict__ Bi, int lcap0, int *__restrict__ ub, int *__restrict__ cap,
                              unsigned long long *sum, int *over)
 {
    const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1502,7 +1504,10 @@ __global__ void k_spgemm_cap(int n, const int *__restrict__ ub, int lcap0, int *
    int o = 0;
    if (r < n)
    {
-      const int u = ub[r];
+      long long u = square ? 1 : 0;
+      for (int ka = Ai[r]; ka < Ai[r + 1]; ka++) { const int k = Aj[ka]; u += Bi[k + 1] - Bi[k]; }
+      if (u > ncols) { u = ncols; }
+      ub[r] = (int) u;
       c = (unsigned long long) (u < lcap0 ? u : lcap0);
       o = u > lcap0;
       cap[r] = (int) c;
@@ -1519,14 +1524,19 @@ __global__ void k_spgemm_cap(int n, const int *__restrict__ ub, int lcap0, int *
    }
 }
 
-extern "C" void gb_spgemm_cap(int n, const int *ub, int lcap0, int *cap, unsigned long long *sum, int *over,
-                              cudaStream_t s)
+extern "C" void gb_spgemm_cap(int n, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int lcap0,
+                              int *ub, int *cap, unsigned long long *sum, int *over, cudaStream_t s)
 {
-   if (n > 0) { k_spgemm_cap<<<gb_blocks(n, 256), 256, 0, s>>>(n, ub, lcap0, cap, sum, over); GB_COUNT(1); }
+   if (n > 0)
+   {
+      k_spgemm_cap<<<gb_blocks(n, 256), 256, 0, s>>>(n, ncols, square, Ai, Aj, Bi, lcap0, ub, cap, sum, over);
+      GB_COUNT(1);
+   }
 }
 
 // one warp per row: the row's cnt entries from its temporary area src[r]
-// (rows with src[r] < 0 were filled in place by the global-table tier)
+// (rows with src[r] < 0 were filled in place by the global-table tier;
+// tv NULL: column indices only)
 __global__ void k_spgemm_gather(int n, const int *__restrict__ Ci, const int *__restrict__ src,
                                 const int *__restrict__ tj, const double *__restrict__ tv, int *__restrict__ Cj,
                                 double *__restrict__ Cv)
@@ -1540,7 +1550,7 @@ __global__ void k_spgemm_gather(int n, const int *__restrict__ Ci, const int *__
    for (int q = lane; q < l; q += 32)
    {
       Cj[d + q] = tj[o + q];
-      Cv[d + q] = tv[o + q];
+      if (tv) { Cv[d + q] = tv[o + q]; }
    }
 }
 
