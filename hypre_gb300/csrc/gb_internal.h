@@ -124,7 +124,6 @@ void       gb_parvec_free(gb_parvec *v);
 /* y = alpha*A*x + beta*y on the library stream, FP64 */
 void gb_matvec(double alpha, gb_parcsr *A, const double *x, double beta, double *y);
 double gb_dot(long long n, const double *x, const double *y);     /* synchronises */
-double gb_axpy_dot(long long n, double a, const double *x, double *y, const double *z);   /* y += a x; (z, y) */
 
 /* --- BoomerAMG ----------------------------------------------------------- */
 typedef struct
@@ -223,6 +222,7 @@ typedef struct
    double              *r, *p, *s, *w;
    double             **V, **Z;
    int                  nV;
+   double              *hdev, *hhost;   /* one Hessenberg column: device and pinned host */
    /* multi-vector PCG (gb_multi.c); last_multi: the last solve had multi-vectors */
    int                  last_multi;
    int                  m_nv, m_n;

@@ -205,6 +205,8 @@ void gb_scaled_copy_f(long long n, float w, const float *f, float *v, cudaStream
 void gb_d2f(long long n, const double *a, float *b, cudaStream_t s);
 void gb_f2d(long long n, const float *a, double *b, cudaStream_t s);
 void gb_dot_d(long long n, const double *x, const double *y, double *part, double *out, cudaStream_t s);
+void gb_axpy_dot_dev_d(long long n, const double *h, const double *x, double *y, const double *z, double *part,
+                       double *out, cudaStream_t s);
 void gb_axpy_dot_d(long long n, double a, const double *x, double *y, const double *z, double *part, double *out,
                    cudaStream_t s);
 void gb_dot2_d(long long n, const double *x, const double *y, const double *z, double *part, double *out,

@@ -25,6 +25,9 @@ static void kry_free_work(gb_krylov *k)
    for (int i = 0; i < k->nV; i++) { gb_dfree(k->V[i]); gb_dfree(k->Z[i]); }
    free(k->V); free(k->Z);
    k->V = k->Z = NULL;
+   gb_dfree(k->hdev);
+   gb_hfree_pinned(k->hhost);
+   k->hdev = k->hhost = NULL;
    k->nV = 0;
    k->n = 0;
 }
@@ -84,6 +87,8 @@ static void ensure_work(gb_krylov *k, int n, int nbasis)
       k->Z = (double **) calloc((size_t) nbasis, sizeof(double *));
       for (int i = 0; i < nbasis; i++) { k->V[i] = (double *) gb_dcalloc(nb); k->Z[i] = (double *) gb_dcalloc(nb); }
       k->nV = nbasis;
+      k->hdev = (double *) gb_dcalloc(sizeof(double) * (size_t) (nbasis + 1));
+      k->hhost = (double *) gb_hmalloc_pinned(sizeof(double) * (size_t) (nbasis + 1));
    }
    k->n = n;
 }
@@ -231,15 +236,20 @@ static int fgmres_solve(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
          gb_parvec pin = wrap_vec(p[i - 1], n), zout = wrap_vec(pre[i - 1], n);
          apply_precond(k, A, &pin, &zout);
          gb_spmv_d(Ad, pre[i - 1], p[i], 0, 1.0, 0.0, NULL, NULL, 0.0, NULL, NULL, st);
-         /* modified Gram-Schmidt; each update of p[i] is fused with the
-          * next inner product (with p[j+1], or p[i]'s own norm at the end) */
-         double hj = gb_dot(n, p[0], p[i]);
+         /* modified Gram-Schmidt on the device: h_0 = (p_0, p_i), then each
+          * update p_i -= h_j p_j (h_j read from device memory) is fused with
+          * the next inner product (with p_{j+1}, or p_i's own norm at the
+          * end); the column comes back to the host once */
+         gb_dot_d(n, p[0], p[i], gb_red_part(), k->hdev, st);
          for (int j = 0; j < i; j++)
          {
-            HH(j, i - 1) = hj;
-            hj = gb_axpy_dot(n, -hj, p[j], p[i], j + 1 < i ? p[j + 1] : p[i]);
+            gb_axpy_dot_dev_d(n, k->hdev + j, p[j], p[i], j + 1 < i ? p[j + 1] : p[i], gb_red_part(),
+                              k->hdev + j + 1, st);
          }
-         double t = sqrt(hj);
+         cudaMemcpyAsync(k->hhost, k->hdev, sizeof(double) * (size_t) (i + 1), cudaMemcpyDeviceToHost, st);
+         gb_sync();
+         for (int j = 0; j < i; j++) { HH(j, i - 1) = k->hhost[j]; }
+         double t = sqrt(k->hhost[i]);
          HH(i, i - 1) = t;
          if (t != 0.0) { gb_scale_d(n, 1.0 / t, p[i], st); }
          for (int j = 1; j < i; j++)

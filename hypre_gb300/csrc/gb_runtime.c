@@ -172,16 +172,6 @@ double gb_dot(long long n, const double *x, const double *y)
    return gb_red_host()[0];
 }
 
-/* y += a x, then (z, y); synchronises */
-double gb_axpy_dot(long long n, double a, const double *x, double *y, const double *z)
-{
-   cudaStream_t s = gb_stream();
-   gb_axpy_dot_d(n, a, x, y, z, gb_red_part(), gb_red_out(), s);
-   cudaMemcpyAsync(gb_red_host(), gb_red_out(), sizeof(double), cudaMemcpyDeviceToHost, s);
-   gb_sync();
-   return gb_red_host()[0];
-}
-
 /* ---------------------------------------------------------------------------
  * Public runtime API
  * ------------------------------------------------------------------------- */

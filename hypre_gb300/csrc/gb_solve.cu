@@ -768,6 +768,32 @@ extern "C" void gb_dot_d(long long n, const double *x, const double *y, double *
    k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
    GB_COUNT(2);
 }
+// as k_axpy_dot_part with a = -(*h), read from device memory (the previous
+// inner product, so the Gram-Schmidt chain needs no host round trip)
+__global__ void __launch_bounds__(256) k_axpy_dot_dev_part(long long n, const double *__restrict__ h,
+                                                           const double *__restrict__ x, double *y, const double *z,
+                                                           double *__restrict__ part)
+{
+   const double a = -(*h);
+   double s = 0.0;
+   for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+   {
+      double yi = y[i] + a * x[i];
+      y[i] = yi;
+      s += z[i] * yi;
+   }
+   double t = block_sum<double>(s);
+   if (threadIdx.x == 0) { part[blockIdx.x] = t; }
+}
+
+extern "C" void gb_axpy_dot_dev_d(long long n, const double *h, const double *x, double *y, const double *z,
+                                  double *part, double *out, cudaStream_t s)
+{
+   k_axpy_dot_dev_part<<<GB_RED_BLOCKS, 256, 0, s>>>(n, h, x, y, z, part);
+   k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
+   GB_COUNT(2);
+}
+
 extern "C" void gb_axpy_dot_d(long long n, double a, const double *x, double *y, const double *z, double *part,
                               double *out, cudaStream_t s)
 {
