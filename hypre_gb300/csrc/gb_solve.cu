@@ -223,19 +223,29 @@ __global__ void k_sell_ptr_blocks(int nslices, const int *__restrict__ w, long l
    if (threadIdx.x == blockDim.x - 1) { bsum[blockIdx.x] = excl + v; }
 }
 
+// block b adds the sum of the earlier blocks' totals to its 1024 slice
+// offsets; the last block also writes the total
 __global__ void k_sell_ptr_fix(int nslices, long long *__restrict__ ptr, const long long *__restrict__ bsum,
                                int nblocks)
 {
-   // one block: exclusive scan of the block sums (nblocks small), then add
-   __shared__ long long off[1024];
-   if (threadIdx.x == 0)
+   __shared__ long long red[32];
+   long long a = 0;
+   for (int k = threadIdx.x; k < (int) blockIdx.x; k += blockDim.x) { a += bsum[k]; }
+   for (int o = 16; o > 0; o >>= 1) { a += __shfl_down_sync(GB_FULL, a, o); }
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   if (lane == 0) { red[wid] = a; }
+   __syncthreads();
+   if (wid == 0)
    {
-      long long a = 0;
-      for (int b = 0; b < nblocks; b++) { off[b] = a; a += bsum[b]; }
-      ptr[nslices] = a;
+      a = lane < (int) (blockDim.x >> 5) ? red[lane] : 0;
+      for (int o = 16; o > 0; o >>= 1) { a += __shfl_down_sync(GB_FULL, a, o); }
+      if (lane == 0) { red[0] = a; }
    }
    __syncthreads();
-   for (int s = threadIdx.x; s < nslices; s += blockDim.x) { ptr[s] += off[s / 1024]; }
+   const long long off = red[0];
+   const int s = blockIdx.x * 1024 + threadIdx.x;
+   if (s < nslices) { ptr[s] += off; }
+   if (blockIdx.x == nblocks - 1 && threadIdx.x == 0) { ptr[nslices] = off + bsum[blockIdx.x]; }
 }
 
 __global__ void k_sell_fill_j(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj,
@@ -393,7 +403,7 @@ extern "C" void gb_sell_struct(int n, const int *Ai, const int *Aj, int lower, i
       long long *bsum = NULL;
       cudaMallocAsync((void **) &bsum, sizeof(long long) * (size_t) nb, s);
       k_sell_ptr_blocks<<<nb, 1024, 0, s>>>(nslices, sl_w, sl_ptr, bsum);
-      k_sell_ptr_fix<<<1, 1024, 0, s>>>(nslices, sl_ptr, bsum, nb);
+      k_sell_ptr_fix<<<nb, 1024, 0, s>>>(nslices, sl_ptr, bsum, nb);
       cudaFreeAsync(bsum, s);
       GB_COUNT(3);
       return;
