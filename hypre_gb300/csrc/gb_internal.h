@@ -35,6 +35,7 @@ double gb_wtime(void);
 void *gb_scratch(int slot, size_t bytes);
 double *gb_red_part(void);                   /* GB_RED_BLOCKS * 4 doubles */
 double *gb_red_out(void);                    /* 8 doubles (device) */
+unsigned int *gb_red_count(void);            /* zeroed counter of one-launch reductions */
 double *gb_red_host(void);                   /* 8 doubles (pinned host) */
 void  gb_release_scratch(void);
 

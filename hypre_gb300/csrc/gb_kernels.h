@@ -204,9 +204,12 @@ void gb_scaled_copy_d(long long n, double w, const double *f, double *v, cudaStr
 void gb_scaled_copy_f(long long n, float w, const float *f, float *v, cudaStream_t s);
 void gb_d2f(long long n, const double *a, float *b, cudaStream_t s);
 void gb_f2d(long long n, const float *a, double *b, cudaStream_t s);
-void gb_dot_d(long long n, const double *x, const double *y, double *part, double *out, cudaStream_t s);
+/* dot products in one launch: the last block to finish sums the partials
+ * (count: a zeroed counter, reset by that block) */
+void gb_dot_d(long long n, const double *x, const double *y, double *part, unsigned int *count, double *out,
+              cudaStream_t s);
 void gb_axpy_dot_dev_d(long long n, const double *h, const double *x, double *y, const double *z, double *part,
-                       double *out, cudaStream_t s);
+                       unsigned int *count, double *out, cudaStream_t s);
 void gb_axpy_dot_d(long long n, double a, const double *x, double *y, const double *z, double *part, double *out,
                    cudaStream_t s);
 void gb_dot2_d(long long n, const double *x, const double *y, const double *z, double *part, double *out,

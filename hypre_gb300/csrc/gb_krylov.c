@@ -240,11 +240,11 @@ static int fgmres_solve(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
           * update p_i -= h_j p_j (h_j read from device memory) is fused with
           * the next inner product (with p_{j+1}, or p_i's own norm at the
           * end); the column comes back to the host once */
-         gb_dot_d(n, p[0], p[i], gb_red_part(), k->hdev, st);
+         gb_dot_d(n, p[0], p[i], gb_red_part(), gb_red_count(), k->hdev, st);
          for (int j = 0; j < i; j++)
          {
             gb_axpy_dot_dev_d(n, k->hdev + j, p[j], p[i], j + 1 < i ? p[j + 1] : p[i], gb_red_part(),
-                              k->hdev + j + 1, st);
+                              gb_red_count(), k->hdev + j + 1, st);
          }
          cudaMemcpyAsync(k->hhost, k->hdev, sizeof(double) * (size_t) (i + 1), cudaMemcpyDeviceToHost, st);
          gb_sync();

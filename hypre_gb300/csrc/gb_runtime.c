@@ -19,6 +19,7 @@ static int g_verbose_errors = -1;
 static void *g_scratch[GB_NSCRATCH];
 static size_t g_scratch_sz[GB_NSCRATCH];
 static double *g_red_part = NULL, *g_red_out = NULL, *g_red_host = NULL;
+static unsigned int *g_red_count = NULL;
 
 void gb_count_launch(int n) { g_launches += n; }
 
@@ -152,11 +153,13 @@ static void red_init(void)
       g_red_part = (double *) gb_dmalloc(sizeof(double) * GB_RED_BLOCKS * 4);
       g_red_out = (double *) gb_dmalloc(sizeof(double) * 8);
       g_red_host = (double *) gb_hmalloc_pinned(sizeof(double) * 8);
+      g_red_count = (unsigned int *) gb_dcalloc(sizeof(unsigned int) * 4);
    }
 }
 double *gb_red_part(void) { red_init(); return g_red_part; }
 double *gb_red_out(void) { red_init(); return g_red_out; }
 double *gb_red_host(void) { red_init(); return g_red_host; }
+unsigned int *gb_red_count(void) { red_init(); return g_red_count; }
 
 void gb_release_scratch(void)
 {
@@ -166,7 +169,7 @@ void gb_release_scratch(void)
 double gb_dot(long long n, const double *x, const double *y)
 {
    cudaStream_t s = gb_stream();
-   gb_dot_d(n, x, y, gb_red_part(), gb_red_out(), s);
+   gb_dot_d(n, x, y, gb_red_part(), gb_red_count(), gb_red_out(), s);
    cudaMemcpyAsync(gb_red_host(), gb_red_out(), sizeof(double), cudaMemcpyDeviceToHost, s);
    gb_sync();
    return gb_red_host()[0];
@@ -187,8 +190,8 @@ HYPRE_Int HYPRE_Finalize(void)
    {
       cudaStreamSynchronize(g_stream);
       gb_release_scratch();
-      if (g_red_part) { gb_dfree(g_red_part); gb_dfree(g_red_out); gb_hfree_pinned(g_red_host); }
-      g_red_part = NULL; g_red_out = NULL; g_red_host = NULL;
+      if (g_red_part) { gb_dfree(g_red_part); gb_dfree(g_red_out); gb_hfree_pinned(g_red_host); gb_dfree(g_red_count); }
+      g_red_part = NULL; g_red_out = NULL; g_red_host = NULL; g_red_count = NULL;
       cudaStreamSynchronize(g_stream);
       if (g_own_stream) { cudaStreamDestroy(g_stream); g_stream = 0; g_own_stream = 0; }
       g_initialized = 0;

@@ -772,17 +772,82 @@ extern "C" void gb_vmul_d(long long n, const double *a, const double *b, double 
 extern "C" void gb_vmul_f(long long n, const float *a, const float *b, float *c, cudaStream_t s)
 { if (n > 0) { k_vmul<float><<<nblk(n, 256), 256, 0, s>>>(n, a, b, c); GB_COUNT(1); } }
 
-extern "C" void gb_dot_d(long long n, const double *x, const double *y, double *part, double *out, cudaStream_t s)
+// Sum of nparts block partials in the order and tree of k_final_sum (1024
+// threads: thread v adds part[v], part[v + 1024], ... from 0, then
+// block_sum), computed by one block of 256 threads that each carry the
+// virtual threads t, t+256, t+512, t+768 -- the same lanes, so every warp
+// shuffle pairs the same values and the result is bit for bit k_final_sum's.
+// Valid in thread 0.
+__device__ double final_sum_1024(const double *part, int nparts)
 {
-   k_dot_part<<<GB_RED_BLOCKS, 256, 0, s>>>(n, x, y, part);
-   k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
-   GB_COUNT(2);
+   __shared__ double red[32];
+   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+   double sk[4];
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+   {
+      double a = 0.0;
+      for (int b = t + 256 * k; b < nparts; b += 1024) { a += __ldcg(part + b); }
+      sk[k] = a;
+   }
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+   {
+      for (int o = 16; o > 0; o >>= 1) { sk[k] += __shfl_down_sync(GB_FULL, sk[k], o); }
+   }
+   __syncthreads();
+   if (lane == 0)
+   {
+#pragma unroll
+      for (int k = 0; k < 4; k++) { red[w + 8 * k] = sk[k]; }
+   }
+   __syncthreads();
+   double r = 0.0;
+   if (w == 0)
+   {
+      r = red[lane];
+      for (int o = 16; o > 0; o >>= 1) { r += __shfl_down_sync(GB_FULL, r, o); }
+   }
+   return r;
 }
-// as k_axpy_dot_part with a = -(*h), read from device memory (the previous
-// inner product, so the Gram-Schmidt chain needs no host round trip)
-__global__ void __launch_bounds__(256) k_axpy_dot_dev_part(long long n, const double *__restrict__ h,
-                                                           const double *__restrict__ x, double *y, const double *z,
-                                                           double *__restrict__ part)
+
+// the block that finishes last (a counter after a fence) sums the partials
+// and resets the counter: one launch per reduction
+__device__ __forceinline__ void finish_sum(double t, double *part, unsigned int *count, double *out)
+{
+   __shared__ int last;
+   if (threadIdx.x == 0)
+   {
+      part[blockIdx.x] = t;
+      __threadfence();
+      last = atomicAdd(count, 1u) == gridDim.x - 1;
+   }
+   __syncthreads();
+   if (!last) { return; }
+   __threadfence();
+   double r = final_sum_1024(part, gridDim.x);
+   if (threadIdx.x == 0) { *out = r; *count = 0u; }
+}
+
+// (x, y) in one launch, the sum as k_dot_part + k_final_sum
+__global__ void __launch_bounds__(256) k_dot_fin(long long n, const double *__restrict__ x,
+                                                 const double *__restrict__ y, double *part, unsigned int *count,
+                                                 double *out)
+{
+   double s = 0.0;
+   for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+   {
+      s += x[i] * y[i];
+   }
+   finish_sum(block_sum<double>(s), part, count, out);
+}
+
+// y -= (*h) x, then (z, y) in one launch (the sum as k_axpy_dot_part +
+// k_final_sum); h is read from device memory (the previous inner product, so
+// the Gram-Schmidt chain needs no host round trip)
+__global__ void __launch_bounds__(256) k_axpy_dot_dev_fin(long long n, const double *__restrict__ h,
+                                                          const double *__restrict__ x, double *y, const double *z,
+                                                          double *part, unsigned int *count, double *out)
 {
    const double a = -(*h);
    double s = 0.0;
@@ -792,16 +857,21 @@ __global__ void __launch_bounds__(256) k_axpy_dot_dev_part(long long n, const do
       y[i] = yi;
       s += z[i] * yi;
    }
-   double t = block_sum<double>(s);
-   if (threadIdx.x == 0) { part[blockIdx.x] = t; }
+   finish_sum(block_sum<double>(s), part, count, out);
+}
+
+extern "C" void gb_dot_d(long long n, const double *x, const double *y, double *part, unsigned int *count,
+                         double *out, cudaStream_t s)
+{
+   k_dot_fin<<<GB_RED_BLOCKS, 256, 0, s>>>(n, x, y, part, count, out);
+   GB_COUNT(1);
 }
 
 extern "C" void gb_axpy_dot_dev_d(long long n, const double *h, const double *x, double *y, const double *z,
-                                  double *part, double *out, cudaStream_t s)
+                                  double *part, unsigned int *count, double *out, cudaStream_t s)
 {
-   k_axpy_dot_dev_part<<<GB_RED_BLOCKS, 256, 0, s>>>(n, h, x, y, z, part);
-   k_final_sum<<<1, 1024, 0, s>>>(GB_RED_BLOCKS, 1, part, out);
-   GB_COUNT(2);
+   k_axpy_dot_dev_fin<<<GB_RED_BLOCKS, 256, 0, s>>>(n, h, x, y, z, part, count, out);
+   GB_COUNT(1);
 }
 
 extern "C" void gb_axpy_dot_d(long long n, double a, const double *x, double *y, const double *z, double *part,
