@@ -34,17 +34,20 @@ __global__ void k_scatter_list(int n, const int *__restrict__ flag, const int *_
    if (i < n && flag[i]) { list[scan[i]] = i; }
 }
 
-// flag[list[t]] = 1 for the nlist distinct entries of a row list
-__global__ void k_list_flags(int nlist, const int *__restrict__ list, int *__restrict__ flag)
+// flag[list[t]] = 1 for the distinct entries of a row list: nlist of them,
+// or *dcount when given (at most nlist)
+__global__ void k_list_flags(int nlist, const int *__restrict__ dcount, const int *__restrict__ list,
+                             int *__restrict__ flag)
 {
-   int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t < nlist) { flag[list[t]] = 1; }
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   const int m = dcount ? *dcount : nlist;
+   if (t < m) { flag[list[t]] = 1; }
 }
 
-extern "C" void gb_list_flags(int nlist, const int *list, int *flag, cudaStream_t s)
+extern "C" void gb_list_flags(int nlist, const int *dcount, const int *list, int *flag, cudaStream_t s)
 {
    if (nlist <= 0) { return; }
-   k_list_flags<<<gb_blocks2(nlist, 256), 256, 0, s>>>(nlist, list, flag);
+   k_list_flags<<<gb_blocks2(nlist, 256), 256, 0, s>>>(nlist, dcount, list, flag);
    GB_COUNT(1);
 }
 

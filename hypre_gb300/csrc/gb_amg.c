@@ -122,18 +122,21 @@ static int scan_total(const int *in, int *out, int n)
 /* Rewrites a list of distinct rows of 0..n-1 in increasing order (flags,
  * scan, scatter): the warps of the next tier then work on neighbouring rows
  * at the same time, whose B rows share the L2. */
-static void sort_row_list(int *list, int nlist, int n)
+static void sort_row_list_n(int *list, int nlist, const int *dcount, int n)
 {
    if (nlist <= 1) { return; }
    cudaStream_t s = gb_stream();
    int *flag = (int *) gb_dcalloc(sizeof(int) * (size_t) (n + 1));
    int *pos = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    if (!flag || !pos) { gb_dfree(flag); gb_dfree(pos); return; }
-   gb_list_flags(nlist, list, flag, s);
-   scan_total(flag, pos, n);
+   gb_list_flags(nlist, dcount, list, flag, s);
+   int *scr = (int *) gb_scratch(0, sizeof(int) * (size_t) gb_scan_scratch_ints(n > 0 ? n : 1));
+   gb_exclusive_scan(flag, pos, n, scr, s);
    gb_scatter_list(n, flag, pos, list, s);
    gb_dfree(flag); gb_dfree(pos);
 }
+
+static void sort_row_list(int *list, int nlist, int n) { sort_row_list_n(list, nlist, NULL, n); }
 
 static int max_of(const int *d, int n)
 {
@@ -204,12 +207,17 @@ typedef struct
    int  gcap, gwarps;
 } gb_tier;
 
+/* one device flag for every tier of a setup: a table that overflows even its
+ * last tier sets it; the setup reads it once at its end */
+static int *g_tier_err = NULL;
+
 static void tier_begin(gb_tier *t, int nrows)
 {
    memset(t, 0, sizeof(*t));
    t->ovf_list = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows > 0 ? nrows : 1));
    t->ovf_n = (int *) gb_dcalloc(sizeof(int) * 2);
-   t->err = (int *) gb_dcalloc(sizeof(int) * 2);
+   if (!g_tier_err) { g_tier_err = (int *) gb_dcalloc(sizeof(int) * 2); }
+   t->err = g_tier_err;
 }
 
 /* after the symbolic shared-memory pass: read the overflow count and, if
@@ -230,8 +238,16 @@ static void tier_global(gb_tier *t, const int *ub, int nub) { tier_global_n(t, u
 
 static int tier_end(gb_tier *t)
 {
-   int e = read_int(t->err);
-   gb_dfree(t->ovf_list); gb_dfree(t->ovf_n); gb_dfree(t->err); gb_dfree(t->gtab);
+   gb_dfree(t->ovf_list); gb_dfree(t->ovf_n); gb_dfree(t->gtab);
+   return 0;
+}
+
+/* the tiers' overflow flag, read (and cleared) once per setup */
+static int tier_errors(void)
+{
+   if (!g_tier_err) { return 0; }
+   int e = read_int(g_tier_err);
+   if (e) { cudaMemsetAsync(g_tier_err, 0, sizeof(int), gb_stream()); }
    return e;
 }
 
@@ -240,7 +256,23 @@ static int tier_end(gb_tier *t)
  * setup (CUDA events on the library stream around each product) */
 static double g_sg_bytes, g_sg_seconds;
 static int g_sg_calls;
-static cudaEvent_t g_sg_ev[2];
+#define GB_SG_EVENTS 96
+static cudaEvent_t g_sg_ev[GB_SG_EVENTS][2];
+static int g_sg_nev;
+
+/* device time of the products recorded since the setup began (one sync) */
+static void spgemm_times_collect(void)
+{
+   if (g_sg_nev == 0) { return; }
+   cudaEventSynchronize(g_sg_ev[g_sg_nev - 1][1]);
+   for (int k = 0; k < g_sg_nev; k++)
+   {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, g_sg_ev[k][0], g_sg_ev[k][1]);
+      g_sg_seconds += ms * 1e-3;
+   }
+   g_sg_nev = 0;
+}
 
 static double csr_bytes(const gb_csr *M) { return 12.0 * (double) M->nnz + 4.0 * ((double) M->nr + 1.0); }
 
@@ -249,17 +281,15 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
 static int spgemm_host(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
 {
    cudaStream_t s = gb_stream();
-   if (!g_sg_ev[0]) { cudaEventCreate(&g_sg_ev[0]); cudaEventCreate(&g_sg_ev[1]); }
-   cudaEventRecord(g_sg_ev[0], s);
+   if (g_sg_nev == GB_SG_EVENTS) { spgemm_times_collect(); }
+   const int k = g_sg_nev++;
+   if (!g_sg_ev[k][0]) { cudaEventCreate(&g_sg_ev[k][0]); cudaEventCreate(&g_sg_ev[k][1]); }
+   cudaEventRecord(g_sg_ev[k][0], s);
    int r = spgemm_host_inner(A, B, square, C);
-   cudaEventRecord(g_sg_ev[1], s);
-   cudaEventSynchronize(g_sg_ev[1]);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, g_sg_ev[0], g_sg_ev[1]);
+   cudaEventRecord(g_sg_ev[k][1], s);
    if (r == 0)
    {
       g_sg_bytes += csr_bytes(A) + csr_bytes(B) + csr_bytes(C);
-      g_sg_seconds += ms * 1e-3;
       g_sg_calls++;
    }
    return r;
@@ -317,34 +347,47 @@ static int spgemm_fused(const gb_csr *A, const gb_csr *B, int square, gb_csr *C,
       gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, tofs, tj, tv, t.ovf_list, t.ovf_n, NULL,
                 NULL, n, NULL, 0, 0, t.err, ub, src, 0, 2, 0, s);
    }
-   int h1 = read_int(t.ovf_n), h2 = 0;
-   if (h1 > 0)
+   /* tier 1 over the rows that did not fit, in row order: areas of 1536
+    * entries after the tier-0 ones.  The list's length stays on the device
+    * (the kernels read it); hover bounds it. */
+   int h2 = 0;
+   if (hover > 0)
    {
-      /* tier 1 over the rows that did not fit, in row order: areas of 1536
-       * entries after the tier-0 ones */
-      sort_row_list(t.ovf_list, h1, n);
-      list2 = (int *) gb_dmalloc(sizeof(int) * (size_t) h1);
+      sort_row_list_n(t.ovf_list, hover, t.ovf_n, n);
+      list2 = (int *) gb_dmalloc(sizeof(int) * (size_t) hover);
       if (rowchunk)
       {
          gb_spgemm_rc(n, square, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, tj, tv, t.ovf_list, t.ovf_n, list2,
-                      n2, h1, t.err, NULL, src, (int) hsum, 2, 1, s);
+                      n2, hover, t.err, NULL, src, (int) hsum, 2, 1, s);
       }
       else
       {
          gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, tj, tv, t.ovf_list, t.ovf_n, list2,
-                   n2, h1, NULL, 0, 0, t.err, NULL, src, (int) hsum, 2, 1, s);
+                   n2, hover, NULL, 0, 0, t.err, NULL, src, (int) hsum, 2, 1, s);
       }
-      h2 = read_int(n2);
+   }
+   /* row pointers; the row total and the global tier's row count come back
+    * together */
+   C->nr = n; C->nc = B->nc;
+   C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   {
+      int *scr = (int *) gb_scratch(0, sizeof(int) * (size_t) gb_scan_scratch_ints(n > 0 ? n : 1));
+      gb_exclusive_scan(cnt, C->i, n, scr, s);
+      int two[2] = {0, 0};
+      cudaMemcpyAsync(&two[0], C->i + n, sizeof(int), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(&two[1], n2, sizeof(int), cudaMemcpyDeviceToHost, s);
+      gb_sync();
+      C->nnz = two[0];
+      h2 = two[1];
    }
    if (h2 > 0)
    {
+      /* rows beyond tier 1: global tables, count, then the row pointers again */
       tier_global_n(&t, ub, n, h2);
       gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, list2, n2, NULL, NULL, h2,
                 t.gtab, t.gcap, t.gwarps, t.err, NULL, NULL, 0, 0, 2, s);
+      C->nnz = scan_total(cnt, C->i, n);
    }
-   C->nr = n; C->nc = B->nc;
-   C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   C->nnz = scan_total(cnt, C->i, n);
    C->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C->nnz ? C->nnz : 1));
    C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
    gb_spgemm_gather(n, C->i, src, tj, tv, C->j, C->v, s);
@@ -1067,6 +1110,7 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    double t_start = gb_wtime();
    g_sg_bytes = g_sg_seconds = 0.0;
    g_sg_calls = 0;
+   g_sg_nev = 0;
 
    memset(amg->setup_times, 0, sizeof(amg->setup_times));
    amg->lev[0].A = A0;
@@ -1154,6 +1198,8 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
       }
    }
    gb_sync();
+   spgemm_times_collect();
+   if (tier_errors()) { gb_error(HYPRE_ERROR_GENERIC, "sparse table overflow in setup"); }
    amg->r_work = (double *) gb_dmalloc(sizeof(double) * (size_t) (amg->lev[0].n ? amg->lev[0].n : 1));
    amg->setup_times[4] = gb_wtime() - t_sm;
    amg->spgemm_bytes = g_sg_bytes;

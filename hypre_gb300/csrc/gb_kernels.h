@@ -111,7 +111,7 @@ void gb_ij_gather(int n, const long long *off, const int *I, const int *scols, c
 void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 /* aggressive coarsening (gb_agg.cu) */
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);
-void gb_list_flags(int nlist, const int *list, int *flag, cudaStream_t s);
+void gb_list_flags(int nlist, const int *dcount, const int *list, int *flag, cudaStream_t s);
 void gb_scatter_list(int n, const int *flag, const int *scan, int *list, cudaStream_t s);
 void gb_strength2(int nc, const int *c2f, const int *f2c, const int *Si, const int *Sj, const int *CF, int *cnt,
                   const int *S2i, int *S2j, int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err,
