@@ -89,6 +89,7 @@ def _declare(L):
         "HYPRE_GB300_GetKernelLaunchCount": [P(C.c_longlong)], "HYPRE_GB300_ResetKernelLaunchCount": [],
         "HYPRE_GB300_BoomerAMGGetSetupTimes": [vp, vp, i32],
         "HYPRE_GB300_BoomerAMGSetCyclePrecision": [vp, i32], "HYPRE_GB300_BoomerAMGSetUseGraph": [vp, i32],
+        "HYPRE_GB300_BoomerAMGSetSetupTables": [vp, i32],
         "HYPRE_GB300_BatchedPCGCreate": [P(vp)], "HYPRE_GB300_BatchedPCGDestroy": [vp],
         "HYPRE_GB300_BatchedPCGSetTol": [vp, f64], "HYPRE_GB300_BatchedPCGSetMaxIter": [vp, i32],
         "HYPRE_GB300_BatchedPCGSetCyclePrecision": [vp, i32],
@@ -286,6 +287,8 @@ class BoomerAMG:
             return L.HYPRE_GB300_BoomerAMGSetCyclePrecision(self.h, value)
         if name == "UseGraph":
             return L.HYPRE_GB300_BoomerAMGSetUseGraph(self.h, value)
+        if name == "SetupTables":
+            return L.HYPRE_GB300_BoomerAMGSetSetupTables(self.h, value)
         return getattr(L, "HYPRE_BoomerAMGSet" + name)(self.h, value)
 
     def num_levels(self):

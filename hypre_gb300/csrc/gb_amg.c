@@ -210,6 +210,9 @@ typedef struct
 /* one device flag for every tier of a setup: a table that overflows even its
  * last tier sets it; the setup reads it once at its end */
 static int *g_tier_err = NULL;
+/* the setup's SetupTables mode 1: every row of the ordered kernels in the
+ * global-memory tier */
+static int g_global_only = 0;
 
 static void tier_begin(gb_tier *t, int nrows)
 {
@@ -403,9 +406,42 @@ static int spgemm_fused(const gb_csr *A, const gb_csr *B, int square, gb_csr *C,
    return 0;
 }
 
+/* every row in global-memory tables (count, then fill) */
+static int spgemm_global(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
+{
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   int *ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_tier t;
+   tier_begin(&t, n);
+   gb_spgemm_ub(n, B->nc, square, A->i, A->j, B->i, ub, s);
+   gb_iota(n, t.ovf_list, t.ovf_n, s);
+   tier_global_n(&t, ub, n, n);
+   if (n > 0)
+   {
+      gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, NULL, NULL, NULL, t.ovf_list, t.ovf_n, NULL,
+                NULL, n, t.gtab, t.gcap, t.gwarps, t.err, NULL, NULL, 0, 0, 2, s);
+   }
+   C->nr = n; C->nc = B->nc;
+   C->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   C->nnz = scan_total(cnt, C->i, n);
+   C->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (C->nnz ? C->nnz : 1));
+   C->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (C->nnz ? C->nnz : 1));
+   if (n > 0)
+   {
+      gb_spgemm(n, square, 0, A->i, A->j, A->v, B->i, B->j, B->v, cnt, C->i, C->j, C->v, t.ovf_list, t.ovf_n, NULL,
+                NULL, n, t.gtab, t.gcap, t.gwarps, t.err, NULL, NULL, 0, 1, 2, s);
+   }
+   tier_end(&t);
+   gb_dfree(ub); gb_dfree(cnt);
+   return 0;
+}
+
 static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_csr *C)
 {
    cudaStream_t s = gb_stream();
+   if (g_global_only) { return spgemm_global(A, B, square, C); }
    {
       const int rc = B->nr > 0 && (long long) B->nnz >= 12LL * (long long) B->nr;
       int f = spgemm_fused(A, B, square, C, rc);
@@ -535,7 +571,7 @@ static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int
    gb_tier t;
    tier_begin(&t, nrows);
    /* thread-per-row only pays off on large levels (many rows, short rows) */
-   int use_thread = nrows >= 65536 && ncols < (1 << 25);
+   int use_thread = nrows >= 65536 && ncols < (1 << 25) && !g_global_only;
    int h1;
    if (use_thread)
    {
@@ -550,7 +586,12 @@ static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int
    int *ub = NULL;
    if (h1 > 0)
    {
-      gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, l1, n1, h1, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 1, s);
+      if (g_global_only) { gb_iota(nrows, t.ovf_list, t.ovf_n, s); }
+      else
+      {
+         gb_extpi_count(nrows, rows, S->i, S->j, CF, cnt, l1, n1, h1, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, 1,
+                        s);
+      }
       if (read_int(t.ovf_n) > 0)
       {
          ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (n > 0 ? n : 1));
@@ -571,8 +612,11 @@ static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int
    if (use_thread) { gb_extpi_fill_t(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, s); }
    if (h1 > 0)
    {
-      gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, l1, n1, h1, NULL, 0, 0,
-                    t.err, 1, s);
+      if (!g_global_only)
+      {
+         gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, l1, n1, h1, NULL, 0, 0,
+                       t.err, 1, s);
+      }
       if (t.h_ovf > 0)
       {
          gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, t.ovf_list, t.ovf_n,
@@ -656,8 +700,16 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    gb_dfree(cap);
    int *tj = (int *) gb_dmalloc(sizeof(int) * (size_t) (hsum > 0 ? hsum : 1));
    int *src = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 > 0 ? nc1 : 1));
-   gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, tofs, tj, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, src, 2, 0,
-                s);
+   if (g_global_only)
+   {
+      gb_iota(nc1, t.ovf_list, t.ovf_n, s);
+      cudaMemsetAsync(src, 0xff, sizeof(int) * (size_t) (nc1 > 0 ? nc1 : 1), s);
+   }
+   else
+   {
+      gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, tofs, tj, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, src, 2,
+                   0, s);
+   }
    tier_global(&t, ub, nc1);
    if (t.h_ovf > 0)
    {
@@ -1111,6 +1163,7 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    g_sg_bytes = g_sg_seconds = 0.0;
    g_sg_calls = 0;
    g_sg_nev = 0;
+   g_global_only = amg->prm.setup_tables == 1;
 
    memset(amg->setup_times, 0, sizeof(amg->setup_times));
    amg->lev[0].A = A0;
@@ -1198,6 +1251,7 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
       }
    }
    gb_sync();
+   g_global_only = 0;
    spgemm_times_collect();
    if (tier_errors()) { gb_error(HYPRE_ERROR_GENERIC, "sparse table overflow in setup"); }
    amg->r_work = (double *) gb_dmalloc(sizeof(double) * (size_t) (amg->lev[0].n ? amg->lev[0].n : 1));
@@ -1645,6 +1699,7 @@ SETTER(HYPRE_BoomerAMGSetChebyEigEst, cheby_eig_est, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetPrintLevel, print_level, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetLogging, logging, HYPRE_Int)
 SETTER(HYPRE_GB300_BoomerAMGSetUseGraph, use_graph, HYPRE_Int)
+SETTER(HYPRE_GB300_BoomerAMGSetSetupTables, setup_tables, HYPRE_Int)
 
 HYPRE_Int HYPRE_BoomerAMGSetMaxLevels(HYPRE_Solver solver, HYPRE_Int v)
 {

@@ -146,6 +146,7 @@ typedef struct
    int    print_level, logging;
    int    cycle_prec;        /* GB_PREC_F64 / F32 / F16 (finest values) */
    int    use_graph;
+   int    setup_tables;      /* 0 automatic tiers, 1 global-memory tables only */
 } gb_amg_params;
 
 typedef struct

@@ -333,6 +333,11 @@ HYPRE_Int HYPRE_GB300_MLPAdamStep(float *params, const float *grad, float *m, fl
 HYPRE_Int HYPRE_GB300_BoomerAMGSetCyclePrecision(HYPRE_Solver solver, HYPRE_Int precision);
 /* Capture each V-cycle as a CUDA graph and replay it (default on). */
 HYPRE_Int HYPRE_GB300_BoomerAMGSetUseGraph(HYPRE_Solver solver, HYPRE_Int use_graph);
+/* Hash tables of the ordered setup kernels (sparse products, second-order
+ * strength, extended+i): 0 = shared-memory tiers first (default), 1 = every
+ * row in global-memory tables (the path long rows take; results are the
+ * same).  No counterpart in the reference. */
+HYPRE_Int HYPRE_GB300_BoomerAMGSetSetupTables(HYPRE_Solver solver, HYPRE_Int mode);
 /* Hierarchy inspection (host copies).  which: 0 = A, 1 = P, 2 = S (pattern).
  * nnz/rows/cols returned; arrays may be NULL to query sizes only. */
 HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCSR(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int which,

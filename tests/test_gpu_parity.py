@@ -70,6 +70,18 @@ def test_hierarchy_aggressive_bitexact(gb, oracle_mod, kind, nx, th, agg):
     _compare_hierarchy(H, amg)
 
 
+@pytest.mark.parametrize("kind,nx,th,agg", [(27, 20, 0.5, 1), (7, 24, 0.25, 1), (7, 12, 0.25, 0)])
+def test_hierarchy_global_tables_bitexact(gb, oracle_mod, kind, nx, th, agg):
+    """Every row of the ordered setup kernels (sparse products, second-order
+    strength, extended+i) in global-memory tables -- the tier that rows too
+    long for shared memory take -- gives the same hierarchy."""
+    O = oracle_mod
+    I, J, V = O.stencil(kind, nx, nx, nx)
+    H, A, amg, bv, xv = _setup_both(gb, O, I, J, V, MaxRowSum=1.0, StrongThreshold=th, AggNumLevels=agg,
+                                    AggInterpType=6, SetupTables=1)
+    _compare_hierarchy(H, amg)
+
+
 def test_aggressive_fgmres_two_stage_gs(gb, oracle_mod):
     """Miniature of the 160^3 configuration: aggressive first level, PMIS 0.5,
     two-stage Gauss-Seidel, FlexGMRES(30)."""
