@@ -396,13 +396,10 @@ __global__ void k_mod_theta(int nf, const int *__restrict__ FFi, const int *__re
    }
 }
 
-extern "C" void gb_mod_extpi_scale(int nf, const int *fl, const int *Ai, const double *Av, const int *FFi,
-                                   const int *FFj, double *FFv, const int *FCi, const double *FCv, double *tmp,
-                                   double *Dq, double *Dw, cudaStream_t s)
+extern "C" void gb_mod_extpi_scale(int nf, int nnzff, const int *fl, const int *Ai, const double *Av,
+                                   const int *FFi, const int *FFj, double *FFv, const int *FCi, const double *FCv,
+                                   double *tmp, double *Dq, double *Dw, cudaStream_t s)
 {
-   int nnzff = 0;
-   cudaMemcpyAsync(&nnzff, FFi + nf, sizeof(int), cudaMemcpyDeviceToHost, s);
-   cudaStreamSynchronize(s);
    cudaMemcpyAsync(tmp, FFv, sizeof(double) * (size_t) nnzff, cudaMemcpyDeviceToDevice, s);
    k_mod_dq_dw<<<gb_blocks2(nf, 256), 256, 0, s>>>(nf, fl, Ai, Av, FFi, FFv, FCi, FCv, Dq, Dw);
    k_mod_theta<<<gb_blocks2(nf, 128), 128, 0, s>>>(nf, FFi, FFj, FFv, tmp, Dq, Dw);

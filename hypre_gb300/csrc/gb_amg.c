@@ -105,10 +105,11 @@ static void amg_free_hierarchy(gb_amg *amg)
  * ------------------------------------------------------------------------ */
 static int read_int(const int *d)
 {
-   int h = 0;
-   cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, gb_stream());
+   int *h = gb_red_ints();
+   h[0] = 0;
+   cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, gb_stream());
    gb_sync();
-   return h;
+   return h[0];
 }
 
 /* exclusive scan into out (n+1), returns total */
@@ -735,9 +736,9 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
       double *measure = (double *) gb_dmalloc(sizeof(double) * (size_t) (nc1 ? nc1 : 1));
       int *ingraph = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 ? nc1 : 1));
       int *counter = (int *) gb_dmalloc(sizeof(int) * 4);
-      int *hcount = (int *) gb_hmalloc_pinned(sizeof(int) * 4);
-      int it = gb_pmis(nc1, S2.i, S2.j, 3, CFN, measure, ingraph, cnt, counter, hcount, 10000, s);
-      gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter); gb_hfree_pinned(hcount);
+      int it = gb_pmis(nc1, S2.nnz, S2.i, S2.j, 3, CFN, measure, ingraph, cnt, counter, gb_red_ints() + 4, 10000,
+                       s);
+      gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter);
       if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS on S2 did not terminate"); return -1; }
    }
    gb_csr_free(&S2);
@@ -763,7 +764,7 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
       double *tmp = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
       double *Dq = (double *) gb_dmalloc(sizeof(double) * (size_t) (nf ? nf : 1));
       double *Dw = (double *) gb_dmalloc(sizeof(double) * (size_t) (nf ? nf : 1));
-      gb_mod_extpi_scale(nf, fl, A->i, A->v, FF.i, FF.j, FF.v, FC.i, FC.v, tmp, Dq, Dw, s);
+      gb_mod_extpi_scale(nf, FF.nnz, fl, A->i, A->v, FF.i, FF.j, FF.v, FC.i, FC.v, tmp, Dq, Dw, s);
       gb_dfree(tmp); gb_dfree(Dq); gb_dfree(Dw);
    }
    gb_csr W;
@@ -816,10 +817,12 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
    memset(&S, 0, sizeof(S));
    S.nr = S.nc = n;
    S.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   gb_strength_count(n, A->i, A->v, prm->strong_threshold, prm->max_row_sum, cnt, s);
+   long long *rkey = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (n ? n : 1));
+   gb_strength_count(n, A->i, A->v, prm->strong_threshold, prm->max_row_sum, cnt, rkey, s);
    S.nnz = scan_total(cnt, S.i, n);
    S.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (S.nnz ? S.nnz : 1));
-   gb_strength_fill(n, A->i, A->j, A->v, prm->strong_threshold, prm->max_row_sum, S.i, S.j, s);
+   gb_strength_fill(n, A->i, A->j, A->v, rkey, S.i, S.j, s);
+   gb_dfree(rkey);
    double t1 = gb_wtime();
    t_phase[0] += t1 - t0;
 
@@ -829,9 +832,8 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
       double *measure = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
       int *ingraph = (int *) gb_dmalloc(sizeof(int) * (size_t) (n ? n : 1));
       int *counter = (int *) gb_dmalloc(sizeof(int) * 4);
-      int *hcount = (int *) gb_hmalloc_pinned(sizeof(int) * 4);
-      int it = gb_pmis(n, S.i, S.j, 0, CF, measure, ingraph, cnt, counter, hcount, 10000, s);
-      gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter); gb_hfree_pinned(hcount);
+      int it = gb_pmis(n, S.nnz, S.i, S.j, 0, CF, measure, ingraph, cnt, counter, gb_red_ints() + 4, 10000, s);
+      gb_dfree(measure); gb_dfree(ingraph); gb_dfree(counter);
       if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS did not terminate"); return -1; }
    }
    double t2 = gb_wtime();

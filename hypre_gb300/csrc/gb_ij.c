@@ -698,10 +698,11 @@ static int row_grow(HYPRE_IJMatrix m, int r, int need)
 
 static int ij_read_int(const int *d)
 {
-   int h = 0;
-   cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, gb_stream());
+   int *h = gb_red_ints() + 1;
+   h[0] = 0;
+   cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, gb_stream());
    gb_sync();
-   return h;
+   return h[0];
 }
 
 /* grows the device staging to hold need entries (stream-ordered copies);

@@ -37,6 +37,7 @@ double *gb_red_part(void);                   /* GB_RED_BLOCKS * 4 doubles */
 double *gb_red_out(void);                    /* 8 doubles (device) */
 unsigned int *gb_red_count(void);            /* zeroed counter of one-launch reductions */
 double *gb_red_host(void);                   /* 8 doubles (pinned host) */
+int *gb_red_ints(void);                      /* 16 ints (pinned host): 0 read-backs, 4-5 PMIS counts */
 void  gb_release_scratch(void);
 
 /* --- matrices and vectors -------------------------------------------------- */

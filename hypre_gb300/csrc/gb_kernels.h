@@ -54,11 +54,14 @@ int  gb_num_sms(void);
 /* scan / setup */
 long long gb_scan_scratch_ints(int n);
 void gb_exclusive_scan(const int *in, int *out, int n, int *scratch, cudaStream_t s);
-void gb_strength_count(int n, const int *Ai, const double *Av, double theta, double mrs, int *cnt, cudaStream_t s);
-void gb_strength_fill(int n, const int *Ai, const int *Aj, const double *Av, double theta, double mrs,
-                      const int *Si, int *Sj, cudaStream_t s);
-int  gb_pmis(int n, const int *Si, const int *Sj, int CF_init, int *CF, double *measure, int *ingraph, int *colcnt,
-             int *d_counter, int *h_counter, int max_iter, cudaStream_t s);   /* synchronises */
+/* rkey: n per-row threshold keys written by the count, read by the fill */
+void gb_strength_count(int n, const int *Ai, const double *Av, double theta, double mrs, int *cnt, long long *rkey,
+                       cudaStream_t s);
+void gb_strength_fill(int n, const int *Ai, const int *Aj, const double *Av, const long long *rkey, const int *Si,
+                      int *Sj, cudaStream_t s);
+/* nnz = Si[n]; d_counter: 4 device ints; h_counter: 2 pinned host ints */
+int  gb_pmis(int n, int nnz, const int *Si, const int *Sj, int CF_init, int *CF, double *measure, int *ingraph,
+             int *colcnt, int *d_counter, int *h_counter, int max_iter, cudaStream_t s);   /* synchronises */
 void gb_cpoint_flags(int n, const int *CF, int *flag, cudaStream_t s);
 void gb_sf_to_f(int n, int *CF, cudaStream_t s);
 void gb_extpi_ub(int n, const int *Si, const int *Sj, const int *CF, int *ub, cudaStream_t s);
@@ -126,9 +129,9 @@ void gb_fffc_count(int nf, const int *fl, const int *Ai, const int *Aj, const in
 void gb_fffc_fill(int nf, const int *fl, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj,
                   const int *CF, const int *f2c, const int *f2f, const int *FFi, int *FFj, double *FFv,
                   const int *FCi, int *FCj, double *FCv, cudaStream_t s);
-void gb_mod_extpi_scale(int nf, const int *fl, const int *Ai, const double *Av, const int *FFi, const int *FFj,
-                        double *FFv, const int *FCi, const double *FCv, double *tmp, double *Dq, double *Dw,
-                        cudaStream_t s);
+void gb_mod_extpi_scale(int nf, int nnzff, const int *fl, const int *Ai, const double *Av, const int *FFi,
+                        const int *FFj, double *FFv, const int *FCi, const double *FCv, double *tmp, double *Dq,
+                        double *Dw, cudaStream_t s);
 void gb_p1_len(int n, const int *CF, const int *f2f, const int *Wi, int *len, cudaStream_t s);
 void gb_p1_fill(int n, const int *CF, const int *f2c, const int *f2f, const int *Wi, const int *Wj, const double *Wv,
                 const int *Pi, int *Pj, double *Pv, cudaStream_t s);

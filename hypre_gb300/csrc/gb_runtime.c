@@ -20,6 +20,7 @@ static void *g_scratch[GB_NSCRATCH];
 static size_t g_scratch_sz[GB_NSCRATCH];
 static double *g_red_part = NULL, *g_red_out = NULL, *g_red_host = NULL;
 static unsigned int *g_red_count = NULL;
+static int *g_red_ints = NULL;
 
 void gb_count_launch(int n) { g_launches += n; }
 
@@ -154,12 +155,14 @@ static void red_init(void)
       g_red_out = (double *) gb_dmalloc(sizeof(double) * 8);
       g_red_host = (double *) gb_hmalloc_pinned(sizeof(double) * 8);
       g_red_count = (unsigned int *) gb_dcalloc(sizeof(unsigned int) * 4);
+      g_red_ints = (int *) gb_hmalloc_pinned(sizeof(int) * 16);
    }
 }
 double *gb_red_part(void) { red_init(); return g_red_part; }
 double *gb_red_out(void) { red_init(); return g_red_out; }
 double *gb_red_host(void) { red_init(); return g_red_host; }
 unsigned int *gb_red_count(void) { red_init(); return g_red_count; }
+int *gb_red_ints(void) { red_init(); return g_red_ints; }
 
 void gb_release_scratch(void)
 {
@@ -190,8 +193,12 @@ HYPRE_Int HYPRE_Finalize(void)
    {
       cudaStreamSynchronize(g_stream);
       gb_release_scratch();
-      if (g_red_part) { gb_dfree(g_red_part); gb_dfree(g_red_out); gb_hfree_pinned(g_red_host); gb_dfree(g_red_count); }
-      g_red_part = NULL; g_red_out = NULL; g_red_host = NULL; g_red_count = NULL;
+      if (g_red_part)
+      {
+         gb_dfree(g_red_part); gb_dfree(g_red_out); gb_hfree_pinned(g_red_host); gb_dfree(g_red_count);
+         gb_hfree_pinned(g_red_ints);
+      }
+      g_red_part = NULL; g_red_out = NULL; g_red_host = NULL; g_red_count = NULL; g_red_ints = NULL;
       cudaStreamSynchronize(g_stream);
       if (g_own_stream) { cudaStreamDestroy(g_stream); g_stream = 0; g_own_stream = 0; }
       g_initialized = 0;

@@ -119,73 +119,114 @@ extern "C" void gb_exclusive_scan(const int *in, int *out, int n, int *scratch, 
 // Strength of connection (reference: src/parcsr_ls/par_strength.c:75-527).
 // S keeps A's column order without the diagonal (the first entry of a row).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void strength_row(const int *Ai, const double *Av, int i, double theta, double mrs,
-                                             double &thr, int &all_weak, int &diag_neg)
+// sign tests on the bit pattern (integer ops; x < 0 and x > 0 as IEEE compares,
+// false for zeros and NaN)
+__device__ __forceinline__ bool gb_lt0(double x)
+{
+   long long b = __double_as_longlong(x);
+   return b < 0 && (b & 0x7fffffffffffffffLL) != 0 && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool gb_gt0(double x)
+{
+   long long b = __double_as_longlong(x);
+   return b > 0 && b <= 0x7ff0000000000000LL;
+}
+
+// Comparisons of matrix values run on integer keys: key(x) = +|x| or -|x|
+// as the integer of the magnitude bits, which orders non-NaN doubles as the
+// IEEE comparisons do (-0 and +0 both map to 0).  FP64 compares are scarce on
+// this GPU; the row sum stays an FP64 sum in the reference's order.
+__device__ __forceinline__ long long gb_okey(double x)
+{
+   long long b = __double_as_longlong(x);
+   return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+
+#define GB_WEAK_ROW ((long long) 0x8000000000000000ULL)
+
+// row i's threshold key, or GB_WEAK_ROW when the row-sum test makes every
+// connection weak
+__device__ __forceinline__ long long strength_row(const int *Ai, const double *Av, int i, double theta, double mrs)
 {
    int b = Ai[i], e = Ai[i + 1];
+   if (b >= e) { return GB_WEAK_ROW; }   // an empty row has no connections
    double diag = Av[b];
    double row_scale = 0.0, row_sum = diag;
+   long long ks = 0;
    if (diag < 0)
    {
-      for (int k = b + 1; k < e; k++) { double v = Av[k]; row_scale = row_scale < v ? v : row_scale; row_sum += v; }
+      for (int k = b + 1; k < e; k++)
+      {
+         double v = Av[k];
+         long long kv = gb_okey(v);
+         if (ks < kv) { ks = kv; row_scale = v; }
+         row_sum += v;
+      }
    }
    else
    {
-      for (int k = b + 1; k < e; k++) { double v = Av[k]; row_scale = row_scale > v ? v : row_scale; row_sum += v; }
+      for (int k = b + 1; k < e; k++)
+      {
+         double v = Av[k];
+         long long kv = gb_okey(v);
+         if (ks > kv) { ks = kv; row_scale = v; }
+         row_sum += v;
+      }
    }
-   all_weak = (fabs(row_sum) > fabs(diag) * mrs) && (mrs < 1.0);
-   thr = theta * row_scale;
-   diag_neg = diag < 0;
+   if ((fabs(row_sum) > fabs(diag) * mrs) && (mrs < 1.0)) { return GB_WEAK_ROW; }
+   return gb_okey(theta * row_scale);
+}
+
+// strong: v > thr for a negative diagonal, v < thr otherwise
+__device__ __forceinline__ int strength_test(double v, long long kt, bool dneg)
+{
+   long long kv = gb_okey(v);
+   return dneg ? kv > kt : kv < kt;
 }
 
 __global__ void k_strength_count(int n, const int *__restrict__ Ai, const double *__restrict__ Av,
-                                 double theta, double mrs, int *__restrict__ cnt)
+                                 double theta, double mrs, int *__restrict__ cnt, long long *__restrict__ rkey)
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i >= n) { return; }
-   double thr; int weak, dneg;
-   strength_row(Ai, Av, i, theta, mrs, thr, weak, dneg);
+   long long kt = strength_row(Ai, Av, i, theta, mrs);
+   rkey[i] = kt;
    int c = 0;
-   if (!weak)
+   if (kt != GB_WEAK_ROW)
    {
-      for (int k = Ai[i] + 1; k < Ai[i + 1]; k++)
-      {
-         double v = Av[k];
-         c += dneg ? !(v <= thr) : !(v >= thr);
-      }
+      const bool dneg = gb_lt0(Av[Ai[i]]);
+      for (int k = Ai[i] + 1; k < Ai[i + 1]; k++) { c += strength_test(Av[k], kt, dneg); }
    }
    cnt[i] = c;
 }
 
 __global__ void k_strength_fill(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
-                                const double *__restrict__ Av, double theta, double mrs,
+                                const double *__restrict__ Av, const long long *__restrict__ rkey,
                                 const int *__restrict__ Si, int *__restrict__ Sj)
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i >= n) { return; }
-   double thr; int weak, dneg;
-   strength_row(Ai, Av, i, theta, mrs, thr, weak, dneg);
-   if (weak) { return; }
+   long long kt = rkey[i];
+   if (kt == GB_WEAK_ROW) { return; }
+   const bool dneg = gb_lt0(Av[Ai[i]]);
    int p = Si[i];
    for (int k = Ai[i] + 1; k < Ai[i + 1]; k++)
    {
-      double v = Av[k];
-      int strong = dneg ? !(v <= thr) : !(v >= thr);
-      if (strong) { Sj[p++] = Aj[k]; }
+      if (strength_test(Av[k], kt, dneg)) { Sj[p++] = Aj[k]; }
    }
 }
 
 extern "C" void gb_strength_count(int n, const int *Ai, const double *Av, double theta, double mrs, int *cnt,
-                                  cudaStream_t s)
+                                  long long *rkey, cudaStream_t s)
 {
-   k_strength_count<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Av, theta, mrs, cnt);
+   k_strength_count<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Av, theta, mrs, cnt, rkey);
    GB_COUNT(1);
 }
 
-extern "C" void gb_strength_fill(int n, const int *Ai, const int *Aj, const double *Av, double theta, double mrs,
+extern "C" void gb_strength_fill(int n, const int *Ai, const int *Aj, const double *Av, const long long *rkey,
                                  const int *Si, int *Sj, cudaStream_t s)
 {
-   k_strength_fill<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, theta, mrs, Si, Sj);
+   k_strength_fill<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, rkey, Si, Sj);
    GB_COUNT(1);
 }
 
@@ -277,11 +318,20 @@ __global__ void k_pmis_init(int n, const int *__restrict__ Si, const int *__rest
    ingraph[i] = g;
 }
 
+// Measures are never negative (a column count plus a draw in (0, 1), or
+// +0.0 once a point leaves the graph), and for non-negative doubles the
+// order of the bit patterns as integers is the numeric order: the passes
+// compare measures with integer instructions (FP64 compares are scarce on
+// this GPU) and the same outcomes.
+#define GB_ONE_BITS 0x3ff0000000000000LL
+
+__device__ __forceinline__ long long gb_mbits(const double *m, int i) { return __double_as_longlong(m[i]); }
+
 __global__ void k_pmis_select(int n, const int *__restrict__ ingraph, const double *__restrict__ measure,
                               int *__restrict__ CF)
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
-   if (i < n && ingraph[i] && measure[i] > 1) { CF[i] = 1; }
+   if (i < n && ingraph[i] && gb_mbits(measure, i) > GB_ONE_BITS) { CF[i] = 1; }
 }
 
 __global__ void k_pmis_remove(int n, const int *__restrict__ ingraph, const double *__restrict__ measure,
@@ -289,13 +339,13 @@ __global__ void k_pmis_remove(int n, const int *__restrict__ ingraph, const doub
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i >= n || !ingraph[i]) { return; }
-   double mi = measure[i];
-   if (!(mi > 1)) { return; }
+   long long mi = gb_mbits(measure, i);
+   if (!(mi > GB_ONE_BITS)) { return; }
    for (int k = Si[i]; k < Si[i + 1]; k++)
    {
       int j = Sj[k];
-      double mj = measure[j];
-      if (mj > 1)
+      long long mj = gb_mbits(measure, j);
+      if (mj > GB_ONE_BITS)
       {
          if (mi > mj) { CF[j] = 0; }
          else if (mj > mi) { CF[i] = 0; }
@@ -308,7 +358,7 @@ __global__ void k_pmis_setcf(int n, const int *__restrict__ ingraph, const doubl
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i >= n || !ingraph[i]) { return; }
-   if (measure[i] < 1) { CF[i] = F_PT; }
+   if (gb_mbits(measure, i) < GB_ONE_BITS) { CF[i] = F_PT; }
    if (CF[i] > 0) { CF[i] = C_PT; return; }
    for (int k = Si[i]; k < Si[i + 1]; k++)
    {
@@ -330,12 +380,33 @@ __global__ void k_pmis_update(int n, int *__restrict__ ingraph, double *__restri
    if ((threadIdx.x & 31) == 0 && b) { atomicAdd(remaining, __popc(b)); }
 }
 
-extern "C" int gb_pmis(int n, const int *Si, const int *Sj, int CF_init, int *CF, double *measure, int *ingraph,
-                       int *colcnt, int *d_counter, int *h_counter, int max_iter, cudaStream_t s)
+// one PMIS pass (par_coarsen.c:2300-2420): the first pass with CF_init skips the
+// selection; the pass's remaining graph size goes to d_counter[slot] and, by
+// an asynchronous copy, to h_counter[slot].  A pass over an empty graph
+// changes nothing.
+static void pmis_pass(int n, int nb, int first, const int *Si, const int *Sj, int CF_init, int *CF,
+                      double *measure, int *ingraph, int *d_counter, int *h_counter, int slot, cudaStream_t s)
 {
-   int nnz = 0;
-   cudaMemcpyAsync(&nnz, Si + n, sizeof(int), cudaMemcpyDeviceToHost, s);
-   cudaStreamSynchronize(s);
+   if (!CF_init || !first)
+   {
+      k_pmis_select<<<nb, 256, 0, s>>>(n, ingraph, measure, CF);
+      k_pmis_remove<<<nb, 256, 0, s>>>(n, ingraph, measure, Si, Sj, CF);
+      GB_COUNT(2);
+   }
+   k_pmis_setcf<<<nb, 256, 0, s>>>(n, ingraph, measure, Si, Sj, CF);
+   cudaMemsetAsync(d_counter + slot, 0, sizeof(int), s);
+   k_pmis_update<<<nb, 256, 0, s>>>(n, ingraph, measure, CF, d_counter + slot);
+   GB_COUNT(2);
+   cudaMemcpyAsync(h_counter + slot, d_counter + slot, sizeof(int), cudaMemcpyDeviceToHost, s);
+}
+
+// Passes run until the graph is empty.  Two passes are kept in flight: the
+// host reads pass k's count while pass k+1 runs, so the GPU does not wait
+// for the host between passes; the one pass queued after the last needed
+// one finds an empty graph.  Returns the number of passes, -1 past max_iter.
+extern "C" int gb_pmis(int n, int nnz, const int *Si, const int *Sj, int CF_init, int *CF, double *measure,
+                       int *ingraph, int *colcnt, int *d_counter, int *h_counter, int max_iter, cudaStream_t s)
+{
    cudaMemsetAsync(colcnt, 0, sizeof(int) * (size_t) (n > 0 ? n : 1), s);
    if (nnz > 0) { k_colcount<<<gb_blocks(nnz, 256), 256, 0, s>>>(nnz, Sj, colcnt); GB_COUNT(1); }
    int nb = gb_blocks(n, 256);
@@ -347,25 +418,27 @@ extern "C" int gb_pmis(int n, const int *Si, const int *Sj, int CF_init, int *CF
    GB_COUNT(1);
    cudaMemcpyAsync(h_counter, d_counter, sizeof(int), cudaMemcpyDeviceToHost, s);
    cudaStreamSynchronize(s);
-   int iter = 0;
-   while (*h_counter > 0)
+   if (h_counter[0] == 0) { return 0; }
+   cudaEvent_t ev[2];
+   cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+   cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+   int queued = 0, checked = 0, result = -1;
+   for (;;)
    {
-      if (iter >= max_iter) { return -1; }
-      if (!CF_init || iter)
+      while (queued < checked + 2 && queued < max_iter)
       {
-         k_pmis_select<<<nb, 256, 0, s>>>(n, ingraph, measure, CF);
-         k_pmis_remove<<<nb, 256, 0, s>>>(n, ingraph, measure, Si, Sj, CF);
-         GB_COUNT(2);
+         pmis_pass(n, nb, queued == 0, Si, Sj, CF_init, CF, measure, ingraph, d_counter, h_counter, queued & 1, s);
+         cudaEventRecord(ev[queued & 1], s);
+         queued++;
       }
-      iter++;
-      k_pmis_setcf<<<nb, 256, 0, s>>>(n, ingraph, measure, Si, Sj, CF);
-      cudaMemsetAsync(d_counter, 0, sizeof(int), s);
-      k_pmis_update<<<nb, 256, 0, s>>>(n, ingraph, measure, CF, d_counter);
-      GB_COUNT(2);
-      cudaMemcpyAsync(h_counter, d_counter, sizeof(int), cudaMemcpyDeviceToHost, s);
-      cudaStreamSynchronize(s);
+      if (checked == queued) { break; }
+      cudaEventSynchronize(ev[checked & 1]);
+      checked++;
+      if (h_counter[(checked - 1) & 1] == 0) { result = checked; break; }
    }
-   return iter;
+   cudaEventDestroy(ev[0]);
+   cudaEventDestroy(ev[1]);
+   return result;
 }
 
 // ---------------------------------------------------------------------------
@@ -669,26 +742,19 @@ extern "C" void gb_extpi_fill(int nrows, const int *rows, const int *Ai, const i
 // chain per warp.  Membership of a fine point in the row's column set is a
 // search of the row's coarse columns (only C points can be members).
 // Rows with more candidates are listed for the warp-per-row kernels.
+// (Key sets in shared memory, 32 KB per 128 threads, made the counting and
+// filling about 10 ms slower on the 160^3 27-point problem than these local
+// arrays, which stay in L1 and L2.)
 // ---------------------------------------------------------------------------
 #define GB_TPR_MAX 64
+#define GB_TPR_BLOCK 128
+typedef int *TprKeys;
 
-// sign tests on the bit pattern (integer ops; x < 0 and x > 0 as IEEE compares,
-// false for zeros and NaN)
-__device__ __forceinline__ bool gb_lt0(double x)
-{
-   long long b = __double_as_longlong(x);
-   return b < 0 && (b & 0x7fffffffffffffffLL) != 0 && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
-}
-__device__ __forceinline__ bool gb_gt0(double x)
-{
-   long long b = __double_as_longlong(x);
-   return b > 0 && b <= 0x7ff0000000000000LL;
-}
 
 /* The row's coarse columns are kept as a sorted set of packed keys
  * (coarse index << 6 | position in discovery order), so a membership test is
  * a binary search; coarse indices stay below 2^25 (checked by the host). */
-__device__ __forceinline__ int tpr_lower(const int *sk, int len, int c)
+__device__ __forceinline__ int tpr_lower(TprKeys sk, int len, int c)
 {
    int lo = 0, hi = len;
    while (lo < hi)
@@ -700,7 +766,7 @@ __device__ __forceinline__ int tpr_lower(const int *sk, int len, int c)
    return lo;
 }
 
-__device__ __forceinline__ int tpr_find(const int *sk, int len, int c)
+__device__ __forceinline__ int tpr_find(TprKeys sk, int len, int c)
 {
    int lo = tpr_lower(sk, len, c);
    return (lo < len && (sk[lo] >> 6) == c) ? (sk[lo] & 63) : -1;
@@ -708,7 +774,7 @@ __device__ __forceinline__ int tpr_find(const int *sk, int len, int c)
 
 // adds coarse column c (new columns take the next position; Pj, when given,
 // receives the columns in discovery order); false beyond GB_TPR_MAX
-__device__ __forceinline__ bool tpr_add(int *sk, int &len, int c, int *Pj)
+__device__ __forceinline__ bool tpr_add(TprKeys sk, int &len, int c, int *Pj)
 {
    int lo = tpr_lower(sk, len, c);
    if (lo < len && (sk[lo] >> 6) == c) { return true; }
@@ -723,7 +789,7 @@ __device__ __forceinline__ bool tpr_add(int *sk, int &len, int c, int *Pj)
 // counts (or fills Pj, when given) the candidate columns of row i in
 // discovery order; returns -1 beyond GB_TPR_MAX
 __device__ int tpr_discover(int i, const int *__restrict__ Si, const int *__restrict__ Sj, const int *__restrict__ CF,
-                            const int *__restrict__ f2c, int *sk, int *Pj)
+                            const int *__restrict__ f2c, TprKeys sk, int *Pj)
 {
    int len = 0;
    for (int k = Si[i]; k < Si[i + 1]; k++)
@@ -746,7 +812,7 @@ __device__ int tpr_discover(int i, const int *__restrict__ Si, const int *__rest
    return len;
 }
 
-__global__ void __launch_bounds__(128) k_extpi_count_t(int nrows, const int *__restrict__ rows,
+__global__ void __launch_bounds__(GB_TPR_BLOCK) k_extpi_count_t(int nrows, const int *__restrict__ rows,
                                                        const int *__restrict__ Si, const int *__restrict__ Sj,
                                                        const int *__restrict__ CF, const int *__restrict__ f2c,
                                                        int *__restrict__ cnt, int *ovf_list, int *ovf_n)
@@ -763,7 +829,7 @@ __global__ void __launch_bounds__(128) k_extpi_count_t(int nrows, const int *__r
    else { cnt[r] = len; }
 }
 
-__global__ void __launch_bounds__(128) k_extpi_fill_t(int nrows, const int *__restrict__ rows,
+__global__ void __launch_bounds__(GB_TPR_BLOCK) k_extpi_fill_t(int nrows, const int *__restrict__ rows,
                                                       const int *__restrict__ Ai, const int *__restrict__ Aj,
                                                       const double *__restrict__ Av, const int *__restrict__ Si,
                                                       const int *__restrict__ Sj, const int *__restrict__ CF,
@@ -846,7 +912,8 @@ extern "C" void gb_iota(int n, int *out, int *count, cudaStream_t s)
 extern "C" void gb_extpi_count_t(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF,
                                  const int *f2c, int *cnt, int *ovf_list, int *ovf_n, cudaStream_t s)
 {
-   k_extpi_count_t<<<gb_blocks(nrows, 128), 128, 0, s>>>(nrows, rows, Si, Sj, CF, f2c, cnt, ovf_list, ovf_n);
+   k_extpi_count_t<<<gb_blocks(nrows, GB_TPR_BLOCK), GB_TPR_BLOCK, 0, s>>>(nrows, rows, Si, Sj, CF, f2c, cnt,
+                                                                         ovf_list, ovf_n);
    GB_COUNT(1);
 }
 
@@ -854,7 +921,8 @@ extern "C" void gb_extpi_fill_t(int nrows, const int *rows, const int *Ai, const
                                 const int *Si, const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj,
                                 double *Pv, cudaStream_t s)
 {
-   k_extpi_fill_t<<<gb_blocks(nrows, 128), 128, 0, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv);
+   k_extpi_fill_t<<<gb_blocks(nrows, GB_TPR_BLOCK), GB_TPR_BLOCK, 0, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c,
+                                                                        Pi, Pj, Pv);
    GB_COUNT(1);
 }
 
@@ -1024,50 +1092,79 @@ __global__ void k_tr_sort(int nc, const int *__restrict__ Ti, int *__restrict__ 
    }
 }
 
-// bitonic sort of one row (minlen <= len <= 2048) by a 256-thread block
+// merge sort of one row (minlen <= len <= 2048) by a 256-thread block.  Runs
+// of width w are merged pairwise; an element's place in the merged run is its
+// place in its own run plus the number of smaller keys in the partner run (a
+// binary search; the keys of a row are distinct).  Keys carry their original
+// position (key << 11 | position), so the values move once, at the end.
 __global__ void __launch_bounds__(256) k_tr_sort_block(int nc, const int *__restrict__ Ti, int *__restrict__ Tj,
                                                       double *__restrict__ Tv, int minlen)
 {
-   __shared__ int key[2048];
-   __shared__ double val[2048];
+   __shared__ long long buf[2][2048];
    for (int c = blockIdx.x; c < nc; c += gridDim.x)
    {
-      int b = Ti[c], e = Ti[c + 1];
-      int len = e - b;
+      const int b = Ti[c], e = Ti[c + 1];
+      const int len = e - b;
       if (len < minlen || len > 2048) { continue; }
-      int m = 1;
-      while (m < len) { m <<= 1; }
-      for (int t = threadIdx.x; t < m; t += blockDim.x)
+      double v[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
       {
-         key[t] = t < len ? Tj[b + t] : 0x7fffffff;
-         val[t] = (t < len && Tv) ? Tv[b + t] : 0.0;
-      }
-      __syncthreads();
-      for (int k = 2; k <= m; k <<= 1)
-      {
-         for (int j = k >> 1; j > 0; j >>= 1)
+         const int t = threadIdx.x + 256 * q;
+         v[q] = 0.0;
+         if (t < len)
          {
-            for (int t = threadIdx.x; t < m; t += blockDim.x)
-            {
-               int p = t ^ j;
-               if (p > t)
-               {
-                  bool up = (t & k) == 0;
-                  int a = key[t], bb = key[p];
-                  if ((a > bb) == up)
-                  {
-                     key[t] = bb; key[p] = a;
-                     double tv = val[t]; val[t] = val[p]; val[p] = tv;
-                  }
-               }
-            }
-            __syncthreads();
+            buf[0][t] = ((long long) Tj[b + t] << 11) | t;
+            if (Tv) { v[q] = Tv[b + t]; }
          }
       }
-      for (int t = threadIdx.x; t < len; t += blockDim.x)
+      __syncthreads();
+      int src = 0;
+      for (int lw = 0; (1 << lw) < len; lw++)
       {
-         Tj[b + t] = key[t];
-         if (Tv) { Tv[b + t] = val[t]; }
+         const int w = 1 << lw;
+         const long long *in = buf[src];
+         long long *out = buf[src ^ 1];
+         for (int t = threadIdx.x; t < len; t += 256)
+         {
+            const long long x = in[t];
+            const int run = t >> lw;
+            const int start = run << lw;
+            const int pstart = (run ^ 1) << lw;
+            int rank = 0;
+            if (pstart < len)
+            {
+               int lo = pstart, hi = min(pstart + w, len);
+               while (lo < hi)
+               {
+                  const int mid = (lo + hi) >> 1;
+                  if (in[mid] < x) { lo = mid + 1; }
+                  else { hi = mid; }
+               }
+               rank = lo - pstart;
+            }
+            out[min(start, pstart) + (t - start) + rank] = x;
+         }
+         __syncthreads();
+         src ^= 1;
+      }
+      // the other buffer is free: stage the values by original position
+      double *vs = reinterpret_cast<double *>(buf[src ^ 1]);
+      if (Tv)
+      {
+#pragma unroll
+         for (int q = 0; q < 8; q++)
+         {
+            const int t = threadIdx.x + 256 * q;
+            if (t < len) { vs[t] = v[q]; }
+         }
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < len; t += 256)
+      {
+         const long long x = buf[src][t];
+         Tj[b + t] = (int) (x >> 11);
+         if (Tv) { Tv[b + t] = vs[x & 2047]; }
       }
       __syncthreads();
    }
