@@ -483,9 +483,11 @@ HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(HYPRE_Int n, const HYPRE_I
    if (!Aout) { gb_error_in_arg(5); return gb_error_flag; }
    gb_runtime_init();
    cudaStream_t s = gb_stream();
-   int nnz = 0;
-   cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int), cudaMemcpyDeviceToHost, s);
+   int *hn = gb_red_ints() + 1;
+   hn[0] = 0;
+   cudaMemcpyAsync(hn, rowptr + n, sizeof(int), cudaMemcpyDeviceToHost, s);
    if (gb_sync()) { return gb_error_flag; }
+   int nnz = hn[0];
    gb_csr A;
    A.nr = n; A.nc = n; A.nnz = nnz;
    A.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
@@ -493,7 +495,7 @@ HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(HYPRE_Int n, const HYPRE_I
    A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
    if (!A.i || !A.j || !A.v) { gb_dfree(A.i); gb_dfree(A.j); gb_dfree(A.v); *Aout = NULL; return gb_error_flag; }
    cudaMemcpyAsync(A.i, rowptr, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToDevice, s);
-   gb_ij_gather(n, NULL, A.i, colidx, values, 0, A.j, A.v, s);
+   gb_ij_gather(n, nnz, NULL, A.i, colidx, values, 0, A.j, A.v, s);
    *Aout = gb_parcsr_wrap(A, 1);
    return gb_error_flag;
 }
@@ -1001,7 +1003,7 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
       A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
       if (!A.i || !A.j || !A.v) { gb_dfree(A.i); gb_dfree(A.j); gb_dfree(A.v); return gb_error_flag; }
       cudaMemcpyAsync(A.i, m->st_rowptr, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToDevice, s);
-      gb_ij_gather(n, NULL, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
+      gb_ij_gather(n, nnz, NULL, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
       if (m->par) { gb_parcsr_free(m->par); }
       m->par = gb_parcsr_wrap(A, 1);
       m->assembled = 1;
@@ -1061,7 +1063,7 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
    }
    cudaMemcpyAsync(A.i, I, sizeof(int) * (size_t) (n + 1), cudaMemcpyHostToDevice, s);
    cudaMemcpyAsync(doff, off, sizeof(long long) * (size_t) (n ? n : 1), cudaMemcpyHostToDevice, s);
-   gb_ij_gather(n, doff, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
+   gb_ij_gather(n, A.nnz, doff, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
    gb_sync();   /* the host buffers above are read by the copies */
    gb_dfree(doff);
    free(I); free(off); free(hc); free(hv);

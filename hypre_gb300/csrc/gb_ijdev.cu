@@ -62,27 +62,31 @@ extern "C" void gb_ij_check(int nrows, const int *start, const int *cols, int nc
    GB_COUNT(1);
 }
 
-// one warp per row r: staged entries off[r] .. off[r]+len (len = I[r+1]-I[r];
-// off NULL: the staging is in row order, off[r] = I[r]) -> J, V at I[r],
-// diagonal first (shift, or swap when swap_diag)
+// LPR lanes per row r (LPR divides 32): staged entries off[r] .. off[r]+len
+// (len = I[r+1]-I[r]; off NULL: the staging is in row order, off[r] = I[r])
+// -> J, V at I[r], diagonal first (shift, or swap when swap_diag)
+template <int LPR>
 __global__ void k_ij_gather(int n, const long long *__restrict__ off, const int *__restrict__ I,
                             const int *__restrict__ scols, const double *__restrict__ svals, int swap_diag,
                             int *__restrict__ J, double *__restrict__ V)
 {
-   const int r = (int) ((blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5);
-   const int lane = threadIdx.x & 31;
-   if (r >= n) { return; }
+   const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+   const int r = (int) (g / LPR);
+   const int lane = (int) (g % LPR);
+   if (r >= n) { return; }   // whole segments leave together
+   const int sbase = (threadIdx.x & 31) & ~(LPR - 1);
+   const unsigned seg = LPR == 32 ? GB_FULL : (((1u << LPR) - 1u) << sbase);
    const int d = I[r], l = I[r + 1] - d;
    const long long o = off ? off[r] : (long long) d;
    // first position of the diagonal
    int dpos = -1;
-   for (int c = 0; c < l && dpos < 0; c += 32)
+   for (int c = 0; c < l && dpos < 0; c += LPR)
    {
       const int q = c + lane;
-      const unsigned m = __ballot_sync(GB_FULL, q < l && scols[o + q] == r);
+      const unsigned m = __ballot_sync(seg, q < l && scols[o + q] == r) >> sbase;
       if (m) { dpos = c + __ffs(m) - 1; }
    }
-   for (int q = lane; q < l; q += 32)
+   for (int q = lane; q < l; q += LPR)
    {
       int src = q;
       if (dpos > 0)
@@ -95,10 +99,17 @@ __global__ void k_ij_gather(int n, const long long *__restrict__ off, const int 
    }
 }
 
-extern "C" void gb_ij_gather(int n, const long long *off, const int *I, const int *scols, const double *svals,
-                             int swap_diag, int *J, double *V, cudaStream_t s)
+extern "C" void gb_ij_gather(int n, long long nnz, const long long *off, const int *I, const int *scols,
+                             const double *svals, int swap_diag, int *J, double *V, cudaStream_t s)
 {
    if (n <= 0) { return; }
-   k_ij_gather<<<(int) (((long long) n * 32 + 255) / 256), 256, 0, s>>>(n, off, I, scols, svals, swap_diag, J, V);
+   const long long avg = nnz / n;
+#define GB_IJG(L)                                                                                                  \
+   k_ij_gather<L><<<(int) (((long long) n * L + 255) / 256), 256, 0, s>>>(n, off, I, scols, svals, swap_diag, J, V)
+   if (avg <= 6) { GB_IJG(4); }
+   else if (avg <= 12) { GB_IJG(8); }
+   else if (avg <= 40) { GB_IJG(16); }
+   else { GB_IJG(32); }
+#undef GB_IJG
    GB_COUNT(1);
 }

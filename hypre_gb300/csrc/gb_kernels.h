@@ -101,16 +101,16 @@ void gb_spgemm(int nrows, int square, int W, const int *Ai, const int *Aj, const
  * gb_spgemm_cap sizes the areas, gb_spgemm_gather moves rows into place */
 void gb_spgemm_cap(int n, int ncols, int square, const int *Ai, const int *Aj, const int *Bi, int lcap0, int *ub,
                    int *cap, unsigned long long *sum, int *over, cudaStream_t s);
-void gb_spgemm_gather(int n, const int *Ci, const int *src, const int *tj, const double *tv, int *Cj, double *Cv,
-                      cudaStream_t s);
+void gb_spgemm_gather(int n, long long nnz, const int *Ci, const int *src, const int *tj, const double *tv, int *Cj,
+                      double *Cv, cudaStream_t s);
 void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj, const double *Av, const int *Bi, const int *Bj,
                   const double *Bv, int *cnt, const int *Ci, int *Cj, double *Cv, int *ovf_list, int *ovf_n,
                   int *out_list, int *out_n, int nlist, int *err, const int *ub, int *src, int fbase, int phase,
                   int tier, cudaStream_t s);
 /* IJ matrix device assembly (gb_ijdev.cu) */
 void gb_ij_check(int nrows, const int *start, const int *cols, int ncol, int *flags, cudaStream_t s);
-void gb_ij_gather(int n, const long long *off, const int *I, const int *scols, const double *svals, int swap_diag,
-                  int *J, double *V, cudaStream_t s);
+void gb_ij_gather(int n, long long nnz, const long long *off, const int *I, const int *scols, const double *svals,
+                  int swap_diag, int *J, double *V, cudaStream_t s);
 void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 /* aggressive coarsening (gb_agg.cu) */
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);

@@ -1043,23 +1043,43 @@ extern "C" void gb_compact_rows(int n, const int *Pi, const int *Pj, const doubl
 // a counting sort: rows of A^T list A's rows in ascending order).  Scatter with
 // atomics, then sort each output row by row index (entries are unique).
 // ---------------------------------------------------------------------------
+// Lanes of a warp that hit the same column share one atomic (neighbouring
+// rows of P share coarse columns); the order within a column is set by the
+// sort afterwards.
 __global__ void k_tr_count(int nnz, const int *__restrict__ Aj, int *__restrict__ cnt)
 {
-   int k = blockIdx.x * blockDim.x + threadIdx.x;
-   if (k < nnz) { atomicAdd(&cnt[Aj[k]], 1); }
+   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+   const int lane = threadIdx.x & 31;
+   const int c = k < nnz ? Aj[k] : -1 - lane;
+   const unsigned m = __match_any_sync(GB_FULL, c);
+   if (c >= 0 && lane == __ffs(m) - 1) { atomicAdd(&cnt[c], __popc(m)); }
 }
 
 __global__ void k_tr_scatter(int nr, const int *__restrict__ Ai, const int *__restrict__ Aj,
                              const double *__restrict__ Av, int *__restrict__ fill, int *__restrict__ Tj,
                              double *__restrict__ Tv)
 {
-   int r = blockIdx.x * blockDim.x + threadIdx.x;
-   if (r >= nr) { return; }
-   for (int k = Ai[r]; k < Ai[r + 1]; k++)
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   const int lane = threadIdx.x & 31;
+   const unsigned lt = (1u << lane) - 1u;
+   int k = 0, e = 0;
+   if (r < nr) { k = Ai[r]; e = Ai[r + 1]; }
+   while (__any_sync(GB_FULL, k < e))
    {
-      int p = atomicAdd(&fill[Aj[k]], 1);
-      Tj[p] = r;
-      if (Av) { Tv[p] = Av[k]; }
+      const bool act = k < e;
+      const int c = act ? Aj[k] : -1 - lane;
+      const unsigned m = __match_any_sync(GB_FULL, c);
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (act && lane == leader) { base = atomicAdd(&fill[c], __popc(m)); }
+      base = __shfl_sync(GB_FULL, base, leader);
+      if (act)
+      {
+         const int p = base + __popc(m & lt);
+         Tj[p] = r;
+         if (Av) { Tv[p] = Av[k]; }
+         k++;
+      }
    }
 }
 
@@ -1634,31 +1654,45 @@ extern "C" void gb_spgemm_cap(int n, int ncols, int square, const int *Ai, const
 // one warp per row: the row's cnt entries from its temporary area src[r]
 // (rows with src[r] < 0 were filled in place by the global-table tier;
 // tv NULL: column indices only)
+// LPR lanes per row (LPR divides 32): short rows share a warp
+template <int LPR>
 __global__ void k_spgemm_gather(int n, const int *__restrict__ Ci, const int *__restrict__ src,
                                 const int *__restrict__ tj, const double *__restrict__ tv, int *__restrict__ Cj,
                                 double *__restrict__ Cv)
 {
-   const int r = (int) ((blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5);
-   const int lane = threadIdx.x & 31;
+   const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+   const int r = (int) (g / LPR);
+   const int lane = (int) (g % LPR);
    if (r >= n) { return; }
    const int o = src[r];
    if (o < 0) { return; }
    const int d = Ci[r], l = Ci[r + 1] - d;
-   for (int q = lane; q < l; q += 32)
+   for (int q = lane; q < l; q += LPR)
    {
       Cj[d + q] = tj[o + q];
       if (tv) { Cv[d + q] = tv[o + q]; }
    }
 }
 
-extern "C" void gb_spgemm_gather(int n, const int *Ci, const int *src, const int *tj, const double *tv, int *Cj,
-                                 double *Cv, cudaStream_t s)
+extern "C" void gb_spgemm_gather(int n, long long nnz, const int *Ci, const int *src, const int *tj, const double *tv,
+                                 int *Cj, double *Cv, cudaStream_t s)
 {
-   if (n > 0)
+   if (n <= 0) { return; }
+   const long long avg = nnz / n;
+   if (avg <= 6)
    {
-      k_spgemm_gather<<<gb_blocks((long long) n * 32, 256), 256, 0, s>>>(n, Ci, src, tj, tv, Cj, Cv);
-      GB_COUNT(1);
+      k_spgemm_gather<4><<<gb_blocks((long long) n * 4, 256), 256, 0, s>>>(n, Ci, src, tj, tv, Cj, Cv);
    }
+   else if (avg <= 12)
+   {
+      k_spgemm_gather<8><<<gb_blocks((long long) n * 8, 256), 256, 0, s>>>(n, Ci, src, tj, tv, Cj, Cv);
+   }
+   else if (avg <= 24)
+   {
+      k_spgemm_gather<16><<<gb_blocks((long long) n * 16, 256), 256, 0, s>>>(n, Ci, src, tj, tv, Cj, Cv);
+   }
+   else { k_spgemm_gather<32><<<gb_blocks((long long) n * 32, 256), 256, 0, s>>>(n, Ci, src, tj, tv, Cj, Cv); }
+   GB_COUNT(1);
 }
 
 // ---------------------------------------------------------------------------
