@@ -286,7 +286,14 @@ def gpu_arm(args):
     e1.record(stream)
     torch.cuda.synchronize()
     spmv_s = e0.elapsed_time(e1) / 1e3 / reps
-    spmv_bytes = nnz * 12 + (n + 1) * 4 + 8 * n + 8 * n
+    # SELL-32 form: FP64 values, column indices as 16-bit offsets from the
+    # row when every |j - i| fits (the library's rule), else int32; x read
+    # once, y written once, slice offsets (int64) and widths (int32)
+    rows_of = np.repeat(np.arange(n, dtype=np.int64), np.diff(I))
+    off = J.astype(np.int64) - rows_of
+    idx_bytes = 2 if (off.max(initial=0) <= 32767 and off.min(initial=0) >= -32768) else 4
+    nsl = (n + 31) // 32
+    spmv_bytes = nnz * (8 + idx_bytes) + 8 * n + 8 * n + 12 * nsl
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
     peak = float(peaks.get("hbm_gbs", 6800.0))
@@ -364,7 +371,8 @@ def gpu_arm(args):
                      "frac": sg["bytes"] / sg["seconds"] / 1e9 / peak, "traffic": sg_traffic,
                      "algorithmic_bytes": sg["bytes"], "launch_seconds": sg["seconds"], "products": sg["products"],
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
-        "roofline_spmv": {"bound": "hbm", "kernel": "SpMV level 0 (FP64 values, int32 indices)",
+        "roofline_spmv": {"bound": "hbm", "kernel": "SpMV level 0, SELL-32 (FP64 values, %s column indices)" % (
+                              "16-bit offset" if idx_bytes == 2 else "int32"),
                           "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                           "traffic": traffic, "algorithmic_bytes": spmv_bytes, "launch_seconds": spmv_s,
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},

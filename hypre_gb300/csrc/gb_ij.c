@@ -32,7 +32,7 @@ static void solveform_free(gb_solveform *f)
 
 static void sellstruct_free(gb_sellstruct *S)
 {
-   gb_dfree(S->w); gb_dfree(S->ptr); gb_dfree(S->j);
+   gb_dfree(S->w); gb_dfree(S->ptr); gb_dfree(S->j); gb_dfree(S->j16);
    memset(S, 0, sizeof(*S));
 }
 
@@ -79,13 +79,20 @@ static int sell_struct(gb_parcsr *M, int lower)
    S->w = (int *) gb_dmalloc(sizeof(int) * (size_t) nsl);
    S->ptr = (long long *) gb_dmalloc(sizeof(long long) * (size_t) (nsl + 1));
    if (!S->w || !S->ptr) { sellstruct_free(S); S->state = -1; return 0; }
-   gb_sell_struct(A->nr, A->i, A->j, lower, nsl, S->w, S->ptr, NULL, s, 0);
-   cudaMemcpyAsync(&S->tot, S->ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
+   int *wide = (int *) gb_dmalloc(sizeof(int));
+   long long *htot = (long long *) (gb_red_ints() + 8);
+   int *hwide = gb_red_ints() + 2;
+   gb_sell_struct(A->nr, A->i, A->j, lower, nsl, S->w, S->ptr, NULL, NULL, wide, s, 0);
+   cudaMemcpyAsync(htot, S->ptr + nsl, sizeof(long long), cudaMemcpyDeviceToHost, s);
+   cudaMemcpyAsync(hwide, wide, sizeof(int), cudaMemcpyDeviceToHost, s);
    gb_sync();
+   gb_dfree(wide);
+   S->tot = *htot;
    if (!lower && (double) S->tot > 1.15 * (double) A->nnz) { sellstruct_free(S); S->state = -1; return 0; }
-   S->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (S->tot ? S->tot : 1));
-   if (!S->j) { sellstruct_free(S); S->state = -1; return 0; }
-   gb_sell_struct(A->nr, A->i, A->j, lower, nsl, S->w, S->ptr, S->j, s, 1);
+   if (*hwide == 0) { S->j16 = (short *) gb_dmalloc(sizeof(short) * (size_t) (S->tot ? S->tot : 1)); }
+   else { S->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (S->tot ? S->tot : 1)); }
+   if (!S->j && !S->j16) { sellstruct_free(S); S->state = -1; return 0; }
+   gb_sell_struct(A->nr, A->i, A->j, lower, nsl, S->w, S->ptr, S->j, S->j16, NULL, s, 1);
    S->state = 1;
    return 1;
 }
@@ -133,6 +140,7 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
       f->desc.fmt = GB_FMT_SELL;
       f->desc.nslices = M->sell.nslices;
       f->desc.sl_ptr = M->sell.ptr; f->desc.sl_w = M->sell.w; f->desc.sl_j = M->sell.j; f->desc.sl_v = f->sl_v;
+      f->desc.sl_j16 = M->sell.j16;
    }
    f->valid = 1;
    return &f->desc;
@@ -162,6 +170,7 @@ const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag)
    f->lo.fmt = GB_FMT_SELL;
    f->lo.nslices = M->lsell.nslices;
    f->lo.sl_ptr = M->lsell.ptr; f->lo.sl_w = M->lsell.w; f->lo.sl_j = M->lsell.j; f->lo.sl_v = f->lo_sl_v;
+   f->lo.sl_j16 = M->lsell.j16;
    f->lo.K = 8;
    f->lo_valid = 1;
    *diag = f->lo_diag;

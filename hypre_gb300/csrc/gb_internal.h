@@ -37,7 +37,9 @@ double *gb_red_part(void);                   /* GB_RED_BLOCKS * 4 doubles */
 double *gb_red_out(void);                    /* 8 doubles (device) */
 unsigned int *gb_red_count(void);            /* zeroed counter of one-launch reductions */
 double *gb_red_host(void);                   /* 8 doubles (pinned host) */
-int *gb_red_ints(void);                      /* 16 ints (pinned host): 0 read-backs, 4-5 PMIS counts */
+/* 16 ints (pinned host, 64-byte aligned): 0 setup read-backs, 1 IJ read-backs,
+ * 2 and 8-9 (one int64) SELL sizing, 4-5 PMIS counts */
+int *gb_red_ints(void);
 void  gb_release_scratch(void);
 
 /* --- matrices and vectors -------------------------------------------------- */
@@ -58,7 +60,9 @@ typedef struct
 
 /* SELL-32 structure of a matrix (whole rows, or their strictly lower parts):
  * slice widths and offsets and column indices, shared by the solve forms of
- * every precision; state 1 built, -1 not used, 0 not tried */
+ * every precision; state 1 built, -1 not used, 0 not tried.  The indices are
+ * kept as 16-bit offsets from the row (j16) when every |j - i| < 2^15 (a
+ * banded matrix: 3-D stencils up to 180 points a side), else as j. */
 typedef struct
 {
    int        state;
@@ -67,6 +71,7 @@ typedef struct
    int       *w;
    long long *ptr;
    int       *j;
+   short     *j16;
 } gb_sellstruct;
 
 /* cached solve-phase form of a matrix in one precision */

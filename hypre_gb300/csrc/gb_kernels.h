@@ -43,6 +43,7 @@ typedef struct
    const long long *sl_ptr;
    const int *sl_w;
    const int *sl_j;
+   const short *sl_j16;  /* 16-bit offsets from the row instead of sl_j (NULL: sl_j) */
    const void *sl_v;
    const float *rs;      /* FP16 forms: values are a_ij / a_ii, rs[i] = a_ii (NULL otherwise) */
 } gb_spmv_desc;
@@ -145,8 +146,10 @@ void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int mode, doub
                const double *b, const double *d, double w, const double *dotz, double *dpart, cudaStream_t st);
 void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int mode, float alpha, float beta, const float *b,
                const float *d, float w, const float *dotz, double *dpart, cudaStream_t st);
+/* stage 0: widths, offsets and *wide (1 when some |j - i| >= 2^15); stage 1:
+ * indices into sl_j, or as offsets into sl_j16 when that is given */
 void gb_sell_struct(int n, const int *Ai, const int *Aj, int lower, int nslices, int *sl_w, long long *sl_ptr,
-                    int *sl_j, cudaStream_t s, int stage);
+                    int *sl_j, short *sl_j16, int *wide, cudaStream_t s, int stage);
 void gb_sell_vals(int n, const int *Ai, const int *Aj, const double *Av, int lower, int scaled, int vprec, int nslices,
                   const int *sl_w, const long long *sl_ptr, void *sl_v, cudaStream_t s);
 void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s);

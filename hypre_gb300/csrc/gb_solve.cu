@@ -125,12 +125,22 @@ __global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__
 // ---------------------------------------------------------------------------
 // SELL-32 SpMV: slice s holds rows 32s..32s+31, element k of row 32s+t at
 // sl_ptr[s] + 32k + t, so a warp's loads are fully coalesced (256 B values,
-// 128 B indices per instruction for FP64).  Padding: column 0, value 0.
+// 128 B indices per instruction for FP64).  Padding: a valid column (the
+// row itself, or the last row for rows past n), value 0.
 // ---------------------------------------------------------------------------
+// column of the element stored as IT at Sj[p] for row i: the index itself, or
+// (IT = short) the offset from the row
+template <typename IT>
+__device__ __forceinline__ int sell_col(const IT *__restrict__ Sj, long long p, int i)
+{
+   if constexpr (sizeof(IT) == 2) { return i + (int) __ldg(Sj + p); }
+   else { return __ldg(Sj + p); }
+}
+
 // GS: the two-stage Gauss-Seidel epilogue (mode 6), which also updates b
-template <typename VT, typename XT, bool GS>
+template <typename VT, typename XT, bool GS, typename IT>
 __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const long long *__restrict__ sl_ptr,
-                                                   const int *__restrict__ sl_w, const int *__restrict__ Sj,
+                                                   const int *__restrict__ sl_w, const IT *__restrict__ Sj,
                                                    const VT *__restrict__ Sv, const XT *__restrict__ x, XT *y,
                                                    int mode, XT alpha, XT beta, const XT *b, const XT *d, XT w,
                                                    const XT *__restrict__ dotz, double *dpart,
@@ -145,12 +155,13 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
    {
       long long base = __ldg(sl_ptr + s) + t;
       int width = __ldg(sl_w + s);
+      const int i = s * 32 + t;
       AT acc0 = 0, acc1 = 0;
       int k = 0;
       for (; k + 1 < width; k += 2)
       {
          long long p0 = base + (long long) k * 32, p1 = p0 + 32;
-         int j0 = __ldg(Sj + p0), j1 = __ldg(Sj + p1);
+         int j0 = sell_col(Sj, p0, i), j1 = sell_col(Sj, p1, i);
          VT a0 = __ldg(Sv + p0), a1 = __ldg(Sv + p1);
          acc0 += Acc<VT, XT>::mul(a0, __ldg(x + j0));
          acc1 += Acc<VT, XT>::mul(a1, __ldg(x + j1));
@@ -158,9 +169,8 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
       if (k < width)
       {
          long long p0 = base + (long long) k * 32;
-         acc0 += Acc<VT, XT>::mul(__ldg(Sv + p0), __ldg(x + __ldg(Sj + p0)));
+         acc0 += Acc<VT, XT>::mul(__ldg(Sv + p0), __ldg(x + sell_col(Sj, p0, i)));
       }
-      int i = s * 32 + t;
       if (i < n)
       {
          XT si = (XT) (acc0 + acc1);
@@ -182,21 +192,31 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
 // rows; lower: only the entries j < i), offsets, then column indices and
 // values (values converted to VT, optionally divided by the row's first
 // entry for the row-scaled FP16 forms).  One warp per slice, one lane per row.
+// *wide = 1 when a kept entry is 2^15 or more columns from its row
 __global__ void k_sell_width(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj, int lower,
-                             int *__restrict__ w)
+                             int *__restrict__ w, int *wide)
 {
    const int i = blockIdx.x * blockDim.x + threadIdx.x;
    const int s = i >> 5;
    if (s >= nslices) { return; }
    int l = 0;
+   bool far = false;
    if (i < n)
    {
       const int b = Ai[i], e = Ai[i + 1];
-      if (!lower) { l = e - b; }
-      else { for (int k = b; k < e; k++) { l += Aj[k] < i; } }
+      for (int k = b; k < e; k++)
+      {
+         const int j = Aj[k];
+         if (!lower || j < i)
+         {
+            l++;
+            far |= j - i > 32767 || i - j > 32768;
+         }
+      }
    }
    for (int o = 16; o > 0; o >>= 1) { l = max(l, __shfl_xor_sync(GB_FULL, l, o)); }
    if ((i & 31) == 0) { w[s] = l; }
+   if (__any_sync(GB_FULL, far) && (i & 31) == 0) { *wide = 1; }
 }
 
 // slice offsets: block-level scans of width*32 (int64), then block offsets
@@ -248,26 +268,31 @@ __global__ void k_sell_ptr_fix(int nslices, long long *__restrict__ ptr, const l
    if (blockIdx.x == nblocks - 1 && threadIdx.x == 0) { ptr[nslices] = off + bsum[blockIdx.x]; }
 }
 
+// IT = short: offsets j - i (checked to fit by k_sell_width)
+template <typename IT>
 __global__ void k_sell_fill_j(int n, int nslices, const int *__restrict__ Ai, const int *__restrict__ Aj,
                               const long long *__restrict__ ptr, const int *__restrict__ w, int lower,
-                              int *__restrict__ Sj)
+                              IT *__restrict__ Sj)
 {
    const int i = blockIdx.x * blockDim.x + threadIdx.x;
    const int s = i >> 5;
    if (s >= nslices) { return; }
    const int width = w[s];
    const long long base = ptr[s] + (i & 31);
+   const int rel = sizeof(IT) == 2 ? i : 0;
    int k = 0;
    if (i < n)
    {
       for (int q = Ai[i]; q < Ai[i + 1]; q++)
       {
          const int j = Aj[q];
-         if (!lower || j < i) { Sj[base + (long long) k * 32] = j; k++; }
+         if (!lower || j < i) { Sj[base + (long long) k * 32] = (IT) (j - rel); k++; }
       }
    }
-   // padding: the row's own index (a valid column) with value 0
-   for (; k < width; k++) { Sj[base + (long long) k * 32] = i < n ? i : 0; }
+   // padding: the row's own index (rows past n: the last row, at most 31
+   // rows back) with value 0
+   const int pad = i < n ? i : (n > 0 ? n - 1 : 0);
+   for (; k < width; k++) { Sj[base + (long long) k * 32] = (IT) (pad - rel); }
 }
 
 template <typename VT>
@@ -338,17 +363,20 @@ static void spmv_dispatch(const gb_spmv_desc *A, const XT *x, XT *y, int mode, X
    {
       int nsl = A->nslices;
       int blocks = dpart ? GB_RED_BLOCKS : nblk((long long) nsl * 32, T);
+#define GB_SELL(GS, IT, J)                                                                                         \
+   k_spmv_sell<VT, XT, GS, IT><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, J, (const VT *) A->sl_v, x, y, \
+                                                     mode, alpha, beta, b, d, w, dotz, dpart, A->rs)
       if (mode == GB_EPI_GS)
       {
-         k_spmv_sell<VT, XT, true><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, A->sl_j, (const VT *) A->sl_v,
-                                                        x, y, mode, alpha, beta, b, d, w, dotz, dpart, A->rs);
+         if (A->sl_j16) { GB_SELL(true, short, A->sl_j16); }
+         else { GB_SELL(true, int, A->sl_j); }
       }
       else
       {
-         k_spmv_sell<VT, XT, false><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, A->sl_j,
-                                                         (const VT *) A->sl_v, x, y, mode, alpha, beta, b, d, w, dotz,
-                                                         dpart, A->rs);
+         if (A->sl_j16) { GB_SELL(false, short, A->sl_j16); }
+         else { GB_SELL(false, int, A->sl_j); }
       }
+#undef GB_SELL
    }
    else
    {
@@ -391,14 +419,15 @@ extern "C" void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int m
 }
 
 extern "C" void gb_sell_struct(int n, const int *Ai, const int *Aj, int lower, int nslices, int *sl_w,
-                               long long *sl_ptr, int *sl_j, cudaStream_t s, int stage)
+                               long long *sl_ptr, int *sl_j, short *sl_j16, int *wide, cudaStream_t s, int stage)
 {
    // stage 0: widths + offsets (caller then reads sl_ptr[nslices] to size
-   // the arrays); stage 1: column indices
+   // the arrays) and the wide flag; stage 1: column indices or offsets
    const long long nt = (long long) nslices * 32;
    if (stage == 0)
    {
-      k_sell_width<<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, lower, sl_w);
+      cudaMemsetAsync(wide, 0, sizeof(int), s);
+      k_sell_width<<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, lower, sl_w, wide);
       int nb = nblk(nslices, 1024);
       long long *bsum = NULL;
       cudaMallocAsync((void **) &bsum, sizeof(long long) * (size_t) nb, s);
@@ -408,7 +437,8 @@ extern "C" void gb_sell_struct(int n, const int *Ai, const int *Aj, int lower, i
       GB_COUNT(3);
       return;
    }
-   k_sell_fill_j<<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, sl_ptr, sl_w, lower, sl_j);
+   if (sl_j16) { k_sell_fill_j<short><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, sl_ptr, sl_w, lower, sl_j16); }
+   else { k_sell_fill_j<int><<<nblk(nt, 256), 256, 0, s>>>(n, nslices, Ai, Aj, sl_ptr, sl_w, lower, sl_j); }
    GB_COUNT(1);
 }
 
