@@ -689,10 +689,19 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    /* count and fill in one pass into temporary areas sized by each row's
     * upper bound (capped by the shared-memory table), then the rows that did
     * not fit with global tables (count, then fill in place) */
+   /* every point's candidate list: itself when a C point, then the C points
+    * of its S row (coarse indices) */
+   int *Li = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *lcnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_s2_lists(n, S->i, S->j, CF, f2c1, lcnt, NULL, NULL, s);
+   int nl = scan_total(lcnt, Li, n);
+   gb_dfree(lcnt);
+   int *Lj = (int *) gb_dmalloc(sizeof(int) * (size_t) (nl > 0 ? nl : 1));
+   gb_s2_lists(n, S->i, S->j, CF, f2c1, NULL, Li, Lj, s);
    int *ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 > 0 ? nc1 : 1));
    int *cap = (int *) gb_dmalloc(sizeof(int) * (size_t) (nc1 + 1));
    unsigned long long *dsum = (unsigned long long *) gb_dcalloc(sizeof(unsigned long long));
-   gb_strength2_ub(nc1, c2f1, S->i, S->j, ub, s);
+   gb_strength2_ub(nc1, c2f1, S->i, S->j, Li, ub, s);
    gb_cap_sum(nc1, ub, GB_SPGEMM_LCAP0, cap, dsum, s);
    unsigned long long hsum = 0;
    cudaMemcpyAsync(&hsum, dsum, sizeof(hsum), cudaMemcpyDeviceToHost, s);
@@ -711,13 +720,13 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    }
    else
    {
-      gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, tofs, tj, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, src, 2,
+      gb_strength2(nc1, c2f1, Li, Lj, S->i, S->j, cnt, tofs, tj, t.ovf_list, t.ovf_n, NULL, 0, 0, t.err, src, 2,
                    0, s);
    }
    tier_global(&t, ub, nc1);
    if (t.h_ovf > 0)
    {
-      gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, NULL, NULL, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
+      gb_strength2(nc1, c2f1, Li, Lj, S->i, S->j, cnt, NULL, NULL, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
                    t.err, NULL, 0, 1, s);
    }
    gb_mark_isolated(nc1, c2f1, cnt, CF, s);
@@ -727,10 +736,10 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    gb_spgemm_gather(nc1, S2.nnz, S2.i, src, tj, NULL, S2.j, NULL, s);
    if (t.h_ovf > 0)
    {
-      gb_strength2(nc1, c2f1, f2c1, S->i, S->j, CF, cnt, S2.i, S2.j, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
+      gb_strength2(nc1, c2f1, Li, Lj, S->i, S->j, cnt, S2.i, S2.j, t.ovf_list, t.ovf_n, t.gtab, t.gcap, t.gwarps,
                    t.err, NULL, 1, 1, s);
    }
-   gb_dfree(tofs); gb_dfree(tj); gb_dfree(src);
+   gb_dfree(tofs); gb_dfree(tj); gb_dfree(src); gb_dfree(Li); gb_dfree(Lj);
    if (tier_end(&t)) { gb_error(HYPRE_ERROR_GENERIC, "second-order strength overflow"); return -1; }
    gb_dfree(ub);
    /* PMIS on S2 with CF_init 3 */

@@ -117,11 +117,15 @@ void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);
 void gb_list_flags(int nlist, const int *dcount, const int *list, int *flag, cudaStream_t s);
 void gb_scatter_list(int n, const int *flag, const int *scan, int *list, cudaStream_t s);
-void gb_strength2(int nc, const int *c2f, const int *f2c, const int *Si, const int *Sj, const int *CF, int *cnt,
+/* second-order strength: the candidate lists (Lj NULL: counts into cnt;
+ * else the lists at Li), then the rows */
+void gb_s2_lists(int n, const int *Si, const int *Sj, const int *CF, const int *f2c, int *cnt, const int *Li,
+                 int *Lj, cudaStream_t s);
+void gb_strength2(int nc, const int *c2f, const int *Li, const int *Lj, const int *Si, const int *Sj, int *cnt,
                   const int *S2i, int *S2j, int *ovf_list, int *ovf_n, int *gtab, int gcap, int gwarps, int *err,
                   int *src, int fill, int tier, cudaStream_t s);
+void gb_strength2_ub(int nc, const int *c2f, const int *Si, const int *Sj, const int *Li, int *ub, cudaStream_t s);
 void gb_cap_sum(int n, const int *ub, int lcap, int *cap, unsigned long long *sum, cudaStream_t s);
-void gb_strength2_ub(int nc, const int *c2f, const int *Si, const int *Sj, int *ub, cudaStream_t s);
 void gb_mark_isolated(int nc, const int *c2f, const int *cnt, int *CF, cudaStream_t s);
 void gb_correct_cf2(int n, const int *f2c, const int *CFN, int *CF, cudaStream_t s);
 void gb_cf_clamp(int n, int *CF, cudaStream_t s);
