@@ -367,6 +367,7 @@ __global__ void k_fffc_count(int nf, const int *__restrict__ fl, const int *__re
    cfc[r] = fc;
 }
 
+template <int LPR>
 __global__ void k_fffc_fill(int nf, const int *__restrict__ fl, const int *__restrict__ Ai,
                             const int *__restrict__ Aj, const double *__restrict__ Av, const int *__restrict__ Si,
                             const int *__restrict__ Sj, const int *__restrict__ CF, const int *__restrict__ f2c,
@@ -374,14 +375,18 @@ __global__ void k_fffc_fill(int nf, const int *__restrict__ fl, const int *__res
                             double *__restrict__ FFv, const int *__restrict__ FCi, int *__restrict__ FCj,
                             double *__restrict__ FCv)
 {
-   /* one warp per F row.  S_i is A_i's off-diagonal columns filtered in
-    * order (the reference looks each S entry up in A_i), and A_i's columns
-    * are distinct, so an A entry is strong iff its column occurs among the
-    * next 32 unmatched S entries; ballot prefixes keep the A order, which
-    * is the S order of the sequential fill */
-   int r = (int) ((blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5);
-   int lane = threadIdx.x & 31;
-   if (r >= nf) { return; }
+   /* LPR lanes per F row (a segment of the warp).  S_i is A_i's
+    * off-diagonal columns filtered in order (the reference looks each S
+    * entry up in A_i), and A_i's columns are distinct, so an A entry of a
+    * chunk of LPR is strong iff its column occurs among the next LPR
+    * unmatched S entries; ballot prefixes keep the A order, which is the S
+    * order of the sequential fill */
+   const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+   const int r = (int) (g / LPR);
+   const int lane = (int) (g % LPR);
+   if (r >= nf) { return; }   // whole segments leave together
+   const int sbase = (threadIdx.x & 31) & ~(LPR - 1);
+   const unsigned seg = LPR == 32 ? 0xffffffffu : (((1u << LPR) - 1u) << sbase);
    int i = fl[r];
    int pf = FFi[r], pc = FCi[r];
    int a0 = Ai[i], a1 = Ai[i + 1];
@@ -390,17 +395,17 @@ __global__ void k_fffc_fill(int nf, const int *__restrict__ fl, const int *__res
    pf += hasdiag;
    int s0 = Si[i], s1 = Si[i + 1];
    unsigned lt = (1u << lane) - 1u;
-   for (int base = a0 + hasdiag; base < a1 && s0 < s1; base += 32)
+   for (int base = a0 + hasdiag; base < a1 && s0 < s1; base += LPR)
    {
       int p = base + lane;
       int c = (p < a1) ? Aj[p] : -1;
-      int ns = min(32, s1 - s0);
+      int ns = min(LPR, s1 - s0);
       int sj = (lane < ns) ? Sj[s0 + lane] : -2;
       bool in = false;
-      for (int t = 0; t < ns; t++) { in |= (c == __shfl_sync(0xffffffffu, sj, t)); }
+      for (int t = 0; t < ns; t++) { in |= (c == __shfl_sync(seg, sj, t, LPR)); }
       bool isc = in && CF[c] > 0;
       bool isf = in && !isc;
-      unsigned bc = __ballot_sync(0xffffffffu, isc), bf = __ballot_sync(0xffffffffu, isf);
+      unsigned bc = __ballot_sync(seg, isc) >> sbase, bf = __ballot_sync(seg, isf) >> sbase;
       if (isc) { int q = pc + __popc(bc & lt); FCj[q] = f2c[c]; FCv[q] = Av[p]; }
       if (isf) { int q = pf + __popc(bf & lt); FFj[q] = f2f[c]; FFv[q] = Av[p]; }
       pc += __popc(bc);
@@ -416,12 +421,20 @@ extern "C" void gb_fffc_count(int nf, const int *fl, const int *Ai, const int *A
    GB_COUNT(1);
 }
 
-extern "C" void gb_fffc_fill(int nf, const int *fl, const int *Ai, const int *Aj, const double *Av, const int *Si,
-                             const int *Sj, const int *CF, const int *f2c, const int *f2f, const int *FFi, int *FFj,
-                             double *FFv, const int *FCi, int *FCj, double *FCv, cudaStream_t s)
+extern "C" void gb_fffc_fill(int nf, int nrows, long long nnz, const int *fl, const int *Ai, const int *Aj,
+                             const double *Av, const int *Si, const int *Sj, const int *CF, const int *f2c,
+                             const int *f2f, const int *FFi, int *FFj, double *FFv, const int *FCi, int *FCj,
+                             double *FCv, cudaStream_t s)
 {
-   k_fffc_fill<<<gb_blocks2((long long) nf * 32, 256), 256, 0, s>>>(nf, fl, Ai, Aj, Av, Si, Sj, CF, f2c, f2f, FFi, FFj, FFv, FCi,
-                                                   FCj, FCv);
+   // lanes per row from the mean row length of A (27-point: 16)
+   const long long avg = nf > 0 ? (long long) nnz / (nrows > 0 ? nrows : 1) : 0;
+#define GB_FFFC(L)                                                                                                 \
+   k_fffc_fill<L><<<gb_blocks2((long long) nf * L, 256), 256, 0, s>>>(nf, fl, Ai, Aj, Av, Si, Sj, CF, f2c, f2f, FFi, \
+                                                                      FFj, FFv, FCi, FCj, FCv)
+   if (avg <= 10) { GB_FFFC(8); }
+   else if (avg <= 40) { GB_FFFC(16); }
+   else { GB_FFFC(32); }
+#undef GB_FFFC
    GB_COUNT(1);
 }
 

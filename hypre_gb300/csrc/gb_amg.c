@@ -771,7 +771,8 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    FF.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
    FC.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FC.nnz ? FC.nnz : 1));
    FC.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FC.nnz ? FC.nnz : 1));
-   gb_fffc_fill(nf, fl, A->i, A->j, A->v, S->i, S->j, CF, f2c1, f2f, FF.i, FF.j, FF.v, FC.i, FC.j, FC.v, s);
+   gb_fffc_fill(nf, n, A->nnz, fl, A->i, A->j, A->v, S->i, S->j, CF, f2c1, f2f, FF.i, FF.j, FF.v, FC.i, FC.j, FC.v,
+                s);
    {
       double *tmp = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
       double *Dq = (double *) gb_dmalloc(sizeof(double) * (size_t) (nf ? nf : 1));

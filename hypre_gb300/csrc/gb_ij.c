@@ -135,8 +135,23 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
    f->desc.fmt = GB_FMT_CSR;
    if (sell_struct(M, 0))
    {
-      f->sl_v = gb_dmalloc(vbytes(vprec) * (size_t) (M->sell.tot ? M->sell.tot : 1));
-      gb_sell_vals(A->nr, A->i, A->j, A->v, 0, scaled, vprec, M->sell.nslices, M->sell.w, M->sell.ptr, f->sl_v, s);
+      /* FP64 values that are all exact in FP32 (stencils with small integer
+       * coefficients) are held as FP32 and widened exactly in the kernel */
+      int svp = vprec;
+      if (vprec == GB_PREC_F64)
+      {
+         int *flag = (int *) gb_dmalloc(sizeof(int));
+         int *hflag = gb_red_ints() + 3;
+         gb_exact32(A->nnz, A->v, flag, s);
+         cudaMemcpyAsync(hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+         gb_sync();
+         gb_dfree(flag);
+         f->exact32 = *hflag == 0;
+         if (f->exact32) { svp = GB_PREC_F32; }
+      }
+      f->sl_v = gb_dmalloc(vbytes(svp) * (size_t) (M->sell.tot ? M->sell.tot : 1));
+      gb_sell_vals(A->nr, A->i, A->j, A->v, 0, scaled, svp, M->sell.nslices, M->sell.w, M->sell.ptr, f->sl_v, s);
+      f->desc.sl_v32 = f->exact32;
       f->desc.fmt = GB_FMT_SELL;
       f->desc.nslices = M->sell.nslices;
       f->desc.sl_ptr = M->sell.ptr; f->desc.sl_w = M->sell.w; f->desc.sl_j = M->sell.j; f->desc.sl_v = f->sl_v;
@@ -155,8 +170,9 @@ const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag)
    cudaStream_t s = gb_stream();
    gb_csr *A = &M->A;
    int n = A->nr;
-   f->lo_sl_v = gb_dmalloc(vbytes(vprec) * (size_t) (M->lsell.tot ? M->lsell.tot : 1));
-   gb_sell_vals(n, A->i, A->j, A->v, 1, vprec == GB_PREC_F16, vprec, M->lsell.nslices, M->lsell.w, M->lsell.ptr,
+   const int svp = (vprec == GB_PREC_F64 && f->exact32) ? GB_PREC_F32 : vprec;
+   f->lo_sl_v = gb_dmalloc(vbytes(svp) * (size_t) (M->lsell.tot ? M->lsell.tot : 1));
+   gb_sell_vals(n, A->i, A->j, A->v, 1, vprec == GB_PREC_F16, svp, M->lsell.nslices, M->lsell.w, M->lsell.ptr,
                 f->lo_sl_v, s);
    /* the diagonal in the vector precision (FP16 forms: unit diagonal) */
    if (vprec != GB_PREC_F16)
@@ -171,6 +187,7 @@ const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag)
    f->lo.nslices = M->lsell.nslices;
    f->lo.sl_ptr = M->lsell.ptr; f->lo.sl_w = M->lsell.w; f->lo.sl_j = M->lsell.j; f->lo.sl_v = f->lo_sl_v;
    f->lo.sl_j16 = M->lsell.j16;
+   f->lo.sl_v32 = vprec == GB_PREC_F64 && f->exact32;
    f->lo.K = 8;
    f->lo_valid = 1;
    *diag = f->lo_diag;

@@ -38,7 +38,7 @@ double *gb_red_out(void);                    /* 8 doubles (device) */
 unsigned int *gb_red_count(void);            /* zeroed counter of one-launch reductions */
 double *gb_red_host(void);                   /* 8 doubles (pinned host) */
 /* 16 ints (pinned host, 64-byte aligned): 0 setup read-backs, 1 IJ read-backs,
- * 2 and 8-9 (one int64) SELL sizing, 4-5 PMIS counts */
+ * 2 and 8-9 (one int64) SELL sizing, 3 FP32-exactness flag, 4-5 PMIS counts */
 int *gb_red_ints(void);
 void  gb_release_scratch(void);
 
@@ -81,7 +81,8 @@ typedef struct
    int          vprec;
    gb_spmv_desc desc;
    void        *vals;      /* CSR values in vprec (NULL when vprec == F64) */
-   void        *sl_v;      /* SELL values in vprec */
+   void        *sl_v;      /* SELL values in vprec (FP64 form: FP32 when exact32) */
+   int          exact32;   /* FP64 form: every value is zero or a normal FP32 number */
    float       *rs;        /* FP16 form: row scales a_ii */
    /* strictly lower part as SELL-32 and the diagonal (in the vector
     * precision; none for the unit-diagonal FP16 form), for two-stage

@@ -45,6 +45,7 @@ typedef struct
    const int *sl_j;
    const short *sl_j16;  /* 16-bit offsets from the row instead of sl_j (NULL: sl_j) */
    const void *sl_v;
+   int        sl_v32;    /* FP64 form whose SELL values are held as FP32 (every value exact in FP32) */
    const float *rs;      /* FP16 forms: values are a_ij / a_ii, rs[i] = a_ii (NULL otherwise) */
 } gb_spmv_desc;
 
@@ -131,9 +132,10 @@ void gb_correct_cf2(int n, const int *f2c, const int *CFN, int *CF, cudaStream_t
 void gb_cf_clamp(int n, int *CF, cudaStream_t s);
 void gb_fffc_count(int nf, const int *fl, const int *Ai, const int *Aj, const int *Si, const int *Sj, const int *CF,
                    int *cff, int *cfc, cudaStream_t s);
-void gb_fffc_fill(int nf, const int *fl, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj,
-                  const int *CF, const int *f2c, const int *f2f, const int *FFi, int *FFj, double *FFv,
-                  const int *FCi, int *FCj, double *FCv, cudaStream_t s);
+/* nrows, nnz: A's size (the mean row length picks the lanes per row) */
+void gb_fffc_fill(int nf, int nrows, long long nnz, const int *fl, const int *Ai, const int *Aj, const double *Av,
+                  const int *Si, const int *Sj, const int *CF, const int *f2c, const int *f2f, const int *FFi,
+                  int *FFj, double *FFv, const int *FCi, int *FCj, double *FCv, cudaStream_t s);
 void gb_mod_extpi_scale(int nf, int nnzff, const int *fl, const int *Ai, const double *Av, const int *FFi,
                         const int *FFj, double *FFv, const int *FCi, const double *FCv, double *tmp, double *Dq,
                         double *Dw, cudaStream_t s);
@@ -157,6 +159,8 @@ void gb_sell_struct(int n, const int *Ai, const int *Aj, int lower, int nslices,
 void gb_sell_vals(int n, const int *Ai, const int *Aj, const double *Av, int lower, int scaled, int vprec, int nslices,
                   const int *sl_w, const long long *sl_ptr, void *sl_v, cudaStream_t s);
 void gb_convert_vals(long long nnz, const double *in, void *out, int vprec, cudaStream_t s);
+/* *flag = 1 unless every value is zero or a normal FP32 number exactly */
+void gb_exact32(long long nnz, const double *v, int *flag, cudaStream_t s);
 void gb_row_scaled_half(int n, const int *Ai, const double *Av, void *out, float *rs, cudaStream_t s);
 void gb_gs_first_d(int n, const int *Ai, const double *Av, double *v, double *u, cudaStream_t s);
 void gb_gs_first_f(int n, const int *Ai, const void *Av, int vprec, const float *rs, float *v, float *u,

@@ -33,6 +33,44 @@ template <> struct Acc<__half, float>
    typedef float T;
    static __device__ __forceinline__ float mul(__half a, float x) { return __half2float(a) * x; }
 };
+// FP64 values held as FP32 because every one of them is a normal FP32 number
+// or zero (checked when the form is built): widened exactly with integer
+// operations (exponent rebiased by 1023 - 127, mantissa shifted by 29 bits),
+// so the products and sums are those of the FP64 values, bit for bit
+__device__ __forceinline__ double gb_widen_exact(float a)
+{
+   const unsigned u = __float_as_uint(a);
+   const unsigned long long sign = (unsigned long long) (u & 0x80000000u) << 32;
+   const unsigned em = u & 0x7fffffffu;
+   if (em == 0) { return __longlong_as_double((long long) sign); }
+   return __longlong_as_double((long long) (sign | (((unsigned long long) em << 29) + (896ULL << 52))));
+}
+template <> struct Acc<float, double>
+{
+   typedef double T;
+   static __device__ __forceinline__ double mul(float a, double x) { return gb_widen_exact(a) * x; }
+};
+
+// flag = 1 when some value is not zero or a normal FP32 number exactly
+__global__ void k_exact32(long long nnz, const double *__restrict__ v, int *flag)
+{
+   const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+   bool bad = false;
+   if (k < nnz)
+   {
+      const double x = v[k];
+      const float f = (float) x;
+      const unsigned e = (__float_as_uint(f) >> 23) & 0xffu;
+      bad = x != 0.0 && ((double) f != x || e == 0u || e == 0xffu);
+   }
+   if (__any_sync(GB_FULL, bad) && (threadIdx.x & 31) == 0) { *flag = 1; }
+}
+
+extern "C" void gb_exact32(long long nnz, const double *v, int *flag, cudaStream_t s)
+{
+   cudaMemsetAsync(flag, 0, sizeof(int), s);
+   if (nnz > 0) { k_exact32<<<nblk(nnz, 256), 256, 0, s>>>(nnz, v, flag); GB_COUNT(1); }
+}
 
 // Epilogue of a row: mode 0  y = alpha*s + beta*b
 //                    mode 1  y = x_i + w*(b_i - s)/d_i   (l1 / diagonal Jacobi)
@@ -402,7 +440,11 @@ extern "C" void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int
                           const double *b, const double *d, double w, const double *dotz, double *dpart,
                           cudaStream_t st)
 {
-   spmv_dispatch<double, double>(A, x, y, mode, alpha, beta, b, d, w, dotz, dpart, st);
+   if (A->fmt == GB_FMT_SELL && A->sl_v32)
+   {
+      spmv_dispatch<float, double>(A, x, y, mode, alpha, beta, b, d, w, dotz, dpart, st);
+   }
+   else { spmv_dispatch<double, double>(A, x, y, mode, alpha, beta, b, d, w, dotz, dpart, st); }
 }
 
 extern "C" void gb_spmv_f(const gb_spmv_desc *A, const float *x, float *y, int mode, float alpha, float beta,
