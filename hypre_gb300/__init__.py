@@ -54,7 +54,12 @@ def _declare(L):
         "HYPRE_IJVectorInitialize": [vp], "HYPRE_IJVectorSetValues": [vp, i32, vp, vp],
         "HYPRE_IJVectorAddToValues": [vp, i32, vp, vp], "HYPRE_IJVectorAssemble": [vp],
         "HYPRE_IJVectorGetObject": [vp, P(vp)], "HYPRE_IJVectorGetValues": [vp, i32, vp, vp],
-        "HYPRE_IJVectorDestroy": [vp],
+        "HYPRE_IJVectorDestroy": [vp], "HYPRE_IJVectorGetLocalRange": [vp, P(i32), P(i32)],
+        "HYPRE_IJMatrixRead": [C.c_char_p, i32, i32, P(vp)], "HYPRE_IJMatrixReadMM": [C.c_char_p, i32, i32, P(vp)],
+        "HYPRE_IJMatrixReadBinary": [C.c_char_p, i32, i32, P(vp)],
+        "HYPRE_IJMatrixPrint": [vp, C.c_char_p], "HYPRE_IJMatrixPrintBinary": [vp, C.c_char_p],
+        "HYPRE_IJVectorRead": [C.c_char_p, i32, i32, P(vp)], "HYPRE_IJVectorReadBinary": [C.c_char_p, i32, i32, P(vp)],
+        "HYPRE_IJVectorPrint": [vp, C.c_char_p], "HYPRE_IJVectorPrintBinary": [vp, C.c_char_p],
         "HYPRE_ParVectorCreate": [i32, i32, vp, P(vp)], "HYPRE_ParVectorInitialize": [vp],
         "HYPRE_ParVectorDestroy": [vp],
         "HYPRE_ParVectorInnerProd": [vp, vp, P(f64)], "HYPRE_ParVectorSetConstantValues": [vp, f64],

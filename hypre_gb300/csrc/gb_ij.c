@@ -999,16 +999,30 @@ static HYPRE_Int ijm_put(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, co
    return gb_error_flag;
 }
 
+/* ncols NULL: one column per row (the reference accepts it,
+ * src/IJ_mv/HYPRE_IJMatrix.c:271-320, and its setters read 1) */
+static HYPRE_Int ijm_put_ones(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, const HYPRE_BigInt *rows,
+                              const HYPRE_BigInt *cols, const HYPRE_Complex *values, int add)
+{
+   if (ncols || nrows <= 0) { return ijm_put(m, nrows, ncols, rows, cols, values, add); }
+   int *ones = (int *) malloc(sizeof(int) * (size_t) nrows);
+   if (!ones) { gb_error(HYPRE_ERROR_MEMORY, "IJ matrix"); return gb_error_flag; }
+   for (int t = 0; t < nrows; t++) { ones[t] = 1; }
+   ijm_put(m, nrows, ones, rows, cols, values, add);
+   free(ones);
+   return gb_error_flag;
+}
+
 HYPRE_Int HYPRE_IJMatrixSetValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, const HYPRE_BigInt *rows,
                                   const HYPRE_BigInt *cols, const HYPRE_Complex *values)
 {
-   return ijm_put(m, nrows, ncols, rows, cols, values, 0);
+   return ijm_put_ones(m, nrows, ncols, rows, cols, values, 0);
 }
 
 HYPRE_Int HYPRE_IJMatrixAddToValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int *ncols, const HYPRE_BigInt *rows,
                                     const HYPRE_BigInt *cols, const HYPRE_Complex *values)
 {
-   return ijm_put(m, nrows, ncols, rows, cols, values, 1);
+   return ijm_put_ones(m, nrows, ncols, rows, cols, values, 1);
 }
 
 HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
@@ -1188,6 +1202,16 @@ HYPRE_Int HYPRE_IJVectorCreate(MPI_Comm comm, HYPRE_BigInt jlower, HYPRE_BigInt 
    v->jlower = jlower; v->jupper = jupper; v->n = jupper - jlower + 1;
    v->num_components = 1;
    *vector = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorGetLocalRange(HYPRE_IJVector v, HYPRE_BigInt *jlower, HYPRE_BigInt *jupper)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (!jlower) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!jupper) { gb_error_in_arg(3); return gb_error_flag; }
+   *jlower = v->jlower;
+   *jupper = v->jupper;
    return gb_error_flag;
 }
 

@@ -106,6 +106,17 @@ HYPRE_Int HYPRE_IJMatrixGetObject(HYPRE_IJMatrix matrix, void **object);  /* :31
 HYPRE_Int HYPRE_IJMatrixSetRowSizes(HYPRE_IJMatrix matrix, const HYPRE_Int *sizes); /* :321 */
 HYPRE_Int HYPRE_IJMatrixSetDiagOffdSizes(HYPRE_IJMatrix matrix, const HYPRE_Int *diag_sizes,
                                          const HYPRE_Int *offdiag_sizes);  /* :336 */
+/* files, one process: "<filename>.00000" (IJ text), "<filename>" (Matrix
+ * Market coordinate real/integer, general or symmetric), "<filename>.00000.bin"
+ * (binary IJ, 32- or 64-bit indices, FP32 or FP64 values); type HYPRE_PARCSR */
+HYPRE_Int HYPRE_IJMatrixRead(const char *filename, MPI_Comm comm, HYPRE_Int type,
+                             HYPRE_IJMatrix *matrix);                      /* :406 */
+HYPRE_Int HYPRE_IJMatrixReadMM(const char *filename, MPI_Comm comm, HYPRE_Int type,
+                               HYPRE_IJMatrix *matrix);                    /* :414 */
+HYPRE_Int HYPRE_IJMatrixPrint(HYPRE_IJMatrix matrix, const char *filename); /* :422 */
+HYPRE_Int HYPRE_IJMatrixPrintBinary(HYPRE_IJMatrix matrix, const char *filename); /* :452 */
+HYPRE_Int HYPRE_IJMatrixReadBinary(const char *filename, MPI_Comm comm, HYPRE_Int type,
+                                   HYPRE_IJMatrix *matrix);                /* :458 */
 
 /* --- IJ vector: src/IJ_mv/HYPRE_IJ_mv.h ------------------------------------ */
 HYPRE_Int HYPRE_IJVectorCreate(MPI_Comm comm, HYPRE_BigInt jlower, HYPRE_BigInt jupper,
@@ -123,6 +134,14 @@ HYPRE_Int HYPRE_IJVectorGetValues(HYPRE_IJVector vector, HYPRE_Int nvalues,
                                   const HYPRE_BigInt *indices, HYPRE_Complex *values); /* :667 */
 HYPRE_Int HYPRE_IJVectorSetObjectType(HYPRE_IJVector vector, HYPRE_Int type); /* :680 */
 HYPRE_Int HYPRE_IJVectorGetObject(HYPRE_IJVector vector, void **object);  /* :701 */
+HYPRE_Int HYPRE_IJVectorGetLocalRange(HYPRE_IJVector vector, HYPRE_BigInt *jlower,
+                                      HYPRE_BigInt *jupper);               /* :692 */
+HYPRE_Int HYPRE_IJVectorRead(const char *filename, MPI_Comm comm, HYPRE_Int type,
+                             HYPRE_IJVector *vector);                      /* :715 */
+HYPRE_Int HYPRE_IJVectorReadBinary(const char *filename, MPI_Comm comm, HYPRE_Int type,
+                                   HYPRE_IJVector *vector);                /* :723 */
+HYPRE_Int HYPRE_IJVectorPrint(HYPRE_IJVector vector, const char *filename); /* :731 */
+HYPRE_Int HYPRE_IJVectorPrintBinary(HYPRE_IJVector vector, const char *filename); /* :737 */
 
 /* --- ParCSR matrix / vector: src/parcsr_mv/HYPRE_parcsr_mv.h --------------- */
 HYPRE_Int HYPRE_ParCSRMatrixGetDims(HYPRE_ParCSRMatrix matrix, HYPRE_BigInt *M, HYPRE_BigInt *N); /* :105 */
