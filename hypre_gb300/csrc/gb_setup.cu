@@ -31,7 +31,9 @@ static int gb_blocks(long long n, int t) { long long b = (n + t - 1) / t; return
 #define SCAN_PER 4
 #define SCAN_TILE (SCAN_T * SCAN_PER)
 
-__global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, int *__restrict__ sums, int n)
+// last: where a single-tile scan also writes its total (out + n), else NULL
+__global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, int *__restrict__ sums, int n,
+                            int *last)
 {
    __shared__ int ws[SCAN_T / 32];
    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER;
@@ -53,7 +55,11 @@ __global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, i
    __syncthreads();
    int excl = x - loc + (wid > 0 ? ws[wid - 1] : 0);
    for (int k = 0; k < SCAN_PER; k++) { int idx = base + k; if (idx < n) { out[idx] = excl; } excl += v[k]; }
-   if (threadIdx.x == SCAN_T - 1) { sums[blockIdx.x] = excl; }
+   if (threadIdx.x == SCAN_T - 1)
+   {
+      sums[blockIdx.x] = excl;
+      if (last) { *last = excl; }
+   }
 }
 
 __global__ void k_scan_add(int *__restrict__ out, const int *__restrict__ sums_scanned, int n)
@@ -88,15 +94,10 @@ static void scan_rec(const int *in, int *out, int n, int *scratch, cudaStream_t 
 {
    int nb = gb_blocks(n, SCAN_TILE);
    int *sums = scratch;            // nb+1 entries (exclusive-scanned in place below)
-   k_scan_tile<<<nb, SCAN_T, 0, s>>>(in, out, sums, n);
+   // one tile: the tile kernel writes the total to out[n] itself
+   k_scan_tile<<<nb, SCAN_T, 0, s>>>(in, out, sums, n, nb == 1 ? out + n : nullptr);
    GB_COUNT(1);
-   if (nb == 1)
-   {
-      // sums[0] holds the total; out[n] = total
-      k_set_last<<<1, 1, 0, s>>>(out, n, sums);
-      GB_COUNT(1);
-      return;
-   }
+   if (nb == 1) { return; }
    int *sums_out = scratch + nb + 1;
    scan_rec(sums, sums_out, nb, sums_out + nb + 1, s);
    k_scan_add<<<nb, SCAN_T, 0, s>>>(out, sums_out, n);
@@ -293,6 +294,8 @@ extern "C" void gb_diag_inv_sqrt(int n, const int *Ai, const int *Aj, const doub
    if (n > 0) { k_diag_inv_sqrt<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, ds); GB_COUNT(1); }
 }
 
+// (one atomic per entry: grouping a warp's equal columns with
+// __match_any_sync first made the level-0 count 2x slower)
 __global__ void k_colcount(int nnz, const int *__restrict__ Sj, int *__restrict__ colcnt)
 {
    int k = blockIdx.x * blockDim.x + threadIdx.x;

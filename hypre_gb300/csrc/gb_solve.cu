@@ -51,25 +51,37 @@ template <> struct Acc<float, double>
    static __device__ __forceinline__ double mul(float a, double x) { return gb_widen_exact(a) * x; }
 };
 
-// flag = 1 when some value is not zero or a normal FP32 number exactly
-__global__ void k_exact32(long long nnz, const double *__restrict__ v, int *flag)
+static int num_sms();
+
+// flag = 1 when some value is not zero or a normal FP32 number exactly.
+// Integer tests on the bits (FP64 conversions and compares would hold the
+// scarce FP64 pipe: 0.81 ms for the 109M values of a 160^3 27-point matrix):
+// the biased exponent within FP32's normal range (897..1150) and the 29
+// mantissa bits below FP32's precision zero.  Grid-stride, at most one write
+// per block.
+__global__ void __launch_bounds__(256) k_exact32(long long nnz, const double *__restrict__ v, int *flag)
 {
-   const long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x;
    bool bad = false;
-   if (k < nnz)
+   for (long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < nnz && !bad;
+        k += (long long) gridDim.x * blockDim.x)
    {
-      const double x = v[k];
-      const float f = (float) x;
-      const unsigned e = (__float_as_uint(f) >> 23) & 0xffu;
-      bad = x != 0.0 && ((double) f != x || e == 0u || e == 0xffu);
+      const unsigned long long mag = (unsigned long long) __double_as_longlong(v[k]) & 0x7fffffffffffffffULL;
+      const unsigned e = (unsigned) (mag >> 52);
+      bad = mag != 0 && ((mag & 0x1fffffffULL) != 0 || e < 897u || e > 1150u);
    }
-   if (__any_sync(GB_FULL, bad) && (threadIdx.x & 31) == 0) { *flag = 1; }
+   if (__syncthreads_or(bad) && threadIdx.x == 0) { *flag = 1; }
 }
 
 extern "C" void gb_exact32(long long nnz, const double *v, int *flag, cudaStream_t s)
 {
    cudaMemsetAsync(flag, 0, sizeof(int), s);
-   if (nnz > 0) { k_exact32<<<nblk(nnz, 256), 256, 0, s>>>(nnz, v, flag); GB_COUNT(1); }
+   if (nnz > 0)
+   {
+      const long long want = (nnz + 255) / 256;
+      const int blocks = (int) (want < (long long) num_sms() * 8 ? want : (long long) num_sms() * 8);
+      k_exact32<<<blocks, 256, 0, s>>>(nnz, v, flag);
+      GB_COUNT(1);
+   }
 }
 
 // Epilogue of a row: mode 0  y = alpha*s + beta*b
