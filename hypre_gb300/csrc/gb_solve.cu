@@ -45,6 +45,28 @@ __device__ __forceinline__ double gb_widen_exact(float a)
    if (em == 0) { return __longlong_as_double((long long) sign); }
    return __longlong_as_double((long long) (sign | (((unsigned long long) em << 29) + (896ULL << 52))));
 }
+// FP64 -> FP32, rounded to nearest even, with integer operations when the
+// result is a normal FP32 number (biased FP64 exponent 897..1150): the FP64
+// pipe is scarce on this GPU and a conversion instruction would use it.  The
+// 29 dropped mantissa bits decide the rounding (above half: up; exactly half:
+// to the even neighbour); a carry out of the mantissa moves to the exponent
+// (to infinity past the largest FP32).  Other values take the conversion.
+__device__ __forceinline__ float gb_narrow_rn(double x)
+{
+   const unsigned long long b = (unsigned long long) __double_as_longlong(x);
+   const unsigned long long mag = b & 0x7fffffffffffffffULL;
+   const unsigned e = (unsigned) (mag >> 52);
+   if (e < 897u || e > 1150u) { return (float) x; }
+   const unsigned long long m = mag & 0xfffffffffffffULL;
+   unsigned f = ((e - 896u) << 23) | (unsigned) (m >> 29);
+   const unsigned rem = (unsigned) (m & 0x1fffffffULL);
+   f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+   return __uint_as_float(f | ((unsigned) (b >> 63) << 31));
+}
+
+template <typename VT> __device__ __forceinline__ VT gb_to_vt(double x) { return (VT) x; }
+template <> __device__ __forceinline__ float gb_to_vt<float>(double x) { return gb_narrow_rn(x); }
+
 template <> struct Acc<float, double>
 {
    typedef double T;
@@ -369,7 +391,7 @@ __global__ void k_sell_fill_v(int n, int nslices, const int *__restrict__ Ai, co
       {
          if (!lower || Aj[q] < i)
          {
-            Sv[base + (long long) k * 32] = (VT) (scaled ? Av[q] / d : Av[q]);
+            Sv[base + (long long) k * 32] = gb_to_vt<VT>(scaled ? Av[q] / d : Av[q]);
             k++;
          }
       }
@@ -381,7 +403,7 @@ template <typename VT>
 __global__ void k_convert_vals(long long nnz, const double *__restrict__ in, VT *__restrict__ out)
 {
    long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
-   if (k < nnz) { out[k] = (VT) in[k]; }
+   if (k < nnz) { out[k] = gb_to_vt<VT>(in[k]); }
 }
 
 // ---------------------------------------------------------------------------
