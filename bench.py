@@ -14,8 +14,14 @@ Arms:
   default            GPU path (FP64 setup, FP32 or FP16-finest V-cycle inside
                      FP64 FlexGMRES; `value` is the faster of the two); the
                      plain FP64 GPU path is timed alongside (`fp64_plain`)
-  --impl reference   the reference algorithm on the host cores (the CPU
-                     oracle restatement, all threads), on a bounded sample
+  --impl reference   the reference library itself (hypre's CPU path, OpenMP
+                     build, all host threads) on the same full workload; the
+                     oracle port when the reference was not built here
+
+The default run also times one reference run of the same workload
+(`cpu_baseline`) and records `parity`: the GPU FP64 hierarchy (per-level
+rows, nnz, SHA-256 of CF markers and of A's and P's patterns and values) and
+FlexGMRES residual history against the reference's.
 
 Inputs are larger than L2 (the level-0 matrix alone is 1.3 GB), so no L2
 flush is done between steps.
@@ -57,7 +63,6 @@ def parse():
     ap.add_argument("--arms", default="fp64_plain,fp32_cycle,fp16_finest",
                     help="comma-separated arms to time (profiling runs use fp32_cycle alone)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end IJ arm (profiling runs)")
-    ap.add_argument("--cpu-sample-n", type=int, default=80)
     ap.add_argument("--spmv-only", action="store_true",
                     help="only the level-0 FP64 SpMV loop of the roofline measurement (for profiling)")
     ap.add_argument("--workload", default="laplace27_160",
@@ -233,6 +238,7 @@ def gpu_arm(args):
 
     out = {}
     res = {}
+    gpu_dig = None
     arms = [a for a in (("fp64_plain", 0), ("fp32_cycle", 1), ("fp16_finest", 2)) if a[0] in args.arms.split(",")]
     if not any(a[0] == "fp32_cycle" for a in arms):
         arms.append(("fp32_cycle", 1))
@@ -252,6 +258,12 @@ def gpu_arm(args):
                           setup_seconds=float(t[5]), setup_phase_seconds=[float(v) for v in t[:5]],
                           true_relres=true_relres(), launches_per_step=launches, clocks=cs.summary(),
                           spgemm={"bytes": sgb.value, "seconds": sgs.value, "products": sgc.value})
+        if label == "fp64_plain" and rank == 0 and not args.no_cpu_baseline:
+            # the FP64 hierarchy and history of the last timed step, for the
+            # parity record against the reference's run of the same workload
+            hist = np.zeros(512); nh = C.c_int()
+            L.HYPRE_GB300_KrylovGetResidualHistory(pcg, 512, hist.ctypes.data, C.byref(nh))
+            gpu_dig = gpu_hierarchy_digests(gb, amg, hist[: nh.value])
         if label in ("fp32_cycle", "fp16_finest"):
             solvers[label] = (amg, pcg)
         else:
@@ -351,10 +363,16 @@ def gpu_arm(args):
     h2d = nnz * (4 + 8) + (n + 1) * 4 + 8 * n
     d2h = 8 * n
 
-    # ---- CPU baseline: the reference algorithm (oracle restatement) on the host cores
+    # ---- CPU baseline: the reference library itself on the same workload, all
+    # host cores; its hierarchy digests and history give the parity record
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.cpu_sample_n, n1)
+        cpu, ref = cpu_baseline(n1, digest=gpu_dig is not None)
+        if gpu_dig is not None and ref is not None:
+            what = ("the reference library (OpenMP build, %d threads), same workload" % cpu["cores"]
+                    if cpu["kind"] == "reference" else "the oracle port, same workload")
+            parity = parity_record(gpu_dig, ref, res["fp64_plain"]["iterations"], what)
 
     best = res[mixed]
     result = {
@@ -385,6 +403,7 @@ def gpu_arm(args):
                           "traffic": traffic, "algorithmic_bytes": spmv_bytes, "launch_seconds": spmv_s,
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "cpu_baseline": cpu,
+        "parity": parity,
         "clocks": best["clocks"],
     }
     if rank == 0:
@@ -393,16 +412,118 @@ def gpu_arm(args):
         torch.distributed.destroy_process_group()
 
 
-def cpu_baseline(sample_n, full_n, threads=None):
-    """Times the CPU restatement of the reference algorithm (oracle) with all
-    host threads on a smaller grid of the same workload and scales the time
-    by the unknown count (the method's cost is linear in the unknowns)."""
+def ref_binary():
+    """The reference library's OpenMP build with its timing/digest driver
+    (oracle/ref/Makefile via build()), or None when it was not built here."""
+    p = os.path.join(ROOT, "oracle", "_ref", os.uname().machine, "omp", "amg_ref_dump")
+    return p if os.access(p, os.X_OK) else None
+
+
+def run_reference(n1, repeat=1, digest=False, threads=None):
+    """Runs the reference library itself (hypre's CPU BoomerAMG + FlexGMRES(30),
+    OpenMP build, all host threads) on the full workload: the 27-point
+    Laplacian on an n1^3 grid, the right-hand side of seed 22775 normalised to
+    unit 2-norm, x0 = 0, the bench's solver settings.  `repeat` complete
+    setup+solve runs, each timed with CLOCK_MONOTONIC around
+    HYPRE_ParCSRFlexGMRESSetup and HYPRE_ParCSRFlexGMRESSolve.  Returns the
+    driver's JSON summary (times, iterations, history, per-level digests)."""
+    import tempfile
+    exe = ref_binary()
+    threads = threads or os.cpu_count()
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "ref.json")
+        cmd = [exe, "-lap27", str(n1), str(n1), str(n1), "-th", str(SOLVER["theta"]), "-mxrs", "1.0",
+               "-Pmx", str(SOLVER["pmx"]), "-agg_nl", str(SOLVER["agg_nl"]), "-agg_interp", str(SOLVER["agg_interp"]),
+               "-rlx", str(SOLVER["relax"]), "-coarse_th", "9", "-solver", "61", "-k", str(SOLVER["kdim"]),
+               "-tol", "1e-8", "-maxit", "200", "-repeat", str(repeat), "-threads", str(threads), "-json", out]
+        if digest:
+            cmd.append("-digest")
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference run failed: " + r.stderr[-500:])
+        return json.load(open(out))
+
+
+def _digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def gpu_hierarchy_digests(gb, amg_h, hist):
+    """Per-level rows, nnz and SHA-256 digests (the reference driver's byte
+    streams: int32 row pointers then column indices, float64 values, int32 CF
+    markers) of the GPU hierarchy, read back through the C ABI."""
+    amg = gb.BoomerAMG.__new__(gb.BoomerAMG)
+    amg.h = amg_h
+    nl = amg.num_levels()
+    d = dict(levels=nl, rows=[], nnz_levels=[], A_pattern=[], A_values=[], A_abs_sum=[], P_pattern=[],
+             P_values=[], P_abs_sum=[], CF=[], history=[float(v) for v in hist])
+    for l in range(nl):
+        I, J, V, _ = amg.level_csr(l, "A")
+        d["rows"].append(len(I) - 1)
+        d["nnz_levels"].append(int(I[-1]))
+        d["A_pattern"].append(_digest(I.astype("<i4"), J.astype("<i4")))
+        d["A_values"].append(_digest(V.astype("<f8")))
+        d["A_abs_sum"].append(float(np.abs(V).sum()))
+        if l < nl - 1:
+            Ip, Jp, Vp, _ = amg.level_csr(l, "P")
+            d["P_pattern"].append(_digest(Ip.astype("<i4"), Jp.astype("<i4")))
+            d["P_values"].append(_digest(Vp.astype("<f8")))
+            d["P_abs_sum"].append(float(np.abs(Vp).sum()))
+            d["CF"].append(_digest(amg.level_cf(l, len(I) - 1).astype("<i4")))
+        del I, J, V
+    return d
+
+
+def parity_record(g, r, gpu_iters, what):
+    """Compares the GPU FP64 hierarchy and residual history with the
+    reference's run of the same workload."""
+    nl = min(g["levels"], r["levels"])
+    same = lambda k: [g[k][l] == r[k][l] for l in range(min(len(g[k]), len(r[k])))]
+    hg = np.asarray(g["history"]); hr = np.asarray(r.get("history", []), dtype=float)
+    hr = hr / hr[0] if len(hr) else hr       # the reference keeps absolute norms; b-norm = r0-norm (x0 = 0)
+    m = min(len(hg), len(hr))
+    hist_rel = float(np.max(np.abs(hg[:m] - hr[:m]) / hr[:m])) if m else None
+    abs_rel = lambda k: float(max([abs(a - b) / b for a, b in zip(g[k], r[k]) if b] or [0.0]))
+    rec = {"against": what, "levels": [g["levels"], r["levels"]],
+           "rows_nnz_equal": g["rows"] == [int(v) for v in r["rows"]] and
+                             g["nnz_levels"] == [int(v) for v in r["nnz_levels"]],
+           "A_pattern_sha256_equal": all(same("A_pattern")) and g["levels"] == r["levels"],
+           "P_pattern_sha256_equal": all(same("P_pattern")) and g["levels"] == r["levels"],
+           "CF_sha256_equal": all(same("CF")) and g["levels"] == r["levels"],
+           "A_values_bit_exact": all(same("A_values")), "P_values_bit_exact": all(same("P_values")),
+           "A_abs_sum_max_rel": abs_rel("A_abs_sum"), "P_abs_sum_max_rel": abs_rel("P_abs_sum"),
+           "iterations": [gpu_iters, r["iterations"]], "history_max_rel": hist_rel, "history_tol": 1e-10,
+           "level_rows": g["rows"], "level_nnz": g["nnz_levels"], "A0_pattern_sha256": g["A_pattern"][0]}
+    rec["green"] = bool(rec["rows_nnz_equal"] and rec["A_pattern_sha256_equal"] and rec["P_pattern_sha256_equal"]
+                        and rec["CF_sha256_equal"] and rec["A_abs_sum_max_rel"] <= 1e-12
+                        and rec["P_abs_sum_max_rel"] <= 1e-12 and abs(gpu_iters - r["iterations"]) <= 1
+                        and hist_rel is not None and hist_rel <= 1e-10)
+    return rec
+
+
+def cpu_baseline(full_n, digest=False):
+    """One run of the reference library itself on the full workload (all host
+    threads); falls back to the oracle port (the CPU restatement, also on the
+    full workload) when the reference was not built on this machine."""
+    if ref_binary():
+        r = run_reference(full_n, repeat=1, digest=digest)
+        v = r["setup_seconds"][0] + r["solve_seconds"][0]
+        info = {"value": v, "unit": "s", "cores": r["threads"], "kind": "reference",
+                "sample": f"the full workload (27-point {full_n}^3, {r['nnz']} nonzeros), one setup+solve of the "
+                          f"reference library (OpenMP build, {r['threads']} threads): setup "
+                          f"{r['setup_seconds'][0]:.2f} s + solve {r['solve_seconds'][0]:.2f} s, "
+                          f"{r['iterations']} iterations"}
+        return info, r
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from hypre_gb300 import problems as G
-    threads = threads or os.cpu_count()
+    threads = os.cpu_count()
     O.set_threads(threads)
-    I, J, V = G.laplace(27, sample_n, sample_n, sample_n)
+    I, J, V = G.laplace(27, full_n, full_n, full_n)
     b = G.rhs(len(I) - 1)
     t0 = time.perf_counter()
     H = O.Hierarchy(I, J, V, O.default_params(max_row_sum=1.0, strong_threshold=SOLVER["theta"],
@@ -411,29 +532,60 @@ def cpu_baseline(sample_n, full_n, threads=None):
     t1 = time.perf_counter()
     x, rel, it = H.fgmres(b, tol=1e-8, maxit=200, kdim=SOLVER["kdim"])
     t2 = time.perf_counter()
-    scale = (full_n ** 3) / (sample_n ** 3)
-    return {"value": (t2 - t0) * scale, "unit": "s", "cores": threads, "kind": "port",
-            "sample": f"27-point {sample_n}^3 (same solver settings), setup {t1 - t0:.2f} s + solve {t2 - t1:.2f} s "
-                      f"({it} its), scaled by unknowns x{scale:.1f} to {full_n}^3"}
+    info = {"value": t2 - t0, "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"the full workload (27-point {full_n}^3), one setup+solve of the oracle port (the reference "
+                      f"was not built on this machine): setup {t1 - t0:.2f} s + solve {t2 - t1:.2f} s ({it} its)"}
+    r = None
+    if digest:
+        nl = H.num_levels
+        r = dict(n=len(I) - 1, levels=nl, iterations=it, history=[float(v) for v in rel], rows=[], nnz_levels=[],
+                 A_pattern=[], A_values=[], A_abs_sum=[], P_pattern=[], P_values=[], P_abs_sum=[], CF=[])
+        for l in range(nl):
+            Ia, Ja, Va, _ = H.csr("A", l)
+            r["rows"].append(len(Ia) - 1); r["nnz_levels"].append(int(Ia[-1]))
+            r["A_pattern"].append(_digest(Ia.astype("<i4"), Ja.astype("<i4"))); r["A_values"].append(_digest(Va))
+            r["A_abs_sum"].append(float(np.abs(Va).sum()))
+            if l < nl - 1:
+                Ip, Jp, Vp, _ = H.csr("P", l)
+                r["P_pattern"].append(_digest(Ip.astype("<i4"), Jp.astype("<i4"))); r["P_values"].append(_digest(Vp))
+                r["P_abs_sum"].append(float(np.abs(Vp).sum()))
+                r["CF"].append(_digest(H.cf(l).astype("<i4")))
+    return info, r
 
 
 def reference_arm(args):
+    """The reference library itself (hypre, OpenMP build, all host threads)
+    on the full workload: W + K complete setup+solve runs, the mean of the
+    last K reported.  Falls back to the oracle port when the reference was not
+    built on this machine (`kind` says which)."""
     rank, world = dist_info()
     if rank != 0:
         return
-    times = []
-    info = None
-    for _ in range(args.warmup):
-        cpu_baseline(args.cpu_sample_n, args.n)
-    for _ in range(args.steps):
-        info = cpu_baseline(args.cpu_sample_n, args.n)
-        times.append(info["value"])
-    v = float(np.mean(times))
-    info["value"] = v
+    if ref_binary():
+        r = run_reference(args.n, repeat=args.warmup + args.steps)
+        tot = [a + b for a, b in zip(r["setup_seconds"], r["solve_seconds"])][args.warmup:]
+        v = float(np.mean(tot))
+        info = {"value": v, "unit": "s", "cores": r["threads"], "kind": "reference",
+                "sample": f"the full workload, every step: 27-point {args.n}^3 ({r['nnz']} nonzeros), "
+                          f"setup+solve of the reference library (OpenMP build, {r['threads']} threads), "
+                          f"mean setup {np.mean(r['setup_seconds'][args.warmup:]):.2f} s + solve "
+                          f"{np.mean(r['solve_seconds'][args.warmup:]):.2f} s, {r['iterations']} iterations, "
+                          f"final rel. res {r['final_relres']:.3e}"}
+    else:
+        times = []
+        for _ in range(args.warmup):
+            cpu_baseline(args.n)
+        for _ in range(args.steps):
+            info, _ = cpu_baseline(args.n)
+            times.append(info["value"])
+        v = float(np.mean(times))
+        info["value"] = v
+    cfg = dict(WORKLOAD, **({} if args.n == 160 else {"workload": f"laplace27_{args.n}", "grid": [args.n] * 3,
+                                                       "unknowns": args.n ** 3, "nnz": None}))
     print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
                       "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
                       "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                      "data": "synthetic (seeded generator)", "config": WORKLOAD, "cpu_baseline": info,
+                      "data": "synthetic (seeded generator)", "config": cfg, "cpu_baseline": info,
                       "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 

@@ -372,7 +372,9 @@ HYPRE_Int HYPRE_ParCSRMatrixMatvec(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HY
                                    HYPRE_Complex beta, HYPRE_ParVector y)
 {
    if (!check_mat(A, 2) || !check_vec(x, 3) || !check_vec(y, 5)) { return gb_error_flag; }
-   if (x->n != A->A.nc || y->n != A->A.nr) { gb_error_in_arg(3); return gb_error_flag; }
+   /* single vectors only (multi-vectors go through the multi-RHS Krylov path) */
+   if (x->n != A->A.nc || x->num_vectors != 1) { gb_error_in_arg(3); return gb_error_flag; }
+   if (y->n != A->A.nr || y->num_vectors != 1) { gb_error_in_arg(5); return gb_error_flag; }
    gb_matvec(alpha, A, x->d, beta, y->d);
    return gb_error_flag;
 }
@@ -382,7 +384,8 @@ HYPRE_Int HYPRE_ParCSRMatrixMatvecT(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, H
                                     HYPRE_Complex beta, HYPRE_ParVector y)
 {
    if (!check_mat(A, 2) || !check_vec(x, 3) || !check_vec(y, 5)) { return gb_error_flag; }
-   if (x->n != A->A.nr || y->n != A->A.nc) { gb_error_in_arg(3); return gb_error_flag; }
+   if (x->n != A->A.nr || x->num_vectors != 1) { gb_error_in_arg(3); return gb_error_flag; }
+   if (y->n != A->A.nc || y->num_vectors != 1) { gb_error_in_arg(5); return gb_error_flag; }
    extern gb_parcsr *gb_transpose(gb_parcsr *A);
    gb_parcsr *T = gb_transpose(A);
    if (!T) { return gb_error_flag; }

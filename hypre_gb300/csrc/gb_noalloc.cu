@@ -2,12 +2,14 @@
 // the transpose of A built in a fixed, file-scope device array instead of
 // freshly allocated memory.
 //
-// Callers that cannot allocate device memory use it: code that runs while a
-// stream is being captured into a CUDA graph (an allocation there would break
-// the capture), and hosts whose device memory belongs to another allocator
-// (a framework that hands this library raw pointers and forbids it to grow
-// its own pool).  HYPRE_ParCSRMatrixMatvecT, by contrast, allocates the
-// transpose on every call.
+// Callers that cannot let the library allocate device memory use it: code
+// that enqueues work while a stream is being captured into a CUDA graph, and
+// hosts whose device memory belongs to another allocator (a framework that
+// hands this library raw pointers and forbids it to grow its own pool).
+// HYPRE_ParCSRMatrixMatvecT, by contrast, allocates the transpose from the
+// library's stream-ordered pool on every call (growing the pool) and
+// synchronises the stream before freeing it; this form only enqueues work on
+// the library's stream.
 //
 // Limit: the transpose, its row pointers and the scan workspace must fit in
 // GB_NOALLOC_SCRATCH_BYTES (32 MiB, for example about 2.6 million nonzeros
@@ -22,7 +24,9 @@
 //
 // The first call on each device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture.
+// before any stream capture.  Like every entry point of the library, it runs
+// on the library's one stream: the current device must be that stream's
+// device, else the call returns HYPRE_ERROR_GENERIC without enqueuing work.
 #include "gb_internal.h"
 
 #define GB_NOALLOC_SCRATCH_BYTES (32u << 20)
@@ -64,7 +68,8 @@ extern "C" HYPRE_Int HYPRE_GB300_ParCSRMatrixMatvecTNoAlloc(HYPRE_Complex alpha,
    if (!x || x->magic != GB_MAGIC_VEC) { gb_error_in_arg(3); return gb_error_flag; }
    if (!y || y->magic != GB_MAGIC_VEC) { gb_error_in_arg(5); return gb_error_flag; }
    const gb_csr *M = &A->A;
-   if (x->n != M->nr || y->n != M->nc) { gb_error_in_arg(3); return gb_error_flag; }
+   if (x->n != M->nr || x->num_vectors != 1) { gb_error_in_arg(3); return gb_error_flag; }
+   if (y->n != M->nc || y->num_vectors != 1) { gb_error_in_arg(5); return gb_error_flag; }
    int nc = M->nc, nr = M->nr, nnz = M->nnz;
 
    /* layout of the transpose inside the fixed array */
@@ -85,6 +90,15 @@ extern "C" HYPRE_Int HYPRE_GB300_ParCSRMatrixMatvecTNoAlloc(HYPRE_Complex alpha,
       gb_error_in_arg(2);
       return gb_error_flag;
    }
+   cudaStream_t s = gb_stream();
+   int dev = 0, sdev = 0;
+   if (!gb_cuda_ok(cudaGetDevice(&dev), "cudaGetDevice") ||
+       !gb_cuda_ok(cudaStreamGetDevice(s, &sdev), "cudaStreamGetDevice")) { return gb_error_flag; }
+   if (dev != sdev)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "MatvecTNoAlloc: the current device is not the library stream's device");
+      return gb_error_flag;
+   }
    unsigned char *base = noalloc_base();
    if (!base) { return gb_error_flag; }
    int *cnt = (int *) (base + o_cnt);
@@ -93,7 +107,6 @@ extern "C" HYPRE_Int HYPRE_GB300_ParCSRMatrixMatvecTNoAlloc(HYPRE_Complex alpha,
    int *scan = (int *) (base + o_scan);
    int *Tj = (int *) (base + o_tj);
    double *Tv = (double *) (base + o_tv);
-   cudaStream_t s = gb_stream();
 
    /* counters start at zero on every call (the array keeps the last call's data) */
    cudaMemsetAsync(cnt, 0, sizeof(int) * ((size_t) nc + 1), s);

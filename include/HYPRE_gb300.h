@@ -407,11 +407,14 @@ HYPRE_Int HYPRE_GB300_GetKernelLaunchCount(long long *count);
 HYPRE_Int HYPRE_GB300_ResetKernelLaunchCount(void);
 /* y = alpha * A^T x + beta * y without allocating device memory: the transpose
  * of A is built in a fixed device array of 32 MiB compiled into the library,
- * for callers that cannot allocate (code running under CUDA-graph stream
- * capture, or hosts whose device memory is owned by another allocator).
- * Matrices whose transpose does not fit are rejected with HYPRE_ERROR_ARG.
- * All calls share the array, so calls that overlap on the GPU race; the first
- * call on a device looks the array up and should come before any capture.
+ * for callers that cannot let the library allocate (code enqueuing work under
+ * CUDA-graph stream capture, or hosts whose device memory is owned by another
+ * allocator).  The allocating form grows the library's pool and synchronises
+ * its stream; this one only enqueues work on the library's stream, whose
+ * device must be the current one (else HYPRE_ERROR_GENERIC).  Matrices whose
+ * transpose does not fit are rejected with HYPRE_ERROR_ARG.  All calls share
+ * the array, so calls that overlap on the GPU race; the first call on a
+ * device looks the array up and should come before any capture.
  * No counterpart in the reference (its MatvecT, HYPRE_ParCSRMatrixMatvecT
  * above, is the allocating form). */
 HYPRE_Int HYPRE_GB300_ParCSRMatrixMatvecTNoAlloc(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,

@@ -1,5 +1,6 @@
 /* Build configuration for compiling the reference library's CPU path directly
- * with gcc (serial, no MPI, internal BLAS/LAPACK, 32-bit ints, double values).
+ * with gcc (one process, no MPI, internal BLAS/LAPACK, 32-bit ints, double
+ * values; the reference's OpenMP loops when GB_REF_OPENMP is defined).
  * Written for this project's oracle recipe; the reference normally generates
  * this header from its own build system. */
 #ifndef HYPRE_CONFIG_H
@@ -15,6 +16,9 @@
 #define HYPRE_USING_HYPRE_BLAS 1
 #define HYPRE_USING_HYPRE_LAPACK 1
 #define HYPRE_USING_HOST_MEMORY 1
+#ifdef GB_REF_OPENMP
+#define HYPRE_USING_OPENMP 1
+#endif
 #define HYPRE_FMANGLE 0
 #define HYPRE_FMANGLE_BLAS 0
 #define HYPRE_FMANGLE_LAPACK 0

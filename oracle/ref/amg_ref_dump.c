@@ -8,6 +8,17 @@
  *
  * Record file format (little endian): repeated
  *   char name[32]; int32 dtype (0=int32, 1=float64); int64 count; data[count]
+ *
+ * Timing and digest mode (the CPU reference timed by bench.py and the
+ * parity record at full size):
+ *   -repeat R    R complete setup+solve runs (new solver objects, x0 = 0 each
+ *                time), setup and solve timed with CLOCK_MONOTONIC
+ *   -threads T   OpenMP threads of the reference's threaded loops (OpenMP build)
+ *   -json F      write a JSON summary instead of the record file: per-run
+ *                times, iterations, residual history, per level rows and nnz
+ *   -digest      with -json: per level also SHA-256 digests of A's and P's
+ *                patterns (row pointers then column indices, int32) and values
+ *                (float64), of the CF markers, and the sums of |values|
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -21,6 +32,10 @@
 #include "_hypre_parcsr_ls.h"
 #include "_hypre_krylov.h"
 #include "HYPRE_krylov.h"
+#include "sha256.h"
+#ifdef GB_REF_OPENMP
+#include <omp.h>
+#endif
 
 static FILE *g_out = NULL;
 
@@ -111,6 +126,39 @@ static void dump_csr(const char *pfx, int lvl, hypre_CSRMatrix *M, int with_data
    }
 }
 
+static void digest_csr(hypre_CSRMatrix *M, char pat[65], char val[65], double *abs_sum)
+{
+   int nr = hypre_CSRMatrixNumRows(M);
+   int *I = hypre_CSRMatrixI(M);
+   int nnz = I[nr];
+   double *D = hypre_CSRMatrixData(M);
+   sha256_ctx s;
+   sha256_init(&s);
+   sha256_update(&s, I, sizeof(int) * (size_t)(nr + 1));
+   sha256_update(&s, hypre_CSRMatrixJ(M), sizeof(int) * (size_t) nnz);
+   sha256_hex(&s, pat);
+   sha256_init(&s);
+   sha256_update(&s, D, sizeof(double) * (size_t) nnz);
+   sha256_hex(&s, val);
+   double a = 0.0;
+   for (int k = 0; k < nnz; k++) { a += fabs(D[k]); }
+   *abs_sum = a;
+}
+
+static void json_strs(FILE *f, const char *key, char (*v)[65], int n, int last)
+{
+   fprintf(f, "\"%s\": [", key);
+   for (int i = 0; i < n; i++) { fprintf(f, "%s\"%s\"", i ? ", " : "", v[i]); }
+   fprintf(f, "]%s\n", last ? "" : ",");
+}
+
+static void json_nums(FILE *f, const char *key, const double *v, int n, int last)
+{
+   fprintf(f, "\"%s\": [", key);
+   for (int i = 0; i < n; i++) { fprintf(f, "%s%.17g", i ? ", " : "", v[i]); }
+   fprintf(f, "]%s\n", last ? "" : ",");
+}
+
 int main(int argc, char **argv)
 {
    int kind = 7, nx = 10, ny = 10, nz = 10;
@@ -120,6 +168,8 @@ int main(int argc, char **argv)
    int relax = 18, relax_coarse = 9, coarse_th = 9, maxit = 100, solver = 1, kdim = 30;
    int max_levels = 25, dump_levels = 1, seed = 22775, cheby_order = 2, relax_order = 0;
    int coarsen = 8, precond = 1, keep_t = 0, rhs_ones = 0;
+   int repeat = 1, threads = 0, want_digest = 0;
+   const char *jsonfile = NULL;
    double cheby_fraction = 0.3;
 
    for (int a = 1; a < argc; a++)
@@ -156,6 +206,10 @@ int main(int argc, char **argv)
       else if (ARG("-precond")) { precond = atoi(argv[++a]); }
       else if (ARG("-keepT")) { keep_t = atoi(argv[++a]); }
       else if (ARG("-relax_order")) { relax_order = atoi(argv[++a]); }
+      else if (ARG("-repeat")) { repeat = atoi(argv[++a]); }
+      else if (ARG("-threads")) { threads = atoi(argv[++a]); }
+      else if (ARG("-json")) { jsonfile = argv[++a]; }
+      else if (strcmp(argv[a], "-digest") == 0) { want_digest = 1; }
       else if (strcmp(argv[a], "-rhsones") == 0) { rhs_ones = 1; }
       else { fprintf(stderr, "unknown/incomplete arg %s\n", argv[a]); return 2; }
 #undef ARG
@@ -175,9 +229,19 @@ int main(int argc, char **argv)
       n = nx * ny * nz;
    }
 
+   if (repeat < 1) { repeat = 1; }
+#ifdef GB_REF_OPENMP
+   if (threads > 0) { omp_set_num_threads(threads); }
+   threads = omp_get_max_threads();
+#else
+   threads = 1;
+#endif
    HYPRE_Initialize();
-   g_out = fopen(outfile, "wb");
-   if (!g_out) { return 2; }
+   if (!jsonfile)
+   {
+      g_out = fopen(outfile, "wb");
+      if (!g_out) { return 2; }
+   }
 
    /* --- IJ assembly, one SetValues call per row (user order kept, diagonal first) --- */
    HYPRE_IJMatrix ij_A;
@@ -227,10 +291,26 @@ int main(int argc, char **argv)
    HYPRE_IJVectorAssemble(ij_x);
    HYPRE_IJVectorGetObject(ij_x, (void **) &x);
    HYPRE_ParVectorSetConstantValues(x, 0.0);
-   rec("b", 1, n, hypre_VectorData(hypre_ParVectorLocalVector((hypre_ParVector *) b)));
+   if (!jsonfile) { rec("b", 1, n, hypre_VectorData(hypre_ParVectorLocalVector((hypre_ParVector *) b))); }
 
+   double *run_setup = malloc(sizeof(double) * repeat), *run_solve = malloc(sizeof(double) * repeat);
+   HYPRE_Solver amg = NULL, ks = NULL;
+   double t0, t_setup = 0, t_solve = 0;
+   int iters = 0;
+   double final_res = 0;
+   const double *hist = NULL;
+   for (int r = 0; r < repeat; r++)
+   {
+   if (r > 0)
+   {
+      /* the previous run's solver objects; the last run's are kept for the dumps */
+      if (solver == 1) { HYPRE_ParCSRPCGDestroy(ks); }
+      else if (solver == 61) { HYPRE_ParCSRFlexGMRESDestroy(ks); }
+      HYPRE_BoomerAMGDestroy(amg);
+      ks = NULL;
+      HYPRE_ParVectorSetConstantValues(x, 0.0);
+   }
    /* --- BoomerAMG as preconditioner (one V-cycle, tol 0) --- */
-   HYPRE_Solver amg;
    HYPRE_BoomerAMGCreate(&amg);
    HYPRE_BoomerAMGSetCoarsenType(amg, coarsen);
    HYPRE_BoomerAMGSetStrongThreshold(amg, theta);
@@ -266,10 +346,6 @@ int main(int argc, char **argv)
       HYPRE_BoomerAMGSetTol(amg, tol);
    }
 
-   HYPRE_Solver ks = NULL;
-   double t0, t_setup, t_solve;
-   int iters = 0;
-   double final_res = 0;
    if (solver == 1)
    {
       HYPRE_ParCSRPCGCreate(hypre_MPI_COMM_WORLD, &ks);
@@ -290,7 +366,7 @@ int main(int argc, char **argv)
       HYPRE_PCGGetNumIterations(ks, &iters);
       HYPRE_PCGGetFinalRelativeResidualNorm(ks, &final_res);
       hypre_PCGData *pd = (hypre_PCGData *) ks;
-      if (pd->rel_norms) { rec("relres", 1, iters + 1, pd->rel_norms); }
+      hist = pd->rel_norms;
    }
    else if (solver == 61)
    {
@@ -298,7 +374,8 @@ int main(int argc, char **argv)
       HYPRE_FlexGMRESSetKDim(ks, kdim);
       HYPRE_FlexGMRESSetMaxIter(ks, maxit);
       HYPRE_FlexGMRESSetTol(ks, tol);
-      HYPRE_FlexGMRESSetPrintLevel(ks, 0);
+      /* print level 1 keeps the residual norm of every iteration (norms[]) */
+      HYPRE_FlexGMRESSetPrintLevel(ks, 1);
       HYPRE_FlexGMRESSetLogging(ks, 1);
       HYPRE_FlexGMRESSetPrecond(ks, (HYPRE_PtrToSolverFcn) HYPRE_BoomerAMGSolve,
                                 (HYPRE_PtrToSolverFcn) HYPRE_BoomerAMGSetup, amg);
@@ -311,7 +388,7 @@ int main(int argc, char **argv)
       HYPRE_FlexGMRESGetNumIterations(ks, &iters);
       HYPRE_FlexGMRESGetFinalRelativeResidualNorm(ks, &final_res);
       hypre_FlexGMRESData *gd = (hypre_FlexGMRESData *) ks;
-      if (gd->norms) { rec("resnorms", 1, iters + 1, gd->norms); }
+      hist = gd->norms;
    }
    else
    {
@@ -327,6 +404,64 @@ int main(int argc, char **argv)
       HYPRE_BoomerAMGGetNumIterations(amg, &iters);
       HYPRE_BoomerAMGGetFinalRelativeResidualNorm(amg, &final_res);
    }
+   run_setup[r] = t_setup;
+   run_solve[r] = t_solve;
+   }
+   if (jsonfile)
+   {
+      hypre_ParAMGData *ad = (hypre_ParAMGData *) amg;
+      int nl = hypre_ParAMGDataNumLevels(ad);
+      char (*apat)[65] = malloc(65 * (size_t) nl), (*aval)[65] = malloc(65 * (size_t) nl);
+      char (*ppat)[65] = malloc(65 * (size_t) nl), (*pval)[65] = malloc(65 * (size_t) nl);
+      char (*cfd)[65] = malloc(65 * (size_t) nl);
+      double *rows = malloc(sizeof(double) * nl), *nzs = malloc(sizeof(double) * nl);
+      double *aabs = malloc(sizeof(double) * nl), *pabs = malloc(sizeof(double) * nl);
+      for (int l = 0; l < nl; l++)
+      {
+         hypre_CSRMatrix *Ad = hypre_ParCSRMatrixDiag(hypre_ParAMGDataAArray(ad)[l]);
+         rows[l] = hypre_CSRMatrixNumRows(Ad);
+         nzs[l] = hypre_CSRMatrixI(Ad)[hypre_CSRMatrixNumRows(Ad)];
+         strcpy(apat[l], ""); strcpy(aval[l], ""); aabs[l] = 0.0;
+         strcpy(ppat[l], ""); strcpy(pval[l], ""); strcpy(cfd[l], ""); pabs[l] = 0.0;
+         if (!want_digest) { continue; }
+         digest_csr(Ad, apat[l], aval[l], &aabs[l]);
+         if (l < nl - 1)
+         {
+            digest_csr(hypre_ParCSRMatrixDiag(hypre_ParAMGDataPArray(ad)[l]), ppat[l], pval[l], &pabs[l]);
+            hypre_IntArray *cf = hypre_ParAMGDataCFMarkerArray(ad)[l];
+            if (cf)
+            {
+               sha256_ctx sc;
+               sha256_init(&sc);
+               sha256_update(&sc, hypre_IntArrayData(cf), sizeof(int) * (size_t) hypre_IntArraySize(cf));
+               sha256_hex(&sc, cfd[l]);
+            }
+         }
+      }
+      FILE *f = fopen(jsonfile, "w");
+      if (!f) { return 2; }
+      fprintf(f, "{\n\"n\": %d, \"nnz\": %d, \"threads\": %d, \"levels\": %d, \"iterations\": %d,\n",
+              n, nnz, threads, nl, iters);
+      fprintf(f, "\"final_relres\": %.17g,\n", final_res);
+      json_nums(f, "setup_seconds", run_setup, repeat, 0);
+      json_nums(f, "solve_seconds", run_solve, repeat, 0);
+      if (hist) { json_nums(f, "history", hist, iters + 1, 0); }
+      json_nums(f, "rows", rows, nl, 0);
+      json_nums(f, "nnz_levels", nzs, nl, 0);
+      json_nums(f, "A_abs_sum", aabs, nl, 0);
+      json_nums(f, "P_abs_sum", pabs, nl - 1 > 0 ? nl - 1 : 0, 0);
+      json_strs(f, "A_pattern", apat, nl, 0);
+      json_strs(f, "A_values", aval, nl, 0);
+      json_strs(f, "P_pattern", ppat, nl - 1 > 0 ? nl - 1 : 0, 0);
+      json_strs(f, "P_values", pval, nl - 1 > 0 ? nl - 1 : 0, 0);
+      json_strs(f, "CF", cfd, nl - 1 > 0 ? nl - 1 : 0, 1);
+      fprintf(f, "}\n");
+      fclose(f);
+      printf("levels %d iters %d final_relres %.6e setup %.4f s solve %.4f s (%d threads)\n",
+             nl, iters, final_res, t_setup, t_solve, threads);
+      return 0;
+   }
+   if (hist) { rec(solver == 1 ? "relres" : "resnorms", 1, iters + 1, hist); }
    rec("iters", 0, 1, &iters);
    rec("final_relres", 1, 1, &final_res);
    rec("t_setup", 1, 1, &t_setup);

@@ -2,7 +2,7 @@
 itself.
 
 The reference's serial CPU BoomerAMG path is compiled from its own sources by
-oracle/ref/Makefile into oracle/_ref/amg_ref_dump (a driver that builds the
+oracle/ref/Makefile into oracle/_ref/<machine>/amg_ref_dump (a driver that builds the
 7/27-point Laplacian, runs BoomerAMG-PCG or -FlexGMRES through the public API
 and dumps every level of the hierarchy).  This script runs it single-threaded
 on each case below and stores what the tests compare against:
@@ -26,7 +26,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-DUMP = os.path.join(ROOT, "oracle", "_ref", "amg_ref_dump")
+DUMP = os.path.join(ROOT, "oracle", "_ref", os.uname().machine, "amg_ref_dump")
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402  (only read_records)
