@@ -66,9 +66,10 @@ def parse():
     ap.add_argument("--spmv-only", action="store_true",
                     help="only the level-0 FP64 SpMV loop of the roofline measurement (for profiling)")
     ap.add_argument("--workload", default="laplace27_160",
-                    choices=["laplace27_160", "batch512", "multi64", "learned128", "fv256"],
+                    choices=["laplace27_160", "batch512", "multi64", "learned128", "fv256", "spgemm128"],
                     help="laplace27_160: the headline line; the others measure the batched, multi-RHS, "
-                         "learned-parameter and mixed-precision FV configurations")
+                         "learned-parameter and mixed-precision FV configurations and the reference's "
+                         "SpGEMM benchmark (A*A)")
     return ap.parse_args()
 
 
@@ -623,6 +624,65 @@ def suite_arm(args):
     L.HYPRE_Initialize()
     csr = lambda I, J, V: __import__("scipy.sparse", fromlist=["csr_matrix"]).csr_matrix(
         (V, J, I), shape=(len(I) - 1, len(I) - 1))
+    if args.workload == "spgemm128":
+        # the reference's SpGEMM benchmark (src/test/TEST_bench/benchmark_spgemm.jobs:13-16):
+        # C = A*A of the 7/27-point Laplacians on 128^3 and the 5/9-point ones on
+        # 1024^2; nonzero counts and MI250X times saved by the reference
+        # (benchmark_spgemm.saved.tioga, benchmark_spgemm.perf.saved.tioga)
+        golden = {"lap7_128": (51742208, 0.019578), "lap27_128": (254840104, 0.076419),
+                  "lap5_1024": (13611012, 0.008474), "lap9_1024": (26152996, 0.009719)}
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        sp = C.c_void_p(); L.HYPRE_GB300_GetStream(C.byref(sp))
+        lst = torch.cuda.ExternalStream(sp.value)
+        cases = []
+        for name, (nnz_ref, t_ref) in golden.items():
+            if name.startswith("lap5") or name.startswith("lap9"):
+                I, J, V = G.laplace(7 if name.startswith("lap5") else 27, 1024, 1024, 1)
+                dg = J == np.repeat(np.arange(len(I) - 1), np.diff(I))
+                V = np.where(dg, 4.0 if name.startswith("lap5") else 8.0, V)
+            else:
+                I, J, V = G.laplace(7 if name == "lap7_128" else 27, 128, 128, 128)
+            n = len(I) - 1
+            A = C.c_void_p()
+            gb.check(L.HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(n, I.ctypes.data, J.ctypes.data, V.ctypes.data,
+                                                                 C.byref(A)), "matrix")
+            for _ in range(args.warmup):
+                L.HYPRE_ParCSRMatrixDestroy(gb.matmat(A, A))
+            torch.cuda.synchronize()
+            walls, devs = [], []
+            nnz_c = None
+            for _ in range(args.steps):
+                e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+                t0 = time.perf_counter()
+                e0.record(lst)
+                Cm = gb.matmat(A, A)
+                e1.record(lst)
+                torch.cuda.synchronize()
+                walls.append(time.perf_counter() - t0)
+                devs.append(e0.elapsed_time(e1) / 1e3)
+                nr, nz = C.c_int(), C.c_int()
+                L.HYPRE_GB300_ParCSRMatrixCopyToHostCSR(Cm, C.byref(nr), C.byref(nz), None, None, None)
+                nnz_c = nz.value
+                L.HYPRE_ParCSRMatrixDestroy(Cm)
+            L.HYPRE_GB300_ParCSRMatrixDestroy(A)
+            t = float(np.median(walls))
+            byts = 2 * (12.0 * len(J) + 4.0 * (n + 1)) + 12.0 * nnz_c + 4.0 * (n + 1)
+            cases.append({"case": name, "rows": n, "nnz_A": len(J), "nnz_C": nnz_c, "nnz_reference": nnz_ref,
+                          "nnz_equal": nnz_c == nnz_ref, "seconds": t, "device_seconds": float(np.median(devs)),
+                          "mi250x_seconds": t_ref, "speedup_vs_mi250x": t_ref / t,
+                          "algorithmic_bytes": byts, "achieved_gbs": byts / t / 1e9, "frac": byts / t / 1e9 / peak})
+        top = cases[1]
+        _line("SpGEMM C = A*A seconds, 27-point 128^3 (HYPRE_ParCSRMatrixMatmat)", top["seconds"], "s", args,
+              {"workload": "spgemm_lap27_128", "operation": "C = A*A, ordered (reference column and summation order)",
+               "l2": "inputs larger than L2, no flush"}, "f64",
+              {"vs_baseline": top["seconds"] / 0.076419, "baseline": "MI250X (1 GCD) 0.076419 s, "
+               "benchmark_spgemm.perf.saved.tioga", "cases": cases,
+               "roofline": {"bound": "hbm", "achieved": top["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                            "frac": top["frac"], "traffic": None,
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}})
+        return
     if args.workload == "batch512":
         I, J, V, off, ns, eps = G.aniso2d_batch(512, seed=11)
         n = len(I) - 1

@@ -66,6 +66,7 @@ def _declare(L):
         "HYPRE_ParVectorCopy": [vp, vp], "HYPRE_ParVectorScale": [f64, vp], "HYPRE_ParVectorAxpy": [f64, vp, vp],
         "HYPRE_ParVectorSetRandomValues": [vp, i32],
         "HYPRE_ParCSRMatrixMatvec": [f64, vp, vp, f64, vp], "HYPRE_ParCSRMatrixMatvecT": [f64, vp, vp, f64, vp],
+        "HYPRE_ParCSRMatrixMatmat": [vp, vp, P(vp)], "HYPRE_ParCSRMatrixDestroy": [vp],
         "HYPRE_BoomerAMGCreate": [P(vp)], "HYPRE_BoomerAMGDestroy": [vp],
         "HYPRE_BoomerAMGSetup": [vp, vp, vp, vp], "HYPRE_BoomerAMGSolve": [vp, vp, vp, vp],
         "HYPRE_BoomerAMGGetNumIterations": [vp, P(i32)], "HYPRE_BoomerAMGGetFinalRelativeResidualNorm": [vp, P(f64)],
@@ -183,6 +184,14 @@ def parcsr_to_host(par):
     check(L.HYPRE_GB300_ParCSRMatrixCopyToHostCSR(par, None, None, I.ctypes.data, J.ctypes.data, V.ctypes.data),
           "CopyToHostCSR")
     return I, J[:nnz.value], V[:nnz.value]
+
+
+def matmat(A, B):
+    """C = A*B (HYPRE_ParCSRMatrixMatmat) of two ParCSR handles; returns C's
+    handle, which the caller destroys (HYPRE_ParCSRMatrixDestroy)."""
+    Cp = C.c_void_p()
+    check(lib().HYPRE_ParCSRMatrixMatmat(A, B, C.byref(Cp)), "Matmat")
+    return Cp
 
 
 class IJMatrix:

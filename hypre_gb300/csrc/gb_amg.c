@@ -558,6 +558,57 @@ static int spgemm_host_inner(const gb_csr *A, const gb_csr *B, int square, gb_cs
    return 0;
 }
 
+/* --------------------------------------------------------------------------
+ * C = A * B (HYPRE_ParCSRMatrixMatmat, src/parcsr_mv/HYPRE_parcsr_matrix.c:457
+ * -> hypre_ParCSRMatMatHost, src/parcsr_mv/par_csr_triplemat.c:20 ->
+ * hypre_CSRMatrixMultiplyHost, src/seq_mv/csr_matop.c:693 on one process).
+ * The reference's product: columns of each row in first-discovery order,
+ * each entry's terms summed in product order; when C is square and A has no
+ * empty rows (A's row-nonzero list is unset) every row starts with its
+ * diagonal, stored as 0 and then summed into; an empty A or B gives an empty
+ * C.  The ordered sparse-product kernels of the setup compute it.
+ * ------------------------------------------------------------------------ */
+HYPRE_Int HYPRE_ParCSRMatrixMatmat(HYPRE_ParCSRMatrix A, HYPRE_ParCSRMatrix B, HYPRE_ParCSRMatrix *C)
+{
+   if (!A || A->magic != GB_MAGIC_MAT) { gb_error_in_arg(1); return gb_error_flag; }
+   if (!B || B->magic != GB_MAGIC_MAT) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!C) { gb_error_in_arg(3); return gb_error_flag; }
+   *C = NULL;
+   if (A->A.nc != B->A.nr)
+   {
+      gb_error(HYPRE_ERROR_ARG, "Matmat: incompatible matrix dimensions");
+      gb_error_in_arg(1);
+      return gb_error_flag;
+   }
+   gb_csr P;
+   memset(&P, 0, sizeof(P));
+   if (A->A.nnz == 0 || B->A.nnz == 0)
+   {
+      P.nr = A->A.nr; P.nc = B->A.nc; P.nnz = 0;
+      P.i = (int *) gb_dcalloc(sizeof(int) * (size_t) (P.nr + 1));
+      P.j = (int *) gb_dmalloc(sizeof(int));
+      P.v = (double *) gb_dmalloc(sizeof(double));
+      if (!P.i || !P.j || !P.v) { gb_dfree(P.i); gb_dfree(P.j); gb_dfree(P.v); return gb_error_flag; }
+   }
+   else
+   {
+      int square = A->A.nr == B->A.nc;
+      if (square)
+      {
+         int *empty = (int *) gb_dcalloc(sizeof(int));
+         if (!empty) { return gb_error_flag; }
+         gb_count_empty_rows(A->A.nr, A->A.i, empty, gb_stream());
+         square = read_int(empty) == 0;
+         gb_dfree(empty);
+      }
+      if (spgemm_host_inner(&A->A, &B->A, square, &P) != 0) { return gb_error_flag; }
+   }
+   gb_parcsr *out = gb_parcsr_wrap(P, 1);
+   if (!out) { gb_dfree(P.i); gb_dfree(P.j); gb_dfree(P.v); return gb_error_flag; }
+   *C = out;
+   return gb_error_flag;
+}
+
 /* extended+i rows for fine points rows[r] (all points when rows == NULL).
  * Tier 0: one thread per row (rows with <= 64 candidates); tier 1: one warp
  * per row with shared-memory tables; tier 2: global-memory tables. */

@@ -535,6 +535,16 @@ HYPRE_Int HYPRE_GB300_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix A)
    return gb_error_flag;
 }
 
+/* src/parcsr_mv/HYPRE_parcsr_matrix.c:39 (matrices the caller owns, such as
+ * HYPRE_ParCSRMatrixMatmat's product; a matrix handed out by
+ * HYPRE_IJMatrixGetObject belongs to its IJ matrix, as in the reference) */
+HYPRE_Int HYPRE_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix matrix)
+{
+   if (!matrix || matrix->magic != GB_MAGIC_MAT) { gb_error_in_arg(1); return gb_error_flag; }
+   gb_parcsr_free(matrix);
+   return gb_error_flag;
+}
+
 /* --------------------------------------------------------------------------
  * IJ matrix: host staging rows (arena), assembled into a device ParCSR
  * ------------------------------------------------------------------------ */

@@ -906,6 +906,24 @@ __global__ void k_iota(int n, int *__restrict__ out, int *__restrict__ count)
    if (i == 0) { *count = n; }
 }
 
+/* number of empty rows (row pointer steps of zero), added into *count */
+__global__ void k_count_empty_rows(int n, const int *__restrict__ Ai, int *__restrict__ count)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   int e = (i < n) && (Ai[i + 1] == Ai[i]);
+   e = __syncthreads_count(e);
+   if (threadIdx.x == 0 && e) { atomicAdd(count, e); }
+}
+
+extern "C" void gb_count_empty_rows(int n, const int *Ai, int *count, cudaStream_t s)
+{
+   if (n > 0)
+   {
+      k_count_empty_rows<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, count);
+      GB_COUNT(1);
+   }
+}
+
 extern "C" void gb_iota(int n, int *out, int *count, cudaStream_t s)
 {
    k_iota<<<gb_blocks(n, 256), 256, 0, s>>>(n, out, count);

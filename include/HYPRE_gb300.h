@@ -157,6 +157,11 @@ HYPRE_Int HYPRE_ParCSRMatrixMatvec(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HY
                                    HYPRE_Complex beta, HYPRE_ParVector y); /* :285 */
 HYPRE_Int HYPRE_ParCSRMatrixMatvecT(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,
                                     HYPRE_Complex beta, HYPRE_ParVector y); /* :295 */
+/* C = A * B with the reference's column order and summation order (the
+ * single-process CSR product); the caller owns C */
+HYPRE_Int HYPRE_ParCSRMatrixMatmat(HYPRE_ParCSRMatrix A, HYPRE_ParCSRMatrix B,
+                                   HYPRE_ParCSRMatrix *C);                 /* :305 */
+HYPRE_Int HYPRE_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix matrix);           /* :75 */
 HYPRE_Int HYPRE_ParVectorCreate(MPI_Comm comm, HYPRE_BigInt global_size, HYPRE_BigInt *partitioning,
                                 HYPRE_ParVector *vector);                  /* :179 */
 HYPRE_Int HYPRE_ParVectorDestroy(HYPRE_ParVector vector);                 /* :188 */

@@ -679,13 +679,19 @@ int or_rap(const or_csr *P, const or_csr *A, or_csr *Ac)
 
 /* general product C = A*B with columns in discovery order (row-wise marker
  * SpGEMM, the order hypre_ParMatmul's diag part produces) */
+static int matmul_ex(const or_csr *A, const or_csr *B, or_csr *C, int square);
+
 int or_matmul(const or_csr *A, const or_csr *B, or_csr *C)
 {
    /* hypre_ParMatmul, src/parcsr_mv/par_csr_matop.c:348 (one process): row-wise
     * marker product, columns in discovery order, first contribution stored,
     * later ones added; a square product places its diagonal first (:688-697). */
+   return matmul_ex(A, B, C, A->nr == B->nc);
+}
+
+static int matmul_ex(const or_csr *A, const or_csr *B, or_csr *C, int square)
+{
    int n = A->nr, m = B->nc;
-   int square = (n == m);
    int *Ci = xcalloc(n + 1, sizeof(int));
    int *mk = xmalloc(sizeof(int) * (m ? m : 1));
    for (int k = 0; k < m; k++) { mk[k] = -1; }
@@ -1876,6 +1882,35 @@ int or_fgmres_flat(int n, const int *Ai, const int *Aj, const double *Av, or_hie
 }
 int or_vcycle_flat(or_hierarchy *H, const double *f, double *u) { return or_amg_vcycle(H, f, u); }
 void or_free_ptr(void *p) { free(p); }
+
+/* C = A*B as HYPRE_ParCSRMatrixMatmat computes it on one process
+ * (src/parcsr_mv/HYPRE_parcsr_matrix.c:457 -> par_csr_triplemat.c:20 ->
+ * hypre_CSRMatrixMultiplyHost, src/seq_mv/csr_matop.c:693-933): an empty A or
+ * B gives an empty C (:745-752); a square product reserves each row's
+ * diagonal first (stored as 0, then summed into, :900-909) unless A has a
+ * row-nonzero list, which IJ assembly sets when some but not all rows of A
+ * are empty (src/IJ_mv/IJMatrix_parcsr.c:3053, src/seq_mv/csr_matrix.c:354-400);
+ * then each non-empty row takes columns in first-discovery order only.
+ * Returns nnz(C); *Ci (nra+1), *Cj, *Cv are malloc'd (or_free_ptr). */
+int or_matmat_flat(int nra, int nca, int ncb, const int *Ai, const int *Aj, const double *Av,
+                   const int *Bi, const int *Bj, const double *Bv, int **Ci, int **Cj, double **Cv)
+{
+   or_csr A = { nra, nca, (int *) Ai, (int *) Aj, (double *) Av };
+   or_csr B = { nca, ncb, (int *) Bi, (int *) Bj, (double *) Bv };
+   or_csr C;
+   int empty_rows = 0;
+   for (int i = 0; i < nra; i++) { empty_rows += Ai[i + 1] == Ai[i]; }
+   if (Ai[nra] == 0 || Bi[nca] == 0)
+   {
+      *Ci = xcalloc(nra + 1, sizeof(int));
+      *Cj = xmalloc(sizeof(int));
+      *Cv = xmalloc(sizeof(double));
+      return 0;
+   }
+   matmul_ex(&A, &B, &C, nra == ncb && empty_rows == 0);
+   *Ci = C.i; *Cj = C.j; *Cv = C.v;
+   return C.i[nra];
+}
 int or_gen_stencil_flat(int kind, int nx, int ny, int nz, int **i, int **j, double **v)
 {
    or_csr A;

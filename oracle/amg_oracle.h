@@ -92,6 +92,8 @@ int    or_transpose(const or_csr *A, or_csr *AT);
 int    or_rap(const or_csr *P, const or_csr *A, or_csr *Ac);
 int    or_l1_norms(const or_csr *A, int option, double *l1);
 int    or_matmul(const or_csr *A, const or_csr *B, or_csr *C);
+int    or_matmat_flat(int nra, int nca, int ncb, const int *Ai, const int *Aj, const double *Av,
+                      const int *Bi, const int *Bj, const double *Bv, int **Ci, int **Cj, double **Cv);
 int    or_strength2(const or_csr *S, int *CF, int num_paths, or_csr *S2);
 void   or_correct_cf2(int n, int *CF, const int *CFN);
 int    or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P);

@@ -70,6 +70,8 @@ def lib():
         L.or_gen_stencil_flat.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int,
                                           P(P(C.c_int)), P(P(C.c_int)), P(P(C.c_double))]
         L.or_free_ptr.argtypes = [C.c_void_p]
+        L.or_matmat_flat.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 6 + \
+            [P(P(C.c_int)), P(P(C.c_int)), P(P(C.c_double))]
         _lib = L
     return _lib
 
@@ -109,6 +111,25 @@ def stencil(kind, nx, ny, nz):
     I = np.ctypeslib.as_array(pi, (n + 1,)).copy()
     J = np.ctypeslib.as_array(pj, (nnz,)).copy()
     V = np.ctypeslib.as_array(pv, (nnz,)).copy()
+    for p in (pi, pj, pv):
+        L.or_free_ptr(C.cast(p, C.c_void_p))
+    return I, J, V
+
+
+def matmat(A, B, nca, ncb):
+    """C = A*B as the reference's HYPRE_ParCSRMatrixMatmat computes it on one
+    process (column order, summation order, diagonal rule); A and B are
+    (I, J, V) CSR triples with nca and ncb columns."""
+    L = lib()
+    (Ai, Aj, Av), (Bi, Bj, Bv) = [(np.ascontiguousarray(I, np.int32), np.ascontiguousarray(J, np.int32),
+                                   np.ascontiguousarray(V, np.float64)) for I, J, V in (A, B)]
+    nra = len(Ai) - 1
+    pi, pj, pv = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
+    nnz = L.or_matmat_flat(nra, nca, ncb, Ai.ctypes.data, Aj.ctypes.data, Av.ctypes.data, Bi.ctypes.data,
+                           Bj.ctypes.data, Bv.ctypes.data, C.byref(pi), C.byref(pj), C.byref(pv))
+    I = np.ctypeslib.as_array(pi, (nra + 1,)).copy()
+    J = np.ctypeslib.as_array(pj, (max(nnz, 1),))[:nnz].copy()
+    V = np.ctypeslib.as_array(pv, (max(nnz, 1),))[:nnz].copy()
     for p in (pi, pj, pv):
         L.or_free_ptr(C.cast(p, C.c_void_p))
     return I, J, V

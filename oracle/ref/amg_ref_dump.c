@@ -16,6 +16,8 @@
  *   -threads T   OpenMP threads of the reference's threaded loops (OpenMP build)
  *   -json F      write a JSON summary instead of the record file: per-run
  *                times, iterations, residual history, per level rows and nnz
+ *   -matmat      instead of a solve, record C = A*A from HYPRE_ParCSRMatrixMatmat
+ *                (C_i, C_j, C_v) and the product's wall time (t_matmat)
  *   -digest      with -json: per level also SHA-256 digests of A's and P's
  *                patterns (row pointers then column indices, int32) and values
  *                (float64), of the CF markers, and the sums of |values|
@@ -168,7 +170,7 @@ int main(int argc, char **argv)
    int relax = 18, relax_coarse = 9, coarse_th = 9, maxit = 100, solver = 1, kdim = 30;
    int max_levels = 25, dump_levels = 1, seed = 22775, cheby_order = 2, relax_order = 0;
    int coarsen = 8, precond = 1, keep_t = 0, rhs_ones = 0;
-   int repeat = 1, threads = 0, want_digest = 0;
+   int repeat = 1, threads = 0, want_digest = 0, matmat = 0;
    const char *jsonfile = NULL;
    double cheby_fraction = 0.3;
 
@@ -210,6 +212,7 @@ int main(int argc, char **argv)
       else if (ARG("-threads")) { threads = atoi(argv[++a]); }
       else if (ARG("-json")) { jsonfile = argv[++a]; }
       else if (strcmp(argv[a], "-digest") == 0) { want_digest = 1; }
+      else if (strcmp(argv[a], "-matmat") == 0) { matmat = 1; }
       else if (strcmp(argv[a], "-rhsones") == 0) { rhs_ones = 1; }
       else { fprintf(stderr, "unknown/incomplete arg %s\n", argv[a]); return 2; }
 #undef ARG
@@ -260,6 +263,21 @@ int main(int argc, char **argv)
    HYPRE_IJMatrixAssemble(ij_A);
    HYPRE_ParCSRMatrix A;
    HYPRE_IJMatrixGetObject(ij_A, (void **) &A);
+
+   if (matmat)
+   {
+      HYPRE_ParCSRMatrix Cm = NULL;
+      double tm = now_s();
+      HYPRE_ParCSRMatrixMatmat(A, A, &Cm);
+      tm = now_s() - tm;
+      dump_csr("A", 0, hypre_ParCSRMatrixDiag((hypre_ParCSRMatrix *) A), 1);
+      dump_csr("C", 0, hypre_ParCSRMatrixDiag((hypre_ParCSRMatrix *) Cm), 1);
+      rec("t_matmat", 1, 1, &tm);
+      fclose(g_out);
+      printf("A*A: %d rows, nnz %d, %.4f s\n", n,
+             hypre_CSRMatrixNumNonzeros(hypre_ParCSRMatrixDiag((hypre_ParCSRMatrix *) Cm)), tm);
+      return 0;
+   }
 
    /* --- vectors: b = random[-1,1] (seeded), normalised to unit 2-norm; x0 = 0 --- */
    HYPRE_IJVector ij_b, ij_x;

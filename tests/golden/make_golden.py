@@ -10,7 +10,9 @@ on each case below and stores what the tests compare against:
 * small cases: every array of the hierarchy (A, P, S, CF, l1 norms,
   Chebyshev data), the residual history, the solution;
 * large cases: SHA-256 digests of the integer arrays, checksums and a seeded
-  sample of the floating-point arrays, the full residual history.
+  sample of the floating-point arrays, the full residual history;
+* sparse products (mm_*): C = A*A from the reference's
+  HYPRE_ParCSRMatrixMatmat, with the IJ-assembled A it was given.
 
 Usage (needs the reference sources, so it runs only where they are present):
     make -C oracle/ref REF=<reference>/src
@@ -103,11 +105,84 @@ def make(name, c):
                                                   os.path.getsize(path) / 1024))
 
 
+# Sparse products C = A*A through HYPRE_ParCSRMatrixMatmat (full arrays of the
+# IJ-assembled A and of C).  "gen" cases write A to a binary CSR file first.
+MATMAT = {
+    "mm_lap7_10": dict(kind=7, n=(10, 10, 10)),
+    "mm_lap27_9x8x7": dict(kind=27, n=(9, 8, 7)),
+    "mm_lap9pt2d_16": dict(gen="9pt2d", n=16),
+    "mm_empty_rows": dict(gen="empty_rows", n=6),
+    "mm_random_300": dict(gen="random", n=300),
+}
+
+
+def _gen_matrix(c):
+    """Host CSR (I, J, V) of a generated matrix (rows as given; IJ assembly
+    moves each row's diagonal first)."""
+    from hypre_gb300 import problems as P
+    if c["gen"] == "9pt2d":
+        I, J, V = P.laplace(27, c["n"], c["n"], 1)
+        V = np.where(J == np.repeat(np.arange(len(I) - 1), np.diff(I)), 8.0, V)
+        return I, J, V
+    if c["gen"] == "empty_rows":
+        I, J, V = P.laplace(7, c["n"], c["n"], c["n"])
+        n = len(I) - 1
+        keep = np.ones(n, bool)
+        keep[[0, 7, 50, 51, 100, n - 1]] = False
+        rows = np.repeat(np.arange(n), np.diff(I))
+        m = keep[rows]
+        cnt = np.where(keep, np.diff(I), 0)
+        I2 = np.zeros(n + 1, np.int32)
+        np.cumsum(cnt, out=I2[1:])
+        return I2, J[m].astype(np.int32), V[m]
+    rng = np.random.default_rng(5)
+    n = c["n"]
+    rows = []
+    for i in range(n):
+        k = int(rng.integers(0, 9))
+        cols = rng.choice(n, k, replace=False)
+        if rng.random() < 0.8 and i not in cols:
+            cols = np.append(cols, i)
+        rows.append(cols)
+    I = np.zeros(n + 1, np.int32)
+    np.cumsum([len(r) for r in rows], out=I[1:])
+    J = np.concatenate(rows).astype(np.int32)
+    V = rng.standard_normal(len(J))
+    return I, J, V
+
+
+def make_matmat(name, c):
+    tmp = os.path.join("/tmp", "golden_%s.bin" % name)
+    args = [DUMP, "-matmat", "-o", tmp]
+    if "gen" in c:
+        I, J, V = _gen_matrix(c)
+        mat = os.path.join("/tmp", "golden_%s.csr" % name)
+        with open(mat, "wb") as f:
+            np.array([len(I) - 1, len(J)], np.int32).tofile(f)
+            I.astype(np.int32).tofile(f); J.astype(np.int32).tofile(f); V.astype(np.float64).tofile(f)
+        args += ["-mat", mat]
+    else:
+        args += ["-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
+    r = subprocess.run(args, capture_output=True, text=True, env=dict(os.environ, OMP_NUM_THREADS="1"),
+                       check=True)
+    rec = O.read_records(tmp)
+    os.unlink(tmp)
+    out = {"case": np.array(json.dumps(c)), "dump_stdout": np.array(r.stdout)}
+    for key in ("A0_i", "A0_j", "A0_v", "C0_i", "C0_j", "C0_v"):
+        out[key] = rec[key]
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print("%-28s A nnz %d, C nnz %d  %6.1f KB" % (name, len(rec["A0_j"]), len(rec["C0_j"]),
+                                                  os.path.getsize(path) / 1024))
+
+
 def main():
     if not os.path.exists(DUMP):
         sys.exit("build the reference dumper first: make -C oracle/ref REF=<reference>/src")
     for name, c in CASES.items():
         make(name, c)
+    for name, c in MATMAT.items():
+        make_matmat(name, c)
 
 
 if __name__ == "__main__":
