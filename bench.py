@@ -272,6 +272,25 @@ def gpu_arm(args):
             m_o = step_mats.pop(pcg.value, None)
             if m_o is not None:
                 L.HYPRE_GB300_ParCSRMatrixDestroy(m_o)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    # ---- solve-phase SpMV of the mixed-precision cycle: level 0's FP32 form
+    # (and the FP16-valued form of the FP16-finest cycle), CUDA events on the
+    # library stream around back-to-back launches
+    cyc = {}
+    for label, prec in (("fp32", 1), ("fp16", 2)):
+        src = solvers.get("fp32_cycle" if prec == 1 else "fp16_finest")
+        if src is None:
+            continue
+        sec, byt = C.c_double(), C.c_double()
+        gb.check(L.HYPRE_GB300_BoomerAMGLevelSpMVTime(src[0], 0, prec, 20, C.byref(sec), C.byref(byt)), "spmv time")
+        cyc[label] = {"bound": "hbm", "kernel": "SpMV level 0, SELL-32, %s values, FP32 vectors, 16-bit offset "
+                      "column indices" % ("FP32" if prec == 1 else "FP16 (row-scaled)"),
+                      "achieved": byt.value / sec.value / 1e9, "peak": peak, "unit": "GB/s",
+                      "frac": byt.value / sec.value / 1e9 / peak, "traffic": None,
+                      "algorithmic_bytes": byt.value, "launch_seconds": sec.value,
+                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
     # the reported mixed-precision path: the faster of the FP32 cycle and the
     # FP16-finest cycle, provided it reached the tolerance in FP64; the
     # end-to-end step below runs the same solver
@@ -314,9 +333,6 @@ def gpu_arm(args):
     val_bytes = 4 if exact32 else 8
     nsl = (n + 31) // 32
     spmv_bytes = nnz * (val_bytes + idx_bytes) + 8 * n + 8 * n + 12 * nsl
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
-    peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = spmv_bytes / spmv_s / 1e9
     traffic = None
     tf = os.path.join(ROOT, "profiles", "spmv_traffic.json")
@@ -403,6 +419,8 @@ def gpu_arm(args):
                           "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                           "traffic": traffic, "algorithmic_bytes": spmv_bytes, "launch_seconds": spmv_s,
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "roofline_spmv_fp32": cyc.get("fp32"),
+        "roofline_spmv_fp16": cyc.get("fp16"),
         "cpu_baseline": cpu,
         "parity": parity,
         "clocks": best["clocks"],

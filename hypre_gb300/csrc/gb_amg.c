@@ -1967,6 +1967,54 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelCF(HYPRE_Solver solver, HYPRE_Int level, 
    return gb_error_flag;
 }
 
+/* Times the solve-phase SpMV y = A_l x of one level in one value precision
+ * (0 FP64, 1 FP32, 2 FP16 values with FP32 vectors): `reps` launches of the
+ * level's solve form back to back on the library stream between two CUDA
+ * events.  Returns the mean seconds per launch and the algorithmic bytes of
+ * one launch: nnz * (value bytes + index bytes), x read once, y written
+ * once, and the row pointers (CSR) or slice offsets and widths (SELL-32). */
+HYPRE_Int HYPRE_GB300_BoomerAMGLevelSpMVTime(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int prec, HYPRE_Int reps,
+                                             HYPRE_Real *seconds, HYPRE_Real *bytes)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (level < 0 || level >= a->num_levels) { gb_error_in_arg(2); return gb_error_flag; }
+   if (prec < GB_PREC_F64 || prec > GB_PREC_F16) { gb_error_in_arg(3); return gb_error_flag; }
+   if (reps < 1) { gb_error_in_arg(4); return gb_error_flag; }
+   gb_level *L = &a->lev[level];
+   const gb_spmv_desc *d = gb_solve_desc(L->A, prec);
+   if (!d) { return gb_error_flag; }
+   const int n = L->A->A.nr;
+   const size_t xb = prec == GB_PREC_F64 ? 8 : 4;
+   void *x = gb_dcalloc(xb * (size_t) (n > 0 ? n : 1)), *y = gb_dmalloc(xb * (size_t) (n > 0 ? n : 1));
+   if (!x || !y) { gb_dfree(x); gb_dfree(y); return gb_error_flag; }
+   cudaStream_t s = gb_stream();
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0);
+   cudaEventCreate(&e1);
+   for (int r = -1; r < reps; r++)
+   {
+      if (r == 0) { cudaEventRecord(e0, s); }
+      if (prec == GB_PREC_F64) { gb_spmv_d(d, (const double *) x, (double *) y, 0, 1.0, 0.0, NULL, NULL, 0.0, NULL, NULL, s); }
+      else { gb_spmv_f(d, (const float *) x, (float *) y, 0, 1.0f, 0.0f, NULL, NULL, 0.0f, NULL, NULL, s); }
+   }
+   cudaEventRecord(e1, s);
+   gb_sync();
+   float ms = 0.f;
+   cudaEventElapsedTime(&ms, e0, e1);
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   gb_dfree(x);
+   gb_dfree(y);
+   const double nnz = (double) L->A->A.nnz;
+   double vb = prec == GB_PREC_F64 ? (d->fmt == GB_FMT_SELL && d->sl_v32 ? 4.0 : 8.0) : prec == GB_PREC_F32 ? 4.0 : 2.0;
+   double ib = d->fmt == GB_FMT_SELL && d->sl_j16 ? 2.0 : 4.0;
+   double meta = d->fmt == GB_FMT_SELL ? 12.0 * (double) d->nslices : 4.0 * ((double) n + 1.0);
+   if (seconds) { *seconds = ms * 1e-3 / reps; }
+   if (bytes) { *bytes = nnz * (vb + ib) + 2.0 * (double) xb * n + meta + (d->rs ? 4.0 * n : 0.0); }
+   return gb_error_flag;
+}
+
 HYPRE_Int HYPRE_GB300_BoomerAMGGetSpGEMMStats(HYPRE_Solver solver, HYPRE_Real *bytes, HYPRE_Real *seconds,
                                               HYPRE_Int *calls)
 {

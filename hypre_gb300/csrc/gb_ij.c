@@ -524,7 +524,7 @@ HYPRE_Int HYPRE_GB300_ParCSRMatrixCreateFromDeviceCSR(HYPRE_Int n, const HYPRE_I
    A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
    if (!A.i || !A.j || !A.v) { gb_dfree(A.i); gb_dfree(A.j); gb_dfree(A.v); *Aout = NULL; return gb_error_flag; }
    cudaMemcpyAsync(A.i, rowptr, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToDevice, s);
-   gb_ij_gather(n, nnz, NULL, A.i, colidx, values, 0, A.j, A.v, s);
+   gb_ij_gather(n, nnz, NULL, A.i, colidx, values, 0, NULL, A.j, A.v, s);
    *Aout = gb_parcsr_wrap(A, 1);
    return gb_error_flag;
 }
@@ -1038,6 +1038,40 @@ HYPRE_Int HYPRE_IJMatrixAddToValues(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_Int
    return ijm_put_ones(m, nrows, ncols, rows, cols, values, 1);
 }
 
+/* The column each row's assembly moves to the front.  The reference's
+ * assembly of rows put with SetRowSizes (the auxiliary-row path,
+ * src/IJ_mv/IJMatrix_parcsr.c:2800-2930) walks the rows that have space --
+ * a size above zero from SetRowSizes, or entries put into the row
+ * (src/IJ_mv/aux_parcsr_matrix.c:164-215) -- and moves to the front the entry
+ * whose column equals the row's ordinal among those rows (it compares the
+ * column with the walk's index, :2843).  Every row has space unless
+ * SetRowSizes gave some row zero, so the ordinal is the row itself and the
+ * diagonal moves to the front.  Returns a device array of the ordinals when
+ * some differ from the row (NULL otherwise, and always after
+ * SetDiagOffdSizes, whose assembly swaps the true diagonal, :2974-2995).
+ * I: host row pointers of the assembled rows. */
+static int *ijm_front_keys(HYPRE_IJMatrix m, const int *I)
+{
+   if (m->swap_diag || !m->hint) { return NULL; }
+   int n = m->nrows, ord = 0, differs = 0;
+   int *key = (int *) malloc(sizeof(int) * (size_t) (n ? n : 1));
+   if (!key) { gb_error(HYPRE_ERROR_MEMORY, "IJ assembly"); return NULL; }
+   for (int r = 0; r < n; r++)
+   {
+      key[r] = ord;
+      differs |= ord != r;
+      if (m->hint[r] > 0 || I[r + 1] > I[r]) { ord++; }
+   }
+   int *d = NULL;
+   if (differs)
+   {
+      d = (int *) gb_dmalloc(sizeof(int) * (size_t) n);
+      if (d) { cudaMemcpyAsync(d, key, sizeof(int) * (size_t) n, cudaMemcpyHostToDevice, gb_stream()); gb_sync(); }
+   }
+   free(key);
+   return d;
+}
+
 HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
 {
    if (!check_ijm(m, 1)) { return gb_error_flag; }
@@ -1056,7 +1090,24 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
       A.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
       if (!A.i || !A.j || !A.v) { gb_dfree(A.i); gb_dfree(A.j); gb_dfree(A.v); return gb_error_flag; }
       cudaMemcpyAsync(A.i, m->st_rowptr, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToDevice, s);
-      gb_ij_gather(n, nnz, NULL, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
+      int *key = NULL;
+      if (m->hint && !m->swap_diag)
+      {
+         int z = 0;
+         for (int r = 0; r < n && !z; r++) { z = m->hint[r] <= 0; }
+         if (z)
+         {
+            /* some row was given no space: the front rule needs the row lengths */
+            int *hI = (int *) malloc(sizeof(int) * (size_t) (n + 1));
+            if (!hI) { gb_error(HYPRE_ERROR_MEMORY, "IJ assembly"); return gb_error_flag; }
+            cudaMemcpyAsync(hI, m->st_rowptr, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToHost, s);
+            gb_sync();
+            key = ijm_front_keys(m, hI);
+            free(hI);
+         }
+      }
+      gb_ij_gather(n, nnz, NULL, A.i, m->st_cols, m->st_vals, m->swap_diag, key, A.j, A.v, s);
+      gb_dfree(key);
       if (m->par) { gb_parcsr_free(m->par); }
       m->par = gb_parcsr_wrap(A, 1);
       m->assembled = 1;
@@ -1116,9 +1167,11 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
    }
    cudaMemcpyAsync(A.i, I, sizeof(int) * (size_t) (n + 1), cudaMemcpyHostToDevice, s);
    cudaMemcpyAsync(doff, off, sizeof(long long) * (size_t) (n ? n : 1), cudaMemcpyHostToDevice, s);
-   gb_ij_gather(n, A.nnz, doff, A.i, m->st_cols, m->st_vals, m->swap_diag, A.j, A.v, s);
+   int *key = ijm_front_keys(m, I);
+   gb_ij_gather(n, A.nnz, doff, A.i, m->st_cols, m->st_vals, m->swap_diag, key, A.j, A.v, s);
    gb_sync();   /* the host buffers above are read by the copies */
    gb_dfree(doff);
+   gb_dfree(key);
    free(I); free(off); free(hc); free(hv);
    if (m->par) { gb_parcsr_free(m->par); }
    m->par = gb_parcsr_wrap(A, 1);

@@ -64,11 +64,13 @@ extern "C" void gb_ij_check(int nrows, const int *start, const int *cols, int nc
 
 // LPR lanes per row r (LPR divides 32): staged entries off[r] .. off[r]+len
 // (len = I[r+1]-I[r]; off NULL: the staging is in row order, off[r] = I[r])
-// -> J, V at I[r], diagonal first (shift, or swap when swap_diag)
+// -> J, V at I[r], diagonal first (shift, or swap when swap_diag).  key
+// (optional): the column moved to the front of row r is key[r] instead of r
+// (the reference's rule when some rows have no space, see gb_ij.c)
 template <int LPR>
 __global__ void k_ij_gather(int n, const long long *__restrict__ off, const int *__restrict__ I,
                             const int *__restrict__ scols, const double *__restrict__ svals, int swap_diag,
-                            int *__restrict__ J, double *__restrict__ V)
+                            const int *__restrict__ key, int *__restrict__ J, double *__restrict__ V)
 {
    const long long g = blockIdx.x * (long long) blockDim.x + threadIdx.x;
    const int r = (int) (g / LPR);
@@ -78,12 +80,13 @@ __global__ void k_ij_gather(int n, const long long *__restrict__ off, const int 
    const unsigned seg = LPR == 32 ? GB_FULL : (((1u << LPR) - 1u) << sbase);
    const int d = I[r], l = I[r + 1] - d;
    const long long o = off ? off[r] : (long long) d;
+   const int front = key ? key[r] : r;
    // first position of the diagonal
    int dpos = -1;
    for (int c = 0; c < l && dpos < 0; c += LPR)
    {
       const int q = c + lane;
-      const unsigned m = __ballot_sync(seg, q < l && scols[o + q] == r) >> sbase;
+      const unsigned m = __ballot_sync(seg, q < l && scols[o + q] == front) >> sbase;
       if (m) { dpos = c + __ffs(m) - 1; }
    }
    for (int q = lane; q < l; q += LPR)
@@ -100,12 +103,13 @@ __global__ void k_ij_gather(int n, const long long *__restrict__ off, const int 
 }
 
 extern "C" void gb_ij_gather(int n, long long nnz, const long long *off, const int *I, const int *scols,
-                             const double *svals, int swap_diag, int *J, double *V, cudaStream_t s)
+                             const double *svals, int swap_diag, const int *key, int *J, double *V, cudaStream_t s)
 {
    if (n <= 0) { return; }
    const long long avg = nnz / n;
 #define GB_IJG(L)                                                                                                  \
-   k_ij_gather<L><<<(int) (((long long) n * L + 255) / 256), 256, 0, s>>>(n, off, I, scols, svals, swap_diag, J, V)
+   k_ij_gather<L><<<(int) (((long long) n * L + 255) / 256), 256, 0, s>>>(n, off, I, scols, svals, swap_diag, key, \
+                                                                          J, V)
    if (avg <= 6) { GB_IJG(4); }
    else if (avg <= 12) { GB_IJG(8); }
    else if (avg <= 40) { GB_IJG(16); }

@@ -113,7 +113,7 @@ void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj, const dou
 /* IJ matrix device assembly (gb_ijdev.cu) */
 void gb_ij_check(int nrows, const int *start, const int *cols, int ncol, int *flags, cudaStream_t s);
 void gb_ij_gather(int n, long long nnz, const long long *off, const int *I, const int *scols, const double *svals,
-                  int swap_diag, int *J, double *V, cudaStream_t s);
+                  int swap_diag, const int *key, int *J, double *V, cudaStream_t s);
 void gb_rowlen_max(int n, const int *Bi, int *out, cudaStream_t s);
 /* aggressive coarsening (gb_agg.cu) */
 void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s);

@@ -375,6 +375,11 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelL1(HYPRE_Solver solver, HYPRE_Int level, 
  * (CUDA events on the library stream around each product) and their count. */
 HYPRE_Int HYPRE_GB300_BoomerAMGGetSpGEMMStats(HYPRE_Solver solver, HYPRE_Real *bytes, HYPRE_Real *seconds,
                                               HYPRE_Int *calls);
+/* Mean device seconds of the solve-phase SpMV y = A_l x of one level in one
+ * value precision (0 FP64, 1 FP32, 2 FP16 values with FP32 vectors) over
+ * `reps` back-to-back launches, and its algorithmic bytes per launch. */
+HYPRE_Int HYPRE_GB300_BoomerAMGLevelSpMVTime(HYPRE_Solver solver, HYPRE_Int level, HYPRE_Int prec, HYPRE_Int reps,
+                                             HYPRE_Real *seconds, HYPRE_Real *bytes);
 /* Chebyshev smoother data of a level (relax type 16): the ChebyOrder
  * coefficients of s(t) in u <- u + s(A) r, eig[0..1] = max/min eigenvalue
  * estimates, ds = D^{-1/2} (n values); any pointer may be NULL. */

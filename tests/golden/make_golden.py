@@ -12,7 +12,8 @@ on each case below and stores what the tests compare against:
 * large cases: SHA-256 digests of the integer arrays, checksums and a seeded
   sample of the floating-point arrays, the full residual history;
 * sparse products (mm_*): C = A*A from the reference's
-  HYPRE_ParCSRMatrixMatmat, with the IJ-assembled A it was given.
+  HYPRE_ParCSRMatrixMatmat, with the IJ-assembled A it was given and, for
+  generated matrices, the rows as they were put (in_i, in_j, in_v).
 
 Usage (needs the reference sources, so it runs only where they are present):
     make -C oracle/ref REF=<reference>/src
@@ -154,8 +155,10 @@ def _gen_matrix(c):
 def make_matmat(name, c):
     tmp = os.path.join("/tmp", "golden_%s.bin" % name)
     args = [DUMP, "-matmat", "-o", tmp]
+    inp = {}
     if "gen" in c:
         I, J, V = _gen_matrix(c)
+        inp = {"in_i": I.astype(np.int32), "in_j": J.astype(np.int32), "in_v": V.astype(np.float64)}
         mat = os.path.join("/tmp", "golden_%s.csr" % name)
         with open(mat, "wb") as f:
             np.array([len(I) - 1, len(J)], np.int32).tofile(f)
@@ -170,6 +173,7 @@ def make_matmat(name, c):
     out = {"case": np.array(json.dumps(c)), "dump_stdout": np.array(r.stdout)}
     for key in ("A0_i", "A0_j", "A0_v", "C0_i", "C0_j", "C0_v"):
         out[key] = rec[key]
+    out.update(inp)      # the rows as put (one SetValues per row after SetRowSizes)
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **out)
     print("%-28s A nnz %d, C nnz %d  %6.1f KB" % (name, len(rec["A0_j"]), len(rec["C0_j"]),

@@ -29,7 +29,12 @@ def random_rows(n, seed, maxlen=80, dup_rows=()):
     return rows
 
 
-def expected_csr(rows, swap=False, adds=()):
+def expected_csr(rows, swap=False, adds=(), sizes=None):
+    """The reference's assembly of the puts.  With SetRowSizes (not swap) the
+    entry moved to the front of row r is the one whose column is r's ordinal
+    among the rows that have space (a size above zero or entries): r itself
+    unless some earlier row was given size 0 and no entries
+    (IJMatrix_parcsr.c:2830-2906, aux_parcsr_matrix.c:164-215)."""
     out = []
     for r, (cols, vals) in enumerate(rows):
         ec, ev = [], []
@@ -49,10 +54,14 @@ def expected_csr(rows, swap=False, adds=()):
                 ec.append(c)
                 ev.append(v)
     I, J, V = [0], [], []
+    ordinal = 0
     for r, (ec, ev) in enumerate(out):
         ec, ev = list(ec), list(ev)
-        if r in ec:
-            d = ec.index(r)
+        front = r if (swap or sizes is None) else ordinal
+        if sizes is not None and (sizes[r] > 0 or len(ec) > 0):
+            ordinal += 1
+        if front in ec:
+            d = ec.index(front)
             if d > 0:
                 if swap:
                     ec[0], ec[d] = ec[d], ec[0]
@@ -66,13 +75,14 @@ def expected_csr(rows, swap=False, adds=()):
     return np.array(I, np.int32), np.array(J, np.int32), np.array(V, np.float64)
 
 
-def assemble(gb, rows, bulk, swap=False, adds=(), extra=None, strict=True):
+def assemble(gb, rows, bulk, swap=False, adds=(), extra=None, strict=True, sizes=None):
     L = gb.lib()
     n = len(rows)
     h = C.c_void_p()
     gb.check(L.HYPRE_IJMatrixCreate(0, 0, n - 1, 0, n - 1, C.byref(h)), "create")
     L.HYPRE_IJMatrixSetObjectType(h, gb.HYPRE_PARCSR)
-    sizes = np.array([max(len(c), 1) for c, _ in rows], np.int32)
+    if sizes is None:
+        sizes = np.array([max(len(c), 1) for c, _ in rows], np.int32)
     if swap:
         L.HYPRE_IJMatrixSetDiagOffdSizes(h, sizes.ctypes.data, None)
     else:
@@ -124,6 +134,23 @@ def test_bulk_and_per_row_puts_match_reference_rules(gb, swap):
     assert len(exp[1]) >= 65536          # large enough for the device path
     same(assemble(gb, rows, bulk=True, swap=swap), exp)
     same(assemble(gb, rows, bulk=False, swap=swap), exp)
+    assert gb.lib().HYPRE_GetError() == 0
+
+
+def test_rows_without_space_shift_the_front_entry(gb):
+    """SetRowSizes with zeros for the empty rows (as the reference's drivers
+    pass the row lengths): the reference moves to the front the entry whose
+    column is the row's ordinal among the rows with space, not the diagonal.
+    Device path (one large put) and host path (a put per row) alike."""
+    rows = random_rows(6000, seed=9)
+    for r in range(0, 6000, 7):
+        rows[r] = ([], [])
+    sizes = np.array([len(c) for c, _ in rows], np.int32)
+    exp = expected_csr(rows, sizes=sizes)
+    assert len(exp[1]) >= 65536
+    assert not np.array_equal(exp[1], expected_csr(rows)[1])     # the rule changes the result here
+    same(assemble(gb, rows, bulk=True, sizes=sizes), exp)
+    same(assemble(gb, rows, bulk=False, sizes=sizes), exp)
     assert gb.lib().HYPRE_GetError() == 0
 
 

@@ -3,8 +3,8 @@
 * Against the reference library itself: every mm_* fixture (C = A*A written
   by the reference's HYPRE_ParCSRMatrixMatmat on its IJ-assembled A, including
   a matrix with empty rows, where the reference reserves no diagonal, and a
-  random unsymmetric one) is reproduced bit for bit -- row pointers, column
-  order and FP64 values.
+  random unsymmetric one) is reproduced bit for bit -- the IJ-assembled A
+  from the same puts, then C's row pointers, column order and FP64 values.
 * The reference's own SpGEMM benchmark (src/test/TEST_bench/benchmark_spgemm.jobs:13-16,
   saved output benchmark_spgemm.saved.tioga): the A^2 nonzero counts of the
   7-point and 27-point Laplacians on 128^3 and of the 5-point and 9-point
@@ -32,11 +32,20 @@ def _host_matrix(gb, I, J, V):
     return A
 
 
+def _put_rows(g):
+    """The rows as the reference driver put them (SetRowSizes, then the rows)."""
+    if "in_i" in g:
+        return g["in_i"], g["in_j"], g["in_v"]
+    from hypre_gb300 import problems as P
+    return P.laplace(g["case"]["kind"], *g["case"]["n"])
+
+
 @pytest.mark.parametrize("name", G.matmat_names())
 def test_matmat_matches_reference(gb, name):
     g = G.load(name)
-    A = _host_matrix(gb, g["A0_i"], g["A0_j"], g["A0_v"])
-    # the upload keeps the reference's assembled row order
+    ij = gb.IJMatrix(*_put_rows(g))
+    A = ij.par
+    # IJ assembly gives the reference's assembled rows (order included)
     Ia, Ja, Va = gb.parcsr_to_host(A)
     assert np.array_equal(Ia, g["A0_i"]) and np.array_equal(Ja, g["A0_j"]) and np.array_equal(Va, g["A0_v"])
     for rep in range(2):
@@ -46,7 +55,7 @@ def test_matmat_matches_reference(gb, name):
         assert np.array_equal(Cj, g["C0_j"]), f"{name} column order (call {rep})"
         assert np.array_equal(Cv, g["C0_v"]), f"{name} values (call {rep})"
         gb.check(gb.lib().HYPRE_ParCSRMatrixDestroy(Cm))
-    gb.lib().HYPRE_GB300_ParCSRMatrixDestroy(A)
+    ij.destroy()
 
 
 def test_matmat_rejects_incompatible(gb):
