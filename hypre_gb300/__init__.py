@@ -295,7 +295,10 @@ class BoomerAMG:
     def set(self, name, value):
         L = lib()
         if name == "CycleRelaxType":
-            return L.HYPRE_BoomerAMGSetCycleRelaxType(self.h, value[0], value[1])
+            # (type, part), or a list of them
+            for t, k in (value if isinstance(value, list) else [value]):
+                r = L.HYPRE_BoomerAMGSetCycleRelaxType(self.h, t, k)
+            return r
         if name == "CycleNumSweeps":
             return L.HYPRE_BoomerAMGSetCycleNumSweeps(self.h, value[0], value[1])
         if name == "CyclePrecision":

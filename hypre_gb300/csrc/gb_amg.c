@@ -71,6 +71,8 @@ static void level_free_vectors(gb_level *L)
    gb_dfree(L->F); gb_dfree(L->U); gb_dfree(L->U2); gb_dfree(L->V);
    gb_dfree(L->Ff); gb_dfree(L->Uf); gb_dfree(L->U2f); gb_dfree(L->Vf);
    gb_dfree(L->cheb_ds); gb_dfree(L->cheb_dsf); gb_dfree(L->W); gb_dfree(L->Wf);
+   gb_dfree(L->hgs_flags); gb_dfree(L->hgs_t); gb_dfree(L->hgs_tf);
+   L->hgs_flags = NULL; L->hgs_t = NULL; L->hgs_tf = NULL;
    L->F = L->U = L->U2 = L->V = NULL;
    L->Ff = L->Uf = L->U2f = L->Vf = NULL;
    L->cheb_ds = L->W = NULL;
@@ -98,6 +100,7 @@ static void amg_free_hierarchy(gb_amg *amg)
    amg->r_work = NULL;
    amg->num_levels = 0;
    amg->setup_done = 0;
+   amg->uses_hgs = 0;
 }
 
 /* --------------------------------------------------------------------------
@@ -951,7 +954,32 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
    return 1;
 }
 
-static int relax_l1_option(int type) { return type == 18 ? 1 : 5; }
+/* hybrid Gauss-Seidel relax types (gb_hgs.cu) */
+static int hgs_type(int t) { return t == 3 || t == 4 || t == 6 || t == 8 || t == 13 || t == 14; }
+
+/* l1-norm option of a level (par_amg_setup.c:3298-3496): the relax types of
+ * the level (down and up, or the coarsest's) pick it; later rules override
+ * earlier ones as in the reference: 8/13/14 -> option 4, 18 -> 1, and
+ * 7/11/12 -> 5 (also the default here) */
+static int relax_l1_option_level(const gb_amg_params *prm, int l, int nl)
+{
+   const int last = l == nl - 1;
+   const int a = last ? prm->relax_type[3] : prm->relax_type[1];
+   const int b = last ? prm->relax_type[3] : prm->relax_type[2];
+   int opt = 5;
+   if (a == 8 || a == 13 || a == 14 || b == 8 || b == 13 || b == 14) { opt = 4; }
+   if (a == 18 || b == 18) { opt = 1; }
+   /* 7/11/12 in any part of the cycle (the coarsest's only on the last level) */
+   const int *t = prm->relax_type;
+   if (t[1] == 7 || t[2] == 7 || (t[3] == 7 && last) || t[1] == 11 || t[2] == 11 || (t[3] == 11 && last) ||
+       t[1] == 12 || t[2] == 12 || (t[3] == 12 && last)) { opt = 5; }
+   return opt;
+}
+
+/* device flag set by a hybrid Gauss-Seidel sweep whose dependency wait ran
+ * out; read back once per solve (only when a hybrid sweep ran) */
+static int *g_hgs_err = NULL;
+static int g_hgs_used = 0;
 
 /* --------------------------------------------------------------------------
  * Chebyshev smoother setup
@@ -1259,9 +1287,8 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    {
       gb_level *L = &amg->lev[l];
       int n = L->n;
-      int type = (l == amg->num_levels - 1) ? prm->relax_type[3] : prm->relax_type[1];
       L->l1 = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
-      gb_l1_norms(n, L->A->A.i, L->A->A.j, L->A->A.v, relax_l1_option(type), L->l1, s);
+      gb_l1_norms(n, L->A->A.i, L->A->A.j, L->A->A.v, relax_l1_option_level(prm, l, amg->num_levels), L->l1, s);
       L->l1f = (float *) gb_dmalloc(sizeof(float) * (size_t) (n ? n : 1));
       gb_d2f(n, L->l1, L->l1f, s);
       L->relax_w = prm->level_relax_weight ? prm->level_relax_weight[l] : prm->relax_weight;
@@ -1271,6 +1298,16 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
       size_t nf = sizeof(float) * (size_t) (n ? n : 1);
       L->Ff = (float *) gb_dcalloc(nf); L->Uf = (float *) gb_dcalloc(nf);
       L->U2f = (float *) gb_dcalloc(nf); L->Vf = (float *) gb_dcalloc(nf);
+      const int last = l == amg->num_levels - 1;
+      if ((!last && (hgs_type(prm->relax_type[1]) || hgs_type(prm->relax_type[2]))) ||
+          (last && hgs_type(prm->relax_type[3])))
+      {
+         L->hgs_flags = (int *) gb_dcalloc(sizeof(int) * ((size_t) n + 1));
+         L->hgs_t = (double *) gb_dcalloc(nb);
+         L->hgs_tf = (float *) gb_dcalloc(nf);
+         if (!g_hgs_err) { g_hgs_err = (int *) gb_dcalloc(sizeof(int)); }
+         amg->uses_hgs = 1;
+      }
    }
    /* coarsest grid: dense inverse (par_gauss_elim.c:33) */
    {
@@ -1295,6 +1332,8 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
       int vp0 = prm->cycle_prec == GB_PREC_F16 && l == 0 ? GB_PREC_F16 : vp;
       gb_solve_desc(L->A, vp0);
       if (vp0 != GB_PREC_F64) { gb_solve_desc(L->A, GB_PREC_F64); }
+      /* hybrid Gauss-Seidel in the FP16-finest cycle sweeps FP32 CSR values */
+      if (vp0 == GB_PREC_F16 && L->hgs_flags) { gb_solve_desc(L->A, GB_PREC_F32); }
       if (L->P) { gb_solve_desc(L->P, vp); gb_solve_desc(L->R, vp); }
       /* lower-part forms for two-stage Gauss-Seidel (built here, outside any
        * graph capture of the cycle) */
@@ -1373,6 +1412,84 @@ static void twostage_gs_d(gb_amg *amg, int l, int inner, const double *f, double
    }
 }
 
+/* Hybrid Gauss-Seidel relaxation in place on u (relax 3/4: forward/backward,
+ * 6: symmetric; 13/14/8: the same with l1 norms; par_relax.c:954-1377):
+ * one relaxation is one sweep, or a forward and a backward sweep (6, 8).
+ * Unscaled (weight and outer weight 1): 3/4/6 leave the diagonal out of the
+ * sum and divide by it, 8/13/14 include it and add res / l1; scaled: the
+ * reference's weighted form over the values from before the relaxation. */
+static void hybrid_gs_d(gb_amg *amg, int l, int type, const double *f, double *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   const int n = L->n;
+   if (u_zero) { gb_fill_d(n, u, 0.0, s); }
+   const double w = L->relax_w, omega = 1.0;
+   const int scaled = !(w == 1.0 && omega == 1.0);
+   const int l1 = type == 8 || type == 13 || type == 14;
+   const int skip = l1 ? scaled : 1;
+   double *ut = NULL;
+   if (scaled)
+   {
+      ut = L->hgs_t;
+      cudaMemcpyAsync(ut, u, sizeof(double) * (size_t) n, cudaMemcpyDeviceToDevice, s);
+   }
+   const int dir0 = (type == 4 || type == 14) ? -1 : 1;
+   const int nsw = (type == 6 || type == 8) ? 2 : 1;
+   const gb_csr *A = &L->A->A;
+   for (int k = 0; k < nsw; k++)
+   {
+      gb_hgs_sweep_d(n, A->i, A->j, A->v, f, u, L->V, ut, l1 ? L->l1 : NULL, k == 0 ? dir0 : -dir0, skip, w, omega,
+                     L->hgs_flags, g_hgs_err, s);
+   }
+   g_hgs_used = 1;
+}
+
+static void hybrid_gs_f(gb_amg *amg, int l, int type, const float *f, float *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   const int n = L->n;
+   if (u_zero) { gb_fill_f(n, u, 0.f, s); }
+   const double w = L->relax_w, omega = 1.0;
+   const int scaled = !(w == 1.0 && omega == 1.0);
+   const int l1 = type == 8 || type == 13 || type == 14;
+   const int skip = l1 ? scaled : 1;
+   float *ut = NULL;
+   if (scaled)
+   {
+      ut = L->hgs_tf;
+      cudaMemcpyAsync(ut, u, sizeof(float) * (size_t) n, cudaMemcpyDeviceToDevice, s);
+   }
+   const int dir0 = (type == 4 || type == 14) ? -1 : 1;
+   const int nsw = (type == 6 || type == 8) ? 2 : 1;
+   const gb_spmv_desc *A = gb_solve_desc(L->A, GB_PREC_F32);
+   for (int k = 0; k < nsw; k++)
+   {
+      gb_hgs_sweep_f(n, A->i, A->j, (const float *) A->v, f, u, L->Vf, ut, l1 ? L->l1f : NULL,
+                     k == 0 ? dir0 : -dir0, skip, w, omega, L->hgs_flags, g_hgs_err, s);
+   }
+   g_hgs_used = 1;
+}
+
+/* HYPRE_ERROR_GENERIC when a hybrid Gauss-Seidel sweep since the last check
+ * gave up waiting on a dependency (reads one int; only after a sweep ran) */
+int gb_amg_check_sweeps(void)
+{
+   if (!g_hgs_used || !g_hgs_err) { return 0; }
+   int h = 0;
+   cudaMemcpyAsync(&h, g_hgs_err, sizeof(int), cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   g_hgs_used = 0;
+   if (h)
+   {
+      cudaMemsetAsync(g_hgs_err, 0, sizeof(int), gb_stream());
+      gb_error(HYPRE_ERROR_GENERIC, "hybrid Gauss-Seidel sweep: a dependency wait ran out");
+      return 1;
+   }
+   return 0;
+}
+
 /* Chebyshev smoother, in place on u (hypre_ParCSRRelax_Cheby_SolveHost,
  * src/parcsr_ls/par_cheby_solve.c:194): r = D^{-1/2}(f - Au), then the
  * polynomial by Horner steps, each one SpMV with a fused epilogue. */
@@ -1436,6 +1553,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       {
          if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], uz && sw == 0); }
          else if (type == 16) { cheby_d(amg, l, F[l], U[l], uz && sw == 0); }
+         else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], uz && sw == 0); }
          else
          {
             if (uz && sw == 0) { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
@@ -1456,6 +1574,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       gb_level *L = &amg->lev[l];
       if (amg->coarse_inv) { gb_dense_apply_d(amg->coarse_n, amg->coarse_inv, F[l], U[l], s); }
       else if (nl == 1 && !u0_zero && prm->relax_type[3] == 16) { cheby_d(amg, l, F[l], U[l], 0); }
+      else if (nl == 1 && !u0_zero && hgs_type(prm->relax_type[3])) { hybrid_gs_d(amg, l, prm->relax_type[3], F[l], U[l], 0); }
       else if (nl == 1 && !u0_zero)
       {
          relax_d(amg, l, prm->relax_type[3], F[l], U[l], L->U2, 0);
@@ -1466,6 +1585,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
          int type = prm->relax_type[3];
          if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
          else if (type == 16) { cheby_d(amg, l, F[l], U[l], 1); }
+         else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], 1); }
          else { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
       }
    }
@@ -1477,10 +1597,11 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       gb_spmv_d(gb_solve_desc(L->P, GB_PREC_F64), U[l + 1], L->U2, 0, 1.0, 1.0, U[l], NULL, 0.0, NULL, NULL, s);
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
-         if (type == 11 || type == 12 || type == 16)
+         if (type == 11 || type == 12 || type == 16 || hgs_type(type))
          {
             if (sw == 0) { cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
             if (type == 16) { cheby_d(amg, l, F[l], U[l], 0); }
+            else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], 0); }
             else { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0); }
          }
          else
@@ -1557,6 +1678,7 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
       {
          if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], sw == 0); }
          else if (type == 16) { cheby_f(amg, l, F[l], U[l], sw == 0); }
+         else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], sw == 0); }
          else if (sw == 0) { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
          else
          {
@@ -1575,6 +1697,7 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
          int type = prm->relax_type[3];
          if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
          else if (type == 16) { cheby_f(amg, l, F[l], U[l], 1); }
+         else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], 1); }
          else { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
       }
    }
@@ -1585,10 +1708,11 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
       gb_spmv_f(gb_solve_desc(L->P, GB_PREC_F32), U[l + 1], L->U2f, 0, 1.f, 1.f, U[l], NULL, 0.f, NULL, NULL, s);
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
-         if (type == 11 || type == 12 || type == 16)
+         if (type == 11 || type == 12 || type == 16 || hgs_type(type))
          {
             if (sw == 0) { cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
             if (type == 16) { cheby_f(amg, l, F[l], U[l], 0); }
+            else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], 0); }
             else { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0); }
          }
          else if (sw == 0) { relax_f(amg, l, type, F[l], L->U2f, U[l], 0); }
@@ -1614,6 +1738,7 @@ int gb_amg_cycle(gb_amg *amg, const double *f, double *u)
 {
    cudaStream_t s = gb_stream();
    int prec = amg->prm.cycle_prec;
+   if (amg->uses_hgs) { g_hgs_used = 1; }
    if (amg->prm.use_graph)
    {
       if (amg->graph && (amg->graph_f != f || amg->graph_u != u || amg->graph_prec != prec))
@@ -1725,6 +1850,7 @@ HYPRE_Int HYPRE_BoomerAMGSolve(HYPRE_Solver solver, HYPRE_ParCSRMatrix A, HYPRE_
    }
    a->num_iterations = iter;
    a->rel_resid = rel;
+   gb_amg_check_sweeps();
    return gb_error_flag;
 }
 
@@ -1805,7 +1931,8 @@ HYPRE_Int HYPRE_BoomerAMGSetCycleType(HYPRE_Solver solver, HYPRE_Int v)
 
 static int relax_supported(int t)
 {
-   return t == 18 || t == 7 || t == 11 || t == 12 || t == 16 || t == 9 || t == 99 || t == 19 || t == 98;
+   return t == 18 || t == 7 || t == 11 || t == 12 || t == 16 || t == 9 || t == 99 || t == 19 || t == 98 ||
+          hgs_type(t);
 }
 
 HYPRE_Int HYPRE_BoomerAMGSetRelaxType(HYPRE_Solver solver, HYPRE_Int v)

@@ -1,0 +1,161 @@
+// Hybrid Gauss-Seidel sweeps (relax types 3, 4, 6, 8, 13, 14), bit for bit
+// the reference's single-process loops (src/parcsr_ls/par_relax.h:13-330,
+// hypre_HybridGaussSeidelNS and hypre_HybridGaussSeidel, driven by
+// hypre_BoomerAMGRelaxHybridGaussSeidel_core, par_relax.c:692-945).
+//
+// A sweep visits the rows in order (forward: 0..n-1, backward: n-1..0).  Row
+// i reads the values the sweep already produced for the rows before it and
+// the values from before the sweep for the rows after it, and sums its terms
+// in CSR order.  On the GPU each warp takes the next row of the sweep from an
+// atomic counter; a row waits only for the earlier rows its entries refer to
+// (their flags, set with release semantics after the value is stored), so
+// rows without such a dependency run at once and the sweep's critical path is
+// the dependency depth of the matrix, not its row count.  Rows are handed out
+// in sweep order to running warps, so the earliest unfinished row never waits
+// on a row that no warp holds: the sweep always progresses.  Every wait is
+// bounded (GB_HGS_SPIN polls); a wait that runs out sets *err and the sweep
+// finishes with an undefined result, which the host reports.
+//
+// The products, sums and divisions use explicit round-to-nearest operations
+// in the reference's order, so the FP64 sweep equals the sequential loop.
+#include "gb_device.cuh"
+
+#define GB_HGS_SPIN (1 << 21)
+
+__device__ __forceinline__ int hgs_ld_acquire(const int *p)
+{
+   int v;
+   asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+   return v;
+}
+
+__device__ __forceinline__ void hgs_st_release(int *p, int v)
+{
+   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ double hgs_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float hgs_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double hgs_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float hgs_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double hgs_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float hgs_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double hgs_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float hgs_div(float a, float b) { return __fdiv_rn(a, b); }
+
+// One sweep.  u: values updated in place; uo: u as it was when the sweep
+// started (read for the rows not yet visited and for the row's own entry);
+// ut: u before the first sweep of the relaxation (the scaled form's second
+// sum, hypre's Vtemp), NULL when unscaled; dvec: l1 norms (relax 8/13/14) or
+// NULL for the diagonal (the row's first entry).  skip: the row's first
+// (diagonal) entry is left out of the sums.  flags[0..n-1] and flags[n] (the
+// row counter) start at zero.
+template <typename T>
+__global__ void __launch_bounds__(256) k_hgs(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                                             const T *__restrict__ Av, const T *__restrict__ f, T *u,
+                                             const T *__restrict__ uo, const T *__restrict__ ut,
+                                             const T *__restrict__ dvec, int dir, int skip, T w, T omega, T prod,
+                                             int *flags, int *err)
+{
+   const int lane = threadIdx.x & 31;
+   int *counter = flags + n;
+   for (;;)
+   {
+      int t = 0;
+      if (lane == 0) { t = atomicAdd(counter, 1); }
+      t = __shfl_sync(GB_FULL, t, 0);
+      if (t >= n) { break; }
+      const int i = dir > 0 ? t : n - 1 - t;
+      const int b = Ai[i], e = Ai[i + 1];
+      const T aii = e > b ? Av[b] : (T) 0;
+      const T di = dvec ? dvec[i] : aii;
+      T ui = uo[i];
+      if (di != (T) 0)
+      {
+         T res = f[i], res0 = 0, res2 = 0;
+         for (int c = b + skip; c < e; c += 32)
+         {
+            const int k = c + lane;
+            T p = 0, p2 = 0;
+            if (k < e)
+            {
+               const int col = Aj[k];
+               const T a = Av[k];
+               T v;
+               if (dir > 0 ? col < i : col > i)
+               {
+                  // a row the sweep visited before this one: wait for its value
+                  int spins = 0;
+                  while (hgs_ld_acquire(flags + col) == 0)
+                  {
+                     if (++spins > GB_HGS_SPIN || *(volatile int *) err) { atomicExch(err, 1); break; }
+                     __nanosleep(64);
+                  }
+                  v = __ldcg(u + col);
+               }
+               else { v = uo[col]; }
+               p = hgs_mul(a, v);
+               if (ut) { p2 = hgs_mul(a, ut[col]); }
+            }
+            const int cnt = min(32, e - c);
+            for (int q = 0; q < cnt; q++)
+            {
+               const T pq = __shfl_sync(GB_FULL, p, q);
+               if (ut)
+               {
+                  const T p2q = __shfl_sync(GB_FULL, p2, q);
+                  res0 = hgs_sub(res0, pq);
+                  res2 = hgs_add(res2, p2q);
+               }
+               else { res = hgs_sub(res, pq); }
+            }
+         }
+         if (ut)
+         {
+            // u = (skip ? u * prod : u) + w * (omega * f + res0 + (1 - omega) * res2) / d
+            const T s = hgs_add(hgs_add(hgs_mul(omega, res), res0), hgs_mul(hgs_sub((T) 1, omega), res2));
+            const T upd = hgs_div(hgs_mul(w, s), di);
+            ui = hgs_add(skip ? hgs_mul(ui, prod) : ui, upd);
+         }
+         else if (skip) { ui = hgs_div(res, di); }
+         else { ui = hgs_add(ui, hgs_div(res, di)); }
+      }
+      if (lane == 0)
+      {
+         u[i] = ui;
+         hgs_st_release(flags + i, 1);
+      }
+      __syncwarp();
+   }
+}
+
+template <typename T>
+static void hgs_sweep(int n, const int *Ai, const int *Aj, const T *Av, const T *f, T *u, T *uo, const T *ut,
+                      const T *dvec, int dir, int skip, double w, double omega, int *flags, int *err, cudaStream_t s)
+{
+   if (n <= 0) { return; }
+   cudaMemsetAsync(flags, 0, sizeof(int) * ((size_t) n + 1), s);
+   cudaMemcpyAsync(uo, u, sizeof(T) * (size_t) n, cudaMemcpyDeviceToDevice, s);
+   // a warp per row in flight; enough warps to cover a dependency front of a
+   // few thousand rows, few enough that the spinning warps leave issue slots
+   long long warps = n < 152LL * 16 ? n : 152LL * 16;
+   int blocks = (int) ((warps * 32 + 255) / 256);
+   const double prod = 1.0 - w * omega;
+   k_hgs<T><<<blocks, 256, 0, s>>>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, (T) w, (T) omega, (T) prod, flags,
+                                   err);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_hgs_sweep_d(int n, const int *Ai, const int *Aj, const double *Av, const double *f, double *u,
+                               double *uo, const double *ut, const double *dvec, int dir, int skip, double w,
+                               double omega, int *flags, int *err, cudaStream_t s)
+{
+   hgs_sweep<double>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
+}
+
+extern "C" void gb_hgs_sweep_f(int n, const int *Ai, const int *Aj, const float *Av, const float *f, float *u,
+                               float *uo, const float *ut, const float *dvec, int dir, int skip, double w,
+                               double omega, int *flags, int *err, cudaStream_t s)
+{
+   hgs_sweep<float>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
+}

@@ -177,6 +177,11 @@ typedef struct
    double     cheb_eig[2];
    double    *cheb_ds, *W;
    float     *cheb_dsf, *Wf;
+   /* hybrid Gauss-Seidel (relax 3, 4, 6, 8, 13, 14): row flags and counter
+    * (n + 1 ints) and the relaxation's starting values (scaled forms) */
+   int       *hgs_flags;
+   double    *hgs_t;
+   float     *hgs_tf;
 } gb_level;
 
 typedef struct
@@ -202,11 +207,13 @@ typedef struct
    double        learned_theta;
    double        learned_w[32];
    void         *multi_ws;      /* multi-vector cycle work space (gb_multi.c) */
+   int           uses_hgs;      /* some level relaxes with hybrid Gauss-Seidel */
    double        spgemm_bytes, spgemm_seconds;   /* sparse products of the last setup */
    int           spgemm_calls;
 } gb_amg;
 
 int gb_amg_cycle(gb_amg *amg, const double *f, double *u);   /* one V-cycle, u from zero */
+int gb_amg_check_sweeps(void);   /* HYPRE_ERROR_GENERIC after a hybrid Gauss-Seidel wait ran out */
 int gb_amg_setup(gb_amg *amg, gb_parcsr *A0);
 /* learned parameters (gb_learn.c): strength threshold from the finest level's
  * rows before coarsening, smoother weight per level after the hierarchy */

@@ -148,6 +148,17 @@ void gb_block_inverse(int nsys, const int *off, const int *Ai, const int *Aj, co
                       const long long *doff, double *D, double *W, cudaStream_t s);
 void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, double *D, double *W, cudaStream_t s);
 
+/* hybrid Gauss-Seidel sweep (gb_hgs.cu): dir +1 forward, -1 backward; uo
+ * receives u's values from before the sweep; ut: the scaled form's starting
+ * values (NULL: unscaled); dvec: l1 norms or NULL (diagonal); flags: n + 1
+ * ints; *err set when a dependency wait ran out */
+void gb_hgs_sweep_d(int n, const int *Ai, const int *Aj, const double *Av, const double *f, double *u, double *uo,
+                    const double *ut, const double *dvec, int dir, int skip, double w, double omega, int *flags,
+                    int *err, cudaStream_t s);
+void gb_hgs_sweep_f(int n, const int *Ai, const int *Aj, const float *Av, const float *f, float *u, float *uo,
+                    const float *ut, const float *dvec, int dir, int skip, double w, double omega, int *flags,
+                    int *err, cudaStream_t s);
+
 /* solve phase */
 void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int mode, double alpha, double beta,
                const double *b, const double *d, double w, const double *dotz, double *dpart, cudaStream_t st);

@@ -396,8 +396,9 @@ static HYPRE_Int kry_solve(HYPRE_Solver solver, HYPRE_Matrix A, HYPRE_Vector b, 
       gb_error_in_arg(3);
       return gb_error_flag;
    }
-   if (k->magic == GB_MAGIC_PCG) { return pcg_solve(k, M, bv, xv); }
-   return fgmres_solve(k, M, bv, xv);
+   HYPRE_Int r = k->magic == GB_MAGIC_PCG ? pcg_solve(k, M, bv, xv) : fgmres_solve(k, M, bv, xv);
+   if (gb_amg_check_sweeps()) { r = gb_error_flag; }
+   return r;
 }
 
 HYPRE_Int HYPRE_PCGSetup(HYPRE_Solver s, HYPRE_Matrix A, HYPRE_Vector b, HYPRE_Vector x) { return kry_setup(s, A, b, x); }

@@ -1971,7 +1971,8 @@ __global__ void k_l1(int n, const int *__restrict__ Ai, const int *__restrict__ 
       if (Aj[k] == i) { d = v; }
       s += fabs(v);
    }
-   double r = option == 1 ? s : (d != 0.0 ? d : 1.0);
+   // option 1: sum |a_ij|; 4 (one process): |a_ii|; 5: a_ii, 0 -> 1
+   double r = option == 1 ? s : option == 4 ? fabs(d) : (d != 0.0 ? d : 1.0);
    if (d < 0.0) { r = -r; }
    l1[i] = r;
 }

@@ -1032,7 +1032,8 @@ int or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P
 
 /* ------------------------------------------------------------------------ */
 /* l1 norms, hypre_ParCSRComputeL1Norms src/parcsr_ls/ams.c:517-790          */
-/* option 1: sum |a_ij| (relax 18); option 5: diagonal, 0 -> 1 (relax 7/11/12) */
+/* option 1: sum |a_ij| (relax 18); option 4: |a_ii| on one process (relax  */
+/* 8/13/14); option 5: diagonal, 0 -> 1 (relax 7/11/12)                      */
 /* ------------------------------------------------------------------------ */
 
 int or_l1_norms(const or_csr *A, int option, double *l1)
@@ -1049,6 +1050,7 @@ int or_l1_norms(const or_csr *A, int option, double *l1)
       }
       double v;
       if (option == 1) { v = s; }
+      else if (option == 4) { v = fabs(d); }   /* one process: |a_ii| (ams.c:649-684) */
       else { v = d != 0.0 ? d : 1.0; }
       if (d < 0.0) { v = -v; }   /* negative-definite rows, :747-770 */
       l1[i] = v;
@@ -1450,6 +1452,53 @@ static void relax_cheby(const or_csr *A, const double *f, const double *ds, cons
    for (int i = 0; i < n; i++) { u[i] = o[i] + ds[i] * u[i]; }
 }
 
+/* Hybrid Gauss-Seidel on one process (relax 3/4/6 and 8/13/14):
+ * hypre_BoomerAMGRelaxHybridGaussSeidel_core src/parcsr_ls/par_relax.c:692-945
+ * with one thread, whose sweeps are hypre_HybridGaussSeidelNS (unscaled,
+ * src/parcsr_ls/par_relax.h:13-108) and hypre_HybridGaussSeidel (scaled,
+ * :222-330).  dir0: direction of the first sweep; nsw: 1, or 2 for the
+ * symmetric types (a forward then a backward sweep); d: l1 norms or NULL
+ * (the row's first entry, the diagonal); skip: leave the first entry out of
+ * the sums.  Vt: the values before the relaxation (the scaled form's Vtemp). */
+static void relax_hybrid_gs(const or_csr *A, const double *f, const double *d, double w, double omega, int dir0,
+                            int nsw, int skip, double *u, double *Vt)
+{
+   int n = A->nr;
+   const int non_scale = w == 1.0 && omega == 1.0;
+   const double prod = 1.0 - w * omega, one_minus_omega = 1.0 - omega;
+   if (!non_scale) { memcpy(Vt, u, sizeof(double) * (size_t) n); }
+   for (int sw = 0; sw < nsw; sw++)
+   {
+      const int dir = sw == 0 ? dir0 : -dir0;
+      const int ib = dir > 0 ? 0 : n - 1, ie = dir > 0 ? n : -1;
+      for (int i = ib; i != ie; i += dir)
+      {
+         const double di = d ? d[i] : A->v[A->i[i]];
+         if (di == 0.0) { continue; }
+         if (non_scale)
+         {
+            double res = f[i];
+            for (int jj = A->i[i] + skip; jj < A->i[i + 1]; jj++) { res -= A->v[jj] * u[A->j[jj]]; }
+            if (skip) { u[i] = res / di; }
+            else { u[i] += res / di; }
+         }
+         else
+         {
+            double res = f[i], res0 = 0.0, res2 = 0.0;
+            for (int jj = A->i[i] + skip; jj < A->i[i + 1]; jj++)
+            {
+               res0 -= A->v[jj] * u[A->j[jj]];
+               res2 += A->v[jj] * Vt[A->j[jj]];
+            }
+            if (skip) { u[i] *= prod; }
+            u[i] += w * (omega * res + res0 + one_minus_omega * res2) / di;
+         }
+      }
+   }
+}
+
+static int hybrid_gs_type(int t) { return t == 3 || t == 4 || t == 6 || t == 8 || t == 13 || t == 14; }
+
 static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u, int u_zero)
 {
    const or_csr *A = &H->A[lvl];
@@ -1464,7 +1513,18 @@ static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u
       free(r); free(o); free(tmp);
       return;
    }
-   if (type == 18 || type == 7)
+   if (hybrid_gs_type(type))
+   {
+      /* par_relax.c:954-1377: 3 forward, 4 backward, 6 symmetric (diagonal);
+       * 13 forward, 14 backward, 8 symmetric (l1 norms; the diagonal term
+       * stays in the sum unless weighted) */
+      const int l1 = type == 8 || type == 13 || type == 14;
+      const double omega = 1.0;
+      const int skip = l1 ? !(w == 1.0 && omega == 1.0) : 1;
+      relax_hybrid_gs(A, f, l1 ? H->l1[lvl] : NULL, w, omega, (type == 4 || type == 14) ? -1 : 1,
+                      (type == 6 || type == 8) ? 2 : 1, skip, u, H->Ztmp);
+   }
+   else if (type == 18 || type == 7)
    {
       relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero);
    }
@@ -1564,8 +1624,17 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
       int n = H->A[l].nr;
       H->F[l] = xcalloc(n, sizeof(double));
       H->U[l] = xcalloc(n, sizeof(double));
-      int type = (l == nl - 1) ? prm->relax_coarse : prm->relax_down;
-      int opt = (type == 18) ? 1 : 5;
+      /* the l1 option of a level (par_amg_setup.c:3298-3496): its relax
+       * types (down and up, or the coarsest's) choose, later rules
+       * overriding earlier ones: 8/13/14 -> 4, 18 -> 1, 7/11/12 -> 5 */
+      const int last = l == nl - 1;
+      const int ta = last ? prm->relax_coarse : prm->relax_down, tb = last ? prm->relax_coarse : prm->relax_up;
+      int opt = 5;
+      if (ta == 8 || ta == 13 || ta == 14 || tb == 8 || tb == 13 || tb == 14) { opt = 4; }
+      if (ta == 18 || tb == 18) { opt = 1; }
+      const int t1 = prm->relax_down, t2 = prm->relax_up, t3 = prm->relax_coarse;
+      if (t1 == 7 || t2 == 7 || (t3 == 7 && last) || t1 == 11 || t2 == 11 || (t3 == 11 && last) ||
+          t1 == 12 || t2 == 12 || (t3 == 12 && last)) { opt = 5; }
       H->l1[l] = xmalloc(sizeof(double) * (n ? n : 1));
       or_l1_norms(&H->A[l], opt, H->l1[l]);
    }

@@ -170,7 +170,7 @@ int main(int argc, char **argv)
    int relax = 18, relax_coarse = 9, coarse_th = 9, maxit = 100, solver = 1, kdim = 30;
    int max_levels = 25, dump_levels = 1, seed = 22775, cheby_order = 2, relax_order = 0;
    int coarsen = 8, precond = 1, keep_t = 0, rhs_ones = 0;
-   int repeat = 1, threads = 0, want_digest = 0, matmat = 0;
+   int repeat = 1, threads = 0, want_digest = 0, matmat = 0, relax_down = -1, relax_up = -1;
    const char *jsonfile = NULL;
    double cheby_fraction = 0.3;
 
@@ -195,6 +195,8 @@ int main(int argc, char **argv)
       else if (ARG("-np")) { num_paths = atoi(argv[++a]); }
       else if (ARG("-rlx")) { relax = atoi(argv[++a]); }
       else if (ARG("-rlx_coarse")) { relax_coarse = atoi(argv[++a]); }
+      else if (ARG("-rlx_down")) { relax_down = atoi(argv[++a]); }
+      else if (ARG("-rlx_up")) { relax_up = atoi(argv[++a]); }
       else if (ARG("-coarse_th")) { coarse_th = atoi(argv[++a]); }
       else if (ARG("-maxit")) { maxit = atoi(argv[++a]); }
       else if (ARG("-solver")) { solver = atoi(argv[++a]); }
@@ -342,6 +344,8 @@ int main(int argc, char **argv)
    HYPRE_BoomerAMGSetAggP12MaxElmts(amg, agg_p12);
    HYPRE_BoomerAMGSetNumPaths(amg, num_paths);
    HYPRE_BoomerAMGSetRelaxType(amg, relax);
+   if (relax_down >= 0) { HYPRE_BoomerAMGSetCycleRelaxType(amg, relax_down, 1); }
+   if (relax_up >= 0) { HYPRE_BoomerAMGSetCycleRelaxType(amg, relax_up, 2); }
    HYPRE_BoomerAMGSetCycleRelaxType(amg, relax_coarse, 3);
    HYPRE_BoomerAMGSetRelaxWt(amg, relax_wt);
    HYPRE_BoomerAMGSetRelaxOrder(amg, relax_order);

@@ -54,12 +54,27 @@ CASES = {
                                solver=1, full=True),
     "lap27_10_cheby2_pcg": dict(kind=27, n=(10, 10, 10), th=0.25, mxrs=0.9, Pmx=4, rlx=16, cheby_order=2,
                                 coarse_th=9, solver=1, full=True),
+    # hybrid Gauss-Seidel: the reference's CPU defaults 13 down / 14 up (l1),
+    # symmetric 6 and 8 (8 also weighted), forward 3 and backward 4
+    "lap7_14_hgs13_14_pcg": dict(kind=7, n=(14, 14, 14), th=0.25, mxrs=1.0, Pmx=4, rlx=13, rlx_down=13, rlx_up=14,
+                                 coarse_th=9, solver=1, full=True),
+    "lap27_12_hgs6_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=6, coarse_th=9, solver=1,
+                              full=True),
+    "lap7_12_hgs8_w08_pcg": dict(kind=7, n=(12, 12, 12), th=0.25, mxrs=1.0, Pmx=4, rlx=8, w=0.8, coarse_th=9,
+                                 solver=1, full=True),
+    "lap27_12_hgs3_fgmres": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=3, coarse_th=9, solver=61,
+                                 k=30, full=True),
+    "lap7_13_agg_hgs4_fgmres": dict(kind=7, n=(13, 13, 13), th=0.25, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=6,
+                                    rlx=4, coarse_th=9, solver=61, k=30, full=True),
+    "lap27_30_hgs13_14_pcg": dict(kind=27, n=(30, 30, 30), th=0.5, mxrs=1.0, Pmx=4, rlx=13, rlx_down=13, rlx_up=14,
+                                  coarse_th=9, solver=1, full=False),
 }
 
 
 def dump_args(c, out):
     a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "agg_nl", "agg_interp", "rlx", "coarse_th", "solver", "k", "cheby_order"):
+    for key in ("th", "mxrs", "Pmx", "tr", "agg_nl", "agg_interp", "rlx", "rlx_down", "rlx_up", "w", "coarse_th",
+                "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]
     return a + ["-tol", "1e-8", "-rlx_coarse", "9", "-o", out]

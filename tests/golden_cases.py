@@ -32,8 +32,9 @@ def oracle_params(c):
     """or_amg_params keyword arguments of a golden case."""
     p = dict(strong_threshold=c["th"], max_row_sum=c["mxrs"], p_max_elmts=c["Pmx"],
              trunc_factor=c.get("tr", 0.0), agg_num_levels=c.get("agg_nl", 0),
-             agg_interp_type=c.get("agg_interp", 4), relax_down=c["rlx"], relax_up=c["rlx"], relax_coarse=9,
-             max_coarse_size=c["coarse_th"])
+             agg_interp_type=c.get("agg_interp", 4), relax_down=c.get("rlx_down", c["rlx"]),
+             relax_up=c.get("rlx_up", c["rlx"]), relax_coarse=9, max_coarse_size=c["coarse_th"],
+             relax_weight=c.get("w", 1.0))
     if "cheby_order" in c:
         p["cheby_order"] = c["cheby_order"]
     return p
@@ -42,7 +43,11 @@ def oracle_params(c):
 def amg_params(c):
     """HYPRE_BoomerAMGSet* values of a golden case."""
     p = dict(StrongThreshold=c["th"], MaxRowSum=c["mxrs"], PMaxElmts=c["Pmx"], TruncFactor=c.get("tr", 0.0),
-             AggNumLevels=c.get("agg_nl", 0), RelaxType=c["rlx"], MaxCoarseSize=c["coarse_th"])
+             AggNumLevels=c.get("agg_nl", 0), RelaxType=c["rlx"], MaxCoarseSize=c["coarse_th"],
+             RelaxWt=c.get("w", 1.0))
+    cyc = [(c[k], part) for k, part in (("rlx_down", 1), ("rlx_up", 2)) if k in c]
+    if cyc:
+        p["CycleRelaxType"] = cyc
     if c.get("agg_nl", 0):
         p["AggInterpType"] = c.get("agg_interp", 4)
     if "cheby_order" in c:
