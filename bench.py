@@ -287,6 +287,7 @@ def gpu_arm(args):
         gb.check(L.HYPRE_GB300_BoomerAMGLevelSpMVTime(src[0], 0, prec, 20, C.byref(sec), C.byref(byt)), "spmv time")
         cyc[label] = {"bound": "hbm", "kernel": "SpMV level 0, SELL-32, %s values, FP32 vectors, 16-bit offset "
                       "column indices" % ("FP32" if prec == 1 else "FP16 (row-scaled)"),
+                      "launch_shape": _spmv_shape(L, step_mats.get(src[1].value), prec),
                       "achieved": byt.value / sec.value / 1e9, "peak": peak, "unit": "GB/s",
                       "frac": byt.value / sec.value / 1e9 / peak, "traffic": None,
                       "algorithmic_bytes": byt.value, "launch_seconds": sec.value,
@@ -417,6 +418,7 @@ def gpu_arm(args):
                           "%s column indices)" % ("FP32 (all exact)" if exact32 else "FP64",
                                                   "16-bit offset" if idx_bytes == 2 else "int32"),
                           "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                          "launch_shape": _spmv_shape(L, A, 0),
                           "traffic": traffic, "algorithmic_bytes": spmv_bytes, "launch_seconds": spmv_s,
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "roofline_spmv_fp32": cyc.get("fp32"),
@@ -429,6 +431,17 @@ def gpu_arm(args):
         print(json.dumps(result))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _spmv_shape(L, A, prec):
+    """The autotuned launch shape of a matrix's solve form in one precision
+    (level 0's operator is the matrix the setup was given)."""
+    if A is None:
+        return None
+    f, b, d = C.c_int(), C.c_int(), C.c_int()
+    L.HYPRE_GB300_ParCSRMatrixGetSpMVShape(A, prec, C.byref(f), C.byref(b), C.byref(d))
+    return {"format": "SELL-32" if f.value == 1 else "CSR", "block": b.value,
+            ("prefetch_depth" if f.value == 1 else "lanes_per_row"): d.value}
 
 
 def ref_binary():

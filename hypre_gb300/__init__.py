@@ -111,6 +111,9 @@ def _declare(L):
         "HYPRE_GB300_ParVectorCreateMulti": [i32, i32, P(vp)],
         "HYPRE_GB300_BoomerAMGGetSpGEMMStats": [vp, P(f64), P(f64), P(i32)],
         "HYPRE_GB300_BoomerAMGLevelSpMVTime": [vp, i32, i32, i32, P(f64), P(f64)],
+        "HYPRE_GB300_SetAutotune": [i32],
+        "HYPRE_GB300_ParCSRMatrixGetSpMVShape": [vp, i32, P(i32), P(i32), P(i32)],
+        "HYPRE_GB300_ParCSRMatrixSetSpMVShape": [vp, i32, i32, i32],
         "HYPRE_GB300_KrylovGetMultiNumIterations": [vp, vp],
         "HYPRE_GB300_KrylovGetMultiFinalRelativeResidualNorms": [vp, vp],
         "HYPRE_GB300_KrylovGetMultiResidualHistory": [vp, i32, i32, vp, P(i32)],

@@ -158,6 +158,7 @@ const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec)
       f->desc.sl_j16 = M->sell.j16;
    }
    f->valid = 1;
+   gb_spmv_autotune(&f->desc, A->nnz);
    return &f->desc;
 }
 

@@ -123,6 +123,7 @@ gb_parcsr *gb_parcsr_wrap(gb_csr A, int owns);
 void       gb_parcsr_free(gb_parcsr *M);
 void       gb_csr_free(gb_csr *A);
 const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec);   /* builds lazily */
+void gb_spmv_autotune(gb_spmv_desc *d, long long nnz);        /* gb_tune.c */
 /* strictly lower part of a large matrix for two-stage Gauss-Seidel (NULL for
  * small or wide-row matrices: the CSR kernel is used there); builds lazily */
 const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag);

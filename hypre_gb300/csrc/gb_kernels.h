@@ -47,6 +47,8 @@ typedef struct
    const void *sl_v;
    int        sl_v32;    /* FP64 form whose SELL values are held as FP32 (every value exact in FP32) */
    const float *rs;      /* FP16 forms: values are a_ij / a_ii, rs[i] = a_ii (NULL otherwise) */
+   int        tuneT;     /* autotuned block size (0: default 256) */
+   int        tuneD;     /* autotuned SELL prefetch depth (0: default 4) */
 } gb_spmv_desc;
 
 /* runtime */

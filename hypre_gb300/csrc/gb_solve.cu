@@ -154,7 +154,7 @@ __device__ __forceinline__ T block_sum(T v)
 // dotz (optional): per-block partial sums of y_i * z_i written to dpart.
 // ---------------------------------------------------------------------------
 template <int K, typename VT, typename XT>
-__global__ void __launch_bounds__(256) k_spmv_csr(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+__global__ void __launch_bounds__(512) k_spmv_csr(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
                                                   const VT *__restrict__ Av, const XT *__restrict__ x, XT *y,
                                                   int mode, XT alpha, XT beta, const XT *b, const XT *d, XT w,
                                                   const XT *__restrict__ dotz, double *dpart,
@@ -209,9 +209,15 @@ __device__ __forceinline__ int sell_col(const IT *__restrict__ Sj, long long p, 
    else { return __ldg(Sj + p); }
 }
 
-// GS: the two-stage Gauss-Seidel epilogue (mode 6), which also updates b
-template <typename VT, typename XT, bool GS, typename IT>
-__global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const long long *__restrict__ sl_ptr,
+// GS: the two-stage Gauss-Seidel epilogue (mode 6), which also updates b.
+// D: prefetch depth -- the values, column indices and x entries of D
+// consecutive elements are loaded before their products are summed, so each
+// warp keeps D times 32 loads of each stream in flight.  The row's terms are
+// summed in element order into one accumulator whatever D is, so every depth
+// (and block size) gives the same result bit for bit; the autotuner picks D
+// and the block size per matrix shape.
+template <typename VT, typename XT, bool GS, typename IT, int D>
+__global__ void __launch_bounds__(512) k_spmv_sell(int n, int nslices, const long long *__restrict__ sl_ptr,
                                                    const int *__restrict__ sl_w, const IT *__restrict__ Sj,
                                                    const VT *__restrict__ Sv, const XT *__restrict__ x, XT *y,
                                                    int mode, XT alpha, XT beta, const XT *b, const XT *d, XT w,
@@ -225,27 +231,39 @@ __global__ void __launch_bounds__(256) k_spmv_sell(int n, int nslices, const lon
    double dsum = 0.0;
    for (int s = warp; s < nslices; s += nwarps)
    {
-      long long base = __ldg(sl_ptr + s) + t;
-      int width = __ldg(sl_w + s);
+      const long long base = __ldg(sl_ptr + s) + t;
+      const int width = __ldg(sl_w + s);
       const int i = s * 32 + t;
-      AT acc0 = 0, acc1 = 0;
-      int k = 0;
-      for (; k + 1 < width; k += 2)
+      AT acc = 0;
+      for (int k0 = 0; k0 < width; k0 += D)
       {
-         long long p0 = base + (long long) k * 32, p1 = p0 + 32;
-         int j0 = sell_col(Sj, p0, i), j1 = sell_col(Sj, p1, i);
-         VT a0 = __ldg(Sv + p0), a1 = __ldg(Sv + p1);
-         acc0 += Acc<VT, XT>::mul(a0, __ldg(x + j0));
-         acc1 += Acc<VT, XT>::mul(a1, __ldg(x + j1));
-      }
-      if (k < width)
-      {
-         long long p0 = base + (long long) k * 32;
-         acc0 += Acc<VT, XT>::mul(__ldg(Sv + p0), __ldg(x + sell_col(Sj, p0, i)));
+         VT a[D];
+         int j[D];
+#pragma unroll
+         for (int u = 0; u < D; u++)
+         {
+            if (k0 + u < width)
+            {
+               const long long p = base + (long long) (k0 + u) * 32;
+               j[u] = sell_col(Sj, p, i);
+               a[u] = __ldg(Sv + p);
+            }
+         }
+         XT xv[D];
+#pragma unroll
+         for (int u = 0; u < D; u++)
+         {
+            if (k0 + u < width) { xv[u] = __ldg(x + j[u]); }
+         }
+#pragma unroll
+         for (int u = 0; u < D; u++)
+         {
+            if (k0 + u < width) { acc += Acc<VT, XT>::mul(a[u], xv[u]); }
+         }
       }
       if (i < n)
       {
-         XT si = (XT) (acc0 + acc1);
+         XT si = (XT) acc;
          if (rs) { si *= (XT) rs[i]; }
          XT yi = row_epilogue<XT>(mode, si, i, alpha, beta, b, x, d, w, y);
          y[i] = yi;
@@ -430,14 +448,25 @@ template <typename VT, typename XT>
 static void spmv_dispatch(const gb_spmv_desc *A, const XT *x, XT *y, int mode, XT alpha, XT beta, const XT *b,
                           const XT *d, XT w, const XT *dotz, double *dpart, cudaStream_t st)
 {
-   const int T = 256;
+   // block size and SELL prefetch depth: the autotuned choice, else 256 / 4;
+   // the fused dot products (dpart) need the fixed reduction grid and 256
+   const int T = (A->tuneT && !dpart) ? A->tuneT : 256;
    if (A->fmt == GB_FMT_SELL)
    {
       int nsl = A->nslices;
       int blocks = dpart ? GB_RED_BLOCKS : nblk((long long) nsl * 32, T);
+      const int D = A->tuneD ? A->tuneD : 4;
+#define GB_SELL_D(GS, IT, J, DD)                                                                                  \
+   k_spmv_sell<VT, XT, GS, IT, DD><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, J, (const VT *) A->sl_v, x, \
+                                                         y, mode, alpha, beta, b, d, w, dotz, dpart, A->rs)
 #define GB_SELL(GS, IT, J)                                                                                         \
-   k_spmv_sell<VT, XT, GS, IT><<<blocks, T, 0, st>>>(A->n, nsl, A->sl_ptr, A->sl_w, J, (const VT *) A->sl_v, x, y, \
-                                                     mode, alpha, beta, b, d, w, dotz, dpart, A->rs)
+   switch (D)                                                                                                      \
+   {                                                                                                               \
+      case 1: GB_SELL_D(GS, IT, J, 1); break;                                                                      \
+      case 2: GB_SELL_D(GS, IT, J, 2); break;                                                                      \
+      case 8: GB_SELL_D(GS, IT, J, 8); break;                                                                      \
+      default: GB_SELL_D(GS, IT, J, 4); break;                                                                     \
+   }
       if (mode == GB_EPI_GS)
       {
          if (A->sl_j16) { GB_SELL(true, short, A->sl_j16); }
@@ -449,6 +478,7 @@ static void spmv_dispatch(const gb_spmv_desc *A, const XT *x, XT *y, int mode, X
          else { GB_SELL(false, int, A->sl_j); }
       }
 #undef GB_SELL
+#undef GB_SELL_D
    }
    else
    {

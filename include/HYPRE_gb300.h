@@ -375,6 +375,21 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelL1(HYPRE_Solver solver, HYPRE_Int level, 
  * (CUDA events on the library stream around each product) and their count. */
 HYPRE_Int HYPRE_GB300_BoomerAMGGetSpGEMMStats(HYPRE_Solver solver, HYPRE_Real *bytes, HYPRE_Real *seconds,
                                               HYPRE_Int *calls);
+/* SpMV launch-shape autotuner: on (1, the default unless the environment sets
+ * HYPRE_GB300_AUTOTUNE=0) or off (0).  When on, each solve form of at least
+ * 20,000 rows gets the fastest launch shape of its matrix shape, timed once
+ * per machine and kept in a JSON cache ($HYPRE_GB300_TUNE_CACHE, else
+ * $HOME/.cache/hypre_gb300/spmv_tune.json). */
+HYPRE_Int HYPRE_GB300_SetAutotune(HYPRE_Int on);
+/* The launch shape of a matrix's solve form in one value precision (0 FP64,
+ * 1 FP32, 2 FP16): format (0 CSR, 1 SELL-32), block size, and the SELL
+ * prefetch depth or the CSR lanes per row; and setting it by hand (block 0:
+ * 256; depth 0: 4; lanes 0: unchanged).  Every SELL shape gives the same
+ * result bit for bit; CSR lane counts differ in rounding only. */
+HYPRE_Int HYPRE_GB300_ParCSRMatrixGetSpMVShape(HYPRE_ParCSRMatrix A, HYPRE_Int precision, HYPRE_Int *format,
+                                               HYPRE_Int *block, HYPRE_Int *depth_or_lanes);
+HYPRE_Int HYPRE_GB300_ParCSRMatrixSetSpMVShape(HYPRE_ParCSRMatrix A, HYPRE_Int precision, HYPRE_Int block,
+                                               HYPRE_Int depth_or_lanes);
 /* Mean device seconds of the solve-phase SpMV y = A_l x of one level in one
  * value precision (0 FP64, 1 FP32, 2 FP16 values with FP32 vectors) over
  * `reps` back-to-back launches, and its algorithmic bytes per launch. */
