@@ -64,7 +64,10 @@ def parse():
                     help="comma-separated arms to time (profiling runs use fp32_cycle alone)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end IJ arm (profiling runs)")
     ap.add_argument("--spmv-only", action="store_true",
-                    help="only the level-0 FP64 SpMV loop of the roofline measurement (for profiling)")
+                    help="only the level-0 SpMV loop of the roofline measurement (for profiling)")
+    ap.add_argument("--spmv-prec", type=int, default=0, choices=[0, 1, 2],
+                    help="with --spmv-only: 0 the matrix's FP64 form, 1 the FP32 and 2 the FP16-valued level-0 "
+                         "form of a setup with that cycle precision")
     ap.add_argument("--workload", default="laplace27_160",
                     choices=["laplace27_160", "batch512", "multi64", "learned128", "fv256", "spgemm128"],
                     help="laplace27_160: the headline line; the others measure the batched, multi-RHS, "
@@ -163,11 +166,25 @@ def gpu_arm(args):
     L.HYPRE_GB300_ParVectorCopyFromHost(bv, b.ctypes.data, n)
 
     if args.spmv_only:
-        yv = C.c_void_p(); L.HYPRE_ParVectorCreate(0, n, None, C.byref(yv)); L.HYPRE_ParVectorInitialize(yv)
-        for _ in range(args.warmup + args.steps):
-            gb.check(L.HYPRE_ParCSRMatrixMatvec(1.0, A, bv, 0.0, yv), "matvec")
+        if args.spmv_prec == 0:
+            yv = C.c_void_p(); L.HYPRE_ParVectorCreate(0, n, None, C.byref(yv)); L.HYPRE_ParVectorInitialize(yv)
+            for _ in range(args.warmup + args.steps):
+                gb.check(L.HYPRE_ParCSRMatrixMatvec(1.0, A, bv, 0.0, yv), "matvec")
+        else:
+            # level 0's solve form in the cycle precision, after a setup (the
+            # bench's solver settings): warmup + steps back-to-back launches
+            amg = C.c_void_p(); L.HYPRE_BoomerAMGCreate(C.byref(amg))
+            L.HYPRE_BoomerAMGSetStrongThreshold(amg, SOLVER["theta"]); L.HYPRE_BoomerAMGSetMaxRowSum(amg, 1.0)
+            L.HYPRE_BoomerAMGSetAggNumLevels(amg, SOLVER["agg_nl"])
+            L.HYPRE_BoomerAMGSetAggInterpType(amg, SOLVER["agg_interp"])
+            L.HYPRE_BoomerAMGSetRelaxType(amg, SOLVER["relax"])
+            L.HYPRE_GB300_BoomerAMGSetCyclePrecision(amg, args.spmv_prec)
+            gb.check(L.HYPRE_BoomerAMGSetup(amg, A, bv, xv), "setup")
+            sec, byt = C.c_double(), C.c_double()
+            gb.check(L.HYPRE_GB300_BoomerAMGLevelSpMVTime(amg, 0, args.spmv_prec, args.warmup + args.steps,
+                                                            C.byref(sec), C.byref(byt)), "spmv time")
         torch.cuda.synchronize()
-        print(json.dumps({"spmv_only": True, "launches": args.warmup + args.steps}))
+        print(json.dumps({"spmv_only": True, "precision": args.spmv_prec, "launches": args.warmup + args.steps}))
         return
 
     def make_solver(prec):

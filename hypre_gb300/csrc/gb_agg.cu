@@ -505,6 +505,103 @@ extern "C" void gb_mod_extpi_scale(int nf, int nnzff, const int *fl, const int *
    GB_COUNT(2);
 }
 
+// Scalings of the modified extended interpolation (interp_type 16,
+// hypre_BoomerAMGBuildModExtInterpHost src/parcsr_ls/par_mod_lr_interp.c:
+// 229-355): D_q = FC row sum, D_w = A row sum - FF off-diagonals - D_q;
+// FF's diagonal becomes D_q / D_w, its off-diagonals are divided by D_w and
+// FC is scaled by -1 / D_q (1 when a divisor is zero).
+__global__ void k_modext_scale(int nf, const int *__restrict__ fl, const int *__restrict__ Ai,
+                               const double *__restrict__ Av, const int *__restrict__ FFi, double *__restrict__ FFv,
+                               const int *__restrict__ FCi, double *__restrict__ FCv)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   double q = 0.0;
+   for (int k = FCi[r]; k < FCi[r + 1]; k++) { q += FCv[k]; }
+   int i = fl[r];
+   double w = 0.0;
+   for (int k = Ai[i]; k < Ai[i + 1]; k++) { w += Av[k]; }
+   for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { w -= FFv[k]; }
+   w -= q;
+   const double beta = w != 0.0 ? 1.0 / w : 1.0;
+   FFv[FFi[r]] = beta * q;
+   const double gamma = q != 0.0 ? -1.0 / q : 1.0;
+   for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { FFv[k] *= beta; }
+   for (int k = FCi[r]; k < FCi[r + 1]; k++) { FCv[k] *= gamma; }
+}
+
+// Scalings of the modified extended+e interpolation (interp_type 18,
+// hypre_BoomerAMGBuildModExtPEInterpHost src/parcsr_ls/par_mod_lr_interp.c:
+// 1483-1662).  Pass 1 per F row: D_lambda = mean of FF's off-diagonals,
+// D_beta = FC row sum, D_tmp = D_lambda / (D_beta + D_lambda), D_w = A row
+// sum - FF off-diagonals - D_beta.  Pass 2: D_tau = sum FF_ij D_tmp_j,
+// value = -1 / (D_w + D_tau), theta = D_beta + D_lambda; FF's diagonal
+// becomes value * theta, its off-diagonals are scaled by value and FC by
+// 1 / theta.
+__global__ void k_modpe_rows(int nf, const int *__restrict__ fl, const int *__restrict__ Ai,
+                             const double *__restrict__ Av, const int *__restrict__ FFi,
+                             const double *__restrict__ FFv, const int *__restrict__ FCi,
+                             const double *__restrict__ FCv, double *__restrict__ Dl, double *__restrict__ Db,
+                             double *__restrict__ Dt, double *__restrict__ Dw)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   double lambda = 0.0;
+   for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { lambda += FFv[k]; }
+   const double number = (double) (FFi[r + 1] - FFi[r] - 1);
+   if (number != 0.0) { lambda /= number; }
+   double beta = 0.0;
+   for (int k = FCi[r]; k < FCi[r + 1]; k++) { beta += FCv[k]; }
+   Dt[r] = lambda + beta != 0.0 ? lambda / (beta + lambda) : 0.0;
+   int i = fl[r];
+   double w = 0.0;
+   for (int k = Ai[i]; k < Ai[i + 1]; k++) { w += Av[k]; }
+   for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { w -= FFv[k]; }
+   w -= beta;
+   Dl[r] = lambda;
+   Db[r] = beta;
+   Dw[r] = w;
+}
+
+__global__ void k_modpe_scale(int nf, const int *__restrict__ FFi, const int *__restrict__ FFj,
+                              double *__restrict__ FFv, const int *__restrict__ FCi, double *__restrict__ FCv,
+                              const double *__restrict__ Dl, const double *__restrict__ Db,
+                              const double *__restrict__ Dt, const double *__restrict__ Dw)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   double tau = 0.0;
+   for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { tau += FFv[k] * Dt[FFj[k]]; }
+   double value = Dw[r] + tau;
+   if (value != 0.0) { value = -1.0 / value; }
+   double theta = Db[r] + Dl[r];
+   FFv[FFi[r]] = value * theta;
+   if (theta != 0.0) { theta = 1.0 / theta; }
+   for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { FFv[k] *= value; }
+   for (int k = FCi[r]; k < FCi[r + 1]; k++) { FCv[k] *= theta; }
+}
+
+// the row scalings of the modified interpolations 16, 17 and 18 on FF / FC
+// (work: tmp nnz(FF), D1..D4 nf each)
+extern "C" void gb_mod_interp_scale(int variant, int nf, int nnzff, const int *fl, const int *Ai, const double *Av,
+                                    const int *FFi, const int *FFj, double *FFv, const int *FCi, double *FCv,
+                                    double *tmp, double *D1, double *D2, double *D3, double *D4, cudaStream_t s)
+{
+   if (nf <= 0) { return; }
+   if (variant == 16)
+   {
+      k_modext_scale<<<gb_blocks2(nf, 256), 256, 0, s>>>(nf, fl, Ai, Av, FFi, FFv, FCi, FCv);
+      GB_COUNT(1);
+   }
+   else if (variant == 18)
+   {
+      k_modpe_rows<<<gb_blocks2(nf, 256), 256, 0, s>>>(nf, fl, Ai, Av, FFi, FFv, FCi, FCv, D1, D2, D3, D4);
+      k_modpe_scale<<<gb_blocks2(nf, 256), 256, 0, s>>>(nf, FFi, FFj, FFv, FCi, FCv, D1, D2, D3, D4);
+      GB_COUNT(2);
+   }
+   else { gb_mod_extpi_scale(nf, nnzff, fl, Ai, Av, FFi, FFj, FFv, FCi, FCv, tmp, D1, D2, s); }
+}
+
 // P1 = [I; W] in fine order: C points get (f2c[i], 1), F points W's row f2f[i]
 __global__ void k_p1_len(int n, const int *__restrict__ CF, const int *__restrict__ f2f, const int *__restrict__ Wi,
                          int *__restrict__ len)

@@ -721,6 +721,60 @@ static int number_points(int n, const int *CF, int kind, int v, int *out, int **
    return tot;
 }
 
+/* The modified ("MM") interpolations, P = [I; W] with W = As_FF As_FC
+ * (hypre_BoomerAMGBuildModExtInterpHost / ModExtPIInterpHost /
+ * ModExtPEInterpHost, src/parcsr_ls/par_mod_lr_interp.c:16, :585, :1260;
+ * As_FF / As_FC from hypre_ParCSRMatrixGenerateFFFCHost, src/parcsr_mv/
+ * gen_fffc.c:18): variant 16 extended, 17 extended+i, 18 extended+e.  CF:
+ * C points > 0; f2c: coarse numbers of the C points (nc of them).  P is not
+ * truncated here. */
+static int mm_interp(const gb_csr *A, const gb_csr *S, const int *CF, const int *f2c, int nc, int variant,
+                     gb_csr *P)
+{
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   int *f2f = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *fl = NULL;
+   int nf = number_points(n, CF, 2, 0, f2f, &fl);
+   gb_csr FF, FC;
+   FF.nr = FF.nc = nf; FC.nr = nf; FC.nc = nc;
+   int *cff = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   int *cfc = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   gb_fffc_count(nf, fl, A->i, A->j, S->i, S->j, CF, cff, cfc, s);
+   FF.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   FC.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
+   FF.nnz = scan_total(cff, FF.i, nf);
+   FC.nnz = scan_total(cfc, FC.i, nf);
+   FF.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FF.nnz ? FF.nnz : 1));
+   FF.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
+   FC.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FC.nnz ? FC.nnz : 1));
+   FC.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FC.nnz ? FC.nnz : 1));
+   gb_fffc_fill(nf, n, A->nnz, fl, A->i, A->j, A->v, S->i, S->j, CF, f2c, f2f, FF.i, FF.j, FF.v, FC.i, FC.j, FC.v,
+                s);
+   {
+      double *tmp = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
+      size_t nb = sizeof(double) * (size_t) (nf ? nf : 1);
+      double *D1 = (double *) gb_dmalloc(nb), *D2 = (double *) gb_dmalloc(nb);
+      double *D3 = (double *) gb_dmalloc(nb), *D4 = (double *) gb_dmalloc(nb);
+      gb_mod_interp_scale(variant, nf, FF.nnz, fl, A->i, A->v, FF.i, FF.j, FF.v, FC.i, FC.v, tmp, D1, D2, D3, D4, s);
+      gb_dfree(tmp); gb_dfree(D1); gb_dfree(D2); gb_dfree(D3); gb_dfree(D4);
+   }
+   gb_csr W;
+   if (spgemm_host(&FF, &FC, nf == nc, &W)) { return -1; }
+   gb_csr_free(&FF); gb_csr_free(&FC);
+   P->nr = n; P->nc = nc;
+   int *len = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_p1_len(n, CF, f2f, W.i, len, s);
+   P->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   P->nnz = scan_total(len, P->i, n);
+   P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
+   P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
+   gb_p1_fill(n, CF, f2c, f2f, W.i, W.j, W.v, P->i, P->j, P->v, s);
+   gb_csr_free(&W);
+   gb_dfree(f2f); gb_dfree(fl); gb_dfree(cff); gb_dfree(cfc); gb_dfree(len);
+   return 0;
+}
+
 /* aggressive level (par_amg_setup.c:1311-1358, :1778-1915, agg_interp_type 6):
  * second-order strength, PMIS on it, P = P1 P2 with P1 modified extended+i
  * and P2 partial extended+i.  Returns the number of coarse points. */
@@ -809,44 +863,8 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    }
    gb_csr_free(&S2);
    /* P1: modified extended+i (par_mod_lr_interp.c:585) */
-   int *f2f = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   int *fl = NULL;
-   int nf = number_points(n, CF, 2, 0, f2f, &fl);
-   gb_csr FF, FC;
-   FF.nr = FF.nc = nf; FC.nr = nf; FC.nc = nc1;
-   int *cff = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
-   int *cfc = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
-   gb_fffc_count(nf, fl, A->i, A->j, S->i, S->j, CF, cff, cfc, s);
-   FF.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
-   FC.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nf + 1));
-   FF.nnz = scan_total(cff, FF.i, nf);
-   FC.nnz = scan_total(cfc, FC.i, nf);
-   FF.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FF.nnz ? FF.nnz : 1));
-   FF.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
-   FC.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FC.nnz ? FC.nnz : 1));
-   FC.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FC.nnz ? FC.nnz : 1));
-   gb_fffc_fill(nf, n, A->nnz, fl, A->i, A->j, A->v, S->i, S->j, CF, f2c1, f2f, FF.i, FF.j, FF.v, FC.i, FC.j, FC.v,
-                s);
-   {
-      double *tmp = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF.nnz ? FF.nnz : 1));
-      double *Dq = (double *) gb_dmalloc(sizeof(double) * (size_t) (nf ? nf : 1));
-      double *Dw = (double *) gb_dmalloc(sizeof(double) * (size_t) (nf ? nf : 1));
-      gb_mod_extpi_scale(nf, FF.nnz, fl, A->i, A->v, FF.i, FF.j, FF.v, FC.i, FC.v, tmp, Dq, Dw, s);
-      gb_dfree(tmp); gb_dfree(Dq); gb_dfree(Dw);
-   }
-   gb_csr W;
-   if (spgemm_host(&FF, &FC, nf == nc1, &W)) { return -1; }
-   gb_csr_free(&FF); gb_csr_free(&FC);
    gb_csr P1;
-   P1.nr = n; P1.nc = nc1;
-   int *len = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   gb_p1_len(n, CF, f2f, W.i, len, s);
-   P1.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
-   P1.nnz = scan_total(len, P1.i, n);
-   P1.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P1.nnz ? P1.nnz : 1));
-   P1.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P1.nnz ? P1.nnz : 1));
-   gb_p1_fill(n, CF, f2c1, f2f, W.i, W.j, W.v, P1.i, P1.j, P1.v, s);
-   gb_csr_free(&W);
+   if (mm_interp(A, S, CF, f2c1, nc1, 17, &P1)) { return -1; }
    truncate_host(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
    /* CF correction (par_strength.c:3096) and P2: partial extended+i over the
     * old C points (partial.c:16) */
@@ -860,8 +878,7 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    if (spgemm_host(&P1, &P2, n == nc2, P)) { return -1; }
    truncate_host(P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
    gb_csr_free(&P1); gb_csr_free(&P2);
-   gb_dfree(f2c1); gb_dfree(c2f1); gb_dfree(f2f); gb_dfree(fl); gb_dfree(f2c2); gb_dfree(cnt); gb_dfree(CFN);
-   gb_dfree(cff); gb_dfree(cfc); gb_dfree(len);
+   gb_dfree(f2c1); gb_dfree(c2f1); gb_dfree(f2c2); gb_dfree(cnt); gb_dfree(CFN);
    return nc2;
 }
 
@@ -924,9 +941,13 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
          gb_dfree(cnt); gb_dfree(f2c); gb_dfree(CF); gb_csr_free(&S);
          return 0;
       }
-      /* 4. extended+i interpolation (par_lr_interp.c:1024) and truncation */
-      if (extpi_host(A, &S, CF, f2c, n, NULL, nc, &P)) { return -1; }
-      gb_sf_to_f(n, CF, s);
+      /* 4. extended+i interpolation (par_lr_interp.c:1024) or a modified
+       * (MM) interpolation (16/17/18), then truncation */
+      if (prm->interp_type == 6) { if (extpi_host(A, &S, CF, f2c, n, NULL, nc, &P)) { return -1; } }
+      else if (mm_interp(A, &S, CF, f2c, nc, prm->interp_type, &P)) { return -1; }
+      /* ext+i turns the points without strong couplings (-3) into F points
+       * (par_lr_interp.c:1887-1893); the modified interpolations keep -3 */
+      if (prm->interp_type == 6) { gb_sf_to_f(n, CF, s); }
       truncate_host(&P, prm->trunc_factor, prm->p_max_elmts);
       gb_dfree(f2c);
    }
@@ -1915,7 +1936,12 @@ HYPRE_Int HYPRE_BoomerAMGSetInterpType(HYPRE_Solver solver, HYPRE_Int v)
 {
    gb_amg *a = amg_of(solver, 1);
    if (!a) { return gb_error_flag; }
-   if (v != 6) { gb_error(HYPRE_ERROR_GENERIC, "interp_type: only extended+i (6) is supported"); gb_error_in_arg(2); return gb_error_flag; }
+   if (v != 6 && v != 16 && v != 17 && v != 18)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "interp_type: extended+i (6) and the modified 16, 17, 18 are supported");
+      gb_error_in_arg(2);
+      return gb_error_flag;
+   }
    a->prm.interp_type = v;
    return gb_error_flag;
 }

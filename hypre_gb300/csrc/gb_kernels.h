@@ -142,6 +142,9 @@ void gb_fffc_fill(int nf, int nrows, long long nnz, const int *fl, const int *Ai
 void gb_mod_extpi_scale(int nf, int nnzff, const int *fl, const int *Ai, const double *Av, const int *FFi,
                         const int *FFj, double *FFv, const int *FCi, const double *FCv, double *tmp, double *Dq,
                         double *Dw, cudaStream_t s);
+void gb_mod_interp_scale(int variant, int nf, int nnzff, const int *fl, const int *Ai, const double *Av,
+                         const int *FFi, const int *FFj, double *FFv, const int *FCi, double *FCv, double *tmp,
+                         double *D1, double *D2, double *D3, double *D4, cudaStream_t s);
 void gb_p1_len(int n, const int *CF, const int *f2f, const int *Wi, int *len, cudaStream_t s);
 void gb_p1_fill(int n, const int *CF, const int *f2c, const int *f2f, const int *Wi, const int *Wj, const double *Wv,
                 const int *Pi, int *Pj, double *Pv, cudaStream_t s);

@@ -810,7 +810,19 @@ void or_correct_cf2(int n, int *CF, const int *CFN)
  * hypre_ParCSRMatrixGenerateFFFCHost src/parcsr_mv/gen_fffc.c:18-530:
  * As_FF / As_FC are A restricted to strong connections (FF with the diagonal
  * first), W = As_FF As_FC after the D_q, D_w, D_theta scaling, P = [I; W]. */
+static int mod_interp(const or_csr *A, const or_csr *S, const int *CF, int variant, or_csr *P);
+
 int or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P)
+{
+   return mod_interp(A, S, CF, 17, P);
+}
+
+/* The modified ("MM") interpolations (hypre_BoomerAMGBuildModExtInterpHost
+ * :16-540, ModExtPIInterpHost :585-1215, ModExtPEInterpHost :1260-1855 of
+ * src/parcsr_ls/par_mod_lr_interp.c): variant 16 extended, 17 extended+i,
+ * 18 extended+e.  They share As_FF / As_FC, W = As_FF As_FC and P = [I; W];
+ * they differ in the row scalings applied before the product. */
+static int mod_interp(const or_csr *A, const or_csr *S, const int *CF, int variant, or_csr *P)
 {
    int n = A->nr;
    int *f2c = xmalloc(sizeof(int) * (n ? n : 1)), *f2f = xmalloc(sizeof(int) * (n ? n : 1));
@@ -850,6 +862,63 @@ int or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr 
    }
    double *Dq = xcalloc(nf, sizeof(double)), *Dw = xcalloc(nf, sizeof(double)), *Dt = xcalloc(nf, sizeof(double));
    double *tmp = xmalloc(sizeof(double) * (FFi[nf] ? FFi[nf] : 1));
+   if (variant == 16 || variant == 18)
+   {
+      /* D_w = A row sum - FF off-diagonals - FC row sum (:240-310, :1570-1627) */
+      double *Dl = xcalloc(nf, sizeof(double)), *Dx = xcalloc(nf, sizeof(double));
+      for (int r = 0; r < nf; r++)
+      {
+         if (variant == 18)
+         {
+            for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { Dl[r] += FFv[k]; }
+            double number = (double) (FFi[r + 1] - FFi[r] - 1);
+            if (number != 0.0) { Dl[r] /= number; }
+         }
+         for (int k = FCi[r]; k < FCi[r + 1]; k++) { Dq[r] += FCv[k]; }
+         if (variant == 18 && Dl[r] + Dq[r] != 0.0) { Dx[r] = Dl[r] / (Dq[r] + Dl[r]); }
+      }
+      row = 0;
+      for (int i = 0; i < n; i++)
+      {
+         if (CF[i] > 0) { continue; }
+         for (int k = A->i[i]; k < A->i[i + 1]; k++) { Dw[row] += A->v[k]; }
+         for (int k = FFi[row] + 1; k < FFi[row + 1]; k++) { Dw[row] -= FFv[k]; }
+         Dw[row] -= Dq[row];
+         row++;
+      }
+      for (int r = 0; r < nf; r++)
+      {
+         if (variant == 16)
+         {
+            /* :316-354 */
+            double beta = Dw[r] != 0.0 ? 1.0 / Dw[r] : 1.0;
+            FFv[FFi[r]] = beta * Dq[r];
+            double gamma = Dq[r] != 0.0 ? -1.0 / Dq[r] : 1.0;
+            for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { FFv[k] *= beta; }
+            for (int k = FCi[r]; k < FCi[r + 1]; k++) { FCv[k] *= gamma; }
+         }
+         else
+         {
+            /* D_tau and the scalings, :1629-1662 */
+            for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { Dt[r] += FFv[k] * Dx[FFj[k]]; }
+         }
+      }
+      if (variant == 18)
+      {
+         for (int r = 0; r < nf; r++)
+         {
+            double value = Dw[r] + Dt[r];
+            if (value != 0.0) { value = -1.0 / value; }
+            double theta = Dq[r] + Dl[r];
+            FFv[FFi[r]] = value * theta;
+            if (theta != 0.0) { theta = 1.0 / theta; }
+            for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { FFv[k] *= value; }
+            for (int k = FCi[r]; k < FCi[r + 1]; k++) { FCv[k] *= theta; }
+         }
+      }
+      free(Dl); free(Dx);
+      goto product;
+   }
    for (int r = 0; r < nf; r++) { for (int k = FCi[r]; k < FCi[r + 1]; k++) { Dq[r] += FCv[k]; } }
    memcpy(tmp, FFv, sizeof(double) * FFi[nf]);
    row = 0;
@@ -891,6 +960,7 @@ int or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr 
          for (int j = FFi[r]; j < FFi[r + 1]; j++) { FFv[j] *= theta; }
       }
    }
+product:;
    or_csr FF = { nf, nf, FFi, FFj, FFv }, FC = { nf, nc, FCi, FCj, FCv }, W;
    or_matmul(&FF, &FC, &W);
    /* P = [I; W] in fine order */
@@ -1603,7 +1673,8 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
             or_csr_free(&S); free(CF);
             break;
          }
-         or_extpi_interp(A, &S, CF, &P);
+         if (prm->interp_type == 6) { or_extpi_interp(A, &S, CF, &P); }
+         else { mod_interp(A, &S, CF, prm->interp_type, &P); }   /* 16, 17, 18 */
          or_truncate(&P, prm->trunc_factor, prm->p_max_elmts);
       }
       or_csr Ac;

@@ -68,13 +68,24 @@ CASES = {
                                     rlx=4, coarse_th=9, solver=61, k=30, full=True),
     "lap27_30_hgs13_14_pcg": dict(kind=27, n=(30, 30, 30), th=0.5, mxrs=1.0, Pmx=4, rlx=13, rlx_down=13, rlx_up=14,
                                   coarse_th=9, solver=1, full=False),
+    # the modified ("MM") interpolations: 16 extended, 17 extended+i, 18 extended+e
+    "lap7_14_mm16_pcg": dict(kind=7, n=(14, 14, 14), th=0.25, mxrs=1.0, Pmx=4, interptype=16, rlx=18, coarse_th=9,
+                             solver=1, full=True),
+    "lap27_12_mm17_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, interptype=17, rlx=18, coarse_th=9,
+                              solver=1, full=True),
+    "lap7_16_mm18_pcg": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, interptype=18, rlx=18, coarse_th=9,
+                             solver=1, full=True),
+    "lap27_14_mm18_tr_pcg": dict(kind=27, n=(14, 14, 14), th=0.25, mxrs=0.9, Pmx=3, tr=0.1, interptype=18, rlx=18,
+                                 coarse_th=9, solver=1, full=True),
+    "lap27_30_mm18_pcg": dict(kind=27, n=(30, 30, 30), th=0.5, mxrs=1.0, Pmx=4, interptype=18, rlx=13, rlx_down=13,
+                              rlx_up=14, coarse_th=9, solver=1, full=False),
 }
 
 
 def dump_args(c, out):
     a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "agg_nl", "agg_interp", "rlx", "rlx_down", "rlx_up", "w", "coarse_th",
-                "solver", "k", "cheby_order"):
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "rlx", "rlx_down", "rlx_up", "w",
+                "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]
     return a + ["-tol", "1e-8", "-rlx_coarse", "9", "-o", out]

@@ -34,7 +34,7 @@ def oracle_params(c):
              trunc_factor=c.get("tr", 0.0), agg_num_levels=c.get("agg_nl", 0),
              agg_interp_type=c.get("agg_interp", 4), relax_down=c.get("rlx_down", c["rlx"]),
              relax_up=c.get("rlx_up", c["rlx"]), relax_coarse=9, max_coarse_size=c["coarse_th"],
-             relax_weight=c.get("w", 1.0))
+             relax_weight=c.get("w", 1.0), interp_type=c.get("interptype", 6))
     if "cheby_order" in c:
         p["cheby_order"] = c["cheby_order"]
     return p
@@ -44,7 +44,7 @@ def amg_params(c):
     """HYPRE_BoomerAMGSet* values of a golden case."""
     p = dict(StrongThreshold=c["th"], MaxRowSum=c["mxrs"], PMaxElmts=c["Pmx"], TruncFactor=c.get("tr", 0.0),
              AggNumLevels=c.get("agg_nl", 0), RelaxType=c["rlx"], MaxCoarseSize=c["coarse_th"],
-             RelaxWt=c.get("w", 1.0))
+             RelaxWt=c.get("w", 1.0), InterpType=c.get("interptype", 6))
     cyc = [(c[k], part) for k, part in (("rlx_down", 1), ("rlx_up", 2)) if k in c]
     if cyc:
         p["CycleRelaxType"] = cyc
