@@ -721,6 +721,30 @@ static int number_points(int n, const int *CF, int kind, int v, int *out, int **
    return tot;
 }
 
+/* direct interpolation (interp_type 3, par_interp.c:1873); not truncated here */
+static int dir_interp(const gb_csr *A, const gb_csr *S, const int *CF, const int *f2c, int nc, gb_csr *P)
+{
+   cudaStream_t s = gb_stream();
+   int n = A->nr;
+   int *cnt = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   gb_dir_count(n, S->i, S->j, CF, cnt, s);
+   P->nr = n; P->nc = nc;
+   P->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   P->nnz = scan_total(cnt, P->i, n);
+   P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
+   P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
+   size_t nb = sizeof(double) * (size_t) (n ? n : 1);
+   double *alfa = (double *) gb_dmalloc(nb), *beta = (double *) gb_dmalloc(nb);
+   if (!cnt || !P->i || !P->j || !P->v || !alfa || !beta)
+   {
+      gb_dfree(cnt); gb_dfree(alfa); gb_dfree(beta);
+      return -1;
+   }
+   gb_dir_fill(n, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, alfa, beta, cnt, s);
+   gb_dfree(cnt); gb_dfree(alfa); gb_dfree(beta);
+   return 0;
+}
+
 /* The modified ("MM") interpolations, P = [I; W] with W = As_FF As_FC
  * (hypre_BoomerAMGBuildModExtInterpHost / ModExtPIInterpHost /
  * ModExtPEInterpHost, src/parcsr_ls/par_mod_lr_interp.c:16, :585, :1260;
@@ -944,10 +968,12 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
       /* 4. extended+i interpolation (par_lr_interp.c:1024) or a modified
        * (MM) interpolation (16/17/18), then truncation */
       if (prm->interp_type == 6) { if (extpi_host(A, &S, CF, f2c, n, NULL, nc, &P)) { return -1; } }
+      else if (prm->interp_type == 3) { if (dir_interp(A, &S, CF, f2c, nc, &P)) { return -1; } }
       else if (mm_interp(A, &S, CF, f2c, nc, prm->interp_type, &P)) { return -1; }
-      /* ext+i turns the points without strong couplings (-3) into F points
-       * (par_lr_interp.c:1887-1893); the modified interpolations keep -3 */
-      if (prm->interp_type == 6) { gb_sf_to_f(n, CF, s); }
+      /* ext+i and direct interpolation turn the points without strong
+       * couplings (-3) into F points (par_lr_interp.c:1887-1893,
+       * par_interp.c:2560-2563); the modified interpolations keep -3 */
+      if (prm->interp_type == 6 || prm->interp_type == 3) { gb_sf_to_f(n, CF, s); }
       truncate_host(&P, prm->trunc_factor, prm->p_max_elmts);
       gb_dfree(f2c);
    }
@@ -1936,9 +1962,9 @@ HYPRE_Int HYPRE_BoomerAMGSetInterpType(HYPRE_Solver solver, HYPRE_Int v)
 {
    gb_amg *a = amg_of(solver, 1);
    if (!a) { return gb_error_flag; }
-   if (v != 6 && v != 16 && v != 17 && v != 18)
+   if (v != 6 && v != 3 && v != 16 && v != 17 && v != 18)
    {
-      gb_error(HYPRE_ERROR_GENERIC, "interp_type: extended+i (6) and the modified 16, 17, 18 are supported");
+      gb_error(HYPRE_ERROR_GENERIC, "interp_type: extended+i (6), direct (3) and the modified 16, 17, 18 are supported");
       gb_error_in_arg(2);
       return gb_error_flag;
    }

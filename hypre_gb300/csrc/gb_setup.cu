@@ -906,6 +906,114 @@ __global__ void k_iota(int n, int *__restrict__ out, int *__restrict__ count)
    if (i == 0) { *count = n; }
 }
 
+// ---------------------------------------------------------------------------
+// Direct interpolation (interp_type 3, hypre_BoomerAMGBuildDirInterpHost
+// src/parcsr_ls/par_interp.c:1873-2575, one process).  Count: C rows 1, F
+// rows the C points of their S row.  Fill (thread per row): F row i takes
+// those C points in S order with weight sum a_ij over A's row; alfa =
+// (negative off-diagonal sum) / (negative C-point sum) / a_ii and beta the
+// same for the positive ones, kept per row with a flag when defined.  Scale:
+// the reference keeps alfa and beta from the previous row that defined them
+// (starting from 1), so a row without one looks back for it.
+// ---------------------------------------------------------------------------
+__global__ void k_dir_count(int n, const int *__restrict__ Si, const int *__restrict__ Sj, const int *__restrict__ CF,
+                            int *__restrict__ cnt)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int c = 0;
+   if (CF[i] >= 0) { c = 1; }
+   else { for (int k = Si[i]; k < Si[i + 1]; k++) { c += CF[Sj[k]] > 0; } }
+   cnt[i] = c;
+}
+
+__global__ void k_dir_fill(int n, const int *__restrict__ Ai, const int *__restrict__ Aj,
+                           const double *__restrict__ Av, const int *__restrict__ Si, const int *__restrict__ Sj,
+                           const int *__restrict__ CF, const int *__restrict__ f2c, const int *__restrict__ Pi,
+                           int *__restrict__ Pj, double *__restrict__ Pv, double *__restrict__ alfa,
+                           double *__restrict__ beta, int *__restrict__ flags)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   const int jb = Pi[i];
+   if (CF[i] >= 0)
+   {
+      Pj[jb] = f2c[i];
+      Pv[jb] = 1.0;
+      flags[i] = 0;
+      return;
+   }
+   int c = jb;
+   for (int k = Si[i]; k < Si[i + 1]; k++)
+   {
+      const int i1 = Sj[k];
+      if (CF[i1] >= 0) { Pj[c] = f2c[i1]; Pv[c] = 0.0; c++; }
+   }
+   const double diagonal = Av[Ai[i]];
+   double sNp = 0.0, sNn = 0.0, sPp = 0.0, sPn = 0.0;
+   for (int jj = Ai[i] + 1; jj < Ai[i + 1]; jj++)
+   {
+      const int i1 = Aj[jj];
+      const double a = Av[jj];
+      if (a > 0) { sNp += a; } else { sNn += a; }
+      // position of i1 among the row's strong C points (S order)
+      int pos = -1, q = jb;
+      for (int k = Si[i]; k < Si[i + 1] && pos < 0; k++)
+      {
+         const int j1 = Sj[k];
+         if (CF[j1] >= 0)
+         {
+            if (j1 == i1) { pos = q; }
+            q++;
+         }
+      }
+      if (pos >= 0)
+      {
+         Pv[pos] += a;
+         if (a > 0) { sPp += a; } else { sPn += a; }
+      }
+   }
+   int fl = 0;
+   if (sPn != 0.0) { alfa[i] = sNn / sPn / diagonal; fl |= 1; }
+   if (sPp != 0.0) { beta[i] = sNp / sPp / diagonal; fl |= 2; }
+   flags[i] = fl;
+}
+
+__global__ void k_dir_scale(int n, const int *__restrict__ CF, const int *__restrict__ Pi, double *__restrict__ Pv,
+                            const double *__restrict__ alfa, const double *__restrict__ beta,
+                            const int *__restrict__ flags)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n || CF[i] >= 0) { return; }
+   double a = 1.0, b = 1.0;
+   int k = i;
+   while (k >= 0 && !(flags[k] & 1)) { k--; }
+   if (k >= 0) { a = alfa[k]; }
+   k = i;
+   while (k >= 0 && !(flags[k] & 2)) { k--; }
+   if (k >= 0) { b = beta[k]; }
+   for (int jj = Pi[i]; jj < Pi[i + 1]; jj++)
+   {
+      if (Pv[jj] > 0) { Pv[jj] *= -b; }
+      else { Pv[jj] *= -a; }
+   }
+}
+
+extern "C" void gb_dir_count(int n, const int *Si, const int *Sj, const int *CF, int *cnt, cudaStream_t s)
+{
+   k_dir_count<<<gb_blocks(n, 256), 256, 0, s>>>(n, Si, Sj, CF, cnt);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_dir_fill(int n, const int *Ai, const int *Aj, const double *Av, const int *Si, const int *Sj,
+                            const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv, double *alfa,
+                            double *beta, int *flags, cudaStream_t s)
+{
+   k_dir_fill<<<gb_blocks(n, 128), 128, 0, s>>>(n, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv, alfa, beta, flags);
+   k_dir_scale<<<gb_blocks(n, 256), 256, 0, s>>>(n, CF, Pi, Pv, alfa, beta, flags);
+   GB_COUNT(2);
+}
+
 /* number of empty rows (row pointer steps of zero), added into *count */
 __global__ void k_count_empty_rows(int n, const int *__restrict__ Ai, int *__restrict__ count)
 {

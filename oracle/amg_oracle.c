@@ -315,6 +315,76 @@ int or_coarse_count(int n, const int *CF)
 }
 
 /* ------------------------------------------------------------------------ */
+/* Direct interpolation (interp_type 3), hypre_BoomerAMGBuildDirInterpHost   */
+/* src/parcsr_ls/par_interp.c:1873-2575 (one process, one thread)           */
+/* ------------------------------------------------------------------------ */
+
+/* F point i interpolates from the C points of its S row (S order); weight
+ * a_ij summed per column, then scaled by -alfa (weights <= 0) or -beta
+ * (> 0) with alfa = sum of negative off-diagonals / sum of negative C-point
+ * couplings / a_ii and beta likewise for the positive ones (:2362-2455).
+ * alfa and beta start at 1 once and keep the last value set: a row whose
+ * C-point couplings have no negative (positive) entry reuses the previous
+ * row's alfa (beta) (:2240-2245, :2445-2446).  Points with CF -3 become F
+ * afterwards (:2560-2563). */
+int or_dir_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
+{
+   int n = A->nr;
+   int *f2c = xmalloc(sizeof(int) * (n ? n : 1));
+   int nc = 0;
+   for (int i = 0; i < n; i++) { f2c[i] = CF[i] >= 0 ? nc++ : -1; }
+   int *Pi = xcalloc(n + 1, sizeof(int));
+   for (int i = 0; i < n; i++)
+   {
+      int c = 0;
+      if (CF[i] >= 0) { c = 1; }
+      else { for (int k = S->i[i]; k < S->i[i + 1]; k++) { if (CF[S->j[k]] > 0) { c++; } } }
+      Pi[i + 1] = Pi[i] + c;
+   }
+   int *Pj = xmalloc(sizeof(int) * (Pi[n] ? Pi[n] : 1));
+   double *Pv = xmalloc(sizeof(double) * (Pi[n] ? Pi[n] : 1));
+   int *mark = xmalloc(sizeof(int) * (n ? n : 1));
+   for (int i = 0; i < n; i++) { mark[i] = -1; }
+   double alfa = 1.0, beta = 1.0;
+   for (int i = 0; i < n; i++)
+   {
+      int c = Pi[i];
+      if (CF[i] >= 0) { Pj[c] = f2c[i]; Pv[c] = 1.0; continue; }
+      const int jb = c;
+      for (int k = S->i[i]; k < S->i[i + 1]; k++)
+      {
+         int i1 = S->j[k];
+         if (CF[i1] >= 0) { mark[i1] = c; Pj[c] = f2c[i1]; Pv[c] = 0.0; c++; }
+      }
+      const int je = c;
+      double diagonal = A->v[A->i[i]];
+      double sNp = 0, sNn = 0, sPp = 0, sPn = 0;
+      for (int jj = A->i[i] + 1; jj < A->i[i + 1]; jj++)
+      {
+         int i1 = A->j[jj];
+         double a = A->v[jj];
+         if (a > 0) { sNp += a; } else { sNn += a; }
+         if (mark[i1] >= jb)
+         {
+            Pv[mark[i1]] += a;
+            if (a > 0) { sPp += a; } else { sPn += a; }
+         }
+      }
+      if (sPn != 0.0) { alfa = sNn / sPn / diagonal; }
+      if (sPp != 0.0) { beta = sNp / sPp / diagonal; }
+      for (int jj = jb; jj < je; jj++)
+      {
+         if (Pv[jj] > 0) { Pv[jj] *= -beta; }
+         else { Pv[jj] *= -alfa; }
+      }
+   }
+   for (int i = 0; i < n; i++) { if (CF[i] == SF_PT) { CF[i] = F_PT; } }
+   P->nr = n; P->nc = nc; P->i = Pi; P->j = Pj; P->v = Pv;
+   free(f2c); free(mark);
+   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Extended+i interpolation, hypre_BoomerAMGBuildExtPIInterpHost             */
 /* src/parcsr_ls/par_lr_interp.c:1024-1924 (one process, offd empty)        */
 /* ------------------------------------------------------------------------ */
@@ -1674,6 +1744,7 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
             break;
          }
          if (prm->interp_type == 6) { or_extpi_interp(A, &S, CF, &P); }
+         else if (prm->interp_type == 3) { or_dir_interp(A, &S, CF, &P); }
          else { mod_interp(A, &S, CF, prm->interp_type, &P); }   /* 16, 17, 18 */
          or_truncate(&P, prm->trunc_factor, prm->p_max_elmts);
       }

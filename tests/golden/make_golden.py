@@ -32,7 +32,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 DUMP = os.path.join(ROOT, "oracle", "_ref", os.uname().machine, "amg_ref_dump")
 sys.path.insert(0, ROOT)
 
-from oracle import oracle as O  # noqa: E402  (only read_records)
+from oracle import oracle as O  # noqa: E402  (read_records, stencils)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 # name -> settings (the keys map one to one onto amg_ref_dump's options)
 CASES = {
@@ -79,11 +80,32 @@ CASES = {
                                  coarse_th=9, solver=1, full=True),
     "lap27_30_mm18_pcg": dict(kind=27, n=(30, 30, 30), th=0.5, mxrs=1.0, Pmx=4, interptype=18, rlx=13, rlx_down=13,
                               rlx_up=14, coarse_th=9, solver=1, full=False),
+    # direct interpolation (3), also on jumping coefficients and anisotropy
+    "lap7_16_dir3_pcg": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, interptype=3, rlx=18, coarse_th=9,
+                             solver=1, full=True),
+    "lap27_12_dir3_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, interptype=3, rlx=18, coarse_th=9,
+                              solver=1, full=True),
+    "fv_12_dir3_pcg": dict(gen="fv", n=(12,), seed=3, th=0.25, mxrs=0.9, Pmx=4, interptype=3, rlx=18, coarse_th=9,
+                           solver=1, full=True),
+    "aniso_40_dir3_tr_pcg": dict(gen="aniso", n=(40,), eps=0.001, th=0.25, mxrs=0.9, Pmx=3, tr=0.1, interptype=3,
+                                 rlx=18, coarse_th=9, solver=1, full=True),
+    "fv_12_mm18_pcg": dict(gen="fv", n=(12,), seed=4, th=0.25, mxrs=0.9, Pmx=4, interptype=18, rlx=18, coarse_th=9,
+                           solver=1, full=True),
 }
 
 
 def dump_args(c, out):
-    a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
+    if "gen" in c:
+        import golden_cases as GC
+        I, J, V = GC.matrix(c, O)
+        mat = out + ".csr"
+        with open(mat, "wb") as f:
+            np.array([len(I) - 1, len(J)], np.int32).tofile(f)
+            np.asarray(I, np.int32).tofile(f); np.asarray(J, np.int32).tofile(f)
+            np.asarray(V, np.float64).tofile(f)
+        a = [DUMP, "-mat", mat]
+    else:
+        a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
     for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "rlx", "rlx_down", "rlx_up", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:

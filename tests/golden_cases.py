@@ -28,6 +28,19 @@ def load(name):
     return d
 
 
+def matrix(c, O):
+    """The case's matrix (I, J, V): the reference generators' stencils, or a
+    seeded project generator ("gen": "fv" finite-volume diffusion on n^3
+    cells, "aniso" 2-D anisotropic 5-point with eps) written to the
+    reference driver as a CSR file."""
+    if "gen" not in c:
+        return O.stencil(c["kind"], *c["n"])
+    from hypre_gb300 import problems as P
+    if c["gen"] == "fv":
+        return P.fv_diffusion(c["n"][0], seed=c.get("seed", 0))
+    return P.aniso2d(c["n"][0], c["eps"])
+
+
 def oracle_params(c):
     """or_amg_params keyword arguments of a golden case."""
     p = dict(strong_threshold=c["th"], max_row_sum=c["mxrs"], p_max_elmts=c["Pmx"],
