@@ -612,11 +612,15 @@ HYPRE_Int HYPRE_ParCSRMatrixMatmat(HYPRE_ParCSRMatrix A, HYPRE_ParCSRMatrix B, H
    return gb_error_flag;
 }
 
-/* extended+i rows for fine points rows[r] (all points when rows == NULL).
+/* extended+i rows for fine points rows[r] (all points when rows == NULL);
+ * iterm 0 gives the extended interpolation (interp_type 14,
+ * hypre_BoomerAMGBuildExtInterpHost src/parcsr_ls/par_lr_interp.c:4777),
+ * whose distribution leaves the point itself out of the sums and of the
+ * diagonal (par_lr_interp.c:5279-5325 against :1649-1700).
  * Tier 0: one thread per row (rows with <= 64 candidates); tier 1: one warp
  * per row with shared-memory tables; tier 2: global-memory tables. */
 static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int *f2c, int nrows, const int *rows,
-                      int ncols, gb_csr *P)
+                      int ncols, int iterm, gb_csr *P)
 {
    cudaStream_t s = gb_stream();
    int n = A->nr;
@@ -667,18 +671,18 @@ static int extpi_host(const gb_csr *A, const gb_csr *S, const int *CF, const int
    P->nnz = scan_total(cnt, P->i, nrows);
    P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
    P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
-   if (use_thread) { gb_extpi_fill_t(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, s); }
+   if (use_thread) { gb_extpi_fill_t(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, iterm, s); }
    if (h1 > 0)
    {
       if (!g_global_only)
       {
          gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, l1, n1, h1, NULL, 0, 0,
-                       t.err, 1, s);
+                       t.err, 1, iterm, s);
       }
       if (t.h_ovf > 0)
       {
          gb_extpi_fill(nrows, rows, A->i, A->j, A->v, S->i, S->j, CF, f2c, P->i, P->j, P->v, t.ovf_list, t.ovf_n,
-                       t.h_ovf, t.gtab, t.gcap, t.gwarps, t.err, 2, s);
+                       t.h_ovf, t.gtab, t.gcap, t.gwarps, t.err, 2, iterm, s);
       }
    }
    int e = tier_end(&t);
@@ -896,7 +900,7 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    int *f2c2 = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    int nc2 = number_points(n, CF, 1, 1, f2c2, NULL);
    gb_csr P2;
-   if (extpi_host(A, S, CF, f2c2, nc1, c2f1, nc2, &P2)) { return -1; }
+   if (extpi_host(A, S, CF, f2c2, nc1, c2f1, nc2, 1, &P2)) { return -1; }
    gb_cf_clamp(n, CF, s);
    truncate_host(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
    if (spgemm_host(&P1, &P2, n == nc2, P)) { return -1; }
@@ -967,13 +971,16 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
       }
       /* 4. extended+i interpolation (par_lr_interp.c:1024) or a modified
        * (MM) interpolation (16/17/18), then truncation */
-      if (prm->interp_type == 6) { if (extpi_host(A, &S, CF, f2c, n, NULL, nc, &P)) { return -1; } }
+      if (prm->interp_type == 6 || prm->interp_type == 14)
+      {
+         if (extpi_host(A, &S, CF, f2c, n, NULL, nc, prm->interp_type == 6, &P)) { return -1; }
+      }
       else if (prm->interp_type == 3) { if (dir_interp(A, &S, CF, f2c, nc, &P)) { return -1; } }
       else if (mm_interp(A, &S, CF, f2c, nc, prm->interp_type, &P)) { return -1; }
-      /* ext+i and direct interpolation turn the points without strong
-       * couplings (-3) into F points (par_lr_interp.c:1887-1893,
+      /* ext(+i) and direct interpolation turn the points without strong
+       * couplings (-3) into F points (par_lr_interp.c:1887-1893, :5488-5491,
        * par_interp.c:2560-2563); the modified interpolations keep -3 */
-      if (prm->interp_type == 6 || prm->interp_type == 3) { gb_sf_to_f(n, CF, s); }
+      if (prm->interp_type == 6 || prm->interp_type == 14 || prm->interp_type == 3) { gb_sf_to_f(n, CF, s); }
       truncate_host(&P, prm->trunc_factor, prm->p_max_elmts);
       gb_dfree(f2c);
    }
@@ -1962,9 +1969,10 @@ HYPRE_Int HYPRE_BoomerAMGSetInterpType(HYPRE_Solver solver, HYPRE_Int v)
 {
    gb_amg *a = amg_of(solver, 1);
    if (!a) { return gb_error_flag; }
-   if (v != 6 && v != 3 && v != 16 && v != 17 && v != 18)
+   if (v != 6 && v != 3 && v != 14 && v != 16 && v != 17 && v != 18)
    {
-      gb_error(HYPRE_ERROR_GENERIC, "interp_type: extended+i (6), direct (3) and the modified 16, 17, 18 are supported");
+      gb_error(HYPRE_ERROR_GENERIC,
+               "interp_type: extended+i (6), direct (3), extended (14) and the modified 16, 17, 18 are supported");
       gb_error_in_arg(2);
       return gb_error_flag;
    }

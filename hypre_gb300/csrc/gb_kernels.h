@@ -75,7 +75,7 @@ void gb_extpi_count(int nrows, const int *rows, const int *Si, const int *Sj, co
 void gb_extpi_fill(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av, const int *Si,
                    const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv,
                    const int *in_list, const int *in_n, int n_hint, int *gtab, int gcap, int gwarps, int *err,
-                   int tier, cudaStream_t s);
+                   int tier, int iterm, cudaStream_t s);
 void gb_iota(int n, int *out, int *count, cudaStream_t s);
 void gb_count_empty_rows(int n, const int *Ai, int *count, cudaStream_t s);
 void gb_dir_count(int n, const int *Si, const int *Sj, const int *CF, int *cnt, cudaStream_t s);
@@ -85,7 +85,7 @@ void gb_dir_fill(int n, const int *Ai, const int *Aj, const double *Av, const in
 void gb_extpi_count_t(int nrows, const int *rows, const int *Si, const int *Sj, const int *CF, const int *f2c,
                       int *cnt, int *ovf_list, int *ovf_n, cudaStream_t s);
 void gb_extpi_fill_t(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av, const int *Si,
-                     const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv,
+                     const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj, double *Pv, int iterm,
                      cudaStream_t s);
 void gb_truncate_rows(int n, const int *Pi, int *Pj, double *Pv, double tol, int max_elmts, int *newcnt,
                       cudaStream_t s);

@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill(int nrows, const int *__rest
                                                     const int *__restrict__ f2c, const int *__restrict__ Pi,
                                                     int *__restrict__ Pj, double *__restrict__ Pv,
                                                     const int *in_list, const int *in_n, int *gtab, int gcap,
-                                                    int *err)
+                                                    int *err, int iterm)
 {
    extern __shared__ __align__(16) int sh[];
    const int lane = gb_lane();
@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill(int nrows, const int *__rest
                int i2 = in ? Aj[k] : -1;
                double a2 = in ? Av[k] : 0.0;
                bool sgnneg = neg ? (a2 > 0) : (a2 < 0);    // sgn * a2 < 0
-               bool cond = in && sgnneg && (i2 == i || gb_tab_find(T.hk, T.hp, T.cap, i2) >= 0);
+               bool cond = in && sgnneg && ((iterm && i2 == i) || gb_tab_find(T.hk, T.hp, T.cap, i2) >= 0);
                sum = gb_warp_ordered_sum(a2, cond, sum);
             }
             if (sum != 0)
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(128) k_extpi_fill(int nrows, const int *__rest
                   bool sgnneg = neg ? (a2 > 0) : (a2 < 0);
                   int pos2 = (in && sgnneg) ? gb_tab_find(T.hk, T.hp, T.cap, i2) : -1;
                   if (pos2 >= 0) { P[pos2] += distribute * a2; }
-                  bool dterm = in && i2 == i && sgnneg;
+                  bool dterm = iterm && in && i2 == i && sgnneg;
                   unsigned dm = __ballot_sync(GB_FULL, dterm);
                   if (dm)
                   {
@@ -721,18 +721,18 @@ extern "C" void gb_extpi_count(int nrows, const int *rows, const int *Si, const 
 extern "C" void gb_extpi_fill(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av,
                               const int *Si, const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj,
                               double *Pv, const int *in_list, const int *in_n, int n_hint, int *gtab, int gcap,
-                              int gwarps, int *err, int tier, cudaStream_t s)
+                              int gwarps, int *err, int tier, int iterm, cudaStream_t s)
 {
    if (tier == 1)
    {
       k_extpi_fill<false><<<gb_smem_blocks(n_hint), 128, GB_SMEM_BYTES, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c,
                                                                             Pi, Pj, Pv, in_list, in_n, nullptr, 0,
-                                                                            err);
+                                                                            err, iterm);
    }
    else
    {
       k_extpi_fill<true><<<(gwarps + 3) / 4, 128, 0, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c, Pi, Pj, Pv,
-                                                          in_list, in_n, gtab, gcap, err);
+                                                          in_list, in_n, gtab, gcap, err, iterm);
    }
    GB_COUNT(1);
 }
@@ -837,7 +837,7 @@ __global__ void __launch_bounds__(GB_TPR_BLOCK) k_extpi_fill_t(int nrows, const 
                                                       const double *__restrict__ Av, const int *__restrict__ Si,
                                                       const int *__restrict__ Sj, const int *__restrict__ CF,
                                                       const int *__restrict__ f2c, const int *__restrict__ Pi,
-                                                      int *__restrict__ Pj, double *__restrict__ Pv)
+                                                      int *__restrict__ Pj, double *__restrict__ Pv, int iterm)
 {
    int r = blockIdx.x * blockDim.x + threadIdx.x;
    if (r >= nrows) { return; }
@@ -873,7 +873,7 @@ __global__ void __launch_bounds__(GB_TPR_BLOCK) k_extpi_fill_t(int nrows, const 
             int i2 = Aj[k];
             double a2 = Av[k];
             bool sg = neg ? gb_gt0(a2) : gb_lt0(a2);
-            if (sg && (i2 == i || (CF[i2] >= 0 && tpr_find(sk, len, f2c[i2]) >= 0))) { sum += a2; }
+            if (sg && ((iterm && i2 == i) || (CF[i2] >= 0 && tpr_find(sk, len, f2c[i2]) >= 0))) { sum += a2; }
          }
          if (sum != 0)
          {
@@ -886,7 +886,7 @@ __global__ void __launch_bounds__(GB_TPR_BLOCK) k_extpi_fill_t(int nrows, const 
                if (!sg) { continue; }
                int p2 = CF[i2] >= 0 ? tpr_find(sk, len, f2c[i2]) : -1;
                if (p2 >= 0) { P[p2] += distribute * a2; }
-               if (i2 == i) { diagonal += distribute * a2; }
+               if (iterm && i2 == i) { diagonal += distribute * a2; }
             }
          }
          else { diagonal += a; }
@@ -1048,10 +1048,10 @@ extern "C" void gb_extpi_count_t(int nrows, const int *rows, const int *Si, cons
 
 extern "C" void gb_extpi_fill_t(int nrows, const int *rows, const int *Ai, const int *Aj, const double *Av,
                                 const int *Si, const int *Sj, const int *CF, const int *f2c, const int *Pi, int *Pj,
-                                double *Pv, cudaStream_t s)
+                                double *Pv, int iterm, cudaStream_t s)
 {
    k_extpi_fill_t<<<gb_blocks(nrows, GB_TPR_BLOCK), GB_TPR_BLOCK, 0, s>>>(nrows, rows, Ai, Aj, Av, Si, Sj, CF, f2c,
-                                                                        Pi, Pj, Pv);
+                                                                        Pi, Pj, Pv, iterm);
    GB_COUNT(1);
 }
 

@@ -389,7 +389,17 @@ int or_dir_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
 /* src/parcsr_ls/par_lr_interp.c:1024-1924 (one process, offd empty)        */
 /* ------------------------------------------------------------------------ */
 
-int or_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
+static int ext_interp(const or_csr *A, const or_csr *S, int *CF, int iterm, or_csr *P);
+
+int or_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P) { return ext_interp(A, S, CF, 1, P); }
+
+/* Extended interpolation (interp_type 14), hypre_BoomerAMGBuildExtInterpHost
+ * src/parcsr_ls/par_lr_interp.c:4777-5515: the same pattern and weights
+ * without the point's own term -- the sums and the distribution over a strong
+ * F neighbour's row leave i out (:5279-5325 against :1649-1700). */
+int or_ext_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P) { return ext_interp(A, S, CF, 0, P); }
+
+static int ext_interp(const or_csr *A, const or_csr *S, int *CF, int iterm, or_csr *P)
 {
    int n = A->nr;
    int *f2c = xmalloc(sizeof(int) * (n ? n : 1));
@@ -473,7 +483,7 @@ int or_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
                for (int jj1 = A->i[i1] + 1; jj1 < A->i[i1 + 1]; jj1++)
                {
                   int i2 = A->j[jj1];
-                  if ((pmark[i2] >= begin || i2 == i) && (sgn * A->v[jj1]) < 0) { sum += A->v[jj1]; }
+                  if ((pmark[i2] >= begin || (iterm && i2 == i)) && (sgn * A->v[jj1]) < 0) { sum += A->v[jj1]; }
                }
                if (sum != 0)
                {
@@ -482,7 +492,7 @@ int or_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
                   {
                      int i2 = A->j[jj1];
                      if (pmark[i2] >= begin && (sgn * A->v[jj1]) < 0) { Pv[pmark[i2]] += distribute * A->v[jj1]; }
-                     if (i2 == i && (sgn * A->v[jj1]) < 0) { diagonal += distribute * A->v[jj1]; }
+                     if (iterm && i2 == i && (sgn * A->v[jj1]) < 0) { diagonal += distribute * A->v[jj1]; }
                   }
                }
                else { diagonal += A->v[jj]; }
@@ -1745,6 +1755,7 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
          }
          if (prm->interp_type == 6) { or_extpi_interp(A, &S, CF, &P); }
          else if (prm->interp_type == 3) { or_dir_interp(A, &S, CF, &P); }
+         else if (prm->interp_type == 14) { or_ext_interp(A, &S, CF, &P); }
          else { mod_interp(A, &S, CF, prm->interp_type, &P); }   /* 16, 17, 18 */
          or_truncate(&P, prm->trunc_factor, prm->p_max_elmts);
       }

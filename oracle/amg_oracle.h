@@ -87,6 +87,8 @@ int    or_strength(const or_csr *A, double theta, double max_row_sum, or_csr *S)
 int    or_pmis(const or_csr *S, int CF_init, int *CF);
 int    or_coarse_count(int n, const int *CF);
 int    or_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
+int    or_ext_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
+int    or_dir_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
 int    or_truncate(or_csr *P, double trunc_factor, int max_elmts);
 int    or_transpose(const or_csr *A, or_csr *AT);
 int    or_rap(const or_csr *P, const or_csr *A, or_csr *Ac);

@@ -91,6 +91,15 @@ CASES = {
                                  rlx=18, coarse_th=9, solver=1, full=True),
     "fv_12_mm18_pcg": dict(gen="fv", n=(12,), seed=4, th=0.25, mxrs=0.9, Pmx=4, interptype=18, rlx=18, coarse_th=9,
                            solver=1, full=True),
+    # extended interpolation (14)
+    "lap7_16_ext14_pcg": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, interptype=14, rlx=18, coarse_th=9,
+                              solver=1, full=True),
+    "lap27_12_ext14_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, interptype=14, rlx=18, coarse_th=9,
+                               solver=1, full=True),
+    "fv_14_ext14_tr_pcg": dict(gen="fv", n=(14,), seed=5, th=0.25, mxrs=0.9, Pmx=3, tr=0.1, interptype=14, rlx=18,
+                               coarse_th=9, solver=1, full=True),
+    "lap27_40_ext14_pcg": dict(kind=27, n=(40, 40, 40), th=0.5, mxrs=1.0, Pmx=4, interptype=14, rlx=18, coarse_th=9,
+                               solver=1, full=False),
 }
 
 
