@@ -85,11 +85,17 @@ __global__ void __launch_bounds__(256) k_hgs(int n, const int *__restrict__ Ai, 
                if (dir > 0 ? col < i : col > i)
                {
                   // a row the sweep visited before this one: wait for its value
+                  // (back-off from 32 to 256 ns; the shared error word is read
+                  // only every 1024 polls so that waiting lanes do not all
+                  // hammer one address)
                   int spins = 0;
+                  unsigned ns = 32;
                   while (hgs_ld_acquire(flags + col) == 0)
                   {
-                     if (++spins > GB_HGS_SPIN || *(volatile int *) err) { atomicExch(err, 1); break; }
-                     __nanosleep(64);
+                     if (++spins > GB_HGS_SPIN) { atomicExch(err, 1); break; }
+                     if ((spins & 1023) == 0 && *(volatile int *) err) { break; }
+                     __nanosleep(ns);
+                     if (ns < 256) { ns <<= 1; }
                   }
                   v = __ldcg(u + col);
                }
