@@ -46,7 +46,7 @@ def build(verbose=False, ptxas_info=False):
         obj = os.path.join(OUT, f + ".o")
         if f.endswith(".cu"):
             # the setup kernels reproduce the reference's serial rounding: no FMA contraction
-            fmad = "false" if f in ("gb_setup.cu", "gb_agg.cu", "gb_hgs.cu") else "true"
+            fmad = "false" if f in ("gb_setup.cu", "gb_agg.cu", "gb_hgs.cu", "gb_multipass.cu") else "true"
             cmd = [nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=" + fmad, "-Xcompiler", "-fPIC",
                                    "-c", src, "-o", obj] + inc
             if ptxas_info:

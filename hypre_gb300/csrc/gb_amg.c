@@ -803,9 +803,103 @@ static int mm_interp(const gb_csr *A, const gb_csr *S, const int *CF, const int 
    return 0;
 }
 
-/* aggressive level (par_amg_setup.c:1311-1358, :1778-1915, agg_interp_type 6):
- * second-order strength, PMIS on it, P = P1 P2 with P1 modified extended+i
- * and P2 partial extended+i.  Returns the number of coarse points. */
+/* multipass interpolation (agg_interp_type 4, par_multi_interp.c:16-2130)
+ * after the C/F correction by the second coarsening (CFN, numbered by f2c1
+ * over the CF > 0 points; par_strength.c:3068-3090), truncated with
+ * (agg_trunc_factor, agg_P_max_elmts).  Returns the number of coarse points. */
+static int multipass_interp(const gb_amg_params *prm, const gb_csr *A, const gb_csr *S, int *CF, const int *f2c1,
+                            const int *CFN, gb_csr *P)
+{
+   cudaStream_t s = gb_stream();
+   const int n = A->nr;
+   gb_correct_cf(n, f2c1, CFN, CF, s);
+   int *f2c = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   const int nc = number_points(n, CF, 1, 1, f2c, NULL);
+   int *fscan = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *fl = NULL;
+   const int nf = number_points(n, CF, 1, -1, fscan, &fl);
+   gb_dfree(fscan);
+   size_t ni = sizeof(int) * (size_t) (n ? n : 1);
+   int *assigned = (int *) gb_dmalloc(ni), *rowoff = (int *) gb_dcalloc(ni), *rowlen = (int *) gb_dcalloc(ni);
+   int *degen = (int *) gb_dcalloc(ni);
+   double *alfa = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
+   int *dcnt = (int *) gb_dcalloc(sizeof(int) * 2);
+   unsigned long long *dtot = (unsigned long long *) gb_dcalloc(sizeof(unsigned long long));
+   gb_mp_areas areas;
+   memset(&areas, 0, sizeof(areas));
+   int rc = -1;
+   if (!f2c || !assigned || !rowoff || !rowlen || !degen || !alfa || !dcnt || !dtot) { goto done; }
+   /* passes: breadth-first distance from the C points in S (< 10) */
+   gb_mp_pass(n, S->i, S->j, CF, 1, assigned, dcnt, s);
+   int remaining = nf - read_int(dcnt);
+   int np = 2;                                   /* rows of passes 1 .. np-1 */
+   while (remaining > 0 && np < GB_MP_MAXP)
+   {
+      cudaMemsetAsync(dcnt, 0, sizeof(int), s);
+      gb_mp_pass(n, S->i, S->j, CF, np, assigned, dcnt, s);
+      int c = read_int(dcnt);
+      if (c == 0) { break; }                    /* later passes would find none */
+      remaining -= c;
+      np++;
+   }
+   /* the rows, pass by pass */
+   for (int p = 1; p < np; p++)
+   {
+      int *pscan = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      int *rows = NULL;
+      const int m = number_points(n, assigned, 1, p, pscan, &rows);
+      gb_dfree(pscan);
+      int *ub = (int *) gb_dmalloc(sizeof(int) * (size_t) (m + 1));
+      int *off = (int *) gb_dmalloc(sizeof(int) * (size_t) (m + 1));
+      cudaMemsetAsync(dtot, 0, sizeof(unsigned long long), s);
+      gb_mp_bound(m, rows, S->i, S->j, assigned, p, rowlen, ub, dtot, s);
+      unsigned long long tot = 0;
+      cudaMemcpyAsync(&tot, dtot, sizeof(tot), cudaMemcpyDeviceToHost, s);
+      gb_sync();
+      if (tot > 0x7fffff00ULL)
+      {
+         gb_dfree(rows); gb_dfree(ub); gb_dfree(off);
+         gb_error(HYPRE_ERROR_MEMORY, "multipass interpolation: rows of a pass");
+         goto done;
+      }
+      scan_total(ub, off, m);
+      areas.j[p] = (int *) gb_dmalloc(sizeof(int) * (size_t) (tot ? tot : 1));
+      areas.v[p] = (double *) gb_dmalloc(sizeof(double) * (size_t) (tot ? tot : 1));
+      cudaMemsetAsync(dcnt, 0, sizeof(int), s);
+      gb_mp_rows(m, rows, off, p, A->i, A->j, A->v, S->i, S->j, CF, f2c, assigned, areas.j[p - 1],
+                 areas.v[p - 1], areas.j[p], areas.v[p], rowoff, rowlen, alfa, degen, dcnt, s);
+      if (p == 1 && read_int(dcnt) > 0)
+      {
+         gb_mp_carry1(nf, fl, assigned, degen, alfa, rowoff, rowlen, areas.v[1], s);
+      }
+      gb_dfree(rows); gb_dfree(ub); gb_dfree(off);
+   }
+   {
+      int *len = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      gb_mp_len(n, CF, assigned, rowlen, len, s);
+      P->nr = n; P->nc = nc;
+      P->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      P->nnz = scan_total(len, P->i, n);
+      P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
+      P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
+      gb_mp_gather(n, CF, assigned, f2c, rowoff, &areas, P->i, P->j, P->v, s);
+      gb_dfree(len);
+   }
+   truncate_host(P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
+   gb_sf_to_f(n, CF, s);
+   rc = nc;
+done:
+   gb_sync();
+   for (int p = 0; p < GB_MP_MAXP; p++) { gb_dfree(areas.j[p]); gb_dfree(areas.v[p]); }
+   gb_dfree(f2c); gb_dfree(fl); gb_dfree(assigned); gb_dfree(rowoff); gb_dfree(rowlen); gb_dfree(degen);
+   gb_dfree(alfa); gb_dfree(dcnt); gb_dfree(dtot);
+   return rc;
+}
+
+/* aggressive level (par_amg_setup.c:1311-1358, :1778-1915): second-order
+ * strength and PMIS on it, then agg_interp_type 4 -- multipass interpolation
+ * -- or 6 -- P = P1 P2 with P1 modified extended+i and P2 partial
+ * extended+i.  Returns the number of coarse points. */
 static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb_csr *P)
 {
    gb_amg_params *prm = &amg->prm;
@@ -890,6 +984,12 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
       if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS on S2 did not terminate"); return -1; }
    }
    gb_csr_free(&S2);
+   if (prm->agg_interp_type == 4)
+   {
+      int nc = multipass_interp(prm, A, S, CF, f2c1, CFN, P);
+      gb_dfree(f2c1); gb_dfree(c2f1); gb_dfree(cnt); gb_dfree(CFN);
+      return nc;
+   }
    /* P1: modified extended+i (par_mod_lr_interp.c:585) */
    gb_csr P1;
    if (mm_interp(A, S, CF, f2c1, nc1, 17, &P1)) { return -1; }
@@ -1318,9 +1418,9 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    amg->lev[0].n = A0->A.nr;
    int level = 0;
    int maxl = prm->max_levels < 32 ? prm->max_levels : 32;
-   if (prm->agg_num_levels > 0 && prm->agg_interp_type != 6)
+   if (prm->agg_num_levels > 0 && prm->agg_interp_type != 4 && prm->agg_interp_type != 6)
    {
-      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening: only agg_interp_type 6 is supported");
+      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening: agg_interp_type 4 and 6 are supported");
       return gb_error_flag;
    }
    while (1)
@@ -1334,6 +1434,18 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
       if (amg->lev[level].n <= prm->max_coarse_size) { break; }
    }
    amg->num_levels = level + 1;
+   /* Gaussian elimination only when the coarsest level is within
+    * max_coarse_size -- coarsening can stop above it -- else the coarsest
+    * level relaxes with the down-cycle type (par_amg_setup.c:3162-3178; the
+    * reference also keeps the change in its parameters) */
+   {
+      const int t = prm->relax_type[3];
+      if ((t == 9 || t == 19 || t == 98 || t == 99 || t == 198 || t == 199) &&
+          amg->lev[amg->num_levels - 1].n > prm->max_coarse_size)
+      {
+         prm->relax_type[3] = prm->relax_type[1];
+      }
+   }
    double t_sm = gb_wtime();
    /* smoother setup: l1 norms or diagonal per level (par_amg_setup.c:3352-3496) */
    cudaStream_t s = gb_stream();

@@ -137,6 +137,27 @@ void gb_cap_sum(int n, const int *ub, int lcap, int *cap, unsigned long long *su
 void gb_mark_isolated(int nc, const int *c2f, const int *cnt, int *CF, cudaStream_t s);
 void gb_correct_cf2(int n, const int *f2c, const int *CFN, int *CF, cudaStream_t s);
 void gb_cf_clamp(int n, int *CF, cudaStream_t s);
+/* multipass interpolation (gb_multipass.cu): the areas of the passes' rows */
+#define GB_MP_MAXP 10
+typedef struct
+{
+   int    *j[GB_MP_MAXP];
+   double *v[GB_MP_MAXP];
+} gb_mp_areas;
+void gb_correct_cf(int n, const int *f2c, const int *CFN, int *CF, cudaStream_t s);
+void gb_mp_pass(int n, const int *Si, const int *Sj, const int *CF, int p, int *assigned, int *count,
+                cudaStream_t s);
+void gb_mp_bound(int m, const int *rows, const int *Si, const int *Sj, const int *assigned, int p,
+                 const int *rowlen, int *ub, unsigned long long *total, cudaStream_t s);
+void gb_mp_rows(int m, const int *rows, const int *off, int p, const int *Ai, const int *Aj, const double *Av,
+                const int *Si, const int *Sj, const int *CF, const int *f2c, const int *assigned, const int *qj,
+                const double *qv, int *pj, double *pv, int *rowoff, int *rowlen, double *alfa, int *degen,
+                int *ndegen, cudaStream_t s);
+void gb_mp_carry1(int m, const int *fl, const int *assigned, const int *degen, const double *alfa,
+                  const int *rowoff, const int *rowlen, double *pv, cudaStream_t s);
+void gb_mp_len(int n, const int *CF, const int *assigned, const int *rowlen, int *len, cudaStream_t s);
+void gb_mp_gather(int n, const int *CF, const int *assigned, const int *f2c, const int *rowoff,
+                  const gb_mp_areas *areas, const int *Pi, int *Pj, double *Pv, cudaStream_t s);
 void gb_fffc_count(int nf, const int *fl, const int *Ai, const int *Aj, const int *Si, const int *Sj, const int *CF,
                    int *cff, int *cfc, cudaStream_t s);
 /* nrows, nnz: A's size (the mean row length picks the lanes per row) */

@@ -34,6 +34,7 @@ void or_set_threads(int nthreads)
 
 static void *xmalloc(size_t n) { void *p = malloc(n ? n : 1); if (!p) { abort(); } return p; }
 static void *xcalloc(size_t n, size_t s) { void *p = calloc(n ? n : 1, s ? s : 1); if (!p) { abort(); } return p; }
+static void *xrealloc(void *q, size_t n) { void *p = realloc(q, n ? n : 1); if (!p) { abort(); } return p; }
 
 void or_csr_free(or_csr *A)
 {
@@ -874,6 +875,177 @@ int or_strength2(const or_csr *S, int *CF, int num_paths, or_csr *S2)
    return 0;
 }
 
+/* hypre_BoomerAMGCorrectCFMarkerHost src/parcsr_ls/par_strength.c:3068-3090:
+ * C points take the second coarsening's marker (CF 2, isolated in S2, stays C). */
+void or_correct_cf(int n, int *CF, const int *CFN)
+{
+   int cnt = 0;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] > 0)
+      {
+         if (CF[i] == 1) { CF[i] = CFN[cnt++]; }
+         else { CF[i] = 1; cnt++; }
+      }
+   }
+}
+
+/* Multipass interpolation (agg_interp_type 4), hypre_BoomerAMGBuildMultipassHost
+ * src/parcsr_ls/par_multi_interp.c:16-2130 on one process with one thread and
+ * the default weights (sep_weight 0, :1600-1960).  Passes (:310-512): F points
+ * with a strong C neighbour are pass 1; pass p (< 10) takes the F points with a
+ * strong neighbour of pass p-1; the points are visited in the order the
+ * reference's pass_array reaches them.  Pattern (:540-1105): pass 1 rows hold
+ * their strong C neighbours; a row of pass p the union, in S order, of the rows
+ * of its strong neighbours of pass p-1.  Weights: pass 1 row i takes a_ij of
+ * its strong C neighbours (A order), pass p row i the sums of a_ij p_jk over
+ * its strong neighbours j of pass p-1 (A order); sum_C sums those terms,
+ * sum_N the same plus the row's other off-diagonals (CF != -3), and the row
+ * is scaled by alfa = -sum_N / (sum_C a_ii) -- alfa keeps its last value when
+ * sum_C a_ii is zero (in passes >= 2 that is the row's last product).
+ * Truncated with (trunc_factor, max_elmts); CF -3 becomes -1 (:2098-2104). */
+int or_multipass_interp(const or_csr *A, const or_csr *S, int *CF, double trunc_factor, int max_elmts, or_csr *P)
+{
+   const int n = A->nr, max_passes = 10;
+   int *f2c = xmalloc(sizeof(int) * (n ? n : 1)), *assigned = xmalloc(sizeof(int) * (n ? n : 1));
+   int nf = 0, nc = 0;
+   for (int i = 0; i < n; i++) { if (CF[i] == -1) { nf++; } }
+   int *pass_array = xmalloc(sizeof(int) * (nf ? nf : 1));
+   int p_cnt = nf - 1;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] == 1) { f2c[i] = nc++; assigned[i] = 0; }
+      else if (CF[i] == -1) { pass_array[p_cnt--] = i; assigned[i] = -1; f2c[i] = -1; }
+      else { assigned[i] = -1; f2c[i] = -1; }
+   }
+   int pass_ptr[12] = {0};
+   int cnt = 0;
+   for (int i = nf - 1; i > cnt - 1; i--)
+   {
+      int i1 = pass_array[i];
+      for (int j = S->i[i1]; j < S->i[i1 + 1]; j++) { if (CF[S->j[j]] == 1) { assigned[i1] = 1; } }
+      if (assigned[i1] == 1) { pass_array[i++] = pass_array[cnt]; pass_array[cnt++] = i1; }
+   }
+   pass_ptr[2] = cnt;
+   int pass = 2;
+   while (nf - cnt > 0 && pass < max_passes)
+   {
+      for (int i = nf - 1; i > cnt - 1; i--)
+      {
+         int i1 = pass_array[i];
+         for (int j = S->i[i1]; j < S->i[i1 + 1]; j++)
+         {
+            if (assigned[S->j[j]] == pass - 1)
+            {
+               pass_array[i++] = pass_array[cnt];
+               pass_array[cnt++] = i1;
+               assigned[i1] = pass;
+               break;
+            }
+         }
+      }
+      pass++;
+      pass_ptr[pass] = cnt;
+   }
+   const int num_passes = pass;
+   /* rows: C identity, pass rows built pass by pass (each from the finished
+    * rows of the previous pass) */
+   int **rj = xcalloc(n ? n : 1, sizeof(int *));
+   double **rv = xcalloc(n ? n : 1, sizeof(double *));
+   int *rl = xcalloc(n ? n : 1, sizeof(int));
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] == 1) { rj[i] = xmalloc(sizeof(int)); rv[i] = xmalloc(sizeof(double)); rj[i][0] = f2c[i]; rv[i][0] = 1.0; rl[i] = 1; }
+   }
+   int *mark = xmalloc(sizeof(int) * (n ? n : 1)), *pos = xmalloc(sizeof(int) * (nc ? nc : 1));
+   for (int i = 0; i < n; i++) { mark[i] = -1; }
+   double alfa = 1.0;
+   for (int ps = 1; ps < num_passes; ps++)
+   {
+      if (ps >= 2) { alfa = 1.0; }   /* a fresh parallel region per pass (:1757) */
+      for (int t = pass_ptr[ps]; t < pass_ptr[ps + 1]; t++)
+      {
+         int i1 = pass_array[t];
+         /* pattern: pass 1, the strong C neighbours in A order (:1665-1672);
+          * pass p, the union of the strong pass p-1 neighbours' rows taken
+          * in S order (:1048-1072) */
+         int len = 0, cap = 16;
+         int *cj = xmalloc(sizeof(int) * cap);
+         for (int k = 0; k < nc; k++) { pos[k] = -1; }
+         for (int j = S->i[i1]; j < S->i[i1 + 1]; j++)
+         {
+            int j1 = S->j[j];
+            if (assigned[j1] != ps - 1) { continue; }
+            mark[j1] = i1;
+            if (ps == 1) { continue; }
+            for (int k = 0; k < rl[j1]; k++)
+            {
+               int k1 = rj[j1][k];
+               if (pos[k1] < 0)
+               {
+                  if (len == cap) { cap *= 2; cj = xrealloc(cj, sizeof(int) * cap); }
+                  pos[k1] = len; cj[len++] = k1;
+               }
+            }
+         }
+         if (ps == 1)
+         {
+            for (int j = A->i[i1] + 1; j < A->i[i1 + 1]; j++)
+            {
+               int j1 = A->j[j];
+               if (mark[j1] == i1 && pos[f2c[j1]] < 0)
+               {
+                  if (len == cap) { cap *= 2; cj = xrealloc(cj, sizeof(int) * cap); }
+                  pos[f2c[j1]] = len; cj[len++] = f2c[j1];
+               }
+            }
+         }
+         double *cv = xcalloc(len ? len : 1, sizeof(double));
+         double sum_C = 0.0, sum_N = 0.0;
+         for (int j = A->i[i1] + 1; j < A->i[i1 + 1]; j++)
+         {
+            int j1 = A->j[j];
+            double a = A->v[j];
+            if (ps == 1)
+            {
+               /* :1646-1660: every off-diagonal (CF != -3) in sum_N, strong C in P and sum_C */
+               if (CF[j1] != -3) { sum_N += a; }
+               if (mark[j1] == i1) { cv[pos[f2c[j1]]] = a; sum_C += a; }
+            }
+            else if (mark[j1] == i1)
+            {
+               for (int k = 0; k < rl[j1]; k++)
+               {
+                  alfa = a * rv[j1][k];
+                  cv[pos[rj[j1][k]]] += alfa;
+                  sum_C += alfa;
+                  sum_N += alfa;
+               }
+            }
+            else if (CF[j1] != -3) { sum_N += a; }
+         }
+         double diagonal = A->v[A->i[i1]];
+         if (sum_C * diagonal != 0) { alfa = -sum_N / (sum_C * diagonal); }
+         for (int k = 0; k < len; k++) { cv[k] *= alfa; }
+         rj[i1] = cj; rv[i1] = cv; rl[i1] = len;
+      }
+   }
+   int *Pi = xcalloc(n + 1, sizeof(int));
+   for (int i = 0; i < n; i++) { Pi[i + 1] = Pi[i] + rl[i]; }
+   int *Pj = xmalloc(sizeof(int) * (Pi[n] ? Pi[n] : 1));
+   double *Pv = xmalloc(sizeof(double) * (Pi[n] ? Pi[n] : 1));
+   for (int i = 0; i < n; i++)
+   {
+      if (rl[i]) { memcpy(Pj + Pi[i], rj[i], sizeof(int) * rl[i]); memcpy(Pv + Pi[i], rv[i], sizeof(double) * rl[i]); }
+      free(rj[i]); free(rv[i]);
+   }
+   P->nr = n; P->nc = nc; P->i = Pi; P->j = Pj; P->v = Pv;
+   if (trunc_factor != 0.0 || max_elmts != 0) { or_truncate(P, trunc_factor, max_elmts); }
+   for (int i = 0; i < n; i++) { if (CF[i] == SF_PT) { CF[i] = F_PT; } }
+   free(rj); free(rv); free(rl); free(mark); free(pos); free(f2c); free(assigned); free(pass_array);
+   return 0;
+}
+
 /* hypre_BoomerAMGCorrectCFMarker2Host src/parcsr_ls/par_strength.c:3096:
  * C points that the second coarsening made F become -2, the others 1. */
 void or_correct_cf2(int n, int *CF, const int *CFN)
@@ -1707,6 +1879,7 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
 {
    memset(H, 0, sizeof(*H));
    H->prm = *prm;
+   prm = &H->prm;
    int maxl = prm->max_levels;
    H->A = xcalloc(maxl, sizeof(or_csr));
    H->P = xcalloc(maxl, sizeof(or_csr));
@@ -1734,16 +1907,27 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
          or_strength2(&S, CF, prm->num_paths, &S2);
          int *CFN = xmalloc(sizeof(int) * (S2.nr ? S2.nr : 1));
          or_pmis(&S2, 3, CFN);
-         or_csr P1, P2;
-         or_mod_extpi_interp(A, &S, CF, &P1);
-         or_truncate(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
-         or_correct_cf2(n, CF, CFN);
-         or_partial_extpi_interp(A, &S, CF, &P2);
-         or_truncate(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
-         or_matmul(&P1, &P2, &P);
-         or_truncate(&P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
+         if (prm->agg_interp_type == 4)
+         {
+            /* :1799-1815: CF corrected by the second coarsening, then
+             * multipass interpolation on S */
+            or_correct_cf(n, CF, CFN);
+            or_multipass_interp(A, &S, CF, prm->agg_trunc_factor, prm->agg_p_max_elmts, &P);
+         }
+         else
+         {
+            or_csr P1, P2;
+            or_mod_extpi_interp(A, &S, CF, &P1);
+            or_truncate(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
+            or_correct_cf2(n, CF, CFN);
+            or_partial_extpi_interp(A, &S, CF, &P2);
+            or_truncate(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
+            or_matmul(&P1, &P2, &P);
+            or_truncate(&P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
+            or_csr_free(&P1); or_csr_free(&P2);
+         }
          nc = P.nc;
-         or_csr_free(&S2); or_csr_free(&P1); or_csr_free(&P2); free(CFN);
+         or_csr_free(&S2); free(CFN);
       }
       else
       {
@@ -1770,6 +1954,16 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
    }
    H->num_levels = level + 1;
    int nl = H->num_levels;
+   /* par_amg_setup.c:3162-3178: Gaussian elimination only when the coarsest
+    * level is within max_coarse_size (coarsening can stop above it); else
+    * the coarsest level relaxes with the down-cycle type */
+   {
+      const int t = H->prm.relax_coarse;
+      if ((t == 9 || t == 19 || t == 98 || t == 99 || t == 198 || t == 199) && H->A[nl - 1].nr > max_thresh)
+      {
+         H->prm.relax_coarse = H->prm.relax_down;
+      }
+   }
    H->F = xcalloc(nl, sizeof(double *));
    H->U = xcalloc(nl, sizeof(double *));
    for (int l = 0; l < nl; l++)

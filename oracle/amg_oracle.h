@@ -98,6 +98,8 @@ int    or_matmat_flat(int nra, int nca, int ncb, const int *Ai, const int *Aj, c
                       const int *Bi, const int *Bj, const double *Bv, int **Ci, int **Cj, double **Cv);
 int    or_strength2(const or_csr *S, int *CF, int num_paths, or_csr *S2);
 void   or_correct_cf2(int n, int *CF, const int *CFN);
+void   or_correct_cf(int n, int *CF, const int *CFN);
+int    or_multipass_interp(const or_csr *A, const or_csr *S, int *CF, double trunc_factor, int max_elmts, or_csr *P);
 int    or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P);
 int    or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
 int    or_eig_tridiag(int n, double *d, double *e);

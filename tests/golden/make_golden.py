@@ -98,6 +98,22 @@ CASES = {
                                solver=1, full=True),
     "fv_14_ext14_tr_pcg": dict(gen="fv", n=(14,), seed=5, th=0.25, mxrs=0.9, Pmx=3, tr=0.1, interptype=14, rlx=18,
                                coarse_th=9, solver=1, full=True),
+    # multipass interpolation on the aggressive levels (agg_interp_type 4, the
+    # library default), with and without its truncation
+    "lap27_16_agg4_pcg": dict(kind=27, n=(16, 16, 16), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
+                              coarse_th=9, solver=1, full=True),
+    "lap7_20_agg4x2_pcg": dict(kind=7, n=(20, 20, 20), th=0.25, mxrs=1.0, Pmx=4, agg_nl=2, agg_interp=4, rlx=6,
+                               coarse_th=9, solver=1, full=True),
+    "lap7_18_agg4_pmx_fgmres": dict(kind=7, n=(18, 18, 18), th=0.25, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4,
+                                    agg_Pmx=4, rlx=3, coarse_th=9, solver=61, k=10, full=True),
+    "fv_14_agg4_pcg": dict(gen="fv", n=(14,), seed=6, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
+                           coarse_th=9, solver=1, full=True),
+    "aniso_48_agg4_pcg": dict(gen="aniso", n=(48,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=4,
+                              agg_Pmx=3, rlx=18, coarse_th=9, solver=1, full=True),
+    "zerodiag_14_agg4_fgmres": dict(gen="zerodiag", n=(14,), th=0.25, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
+                                    coarse_th=9, solver=61, k=10, full=True),
+    "lap27_48_agg4_pcg": dict(kind=27, n=(48, 48, 48), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
+                              coarse_th=9, solver=1, full=False),
     "lap27_40_ext14_pcg": dict(kind=27, n=(40, 40, 40), th=0.5, mxrs=1.0, Pmx=4, interptype=14, rlx=18, coarse_th=9,
                                solver=1, full=False),
 }
@@ -106,7 +122,7 @@ CASES = {
 def dump_args(c, out):
     if "gen" in c:
         import golden_cases as GC
-        I, J, V = GC.matrix(c, O)
+        I, J, V = GC.generate(c)
         mat = out + ".csr"
         with open(mat, "wb") as f:
             np.array([len(I) - 1, len(J)], np.int32).tofile(f)
@@ -115,7 +131,7 @@ def dump_args(c, out):
         a = [DUMP, "-mat", mat]
     else:
         a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "rlx", "rlx_down", "rlx_up", "w",
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "rlx", "rlx_down", "rlx_up", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]
@@ -140,6 +156,12 @@ def make(name, c):
     os.unlink(tmp)
     out = {"case": np.array(json.dumps({k: v for k, v in c.items() if k != "full"})),
            "dump_stdout": np.array(r.stdout)}
+    if "gen" in c:
+        # the rows the driver was given: the generators use numpy's exp, whose
+        # last bits differ between machines
+        import golden_cases as GC
+        I, J, V = GC.generate(c)
+        out.update(in_i=np.asarray(I, np.int32), in_j=np.asarray(J, np.int32), in_v=np.asarray(V, np.float64))
     for key in ("iters", "final_relres", "nlev", "lev_rows", "lev_nnz", "relres", "resnorms"):
         if key in rec:
             out[key] = rec[key]
@@ -240,10 +262,13 @@ def make_matmat(name, c):
 def main():
     if not os.path.exists(DUMP):
         sys.exit("build the reference dumper first: make -C oracle/ref REF=<reference>/src")
+    only = set(sys.argv[1:])          # case names to remake (default: all)
     for name, c in CASES.items():
-        make(name, c)
+        if not only or name in only:
+            make(name, c)
     for name, c in MATMAT.items():
-        make_matmat(name, c)
+        if not only or name in only:
+            make_matmat(name, c)
 
 
 if __name__ == "__main__":

@@ -28,16 +28,31 @@ def load(name):
     return d
 
 
-def matrix(c, O):
-    """The case's matrix (I, J, V): the reference generators' stencils, or a
-    seeded project generator ("gen": "fv" finite-volume diffusion on n^3
-    cells, "aniso" 2-D anisotropic 5-point with eps) written to the
-    reference driver as a CSR file."""
+def matrix(c, O, g=None):
+    """The case's matrix (I, J, V): the reference generators' stencils, or,
+    for a generated case, the rows the reference driver was given (stored in
+    the record g as in_i, in_j, in_v)."""
     if "gen" not in c:
         return O.stencil(c["kind"], *c["n"])
+    if g is not None and "in_i" in g:
+        return g["in_i"], g["in_j"], g["in_v"]
+    return generate(c)
+
+
+def generate(c):
+    """A seeded project generator ("gen": "fv" finite-volume diffusion on n^3
+    cells, "aniso" 2-D anisotropic 5-point with eps, "zerodiag" the 7-point
+    Laplacian on n^3 with the diagonal of every row i = 5 mod 11 set to zero,
+    so that interpolation rows meet a zero diagonal)."""
     from hypre_gb300 import problems as P
     if c["gen"] == "fv":
         return P.fv_diffusion(c["n"][0], seed=c.get("seed", 0))
+    if c["gen"] == "zerodiag":
+        n = c["n"][0]
+        I, J, V = P.laplace(7, n, n, n)
+        rows = np.repeat(np.arange(len(I) - 1), np.diff(I))
+        V = np.where((J == rows) & (rows % 11 == 5), 0.0, V)
+        return I, J, V
     return P.aniso2d(c["n"][0], c["eps"])
 
 
@@ -50,6 +65,8 @@ def oracle_params(c):
              relax_weight=c.get("w", 1.0), interp_type=c.get("interptype", 6))
     if "cheby_order" in c:
         p["cheby_order"] = c["cheby_order"]
+    if "agg_Pmx" in c:
+        p["agg_p_max_elmts"] = c["agg_Pmx"]
     return p
 
 
@@ -63,6 +80,8 @@ def amg_params(c):
         p["CycleRelaxType"] = cyc
     if c.get("agg_nl", 0):
         p["AggInterpType"] = c.get("agg_interp", 4)
+    if "agg_Pmx" in c:
+        p["AggPMaxElmts"] = c["agg_Pmx"]
     if "cheby_order" in c:
         p["ChebyOrder"] = c["cheby_order"]
     return p

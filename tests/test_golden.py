@@ -20,7 +20,7 @@ def O(oracle_mod):
 def test_oracle_matches_reference(O, name):
     g = G.load(name)
     c = g["case"]
-    I, J, V = G.matrix(c, O)
+    I, J, V = G.matrix(c, O, g)
     H = O.Hierarchy(I, J, V, O.default_params(**G.oracle_params(c)))
     G.check_hierarchy(g, H.num_levels, lambda w, l: H.csr(w, l)[:3], H.cf, H.l1,
                       cheby=lambda l, o: H.cheby(l, o), value_rtol=0.0, cheby_rtol=0.0)

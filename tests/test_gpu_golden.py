@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 def test_gpu_matches_reference(gb, oracle_mod, name):
     g = G.load(name)
     c = g["case"]
-    I, J, V = G.matrix(c, oracle_mod)
+    I, J, V = G.matrix(c, oracle_mod, g)
     n = len(I) - 1
     b = oracle_mod.rhs_normalised(n)
     G.check_array(g, "b", b)
