@@ -268,12 +268,13 @@ def gpu_arm(args):
             dev_s, wall_s = timed(lambda: step(pcg, amg), args.steps, args.warmup)
         launches = gb.kernel_launches() // max(1, args.steps + args.warmup)
         it = C.c_int(); L.HYPRE_FlexGMRESGetNumIterations(pcg, C.byref(it))
-        t = np.zeros(6); L.HYPRE_GB300_BoomerAMGGetSetupTimes(amg, t.ctypes.data, 6)
+        t = np.zeros(8); L.HYPRE_GB300_BoomerAMGGetSetupTimes(amg, t.ctypes.data, 8)
         nl = C.c_int(); L.HYPRE_BoomerAMGGetNumLevels(amg, C.byref(nl))
         sgb, sgs, sgc = C.c_double(), C.c_double(), C.c_int()
         L.HYPRE_GB300_BoomerAMGGetSpGEMMStats(amg, C.byref(sgb), C.byref(sgs), C.byref(sgc))
         res[label] = dict(seconds=dev_s, wall_seconds=wall_s, iterations=it.value, levels=nl.value,
                           setup_seconds=float(t[5]), setup_phase_seconds=[float(v) for v in t[:5]],
+                          setup_host_waits=int(t[6]), setup_host_wait_seconds=float(t[7]),
                           true_relres=true_relres(), launches_per_step=launches, clocks=cs.summary(),
                           spgemm={"bytes": sgb.value, "seconds": sgs.value, "products": sgc.value})
         if label == "fp64_plain" and rank == 0 and not args.no_cpu_baseline:

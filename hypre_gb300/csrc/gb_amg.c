@@ -1414,6 +1414,8 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    g_global_only = amg->prm.setup_tables == 1;
 
    memset(amg->setup_times, 0, sizeof(amg->setup_times));
+   const long long sync0 = gb_sync_calls;
+   const double tsync0 = gb_sync_seconds;
    amg->lev[0].A = A0;
    amg->lev[0].n = A0->A.nr;
    int level = 0;
@@ -1531,6 +1533,8 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    amg->spgemm_seconds = g_sg_seconds;
    amg->spgemm_calls = g_sg_calls;
    amg->setup_times[5] = gb_wtime() - t_start;
+   amg->setup_times[6] = (double) (gb_sync_calls - sync0);
+   amg->setup_times[7] = gb_sync_seconds - tsync0;
    amg->setup_done = 1;
    return gb_error_flag;
 }
@@ -2228,7 +2232,7 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetSetupTimes(HYPRE_Solver solver, HYPRE_Real *t,
 {
    gb_amg *a = amg_of(solver, 1);
    if (!a || !t) { return gb_error_flag; }
-   for (int k = 0; k < n && k < 6; k++) { t[k] = a->setup_times[k]; }
+   for (int k = 0; k < n && k < 8; k++) { t[k] = a->setup_times[k]; }
    return gb_error_flag;
 }
 

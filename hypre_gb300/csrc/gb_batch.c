@@ -241,10 +241,16 @@ HYPRE_Int HYPRE_GB300_BatchedPCGSetup(HYPRE_Solver solver, HYPRE_Solver amg_solv
       batch_free_setup(b);
       return gb_error_flag;
    }
-   /* one BoomerAMG setup for the whole block-diagonal matrix */
-   if (gb_amg_setup(amg, A)) { batch_free_setup(b); return gb_error_flag; }
+   /* one BoomerAMG setup for the whole block-diagonal matrix.  Its coarsest
+    * level holds every system's coarsest block and may exceed max_coarse_size,
+    * where the single-system setup switches the coarsest relaxation to the
+    * down-cycle type; each system's block is solved directly here, so the
+    * coarsest type is kept. */
+   const int ct = prm->relax_type[3];
+   const int setup_rc = gb_amg_setup(amg, A);
+   prm->relax_type[3] = ct;
+   if (setup_rc) { batch_free_setup(b); return gb_error_flag; }
    int nl = amg->num_levels;
-   int ct = prm->relax_type[3];
    if (!(ct == 9 || ct == 19 || ct == 98 || ct == 99))
    {
       gb_error(HYPRE_ERROR_GENERIC, "batched PCG: the coarsest level needs a direct solve (relax 9/19/98/99)");

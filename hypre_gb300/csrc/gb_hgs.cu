@@ -43,6 +43,36 @@ __device__ __forceinline__ float hgs_sub(float a, float b) { return __fsub_rn(a,
 __device__ __forceinline__ double hgs_div(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ float hgs_div(float a, float b) { return __fdiv_rn(a, b); }
 
+// Waits until the rows of the lanes with dep set have been written.  One lane
+// polls at a time -- the dependency nearest this row in sweep order, usually
+// the last to finish -- and then every waiting lane checks its flag once, so
+// a warp keeps one poll in flight instead of one per neighbour (thousands of
+// warps polling every neighbour's flag saturated the L2).  Each poll loop is
+// bounded: when it runs out, or another warp's did (*err), the wait ends.
+__device__ __forceinline__ void hgs_wait(bool dep, int col, const int *flags, int *err, int lane, int dir)
+{
+   unsigned pending = __ballot_sync(GB_FULL, dep && hgs_ld_acquire(flags + col) == 0);
+   while (pending)
+   {
+      const int L = dir > 0 ? 31 - __clz(pending) : __ffs(pending) - 1;
+      int bail = 0;
+      if (lane == L)
+      {
+         int spins = 0;
+         unsigned ns = 32;
+         while (hgs_ld_acquire(flags + col) == 0)
+         {
+            if (++spins > GB_HGS_SPIN) { atomicExch(err, 1); bail = 1; break; }
+            if ((spins & 1023) == 0 && *(volatile int *) err) { bail = 1; break; }
+            __nanosleep(ns);
+            if (ns < 256) { ns <<= 1; }
+         }
+      }
+      if (__shfl_sync(GB_FULL, bail, L)) { break; }
+      pending = __ballot_sync(GB_FULL, ((pending >> lane) & 1u) && hgs_ld_acquire(flags + col) == 0);
+   }
+}
+
 // One sweep.  u: values updated in place; uo: u as it was when the sweep
 // started (read for the rows not yet visited and for the row's own entry);
 // ut: u before the first sweep of the relaxation (the scaled form's second
@@ -76,30 +106,19 @@ __global__ void __launch_bounds__(256) k_hgs(int n, const int *__restrict__ Ai, 
          for (int c = b + skip; c < e; c += 32)
          {
             const int k = c + lane;
+            int col = 0;
+            bool dep = false;
+            if (k < e)
+            {
+               col = Aj[k];
+               dep = dir > 0 ? col < i : col > i;   // visited by the sweep before this row
+            }
+            hgs_wait(dep, col, flags, err, lane, dir);
             T p = 0, p2 = 0;
             if (k < e)
             {
-               const int col = Aj[k];
                const T a = Av[k];
-               T v;
-               if (dir > 0 ? col < i : col > i)
-               {
-                  // a row the sweep visited before this one: wait for its value
-                  // (back-off from 32 to 256 ns; the shared error word is read
-                  // only every 1024 polls so that waiting lanes do not all
-                  // hammer one address)
-                  int spins = 0;
-                  unsigned ns = 32;
-                  while (hgs_ld_acquire(flags + col) == 0)
-                  {
-                     if (++spins > GB_HGS_SPIN) { atomicExch(err, 1); break; }
-                     if ((spins & 1023) == 0 && *(volatile int *) err) { break; }
-                     __nanosleep(ns);
-                     if (ns < 256) { ns <<= 1; }
-                  }
-                  v = __ldcg(u + col);
-               }
-               else { v = uo[col]; }
+               const T v = dep ? __ldcg(u + col) : uo[col];
                p = hgs_mul(a, v);
                if (ut) { p2 = hgs_mul(a, ut[col]); }
             }

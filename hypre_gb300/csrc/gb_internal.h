@@ -30,6 +30,8 @@ void  gb_dfree(void *p);
 void *gb_hmalloc_pinned(size_t bytes);
 void  gb_hfree_pinned(void *p);
 int   gb_sync(void);                         /* stream sync + error check */
+extern long long gb_sync_calls;              /* gb_sync calls and seconds waited */
+extern double    gb_sync_seconds;
 double gb_wtime(void);
 /* scratch buffers reused across calls (grow-only, stream ordered) */
 void *gb_scratch(int slot, size_t bytes);
@@ -195,7 +197,7 @@ typedef struct
    int           coarse_n;
    int           num_iterations;
    double        rel_resid;
-   double        setup_times[6];
+   double        setup_times[8];   /* phases [0..4], total [5], host syncs [6], seconds in them [7] */
    int           setup_done;
    /* CUDA graph of one V-cycle for given (f, u) device pointers */
    cudaGraphExec_t graph;

@@ -121,9 +121,16 @@ void gb_hfree_pinned(void *p)
    if (p) { cudaFreeHost(p); }
 }
 
+/* host waits on the library stream: count and seconds (setup diagnostics) */
+long long gb_sync_calls = 0;
+double gb_sync_seconds = 0.0;
+
 int gb_sync(void)
 {
+   const double t0 = gb_wtime();
    cudaError_t e = cudaStreamSynchronize(gb_stream());
+   gb_sync_seconds += gb_wtime() - t0;
+   gb_sync_calls++;
    if (e == cudaSuccess) { e = cudaGetLastError(); }
    return gb_cuda_ok(e, "kernel") ? 0 : 1;
 }

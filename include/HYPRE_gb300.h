@@ -444,8 +444,11 @@ HYPRE_Int HYPRE_GB300_ResetKernelLaunchCount(void);
  * above, is the allocating form). */
 HYPRE_Int HYPRE_GB300_ParCSRMatrixMatvecTNoAlloc(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, HYPRE_ParVector x,
                                                 HYPRE_Complex beta, HYPRE_ParVector y);
-/* Per-phase timings of the last setup (seconds, CUDA events):
- * [0] strength [1] coarsening [2] interpolation [3] RAP [4] smoother setup [5] total */
+/* Per-phase timings of the last setup (seconds, host clock; the phases end
+ * at host read-backs, so they are close to device time): [0] strength [1] coarsening
+ * [2] interpolation [3] RAP [4] smoother setup [5] total; [6] the number of
+ * times the host waited for the stream during setup, [7] seconds spent in
+ * those waits. */
 HYPRE_Int HYPRE_GB300_BoomerAMGGetSetupTimes(HYPRE_Solver solver, HYPRE_Real *times, HYPRE_Int n);
 
 #ifdef __cplusplus
