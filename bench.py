@@ -368,15 +368,26 @@ def gpu_arm(args):
     ncols = np.diff(I).astype(np.int32)
     rows = np.arange(n, dtype=np.int32)
 
-    def e2e_step():
+    def e2e_step(parts=None):
+        # parts (an untimed extra run): host seconds per stage, the stream
+        # drained at each boundary
+        def mark(name):
+            if parts is not None:
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                parts.append((name, t))
+        mark("start")
         ijA = C.c_void_p()
         L.HYPRE_IJMatrixCreate(0, 0, n - 1, 0, n - 1, C.byref(ijA))
         L.HYPRE_IJMatrixSetObjectType(ijA, gb.HYPRE_PARCSR)
         L.HYPRE_IJMatrixSetRowSizes(ijA, ncols.ctypes.data)
         L.HYPRE_IJMatrixInitialize(ijA)
+        mark("ij_create_init")
         L.HYPRE_IJMatrixSetValues(ijA, n, ncols.ctypes.data, rows.ctypes.data, hJ.data_ptr(), hV.data_ptr())
+        mark("ij_setvalues")
         L.HYPRE_IJMatrixAssemble(ijA)
         pA = C.c_void_p(); L.HYPRE_IJMatrixGetObject(ijA, C.byref(pA))
+        mark("ij_assemble")
         ijb = C.c_void_p(); ijx = C.c_void_p()
         L.HYPRE_IJVectorCreate(0, 0, n - 1, C.byref(ijb)); L.HYPRE_IJVectorSetObjectType(ijb, gb.HYPRE_PARCSR)
         L.HYPRE_IJVectorInitialize(ijb); L.HYPRE_IJVectorSetValues(ijb, n, None, hb.data_ptr())
@@ -385,13 +396,22 @@ def gpu_arm(args):
         L.HYPRE_IJVectorInitialize(ijx); L.HYPRE_IJVectorAssemble(ijx)
         pb = C.c_void_p(); px = C.c_void_p()
         L.HYPRE_IJVectorGetObject(ijb, C.byref(pb)); L.HYPRE_IJVectorGetObject(ijx, C.byref(px))
+        mark("ij_vectors")
         gb.check(L.HYPRE_ParCSRFlexGMRESSetup(pcg, pA, pb, px), "e2e setup")
+        mark("setup")
         gb.check(L.HYPRE_ParCSRFlexGMRESSolve(pcg, pA, pb, px), "e2e solve")
+        mark("solve")
         L.HYPRE_IJVectorGetValues(ijx, n, None, hx.data_ptr())
+        mark("readback")
         L.HYPRE_IJVectorDestroy(ijx); L.HYPRE_IJVectorDestroy(ijb); L.HYPRE_IJMatrixDestroy(ijA)
+        mark("destroy")
 
     e2e_dev, e2e_wall = (None, None) if args.no_e2e else timed(e2e_step, max(1, args.steps), 1)
+    e2e_parts = None
     if not args.no_e2e:
+        pts = []
+        e2e_step(pts)
+        e2e_parts = {pts[k][0]: pts[k][1] - pts[k - 1][1] for k in range(1, len(pts))}
         # the e2e setups released the kept solver's last resident-step hierarchy
         m_k = step_mats.pop(keep[1].value, None)
         if m_k is not None:
@@ -424,7 +444,8 @@ def gpu_arm(args):
         "value_arm": mixed,
         "speedup_mixed_vs_fp64_plain": res["fp64_plain"]["seconds"] / best["seconds"] if "fp64_plain" in res else None,
         "e2e": {"value": e2e_wall, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "device_event_seconds": e2e_dev, "arm": mixed},
+                "device_event_seconds": e2e_dev, "arm": mixed,
+                "stages_seconds": e2e_parts},
         "gpu_launches": best["launches_per_step"],
         "roofline": {"bound": "hbm", "kernel": "k_spgemm: sparse products of one setup (Galerkin R*A, RA*P "
                      "on every level, aggressive level's FF*FC and P1*P2), count + fill passes",

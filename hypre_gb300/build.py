@@ -55,6 +55,8 @@ def build(verbose=False, ptxas_info=False):
         elif f.endswith(".c"):
             cmd = ["gcc", "-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wno-unused-function", "-ffp-contract=off",
                    "-c", src, "-o", obj] + inc
+            if f == "gb_ij.c":
+                cmd.insert(1, "-fopenmp")   # host passes over the rows of large IJ puts
             jobs.append((cmd, obj))
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         outs = list(ex.map(lambda j: _run(j[0]), jobs))
@@ -64,7 +66,7 @@ def build(verbose=False, ptxas_info=False):
                 print(o)
     objs = [o for _, o in jobs]
     tmp = LIB + ".tmp"
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"])
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lgomp", "-lrt", "-ldl", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -1609,8 +1609,8 @@ static void hybrid_gs_d(gb_amg *amg, int l, int type, const double *f, double *u
    const gb_csr *A = &L->A->A;
    for (int k = 0; k < nsw; k++)
    {
-      gb_hgs_sweep_d(n, A->i, A->j, A->v, f, u, L->V, ut, l1 ? L->l1 : NULL, k == 0 ? dir0 : -dir0, skip, w, omega,
-                     L->hgs_flags, g_hgs_err, s);
+      gb_hgs_sweep_d(n, A->nnz, A->i, A->j, A->v, f, u, L->V, ut, l1 ? L->l1 : NULL, k == 0 ? dir0 : -dir0, skip,
+                     w, omega, L->hgs_flags, g_hgs_err, s);
    }
    g_hgs_used = 1;
 }
@@ -1636,7 +1636,7 @@ static void hybrid_gs_f(gb_amg *amg, int l, int type, const float *f, float *u, 
    const gb_spmv_desc *A = gb_solve_desc(L->A, GB_PREC_F32);
    for (int k = 0; k < nsw; k++)
    {
-      gb_hgs_sweep_f(n, A->i, A->j, (const float *) A->v, f, u, L->Vf, ut, l1 ? L->l1f : NULL,
+      gb_hgs_sweep_f(n, L->A->A.nnz, A->i, A->j, (const float *) A->v, f, u, L->Vf, ut, l1 ? L->l1f : NULL,
                      k == 0 ? dir0 : -dir0, skip, w, omega, L->hgs_flags, g_hgs_err, s);
    }
    g_hgs_used = 1;

@@ -47,8 +47,10 @@ __device__ __forceinline__ float hgs_div(float a, float b) { return __fdiv_rn(a,
 // polls at a time -- the dependency nearest this row in sweep order, usually
 // the last to finish -- and then every waiting lane checks its flag once, so
 // a warp keeps one poll in flight instead of one per neighbour (thousands of
-// warps polling every neighbour's flag saturated the L2).  Each poll loop is
-// bounded: when it runs out, or another warp's did (*err), the wait ends.
+// warps polling every neighbour's flag saturated the L2).  Polls are acquire
+// loads, so a lane that has seen its flag set reads the row's value after the
+// writer's release.  Each poll loop is bounded: when it runs out, or another
+// warp's did (*err), the wait ends.
 __device__ __forceinline__ void hgs_wait(bool dep, int col, const int *flags, int *err, int lane, int dir)
 {
    unsigned pending = __ballot_sync(GB_FULL, dep && hgs_ld_acquire(flags + col) == 0);
@@ -154,33 +156,142 @@ __global__ void __launch_bounds__(256) k_hgs(int n, const int *__restrict__ Ai, 
    }
 }
 
+// One sweep of a level whose matrix and vectors fit in shared memory (the
+// coarse levels, whose dependency chains are about as long as their row
+// counts, so that waiting on flags in global memory costs more than running
+// the loop).  The block stages the rows, u, f, the l1 norms and the starting
+// values into shared memory; one warp then runs the reference's loop in sweep
+// order -- in place, so an unvisited row's entry still holds its value from
+// before the sweep -- and the block writes u back.  The arithmetic is that of
+// k_hgs, term for term.
 template <typename T>
-static void hgs_sweep(int n, const int *Ai, const int *Aj, const T *Av, const T *f, T *u, T *uo, const T *ut,
-                      const T *dvec, int dir, int skip, double w, double omega, int *flags, int *err, cudaStream_t s)
+__global__ void __launch_bounds__(512) k_hgs_seq(int n, int nnz, const int *__restrict__ Ai,
+                                                 const int *__restrict__ Aj, const T *__restrict__ Av,
+                                                 const T *__restrict__ f, T *u, const T *__restrict__ ut,
+                                                 const T *__restrict__ dvec, int dir, int skip, T w, T omega, T prod)
+{
+   extern __shared__ __align__(16) unsigned char hgs_smem[];
+   T *su = (T *) hgs_smem;
+   T *sf = su + n;
+   T *sut = sf + n;
+   T *sd = sut + (ut ? n : 0);
+   T *sav = sd + (dvec ? n : 0);
+   int *sai = (int *) (sav + nnz);
+   int *saj = sai + n + 1;
+   const int base = Ai[0];
+   for (int k = threadIdx.x; k < n; k += blockDim.x)
+   {
+      su[k] = u[k];
+      sf[k] = f[k];
+      if (ut) { sut[k] = ut[k]; }
+      if (dvec) { sd[k] = dvec[k]; }
+   }
+   for (int k = threadIdx.x; k <= n; k += blockDim.x) { sai[k] = Ai[k] - base; }
+   for (int k = threadIdx.x; k < nnz; k += blockDim.x)
+   {
+      saj[k] = Aj[base + k];
+      sav[k] = Av[base + k];
+   }
+   __syncthreads();
+   if (threadIdx.x < 32)
+   {
+      const int lane = threadIdx.x;
+      for (int t = 0; t < n; t++)
+      {
+         const int i = dir > 0 ? t : n - 1 - t;
+         const int b = sai[i], e = sai[i + 1];
+         const T aii = e > b ? sav[b] : (T) 0;
+         const T di = dvec ? sd[i] : aii;
+         T ui = su[i];
+         if (di != (T) 0)
+         {
+            T res = sf[i], res0 = 0, res2 = 0;
+            for (int c = b + skip; c < e; c += 32)
+            {
+               const int k = c + lane;
+               T p = 0, p2 = 0;
+               if (k < e)
+               {
+                  const int col = saj[k];
+                  const T a = sav[k];
+                  p = hgs_mul(a, su[col]);
+                  if (ut) { p2 = hgs_mul(a, sut[col]); }
+               }
+               const int cnt = min(32, e - c);
+            for (int q = 0; q < cnt; q++)
+            {
+               const T pq = __shfl_sync(GB_FULL, p, q);
+               if (ut)
+               {
+                  const T p2q = __shfl_sync(GB_FULL, p2, q);
+                  res0 = hgs_sub(res0, pq);
+                  res2 = hgs_add(res2, p2q);
+               }
+               else { res = hgs_sub(res, pq); }
+            }
+            }
+            if (ut)
+            {
+               const T s = hgs_add(hgs_add(hgs_mul(omega, res), res0), hgs_mul(hgs_sub((T) 1, omega), res2));
+               const T upd = hgs_div(hgs_mul(w, s), di);
+               ui = hgs_add(skip ? hgs_mul(ui, prod) : ui, upd);
+            }
+            else if (skip) { ui = hgs_div(res, di); }
+            else { ui = hgs_add(ui, hgs_div(res, di)); }
+         }
+         if (lane == 0) { su[i] = ui; }
+         __syncwarp();
+      }
+   }
+   __syncthreads();
+   for (int k = threadIdx.x; k < n; k += blockDim.x) { u[k] = su[k]; }
+}
+
+#define GB_HGS_SEQ_SMEM (200 * 1024)
+
+template <typename T>
+static void hgs_sweep(int n, long long nnz, const int *Ai, const int *Aj, const T *Av, const T *f, T *u, T *uo,
+                      const T *ut, const T *dvec, int dir, int skip, double w, double omega, int *flags, int *err,
+                      cudaStream_t s)
 {
    if (n <= 0) { return; }
+   const double prod0 = 1.0 - w * omega;
+   const long long smem = (long long) sizeof(T) * (2LL * n + (ut ? n : 0) + (dvec ? n : 0) + nnz) +
+                          4LL * ((long long) n + 1 + nnz);
+   if (smem <= GB_HGS_SEQ_SMEM)
+   {
+      static int attr_set = 0;
+      if (!attr_set)
+      {
+         cudaFuncSetAttribute(k_hgs_seq<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_HGS_SEQ_SMEM);
+         attr_set = 1;
+      }
+      k_hgs_seq<T><<<1, 512, (size_t) smem, s>>>(n, (int) nnz, Ai, Aj, Av, f, u, ut, dvec, dir, skip, (T) w,
+                                                 (T) omega, (T) prod0);
+      GB_COUNT(1);
+      return;
+   }
    cudaMemsetAsync(flags, 0, sizeof(int) * ((size_t) n + 1), s);
    cudaMemcpyAsync(uo, u, sizeof(T) * (size_t) n, cudaMemcpyDeviceToDevice, s);
    // a warp per row in flight; enough warps to cover a dependency front of a
    // few thousand rows, few enough that the spinning warps leave issue slots
    long long warps = n < 152LL * 16 ? n : 152LL * 16;
    int blocks = (int) ((warps * 32 + 255) / 256);
-   const double prod = 1.0 - w * omega;
-   k_hgs<T><<<blocks, 256, 0, s>>>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, (T) w, (T) omega, (T) prod, flags,
+   k_hgs<T><<<blocks, 256, 0, s>>>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, (T) w, (T) omega, (T) prod0, flags,
                                    err);
    GB_COUNT(1);
 }
 
-extern "C" void gb_hgs_sweep_d(int n, const int *Ai, const int *Aj, const double *Av, const double *f, double *u,
-                               double *uo, const double *ut, const double *dvec, int dir, int skip, double w,
-                               double omega, int *flags, int *err, cudaStream_t s)
+extern "C" void gb_hgs_sweep_d(int n, long long nnz, const int *Ai, const int *Aj, const double *Av,
+                               const double *f, double *u, double *uo, const double *ut, const double *dvec, int dir,
+                               int skip, double w, double omega, int *flags, int *err, cudaStream_t s)
 {
-   hgs_sweep<double>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
+   hgs_sweep<double>(n, nnz, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
 }
 
-extern "C" void gb_hgs_sweep_f(int n, const int *Ai, const int *Aj, const float *Av, const float *f, float *u,
-                               float *uo, const float *ut, const float *dvec, int dir, int skip, double w,
+extern "C" void gb_hgs_sweep_f(int n, long long nnz, const int *Ai, const int *Aj, const float *Av, const float *f,
+                               float *u, float *uo, const float *ut, const float *dvec, int dir, int skip, double w,
                                double omega, int *flags, int *err, cudaStream_t s)
 {
-   hgs_sweep<float>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
+   hgs_sweep<float>(n, nnz, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
 }

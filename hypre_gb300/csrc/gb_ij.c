@@ -562,6 +562,7 @@ struct hypre_IJMatrix_struct
    double    *vals;
    long long  arena_len, arena_cap;
    int       *hint;           /* row sizes from SetRowSizes */
+   int        hint_zero;      /* some row was given no space */
    gb_parcsr *par;
    /* device staging: rows put by large SetValues calls are copied straight
     * to the device (row_state 2, entries at dev_off[r]); the others live in
@@ -587,6 +588,55 @@ static int check_ijm(HYPRE_IJMatrix m, int arg)
 {
    if (!m || m->magic != GB_MAGIC_IJM) { gb_error_in_arg(arg); return 0; }
    return 1;
+}
+
+/* Host arrays of one entry per row (row sizes, offsets of a put) are reused
+ * across IJ objects: a fresh allocation of tens of MB pays a page fault per
+ * page on first touch (milliseconds at millions of rows), which a caller that
+ * assembles a matrix every time step would pay every step.  Blocks carry
+ * their size in a 16-byte header; up to four freed blocks of at least 1 MB
+ * are kept (released by HYPRE_Finalize). */
+#define GB_IJ_HCACHE 4
+static void *g_hcache[GB_IJ_HCACHE];
+
+static void *ij_halloc(size_t bytes)
+{
+   int best = -1;
+   for (int k = 0; k < GB_IJ_HCACHE; k++)
+   {
+      if (!g_hcache[k]) { continue; }
+      size_t have = *(size_t *) g_hcache[k];
+      if (have >= bytes && have <= 2 * bytes + (1 << 20) &&
+          (best < 0 || have < *(size_t *) g_hcache[best])) { best = k; }
+   }
+   char *b;
+   if (best >= 0) { b = (char *) g_hcache[best]; g_hcache[best] = NULL; }
+   else
+   {
+      b = (char *) malloc(bytes + 16);
+      if (!b) { return NULL; }
+      *(size_t *) b = bytes;
+   }
+   return b + 16;
+}
+
+static void ij_hfree(void *p)
+{
+   if (!p) { return; }
+   char *b = (char *) p - 16;
+   if (*(size_t *) b >= (1 << 20))
+   {
+      for (int k = 0; k < GB_IJ_HCACHE; k++)
+      {
+         if (!g_hcache[k]) { g_hcache[k] = b; return; }
+      }
+   }
+   free(b);
+}
+
+void gb_ij_release_host_cache(void)
+{
+   for (int k = 0; k < GB_IJ_HCACHE; k++) { free(g_hcache[k]); g_hcache[k] = NULL; }
 }
 
 HYPRE_Int HYPRE_IJMatrixCreate(MPI_Comm comm, HYPRE_BigInt ilower, HYPRE_BigInt iupper, HYPRE_BigInt jlower,
@@ -623,9 +673,19 @@ HYPRE_Int HYPRE_IJMatrixSetRowSizes(HYPRE_IJMatrix m, const HYPRE_Int *sizes)
 {
    if (!check_ijm(m, 1)) { return gb_error_flag; }
    if (!sizes) { gb_error_in_arg(2); return gb_error_flag; }
-   free(m->hint);
-   m->hint = (int *) malloc(sizeof(int) * (size_t) (m->nrows ? m->nrows : 1));
-   memcpy(m->hint, sizes, sizeof(int) * (size_t) m->nrows);
+   ij_hfree(m->hint);
+   m->hint = (int *) ij_halloc(sizeof(int) * (size_t) (m->nrows ? m->nrows : 1));
+   if (!m->hint) { gb_error(HYPRE_ERROR_MEMORY, "IJ row sizes"); return gb_error_flag; }
+   int mn = 1;
+   int *h = m->hint;
+   const int nr = m->nrows;
+   #pragma omp parallel for reduction(min : mn) schedule(static) if (nr > 100000)
+   for (int r = 0; r < nr; r++)
+   {
+      h[r] = sizes[r];
+      mn = sizes[r] < mn ? sizes[r] : mn;
+   }
+   m->hint_zero = mn <= 0;
    return gb_error_flag;
 }
 
@@ -648,7 +708,7 @@ static void ijm_free_stage(HYPRE_IJMatrix m)
    m->row_state = NULL; m->dev_off = NULL;
    gb_dfree(m->st_cols); gb_dfree(m->st_vals); gb_dfree(m->st_rowptr);
    m->st_cols = NULL; m->st_vals = NULL; m->st_rowptr = NULL;
-   free(m->st_hstart);
+   ij_hfree(m->st_hstart);
    m->st_hstart = NULL;
    m->st_len = m->st_cap = 0;
 }
@@ -693,7 +753,7 @@ static int ijm_host_ready(HYPRE_IJMatrix m)
          m->row_len[r] = m->st_hstart[r + 1] - m->st_hstart[r];
          m->row_state[r] = GB_IJ_ROW_DEVICE;
       }
-      free(m->st_hstart);
+      ij_hfree(m->st_hstart);
       m->st_hstart = NULL;
    }
    return 1;
@@ -797,6 +857,47 @@ static int ijm_migrate(HYPRE_IJMatrix m)
    return 1;
 }
 
+/* hstart[t] = the offset of the put's row t (an exclusive scan of ncols,
+ * hstart[nrows] = the total), in blocks on the host's threads; returns
+ * whether the put lists rows ilower, ilower + 1, ... in order */
+static int ij_offsets(int nrows, const int *rows, int ilower, const int *ncols, int *hstart)
+{
+   enum { NB = 64 };
+   long long bsum[NB + 1];
+   int bord[NB];
+   const int nb = nrows > 100000 ? NB : 1;
+   #pragma omp parallel for schedule(static) if (nb > 1)
+   for (int b = 0; b < nb; b++)
+   {
+      const int t0 = (int) ((long long) nrows * b / nb), t1 = (int) ((long long) nrows * (b + 1) / nb);
+      long long acc = 0;
+      int ord = 1;
+      for (int t = t0; t < t1; t++)
+      {
+         ord &= rows[t] - ilower == t;
+         acc += ncols[t];
+      }
+      bsum[b + 1] = acc;
+      bord[b] = ord;
+   }
+   bsum[0] = 0;
+   int inorder = 1;
+   for (int b = 0; b < nb; b++) { bsum[b + 1] += bsum[b]; inorder &= bord[b]; }
+   #pragma omp parallel for schedule(static) if (nb > 1)
+   for (int b = 0; b < nb; b++)
+   {
+      const int t0 = (int) ((long long) nrows * b / nb), t1 = (int) ((long long) nrows * (b + 1) / nb);
+      long long acc = bsum[b];
+      for (int t = t0; t < t1; t++)
+      {
+         hstart[t] = (int) acc;
+         acc += ncols[t];
+      }
+   }
+   hstart[nrows] = (int) bsum[nb];
+   return inorder;
+}
+
 /* SetValues of new rows with many entries: copied from the caller's buffers
  * to the device staging and checked there (columns in range, none repeated
  * within a row).  Returns 1 when the put was taken, 0 when the host path must
@@ -809,14 +910,17 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
    /* sizes first, so the copies of the caller's buffers start before the row
     * checks (they overlap when the buffers are pinned) */
    long long tot = 0;
+   int mn = 0;
+   #pragma omp parallel for reduction(+ : tot) reduction(min : mn) schedule(static) if (nrows > 100000)
    for (int t = 0; t < nrows; t++)
    {
-      if (ncols[t] < 0) { return 0; }
+      mn = ncols[t] < mn ? ncols[t] : mn;
       tot += ncols[t];
    }
+   if (mn < 0) { return 0; }
    if (tot < GB_IJ_DEVICE_MIN || tot > 0x7fffffffLL) { return 0; }
-   int *hstart = (int *) malloc(sizeof(int) * (size_t) (nrows + 1));
-   if (!hstart || !ijm_staging_reserve(m, m->st_len + tot)) { free(hstart); return 0; }
+   int *hstart = (int *) ij_halloc(sizeof(int) * (size_t) (nrows + 1));
+   if (!hstart || !ijm_staging_reserve(m, m->st_len + tot)) { ij_hfree(hstart); return 0; }
    cudaStream_t s = gb_stream();
    cudaMemcpyAsync(m->st_cols + m->st_len, cols, sizeof(int) * (size_t) tot, cudaMemcpyHostToDevice, s);
    cudaMemcpyAsync(m->st_vals + m->st_len, values, sizeof(double) * (size_t) tot, cudaMemcpyHostToDevice, s);
@@ -824,15 +928,7 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
    {
       /* no row holds data yet: a put of every row in order needs no per-row
        * host state (its offsets are the CSR row pointers) */
-      int inorder = 1;
-      long long acc = 0;
-      hstart[0] = 0;
-      for (int t = 0; t < nrows; t++)
-      {
-         inorder &= rows[t] - m->ilower == t;
-         acc += ncols[t];
-         hstart[t + 1] = (int) acc;
-      }
+      const int inorder = ij_offsets(nrows, rows, m->ilower, ncols, hstart);
       if (inorder)
       {
          int *dstart = (int *) gb_dmalloc(sizeof(int) * (size_t) (nrows + 1));
@@ -846,14 +942,14 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
          }
          else { gb_sync(); }
          gb_dfree(flags);
-         if (f != 0) { gb_dfree(dstart); free(hstart); return 0; }
+         if (f != 0) { gb_dfree(dstart); ij_hfree(hstart); return 0; }
          m->st_len = tot;
          m->st_rowptr = dstart;
          m->st_hstart = hstart;
          return 1;
       }
    }
-   if (!ijm_host_ready(m)) { gb_sync(); free(hstart); return 0; }
+   if (!ijm_host_ready(m)) { gb_sync(); ij_hfree(hstart); return 0; }
    /* row offsets within the put; every row valid, new and not repeated in
     * this put (marked pending, unmarked on failure); whether the put is the
     * whole matrix in row order (its offsets are then the CSR row pointers) */
@@ -889,7 +985,7 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
    {
       for (int u = 0; u < (ok ? nrows : t); u++) { m->row_state[rows[u] - m->ilower] = 0; }
       gb_dfree(dstart);
-      free(hstart);
+      ij_hfree(hstart);
       return 0;
    }
    for (int u = 0; u < nrows; u++)
@@ -902,7 +998,7 @@ static int ijm_put_device(HYPRE_IJMatrix m, int nrows, const int *ncols, const i
    m->st_len += tot;
    if (inorder) { m->st_rowptr = dstart; }
    else { gb_dfree(dstart); }
-   free(hstart);
+   ij_hfree(hstart);
    return 1;
 }
 
@@ -1094,9 +1190,7 @@ HYPRE_Int HYPRE_IJMatrixAssemble(HYPRE_IJMatrix m)
       int *key = NULL;
       if (m->hint && !m->swap_diag)
       {
-         int z = 0;
-         for (int r = 0; r < n && !z; r++) { z = m->hint[r] <= 0; }
-         if (z)
+         if (m->hint_zero)
          {
             /* some row was given no space: the front rule needs the row lengths */
             int *hI = (int *) malloc(sizeof(int) * (size_t) (n + 1));
@@ -1229,7 +1323,7 @@ HYPRE_Int HYPRE_IJMatrixDestroy(HYPRE_IJMatrix m)
 {
    if (!m || m->magic != GB_MAGIC_IJM) { return gb_error_flag; }
    ijm_free_stage(m);
-   free(m->hint);
+   ij_hfree(m->hint);
    if (m->par) { gb_parcsr_free(m->par); }
    m->magic = 0;
    free(m);

@@ -126,6 +126,8 @@ void       gb_parcsr_free(gb_parcsr *M);
 void       gb_csr_free(gb_csr *A);
 const gb_spmv_desc *gb_solve_desc(gb_parcsr *M, int vprec);   /* builds lazily */
 void gb_spmv_autotune(gb_spmv_desc *d, long long nnz);        /* gb_tune.c */
+void gb_spmm_autotune(int prec, int nrows, int ncols, long long nnz, int nv, const int *Ai, const int *Aj,
+                      const void *Av, void *x, void *y, int *T, int *U);
 /* strictly lower part of a large matrix for two-stage Gauss-Seidel (NULL for
  * small or wide-row matrices: the CSR kernel is used there); builds lazily */
 const gb_spmv_desc *gb_lower_desc(gb_parcsr *M, int vprec, const void **diag);
@@ -245,6 +247,7 @@ typedef struct
    /* multi-vector PCG (gb_multi.c); last_multi: the last solve had multi-vectors */
    int                  last_multi;
    int                  m_nv, m_n;
+   int                  m_shT, m_shU;     /* SpMM launch shape of the outer products */
    double              *m_r, *m_p, *m_s, *m_dev;
    int                 *m_iters;
    double              *m_relres, *m_hist;

@@ -182,12 +182,12 @@ void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, dou
  * receives u's values from before the sweep; ut: the scaled form's starting
  * values (NULL: unscaled); dvec: l1 norms or NULL (diagonal); flags: n + 1
  * ints; *err set when a dependency wait ran out */
-void gb_hgs_sweep_d(int n, const int *Ai, const int *Aj, const double *Av, const double *f, double *u, double *uo,
-                    const double *ut, const double *dvec, int dir, int skip, double w, double omega, int *flags,
-                    int *err, cudaStream_t s);
-void gb_hgs_sweep_f(int n, const int *Ai, const int *Aj, const float *Av, const float *f, float *u, float *uo,
-                    const float *ut, const float *dvec, int dir, int skip, double w, double omega, int *flags,
-                    int *err, cudaStream_t s);
+void gb_hgs_sweep_d(int n, long long nnz, const int *Ai, const int *Aj, const double *Av, const double *f,
+                    double *u, double *uo, const double *ut, const double *dvec, int dir, int skip, double w,
+                    double omega, int *flags, int *err, cudaStream_t s);
+void gb_hgs_sweep_f(int n, long long nnz, const int *Ai, const int *Aj, const float *Av, const float *f, float *u,
+                    float *uo, const float *ut, const float *dvec, int dir, int skip, double w, double omega,
+                    int *flags, int *err, cudaStream_t s);
 
 /* solve phase */
 void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int mode, double alpha, double beta,

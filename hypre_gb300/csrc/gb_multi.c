@@ -12,9 +12,9 @@
 
 int gb_mdot_blocks(void);
 void gb_spmm_d(int n, int nv, const int *Ai, const int *Aj, const double *Av, const double *x, double *y, int mode,
-               double alpha, double beta, const double *b, const double *d, double w, cudaStream_t s);
+               double alpha, double beta, const double *b, const double *d, double w, int T, int U, cudaStream_t s);
 void gb_spmm_f(int n, int nv, const int *Ai, const int *Aj, const float *Av, const float *x, float *y, int mode,
-               float alpha, float beta, const float *b, const float *d, float w, cudaStream_t s);
+               float alpha, float beta, const float *b, const float *d, float w, int T, int U, cudaStream_t s);
 void gb_mscaled_div_d(long long n, int nv, double w, const double *f, const double *d, double *u, cudaStream_t s);
 void gb_mscaled_div_f(long long n, int nv, float w, const float *f, const float *d, float *u, cudaStream_t s);
 void gb_mdense_d(int nc, int nv, const double *D, const double *f, double *u, cudaStream_t s);
@@ -35,6 +35,9 @@ typedef struct
    double *F[32], *U[32], *U2[32], *V[32];
    float  *Ff[32], *Uf[32], *U2f[32], *Vf[32];
    float  *Avf[32], *Pvf[32], *Rvf[32];
+   /* SpMM launch shapes (block size, rows of x in flight) per level of the
+    * operands A, R, P in FP64 [0] and FP32 [1] */
+   int     shA[32][2][2], shR[32][2][2], shP[32][2][2];
 } gb_multi_ws;
 
 void gb_multi_free(gb_amg *amg)
@@ -83,6 +86,29 @@ static gb_multi_ws *multi_ws(gb_amg *amg, int nv)
          gb_d2f_n(R->nnz, R->v, w->Rvf[l], s);
       }
    }
+   /* launch shapes of every operand, timed on the workspace's vectors */
+   for (int l = 0; l < amg->num_levels; l++)
+   {
+      gb_level *L = &amg->lev[l];
+      gb_csr *A = &L->A->A;
+      for (int pr = 0; pr < 2; pr++)
+      {
+         const int prec = pr ? GB_PREC_F32 : GB_PREC_F64;
+         void *x = pr ? (void *) w->Uf[l] : (void *) w->U[l], *y = pr ? (void *) w->Vf[l] : (void *) w->V[l];
+         gb_spmm_autotune(prec, L->n, L->n, A->nnz, nv, A->i, A->j, pr ? (const void *) w->Avf[l] : (const void *) A->v,
+                          x, y, &w->shA[l][pr][0], &w->shA[l][pr][1]);
+         if (L->P)
+         {
+            gb_csr *P = &L->P->A, *R = &L->R->A;
+            void *xc = pr ? (void *) w->Uf[l + 1] : (void *) w->U[l + 1];
+            void *yc = pr ? (void *) w->Ff[l + 1] : (void *) w->F[l + 1];
+            gb_spmm_autotune(prec, R->nr, L->n, R->nnz, nv, R->i, R->j, pr ? (const void *) w->Rvf[l] : (const void *) R->v,
+                             y, yc, &w->shR[l][pr][0], &w->shR[l][pr][1]);
+            gb_spmm_autotune(prec, P->nr, R->nr, P->nnz, nv, P->i, P->j, pr ? (const void *) w->Pvf[l] : (const void *) P->v,
+                             xc, x, &w->shP[l][pr][0], &w->shP[l][pr][1]);
+         }
+      }
+   }
    amg->multi_ws = w;
    return w;
 }
@@ -112,11 +138,11 @@ static void mcycle_d(gb_amg *amg, gb_multi_ws *w, int nv, const double *f0, doub
       gb_mscaled_div_d(L->n, nv, L->relax_w, F, L->l1, U, s);
       for (int sw = 1; sw < prm->num_sweeps[1]; sw++)
       {
-         gb_spmm_d(L->n, nv, A->i, A->j, A->v, U, w->U2[l], 1, 0.0, 0.0, F, L->l1, L->relax_w, s);
+         gb_spmm_d(L->n, nv, A->i, A->j, A->v, U, w->U2[l], 1, 0.0, 0.0, F, L->l1, L->relax_w, w->shA[l][0][0], w->shA[l][0][1], s);
          cudaMemcpyAsync(U, w->U2[l], sizeof(double) * (size_t) L->n * nv, cudaMemcpyDeviceToDevice, s);
       }
-      gb_spmm_d(L->n, nv, A->i, A->j, A->v, U, w->V[l], 2, -1.0, 1.0, F, NULL, 0.0, s);
-      gb_spmm_d(R->nr, nv, R->i, R->j, R->v, w->V[l], w->F[l + 1], 0, 1.0, 0.0, NULL, NULL, 0.0, s);
+      gb_spmm_d(L->n, nv, A->i, A->j, A->v, U, w->V[l], 2, -1.0, 1.0, F, NULL, 0.0, w->shA[l][0][0], w->shA[l][0][1], s);
+      gb_spmm_d(R->nr, nv, R->i, R->j, R->v, w->V[l], w->F[l + 1], 0, 1.0, 0.0, NULL, NULL, 0.0, w->shR[l][0][0], w->shR[l][0][1], s);
    }
    {
       int l = nl - 1;
@@ -132,17 +158,17 @@ static void mcycle_d(gb_amg *amg, gb_multi_ws *w, int nv, const double *f0, doub
       gb_csr *A = &L->A->A, *P = &L->P->A;
       const double *F = l ? w->F[l] : f0;
       double *U = l ? w->U[l] : u0;
-      gb_spmm_d(P->nr, nv, P->i, P->j, P->v, w->U[l + 1], w->U2[l], 0, 1.0, 1.0, U, NULL, 0.0, s);
+      gb_spmm_d(P->nr, nv, P->i, P->j, P->v, w->U[l + 1], w->U2[l], 0, 1.0, 1.0, U, NULL, 0.0, w->shP[l][0][0], w->shP[l][0][1], s);
       if (prm->num_sweeps[2] == 0)
       {
          cudaMemcpyAsync(U, w->U2[l], sizeof(double) * (size_t) L->n * nv, cudaMemcpyDeviceToDevice, s);
       }
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
-         if (sw == 0) { gb_spmm_d(L->n, nv, A->i, A->j, A->v, w->U2[l], U, 1, 0.0, 0.0, F, L->l1, L->relax_w, s); }
+         if (sw == 0) { gb_spmm_d(L->n, nv, A->i, A->j, A->v, w->U2[l], U, 1, 0.0, 0.0, F, L->l1, L->relax_w, w->shA[l][0][0], w->shA[l][0][1], s); }
          else
          {
-            gb_spmm_d(L->n, nv, A->i, A->j, A->v, U, w->U2[l], 1, 0.0, 0.0, F, L->l1, L->relax_w, s);
+            gb_spmm_d(L->n, nv, A->i, A->j, A->v, U, w->U2[l], 1, 0.0, 0.0, F, L->l1, L->relax_w, w->shA[l][0][0], w->shA[l][0][1], s);
             cudaMemcpyAsync(U, w->U2[l], sizeof(double) * (size_t) L->n * nv, cudaMemcpyDeviceToDevice, s);
          }
       }
@@ -165,11 +191,11 @@ static void mcycle_f(gb_amg *amg, gb_multi_ws *w, int nv, const double *f0, doub
       gb_mscaled_div_f(L->n, nv, wt, F, L->l1f, U, s);
       for (int sw = 1; sw < prm->num_sweeps[1]; sw++)
       {
-         gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], U, w->U2f[l], 1, 0.f, 0.f, F, L->l1f, wt, s);
+         gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], U, w->U2f[l], 1, 0.f, 0.f, F, L->l1f, wt, w->shA[l][1][0], w->shA[l][1][1], s);
          cudaMemcpyAsync(U, w->U2f[l], sizeof(float) * (size_t) L->n * nv, cudaMemcpyDeviceToDevice, s);
       }
-      gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], U, w->Vf[l], 2, -1.f, 1.f, F, NULL, 0.f, s);
-      gb_spmm_f(R->nr, nv, R->i, R->j, w->Rvf[l], w->Vf[l], w->Ff[l + 1], 0, 1.f, 0.f, NULL, NULL, 0.f, s);
+      gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], U, w->Vf[l], 2, -1.f, 1.f, F, NULL, 0.f, w->shA[l][1][0], w->shA[l][1][1], s);
+      gb_spmm_f(R->nr, nv, R->i, R->j, w->Rvf[l], w->Vf[l], w->Ff[l + 1], 0, 1.f, 0.f, NULL, NULL, 0.f, w->shR[l][1][0], w->shR[l][1][1], s);
    }
    {
       int l = nl - 1;
@@ -183,17 +209,17 @@ static void mcycle_f(gb_amg *amg, gb_multi_ws *w, int nv, const double *f0, doub
       gb_csr *A = &L->A->A, *P = &L->P->A;
       float *F = w->Ff[l], *U = w->Uf[l];
       float wt = (float) L->relax_w;
-      gb_spmm_f(P->nr, nv, P->i, P->j, w->Pvf[l], w->Uf[l + 1], w->U2f[l], 0, 1.f, 1.f, U, NULL, 0.f, s);
+      gb_spmm_f(P->nr, nv, P->i, P->j, w->Pvf[l], w->Uf[l + 1], w->U2f[l], 0, 1.f, 1.f, U, NULL, 0.f, w->shP[l][1][0], w->shP[l][1][1], s);
       if (prm->num_sweeps[2] == 0)
       {
          cudaMemcpyAsync(U, w->U2f[l], sizeof(float) * (size_t) L->n * nv, cudaMemcpyDeviceToDevice, s);
       }
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
-         if (sw == 0) { gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], w->U2f[l], U, 1, 0.f, 0.f, F, L->l1f, wt, s); }
+         if (sw == 0) { gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], w->U2f[l], U, 1, 0.f, 0.f, F, L->l1f, wt, w->shA[l][1][0], w->shA[l][1][1], s); }
          else
          {
-            gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], U, w->U2f[l], 1, 0.f, 0.f, F, L->l1f, wt, s);
+            gb_spmm_f(L->n, nv, A->i, A->j, w->Avf[l], U, w->U2f[l], 1, 0.f, 0.f, F, L->l1f, wt, w->shA[l][1][0], w->shA[l][1][1], s);
             cudaMemcpyAsync(U, w->U2f[l], sizeof(float) * (size_t) L->n * nv, cudaMemcpyDeviceToDevice, s);
          }
       }
@@ -263,6 +289,8 @@ int gb_pcg_multi(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
       k->m_relres = (double *) calloc((size_t) nv, sizeof(double));
       k->m_nv = nv;
       k->m_n = n;
+      gb_spmm_autotune(GB_PREC_F64, n, n, A->A.nnz, nv, A->A.i, A->A.j, A->A.v, k->m_p, k->m_s, &k->m_shT,
+                       &k->m_shU);
    }
    free(k->m_hist);
    k->m_hist = (double *) calloc((size_t) nv * (size_t) (k->max_iter + 1), sizeof(double));
@@ -277,7 +305,7 @@ int gb_pcg_multi(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
    gb_sync();
    for (int c = 0; c < nv; c++) { bi[c] = h[c]; active[c] = bi[c] > 0.0; k->m_iters[c] = 0; k->m_relres[c] = 0.0; }
    /* r = b - A x ; p = M r */
-   gb_spmm_d(n, nv, A->A.i, A->A.j, Av, x->d, k->m_r, 2, -1.0, 1.0, b->d, NULL, 0.0, st);
+   gb_spmm_d(n, nv, A->A.i, A->A.j, Av, x->d, k->m_r, 2, -1.0, 1.0, b->d, NULL, 0.0, k->m_shT, k->m_shU, st);
    mprecond(k, amg, n, nv, k->m_r, k->m_p);
    gb_mdot2(n, nv, k->m_r, k->m_p, k->m_r, part, out, st);
    cudaMemcpyAsync(h, out, sizeof(double) * 2 * nv, cudaMemcpyDeviceToHost, st);
@@ -296,7 +324,7 @@ int gb_pcg_multi(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
    while (any && it + 1 <= k->max_iter)
    {
       it++;
-      gb_spmm_d(n, nv, A->A.i, A->A.j, Av, k->m_p, k->m_s, 0, 1.0, 0.0, NULL, NULL, 0.0, st);
+      gb_spmm_d(n, nv, A->A.i, A->A.j, Av, k->m_p, k->m_s, 0, 1.0, 0.0, NULL, NULL, 0.0, k->m_shT, k->m_shU, st);
       gb_mdot2(n, nv, k->m_s, k->m_p, NULL, part, out, st);
       cudaMemcpyAsync(h, out, sizeof(double) * nv, cudaMemcpyDeviceToHost, st);
       gb_sync();

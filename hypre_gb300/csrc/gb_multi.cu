@@ -12,10 +12,18 @@ namespace
 
 inline int nblk(long long n, int b) { return (int) ((n + b - 1) / b); }
 
+__device__ __forceinline__ double mfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
 // Epilogue modes as the single-vector SpMV: 0 y = alpha s + beta b,
 // 1 Jacobi y = x + w (b - s) / d_i, 2 residual y = b - s.
-template <typename VT, typename XT>
-__global__ void __launch_bounds__(256) k_spmm_csr(int n, int nv, const int *__restrict__ Ai,
+// The row's column indices and values are loaded 32 at a time (one
+// coalesced load per lane) and broadcast by shuffles; U neighbour rows of x
+// are loaded before any of them is used, so U gathers per lane are in flight.
+// Each column's sum adds the row's terms in element order whatever U is, so
+// every U gives the same result.
+template <typename VT, typename XT, int U>
+__global__ void __launch_bounds__(512) k_spmm_csr(int n, int nv, const int *__restrict__ Ai,
                                                   const int *__restrict__ Aj, const VT *__restrict__ Av,
                                                   const XT *__restrict__ x, XT *y, int mode, XT alpha, XT beta,
                                                   const XT *b, const XT *d, XT w)
@@ -28,21 +36,43 @@ __global__ void __launch_bounds__(256) k_spmm_csr(int n, int nv, const int *__re
    {
       XT s0 = 0, s1 = 0;
       const int e = Ai[i + 1];
-      int k = Ai[i];
-      for (; k + 1 < e; k += 2)
+      for (int c = Ai[i]; c < e; c += 32)
       {
-         const int j0 = __ldg(Aj + k), j1 = __ldg(Aj + k + 1);
-         const XT a0 = (XT) __ldg(Av + k), a1 = (XT) __ldg(Av + k + 1);
-         const XT *x0 = x + (size_t) j0 * nv, *x1 = x + (size_t) j1 * nv;
-         if (c0) { s0 += a0 * __ldg(x0 + lane); s0 += a1 * __ldg(x1 + lane); }
-         if (c1) { s1 += a0 * __ldg(x0 + lane + 32); s1 += a1 * __ldg(x1 + lane + 32); }
-      }
-      if (k < e)
-      {
-         const int j0 = __ldg(Aj + k);
-         const XT a0 = (XT) __ldg(Av + k);
-         if (c0) { s0 += a0 * __ldg(x + (size_t) j0 * nv + lane); }
-         if (c1) { s1 += a0 * __ldg(x + (size_t) j0 * nv + lane + 32); }
+         const int k = c + lane;
+         int jl = 0;
+         XT al = 0;
+         if (k < e)
+         {
+            jl = __ldg(Aj + k);
+            al = (XT) __ldg(Av + k);
+         }
+         const int m = min(32, e - c);
+         for (int t = 0; t < m; t += U)
+         {
+            XT aa[U], xa[U], xb[U];
+#pragma unroll
+            for (int u = 0; u < U; u++)
+            {
+               const int tt = (t + u) & 31;
+               const int j = __shfl_sync(GB_FULL, jl, tt);
+               aa[u] = __shfl_sync(GB_FULL, al, tt);
+               const bool ok = t + u < m;
+               const XT *xr = x + (size_t) j * nv;
+               xa[u] = ok && c0 ? __ldg(xr + lane) : (XT) 0;
+               xb[u] = ok && c1 ? __ldg(xr + lane + 32) : (XT) 0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++)
+            {
+               if (t + u < m)
+               {
+                  // explicit fused multiply-adds: the same operation whatever
+                  // the compiler would contract in each unrolled variant
+                  if (c0) { s0 = mfma(aa[u], xa[u], s0); }
+                  if (c1) { s1 = mfma(aa[u], xb[u], s1); }
+               }
+            }
+         }
       }
       for (int h = 0; h < 2; h++)
       {
@@ -159,25 +189,37 @@ __global__ void k_mconvert(long long n, const A *__restrict__ a, B *__restrict__
 
 extern "C" int gb_mdot_blocks(void) { return MDOT_BLOCKS; }
 
-extern "C" void gb_spmm_d(int n, int nv, const int *Ai, const int *Aj, const double *Av, const double *x, double *y,
-                          int mode, double alpha, double beta, const double *b, const double *d, double w,
-                          cudaStream_t s)
+template <typename VT, typename XT>
+static void spmm_launch(int n, int nv, const int *Ai, const int *Aj, const VT *Av, const XT *x, XT *y, int mode,
+                        XT alpha, XT beta, const XT *b, const XT *d, XT w, int T, int U, cudaStream_t s)
 {
    if (n <= 0) { return; }
-   int blocks = nblk((long long) n * 32, 256);
-   if (blocks > 152 * 16) { blocks = 152 * 16; }
-   k_spmm_csr<double, double><<<blocks, 256, 0, s>>>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w);
+   if (T != 128 && T != 512) { T = 256; }
+   long long blocks = ((long long) n * 32 + T - 1) / T;
+   const long long cap = 152LL * 16 * 256 / T;
+   if (blocks > cap) { blocks = cap; }
+   const int nb = (int) blocks;
+   if (U == 1) { k_spmm_csr<VT, XT, 1><<<nb, T, 0, s>>>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w); }
+   else if (U == 4) { k_spmm_csr<VT, XT, 4><<<nb, T, 0, s>>>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w); }
+   else if (U == 8) { k_spmm_csr<VT, XT, 8><<<nb, T, 0, s>>>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w); }
+   else { k_spmm_csr<VT, XT, 2><<<nb, T, 0, s>>>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w); }
    GB_COUNT(1);
 }
 
-extern "C" void gb_spmm_f(int n, int nv, const int *Ai, const int *Aj, const float *Av, const float *x, float *y,
-                          int mode, float alpha, float beta, const float *b, const float *d, float w, cudaStream_t s)
+// T: block size (128, 256, 512; 0 = 256), U: neighbour rows of x in flight
+// per lane (1, 2, 4, 8; 0 = 2)
+extern "C" void gb_spmm_d(int n, int nv, const int *Ai, const int *Aj, const double *Av, const double *x, double *y,
+                          int mode, double alpha, double beta, const double *b, const double *d, double w, int T,
+                          int U, cudaStream_t s)
 {
-   if (n <= 0) { return; }
-   int blocks = nblk((long long) n * 32, 256);
-   if (blocks > 152 * 16) { blocks = 152 * 16; }
-   k_spmm_csr<float, float><<<blocks, 256, 0, s>>>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w);
-   GB_COUNT(1);
+   spmm_launch<double, double>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w, T, U, s);
+}
+
+extern "C" void gb_spmm_f(int n, int nv, const int *Ai, const int *Aj, const float *Av, const float *x, float *y,
+                          int mode, float alpha, float beta, const float *b, const float *d, float w, int T, int U,
+                          cudaStream_t s)
+{
+   spmm_launch<float, float>(n, nv, Ai, Aj, Av, x, y, mode, alpha, beta, b, d, w, T, U, s);
 }
 
 extern "C" void gb_mscaled_div_d(long long n, int nv, double w, const double *f, const double *d, double *u,

@@ -194,8 +194,11 @@ HYPRE_Int HYPRE_Initialize(void)
    return gb_error_flag;
 }
 
+void gb_ij_release_host_cache(void);
+
 HYPRE_Int HYPRE_Finalize(void)
 {
+   gb_ij_release_host_cache();
    if (g_initialized)
    {
       cudaStreamSynchronize(g_stream);

@@ -213,6 +213,90 @@ void gb_spmv_autotune(gb_spmv_desc *d, long long nnz)
    cache_save();
 }
 
+void gb_spmm_d(int n, int nv, const int *Ai, const int *Aj, const double *Av, const double *x, double *y, int mode,
+               double alpha, double beta, const double *b, const double *d, double w, int T, int U, cudaStream_t s);
+void gb_spmm_f(int n, int nv, const int *Ai, const int *Aj, const float *Av, const float *x, float *y, int mode,
+               float alpha, float beta, const float *b, const float *d, float w, int T, int U, cudaStream_t s);
+
+/* The launch shape of one sparse operand of the multi-vector cycle (SpMM on
+ * nv interleaved columns): block size {128, 256, 512} x neighbour rows in
+ * flight per lane {1, 2, 4, 8}, every shape summing each column in element
+ * order (identical results).  Timed with x and y as given (their contents
+ * are overwritten: y = A x), kept per (precision, nv, rows, columns, nonzeros)
+ * in the same cache as the SpMV shapes.  Defaults (256, 2) when tuning is off,
+ * the operand is small or the stream is being captured;
+ * $HYPRE_GB300_SPMM_SHAPE = "T,U" sets every operand's shape. */
+void gb_spmm_autotune(int prec, int nrows, int ncols, long long nnz, int nv, const int *Ai, const int *Aj,
+                      const void *Av, void *x, void *y, int *T, int *U)
+{
+   *T = 256;
+   *U = 2;
+   /* HYPRE_GB300_SPMM_SHAPE="T,U" sets the shape of every operand (tests) */
+   const char *forced = getenv("HYPRE_GB300_SPMM_SHAPE");
+   if (forced && forced[0])
+   {
+      int ft = 0, fu = 0;
+      if (sscanf(forced, "%d,%d", &ft, &fu) == 2 && (ft == 128 || ft == 256 || ft == 512) &&
+          (fu == 1 || fu == 2 || fu == 4 || fu == 8))
+      {
+         *T = ft;
+         *U = fu;
+      }
+      return;
+   }
+   if (!tune_enabled() || nrows < GB_TUNE_MIN_ROWS) { return; }
+   cudaStream_t s = gb_stream();
+   enum cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) { cudaGetLastError(); return; }
+   cache_load();
+   char key[GB_TUNE_KEY];
+   snprintf(key, GB_TUNE_KEY, "spmm:%s:nv%d:%d:%d:%lld", prec == GB_PREC_F64 ? "f64" : "f32", nv, nrows, ncols, nnz);
+   tune_entry *hit = tab_find(key);
+   if (hit) { *T = hit->T; *U = hit->D; return; }
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0);
+   cudaEventCreate(&e1);
+   static const int Ts[3] = {128, 256, 512}, Us[4] = {1, 2, 4, 8};
+   tune_entry best;
+   memset(&best, 0, sizeof(best));
+   best.us = 1e30;
+   for (int a = 0; a < 3; a++)
+   {
+      for (int c = 0; c < 4; c++)
+      {
+         const int reps = 5;
+         for (int r = -2; r < reps; r++)
+         {
+            if (r == 0) { cudaEventRecord(e0, s); }
+            if (prec == GB_PREC_F64)
+            {
+               gb_spmm_d(nrows, nv, Ai, Aj, (const double *) Av, (const double *) x, (double *) y, 0, 1.0, 0.0, NULL,
+                         NULL, 0.0, Ts[a], Us[c], s);
+            }
+            else
+            {
+               gb_spmm_f(nrows, nv, Ai, Aj, (const float *) Av, (const float *) x, (float *) y, 0, 1.f, 0.f, NULL,
+                         NULL, 0.f, Ts[a], Us[c], s);
+            }
+         }
+         cudaEventRecord(e1, s);
+         cudaEventSynchronize(e1);
+         float ms = 0.f;
+         cudaEventElapsedTime(&ms, e0, e1);
+         const double us = 1e3 * ms / reps;
+         if (us < best.us) { best.us = us; best.T = Ts[a]; best.D = Us[c]; }
+      }
+   }
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   if (cudaGetLastError() != cudaSuccess || best.us >= 1e30) { return; }
+   *T = best.T;
+   *U = best.D;
+   tune_entry *e = tab_add(key);
+   if (e) { e->T = best.T; e->D = best.D; e->K = 0; e->us = best.us; }
+   cache_save();
+}
+
 /* the shape a form was given (tests and diagnostics) */
 HYPRE_Int HYPRE_GB300_ParCSRMatrixGetSpMVShape(HYPRE_ParCSRMatrix A, HYPRE_Int precision, HYPRE_Int *format,
                                                HYPRE_Int *block, HYPRE_Int *depth_or_lanes)

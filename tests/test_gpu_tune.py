@@ -108,3 +108,58 @@ def test_tuned_solve_matches_default_and_cache_written(gb, tmp_path, monkeypatch
     entries = json.load(open(cache))
     key = "sell:f64v32:i16:%d:%d" % (n, len(J))
     assert key in entries and entries[key][:2] == [s1[1], s1[2]], (entries, s1)
+
+
+def _multi_solve(gb, O, I, J, V, B, prec):
+    n, nv = B.shape
+    A = gb.IJMatrix(I, J, V)
+    amg = gb.BoomerAMG(MaxRowSum=1.0, StrongThreshold=0.5, Tol=0.0, MaxIter=1)
+    amg.set("CyclePrecision", prec)
+    k = gb.Krylov("pcg", tol=1e-8, maxit=100, amg=amg)
+    b1, x1 = gb.IJVector(n, B[:, 0]), gb.IJVector(n, np.zeros(n))
+    k.setup(A, b1, x1)
+    Bm, Xm = gb.MultiVector(B), gb.MultiVector(np.zeros((n, nv)))
+    assert gb.lib().HYPRE_ParCSRPCGSolve(k.h, A.par, Bm.par, Xm.par) == 0
+    its, rel, hist = gb.multi_results(k, nv, 100)
+    X = Xm.values()
+    for o in (k, amg, x1, b1, A):
+        o.destroy()
+    return its, hist, X
+
+
+def test_spmm_shapes_identical(gb, oracle_mod, monkeypatch):
+    """Every SpMM launch shape (block 128/256/512 x 1/2/4/8 rows of x in
+    flight) gives the multi-vector PCG the same iterations, histories and
+    solution, bit for bit, in the FP64 and the FP32 cycle."""
+    O = oracle_mod
+    I, J, V = O.stencil(27, 30, 30, 30)              # 27,000 rows: tuned operands
+    n, nv = len(I) - 1, 6
+    B = np.stack([O.rand_uniform(n, 500 + c) for c in range(nv)], 1)
+    for prec in (0, 1):
+        monkeypatch.setenv("HYPRE_GB300_SPMM_SHAPE", "256,2")
+        ref = _multi_solve(gb, O, I, J, V, B, prec)
+        for T in (128, 256, 512):
+            for U in (1, 2, 4, 8):
+                monkeypatch.setenv("HYPRE_GB300_SPMM_SHAPE", f"{T},{U}")
+                its, hist, X = _multi_solve(gb, O, I, J, V, B, prec)
+                assert np.array_equal(its, ref[0]), (prec, T, U)
+                assert len(hist) == len(ref[1])
+                assert all(np.array_equal(a, b) for a, b in zip(hist, ref[1])), (prec, T, U)
+                assert np.array_equal(X, ref[2]), (prec, T, U)
+
+
+def test_spmm_tuned_cache_written(gb, oracle_mod, tmp_path, monkeypatch):
+    O = oracle_mod
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("HYPRE_GB300_TUNE_CACHE", str(cache))
+    monkeypatch.delenv("HYPRE_GB300_SPMM_SHAPE", raising=False)
+    gb.lib().HYPRE_GB300_SetAutotune(1)
+    I, J, V = O.stencil(27, 29, 30, 31)              # shapes no other test tunes
+    n, nv = len(I) - 1, 7
+    B = np.stack([O.rand_uniform(n, 900 + c) for c in range(nv)], 1)
+    its, hist, X = _multi_solve(gb, O, I, J, V, B, 0)
+    entries = json.load(open(cache))
+    key = "spmm:f64:nv%d:%d:%d:%d" % (nv, n, n, len(J))
+    assert key in entries, sorted(entries)
+    T, U = entries[key][:2]
+    assert T in (128, 256, 512) and U in (1, 2, 4, 8)
