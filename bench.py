@@ -307,7 +307,8 @@ def gpu_arm(args):
                       "column indices" % ("FP32" if prec == 1 else "FP16 (row-scaled)"),
                       "launch_shape": _spmv_shape(L, step_mats.get(src[1].value), prec),
                       "achieved": byt.value / sec.value / 1e9, "peak": peak, "unit": "GB/s",
-                      "frac": byt.value / sec.value / 1e9 / peak, "traffic": None,
+                      "frac": byt.value / sec.value / 1e9 / peak,
+                      "traffic": _traffic_file("spmv_%s_traffic.json" % label, "bytes_per_launch"),
                       "algorithmic_bytes": byt.value, "launch_seconds": sec.value,
                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
     # the reported mixed-precision path: the faster of the FP32 cycle and the
@@ -481,6 +482,15 @@ def _spmv_shape(L, A, prec):
     L.HYPRE_GB300_ParCSRMatrixGetSpMVShape(A, prec, C.byref(f), C.byref(b), C.byref(d))
     return {"format": "SELL-32" if f.value == 1 else "CSR", "block": b.value,
             ("prefetch_depth" if f.value == 1 else "lanes_per_row"): d.value}
+
+
+def _traffic_file(name, key):
+    """A DRAM-traffic figure (ncu dram__bytes_read.sum + dram__bytes_write.sum)
+    committed under profiles/, or None."""
+    tf = os.path.join(ROOT, "profiles", name)
+    if os.path.exists(tf):
+        return json.load(open(tf)).get(key)
+    return None
 
 
 def ref_binary():
