@@ -69,7 +69,7 @@ def parse():
                     help="with --spmv-only: 0 the matrix's FP64 form, 1 the FP32 and 2 the FP16-valued level-0 "
                          "form of a setup with that cycle precision")
     ap.add_argument("--workload", default="laplace27_160",
-                    choices=["laplace27_160", "batch512", "multi64", "learned128", "fv256", "spgemm128"],
+                    choices=["laplace27_160", "batch512", "multi64", "learned128", "fv256", "spgemm128", "mlp4m"],
                     help="laplace27_160: the headline line; the others measure the batched, multi-RHS, "
                          "learned-parameter and mixed-precision FV configurations and the reference's "
                          "SpGEMM benchmark (A*A)")
@@ -762,6 +762,57 @@ def suite_arm(args):
                "roofline": {"bound": "hbm", "achieved": top["achieved_gbs"], "peak": peak, "unit": "GB/s",
                             "frac": top["frac"], "traffic": None,
                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}})
+        return
+    if args.workload == "mlp4m":
+        # the learned part's dense layers alone: forward and gradient of the
+        # per-row MLP (16 -> 64 -> 64 -> 2, BF16 inputs, FP32 accumulation) on
+        # 4,194,304 rows of random features (inputs larger than L2)
+        from hypre_gb300 import learned
+        N = 1 << 22
+        gen = torch.Generator(device="cuda").manual_seed(5)
+        X = torch.randn((N, 16), generator=gen, device="cuda").to(torch.bfloat16)
+        T = torch.randn((N, 2), generator=gen, device="cuda")
+        P = torch.as_tensor(np.asarray(learned.init_params(0), np.float32), device="cuda")
+        out = torch.empty((N, 2), dtype=torch.float32, device="cuda")
+        g = torch.empty(learned.nparam(), dtype=torch.float32, device="cuda")
+        loss = torch.empty(1, dtype=torch.float32, device="cuda")
+        sp = C.c_void_p(); L.HYPRE_GB300_GetStream(C.byref(sp))
+        lst = torch.cuda.ExternalStream(sp.value)
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        torch.cuda.synchronize()
+
+        def timed_op(fn):
+            for _ in range(max(3, args.warmup)):
+                fn()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(lst)
+            for _ in range(args.steps):
+                fn()
+            e1.record(lst)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / 1e3 / args.steps
+
+        tf = timed_op(lambda: gb.check(L.HYPRE_GB300_MLPForward(N, ptr(X), ptr(P), ptr(out)), "forward"))
+        tg = timed_op(lambda: gb.check(L.HYPRE_GB300_MLPGradient(N, ptr(X), ptr(T), ptr(P), ptr(g), ptr(loss)),
+                                       "gradient"))
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        bf16 = float(peaks.get("bf16_tflops", 1900.0))
+        fl_f = 2.0 * (16 * 64 + 64 * 64 + 64 * 2) * N          # forward multiply-adds x 2
+        fl_g = 3.0 * fl_f                                      # forward + two backward products per layer
+        by_f = (32 + 8) * N                                    # BF16 features in, FP32 outputs out
+        by_g = (32 + 8) * N                                    # BF16 features and FP32 targets in
+        _line("MLP forward seconds, 4,194,304 rows (16 -> 64 -> 64 -> 2, BF16 tensor cores)", tf, "s", args,
+              {"workload": "mlp_4m_rows", "layers": [16, 64, 64, 2], "l2": "inputs larger than L2, no flush"},
+              "bf16 in / fp32 accumulate",
+              {"gradient_seconds": tg,
+               "forward": {"tflops": fl_f / tf / 1e12, "frac_of_bf16_peak": fl_f / tf / 1e12 / bf16,
+                           "gbs": by_f / tf / 1e9, "frac_of_hbm": by_f / tf / 1e9 / hbm},
+               "gradient": {"tflops": fl_g / tg / 1e12, "frac_of_bf16_peak": fl_g / tg / 1e12 / bf16,
+                            "gbs": by_g / tg / 1e9, "frac_of_hbm": by_g / tg / 1e9 / hbm},
+               "peaks": {"bf16_tflops": bf16, "hbm_gbs": hbm, "source": "MEASURED_PEAKS.json"}})
         return
     if args.workload == "batch512":
         I, J, V, off, ns, eps = G.aniso2d_batch(512, seed=11)

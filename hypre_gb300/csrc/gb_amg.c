@@ -1428,7 +1428,9 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    while (1)
    {
       int n = amg->lev[level].n;
-      if (level == maxl - 1 || n <= prm->max_coarse_size) { break; }
+      /* the size test follows each coarsening (par_amg_setup.c:3136-3143):
+       * the finest level is coarsened even when it is within max_coarse_size */
+      if (level == maxl - 1) { break; }
       int r = setup_level(amg, level, amg->setup_times);
       if (r < 0) { amg->num_levels = level + 1; return gb_error_flag; }
       if (r == 0) { break; }
@@ -1985,39 +1987,46 @@ HYPRE_Int HYPRE_BoomerAMGSolve(HYPRE_Solver solver, HYPRE_ParCSRMatrix A, HYPRE_
    int n = A->A.nr;
    cudaStream_t s = gb_stream();
    gb_amg_params *prm = &a->prm;
-   /* as a preconditioner (max_iter 1, tol 0) the caller passes x = 0 */
-   double bnorm = 0.0, rel = 0.0;
-   int check = prm->tol > 0.0;
+   /* hypre_BoomerAMGSolve (par_amg_solve.c:150-342): the relative residual
+    * ||b - A x|| / ||b|| (absolute when b = 0; 1 when tol = 0) before the
+    * loop and after every cycle; cycles while it is >= tol and fewer than
+    * max_iter ran; running into max_iter with tol > 0 is a convergence error */
+   const int check = prm->tol > 0.0;
+   double *r = a->r_work;
+   double rel = 1.0, rhs = 0.0;
    if (check)
    {
-      bnorm = sqrt(gb_dot(n, b->d, b->d));
-      if (bnorm == 0.0) { gb_fill_d(n, x->d, 0.0, s); a->num_iterations = 0; a->rel_resid = 0.0; return gb_error_flag; }
-   }
-   double *r = a->r_work;
-   double *e = a->lev[0].U2 == NULL ? NULL : NULL;
-   (void) e;
-   int iter = 0;
-   /* correction form: r = b - A x ; x += M^{-1} r (mathematically the
-    * reference's cycle on (b, x)) */
-   double *corr = (double *) gb_scratch(5, sizeof(double) * (size_t) n);
-   while (iter < prm->max_iter)
-   {
       gb_spmv_d(gb_solve_desc(A, GB_PREC_F64), x->d, r, 2, -1.0, 1.0, b->d, NULL, 0.0, NULL, NULL, s);
+      const double res = sqrt(gb_dot(n, r, r));
+      rhs = sqrt(gb_dot(n, b->d, b->d));
+      rel = rhs != 0.0 ? res / rhs : res;
+   }
+   int iter = 0;
+   double *corr = prm->cycle_prec == GB_PREC_F64 ? NULL : (double *) gb_scratch(5, sizeof(double) * (size_t) n);
+   while (rel >= prm->tol && iter < prm->max_iter)
+   {
+      if (!corr)
+      {
+         /* FP64: the V-cycle on (b, x) in place, as the reference */
+         cycle_d(a, b->d, x->d, 0);
+      }
+      else
+      {
+         /* FP32 / FP16 cycles: iterative refinement, x += M^{-1} (b - A x)
+          * with the FP64 residual */
+         gb_spmv_d(gb_solve_desc(A, GB_PREC_F64), x->d, r, 2, -1.0, 1.0, b->d, NULL, 0.0, NULL, NULL, s);
+         gb_amg_cycle(a, r, corr);
+         gb_axpy_d(n, 1.0, corr, x->d, s);
+      }
+      iter++;
       if (check)
       {
-         rel = sqrt(gb_dot(n, r, r)) / bnorm;
-         if (rel < prm->tol) { break; }
+         gb_spmv_d(gb_solve_desc(A, GB_PREC_F64), x->d, r, 2, -1.0, 1.0, b->d, NULL, 0.0, NULL, NULL, s);
+         const double res = sqrt(gb_dot(n, r, r));
+         rel = rhs != 0.0 ? res / rhs : res;
       }
-      gb_amg_cycle(a, r, corr);
-      gb_axpy_d(n, 1.0, corr, x->d, s);
-      iter++;
    }
-   if (check && iter == prm->max_iter)
-   {
-      gb_spmv_d(gb_solve_desc(A, GB_PREC_F64), x->d, r, 2, -1.0, 1.0, b->d, NULL, 0.0, NULL, NULL, s);
-      rel = sqrt(gb_dot(n, r, r)) / bnorm;
-      if (rel >= prm->tol) { gb_error(HYPRE_ERROR_CONV, NULL); }
-   }
+   if (check && iter == prm->max_iter) { gb_error(HYPRE_ERROR_CONV, NULL); }
    a->num_iterations = iter;
    a->rel_resid = rel;
    gb_amg_check_sweeps();

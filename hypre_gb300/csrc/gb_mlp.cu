@@ -163,29 +163,115 @@ __device__ __forceinline__ void load_x_tile(WarpTiles &T, const bf16 *__restrict
 
 } // namespace
 
-// Inference: out[row][0..1] = MLP(X[row]).
-__global__ void __launch_bounds__(32 * MLP_WARPS) k_mlp_forward(long long N, const bf16 *__restrict__ X,
-                                                                const bf16 *__restrict__ W,
-                                                                const float *__restrict__ P, float *__restrict__ out)
+// Inference: out[row][0..1] = MLP(X[row]).  Each warp streams 16-row tiles.
+// The weights' B fragments stay in registers for the whole kernel (loaded
+// once as 32-bit pairs: W is stored [n][k], so a fragment's two k-neighbours
+// are adjacent), the features' A fragment is four 32-bit loads straight from
+// X (rows of 16 BF16), and a layer's C fragments of n-tiles 2kt and 2kt+1
+// are, after bias, ReLU and rounding to BF16, exactly the next layer's A
+// fragment of k-tile kt -- no shared memory between the layers.  The next
+// tile's features are loaded while the current tile is computed.  The
+// products, sums and roundings are those of the tile-by-tile form of the
+// training kernel's forward pass.
+namespace
 {
-   __shared__ WarpTiles tiles[MLP_WARPS];
-   WarpTiles &T = tiles[threadIdx.x >> 5];
-   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+__device__ __forceinline__ unsigned ld_pair(const bf16 *p) { return *reinterpret_cast<const unsigned *>(p); }
+
+__device__ __forceinline__ unsigned relu_pack(float x, float y)
+{
+   return pack2(__float2bfloat16_rn(fmaxf(x, 0.f)), __float2bfloat16_rn(fmaxf(y, 0.f)));
+}
+
+__device__ __forceinline__ void load_x_frag(unsigned *a, const bf16 *__restrict__ X, long long row0, long long N,
+                                            int g, int t)
+{
+   const long long r0 = row0 + g, r1 = row0 + g + 8;
+   a[0] = r0 < N ? ld_pair(X + r0 * MLP_IN + 2 * t) : 0u;
+   a[1] = r1 < N ? ld_pair(X + r1 * MLP_IN + 2 * t) : 0u;
+   a[2] = r0 < N ? ld_pair(X + r0 * MLP_IN + 2 * t + 8) : 0u;
+   a[3] = r1 < N ? ld_pair(X + r1 * MLP_IN + 2 * t + 8) : 0u;
+}
+} // namespace
+
+__global__ void __launch_bounds__(32 * MLP_WARPS, 3) k_mlp_forward(long long N, const bf16 *__restrict__ X,
+                                                                   const bf16 *__restrict__ W,
+                                                                   const float *__restrict__ P,
+                                                                   float *__restrict__ out)
+{
+   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+   const bf16 *W1 = W + BW_W1, *W2 = W + BW_W2, *W3 = W + BW_W3;
+   // B fragments: W1 (k 16, n 64), W2 (k 64, n 64), W3 (k 64, n 8 padded)
+   unsigned w1[8][2], w2[8][4][2], w3[4][2];
+   float bb1[8][2], bb2[8][2];
+#pragma unroll
+   for (int nt = 0; nt < 8; nt++)
+   {
+      const bf16 *r1 = W1 + (nt * 8 + g) * MLP_IN;
+      w1[nt][0] = ld_pair(r1 + 2 * t);
+      w1[nt][1] = ld_pair(r1 + 2 * t + 8);
+      const bf16 *r2 = W2 + (nt * 8 + g) * MLP_H;
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++)
+      {
+         w2[nt][kt][0] = ld_pair(r2 + kt * 16 + 2 * t);
+         w2[nt][kt][1] = ld_pair(r2 + kt * 16 + 2 * t + 8);
+      }
+      bb1[nt][0] = P[OFF_B1 + nt * 8 + 2 * t];
+      bb1[nt][1] = P[OFF_B1 + nt * 8 + 2 * t + 1];
+      bb2[nt][0] = P[OFF_B2 + nt * 8 + 2 * t];
+      bb2[nt][1] = P[OFF_B2 + nt * 8 + 2 * t + 1];
+   }
+#pragma unroll
+   for (int kt = 0; kt < 4; kt++)
+   {
+      const bf16 *r3 = W3 + g * MLP_H;
+      w3[kt][0] = ld_pair(r3 + kt * 16 + 2 * t);
+      w3[kt][1] = ld_pair(r3 + kt * 16 + 2 * t + 8);
+   }
+   const float b30 = P[OFF_B3], b31 = P[OFF_B3 + 1];
    const long long ntiles = (N + 15) / 16;
    const long long wid = (long long) blockIdx.x * MLP_WARPS + (threadIdx.x >> 5);
    const long long nw = (long long) gridDim.x * MLP_WARPS;
+   unsigned ax[4];
+   if (wid < ntiles) { load_x_frag(ax, X, wid * 16, N, g, t); }
    for (long long tile = wid; tile < ntiles; tile += nw)
    {
-      long long row0 = tile * 16;
-      load_x_tile(T, X, row0, N);
-      float o[4];
-      forward_tile(T, W, P, o);
+      const long long row0 = tile * 16;
+      unsigned a1[4] = {ax[0], ax[1], ax[2], ax[3]};
+      if (tile + nw < ntiles) { load_x_frag(ax, X, (tile + nw) * 16, N, g, t); }
+      // layer 1 -> A fragments of layer 2 (k-tile kt = n-tiles 2kt, 2kt+1)
+      unsigned a2[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++)
+      {
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+         mma16816(c, a1, w1[nt]);
+         a2[nt >> 1][(nt & 1) * 2 + 0] = relu_pack(c[0] + bb1[nt][0], c[1] + bb1[nt][1]);
+         a2[nt >> 1][(nt & 1) * 2 + 1] = relu_pack(c[2] + bb1[nt][0], c[3] + bb1[nt][1]);
+      }
+      // layer 2 -> A fragments of layer 3
+      unsigned a3[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++)
+      {
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+         for (int kt = 0; kt < 4; kt++) { mma16816(c, a2[kt], w2[nt][kt]); }
+         a3[nt >> 1][(nt & 1) * 2 + 0] = relu_pack(c[0] + bb2[nt][0], c[1] + bb2[nt][1]);
+         a3[nt >> 1][(nt & 1) * 2 + 1] = relu_pack(c[2] + bb2[nt][0], c[3] + bb2[nt][1]);
+      }
+      // layer 3 (8 padded outputs; lanes t == 0 hold outputs 0 and 1)
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++) { mma16816(o, a3[kt], w3[kt]); }
       if (t == 0)
       {
-         if (row0 + g < N) { out[(row0 + g) * 2] = o[0]; out[(row0 + g) * 2 + 1] = o[1]; }
-         if (row0 + g + 8 < N) { out[(row0 + g + 8) * 2] = o[2]; out[(row0 + g + 8) * 2 + 1] = o[3]; }
+         if (row0 + g < N) { *reinterpret_cast<float2 *>(out + (row0 + g) * 2) = make_float2(o[0] + b30, o[1] + b31); }
+         if (row0 + g + 8 < N)
+         {
+            *reinterpret_cast<float2 *>(out + (row0 + g + 8) * 2) = make_float2(o[2] + b30, o[3] + b31);
+         }
       }
-      __syncwarp();
    }
 }
 
@@ -479,7 +565,7 @@ extern "C" void gb_mlp_forward(long long N, const void *X, const void *W, const 
 {
    long long tiles = (N + 15) / 16;
    long long blocks = (tiles + MLP_WARPS - 1) / MLP_WARPS;
-   int grid = (int) (blocks < 152 * 16 ? (blocks > 0 ? blocks : 1) : 152 * 16);
+   int grid = (int) (blocks < 152 * 3 ? (blocks > 0 ? blocks : 1) : 152 * 3);
    k_mlp_forward<<<grid, 32 * MLP_WARPS, 0, s>>>(N, (const bf16 *) X, (const bf16 *) W, P, out);
    GB_COUNT(1);
 }

@@ -1893,7 +1893,9 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
    {
       or_csr *A = &H->A[level];
       int n = A->nr;
-      if (level == maxl - 1 || n <= max_thresh) { break; }
+      /* the size test comes after each coarsening (par_amg_setup.c:3136-3143):
+       * the finest level is coarsened even when it is within max_coarse_size */
+      if (level == maxl - 1) { break; }
       or_csr S;
       or_strength(A, prm->strong_threshold, prm->max_row_sum, &S);
       int *CF = xmalloc(sizeof(int) * (n ? n : 1));
@@ -2297,6 +2299,44 @@ int or_fgmres_flat(int n, const int *Ai, const int *Aj, const double *Av, or_hie
    return or_fgmres(&A, H, b, x, tol, maxit, kdim, resn, iters);
 }
 int or_vcycle_flat(or_hierarchy *H, const double *f, double *u) { return or_amg_vcycle(H, f, u); }
+
+/* BoomerAMG as the solver, hypre_BoomerAMGSolve src/parcsr_ls/par_amg_solve.c:
+ * 150-351 (one process, print level and logging 0, convergence type 0): the
+ * relative residual ||b - A x|| / ||b|| (the absolute one when b = 0) before
+ * the loop; V-cycles on (b, x) in place while it is >= tol (1 when tol = 0)
+ * and fewer than maxit cycles ran, the residual after each.  relres[k]: after
+ * k cycles (relres[0] the initial one). */
+int or_amg_solve_flat(int n, const int *Ai, const int *Aj, const double *Av, or_hierarchy *H, const double *b,
+                      double *x, double tol, int maxit, double *relres, int *iters)
+{
+   or_csr A = { n, n, (int *) Ai, (int *) Aj, (double *) Av };
+   double *r = xmalloc(sizeof(double) * (n ? n : 1));
+   double rel = 1.0, rhs = 0.0;
+   if (tol > 0.0)
+   {
+      or_matvec(-1.0, &A, x, 1.0, b, r);
+      double res = sqrt(or_dot(n, r, r));
+      rhs = sqrt(or_dot(n, b, b));
+      rel = rhs != 0.0 ? res / rhs : res;
+   }
+   if (relres) { relres[0] = rel; }
+   int it = 0;
+   while (rel >= tol && it < maxit)
+   {
+      or_amg_vcycle(H, b, x);
+      if (tol > 0.0)
+      {
+         or_matvec(-1.0, &A, x, 1.0, b, r);
+         double res = sqrt(or_dot(n, r, r));
+         rel = rhs != 0.0 ? res / rhs : res;
+      }
+      it++;
+      if (relres) { relres[it] = rel; }
+   }
+   free(r);
+   *iters = it;
+   return 0;
+}
 void or_free_ptr(void *p) { free(p); }
 
 /* C = A*B as HYPRE_ParCSRMatrixMatmat computes it on one process

@@ -111,6 +111,8 @@ int    or_cheby_setup(const or_csr *A, double max_eig, double min_eig, double fr
 int    or_amg_setup(const or_csr *A, const or_amg_params *prm, or_hierarchy *H);
 void   or_amg_free(or_hierarchy *H);
 int    or_amg_vcycle(or_hierarchy *H, const double *f, double *u);
+int    or_amg_solve_flat(int n, const int *Ai, const int *Aj, const double *Av, or_hierarchy *H, const double *b,
+                         double *x, double tol, int maxit, double *relres, int *iters);
 
 /* vectors / matvec */
 void   or_matvec(double alpha, const or_csr *A, const double *x, double beta, const double *b, double *y);

@@ -64,6 +64,8 @@ def lib():
         L.or_fgmres_flat.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_void_p, P(C.c_int)]
         L.or_vcycle_flat.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.or_amg_solve_flat.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_double, C.c_int, C.c_void_p, C.c_void_p]
         L.or_default_params.argtypes = [P(Params)]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_rand_uniform.argtypes = [C.c_int, C.c_int, C.c_void_p]
@@ -206,6 +208,16 @@ class Hierarchy:
         lib().or_fgmres_flat(self.n, self.I.ctypes.data, self.J.ctypes.data, self.V.ctypes.data, self.h,
                              b.ctypes.data, x.ctypes.data, tol, maxit, kdim, res.ctypes.data, C.byref(it))
         return x, res[: it.value + 1], it.value
+
+    def amg_solve(self, b, tol=1e-8, maxit=100):
+        """BoomerAMG as the solver from x = 0: (x, relative residuals, cycles)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.n)
+        rel = np.zeros(maxit + 1)
+        it = C.c_int()
+        lib().or_amg_solve_flat(self.n, self.I.ctypes.data, self.J.ctypes.data, self.V.ctypes.data, self.h,
+                                b.ctypes.data, x.ctypes.data, tol, maxit, rel.ctypes.data, C.byref(it))
+        return x, rel[: it.value + 1], it.value
 
     def vcycle(self, f):
         f = np.ascontiguousarray(f, dtype=np.float64)

@@ -112,6 +112,24 @@ CASES = {
                               agg_Pmx=3, rlx=18, coarse_th=9, solver=1, full=True),
     "zerodiag_14_agg4_fgmres": dict(gen="zerodiag", n=(14,), th=0.25, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
                                     coarse_th=9, solver=61, k=10, full=True),
+    # edge cases: no strong couplings (coarsening stops at once, the single
+    # level is above max_coarse_size and relaxes instead of a direct solve),
+    # a level cap that leaves a large coarsest level, a matrix within
+    # max_coarse_size (direct solve only)
+    "diag_2000_pcg": dict(gen="diag", n=(2000,), th=0.25, mxrs=0.9, Pmx=4, rlx=18, coarse_th=9, solver=1, full=True),
+    "lap27_12_ml2_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=18, coarse_th=9, max_levels=2,
+                             solver=1, full=True),
+    "lap27_12_ml2_hgs6_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=6, coarse_th=9, max_levels=2,
+                                  solver=1, full=True),
+    "lap7_2_pcg": dict(kind=7, n=(2, 2, 2), th=0.25, mxrs=1.0, Pmx=4, rlx=18, coarse_th=9, solver=1, full=True),
+    # BoomerAMG as the solver (V-cycles in place on (b, x) until the relative
+    # residual is below tol)
+    "lap7_16_amg_l1jac": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, rlx=18, coarse_th=9, solver=0,
+                              precond=0, full=True),
+    "lap27_12_amg_hgs3": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=3, coarse_th=9, solver=0,
+                              precond=0, full=True),
+    "lap27_14_agg_amg_gs11": dict(kind=27, n=(14, 14, 14), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=6, rlx=11,
+                                  coarse_th=9, solver=0, precond=0, full=True),
     "lap27_48_agg4_pcg": dict(kind=27, n=(48, 48, 48), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
                               coarse_th=9, solver=1, full=False),
     "lap27_40_ext14_pcg": dict(kind=27, n=(40, 40, 40), th=0.5, mxrs=1.0, Pmx=4, interptype=14, rlx=18, coarse_th=9,
@@ -131,7 +149,7 @@ def dump_args(c, out):
         a = [DUMP, "-mat", mat]
     else:
         a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "rlx", "rlx_down", "rlx_up", "w",
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]

@@ -41,12 +41,16 @@ def matrix(c, O, g=None):
 
 def generate(c):
     """A seeded project generator ("gen": "fv" finite-volume diffusion on n^3
-    cells, "aniso" 2-D anisotropic 5-point with eps, "zerodiag" the 7-point
+    cells, "aniso" 2-D anisotropic 5-point with eps, "diag" a diagonal matrix
+    with entries from 1 to 3 (no strong couplings), "zerodiag" the 7-point
     Laplacian on n^3 with the diagonal of every row i = 5 mod 11 set to zero,
     so that interpolation rows meet a zero diagonal)."""
     from hypre_gb300 import problems as P
     if c["gen"] == "fv":
         return P.fv_diffusion(c["n"][0], seed=c.get("seed", 0))
+    if c["gen"] == "diag":
+        n = c["n"][0]
+        return (np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), np.linspace(1.0, 3.0, n))
     if c["gen"] == "zerodiag":
         n = c["n"][0]
         I, J, V = P.laplace(7, n, n, n)
@@ -67,6 +71,8 @@ def oracle_params(c):
         p["cheby_order"] = c["cheby_order"]
     if "agg_Pmx" in c:
         p["agg_p_max_elmts"] = c["agg_Pmx"]
+    if "max_levels" in c:
+        p["max_levels"] = c["max_levels"]
     return p
 
 
@@ -82,6 +88,8 @@ def amg_params(c):
         p["AggInterpType"] = c.get("agg_interp", 4)
     if "agg_Pmx" in c:
         p["AggPMaxElmts"] = c["agg_Pmx"]
+    if "max_levels" in c:
+        p["MaxLevels"] = c["max_levels"]
     if "cheby_order" in c:
         p["ChebyOrder"] = c["cheby_order"]
     return p
