@@ -33,7 +33,7 @@
 #define MLP_NBW (BW_W3 + MLP_OUTP * MLP_H)
 
 #define MLP_WARPS 4
-#define MLP_GRID 152
+#define MLP_GRID 304   // gradient CTAs: two per SM, a fixed reduction order
 
 typedef __nv_bfloat16 bf16;
 
@@ -54,113 +54,10 @@ __device__ __forceinline__ void mma16816(float *c, const unsigned *a, const unsi
                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// Fragment loaders for m16n8k16 (g = lane / 4, t = lane % 4):
+// Fragment layouts of m16n8k16 (g = lane / 4, t = lane % 4):
 //   A 16x16: {A[g][2t..2t+1]}, {A[g+8][2t..]}, {A[g][2t+8..]}, {A[g+8][2t+8..]}
 //   B 16x8 : {B[2t..2t+1][g]}, {B[2t+8..2t+9][g]}
 //   C 16x8 : c0,c1 = C[g][2t..2t+1], c2,c3 = C[g+8][2t..2t+1]
-// The accessor get(r, c) returns the element (bf16) of the logical matrix.
-template <typename Get>
-__device__ __forceinline__ void load_a(unsigned *a, Get get)
-{
-   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-   a[0] = pack2(get(g, 2 * t), get(g, 2 * t + 1));
-   a[1] = pack2(get(g + 8, 2 * t), get(g + 8, 2 * t + 1));
-   a[2] = pack2(get(g, 2 * t + 8), get(g, 2 * t + 9));
-   a[3] = pack2(get(g + 8, 2 * t + 8), get(g + 8, 2 * t + 9));
-}
-
-template <typename Get>
-__device__ __forceinline__ void load_b(unsigned *b, Get get)
-{
-   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-   b[0] = pack2(get(2 * t, g), get(2 * t + 1, g));
-   b[1] = pack2(get(2 * t + 8, g), get(2 * t + 9, g));
-}
-
-// per-warp shared tiles (BF16)
-struct WarpTiles
-{
-   bf16 X[16][MLP_IN];
-   bf16 H1[16][MLP_H];
-   bf16 H2[16][MLP_H];
-   bf16 dO[16][MLP_OUTP];
-   bf16 dH2[16][MLP_H];
-   bf16 dH1[16][MLP_H];
-};
-
-// Forward of one 16-row tile: fills H1, H2 (BF16) and returns the outputs in
-// C-fragment form o[4] (columns 2t, 2t+1 of rows g and g+8).
-__device__ __forceinline__ void forward_tile(WarpTiles &T, const bf16 *__restrict__ W, const float *__restrict__ P,
-                                             float *o)
-{
-   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-   const bf16 *W1 = W + BW_W1, *W2 = W + BW_W2, *W3 = W + BW_W3;
-   // layer 1: X (16x16) W1^T
-   unsigned a[4];
-   load_a(a, [&](int r, int c) { return T.X[r][c]; });
-   for (int nt = 0; nt < MLP_H / 8; nt++)
-   {
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-      unsigned b[2];
-      load_b(b, [&](int k, int n) { return W1[(nt * 8 + n) * MLP_IN + k]; });
-      mma16816(c, a, b);
-      int n0 = nt * 8 + 2 * t;
-      float b0 = P[OFF_B1 + n0], b1 = P[OFF_B1 + n0 + 1];
-      T.H1[g][n0] = __float2bfloat16_rn(fmaxf(c[0] + b0, 0.f));
-      T.H1[g][n0 + 1] = __float2bfloat16_rn(fmaxf(c[1] + b1, 0.f));
-      T.H1[g + 8][n0] = __float2bfloat16_rn(fmaxf(c[2] + b0, 0.f));
-      T.H1[g + 8][n0 + 1] = __float2bfloat16_rn(fmaxf(c[3] + b1, 0.f));
-   }
-   __syncwarp();
-   // layer 2: H1 (16x64) W2^T
-   for (int nt = 0; nt < MLP_H / 8; nt++)
-   {
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int kt = 0; kt < MLP_H / 16; kt++)
-      {
-         load_a(a, [&](int r, int cc) { return T.H1[r][kt * 16 + cc]; });
-         unsigned b[2];
-         load_b(b, [&](int k, int n) { return W2[(nt * 8 + n) * MLP_H + kt * 16 + k]; });
-         mma16816(c, a, b);
-      }
-      int n0 = nt * 8 + 2 * t;
-      float b0 = P[OFF_B2 + n0], b1 = P[OFF_B2 + n0 + 1];
-      T.H2[g][n0] = __float2bfloat16_rn(fmaxf(c[0] + b0, 0.f));
-      T.H2[g][n0 + 1] = __float2bfloat16_rn(fmaxf(c[1] + b1, 0.f));
-      T.H2[g + 8][n0] = __float2bfloat16_rn(fmaxf(c[2] + b0, 0.f));
-      T.H2[g + 8][n0 + 1] = __float2bfloat16_rn(fmaxf(c[3] + b1, 0.f));
-   }
-   __syncwarp();
-   // layer 3: H2 (16x64) W3^T (8 padded outputs)
-   o[0] = o[1] = o[2] = o[3] = 0.f;
-   for (int kt = 0; kt < MLP_H / 16; kt++)
-   {
-      load_a(a, [&](int r, int cc) { return T.H2[r][kt * 16 + cc]; });
-      unsigned b[2];
-      load_b(b, [&](int k, int n) { return W3[n * MLP_H + kt * 16 + k]; });
-      mma16816(o, a, b);
-   }
-   if (t == 0)
-   {
-      o[0] += P[OFF_B3];
-      o[1] += P[OFF_B3 + 1];
-      o[2] += P[OFF_B3];
-      o[3] += P[OFF_B3 + 1];
-   }
-}
-
-__device__ __forceinline__ void load_x_tile(WarpTiles &T, const bf16 *__restrict__ X, long long row0, long long N)
-{
-   const int lane = threadIdx.x & 31;
-   for (int e = lane; e < 16 * MLP_IN; e += 32)
-   {
-      int r = e / MLP_IN, c = e % MLP_IN;
-      long long row = row0 + r;
-      T.X[r][c] = row < N ? X[row * MLP_IN + c] : __float2bfloat16_rn(0.f);
-   }
-   __syncwarp();
-}
-
 } // namespace
 
 // Inference: out[row][0..1] = MLP(X[row]).  Each warp streams 16-row tiles.
@@ -277,164 +174,260 @@ __global__ void __launch_bounds__(32 * MLP_WARPS, 3) k_mlp_forward(long long N, 
 
 // Training gradients of the mean squared error over N rows.  Writes one
 // partial gradient (MLP_NPARAM floats) and one partial loss per CTA.
-__global__ void __launch_bounds__(32 * MLP_WARPS) k_mlp_grad(long long N, const bf16 *__restrict__ X,
-                                                             const float *__restrict__ Tg,
-                                                             const bf16 *__restrict__ W,
-                                                             const float *__restrict__ P, float inv_n,
-                                                             float *__restrict__ part, float *__restrict__ loss_part)
+//
+// Per 16-row tile, in registers: the forward pass as k_mlp_forward (H1 and H2
+// kept as A fragments), dO = (O - T) / N, dH2 = (dO W3) .* [H2 > 0] and
+// dH1 = (dH2 W2) .* [H1 > 0] chained the same way.  The weight gradients
+// dW = dZ^T A (K = the tile's 16 rows) take their operands from those
+// fragments transposed in registers (movmatrix: the A^T fragment of a 16x16
+// block is the four 8x8 blocks transposed with the off-diagonal pair swapped;
+// the B fragment of an n-tile is its two 8x8 blocks transposed); the bias
+// gradients are the column sums 1^T dZ on the tensor cores.  Each warp adds
+// its tiles' products to its FP32 accumulators in shared memory; the CTA sums
+// its warps in a fixed order, so training is deterministic.
+namespace
+{
+__device__ __forceinline__ unsigned mtrans(unsigned x)
+{
+   unsigned y;
+   asm volatile("movmatrix.sync.aligned.m8n8.trans.b16 %0, %1;" : "=r"(y) : "r"(x));
+   return y;
+}
+
+__device__ __forceinline__ unsigned mask_pack(float c0, float c1, unsigned h)
+{
+   // keep c where the activation (BF16 pair h) is positive, round to BF16
+   const float h0 = __bfloat162float(__ushort_as_bfloat16((unsigned short) (h & 0xffffu)));
+   const float h1 = __bfloat162float(__ushort_as_bfloat16((unsigned short) (h >> 16)));
+   return pack2(__float2bfloat16_rn(h0 > 0.f ? c0 : 0.f), __float2bfloat16_rn(h1 > 0.f ? c1 : 0.f));
+}
+
+// B fragment of n-tile nt of a matrix held as A fragments F[kt][4]
+#define BFRAG(F, nt) {mtrans((F)[(nt) >> 1][((nt) & 1) * 2]), mtrans((F)[(nt) >> 1][((nt) & 1) * 2 + 1])}
+} // namespace
+
+#define GRAD_WARPS 4
+#define GRAD_SMEM (sizeof(float) * GRAD_WARPS * MLP_NPARAM + 2 * sizeof(uint2) * 8 * 4 * 32)
+
+__global__ void __launch_bounds__(32 * GRAD_WARPS, 2) k_mlp_grad(long long N, const bf16 *__restrict__ X,
+                                                                const float *__restrict__ Tg,
+                                                                const bf16 *__restrict__ W,
+                                                                const float *__restrict__ P, float inv_n,
+                                                                float *__restrict__ part,
+                                                                float *__restrict__ loss_part)
 {
    extern __shared__ float smem[];
-   // per-warp gradient accumulators, then tiles
    float *acc = smem + (threadIdx.x >> 5) * MLP_NPARAM;
-   WarpTiles *tiles = (WarpTiles *) (smem + MLP_WARPS * MLP_NPARAM);
-   WarpTiles &T = tiles[threadIdx.x >> 5];
-   __shared__ float lsum[MLP_WARPS];
-   const int lane = threadIdx.x & 31;
-   const int g = lane >> 2, t = lane & 3;
+   uint2 *sw2f = (uint2 *) (smem + GRAD_WARPS * MLP_NPARAM);   // forward W2 fragments [nt][kt][lane]
+   uint2 *sw2b = sw2f + 8 * 4 * 32;                            // backward W2 fragments
+   __shared__ float lsum[GRAD_WARPS];
+   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+   const bf16 *W1 = W + BW_W1, *W2 = W + BW_W2, *W3 = W + BW_W3;
    for (int e = lane; e < MLP_NPARAM; e += 32) { acc[e] = 0.f; }
+   for (int q = threadIdx.x; q < 8 * 4 * 32; q += blockDim.x)
+   {
+      const int nt = q >> 7, kt = (q >> 5) & 3, ln = q & 31, gg = ln >> 2, tt = ln & 3;
+      const bf16 *r2 = W2 + (nt * 8 + gg) * MLP_H + kt * 16;
+      sw2f[q] = make_uint2(ld_pair(r2 + 2 * tt), ld_pair(r2 + 2 * tt + 8));
+      // dH1 = dH2 W2: B[k = H2 index][n = H1 index] = W2[k][n]
+      const int k0 = kt * 16 + 2 * tt, n = nt * 8 + gg;
+      sw2b[q] = make_uint2(pack2(W2[k0 * MLP_H + n], W2[(k0 + 1) * MLP_H + n]),
+                           pack2(W2[(k0 + 8) * MLP_H + n], W2[(k0 + 9) * MLP_H + n]));
+   }
+   unsigned w1[8][2], w3f[4][2], w3b[8];
+   float bb1[8][2], bb2[8][2];
+#pragma unroll
+   for (int nt = 0; nt < 8; nt++)
+   {
+      const bf16 *r1 = W1 + (nt * 8 + g) * MLP_IN;
+      w1[nt][0] = ld_pair(r1 + 2 * t);
+      w1[nt][1] = ld_pair(r1 + 2 * t + 8);
+      // dH2 = dO W3: B[k = output][n = hidden] = W3[k][n], outputs 8..15 zero
+      w3b[nt] = pack2(W3[(2 * t) * MLP_H + nt * 8 + g], W3[(2 * t + 1) * MLP_H + nt * 8 + g]);
+      bb1[nt][0] = P[OFF_B1 + nt * 8 + 2 * t];
+      bb1[nt][1] = P[OFF_B1 + nt * 8 + 2 * t + 1];
+      bb2[nt][0] = P[OFF_B2 + nt * 8 + 2 * t];
+      bb2[nt][1] = P[OFF_B2 + nt * 8 + 2 * t + 1];
+   }
+#pragma unroll
+   for (int kt = 0; kt < 4; kt++)
+   {
+      const bf16 *r3 = W3 + g * MLP_H + kt * 16;
+      w3f[kt][0] = ld_pair(r3 + 2 * t);
+      w3f[kt][1] = ld_pair(r3 + 2 * t + 8);
+   }
+   const float b30 = P[OFF_B3], b31 = P[OFF_B3 + 1];
+   const unsigned ONES = 0x3F803F80u;                          // BF16 pair (1, 1)
+   const unsigned ones[4] = {ONES, ONES, ONES, ONES};
+   __syncthreads();
    float loss = 0.f;
-   const bf16 *W2 = W + BW_W2, *W3 = W + BW_W3;
    const long long ntiles = (N + 15) / 16;
-   const long long wid = (long long) blockIdx.x * MLP_WARPS + (threadIdx.x >> 5);
-   const long long nw = (long long) gridDim.x * MLP_WARPS;
-   __syncwarp();
+   const long long wid = (long long) blockIdx.x * GRAD_WARPS + (threadIdx.x >> 5);
+   const long long nw = (long long) gridDim.x * GRAD_WARPS;
+   unsigned ax[4];
+   if (wid < ntiles) { load_x_frag(ax, X, wid * 16, N, g, t); }
    for (long long tile = wid; tile < ntiles; tile += nw)
    {
-      long long row0 = tile * 16;
-      load_x_tile(T, X, row0, N);
-      float o[4];
-      forward_tile(T, W, P, o);
-      // dO (BF16), loss
-      for (int e = lane; e < 16 * MLP_OUTP; e += 32) { T.dO[e / MLP_OUTP][e % MLP_OUTP] = __float2bfloat16_rn(0.f); }
-      __syncwarp();
+      const long long row0 = tile * 16;
+      unsigned a1[4] = {ax[0], ax[1], ax[2], ax[3]};
+      if (tile + nw < ntiles) { load_x_frag(ax, X, (tile + nw) * 16, N, g, t); }
+      // forward: H1 (a2), H2 (a3), outputs o
+      unsigned a2[4][4], a3[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++)
+      {
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+         mma16816(c, a1, w1[nt]);
+         a2[nt >> 1][(nt & 1) * 2 + 0] = relu_pack(c[0] + bb1[nt][0], c[1] + bb1[nt][1]);
+         a2[nt >> 1][(nt & 1) * 2 + 1] = relu_pack(c[2] + bb1[nt][0], c[3] + bb1[nt][1]);
+      }
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++)
+      {
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+         for (int kt = 0; kt < 4; kt++)
+         {
+            const uint2 b = sw2f[(nt * 4 + kt) * 32 + lane];
+            const unsigned bf[2] = {b.x, b.y};
+            mma16816(c, a2[kt], bf);
+         }
+         a3[nt >> 1][(nt & 1) * 2 + 0] = relu_pack(c[0] + bb2[nt][0], c[1] + bb2[nt][1]);
+         a3[nt >> 1][(nt & 1) * 2 + 1] = relu_pack(c[2] + bb2[nt][0], c[3] + bb2[nt][1]);
+      }
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++) { mma16816(o, a3[kt], w3f[kt]); }
+      // dO = (O - T) / N as an A fragment (outputs 0 and 1 in lanes t == 0)
+      unsigned ad[4] = {0u, 0u, 0u, 0u};
       if (t == 0)
       {
-         for (int h = 0; h < 2; h++)
+         const long long r0 = row0 + g, r1 = row0 + g + 8;
+         if (r0 < N)
          {
-            long long row = row0 + g + 8 * h;
-            if (row < N)
-            {
-               float d0 = o[2 * h] - Tg[row * 2], d1 = o[2 * h + 1] - Tg[row * 2 + 1];
-               loss += d0 * d0 + d1 * d1;
-               T.dO[g + 8 * h][0] = __float2bfloat16_rn(d0 * inv_n);
-               T.dO[g + 8 * h][1] = __float2bfloat16_rn(d1 * inv_n);
-            }
+            const float d0 = o[0] + b30 - Tg[r0 * 2], d1 = o[1] + b31 - Tg[r0 * 2 + 1];
+            loss += d0 * d0 + d1 * d1;
+            ad[0] = pack2(__float2bfloat16_rn(d0 * inv_n), __float2bfloat16_rn(d1 * inv_n));
+         }
+         if (r1 < N)
+         {
+            const float d0 = o[2] + b30 - Tg[r1 * 2], d1 = o[3] + b31 - Tg[r1 * 2 + 1];
+            loss += d0 * d0 + d1 * d1;
+            ad[1] = pack2(__float2bfloat16_rn(d0 * inv_n), __float2bfloat16_rn(d1 * inv_n));
          }
       }
-      __syncwarp();
-      unsigned a[4], b[2];
-      // dH2 = (dO W3) .* [H2 > 0]; K = 8 outputs padded to 16
-      load_a(a, [&](int r, int c) { return c < MLP_OUTP ? T.dO[r][c] : __float2bfloat16_rn(0.f); });
-      for (int nt = 0; nt < MLP_H / 8; nt++)
+      // dH2 = (dO W3) .* [H2 > 0]
+      unsigned dh2[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++)
       {
          float c[4] = {0.f, 0.f, 0.f, 0.f};
-         load_b(b, [&](int k, int n) { return k < MLP_OUTP ? W3[k * MLP_H + nt * 8 + n] : __float2bfloat16_rn(0.f); });
-         mma16816(c, a, b);
-         int n0 = nt * 8 + 2 * t;
-         for (int q = 0; q < 4; q++)
-         {
-            int r = g + 8 * (q >> 1), cc = n0 + (q & 1);
-            float v = __bfloat162float(T.H2[r][cc]) > 0.f ? c[q] : 0.f;
-            T.dH2[r][cc] = __float2bfloat16_rn(v);
-         }
+         const unsigned bf[2] = {w3b[nt], 0u};
+         mma16816(c, ad, bf);
+         dh2[nt >> 1][(nt & 1) * 2 + 0] = mask_pack(c[0], c[1], a3[nt >> 1][(nt & 1) * 2 + 0]);
+         dh2[nt >> 1][(nt & 1) * 2 + 1] = mask_pack(c[2], c[3], a3[nt >> 1][(nt & 1) * 2 + 1]);
       }
-      __syncwarp();
       // dH1 = (dH2 W2) .* [H1 > 0]
-      for (int nt = 0; nt < MLP_H / 8; nt++)
+      unsigned dh1[4][4];
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++)
       {
          float c[4] = {0.f, 0.f, 0.f, 0.f};
-         for (int kt = 0; kt < MLP_H / 16; kt++)
+#pragma unroll
+         for (int kt = 0; kt < 4; kt++)
          {
-            load_a(a, [&](int r, int cc) { return T.dH2[r][kt * 16 + cc]; });
-            load_b(b, [&](int k, int n) { return W2[(kt * 16 + k) * MLP_H + nt * 8 + n]; });
-            mma16816(c, a, b);
+            const uint2 b = sw2b[(nt * 4 + kt) * 32 + lane];
+            const unsigned bf[2] = {b.x, b.y};
+            mma16816(c, dh2[kt], bf);
          }
-         int n0 = nt * 8 + 2 * t;
-         for (int q = 0; q < 4; q++)
-         {
-            int r = g + 8 * (q >> 1), cc = n0 + (q & 1);
-            float v = __bfloat162float(T.H1[r][cc]) > 0.f ? c[q] : 0.f;
-            T.dH1[r][cc] = __float2bfloat16_rn(v);
-         }
+         dh1[nt >> 1][(nt & 1) * 2 + 0] = mask_pack(c[0], c[1], a2[nt >> 1][(nt & 1) * 2 + 0]);
+         dh1[nt >> 1][(nt & 1) * 2 + 1] = mask_pack(c[2], c[3], a2[nt >> 1][(nt & 1) * 2 + 1]);
       }
-      __syncwarp();
-      // weight gradients, K = the 16 rows of the tile
-      // dW3[j][k] = sum_r dO[r][j] H2[r][k]   (M = 8 outputs padded to 16)
-      load_a(a, [&](int m, int k) { return m < MLP_OUTP ? T.dO[k][m] : __float2bfloat16_rn(0.f); });
-      for (int nt = 0; nt < MLP_H / 8; nt++)
+      // dW3 = dO^T H2 (outputs 0 and 1: rows g < 2 of the C fragment), dB3 = 1^T dO
       {
-         float c[4] = {0.f, 0.f, 0.f, 0.f};
-         load_b(b, [&](int k, int n) { return T.H2[k][nt * 8 + n]; });
-         mma16816(c, a, b);
-         if (g < MLP_OUT)
-         {
-            acc[OFF_W3 + g * MLP_H + nt * 8 + 2 * t] += c[0];
-            acc[OFF_W3 + g * MLP_H + nt * 8 + 2 * t + 1] += c[1];
-         }
-      }
-      // dW2[n][k] = sum_r dH2[r][n] H1[r][k]
-      for (int mt = 0; mt < MLP_H / 16; mt++)
-      {
-         load_a(a, [&](int m, int k) { return T.dH2[k][mt * 16 + m]; });
-         for (int nt = 0; nt < MLP_H / 8; nt++)
+         const unsigned at[4] = {mtrans(ad[0]), 0u, mtrans(ad[1]), 0u};
+#pragma unroll
+         for (int nt = 0; nt < 8; nt++)
          {
             float c[4] = {0.f, 0.f, 0.f, 0.f};
-            load_b(b, [&](int k, int n) { return T.H1[k][nt * 8 + n]; });
-            mma16816(c, a, b);
-            int r0 = mt * 16 + g, c0 = nt * 8 + 2 * t;
+            const unsigned bf[2] = BFRAG(a3, nt);
+            mma16816(c, at, bf);
+            if (g < MLP_OUT)
+            {
+               acc[OFF_W3 + g * MLP_H + nt * 8 + 2 * t] += c[0];
+               acc[OFF_W3 + g * MLP_H + nt * 8 + 2 * t + 1] += c[1];
+            }
+         }
+         float c[4] = {0.f, 0.f, 0.f, 0.f};
+         const unsigned bf[2] = {mtrans(ad[0]), mtrans(ad[1])};
+         mma16816(c, ones, bf);
+         if (g == 0 && t == 0) { acc[OFF_B3] += c[0]; acc[OFF_B3 + 1] += c[1]; }
+      }
+      // dW2 = dH2^T H1, dW1 = dH1^T X
+#pragma unroll
+      for (int mt = 0; mt < 4; mt++)
+      {
+         const unsigned at2[4] = {mtrans(dh2[mt][0]), mtrans(dh2[mt][2]), mtrans(dh2[mt][1]), mtrans(dh2[mt][3])};
+         const unsigned at1[4] = {mtrans(dh1[mt][0]), mtrans(dh1[mt][2]), mtrans(dh1[mt][1]), mtrans(dh1[mt][3])};
+         const int r0 = mt * 16 + g;
+#pragma unroll
+         for (int nt = 0; nt < 8; nt++)
+         {
+            float c[4] = {0.f, 0.f, 0.f, 0.f};
+            const unsigned bf[2] = BFRAG(a2, nt);
+            mma16816(c, at2, bf);
+            const int c0 = nt * 8 + 2 * t;
             acc[OFF_W2 + r0 * MLP_H + c0] += c[0];
             acc[OFF_W2 + r0 * MLP_H + c0 + 1] += c[1];
             acc[OFF_W2 + (r0 + 8) * MLP_H + c0] += c[2];
             acc[OFF_W2 + (r0 + 8) * MLP_H + c0 + 1] += c[3];
          }
-      }
-      // dW1[n][k] = sum_r dH1[r][n] X[r][k]
-      for (int mt = 0; mt < MLP_H / 16; mt++)
-      {
-         load_a(a, [&](int m, int k) { return T.dH1[k][mt * 16 + m]; });
-         for (int nt = 0; nt < MLP_IN / 8; nt++)
+         const unsigned xa[1][4] = {{a1[0], a1[1], a1[2], a1[3]}};
+#pragma unroll
+         for (int nt = 0; nt < 2; nt++)
          {
             float c[4] = {0.f, 0.f, 0.f, 0.f};
-            load_b(b, [&](int k, int n) { return T.X[k][nt * 8 + n]; });
-            mma16816(c, a, b);
-            int r0 = mt * 16 + g, c0 = nt * 8 + 2 * t;
+            const unsigned bf[2] = BFRAG(xa, nt);
+            mma16816(c, at1, bf);
+            const int c0 = nt * 8 + 2 * t;
             acc[OFF_W1 + r0 * MLP_IN + c0] += c[0];
             acc[OFF_W1 + r0 * MLP_IN + c0 + 1] += c[1];
             acc[OFF_W1 + (r0 + 8) * MLP_IN + c0] += c[2];
             acc[OFF_W1 + (r0 + 8) * MLP_IN + c0 + 1] += c[3];
          }
       }
-      // bias gradients: column sums over the tile's rows
-      for (int c = lane; c < MLP_H; c += 32)
+      // dB1 = 1^T dH1, dB2 = 1^T dH2 (row 0 of the C fragment)
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++)
       {
-         float s1 = 0.f, s2 = 0.f;
-         for (int r = 0; r < 16; r++) { s1 += __bfloat162float(T.dH1[r][c]); s2 += __bfloat162float(T.dH2[r][c]); }
-         acc[OFF_B1 + c] += s1;
-         acc[OFF_B2 + c] += s2;
+         float c1[4] = {0.f, 0.f, 0.f, 0.f}, c2[4] = {0.f, 0.f, 0.f, 0.f};
+         const unsigned bf1[2] = BFRAG(dh1, nt), bf2[2] = BFRAG(dh2, nt);
+         mma16816(c1, ones, bf1);
+         mma16816(c2, ones, bf2);
+         if (g == 0)
+         {
+            acc[OFF_B1 + nt * 8 + 2 * t] += c1[0];
+            acc[OFF_B1 + nt * 8 + 2 * t + 1] += c1[1];
+            acc[OFF_B2 + nt * 8 + 2 * t] += c2[0];
+            acc[OFF_B2 + nt * 8 + 2 * t + 1] += c2[1];
+         }
       }
-      if (lane < MLP_OUT)
-      {
-         float s3 = 0.f;
-         for (int r = 0; r < 16; r++) { s3 += __bfloat162float(T.dO[r][lane]); }
-         acc[OFF_B3 + lane] += s3;
-      }
-      __syncwarp();
    }
-   for (int o = 16; o > 0; o >>= 1) { loss += __shfl_down_sync(GB_FULL, loss, o); }
+   for (int o2 = 16; o2 > 0; o2 >>= 1) { loss += __shfl_down_sync(GB_FULL, loss, o2); }
    if (lane == 0) { lsum[threadIdx.x >> 5] = loss; }
    __syncthreads();
    // CTA partial: warps summed in a fixed order
    for (int e = threadIdx.x; e < MLP_NPARAM; e += blockDim.x)
    {
-      float s = 0.f;
-      for (int w = 0; w < MLP_WARPS; w++) { s += smem[w * MLP_NPARAM + e]; }
-      part[(size_t) blockIdx.x * MLP_NPARAM + e] = s;
+      float sum = 0.f;
+      for (int w = 0; w < GRAD_WARPS; w++) { sum += smem[w * MLP_NPARAM + e]; }
+      part[(size_t) blockIdx.x * MLP_NPARAM + e] = sum;
    }
    if (threadIdx.x == 0)
    {
-      float s = 0.f;
-      for (int w = 0; w < MLP_WARPS; w++) { s += lsum[w]; }
-      loss_part[blockIdx.x] = s;
+      float sum = 0.f;
+      for (int w = 0; w < GRAD_WARPS; w++) { sum += lsum[w]; }
+      loss_part[blockIdx.x] = sum;
    }
 }
 
@@ -549,7 +542,7 @@ __global__ void k_mean2(long long N, const float *__restrict__ out, double *__re
    }
 }
 
-static size_t grad_smem_bytes(void) { return sizeof(float) * MLP_WARPS * MLP_NPARAM + sizeof(WarpTiles) * MLP_WARPS; }
+static size_t grad_smem_bytes(void) { return GRAD_SMEM; }
 
 extern "C" int gb_mlp_nparam(void) { return MLP_NPARAM; }
 extern "C" int gb_mlp_nbw(void) { return MLP_NBW; }
@@ -584,7 +577,7 @@ extern "C" int gb_mlp_grad(long long N, const void *X, const float *T, const voi
       attr_done = 1;
    }
    float inv_n = N > 0 ? 1.f / (float) N : 0.f;
-   k_mlp_grad<<<MLP_GRID, 32 * MLP_WARPS, sm, s>>>(N, (const bf16 *) X, T, (const bf16 *) W, P, inv_n, part,
+   k_mlp_grad<<<MLP_GRID, 32 * GRAD_WARPS, sm, s>>>(N, (const bf16 *) X, T, (const bf16 *) W, P, inv_n, part,
                                                     loss_part);
    k_mlp_reduce<<<(MLP_NPARAM + 255) / 256, 256, 0, s>>>(MLP_GRID, part, loss_part, 0.5f * inv_n, grad, loss);
    GB_COUNT(2);
