@@ -9,15 +9,19 @@ buffers):
 2. `sweep_labels`: for every (threshold, weight) pair of a grid, one batched
    BoomerAMG setup on the whole batch and one persistent batched PCG solve
    (FP32 V-cycle, l1-Jacobi); the per-system cost is
-   operator complexity x (iterations + SETUP_CYCLES).  Each system's label is
-   its cheapest pair.
+   operator complexity x (iterations + setup_cycles), setup_cycles being the
+   time of a setup in PCG iterations (`calibrate_setup_cycles` measures it on
+   the GPU for a problem of the size the model will serve).  Each system's
+   label is its cheapest pair.
 3. `train`: every row of a system is a sample (its 16 stencil features ->
    the system's label); full-batch Adam on the BF16 tensor-core MLP kernels.
 4. `LearnedSolver.solve`: BoomerAMG with the model (threshold from the finest
    level's rows, weight per level) inside FP64 PCG with the FP32 cycle; the
-   judge compares the convergence factor over the first `judge_iters`
-   iterations with the default parameters' factor and reverts to the defaults
-   when the learned one is worse.
+   judge runs the first `judge_iters` iterations with the learned and with
+   the default parameters and keeps the learned ones only when they are not
+   worse: by convergence factor (`judge="factor"`) or by estimated time
+   (`judge="time"`: measured setup time + measured time per iteration x the
+   iterations the factor predicts to the tolerance).
 """
 import ctypes as C
 
@@ -142,7 +146,31 @@ def make_problems(num, n=12, seed=0, eps_lo=1e-4, eps_hi=1.0):
     return I, np.concatenate(Js).astype(np.int32), np.concatenate(Vs), off.astype(np.int32), eps, ang
 
 
-def sweep_labels(I, J, V, off, thetas=THETAS, weights=WEIGHTS, seed=22775, shape=None):
+def calibrate_setup_cycles(A, bv, xv, prec=1, tol=1e-8, maxit=300):
+    """Time of the default BoomerAMG setup over the time of one PCG iteration
+    with its cycle, measured for A on the GPU: (ratio, setup seconds, seconds
+    per iteration, iterations)."""
+    import time
+    amg = BoomerAMG(StrongThreshold=DEFAULT_THETA, RelaxType=18, RelaxWt=DEFAULT_WEIGHT, Tol=0.0, MaxIter=1)
+    amg.set("CyclePrecision", prec)
+    k = Krylov("pcg", tol=tol, maxit=maxit, amg=amg)
+    xv.set(np.zeros(A.n))
+    for _ in range(2):                       # the second run is the measured one
+        xv.set(np.zeros(A.n))
+        _sync()
+        t0 = time.perf_counter()
+        k.setup(A, bv, xv)
+        _sync()
+        t1 = time.perf_counter()
+        k.solve(A, bv, xv)
+        _sync()
+        t2 = time.perf_counter()
+    its = max(k.iterations(), 1)
+    t_iter = (t2 - t1) / its
+    return (t1 - t0) / t_iter, t1 - t0, t_iter, its
+
+
+def sweep_labels(I, J, V, off, thetas=THETAS, weights=WEIGHTS, seed=22775, shape=None, setup_cycles=SETUP_CYCLES):
     """Per-system cost over the (threshold, weight) grid with the batched
     solver; returns (cost[nθ, nw, nsys], iterations[...], labels[nsys, 2], shape)."""
     n = len(I) - 1
@@ -166,7 +194,7 @@ def sweep_labels(I, J, V, off, thetas=THETAS, weights=WEIGHTS, seed=22775, shape
             it = bp.iterations()
             ok = bp.relres() < 1e-8
             its[i, j] = np.where(ok, it, 10 ** 6)
-            cost[i, j] = bp.complexities() * (its[i, j] + SETUP_CYCLES)
+            cost[i, j] = bp.complexities() * (its[i, j] + setup_cycles)
             del bp, amg
     flat = cost.reshape(-1, nsys)
     best = np.argmin(flat, axis=0)
@@ -197,13 +225,20 @@ class LearnedSolver:
     reverts to the defaults when the learned setup converges more slowly over
     the first `judge_iters` iterations."""
 
-    def __init__(self, params, judge_iters=4, tol=1e-8, maxit=200, prec=1):
+    def __init__(self, params, judge_iters=4, tol=1e-8, maxit=200, prec=1, judge="factor"):
         self.params = np.asarray(params, np.float64)
         self.judge_iters = judge_iters
         self.tol = tol
         self.maxit = maxit
         self.prec = prec
+        self.judge = judge
         self.default_factor = {}
+
+    def estimate(self, f, t_setup, t_iter):
+        """Estimated seconds to the tolerance: setup + iterations predicted by
+        the convergence factor f times the measured time per iteration."""
+        n = self.maxit if not (0.0 < f < 1.0) else min(self.maxit, int(np.ceil(np.log(self.tol) / np.log(f))))
+        return t_setup + t_iter * n
 
     def _solver(self, learned):
         amg = BoomerAMG(StrongThreshold=DEFAULT_THETA, RelaxType=18, RelaxWt=DEFAULT_WEIGHT, Tol=0.0, MaxIter=1)
@@ -215,12 +250,30 @@ class LearnedSolver:
     def factor(self, A, bv, xv, learned):
         """Setup + the first judge_iters PCG iterations from x = 0; returns
         (factor, amg, krylov) with the hierarchy kept for continuing."""
+        import time
+        warm = self.judge == "time"
         amg = self._solver(learned)
         k = Krylov("pcg", tol=self.tol, maxit=self.judge_iters, amg=amg)
         xv.set(np.zeros(A.n))
+        if warm:
+            # warm timings: a first setup and solve pay one-time costs (pool
+            # growth, launch-shape tuning, the cycle's graph capture)
+            k.setup(A, bv, xv)
+        _sync()
+        t0 = time.perf_counter()
         k.setup(A, bv, xv)
+        _sync()
+        t_setup = time.perf_counter() - t0
+        if warm:
+            k.solve(A, bv, xv)
+            xv.set(np.zeros(A.n))
+        _sync()
+        t0 = time.perf_counter()
         k.solve(A, bv, xv)
+        _sync()
+        t_solve = time.perf_counter() - t0
         lib().HYPRE_ClearAllErrors()
+        self.last_times = (t_setup, t_solve / max(k.iterations(), 1))
         return convergence_factor(k.history()), amg, k
 
     def solve(self, A, bv, xv, key=None):
@@ -228,15 +281,18 @@ class LearnedSolver:
         with the chosen parameters.  Returns a dict with the choice, the
         total iterations and both factors."""
         f_l, amg_l, k_l = self.factor(A, bv, xv, True)
+        ts_l, ti_l = self.last_times
         it0 = k_l.iterations()
         x_l = xv.values()
         if key is not None and key in self.default_factor:
-            f_d, amg_d, k_d = self.default_factor[key], None, None
+            (f_d, ts_d, ti_d), amg_d, k_d = self.default_factor[key], None, None
         else:
             f_d, amg_d, k_d = self.factor(A, bv, xv, False)
+            ts_d, ti_d = self.last_times
             if key is not None:
-                self.default_factor[key] = f_d
-        use_learned = f_l <= f_d
+                self.default_factor[key] = (f_d, ts_d, ti_d)
+        est_l, est_d = self.estimate(f_l, ts_l, ti_l), self.estimate(f_d, ts_d, ti_d)
+        use_learned = est_l <= est_d if self.judge == "time" else f_l <= f_d
         theta = C.c_double()
         w = np.zeros(32)
         if use_learned:
@@ -255,6 +311,6 @@ class LearnedSolver:
             rc = k.solve(A, bv, xv)
             it0 += k.iterations()
         return dict(used="learned" if use_learned else "default", iterations=it0, rc=rc,
-                    factor_learned=f_l, factor_default=f_d,
+                    factor_learned=f_l, factor_default=f_d, estimate_learned=est_l, estimate_default=est_d,
                     theta=theta.value if use_learned else DEFAULT_THETA,
                     weights=w[: amg.num_levels()].tolist() if use_learned else None)

@@ -111,3 +111,20 @@ def test_learned_gain_over_defaults(gb):
     print("label distribution (theta, weight):", np.unique(labels, axis=0, return_counts=True))
     print("mean iteration ratio learned/default:", np.mean(ratio))
     assert np.mean(ratio) <= 1.0 + 1e-12
+    # the time judge keeps the set with the smaller estimated time, and the
+    # solve still reaches the tolerance
+    tjudge = learned.LearnedSolver(p, judge_iters=4, judge="time")
+    for s in range(2):
+        a, b = offh[s], offh[s + 1]
+        Ii = Ih[a:b + 1] - Ih[a]
+        Js = Jh[Ih[a]:Ih[b]] - a
+        Vs = Vh[Ih[a]:Ih[b]]
+        n = b - a
+        As = gb.IJMatrix(Ii, Js, Vs)
+        rhs = np.random.default_rng(50 + s).uniform(-1, 1, n)
+        bv, xv = gb.IJVector(n, rhs), gb.IJVector(n, np.zeros(n))
+        res = tjudge.solve(As, bv, xv)
+        assert (res["used"] == "learned") == (res["estimate_learned"] <= res["estimate_default"])
+        import scipy.sparse as sp
+        r = rhs - sp.csr_matrix((Vs, Js, Ii), shape=(n, n)) @ xv.values()
+        assert np.linalg.norm(r) / np.linalg.norm(rhs) < 1e-8
