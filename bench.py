@@ -8,7 +8,14 @@ derived inside the step), BoomerAMG setup and Krylov solve from x0 = 0
 (`value`, seconds, lower is better).
 `e2e` repeats the step through the public IJ interface from host buffers:
 IJ assembly of the matrix and right-hand side from pinned host memory, setup,
-solve and the read-back of x, all inside the timed region.
+solve and the read-back of x, all inside the timed region; `stages_seconds`
+splits one extra, untimed end-to-end call at stream drains.  Each arm reports
+its setup phases and the host's waits on the stream during setup.
+
+Other workloads (`--workload`, one JSON line each): spgemm128 (the
+reference's SpGEMM benchmark, A*A), batch512, multi64, fv256, learned128 and
+mlp4m (the learned part's dense layers alone, TFLOP/s against the measured
+BF16 peak).
 
 Arms:
   default            GPU path (FP64 setup, FP32 or FP16-finest V-cycle inside
