@@ -1046,6 +1046,201 @@ int or_multipass_interp(const or_csr *A, const or_csr *S, int *CF, double trunc_
    return 0;
 }
 
+/* One pass block of the product-form multipass interpolation:
+ * hypre_GenerateMultipassPi src/parcsr_ls/par_mod_multi_interp.c:530-838
+ * (type 8, and the first block of type 9) and the Q part of
+ * hypre_GenerateMultiPi :841-1277 (type 9, Q unscaled plus w).  Rows: the m
+ * points pts[] (a pass, in row order); columns: the points of pass `color`
+ * numbered in row order (col[]).  Entries: the strong neighbours of pass
+ * `color`, in S order, with A's value.  Type 8: w == NULL, the row is scaled
+ * by -rs / (sum * a_ii) with rs = rsum[i1] (sum of the row's off-diagonals),
+ * or by -rs when sum * a_ii is zero.  Type 9: w[r] receives, in A order, the
+ * off-diagonals that did not enter Q; the row is not scaled. */
+static void mmp_block(const or_csr *A, const or_csr *S, const int *pass, const int *col, const int *pts, int m,
+                      int color, double *rsum, double *w, or_csr *Q, int ncols)
+{
+   int *Qi = xcalloc(m + 1, sizeof(int));
+   for (int r = 0; r < m; r++)
+   {
+      const int i1 = pts[r];
+      int c = 0;
+      for (int j = S->i[i1]; j < S->i[i1 + 1]; j++) { if (pass[S->j[j]] == color) { c++; } }
+      Qi[r + 1] = Qi[r] + c;
+   }
+   const int nnz = Qi[m];
+   int *Qj = xmalloc(sizeof(int) * (nnz ? nnz : 1));
+   double *Qv = xmalloc(sizeof(double) * (nnz ? nnz : 1));
+   for (int r = 0; r < m; r++)
+   {
+      const int i1 = pts[r];
+      int q = Qi[r];
+      if (!w)
+      {
+         /* :766-786: S's columns are found in A by a forward walk from the
+          * row start */
+         int j2 = A->i[i1];
+         for (int j = S->i[i1]; j < S->i[i1 + 1]; j++)
+         {
+            const int j1 = S->j[j];
+            while (A->j[j2] != j1) { j2++; }
+            if (pass[j1] == color) { Qj[q] = col[j1]; Qv[q] = A->v[j2]; q++; }
+         }
+         /* :790-823 */
+         double sum = 0.0;
+         for (int k = Qi[r]; k < Qi[r + 1]; k++) { sum += Qv[k]; }
+         const double value = sum * A->v[A->i[i1]];
+         if (value != 0) { rsum[i1] /= value; }
+         for (int k = Qi[r]; k < Qi[r + 1]; k++) { Qv[k] = -Qv[k] * rsum[i1]; }
+      }
+      else
+      {
+         /* :1100-1140: every off-diagonal of A that is not a Q entry goes
+          * to w, in A order */
+         double ws = 0.0;
+         int j2 = A->i[i1] + 1;
+         for (int j = S->i[i1]; j < S->i[i1 + 1]; j++)
+         {
+            const int j1 = S->j[j];
+            while (A->j[j2] != j1) { ws += A->v[j2]; j2++; }
+            if (pass[j1] == color) { Qj[q] = col[j1]; Qv[q] = A->v[j2]; q++; }
+            else { ws += A->v[j2]; }
+            j2++;
+         }
+         while (j2 < A->i[i1 + 1]) { ws += A->v[j2]; j2++; }
+         w[r] = ws;
+      }
+   }
+   Q->nr = m; Q->nc = ncols; Q->i = Qi; Q->j = Qj; Q->v = Qv;
+}
+
+/* Multipass interpolation expressed with sparse products (agg_interp_type 8
+ * and 9), hypre_BoomerAMGBuildModMultipassHost
+ * src/parcsr_ls/par_mod_multi_interp.c:17-525 on one process.  Passes
+ * (:123-270): the C points are pass 1; each round visits the points still
+ * unassigned in row order and gives pass p+1 to those with a strong neighbour
+ * of pass p (the marks of a round do not affect the same round); rounds stop
+ * when none are left, when a round assigns none, or after 9 passes.  Row sums
+ * (:272-312): the off-diagonals of every F row.  Pi[0] interpolates pass 2
+ * from the C points (mmp_block); type 8: Pi[p] = Q_p Pi[p-1] with Q_p the
+ * scaled block of pass p+2 from pass p+1 (hypre_ParMatmul); type 9: Pi[p] =
+ * Q_p Pi[p-1] with Q_p unscaled, then each row r scaled by -(s + w_r) /
+ * (s a_ii) with s the row's sum (-(s + w_r) when s a_ii is zero;
+ * :1236-1265).  P: C rows identity, a pass row the matching row of its Pi;
+ * truncated with (trunc_factor, max_elmts); CF -3 becomes -1 (:507-510).
+ * More than 9 passes is an error (-1), as is an assignment that stalls. */
+int or_mod_multipass_interp(const or_csr *A, const or_csr *S, int *CF, int type, double trunc_factor,
+                            int max_elmts, or_csr *P)
+{
+   const int n = A->nr;
+   int *pass = xcalloc(n ? n : 1, sizeof(int));
+   int *left = xmalloc(sizeof(int) * (n ? n : 1));
+   int *order = xmalloc(sizeof(int) * (n ? n : 1));
+   int starts[12] = {0};
+   int nleft = 0, cnt = 0;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] == 1) { pass[i] = 1; order[cnt++] = i; }
+      else { left[nleft++] = i; }
+   }
+   const int nc = cnt;
+   starts[1] = cnt;
+   int num_passes = 1, cur = 1, rc = 0;
+   while (nleft > 0)
+   {
+      const int old = nleft;
+      int keep = 0;
+      for (int t = 0; t < old; t++)
+      {
+         const int i1 = left[t];
+         int hit = 0;
+         for (int j = S->i[i1]; j < S->i[i1 + 1]; j++) { if (pass[S->j[j]] == cur) { hit = 1; break; } }
+         if (hit) { pass[i1] = cur + 1; order[cnt++] = i1; }
+         else { left[keep++] = i1; }
+      }
+      nleft = keep;
+      cur++;
+      num_passes++;
+      if (num_passes > 9) { rc = -1; break; }
+      starts[num_passes] = cnt;
+      if (nleft == old) { break; }
+   }
+   free(left);
+   if (rc) { free(pass); free(order); return -1; }
+   double *rsum = xcalloc(n ? n : 1, sizeof(double));
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] < 0) { for (int j = A->i[i] + 1; j < A->i[i + 1]; j++) { rsum[i] += A->v[j]; } }
+   }
+   /* column numbering of each pass: row order among its points */
+   int *col = xmalloc(sizeof(int) * (n ? n : 1));
+   {
+      int pc[12] = {0};
+      for (int i = 0; i < n; i++) { col[i] = pass[i] > 0 ? pc[pass[i]]++ : -1; }
+   }
+   const int nblk = num_passes - 1;
+   or_csr *Pi = xcalloc(nblk > 0 ? nblk : 1, sizeof(or_csr));
+   for (int b = 0; b < nblk; b++)
+   {
+      const int m = starts[b + 2] - starts[b + 1];
+      const int *pts = order + starts[b + 1];
+      if (b == 0) { mmp_block(A, S, pass, col, pts, m, 1, rsum, NULL, &Pi[0], nc); continue; }
+      const int prev_m = starts[b + 1] - starts[b];
+      or_csr Q;
+      double *w = type == 9 ? xmalloc(sizeof(double) * (m ? m : 1)) : NULL;
+      mmp_block(A, S, pass, col, pts, m, b + 1, rsum, w, &Q, prev_m);
+      or_matmul(&Q, &Pi[b - 1], &Pi[b]);
+      if (type == 9)
+      {
+         for (int r = 0; r < m; r++)
+         {
+            const int i1 = pts[r];
+            double s = 0.0;
+            for (int k = Pi[b].i[r]; k < Pi[b].i[r + 1]; k++) { s += Pi[b].v[k]; }
+            const double value = s * A->v[A->i[i1]];
+            s += w[r];
+            if (value != 0) { s /= value; }
+            for (int k = Pi[b].i[r]; k < Pi[b].i[r + 1]; k++) { Pi[b].v[k] = -Pi[b].v[k] * s; }
+         }
+      }
+      free(w);
+      or_csr_free(&Q);
+   }
+   /* assembly (:316-380) */
+   int *Pp = xcalloc(n + 1, sizeof(int));
+   int *blk = xmalloc(sizeof(int) * (n ? n : 1));
+   for (int i = 0; i < n; i++)
+   {
+      blk[i] = -1;
+      if (CF[i] == 1) { Pp[i + 1] = 1; }
+      else if (pass[i] >= 2 && pass[i] - 2 < nblk)
+      {
+         blk[i] = pass[i] - 2;
+         const or_csr *B = &Pi[blk[i]];
+         Pp[i + 1] = B->i[col[i] + 1] - B->i[col[i]];
+      }
+   }
+   for (int i = 0; i < n; i++) { Pp[i + 1] += Pp[i]; }
+   int *Pj = xmalloc(sizeof(int) * (Pp[n] ? Pp[n] : 1));
+   double *Pv = xmalloc(sizeof(double) * (Pp[n] ? Pp[n] : 1));
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] == 1) { Pj[Pp[i]] = col[i]; Pv[Pp[i]] = 1.0; }
+      else if (blk[i] >= 0)
+      {
+         const or_csr *B = &Pi[blk[i]];
+         const int k0 = B->i[col[i]], l = Pp[i + 1] - Pp[i];
+         memcpy(Pj + Pp[i], B->j + k0, sizeof(int) * (size_t) l);
+         memcpy(Pv + Pp[i], B->v + k0, sizeof(double) * (size_t) l);
+      }
+   }
+   P->nr = n; P->nc = nc; P->i = Pp; P->j = Pj; P->v = Pv;
+   if (trunc_factor != 0.0 || max_elmts > 0) { or_truncate(P, trunc_factor, max_elmts); }
+   for (int i = 0; i < n; i++) { if (CF[i] == SF_PT) { CF[i] = F_PT; } }
+   for (int b = 0; b < nblk; b++) { or_csr_free(&Pi[b]); }
+   free(Pi); free(blk); free(col); free(rsum); free(pass); free(order);
+   return 0;
+}
+
 /* hypre_BoomerAMGCorrectCFMarker2Host src/parcsr_ls/par_strength.c:3096:
  * C points that the second coarsening made F become -2, the others 1. */
 void or_correct_cf2(int n, int *CF, const int *CFN)
@@ -1240,6 +1435,143 @@ product:;
    P->nr = n; P->nc = nc; P->i = Pi; P->j = Pj; P->v = Pv;
    or_csr_free(&FF); or_csr_free(&FC); or_csr_free(&W);
    free(f2c); free(f2f); free(Dq); free(Dw); free(Dt); free(tmp);
+   return 0;
+}
+
+/* Modified partial interpolations of the second stage:
+ * variant 5 extended, hypre_BoomerAMGBuildModPartialExtInterpHost
+ * src/parcsr_ls/par_2s_interp.c:15-620; variant 7 extended+e,
+ * hypre_BoomerAMGBuildModPartialExtPEInterpHost :662-1320.  Blocks
+ * (hypre_ParCSRMatrixGenerateFFFC3 / FFFCD3, src/parcsr_mv/gen_fffc.c:568-1105
+ * / 1108-1560): FC over every non-C point (its strong C neighbours in S order),
+ * FF over the CF -2 points (the diagonal, then the strong non-C neighbours in
+ * S order; columns number the non-C points), and for variant 7 D_lambda =
+ * the mean of each non-C row's strong non-C values.  D_q = FC row sums.
+ * Variant 5 (:261-417): D_w = A row sum - FF off-diagonals whose column has
+ * D_q != 0 - D_q; FF's diagonal becomes D_q / D_w and its off-diagonals are
+ * divided by D_w (when D_w != 0); FC rows are scaled by -1 / D_q (0 when D_q
+ * is zero).  Variant 7 (:897-1055): D_inv = 1 / (D_q + D_lambda) (0 when that
+ * is zero), D_tau = sum FF_ij D_lambda_j D_inv_j, D_w = A row sum - FF
+ * off-diagonals whose column has D_inv != 0 + (D_tau - D_q); with beta =
+ * -1 / D_w FF's diagonal becomes beta (D_q + D_lambda) and its off-diagonals
+ * are scaled by beta; FC rows by D_inv.  W = FF FC (hypre_ParMatmul); P over
+ * the old C points in row order (CF 1 identity, CF -2 the row of W), columns
+ * the new C points.  CF is not changed. */
+int or_mod_partial_interp(const or_csr *A, const or_csr *S, const int *CF, int variant, or_csr *P)
+{
+   const int n = A->nr;
+   int *f2c = xmalloc(sizeof(int) * (n ? n : 1)), *f2f = xmalloc(sizeof(int) * (n ? n : 1));
+   int nc = 0, nf = 0, nn = 0;
+   for (int i = 0; i < n; i++)
+   {
+      f2c[i] = f2f[i] = -1;
+      if (CF[i] > 0) { f2c[i] = nc++; }
+      else { f2f[i] = nf++; if (CF[i] == -2) { nn++; } }
+   }
+   int *nlist = xmalloc(sizeof(int) * (nn ? nn : 1));
+   int *FCi = xcalloc(nf + 1, sizeof(int)), *FFi = xcalloc(nn + 1, sizeof(int));
+   for (int i = 0, t = 0; i < n; i++)
+   {
+      if (CF[i] > 0) { continue; }
+      int c = 0, f = 0;
+      for (int k = S->i[i]; k < S->i[i + 1]; k++) { if (CF[S->j[k]] > 0) { c++; } else { f++; } }
+      FCi[f2f[i] + 1] = c;
+      if (CF[i] == -2) { nlist[t] = i; FFi[t + 1] = f + 1; t++; }
+   }
+   for (int r = 0; r < nf; r++) { FCi[r + 1] += FCi[r]; }
+   for (int t = 0; t < nn; t++) { FFi[t + 1] += FFi[t]; }
+   int *FCj = xmalloc(sizeof(int) * (FCi[nf] ? FCi[nf] : 1)), *FFj = xmalloc(sizeof(int) * (FFi[nn] ? FFi[nn] : 1));
+   double *FCv = xmalloc(sizeof(double) * (FCi[nf] ? FCi[nf] : 1));
+   double *FFv = xmalloc(sizeof(double) * (FFi[nn] ? FFi[nn] : 1));
+   double *lam = xcalloc(nf ? nf : 1, sizeof(double));
+   for (int i = 0, t = 0; i < n; i++)
+   {
+      if (CF[i] > 0) { continue; }
+      const int r = f2f[i], isnew = CF[i] == -2;
+      int qc = FCi[r], qf = isnew ? FFi[t] : 0;
+      if (isnew) { FFj[qf] = f2f[A->j[A->i[i]]]; FFv[qf] = A->v[A->i[i]]; qf++; }
+      double sum = 0;
+      for (int k = S->i[i]; k < S->i[i + 1]; k++)
+      {
+         const int js = S->j[k];
+         int ja = A->i[i] + 1;
+         while (A->j[ja] != js) { ja++; }
+         if (CF[js] > 0) { FCj[qc] = f2c[js]; FCv[qc] = A->v[ja]; qc++; }
+         else
+         {
+            sum += 1;
+            lam[r] += A->v[ja];
+            if (isnew) { FFj[qf] = f2f[js]; FFv[qf] = A->v[ja]; qf++; }
+         }
+      }
+      if (sum != 0.0) { lam[r] = lam[r] / sum; }
+      if (isnew) { t++; }
+   }
+   double *Dq = xcalloc(nf ? nf : 1, sizeof(double)), *Dinv = xcalloc(nf ? nf : 1, sizeof(double));
+   for (int r = 0; r < nf; r++)
+   {
+      for (int k = FCi[r]; k < FCi[r + 1]; k++) { Dq[r] += FCv[k]; }
+      if (variant == 7 && Dq[r] + lam[r] != 0.0) { Dinv[r] = 1.0 / (Dq[r] + lam[r]); }
+   }
+   for (int t = 0; t < nn; t++)
+   {
+      const int i = nlist[t], self = f2f[i];
+      double tau = 0.0, w = 0.0;
+      if (variant == 7)
+      {
+         for (int k = FFi[t] + 1; k < FFi[t + 1]; k++) { tau += FFv[k] * lam[FFj[k]] * Dinv[FFj[k]]; }
+      }
+      for (int k = A->i[i]; k < A->i[i + 1]; k++) { w += A->v[k]; }
+      if (variant == 7)
+      {
+         for (int k = FFi[t] + 1; k < FFi[t + 1]; k++) { if (Dinv[FFj[k]] != 0.0) { w -= FFv[k]; } }
+         w += tau - Dq[self];
+         if (w != 0.0)
+         {
+            const double beta = -1.0 / w;
+            FFv[FFi[t]] = beta * (Dq[self] + lam[self]);
+            for (int k = FFi[t] + 1; k < FFi[t + 1]; k++) { FFv[k] *= beta; }
+         }
+      }
+      else
+      {
+         for (int k = FFi[t] + 1; k < FFi[t + 1]; k++) { if (Dq[FFj[k]] != 0.0) { w -= FFv[k]; } }
+         w -= Dq[self];
+         if (w != 0.0)
+         {
+            const double beta = 1.0 / w;
+            FFv[FFi[t]] = beta * Dq[self];
+            for (int k = FFi[t] + 1; k < FFi[t + 1]; k++) { FFv[k] *= beta; }
+         }
+      }
+   }
+   for (int r = 0; r < nf; r++)
+   {
+      double gamma;
+      if (variant == 7) { gamma = Dinv[r]; }
+      else { gamma = Dq[r] != 0.0 ? -1.0 / Dq[r] : 0.0; }
+      for (int k = FCi[r]; k < FCi[r + 1]; k++) { FCv[k] *= gamma; }
+   }
+   or_csr FF = {nn, nf, FFi, FFj, FFv}, FC = {nf, nc, FCi, FCj, FCv}, W;
+   or_matmul(&FF, &FC, &W);
+   int nco = nc + nn;
+   int *Pi = xcalloc(nco + 1, sizeof(int));
+   int *Pj = xmalloc(sizeof(int) * (size_t) (nc + W.i[nn] ? nc + W.i[nn] : 1));
+   double *Pv = xmalloc(sizeof(double) * (size_t) (nc + W.i[nn] ? nc + W.i[nn] : 1));
+   int c = 0, rowp = 0, t = 0;
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] > 0) { Pj[c] = f2c[i]; Pv[c] = 1.0; c++; Pi[++rowp] = c; }
+      else if (CF[i] == -2)
+      {
+         for (int k = W.i[t]; k < W.i[t + 1]; k++) { Pj[c] = W.j[k]; Pv[c] = W.v[k]; c++; }
+         t++;
+         Pi[++rowp] = c;
+      }
+   }
+   P->nr = nco; P->nc = nc; P->i = Pi; P->j = Pj; P->v = Pv;
+   or_csr_free(&FF); or_csr_free(&FC); or_csr_free(&W);
+   free(f2c); free(f2f); free(nlist); free(lam); free(Dq); free(Dinv);
    return 0;
 }
 
@@ -1904,7 +2236,7 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
       int nc;
       if (level < prm->agg_num_levels)
       {
-         /* par_amg_setup.c:1311-1358 and :1778-1915 (agg_interp_type 6) */
+         /* par_amg_setup.c:1311-1358 and :1778-1915 (agg_interp_type 1, 4-9) */
          or_csr S2;
          or_strength2(&S, CF, prm->num_paths, &S2);
          int *CFN = xmalloc(sizeof(int) * (S2.nr ? S2.nr : 1));
@@ -1916,13 +2248,29 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
             or_correct_cf(n, CF, CFN);
             or_multipass_interp(A, &S, CF, prm->agg_trunc_factor, prm->agg_p_max_elmts, &P);
          }
+         else if (prm->agg_interp_type == 8 || prm->agg_interp_type == 9)
+         {
+            /* :1799-1824: the same correction, then the product form */
+            or_correct_cf(n, CF, CFN);
+            if (or_mod_multipass_interp(A, &S, CF, prm->agg_interp_type, prm->agg_trunc_factor,
+                                        prm->agg_p_max_elmts, &P))
+            {
+               or_csr_free(&S2); free(CFN); or_csr_free(&S); free(CF);
+               return -1;
+            }
+         }
          else
          {
+            /* :1778-1915: P1 over the first coarsening, the CF correction,
+             * P2 over the old C points, P = P1 P2 */
             or_csr P1, P2;
-            or_mod_extpi_interp(A, &S, CF, &P1);
+            const int t = prm->agg_interp_type;
+            if (t == 1) { or_extpi_interp(A, &S, CF, &P1); }
+            else { mod_interp(A, &S, CF, t == 5 ? 16 : t == 7 ? 18 : 17, &P1); }
             or_truncate(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
             or_correct_cf2(n, CF, CFN);
-            or_partial_extpi_interp(A, &S, CF, &P2);
+            if (t == 1 || t == 6) { or_partial_extpi_interp(A, &S, CF, &P2); }
+            else { or_mod_partial_interp(A, &S, CF, t, &P2); }
             or_truncate(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
             or_matmul(&P1, &P2, &P);
             or_truncate(&P, prm->agg_trunc_factor, prm->agg_p_max_elmts);

@@ -100,6 +100,9 @@ int    or_strength2(const or_csr *S, int *CF, int num_paths, or_csr *S2);
 void   or_correct_cf2(int n, int *CF, const int *CFN);
 void   or_correct_cf(int n, int *CF, const int *CFN);
 int    or_multipass_interp(const or_csr *A, const or_csr *S, int *CF, double trunc_factor, int max_elmts, or_csr *P);
+int    or_mod_multipass_interp(const or_csr *A, const or_csr *S, int *CF, int type, double trunc_factor,
+                               int max_elmts, or_csr *P);
+int    or_mod_partial_interp(const or_csr *A, const or_csr *S, const int *CF, int variant, or_csr *P);
 int    or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P);
 int    or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
 int    or_eig_tridiag(int n, double *d, double *e);

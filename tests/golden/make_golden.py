@@ -112,6 +112,35 @@ CASES = {
                               agg_Pmx=3, rlx=18, coarse_th=9, solver=1, full=True),
     "zerodiag_14_agg4_fgmres": dict(gen="zerodiag", n=(14,), th=0.25, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
                                     coarse_th=9, solver=61, k=10, full=True),
+    # multipass interpolation in product form (agg_interp_type 8: each pass
+    # block a scaled Q times the previous block; 9: Q times the previous block,
+    # then scaled with the row's weak sum)
+    "lap27_16_agg8_pcg": dict(kind=27, n=(16, 16, 16), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=8, rlx=18,
+                              coarse_th=9, solver=1, full=True),
+    "lap7_20_agg9x2_pcg": dict(kind=7, n=(20, 20, 20), th=0.25, mxrs=1.0, Pmx=4, agg_nl=2, agg_interp=9, rlx=18,
+                               coarse_th=9, solver=1, full=True),
+    "fv_14_agg8_pmx_pcg": dict(gen="fv", n=(14,), seed=7, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=8,
+                               agg_Pmx=4, rlx=18, coarse_th=9, solver=1, full=True),
+    "aniso_48_agg9_pcg": dict(gen="aniso", n=(48,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=9,
+                              agg_Pmx=3, rlx=18, coarse_th=9, solver=1, full=True),
+    "aniso_48_agg8_pcg": dict(gen="aniso", n=(48,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=8,
+                              rlx=18, coarse_th=9, solver=1, full=True),
+    # two-stage interpolation on the aggressive levels with the other first /
+    # second stages: 5 modified extended / modified partial extended, 7
+    # modified extended+e / modified partial extended+e, 1 extended+i /
+    # partial extended+i
+    "lap27_16_agg5_pcg": dict(kind=27, n=(16, 16, 16), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=5, rlx=18,
+                              coarse_th=9, solver=1, full=True),
+    "lap7_18_agg7_fgmres": dict(kind=7, n=(18, 18, 18), th=0.25, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=7, rlx=18,
+                                coarse_th=9, solver=61, k=10, full=True),
+    "fv_14_agg5x2_p12_pcg": dict(gen="fv", n=(14,), seed=8, th=0.25, mxrs=0.9, Pmx=4, agg_nl=2, agg_interp=5,
+                                 agg_P12_mx=3, agg_Pmx=4, rlx=18, coarse_th=9, solver=1, full=True),
+    "lap27_16_agg7_p12_pcg": dict(kind=27, n=(16, 16, 16), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=7,
+                                  agg_P12_mx=4, rlx=18, coarse_th=9, solver=1, full=True),
+    "lap7_20_agg1x2_pcg": dict(kind=7, n=(20, 20, 20), th=0.25, mxrs=1.0, Pmx=4, agg_nl=2, agg_interp=1, rlx=18,
+                               coarse_th=9, solver=1, full=True),
+    "aniso_48_agg7_pcg": dict(gen="aniso", n=(48,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=7,
+                              rlx=18, coarse_th=9, solver=1, full=True),
     # edge cases: no strong couplings (coarsening stops at once, the single
     # level is above max_coarse_size and relaxes instead of a direct solve),
     # a level cap that leaves a large coarsest level, a matrix within
@@ -149,7 +178,7 @@ def dump_args(c, out):
         a = [DUMP, "-mat", mat]
     else:
         a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "w",
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]

@@ -71,6 +71,8 @@ def oracle_params(c):
         p["cheby_order"] = c["cheby_order"]
     if "agg_Pmx" in c:
         p["agg_p_max_elmts"] = c["agg_Pmx"]
+    if "agg_P12_mx" in c:
+        p["agg_p12_max_elmts"] = c["agg_P12_mx"]
     if "max_levels" in c:
         p["max_levels"] = c["max_levels"]
     return p
@@ -88,6 +90,8 @@ def amg_params(c):
         p["AggInterpType"] = c.get("agg_interp", 4)
     if "agg_Pmx" in c:
         p["AggPMaxElmts"] = c["agg_Pmx"]
+    if "agg_P12_mx" in c:
+        p["AggP12MaxElmts"] = c["agg_P12_mx"]
     if "max_levels" in c:
         p["MaxLevels"] = c["max_levels"]
     if "cheby_order" in c:
