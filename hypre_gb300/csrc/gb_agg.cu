@@ -27,6 +27,11 @@ __global__ void k_flag_nonpos(int n, const int *__restrict__ CF, int *__restrict
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i < n) { flag[i] = CF[i] <= 0; }
 }
+__global__ void k_flag_pos_or(int n, const int *__restrict__ CF, int v, int *__restrict__ flag)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) { flag[i] = CF[i] > 0 || CF[i] == v; }
+}
 // inverse of a scanned flag: list[scan[i]] = i where flag[i]
 __global__ void k_scatter_list(int n, const int *__restrict__ flag, const int *__restrict__ scan, int *__restrict__ list)
 {
@@ -53,9 +58,10 @@ extern "C" void gb_list_flags(int nlist, const int *dcount, const int *list, int
 
 extern "C" void gb_flags(int n, const int *CF, int kind, int v, int *flag, cudaStream_t s)
 {
-   // kind 0: CF > 0 ; 1: CF == v ; 2: CF <= 0
+   // kind 0: CF > 0 ; 1: CF == v ; 2: CF <= 0 ; 3: CF > 0 or CF == v
    if (kind == 0) { k_flag_pos<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, flag); }
    else if (kind == 1) { k_flag_eq<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, v, flag); }
+   else if (kind == 3) { k_flag_pos_or<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, v, flag); }
    else { k_flag_nonpos<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, flag); }
    GB_COUNT(1);
 }
@@ -637,5 +643,153 @@ extern "C" void gb_p1_fill(int n, const int *CF, const int *f2c, const int *f2f,
                            const double *Wv, const int *Pi, int *Pj, double *Pv, cudaStream_t s)
 {
    k_p1_fill<<<gb_blocks2(n, 256), 256, 0, s>>>(n, CF, f2c, f2f, Wi, Wj, Wv, Pi, Pj, Pv);
+   GB_COUNT(1);
+}
+
+// ---------------------------------------------------------------------------
+// Modified partial interpolations of the second stage on an aggressive level
+// (variant 5 extended: hypre_BoomerAMGBuildModPartialExtInterpHost
+// src/parcsr_ls/par_2s_interp.c:15-620; variant 7 extended+e:
+// hypre_BoomerAMGBuildModPartialExtPEInterpHost :662-1320).  F rows r (every
+// non-C point): D_q = FC row sum; variant 7: D_lambda = the mean of the row's
+// strong non-C values (FF's off-diagonals over the full F list, as
+// hypre_ParCSRMatrixGenerateFFFCD3 src/parcsr_mv/gen_fffc.c:1497-1560 sums
+// them) and D_inv = 1 / (D_q + D_lambda), 0 when that is zero.
+// ---------------------------------------------------------------------------
+__global__ void k_modp_dq(int variant, int nf, const int *__restrict__ FFi, const double *__restrict__ FFv,
+                          const int *__restrict__ FCi, const double *__restrict__ FCv, double *__restrict__ Dq,
+                          double *__restrict__ Dl, double *__restrict__ Dinv)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   double q = 0.0;
+   for (int k = FCi[r]; k < FCi[r + 1]; k++) { q += FCv[k]; }
+   Dq[r] = q;
+   if (variant == 7)
+   {
+      double l = 0.0, c = 0.0;
+      for (int k = FFi[r] + 1; k < FFi[r + 1]; k++) { c += 1; l += FFv[k]; }
+      if (c != 0.0) { l = l / c; }
+      Dl[r] = l;
+      Dinv[r] = q + l != 0.0 ? 1.0 / (q + l) : 0.0;
+   }
+}
+
+// the CF -2 rows (t-th: point nl[t], F index f2f[nl[t]]) of FF (:261-393,
+// :897-1042): D_w = A row sum - the FF off-diagonals whose column has D_q != 0
+// (variant 7: D_inv != 0), minus D_q (variant 7: plus D_tau - D_q, D_tau =
+// sum FF_ij D_lambda_j D_inv_j); when D_w != 0 the diagonal becomes
+// D_q / D_w and the off-diagonals are divided by D_w (variant 7: with
+// beta = -1 / D_w, the diagonal beta (D_q + D_lambda), off-diagonals * beta)
+__global__ void k_modp_rows(int variant, int nn, const int *__restrict__ nl, const int *__restrict__ f2f,
+                            const int *__restrict__ Ai, const double *__restrict__ Av, const int *__restrict__ FFi,
+                            const int *__restrict__ FFj, double *__restrict__ FFv, const double *__restrict__ Dq,
+                            const double *__restrict__ Dl, const double *__restrict__ Dinv)
+{
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= nn) { return; }
+   const int i = nl[t], self = f2f[i];
+   const int f0 = FFi[t], f1 = FFi[t + 1];
+   double w = 0.0;
+   if (variant == 7)
+   {
+      double tau = 0.0;
+      for (int k = f0 + 1; k < f1; k++) { const int c = FFj[k]; tau += FFv[k] * Dl[c] * Dinv[c]; }
+      for (int k = Ai[i]; k < Ai[i + 1]; k++) { w += Av[k]; }
+      for (int k = f0 + 1; k < f1; k++) { if (Dinv[FFj[k]] != 0.0) { w -= FFv[k]; } }
+      w += tau - Dq[self];
+      if (w != 0.0)
+      {
+         const double beta = -1.0 / w;
+         FFv[f0] = beta * (Dq[self] + Dl[self]);
+         for (int k = f0 + 1; k < f1; k++) { FFv[k] *= beta; }
+      }
+   }
+   else
+   {
+      for (int k = Ai[i]; k < Ai[i + 1]; k++) { w += Av[k]; }
+      for (int k = f0 + 1; k < f1; k++) { if (Dq[FFj[k]] != 0.0) { w -= FFv[k]; } }
+      w -= Dq[self];
+      if (w != 0.0)
+      {
+         const double beta = 1.0 / w;
+         FFv[f0] = beta * Dq[self];
+         for (int k = f0 + 1; k < f1; k++) { FFv[k] *= beta; }
+      }
+   }
+}
+
+// FC rows scaled by -1 / D_q (0 when D_q is zero); variant 7 by D_inv
+__global__ void k_modp_fc(int variant, int nf, const int *__restrict__ FCi, double *__restrict__ FCv,
+                          const double *__restrict__ Dq, const double *__restrict__ Dinv)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nf) { return; }
+   double g;
+   if (variant == 7) { g = Dinv[r]; }
+   else { g = Dq[r] != 0.0 ? -1.0 / Dq[r] : 0.0; }
+   for (int k = FCi[r]; k < FCi[r + 1]; k++) { FCv[k] *= g; }
+}
+
+extern "C" void gb_modp_scale(int variant, int nf, int nn, const int *nl, const int *f2f, const int *Ai,
+                              const double *Av, const int *FFai, const double *FFav, const int *FCi, double *FCv,
+                              const int *FFi, const int *FFj, double *FFv, double *Dq, double *Dl, double *Dinv,
+                              cudaStream_t s)
+{
+   if (nf > 0) { k_modp_dq<<<gb_blocks2(nf, 256), 256, 0, s>>>(variant, nf, FFai, FFav, FCi, FCv, Dq, Dl, Dinv); }
+   if (nn > 0)
+   {
+      k_modp_rows<<<gb_blocks2(nn, 128), 128, 0, s>>>(variant, nn, nl, f2f, Ai, Av, FFi, FFj, FFv, Dq, Dl, Dinv);
+   }
+   if (nf > 0) { k_modp_fc<<<gb_blocks2(nf, 256), 256, 0, s>>>(variant, nf, FCi, FCv, Dq, Dinv); }
+   GB_COUNT(3);
+}
+
+// P over the old C points (oc, in row order): CF 1 rows the identity (f2c),
+// CF -2 rows the row nscan[i] of W
+__global__ void k_modp_len(int nco, const int *__restrict__ oc, const int *__restrict__ CF,
+                           const int *__restrict__ nscan, const int *__restrict__ Wi, int *__restrict__ len)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nco) { return; }
+   const int i = oc[r];
+   len[r] = CF[i] > 0 ? 1 : Wi[nscan[i] + 1] - Wi[nscan[i]];
+}
+
+__global__ void k_modp_gather(int nco, const int *__restrict__ oc, const int *__restrict__ CF,
+                              const int *__restrict__ f2c, const int *__restrict__ nscan, const int *__restrict__ Wi,
+                              const int *__restrict__ Wj, const double *__restrict__ Wv, const int *__restrict__ Pi,
+                              int *__restrict__ Pj, double *__restrict__ Pv)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nco) { return; }
+   const int i = oc[r], o = Pi[r];
+   if (CF[i] > 0)
+   {
+      Pj[o] = f2c[i];
+      Pv[o] = 1.0;
+      return;
+   }
+   const int k0 = Wi[nscan[i]], l = Pi[r + 1] - o;
+   for (int q = 0; q < l; q++)
+   {
+      Pj[o + q] = Wj[k0 + q];
+      Pv[o + q] = Wv[k0 + q];
+   }
+}
+
+extern "C" void gb_modp_len(int nco, const int *oc, const int *CF, const int *nscan, const int *Wi, int *len,
+                            cudaStream_t s)
+{
+   if (nco <= 0) { return; }
+   k_modp_len<<<gb_blocks2(nco, 256), 256, 0, s>>>(nco, oc, CF, nscan, Wi, len);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_modp_gather(int nco, const int *oc, const int *CF, const int *f2c, const int *nscan, const int *Wi,
+                               const int *Wj, const double *Wv, const int *Pi, int *Pj, double *Pv, cudaStream_t s)
+{
+   if (nco <= 0) { return; }
+   k_modp_gather<<<gb_blocks2(nco, 256), 256, 0, s>>>(nco, oc, CF, f2c, nscan, Wi, Wj, Wv, Pi, Pj, Pv);
    GB_COUNT(1);
 }

@@ -896,10 +896,209 @@ done:
    return rc;
 }
 
+/* an empty CSR block with nc columns */
+static void csr_empty(gb_csr *M, int nc)
+{
+   memset(M, 0, sizeof(*M));
+   M->nc = nc;
+   M->i = (int *) gb_dcalloc(sizeof(int));
+   M->j = (int *) gb_dmalloc(sizeof(int));
+   M->v = (double *) gb_dmalloc(sizeof(double));
+}
+
+/* the modified partial interpolations of the second stage (agg_interp_type
+ * 5 and 7; par_2s_interp.c:15-620, :662-1320): the F/C blocks of every non-C
+ * point (FC, and FF for D_lambda) and of the CF -2 points (FF), the D
+ * scalings, W = FF FC (hypre_ParMatmul), P over the old C points in row order
+ * (CF 1 identity, CF -2 the row of W); f2c / nc number the new C points */
+static int mm_partial_interp(const gb_csr *A, const gb_csr *S, const int *CF, const int *f2c, int nc, int variant,
+                             gb_csr *P)
+{
+   cudaStream_t s = gb_stream();
+   const int n = A->nr;
+   int *f2f = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *nscan = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+   int *fl = NULL, *nl = NULL;
+   const int nf = number_points(n, CF, 2, 0, f2f, &fl);
+   const int nn = number_points(n, CF, 1, -2, nscan, &nl);
+   /* blocks over a row list: FF (diagonal first) and FC */
+   gb_csr FF[2], FC[2];
+   const int m[2] = {nf, nn};
+   const int *lst[2] = {fl, nl};
+   for (int b = 0; b < 2; b++)
+   {
+      const int r = m[b];
+      memset(&FF[b], 0, sizeof(gb_csr));
+      memset(&FC[b], 0, sizeof(gb_csr));
+      FF[b].nr = r; FF[b].nc = nf; FC[b].nr = r; FC[b].nc = nc;
+      int *cff = (int *) gb_dmalloc(sizeof(int) * (size_t) (r + 1));
+      int *cfc = (int *) gb_dmalloc(sizeof(int) * (size_t) (r + 1));
+      if (r > 0) { gb_fffc_count(r, lst[b], A->i, A->j, S->i, S->j, CF, cff, cfc, s); }
+      FF[b].i = (int *) gb_dmalloc(sizeof(int) * (size_t) (r + 1));
+      FC[b].i = (int *) gb_dmalloc(sizeof(int) * (size_t) (r + 1));
+      FF[b].nnz = scan_total(cff, FF[b].i, r);
+      FC[b].nnz = scan_total(cfc, FC[b].i, r);
+      gb_dfree(cff); gb_dfree(cfc);
+      FF[b].j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FF[b].nnz ? FF[b].nnz : 1));
+      FF[b].v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FF[b].nnz ? FF[b].nnz : 1));
+      FC[b].j = (int *) gb_dmalloc(sizeof(int) * (size_t) (FC[b].nnz ? FC[b].nnz : 1));
+      FC[b].v = (double *) gb_dmalloc(sizeof(double) * (size_t) (FC[b].nnz ? FC[b].nnz : 1));
+      if (r > 0)
+      {
+         gb_fffc_fill(r, n, A->nnz, lst[b], A->i, A->j, A->v, S->i, S->j, CF, f2c, f2f, FF[b].i, FF[b].j, FF[b].v,
+                      FC[b].i, FC[b].j, FC[b].v, s);
+      }
+   }
+   {
+      const size_t nb = sizeof(double) * (size_t) (nf ? nf : 1);
+      double *Dq = (double *) gb_dmalloc(nb), *Dl = (double *) gb_dmalloc(nb), *Dinv = (double *) gb_dmalloc(nb);
+      gb_modp_scale(variant, nf, nn, nl, f2f, A->i, A->v, FF[0].i, FF[0].v, FC[0].i, FC[0].v, FF[1].i, FF[1].j,
+                    FF[1].v, Dq, Dl, Dinv, s);
+      gb_dfree(Dq); gb_dfree(Dl); gb_dfree(Dinv);
+   }
+   gb_csr W;
+   int rc = -1;
+   if (nn == 0) { csr_empty(&W, nc); }
+   else if (spgemm_host(&FF[1], &FC[0], nn == nc, &W)) { goto done; }
+   {
+      int *oscan = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      int *oc = NULL;
+      int *flag = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      gb_flags(n, CF, 3, -2, flag, s);
+      const int nco = scan_total(flag, oscan, n);
+      oc = (int *) gb_dmalloc(sizeof(int) * (size_t) (nco > 0 ? nco : 1));
+      gb_scatter_list(n, flag, oscan, oc, s);
+      gb_dfree(flag); gb_dfree(oscan);
+      int *len = (int *) gb_dmalloc(sizeof(int) * (size_t) (nco + 1));
+      gb_modp_len(nco, oc, CF, nscan, W.i, len, s);
+      P->nr = nco; P->nc = nc;
+      P->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (nco + 1));
+      P->nnz = scan_total(len, P->i, nco);
+      P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
+      P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
+      gb_modp_gather(nco, oc, CF, f2c, nscan, W.i, W.j, W.v, P->i, P->j, P->v, s);
+      gb_dfree(len); gb_dfree(oc);
+   }
+   gb_csr_free(&W);
+   rc = 0;
+done:
+   for (int b = 0; b < 2; b++) { gb_csr_free(&FF[b]); gb_csr_free(&FC[b]); }
+   gb_dfree(f2f); gb_dfree(nscan); gb_dfree(fl); gb_dfree(nl);
+   return rc;
+}
+
+/* multipass interpolation in product form (agg_interp_type 8 and 9,
+ * par_mod_multi_interp.c:17-525) after the C/F correction by the second
+ * coarsening: passes by rounds (C points 1; a point left takes pass p+1 in
+ * the round that finds a strong neighbour of pass p; more than 9 passes is an
+ * error), one block of rows per pass (pass 2 from the C points; later passes
+ * a sparse product with the previous block), P assembled from the blocks and
+ * truncated with (agg_trunc_factor, agg_P_max_elmts).  Returns the number of
+ * coarse points. */
+static int mod_multipass_interp(const gb_amg_params *prm, const gb_csr *A, const gb_csr *S, int *CF, const int *f2c1,
+                                const int *CFN, gb_csr *P)
+{
+   cudaStream_t s = gb_stream();
+   const int n = A->nr, type = prm->agg_interp_type;
+   gb_correct_cf(n, f2c1, CFN, CF, s);
+   const size_t ni = sizeof(int) * (size_t) (n ? n : 1);
+   int *pass = (int *) gb_dmalloc(ni), *col = (int *) gb_dmalloc(ni);
+   int *dcnt = (int *) gb_dcalloc(sizeof(int));
+   double *rsum = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
+   int *rows[GB_MMP_MAXB + 3];
+   int cnt[GB_MMP_MAXB + 3];
+   gb_csr B[GB_MMP_MAXB];
+   memset(rows, 0, sizeof(rows));
+   memset(cnt, 0, sizeof(cnt));
+   memset(B, 0, sizeof(B));
+   int nblk = 0, rc = -1;
+   if (!pass || !col || !dcnt || !rsum) { goto done; }
+   gb_mmp_init(n, CF, pass, dcnt, s);
+   const int nc = read_int(dcnt);
+   int remaining = n - nc, num_passes = 1;
+   while (remaining > 0)
+   {
+      cudaMemsetAsync(dcnt, 0, sizeof(int), s);
+      gb_mmp_round(n, S->i, S->j, num_passes, pass, dcnt, s);
+      const int c = read_int(dcnt);
+      remaining -= c;
+      num_passes++;
+      if (num_passes > 9)
+      {
+         gb_error(HYPRE_ERROR_GENERIC, "multipass interpolation: more than 9 passes");
+         goto done;
+      }
+      if (c == 0) { break; }
+   }
+   for (int p = 1; p <= num_passes; p++)
+   {
+      int *scan = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      cnt[p] = number_points(n, pass, 1, p, scan, &rows[p]);
+      gb_mmp_col(n, pass, p, scan, col, s);
+      gb_dfree(scan);
+   }
+   gb_mmp_rowsum(n, CF, A->i, A->v, rsum, s);
+   nblk = num_passes - 1;
+   for (int b = 0; b < nblk; b++)
+   {
+      const int m = cnt[b + 2], color = b + 1;
+      const int *rws = rows[b + 2];
+      gb_csr Q;
+      memset(&Q, 0, sizeof(Q));
+      Q.nr = m;
+      Q.nc = cnt[b + 1];
+      Q.i = (int *) gb_dmalloc(sizeof(int) * (size_t) (m + 1));
+      int *qc = (int *) gb_dmalloc(sizeof(int) * (size_t) (m + 1));
+      gb_mmp_count(m, rws, S->i, S->j, pass, color, qc, s);
+      Q.nnz = scan_total(qc, Q.i, m);
+      gb_dfree(qc);
+      Q.j = (int *) gb_dmalloc(sizeof(int) * (size_t) (Q.nnz ? Q.nnz : 1));
+      Q.v = (double *) gb_dmalloc(sizeof(double) * (size_t) (Q.nnz ? Q.nnz : 1));
+      double *w = (type == 9 && b > 0) ? (double *) gb_dmalloc(sizeof(double) * (size_t) (m ? m : 1)) : NULL;
+      gb_mmp_fill(m, rws, A->i, A->j, A->v, S->i, S->j, pass, col, color, Q.i, Q.j, Q.v, rsum, w, s);
+      if (b == 0) { B[0] = Q; continue; }
+      /* hypre_ParMatmul (:354-356): square when Q's rows match the
+       * previous block's columns */
+      int r = 0;
+      if (m == 0) { csr_empty(&B[b], B[b - 1].nc); }
+      else { r = spgemm_host(&Q, &B[b - 1], Q.nr == B[b - 1].nc, &B[b]); }
+      gb_csr_free(&Q);
+      if (!r && w) { gb_mmp_scale9(m, rws, A->i, A->v, B[b].i, B[b].v, w, s); }
+      gb_dfree(w);
+      if (r) { goto done; }
+   }
+   {
+      gb_mmp_blocks blk;
+      memset(&blk, 0, sizeof(blk));
+      blk.nblk = nblk;
+      for (int b = 0; b < nblk; b++) { blk.i[b] = B[b].i; blk.j[b] = B[b].j; blk.v[b] = B[b].v; }
+      int *len = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      gb_mmp_len(n, CF, pass, col, &blk, len, s);
+      P->nr = n; P->nc = nc;
+      P->i = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
+      P->nnz = scan_total(len, P->i, n);
+      P->j = (int *) gb_dmalloc(sizeof(int) * (size_t) (P->nnz ? P->nnz : 1));
+      P->v = (double *) gb_dmalloc(sizeof(double) * (size_t) (P->nnz ? P->nnz : 1));
+      gb_mmp_gather(n, CF, pass, col, &blk, P->i, P->j, P->v, s);
+      gb_dfree(len);
+   }
+   truncate_host(P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
+   gb_sf_to_f(n, CF, s);
+   rc = nc;
+done:
+   gb_sync();
+   for (int b = 0; b < GB_MMP_MAXB; b++) { gb_csr_free(&B[b]); }
+   for (int p = 0; p < GB_MMP_MAXB + 3; p++) { gb_dfree(rows[p]); }
+   gb_dfree(pass); gb_dfree(col); gb_dfree(dcnt); gb_dfree(rsum);
+   return rc;
+}
+
 /* aggressive level (par_amg_setup.c:1311-1358, :1778-1915): second-order
- * strength and PMIS on it, then agg_interp_type 4 -- multipass interpolation
- * -- or 6 -- P = P1 P2 with P1 modified extended+i and P2 partial
- * extended+i.  Returns the number of coarse points. */
+ * strength and PMIS on it, then multipass interpolation (agg_interp_type 4;
+ * 8 and 9 in product form) or a two-stage P = P1 P2 (1: extended+i and
+ * partial extended+i; 5, 6, 7: modified extended, extended+i, extended+e
+ * and the matching partial second stage).  Returns the number of coarse
+ * points. */
 static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb_csr *P)
 {
    gb_amg_params *prm = &amg->prm;
@@ -984,24 +1183,38 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
       if (it < 0) { gb_error(HYPRE_ERROR_GENERIC, "PMIS on S2 did not terminate"); return -1; }
    }
    gb_csr_free(&S2);
-   if (prm->agg_interp_type == 4)
+   if (prm->agg_interp_type == 4 || prm->agg_interp_type == 8 || prm->agg_interp_type == 9)
    {
-      int nc = multipass_interp(prm, A, S, CF, f2c1, CFN, P);
+      int nc = prm->agg_interp_type == 4 ? multipass_interp(prm, A, S, CF, f2c1, CFN, P)
+                                         : mod_multipass_interp(prm, A, S, CF, f2c1, CFN, P);
       gb_dfree(f2c1); gb_dfree(c2f1); gb_dfree(cnt); gb_dfree(CFN);
       return nc;
    }
-   /* P1: modified extended+i (par_mod_lr_interp.c:585) */
+   /* P1 over the first coarsening (par_amg_setup.c:1778-1847): extended+i
+    * (agg_interp_type 1; turns CF -3 into -1), modified extended (5),
+    * modified extended+i (6), modified extended+e (7) */
+   const int at = prm->agg_interp_type;
    gb_csr P1;
-   if (mm_interp(A, S, CF, f2c1, nc1, 17, &P1)) { return -1; }
+   if (at == 1)
+   {
+      if (extpi_host(A, S, CF, f2c1, n, NULL, nc1, 1, &P1)) { return -1; }
+      gb_sf_to_f(n, CF, s);
+   }
+   else if (mm_interp(A, S, CF, f2c1, nc1, at == 5 ? 16 : at == 7 ? 18 : 17, &P1)) { return -1; }
    truncate_host(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
-   /* CF correction (par_strength.c:3096) and P2: partial extended+i over the
-    * old C points (partial.c:16) */
+   /* CF correction (par_strength.c:3096) and P2 over the old C points: partial
+    * extended+i (1, 6; partial.c:16, CF below -1 becomes -1), modified partial
+    * extended (5) or extended+e (7; par_2s_interp.c, CF kept) */
    gb_correct_cf2(n, f2c1, CFN, CF, s);
    int *f2c2 = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    int nc2 = number_points(n, CF, 1, 1, f2c2, NULL);
    gb_csr P2;
-   if (extpi_host(A, S, CF, f2c2, nc1, c2f1, nc2, 1, &P2)) { return -1; }
-   gb_cf_clamp(n, CF, s);
+   if (at == 1 || at == 6)
+   {
+      if (extpi_host(A, S, CF, f2c2, nc1, c2f1, nc2, 1, &P2)) { return -1; }
+      gb_cf_clamp(n, CF, s);
+   }
+   else if (mm_partial_interp(A, S, CF, f2c2, nc2, at, &P2)) { return -1; }
    truncate_host(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
    if (spgemm_host(&P1, &P2, n == nc2, P)) { return -1; }
    truncate_host(P, prm->agg_trunc_factor, prm->agg_p_max_elmts);
@@ -1420,14 +1633,13 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    amg->lev[0].n = A0->A.nr;
    int level = 0;
    int maxl = prm->max_levels < 32 ? prm->max_levels : 32;
-   if (prm->agg_num_levels > 0 && prm->agg_interp_type != 4 && prm->agg_interp_type != 6)
+   if (prm->agg_num_levels > 0 && !(prm->agg_interp_type == 1 || (prm->agg_interp_type >= 4 && prm->agg_interp_type <= 9)))
    {
-      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening: agg_interp_type 4 and 6 are supported");
+      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening: agg_interp_type 1 and 4-9 are supported");
       return gb_error_flag;
    }
    while (1)
    {
-      int n = amg->lev[level].n;
       /* the size test follows each coarsening (par_amg_setup.c:3136-3143):
        * the finest level is coarsened even when it is within max_coarse_size */
       if (level == maxl - 1) { break; }

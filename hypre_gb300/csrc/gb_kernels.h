@@ -158,6 +158,31 @@ void gb_mp_carry1(int m, const int *fl, const int *assigned, const int *degen, c
 void gb_mp_len(int n, const int *CF, const int *assigned, const int *rowlen, int *len, cudaStream_t s);
 void gb_mp_gather(int n, const int *CF, const int *assigned, const int *f2c, const int *rowoff,
                   const gb_mp_areas *areas, const int *Pi, int *Pj, double *Pv, cudaStream_t s);
+/* multipass interpolation in product form (gb_multipass.cu): the blocks of
+ * passes 2 .. nblk+1 (rows: the pass's points in row order) */
+#define GB_MMP_MAXB 8
+typedef struct
+{
+   const int    *i[GB_MMP_MAXB];
+   const int    *j[GB_MMP_MAXB];
+   const double *v[GB_MMP_MAXB];
+   int           nblk;
+} gb_mmp_blocks;
+void gb_mmp_init(int n, const int *CF, int *pass, int *count, cudaStream_t s);
+void gb_mmp_round(int n, const int *Si, const int *Sj, int cur, int *pass, int *count, cudaStream_t s);
+void gb_mmp_col(int n, const int *pass, int p, const int *scan, int *col, cudaStream_t s);
+void gb_mmp_rowsum(int n, const int *CF, const int *Ai, const double *Av, double *rsum, cudaStream_t s);
+void gb_mmp_count(int m, const int *rows, const int *Si, const int *Sj, const int *pass, int color, int *cnt,
+                  cudaStream_t s);
+void gb_mmp_fill(int m, const int *rows, const int *Ai, const int *Aj, const double *Av, const int *Si,
+                 const int *Sj, const int *pass, const int *col, int color, const int *Qi, int *Qj, double *Qv,
+                 const double *rsum, double *w, cudaStream_t s);
+void gb_mmp_scale9(int m, const int *rows, const int *Ai, const double *Av, const int *Bi, double *Bv,
+                   const double *w, cudaStream_t s);
+void gb_mmp_len(int n, const int *CF, const int *pass, const int *col, const gb_mmp_blocks *B, int *len,
+                cudaStream_t s);
+void gb_mmp_gather(int n, const int *CF, const int *pass, const int *col, const gb_mmp_blocks *B, const int *Pi,
+                   int *Pj, double *Pv, cudaStream_t s);
 void gb_fffc_count(int nf, const int *fl, const int *Ai, const int *Aj, const int *Si, const int *Sj, const int *CF,
                    int *cff, int *cfc, cudaStream_t s);
 /* nrows, nnz: A's size (the mean row length picks the lanes per row) */
@@ -167,6 +192,12 @@ void gb_fffc_fill(int nf, int nrows, long long nnz, const int *fl, const int *Ai
 void gb_mod_extpi_scale(int nf, int nnzff, const int *fl, const int *Ai, const double *Av, const int *FFi,
                         const int *FFj, double *FFv, const int *FCi, const double *FCv, double *tmp, double *Dq,
                         double *Dw, cudaStream_t s);
+void gb_modp_scale(int variant, int nf, int nn, const int *nl, const int *f2f, const int *Ai, const double *Av,
+                   const int *FFai, const double *FFav, const int *FCi, double *FCv, const int *FFi, const int *FFj,
+                   double *FFv, double *Dq, double *Dl, double *Dinv, cudaStream_t s);
+void gb_modp_len(int nco, const int *oc, const int *CF, const int *nscan, const int *Wi, int *len, cudaStream_t s);
+void gb_modp_gather(int nco, const int *oc, const int *CF, const int *f2c, const int *nscan, const int *Wi,
+                    const int *Wj, const double *Wv, const int *Pi, int *Pj, double *Pv, cudaStream_t s);
 void gb_mod_interp_scale(int variant, int nf, int nnzff, const int *fl, const int *Ai, const double *Av,
                          const int *FFi, const int *FFj, double *FFv, const int *FCi, double *FCv, double *tmp,
                          double *D1, double *D2, double *D3, double *D4, cudaStream_t s);

@@ -345,3 +345,255 @@ extern "C" void gb_mp_gather(int n, const int *CF, const int *assigned, const in
    k_mp_gather<<<mp_blocks(n, 256), 256, 0, s>>>(n, CF, assigned, f2c, rowoff, *areas, Pi, Pj, Pv);
    GB_COUNT(1);
 }
+
+// ---------------------------------------------------------------------------
+// Multipass interpolation in product form (agg_interp_type 8 and 9,
+// hypre_BoomerAMGBuildModMultipassHost src/parcsr_ls/par_mod_multi_interp.c:
+// 17-525, hypre_GenerateMultipassPi :530-838, hypre_GenerateMultiPi
+// :841-1277).
+//
+// Passes.  C points are pass 1; in round p the points without a pass that
+// have a strong neighbour of pass p take pass p+1 (the reference visits them
+// in row order, but a mark of the round, p+1, never equals p, so the result
+// does not depend on the order and one kernel per round assigns it).  Within
+// a pass the points are numbered in row order: they are the rows of that
+// pass's block and the columns of the next pass's Q.
+// ---------------------------------------------------------------------------
+
+// pass = 1 for C points, 0 otherwise; *count = the C points
+__global__ void k_mmp_init(int n, const int *__restrict__ CF, int *__restrict__ pass, int *count)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const bool c = i < n && CF[i] == C_PT;
+   if (i < n) { pass[i] = c ? 1 : 0; }
+   const unsigned b = __ballot_sync(0xffffffffu, c);
+   if ((threadIdx.x & 31) == 0 && b) { atomicAdd(count, __popc(b)); }
+}
+
+extern "C" void gb_mmp_init(int n, const int *CF, int *pass, int *count, cudaStream_t s)
+{
+   k_mmp_init<<<mp_blocks(n, 256), 256, 0, s>>>(n, CF, pass, count);
+   GB_COUNT(1);
+}
+
+// round `cur`: points without a pass and with a strong neighbour of pass cur
+// take pass cur+1 (in place); *count += the points marked
+__global__ void k_mmp_round(int n, const int *__restrict__ Si, const int *__restrict__ Sj, int cur, int *pass,
+                            int *count)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   bool hit = false;
+   if (i < n && pass[i] == 0)
+   {
+      for (int k = Si[i]; k < Si[i + 1]; k++)
+      {
+         if (pass[Sj[k]] == cur) { hit = true; break; }
+      }
+      if (hit) { pass[i] = cur + 1; }
+   }
+   const unsigned b = __ballot_sync(0xffffffffu, hit);
+   if ((threadIdx.x & 31) == 0 && b) { atomicAdd(count, __popc(b)); }
+}
+
+extern "C" void gb_mmp_round(int n, const int *Si, const int *Sj, int cur, int *pass, int *count, cudaStream_t s)
+{
+   k_mmp_round<<<mp_blocks(n, 256), 256, 0, s>>>(n, Si, Sj, cur, pass, count);
+   GB_COUNT(1);
+}
+
+// col[i] = scan[i] for the points of pass p (their number within the pass)
+__global__ void k_mmp_col(int n, const int *__restrict__ pass, int p, const int *__restrict__ scan,
+                          int *__restrict__ col)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n && pass[i] == p) { col[i] = scan[i]; }
+}
+
+extern "C" void gb_mmp_col(int n, const int *pass, int p, const int *scan, int *col, cudaStream_t s)
+{
+   k_mmp_col<<<mp_blocks(n, 256), 256, 0, s>>>(n, pass, p, scan, col);
+   GB_COUNT(1);
+}
+
+// rsum[i] = the sum of the off-diagonals of F row i in A order (:272-312;
+// the diagonal is the row's first entry), 0 for C rows
+__global__ void k_mmp_rowsum(int n, const int *__restrict__ CF, const int *__restrict__ Ai,
+                             const double *__restrict__ Av, double *__restrict__ rsum)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   double s = 0.0;
+   if (CF[i] < 0)
+   {
+      for (int k = Ai[i] + 1; k < Ai[i + 1]; k++) { s += Av[k]; }
+   }
+   rsum[i] = s;
+}
+
+extern "C" void gb_mmp_rowsum(int n, const int *CF, const int *Ai, const double *Av, double *rsum, cudaStream_t s)
+{
+   k_mmp_rowsum<<<mp_blocks(n, 256), 256, 0, s>>>(n, CF, Ai, Av, rsum);
+   GB_COUNT(1);
+}
+
+// entries of the block rows: strong neighbours of pass `color`
+__global__ void k_mmp_count(int m, const int *__restrict__ rows, const int *__restrict__ Si,
+                            const int *__restrict__ Sj, const int *__restrict__ pass, int color, int *__restrict__ cnt)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= m) { return; }
+   const int i1 = rows[r];
+   int c = 0;
+   for (int k = Si[i1]; k < Si[i1 + 1]; k++) { c += pass[Sj[k]] == color; }
+   cnt[r] = c;
+}
+
+extern "C" void gb_mmp_count(int m, const int *rows, const int *Si, const int *Sj, const int *pass, int color,
+                             int *cnt, cudaStream_t s)
+{
+   if (m <= 0) { return; }
+   k_mmp_count<<<mp_blocks(m, 256), 256, 0, s>>>(m, rows, Si, Sj, pass, color, cnt);
+   GB_COUNT(1);
+}
+
+// Block rows (one thread per row).  The row's strong neighbours of pass
+// `color` in S order with A's values (S's columns are found in A by a forward
+// walk: S is a subsequence of A's off-diagonals).  w == NULL
+// (hypre_GenerateMultipassPi :766-823): the row is scaled by -rs with
+// rs = rsum / (sum a_ii), or rs = rsum when sum a_ii is zero.  w != NULL (the
+// Q of hypre_GenerateMultiPi :1100-1140): the row stays unscaled and w[r]
+// sums, in A order, every off-diagonal that is not an entry.
+__global__ void k_mmp_fill(int m, const int *__restrict__ rows, const int *__restrict__ Ai,
+                           const int *__restrict__ Aj, const double *__restrict__ Av, const int *__restrict__ Si,
+                           const int *__restrict__ Sj, const int *__restrict__ pass, const int *__restrict__ col,
+                           int color, const int *__restrict__ Qi, int *__restrict__ Qj, double *__restrict__ Qv,
+                           const double *__restrict__ rsum, double *__restrict__ w)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= m) { return; }
+   const int i1 = rows[r];
+   const int a1 = Ai[i1 + 1];
+   const int q0 = Qi[r];
+   int q = q0;
+   if (!w)
+   {
+      int j2 = Ai[i1];
+      for (int k = Si[i1]; k < Si[i1 + 1]; k++)
+      {
+         const int j1 = Sj[k];
+         while (j2 < a1 && Aj[j2] != j1) { j2++; }
+         if (j2 == a1) { break; }
+         if (pass[j1] == color) { Qj[q] = col[j1]; Qv[q] = Av[j2]; q++; }
+      }
+      double sum = 0.0;
+      for (int k = q0; k < q; k++) { sum += Qv[k]; }
+      const double value = sum * Av[Ai[i1]];
+      double rs = rsum[i1];
+      if (value != 0) { rs /= value; }
+      for (int k = q0; k < q; k++) { Qv[k] = -Qv[k] * rs; }
+   }
+   else
+   {
+      double ws = 0.0;
+      int j2 = Ai[i1] + 1;
+      for (int k = Si[i1]; k < Si[i1 + 1]; k++)
+      {
+         const int j1 = Sj[k];
+         while (j2 < a1 && Aj[j2] != j1) { ws += Av[j2]; j2++; }
+         if (j2 == a1) { break; }
+         if (pass[j1] == color) { Qj[q] = col[j1]; Qv[q] = Av[j2]; q++; }
+         else { ws += Av[j2]; }
+         j2++;
+      }
+      while (j2 < a1) { ws += Av[j2]; j2++; }
+      w[r] = ws;
+   }
+}
+
+extern "C" void gb_mmp_fill(int m, const int *rows, const int *Ai, const int *Aj, const double *Av, const int *Si,
+                            const int *Sj, const int *pass, const int *col, int color, const int *Qi, int *Qj,
+                            double *Qv, const double *rsum, double *w, cudaStream_t s)
+{
+   if (m <= 0) { return; }
+   k_mmp_fill<<<mp_blocks(m, 128), 128, 0, s>>>(m, rows, Ai, Aj, Av, Si, Sj, pass, col, color, Qi, Qj, Qv, rsum,
+                                                 w);
+   GB_COUNT(1);
+}
+
+// type 9 rows after the product (:1236-1265): s = the row's sum,
+// value = s a_ii, s += w[r], s /= value when value is not zero, entries *= -s
+__global__ void k_mmp_scale9(int m, const int *__restrict__ rows, const int *__restrict__ Ai,
+                             const double *__restrict__ Av, const int *__restrict__ Bi, double *__restrict__ Bv,
+                             const double *__restrict__ w)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= m) { return; }
+   double s = 0.0;
+   for (int k = Bi[r]; k < Bi[r + 1]; k++) { s += Bv[k]; }
+   const double value = s * Av[Ai[rows[r]]];
+   s += w[r];
+   if (value != 0) { s /= value; }
+   for (int k = Bi[r]; k < Bi[r + 1]; k++) { Bv[k] = -Bv[k] * s; }
+}
+
+extern "C" void gb_mmp_scale9(int m, const int *rows, const int *Ai, const double *Av, const int *Bi, double *Bv,
+                              const double *w, cudaStream_t s)
+{
+   if (m <= 0) { return; }
+   k_mmp_scale9<<<mp_blocks(m, 128), 128, 0, s>>>(m, rows, Ai, Av, Bi, Bv, w);
+   GB_COUNT(1);
+}
+
+// P's row lengths: 1 for C points, the length of the row `col` of the block
+// of the point's pass (pass - 2), 0 for points without a pass
+__global__ void k_mmp_len(int n, const int *__restrict__ CF, const int *__restrict__ pass,
+                          const int *__restrict__ col, gb_mmp_blocks B, int *__restrict__ len)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   int l = 0;
+   if (CF[i] == C_PT) { l = 1; }
+   else
+   {
+      const int b = pass[i] - 2;
+      if (b >= 0 && b < B.nblk) { l = B.i[b][col[i] + 1] - B.i[b][col[i]]; }
+   }
+   len[i] = l;
+}
+
+__global__ void k_mmp_gather(int n, const int *__restrict__ CF, const int *__restrict__ pass,
+                             const int *__restrict__ col, gb_mmp_blocks B, const int *__restrict__ Pi,
+                             int *__restrict__ Pj, double *__restrict__ Pv)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) { return; }
+   const int o = Pi[i], l = Pi[i + 1] - o;
+   if (CF[i] == C_PT)
+   {
+      Pj[o] = col[i];
+      Pv[o] = 1.0;
+      return;
+   }
+   if (l == 0) { return; }
+   const int b = pass[i] - 2;
+   const int k0 = B.i[b][col[i]];
+   for (int q = 0; q < l; q++)
+   {
+      Pj[o + q] = B.j[b][k0 + q];
+      Pv[o + q] = B.v[b][k0 + q];
+   }
+}
+
+extern "C" void gb_mmp_len(int n, const int *CF, const int *pass, const int *col, const gb_mmp_blocks *B, int *len,
+                           cudaStream_t s)
+{
+   k_mmp_len<<<mp_blocks(n, 256), 256, 0, s>>>(n, CF, pass, col, *B, len);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_mmp_gather(int n, const int *CF, const int *pass, const int *col, const gb_mmp_blocks *B,
+                              const int *Pi, int *Pj, double *Pv, cudaStream_t s)
+{
+   k_mmp_gather<<<mp_blocks(n, 256), 256, 0, s>>>(n, CF, pass, col, *B, Pi, Pj, Pv);
+   GB_COUNT(1);
+}
