@@ -1692,6 +1692,14 @@ int or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P
 
 int or_l1_norms(const or_csr *A, int option, double *l1)
 {
+   return or_l1_norms_cf(A, option, NULL, l1);
+}
+
+/* CF != NULL (option 1 with relax_order 1, par_amg_setup.c:3352-3360): the
+ * row sum takes only the columns of the row's own CF value
+ * (hypre_CSRMatrixComputeRowSumHost src/seq_mv/csr_matop.c:1866-1905) */
+int or_l1_norms_cf(const or_csr *A, int option, const int *CF, double *l1)
+{
    int n = A->nr;
    #pragma omp parallel for schedule(static)
    for (int i = 0; i < n; i++)
@@ -1700,6 +1708,7 @@ int or_l1_norms(const or_csr *A, int option, double *l1)
       for (int k = A->i[i]; k < A->i[i + 1]; k++)
       {
          if (A->j[k] == i) { d = A->v[k]; }
+         if (CF && CF[i] != CF[A->j[k]]) { continue; }
          s += fabs(A->v[k]);
       }
       double v;
@@ -1786,14 +1795,34 @@ static void gselim(double *A, double *x, int n)
 /* ------------------------------------------------------------------------ */
 
 static void relax_l1_jacobi(const or_csr *A, const double *f, const double *l1, double w,
-                            double *u, double *V, int u_zero)
+                            double *u, double *V, int u_zero, const int *CF, int pts)
 {
    /* hypre_BoomerAMGRelax7Jacobi src/parcsr_ls/par_relax.c:1178 (relax 18 calls it
-    * for relax_points == 0, :338-365): V = w(f - Au); u += V / l1 */
+    * for relax_points == 0, :338-365): V = w(f - Au); u += V / l1, with
+    * relax_points != 0 only where CF == relax_points (:1237-1240) */
    int n = A->nr;
    if (u_zero) { for (int i = 0; i < n; i++) { V[i] = w * f[i]; } }
    else { or_matvec(-w, A, u, w, f, V); }
-   for (int i = 0; i < n; i++) { u[i] += V[i] / l1[i]; }
+   for (int i = 0; i < n; i++) { if (!pts || CF[i] == pts) { u[i] += V[i] / l1[i]; } }
+}
+
+static void relax_jacobi_cf(const or_csr *A, const double *f, const double *l1, double w, double *u, double *V,
+                            const int *CF, int pts)
+{
+   /* relax 18 with relax_points != 0 on the host,
+    * hypre_BoomerAMGRelaxWeightedJacobi_core src/parcsr_ls/par_relax.c:180-320
+    * (Skip_diag 0): over the values from before the relaxation, rows with
+    * CF == relax_points and l1 != 0 take u += w * (f - A u) / l1, the
+    * residual summed in row order */
+   int n = A->nr;
+   memcpy(V, u, sizeof(double) * (size_t) n);
+   for (int i = 0; i < n; i++)
+   {
+      if (CF[i] != pts || l1[i] == 0.0) { continue; }
+      double res = f[i];
+      for (int jj = A->i[i]; jj < A->i[i + 1]; jj++) { res -= A->v[jj] * V[A->j[jj]]; }
+      u[i] += w * res / l1[i];
+   }
 }
 
 static void relax_two_stage_gs(const or_csr *A, const double *f, double w, int inner,
@@ -2115,7 +2144,7 @@ static void relax_cheby(const or_csr *A, const double *f, const double *ds, cons
  * (the row's first entry, the diagonal); skip: leave the first entry out of
  * the sums.  Vt: the values before the relaxation (the scaled form's Vtemp). */
 static void relax_hybrid_gs(const or_csr *A, const double *f, const double *d, double w, double omega, int dir0,
-                            int nsw, int skip, double *u, double *Vt)
+                            int nsw, int skip, double *u, double *Vt, const int *CF, int pts)
 {
    int n = A->nr;
    const int non_scale = w == 1.0 && omega == 1.0;
@@ -2128,7 +2157,7 @@ static void relax_hybrid_gs(const or_csr *A, const double *f, const double *d, d
       for (int i = ib; i != ie; i += dir)
       {
          const double di = d ? d[i] : A->v[A->i[i]];
-         if (di == 0.0) { continue; }
+         if (di == 0.0 || (pts && CF[i] != pts)) { continue; }
          if (non_scale)
          {
             double res = f[i];
@@ -2153,8 +2182,12 @@ static void relax_hybrid_gs(const or_csr *A, const double *f, const double *d, d
 
 static int hybrid_gs_type(int t) { return t == 3 || t == 4 || t == 6 || t == 8 || t == 13 || t == 14; }
 
-static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u, int u_zero)
+/* One relaxation (hypre_BoomerAMGRelax src/parcsr_ls/par_relax.c:20-172);
+ * pts: relax_points (0 all points; 1 / -1 only the points with that CF value,
+ * for the smoothers that look at it: Jacobi and hybrid Gauss-Seidel) */
+static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u, int u_zero, int pts)
 {
+   const int *CF = pts ? H->CF[lvl] : NULL;
    const or_csr *A = &H->A[lvl];
    double w = H->prm.relax_weight;
    if (type == 16)
@@ -2176,11 +2209,15 @@ static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u
       const double omega = 1.0;
       const int skip = l1 ? !(w == 1.0 && omega == 1.0) : 1;
       relax_hybrid_gs(A, f, l1 ? H->l1[lvl] : NULL, w, omega, (type == 4 || type == 14) ? -1 : 1,
-                      (type == 6 || type == 8) ? 2 : 1, skip, u, H->Ztmp);
+                      (type == 6 || type == 8) ? 2 : 1, skip, u, H->Ztmp, CF, pts);
+   }
+   else if (type == 18 && pts)
+   {
+      relax_jacobi_cf(A, f, H->l1[lvl], w, u, H->Vtmp, CF, pts);
    }
    else if (type == 18 || type == 7)
    {
-      relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero);
+      relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero, CF, pts);
    }
    else if (type == 11 || type == 12)
    {
@@ -2188,8 +2225,25 @@ static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u
    }
    else
    {
-      relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero);
+      relax_l1_jacobi(A, f, H->l1[lvl], w, u, H->Vtmp, u_zero, CF, pts);
    }
+}
+
+/* hypre_BoomerAMGRelaxIF src/parcsr_ls/par_relax_interface.c:20-64: with
+ * relax_order 1 a relaxation of the down (up) cycle is two, over the C then
+ * the F points (F then C); the coarsest level and a single-level hierarchy
+ * relax all points (par_cycle.c:441-452).  Smoothers that ignore the points
+ * (two-stage Gauss-Seidel) then simply run twice; Chebyshev is not routed
+ * through it (:545-556). */
+static void relax_if(or_hierarchy *H, int lvl, int type, int cycle_param, const double *f, double *u, int u_zero)
+{
+   if (H->prm.relax_order == 1 && cycle_param < 3 && H->num_levels > 1 && type != 16)
+   {
+      const int p0 = cycle_param < 2 ? 1 : -1;
+      relax(H, lvl, type, f, u, u_zero, p0);
+      relax(H, lvl, type, f, u, 0, -p0);
+   }
+   else { relax(H, lvl, type, f, u, u_zero, 0); }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -2288,7 +2342,7 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
             break;
          }
          if (prm->interp_type == 6) { or_extpi_interp(A, &S, CF, &P); }
-         else if (prm->interp_type == 3) { or_dir_interp(A, &S, CF, &P); }
+         else if (prm->interp_type == 3 || prm->interp_type == 15) { or_dir_interp(A, &S, CF, &P); }   /* par_interp.c:2580-2610 */
          else if (prm->interp_type == 14) { or_ext_interp(A, &S, CF, &P); }
          else { mod_interp(A, &S, CF, prm->interp_type, &P); }   /* 16, 17, 18 */
          or_truncate(&P, prm->trunc_factor, prm->p_max_elmts);
@@ -2333,7 +2387,7 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
       if (t1 == 7 || t2 == 7 || (t3 == 7 && last) || t1 == 11 || t2 == 11 || (t3 == 11 && last) ||
           t1 == 12 || t2 == 12 || (t3 == 12 && last)) { opt = 5; }
       H->l1[l] = xmalloc(sizeof(double) * (n ? n : 1));
-      or_l1_norms(&H->A[l], opt, H->l1[l]);
+      or_l1_norms_cf(&H->A[l], opt, (opt == 1 && !last && prm->relax_order) ? H->CF[l] : NULL, H->l1[l]);
    }
    H->Vtmp = xcalloc(H->A[0].nr, sizeof(double));
    H->Ztmp = xcalloc(H->A[0].nr, sizeof(double));
@@ -2402,7 +2456,7 @@ int or_amg_vcycle(or_hierarchy *H, const double *f, double *u)
    {
       for (int s = 0; s < H->prm.num_sweeps; s++)
       {
-         relax(H, l, H->prm.relax_down, H->F[l], H->U[l], (l > 0 || u0_zero) && s == 0);
+         relax_if(H, l, H->prm.relax_down, 1, H->F[l], H->U[l], (l > 0 || u0_zero) && s == 0);
       }
       /* residual and restriction (:739-807) */
       or_matvec(-1.0, &H->A[l], H->U[l], 1.0, H->F[l], H->Vtmp);
@@ -2423,7 +2477,7 @@ int or_amg_vcycle(or_hierarchy *H, const double *f, double *u)
       }
       else
       {
-         relax(H, l, H->prm.relax_coarse, H->F[l], H->U[l], 1);
+         relax(H, l, H->prm.relax_coarse, H->F[l], H->U[l], 1, 0);
       }
    }
    for (int l = nl - 2; l >= 0; l--)
@@ -2432,7 +2486,7 @@ int or_amg_vcycle(or_hierarchy *H, const double *f, double *u)
       or_matvec(1.0, &H->P[l], H->U[l + 1], 1.0, H->U[l], H->U[l]);
       for (int s = 0; s < H->prm.num_sweeps; s++)
       {
-         relax(H, l, H->prm.relax_up, H->F[l], H->U[l], 0);
+         relax_if(H, l, H->prm.relax_up, 2, H->F[l], H->U[l], 0);
       }
    }
    memcpy(u, H->U[0], sizeof(double) * n0);

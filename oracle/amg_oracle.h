@@ -52,6 +52,7 @@ typedef struct
    int    cheby_scale;        /* 1 */
    int    cheby_variant;      /* 0 */
    int    cheby_eig_est;      /* 10 */
+   int    relax_order;        /* 0 lexicographic, 1 C/F (C then F down, F then C up) */
 } or_amg_params;
 
 typedef struct
@@ -93,6 +94,7 @@ int    or_truncate(or_csr *P, double trunc_factor, int max_elmts);
 int    or_transpose(const or_csr *A, or_csr *AT);
 int    or_rap(const or_csr *P, const or_csr *A, or_csr *Ac);
 int    or_l1_norms(const or_csr *A, int option, double *l1);
+int    or_l1_norms_cf(const or_csr *A, int option, const int *CF, double *l1);
 int    or_matmul(const or_csr *A, const or_csr *B, or_csr *C);
 int    or_matmat_flat(int nra, int nca, int ncb, const int *Ai, const int *Aj, const double *Av,
                       const int *Bi, const int *Bj, const double *Bv, int **Ci, int **Cj, double **Cv);

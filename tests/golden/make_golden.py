@@ -87,6 +87,9 @@ CASES = {
                               solver=1, full=True),
     "fv_12_dir3_pcg": dict(gen="fv", n=(12,), seed=3, th=0.25, mxrs=0.9, Pmx=4, interptype=3, rlx=18, coarse_th=9,
                            solver=1, full=True),
+    # BAMG-direct (15): the reference's host path builds the direct interpolation
+    "lap27_12_bamg15_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, interptype=15, rlx=18, coarse_th=9,
+                                solver=1, full=True),
     "aniso_40_dir3_tr_pcg": dict(gen="aniso", n=(40,), eps=0.001, th=0.25, mxrs=0.9, Pmx=3, tr=0.1, interptype=3,
                                  rlx=18, coarse_th=9, solver=1, full=True),
     "fv_12_mm18_pcg": dict(gen="fv", n=(12,), seed=4, th=0.25, mxrs=0.9, Pmx=4, interptype=18, rlx=18, coarse_th=9,
@@ -141,6 +144,24 @@ CASES = {
                                coarse_th=9, solver=1, full=True),
     "aniso_48_agg7_pcg": dict(gen="aniso", n=(48,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=7,
                               rlx=18, coarse_th=9, solver=1, full=True),
+    # C/F relaxation (relax_order 1): C then F points on the way down, F then
+    # C on the way up; l1-Jacobi with l1 norms over the row's own C/F class,
+    # Jacobi, hybrid Gauss-Seidel (forward/backward/symmetric, l1, weighted),
+    # two-stage Gauss-Seidel (which ignores the points, so it runs twice)
+    "lap7_14_cf18_pcg": dict(kind=7, n=(14, 14, 14), th=0.25, mxrs=1.0, Pmx=4, rlx=18, relax_order=1, coarse_th=9,
+                             solver=1, full=True),
+    "lap27_16_agg4_cf18_pcg": dict(kind=27, n=(16, 16, 16), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4, rlx=18,
+                                   relax_order=1, coarse_th=9, solver=1, full=True),
+    "fv_12_cf7_w07_fgmres": dict(gen="fv", n=(12,), seed=9, th=0.25, mxrs=0.9, Pmx=4, rlx=7, w=0.7, relax_order=1,
+                                 coarse_th=9, solver=61, k=30, full=True),
+    "lap7_12_cf6_pcg": dict(kind=7, n=(12, 12, 12), th=0.25, mxrs=1.0, Pmx=4, rlx=6, relax_order=1, coarse_th=9,
+                            solver=1, full=True),
+    "lap27_12_cf13_14_fgmres": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=13, rlx_down=13, rlx_up=14,
+                                    relax_order=1, coarse_th=9, solver=61, k=30, full=True),
+    "lap7_13_cf11_fgmres": dict(kind=7, n=(13, 13, 13), th=0.25, mxrs=1.0, Pmx=4, rlx=11, relax_order=1,
+                                coarse_th=9, solver=61, k=30, full=True),
+    "aniso_40_cf8_w08_pcg": dict(gen="aniso", n=(40,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, rlx=8, w=0.8,
+                                 relax_order=1, coarse_th=9, solver=1, full=True),
     # edge cases: no strong couplings (coarsening stops at once, the single
     # level is above max_coarse_size and relaxes instead of a direct solve),
     # a level cap that leaves a large coarsest level, a matrix within
@@ -178,7 +199,7 @@ def dump_args(c, out):
         a = [DUMP, "-mat", mat]
     else:
         a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "w",
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "relax_order", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]

@@ -73,6 +73,8 @@ def oracle_params(c):
         p["agg_p_max_elmts"] = c["agg_Pmx"]
     if "agg_P12_mx" in c:
         p["agg_p12_max_elmts"] = c["agg_P12_mx"]
+    if "relax_order" in c:
+        p["relax_order"] = c["relax_order"]
     if "max_levels" in c:
         p["max_levels"] = c["max_levels"]
     return p
@@ -92,6 +94,8 @@ def amg_params(c):
         p["AggPMaxElmts"] = c["agg_Pmx"]
     if "agg_P12_mx" in c:
         p["AggP12MaxElmts"] = c["agg_P12_mx"]
+    if "relax_order" in c:
+        p["RelaxOrder"] = c["relax_order"]
     if "max_levels" in c:
         p["MaxLevels"] = c["max_levels"]
     if "cheby_order" in c:

@@ -240,3 +240,37 @@ def test_error_flags(gb):
     L.HYPRE_ClearAllErrors()
     assert L.HYPRE_BoomerAMGSetup(None, None, None, None) & gb.HYPRE_ERROR_ARG
     L.HYPRE_ClearAllErrors()
+
+
+
+def test_unsupported_options_are_refused(gb, oracle_mod):
+    """Option values without a bit-exact implementation return
+    HYPRE_ERROR_GENERIC instead of silently running something else; the
+    supported ones (including BAMG-direct 15, which the reference's host path
+    builds as the direct interpolation) are accepted."""
+    import ctypes as C
+    L = gb.lib()
+    amg = gb.BoomerAMG()
+    for v in (0, 1, 2, 4, 5, 8):
+        L.HYPRE_ClearAllErrors()
+        assert amg.set("InterpType", v) & gb.HYPRE_ERROR_GENERIC, v
+    for v in (3, 6, 14, 15, 16, 17, 18):
+        L.HYPRE_ClearAllErrors()
+        assert amg.set("InterpType", v) == 0, v
+    L.HYPRE_ClearAllErrors()
+    amg.destroy()
+    # aggressive interpolation types are checked at setup: the two-stage
+    # standard (2) and extended (3) ones are refused
+    I, J, V = oracle_mod.stencil(7, 8, 8, 8)
+    n = len(I) - 1
+    A = gb.IJMatrix(I, J, V)
+    b, x = gb.IJVector(n, np.ones(n)), gb.IJVector(n, np.zeros(n))
+    for at, ok in ((2, False), (3, False), (8, True)):
+        amg = gb.BoomerAMG(MaxRowSum=1.0, StrongThreshold=0.25, AggNumLevels=1, AggInterpType=at, Tol=0.0,
+                           MaxIter=1)
+        L.HYPRE_ClearAllErrors()
+        err = L.HYPRE_BoomerAMGSetup(amg.h, A.par, b.par, x.par)
+        assert bool(err & gb.HYPRE_ERROR_GENERIC) != ok, at
+        L.HYPRE_ClearAllErrors()
+        amg.destroy()
+    A.destroy(); b.destroy(); x.destroy()
