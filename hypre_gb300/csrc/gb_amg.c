@@ -1288,12 +1288,20 @@ static int setup_level(gb_amg *amg, int l, double *t_phase)
       {
          if (extpi_host(A, &S, CF, f2c, n, NULL, nc, prm->interp_type == 6, &P)) { return -1; }
       }
-      else if (prm->interp_type == 3) { if (dir_interp(A, &S, CF, f2c, nc, &P)) { return -1; } }
+      /* 15 (BAMG-direct) is the direct interpolation on the reference's
+       * host path, which does not look at interp_type (par_interp.c:2580-2610) */
+      else if (prm->interp_type == 3 || prm->interp_type == 15)
+      {
+         if (dir_interp(A, &S, CF, f2c, nc, &P)) { return -1; }
+      }
       else if (mm_interp(A, &S, CF, f2c, nc, prm->interp_type, &P)) { return -1; }
       /* ext(+i) and direct interpolation turn the points without strong
        * couplings (-3) into F points (par_lr_interp.c:1887-1893, :5488-5491,
        * par_interp.c:2560-2563); the modified interpolations keep -3 */
-      if (prm->interp_type == 6 || prm->interp_type == 14 || prm->interp_type == 3) { gb_sf_to_f(n, CF, s); }
+      if (prm->interp_type == 6 || prm->interp_type == 14 || prm->interp_type == 3 || prm->interp_type == 15)
+      {
+         gb_sf_to_f(n, CF, s);
+      }
       truncate_host(&P, prm->trunc_factor, prm->p_max_elmts);
       gb_dfree(f2c);
    }
@@ -1670,7 +1678,11 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
       gb_level *L = &amg->lev[l];
       int n = L->n;
       L->l1 = (double *) gb_dmalloc(sizeof(double) * (size_t) (n ? n : 1));
-      gb_l1_norms(n, L->A->A.i, L->A->A.j, L->A->A.v, relax_l1_option_level(prm, l, amg->num_levels), L->l1, s);
+      /* with relax_order the l1-Jacobi norms of the levels above the coarsest
+       * sum over the row's own C/F class (par_amg_setup.c:3352-3360) */
+      const int opt = relax_l1_option_level(prm, l, amg->num_levels);
+      const int *cfl = (opt == 1 && prm->relax_order && l < amg->num_levels - 1) ? L->CF : NULL;
+      gb_l1_norms(n, L->A->A.i, L->A->A.j, L->A->A.v, opt, cfl, L->l1, s);
       L->l1f = (float *) gb_dmalloc(sizeof(float) * (size_t) (n ? n : 1));
       gb_d2f(n, L->l1, L->l1f, s);
       L->relax_w = prm->level_relax_weight ? prm->level_relax_weight[l] : prm->relax_weight;
@@ -1802,7 +1814,7 @@ static void twostage_gs_d(gb_amg *amg, int l, int inner, const double *f, double
  * Unscaled (weight and outer weight 1): 3/4/6 leave the diagonal out of the
  * sum and divide by it, 8/13/14 include it and add res / l1; scaled: the
  * reference's weighted form over the values from before the relaxation. */
-static void hybrid_gs_d(gb_amg *amg, int l, int type, const double *f, double *u, int u_zero)
+static void hybrid_gs_d(gb_amg *amg, int l, int type, const double *f, double *u, int u_zero, int pts)
 {
    gb_level *L = &amg->lev[l];
    cudaStream_t s = gb_stream();
@@ -1824,12 +1836,12 @@ static void hybrid_gs_d(gb_amg *amg, int l, int type, const double *f, double *u
    for (int k = 0; k < nsw; k++)
    {
       gb_hgs_sweep_d(n, A->nnz, A->i, A->j, A->v, f, u, L->V, ut, l1 ? L->l1 : NULL, k == 0 ? dir0 : -dir0, skip,
-                     w, omega, L->hgs_flags, g_hgs_err, s);
+                     w, omega, L->CF, pts, L->hgs_flags, g_hgs_err, s);
    }
    g_hgs_used = 1;
 }
 
-static void hybrid_gs_f(gb_amg *amg, int l, int type, const float *f, float *u, int u_zero)
+static void hybrid_gs_f(gb_amg *amg, int l, int type, const float *f, float *u, int u_zero, int pts)
 {
    gb_level *L = &amg->lev[l];
    cudaStream_t s = gb_stream();
@@ -1851,7 +1863,7 @@ static void hybrid_gs_f(gb_amg *amg, int l, int type, const float *f, float *u, 
    for (int k = 0; k < nsw; k++)
    {
       gb_hgs_sweep_f(n, L->A->A.nnz, A->i, A->j, (const float *) A->v, f, u, L->Vf, ut, l1 ? L->l1f : NULL,
-                     k == 0 ? dir0 : -dir0, skip, w, omega, L->hgs_flags, g_hgs_err, s);
+                     k == 0 ? dir0 : -dir0, skip, w, omega, L->CF, pts, L->hgs_flags, g_hgs_err, s);
    }
    g_hgs_used = 1;
 }
@@ -1919,11 +1931,43 @@ static void cheby_f(gb_amg *amg, int l, const float *f, float *u, int u_zero)
    gb_spmv_f(A, q, u, GB_EPI_CHEB_LAST, (float) c[0], 0.0f, r, ds, 0.0f, NULL, NULL, s);
 }
 
+/* One relaxation in place on u of the points of class pts (C/F relaxation,
+ * hypre_BoomerAMGRelaxIF src/parcsr_ls/par_relax_interface.c:20-64 into
+ * hypre_BoomerAMGRelax): the Jacobi types update the rows with CF == pts (and
+ * a nonzero divisor) from one Jacobi step over the values from before the
+ * relaxation; hybrid Gauss-Seidel sweeps leave the other rows as they are;
+ * two-stage Gauss-Seidel ignores the points and relaxes all of them. */
+static void relax_points_d(gb_amg *amg, int l, int type, const double *f, double *u, int u_zero, int pts)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, f, u, u_zero); }
+   else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, f, u, u_zero, pts); }
+   else
+   {
+      if (u_zero) { gb_fill_d(L->n, u, 0.0, s); }
+      relax_d(amg, l, type, f, u, L->U2, u_zero);
+      gb_select_points_d(L->n, L->CF, pts, L->l1, L->U2, u, s);
+   }
+}
+
+/* relax_order 1 above the coarsest level: a relaxation of the down cycle
+ * (cycle_param 1) is two, over the C and then the F points; of the up cycle
+ * (2) over the F and then the C points (par_relax_interface.c:36-56) */
+static void relax_cf_d(gb_amg *amg, int l, int type, int cycle_param, const double *f, double *u, int u_zero)
+{
+   const int p0 = cycle_param < 2 ? 1 : -1;
+   relax_points_d(amg, l, type, f, u, u_zero, p0);
+   relax_points_d(amg, l, type, f, u, 0, -p0);
+}
+
 static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
 {
    gb_amg_params *prm = &amg->prm;
    cudaStream_t s = gb_stream();
    int nl = amg->num_levels;
+   /* C/F relaxation order above the coarsest level (par_cycle.c:441-452) */
+   const int cf = prm->relax_order == 1 && nl > 1;
    const double *F[32];
    double *U[32];
    F[0] = f0; U[0] = u0;
@@ -1935,9 +1979,10 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       int uz = (l > 0) || u0_zero;
       for (int sw = 0; sw < prm->num_sweeps[1]; sw++)
       {
-         if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], uz && sw == 0); }
+         if (cf && type != 16) { relax_cf_d(amg, l, type, 1, F[l], U[l], uz && sw == 0); }
+         else if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], uz && sw == 0); }
          else if (type == 16) { cheby_d(amg, l, F[l], U[l], uz && sw == 0); }
-         else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], uz && sw == 0); }
+         else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], uz && sw == 0, 0); }
          else
          {
             if (uz && sw == 0) { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
@@ -1958,7 +2003,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       gb_level *L = &amg->lev[l];
       if (amg->coarse_inv) { gb_dense_apply_d(amg->coarse_n, amg->coarse_inv, F[l], U[l], s); }
       else if (nl == 1 && !u0_zero && prm->relax_type[3] == 16) { cheby_d(amg, l, F[l], U[l], 0); }
-      else if (nl == 1 && !u0_zero && hgs_type(prm->relax_type[3])) { hybrid_gs_d(amg, l, prm->relax_type[3], F[l], U[l], 0); }
+      else if (nl == 1 && !u0_zero && hgs_type(prm->relax_type[3])) { hybrid_gs_d(amg, l, prm->relax_type[3], F[l], U[l], 0, 0); }
       else if (nl == 1 && !u0_zero)
       {
          relax_d(amg, l, prm->relax_type[3], F[l], U[l], L->U2, 0);
@@ -1969,7 +2014,7 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
          int type = prm->relax_type[3];
          if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
          else if (type == 16) { cheby_d(amg, l, F[l], U[l], 1); }
-         else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], 1); }
+         else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], 1, 0); }
          else { relax_d(amg, l, type, F[l], U[l], U[l], 1); }
       }
    }
@@ -1979,13 +2024,19 @@ static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
       int type = prm->relax_type[2];
       /* u_f += P u_c written to U2, then the post-smoother writes back into U */
       gb_spmv_d(gb_solve_desc(L->P, GB_PREC_F64), U[l + 1], L->U2, 0, 1.0, 1.0, U[l], NULL, 0.0, NULL, NULL, s);
+      if (cf && type != 16)
+      {
+         cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+         for (int sw = 0; sw < prm->num_sweeps[2]; sw++) { relax_cf_d(amg, l, type, 2, F[l], U[l], 0); }
+         continue;
+      }
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
          if (type == 11 || type == 12 || type == 16 || hgs_type(type))
          {
             if (sw == 0) { cudaMemcpyAsync(U[l], L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
             if (type == 16) { cheby_d(amg, l, F[l], U[l], 0); }
-            else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], 0); }
+            else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, F[l], U[l], 0, 0); }
             else { twostage_gs_d(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0); }
          }
          else
@@ -2045,11 +2096,33 @@ static void twostage_gs_f(gb_amg *amg, int l, int inner, const float *f, float *
    }
 }
 
+static void relax_points_f(gb_amg *amg, int l, int type, const float *f, float *u, int u_zero, int pts)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, f, u, u_zero); }
+   else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, f, u, u_zero, pts); }
+   else
+   {
+      if (u_zero) { gb_fill_f(L->n, u, 0.f, s); }
+      relax_f(amg, l, type, f, u, L->U2f, u_zero);
+      gb_select_points_f(L->n, L->CF, pts, L->l1f, L->U2f, u, s);
+   }
+}
+
+static void relax_cf_f(gb_amg *amg, int l, int type, int cycle_param, const float *f, float *u, int u_zero)
+{
+   const int p0 = cycle_param < 2 ? 1 : -1;
+   relax_points_f(amg, l, type, f, u, u_zero, p0);
+   relax_points_f(amg, l, type, f, u, 0, -p0);
+}
+
 static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
 {
    gb_amg_params *prm = &amg->prm;
    cudaStream_t s = gb_stream();
    int nl = amg->num_levels;
+   const int cf = prm->relax_order == 1 && nl > 1;
    float *F[32] = {0}, *U[32] = {0};
    for (int l = 0; l < nl; l++) { F[l] = amg->lev[l].Ff; U[l] = amg->lev[l].Uf; }
    gb_d2f(amg->lev[0].n, f0d, F[0], s);
@@ -2060,9 +2133,10 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
       int vp = (prm->cycle_prec == GB_PREC_F16 && l == 0) ? GB_PREC_F16 : GB_PREC_F32;
       for (int sw = 0; sw < prm->num_sweeps[1]; sw++)
       {
-         if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], sw == 0); }
+         if (cf && type != 16) { relax_cf_f(amg, l, type, 1, F[l], U[l], sw == 0); }
+         else if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], sw == 0); }
          else if (type == 16) { cheby_f(amg, l, F[l], U[l], sw == 0); }
-         else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], sw == 0); }
+         else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], sw == 0, 0); }
          else if (sw == 0) { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
          else
          {
@@ -2081,7 +2155,7 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
          int type = prm->relax_type[3];
          if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 1); }
          else if (type == 16) { cheby_f(amg, l, F[l], U[l], 1); }
-         else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], 1); }
+         else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], 1, 0); }
          else { relax_f(amg, l, type, F[l], U[l], U[l], 1); }
       }
    }
@@ -2090,13 +2164,19 @@ static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
       gb_level *L = &amg->lev[l];
       int type = prm->relax_type[2];
       gb_spmv_f(gb_solve_desc(L->P, GB_PREC_F32), U[l + 1], L->U2f, 0, 1.f, 1.f, U[l], NULL, 0.f, NULL, NULL, s);
+      if (cf && type != 16)
+      {
+         cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+         for (int sw = 0; sw < prm->num_sweeps[2]; sw++) { relax_cf_f(amg, l, type, 2, F[l], U[l], 0); }
+         continue;
+      }
       for (int sw = 0; sw < prm->num_sweeps[2]; sw++)
       {
          if (type == 11 || type == 12 || type == 16 || hgs_type(type))
          {
             if (sw == 0) { cudaMemcpyAsync(U[l], L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s); }
             if (type == 16) { cheby_f(amg, l, F[l], U[l], 0); }
-            else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], 0); }
+            else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, F[l], U[l], 0, 0); }
             else { twostage_gs_f(amg, l, type == 11 ? 1 : 2, F[l], U[l], 0); }
          }
          else if (sw == 0) { relax_f(amg, l, type, F[l], L->U2f, U[l], 0); }
@@ -2306,10 +2386,10 @@ HYPRE_Int HYPRE_BoomerAMGSetInterpType(HYPRE_Solver solver, HYPRE_Int v)
 {
    gb_amg *a = amg_of(solver, 1);
    if (!a) { return gb_error_flag; }
-   if (v != 6 && v != 3 && v != 14 && v != 16 && v != 17 && v != 18)
+   if (v != 6 && v != 3 && v != 15 && v != 14 && v != 16 && v != 17 && v != 18)
    {
-      gb_error(HYPRE_ERROR_GENERIC,
-               "interp_type: extended+i (6), direct (3), extended (14) and the modified 16, 17, 18 are supported");
+      gb_error(HYPRE_ERROR_GENERIC, "interp_type: extended+i (6), direct (3, 15), extended (14) and the modified "
+                                    "16, 17, 18 are supported");
       gb_error_in_arg(2);
       return gb_error_flag;
    }
@@ -2358,7 +2438,13 @@ HYPRE_Int HYPRE_BoomerAMGSetRelaxOrder(HYPRE_Solver solver, HYPRE_Int v)
 {
    gb_amg *a = amg_of(solver, 1);
    if (!a) { return gb_error_flag; }
-   if (v != 0) { gb_error(HYPRE_ERROR_GENERIC, "relax_order: only 0 (lexicographic) is supported"); }
+   if (v != 0 && v != 1)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "relax_order: 0 (lexicographic) and 1 (C/F) are supported");
+      gb_error_in_arg(2);
+      return gb_error_flag;
+   }
+   a->prm.relax_order = v;
    return gb_error_flag;
 }
 

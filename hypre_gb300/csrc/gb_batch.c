@@ -211,6 +211,11 @@ HYPRE_Int HYPRE_GB300_BatchedPCGSetup(HYPRE_Solver solver, HYPRE_Solver amg_solv
          return gb_error_flag;
       }
    }
+   if (prm->relax_order != 0)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "batched PCG: relax_order must be 0 (lexicographic)");
+      return gb_error_flag;
+   }
    if (prm->agg_num_levels > 0)
    {
       gb_error(HYPRE_ERROR_GENERIC, "batched PCG: aggressive coarsening is not supported");

@@ -75,7 +75,9 @@ __device__ __forceinline__ void hgs_wait(bool dep, int col, const int *flags, in
    }
 }
 
-// One sweep.  u: values updated in place; uo: u as it was when the sweep
+// One sweep.  cf / pts: with pts != 0 only the rows with cf == pts relax
+// (C/F relaxation; the others keep their values, par_relax.h:45,77).
+// u: values updated in place; uo: u as it was when the sweep
 // started (read for the rows not yet visited and for the row's own entry);
 // ut: u before the first sweep of the relaxation (the scaled form's second
 // sum, hypre's Vtemp), NULL when unscaled; dvec: l1 norms (relax 8/13/14) or
@@ -87,7 +89,7 @@ __global__ void __launch_bounds__(256) k_hgs(int n, const int *__restrict__ Ai, 
                                              const T *__restrict__ Av, const T *__restrict__ f, T *u,
                                              const T *__restrict__ uo, const T *__restrict__ ut,
                                              const T *__restrict__ dvec, int dir, int skip, T w, T omega, T prod,
-                                             int *flags, int *err)
+                                             const int *__restrict__ cf, int pts, int *flags, int *err)
 {
    const int lane = threadIdx.x & 31;
    int *counter = flags + n;
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(256) k_hgs(int n, const int *__restrict__ Ai, 
       const T aii = e > b ? Av[b] : (T) 0;
       const T di = dvec ? dvec[i] : aii;
       T ui = uo[i];
-      if (di != (T) 0)
+      if (di != (T) 0 && (pts == 0 || cf[i] == pts))
       {
          T res = f[i], res0 = 0, res2 = 0;
          for (int c = b + skip; c < e; c += 32)
@@ -168,7 +170,8 @@ template <typename T>
 __global__ void __launch_bounds__(512) k_hgs_seq(int n, int nnz, const int *__restrict__ Ai,
                                                  const int *__restrict__ Aj, const T *__restrict__ Av,
                                                  const T *__restrict__ f, T *u, const T *__restrict__ ut,
-                                                 const T *__restrict__ dvec, int dir, int skip, T w, T omega, T prod)
+                                                 const T *__restrict__ dvec, int dir, int skip, T w, T omega, T prod,
+                                                 const int *__restrict__ cf, int pts)
 {
    extern __shared__ __align__(16) unsigned char hgs_smem[];
    T *su = (T *) hgs_smem;
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(512) k_hgs_seq(int n, int nnz, const int *__re
          const T aii = e > b ? sav[b] : (T) 0;
          const T di = dvec ? sd[i] : aii;
          T ui = su[i];
-         if (di != (T) 0)
+         if (di != (T) 0 && (pts == 0 || cf[i] == pts))
          {
             T res = sf[i], res0 = 0, res2 = 0;
             for (int c = b + skip; c < e; c += 32)
@@ -251,8 +254,8 @@ __global__ void __launch_bounds__(512) k_hgs_seq(int n, int nnz, const int *__re
 
 template <typename T>
 static void hgs_sweep(int n, long long nnz, const int *Ai, const int *Aj, const T *Av, const T *f, T *u, T *uo,
-                      const T *ut, const T *dvec, int dir, int skip, double w, double omega, int *flags, int *err,
-                      cudaStream_t s)
+                      const T *ut, const T *dvec, int dir, int skip, double w, double omega, const int *cf, int pts,
+                      int *flags, int *err, cudaStream_t s)
 {
    if (n <= 0) { return; }
    const double prod0 = 1.0 - w * omega;
@@ -267,7 +270,7 @@ static void hgs_sweep(int n, long long nnz, const int *Ai, const int *Aj, const 
          attr_set = 1;
       }
       k_hgs_seq<T><<<1, 512, (size_t) smem, s>>>(n, (int) nnz, Ai, Aj, Av, f, u, ut, dvec, dir, skip, (T) w,
-                                                 (T) omega, (T) prod0);
+                                                 (T) omega, (T) prod0, cf, pts);
       GB_COUNT(1);
       return;
    }
@@ -277,21 +280,48 @@ static void hgs_sweep(int n, long long nnz, const int *Ai, const int *Aj, const 
    // few thousand rows, few enough that the spinning warps leave issue slots
    long long warps = n < 152LL * 16 ? n : 152LL * 16;
    int blocks = (int) ((warps * 32 + 255) / 256);
-   k_hgs<T><<<blocks, 256, 0, s>>>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, (T) w, (T) omega, (T) prod0, flags,
-                                   err);
+   k_hgs<T><<<blocks, 256, 0, s>>>(n, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, (T) w, (T) omega, (T) prod0, cf,
+                                   pts, flags, err);
    GB_COUNT(1);
 }
 
 extern "C" void gb_hgs_sweep_d(int n, long long nnz, const int *Ai, const int *Aj, const double *Av,
                                const double *f, double *u, double *uo, const double *ut, const double *dvec, int dir,
-                               int skip, double w, double omega, int *flags, int *err, cudaStream_t s)
+                               int skip, double w, double omega, const int *cf, int pts, int *flags, int *err,
+                               cudaStream_t s)
 {
-   hgs_sweep<double>(n, nnz, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
+   hgs_sweep<double>(n, nnz, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, cf, pts, flags, err, s);
 }
 
 extern "C" void gb_hgs_sweep_f(int n, long long nnz, const int *Ai, const int *Aj, const float *Av, const float *f,
                                float *u, float *uo, const float *ut, const float *dvec, int dir, int skip, double w,
-                               double omega, int *flags, int *err, cudaStream_t s)
+                               double omega, const int *cf, int pts, int *flags, int *err, cudaStream_t s)
 {
-   hgs_sweep<float>(n, nnz, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, flags, err, s);
+   hgs_sweep<float>(n, nnz, Ai, Aj, Av, f, u, uo, ut, dvec, dir, skip, w, omega, cf, pts, flags, err, s);
+}
+
+// C/F Jacobi half-relaxation: the rows of class pts (and a nonzero divisor)
+// take the Jacobi value t, the others keep u
+template <typename T>
+__global__ void k_select_points(int n, const int *__restrict__ cf, int pts, const T *__restrict__ d,
+                                const T *__restrict__ t, T *__restrict__ u)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n && cf[i] == pts && d[i] != (T) 0) { u[i] = t[i]; }
+}
+
+extern "C" void gb_select_points_d(int n, const int *CF, int pts, const double *d, const double *t, double *u,
+                                   cudaStream_t s)
+{
+   if (n <= 0) { return; }
+   k_select_points<double><<<(n + 255) / 256, 256, 0, s>>>(n, CF, pts, d, t, u);
+   GB_COUNT(1);
+}
+
+extern "C" void gb_select_points_f(int n, const int *CF, int pts, const float *d, const float *t, float *u,
+                                   cudaStream_t s)
+{
+   if (n <= 0) { return; }
+   k_select_points<float><<<(n + 255) / 256, 256, 0, s>>>(n, CF, pts, d, t, u);
+   GB_COUNT(1);
 }

@@ -148,6 +148,7 @@ typedef struct
    int    max_levels, max_coarse_size, min_coarse_size;
    int    relax_type[4];     /* [1] down, [2] up, [3] coarsest (reference grid_relax_type) */
    int    num_sweeps[4];
+   int    relax_order;       /* 0 lexicographic, 1 C/F (C then F down, F then C up) */
    double relax_weight;
    double *level_relax_weight;   /* optional, per level */
    int    cheby_order, cheby_scale, cheby_variant, cheby_eig_est;

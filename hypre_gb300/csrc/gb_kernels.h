@@ -204,7 +204,8 @@ void gb_mod_interp_scale(int variant, int nf, int nnzff, const int *fl, const in
 void gb_p1_len(int n, const int *CF, const int *f2f, const int *Wi, int *len, cudaStream_t s);
 void gb_p1_fill(int n, const int *CF, const int *f2c, const int *f2f, const int *Wi, const int *Wj, const double *Wv,
                 const int *Pi, int *Pj, double *Pv, cudaStream_t s);
-void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, double *l1, cudaStream_t s);
+void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, const int *CF, double *l1,
+                 cudaStream_t s);
 void gb_block_inverse(int nsys, const int *off, const int *Ai, const int *Aj, const double *Av,
                       const long long *doff, double *D, double *W, cudaStream_t s);
 void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, double *D, double *W, cudaStream_t s);
@@ -215,10 +216,14 @@ void gb_dense_inverse(int n, const int *Ai, const int *Aj, const double *Av, dou
  * ints; *err set when a dependency wait ran out */
 void gb_hgs_sweep_d(int n, long long nnz, const int *Ai, const int *Aj, const double *Av, const double *f,
                     double *u, double *uo, const double *ut, const double *dvec, int dir, int skip, double w,
-                    double omega, int *flags, int *err, cudaStream_t s);
+                    double omega, const int *cf, int pts, int *flags, int *err, cudaStream_t s);
 void gb_hgs_sweep_f(int n, long long nnz, const int *Ai, const int *Aj, const float *Av, const float *f, float *u,
                     float *uo, const float *ut, const float *dvec, int dir, int skip, double w, double omega,
-                    int *flags, int *err, cudaStream_t s);
+                    const int *cf, int pts, int *flags, int *err, cudaStream_t s);
+/* u[i] = t[i] where CF[i] == pts and d[i] != 0 (the points a C/F Jacobi
+ * half-relaxation updates) */
+void gb_select_points_d(int n, const int *CF, int pts, const double *d, const double *t, double *u, cudaStream_t s);
+void gb_select_points_f(int n, const int *CF, int pts, const float *d, const float *t, float *u, cudaStream_t s);
 
 /* solve phase */
 void gb_spmv_d(const gb_spmv_desc *A, const double *x, double *y, int mode, double alpha, double beta,

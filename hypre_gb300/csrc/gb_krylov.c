@@ -519,7 +519,7 @@ HYPRE_Int HYPRE_ParCSRDiagScaleSetup(HYPRE_Solver solver, HYPRE_ParCSRMatrix A, 
    {
       A->diag = (double *) gb_dmalloc(sizeof(double) * (size_t) (A->A.nr ? A->A.nr : 1));
       /* option 5 of the l1-norm kernel: the diagonal, 0 -> 1 (sign kept) */
-      gb_l1_norms(A->A.nr, A->A.i, A->A.j, A->A.v, 5, A->diag, gb_stream());
+      gb_l1_norms(A->A.nr, A->A.i, A->A.j, A->A.v, 5, NULL, A->diag, gb_stream());
    }
    return gb_error_flag;
 }

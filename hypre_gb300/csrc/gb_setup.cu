@@ -2068,27 +2068,31 @@ extern "C" void gb_spgemm_rc(int nrows, int square, const int *Ai, const int *Aj
 // option 1: sum_j |a_ij|; option 5: a_ii (0 -> 1); rows with a_ii < 0 negated.
 // ---------------------------------------------------------------------------
 __global__ void k_l1(int n, const int *__restrict__ Ai, const int *__restrict__ Aj, const double *__restrict__ Av,
-                     int option, double *__restrict__ l1)
+                     int option, const int *__restrict__ CF, double *__restrict__ l1)
 {
    int i = blockIdx.x * blockDim.x + threadIdx.x;
    if (i >= n) { return; }
    double d = 0.0, s = 0.0;
+   const int ci = CF ? CF[i] : 0;
    for (int k = Ai[i]; k < Ai[i + 1]; k++)
    {
       double v = Av[k];
       if (Aj[k] == i) { d = v; }
+      if (CF && CF[Aj[k]] != ci) { continue; }
       s += fabs(v);
    }
-   // option 1: sum |a_ij|; 4 (one process): |a_ii|; 5: a_ii, 0 -> 1
+   // option 1: sum |a_ij| (with CF: over the columns of the row's own C/F
+   // class, hypre_CSRMatrixComputeRowSumHost src/seq_mv/csr_matop.c:1866);
+   // 4 (one process): |a_ii|; 5: a_ii, 0 -> 1
    double r = option == 1 ? s : option == 4 ? fabs(d) : (d != 0.0 ? d : 1.0);
    if (d < 0.0) { r = -r; }
    l1[i] = r;
 }
 
-extern "C" void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, double *l1,
-                            cudaStream_t s)
+extern "C" void gb_l1_norms(int n, const int *Ai, const int *Aj, const double *Av, int option, const int *CF,
+                            double *l1, cudaStream_t s)
 {
-   k_l1<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, option, l1);
+   k_l1<<<gb_blocks(n, 256), 256, 0, s>>>(n, Ai, Aj, Av, option, CF, l1);
    GB_COUNT(1);
 }
 
