@@ -68,6 +68,7 @@ void or_default_params(or_amg_params *p)
    p->cheby_fraction = 0.3;
    p->cheby_scale = 1;
    p->cheby_eig_est = 10;
+   p->cycle_type = 1;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -2441,55 +2442,79 @@ void or_amg_free(or_hierarchy *H)
 }
 
 /* ------------------------------------------------------------------------ */
-/* V(1,1) cycle, hypre_BoomerAMGCycle src/parcsr_ls/par_cycle.c:23-889       */
+/* One cycle, hypre_BoomerAMGCycle src/parcsr_ls/par_cycle.c:23-889: the     */
+/* reference's level counters choose the next level (V, W and F cycles)      */
 /* ------------------------------------------------------------------------ */
 
 int or_amg_vcycle(or_hierarchy *H, const double *f, double *u)
 {
-   int nl = H->num_levels;
-   int n0 = H->A[0].nr;
+   const int nl = H->num_levels;
+   const int n0 = H->A[0].nr;
+   const int ct = H->prm.cycle_type, fcycle = H->prm.fcycle;
    memcpy(H->F[0], f, sizeof(double) * n0);
    memcpy(H->U[0], u, sizeof(double) * n0);
-   int u0_zero = 1;
-   for (int i = 0; i < n0; i++) { if (u[i] != 0.0) { u0_zero = 0; break; } }
-   for (int l = 0; l < nl - 1; l++)
+   int *counter = xcalloc(nl, sizeof(int)), *zero = xcalloc(nl, sizeof(int));
+   zero[0] = 1;
+   for (int i = 0; i < n0; i++) { if (u[i] != 0.0) { zero[0] = 0; break; } }
+   /* :227-238 */
+   counter[0] = 1;
+   for (int k = 1; k < nl; k++) { counter[k] = fcycle ? 1 : ct; }
+   int fcycle_lev = nl - 2, level = 0, cycle_param = nl == 1 ? 3 : 1;
+   for (;;)
    {
-      for (int s = 0; s < H->prm.num_sweeps; s++)
+      /* relaxation (:430-660): the coarsest level's direct solve, or
+       * num_sweeps relaxations of the cycle part's type */
+      if (level == nl - 1)
       {
-         relax_if(H, l, H->prm.relax_down, 1, H->F[l], H->U[l], (l > 0 || u0_zero) && s == 0);
-      }
-      /* residual and restriction (:739-807) */
-      or_matvec(-1.0, &H->A[l], H->U[l], 1.0, H->F[l], H->Vtmp);
-      matvecT(&H->P[l], H->Vtmp, H->F[l + 1]);
-      memset(H->U[l + 1], 0, sizeof(double) * H->A[l + 1].nr);
-   }
-   /* coarsest */
-   {
-      int l = nl - 1;
-      int nn = H->A[l].nr;
-      if (H->coarse_lu)
-      {
-         double *work = xmalloc(sizeof(double) * (size_t) nn * nn);
-         memcpy(work, H->coarse_lu, sizeof(double) * (size_t) nn * nn);
-         memcpy(H->U[l], H->F[l], sizeof(double) * nn);
-         gselim(work, H->U[l], nn);
-         free(work);
+         const int nn = H->A[level].nr;
+         if (H->coarse_lu)
+         {
+            double *work = xmalloc(sizeof(double) * (size_t) nn * nn);
+            memcpy(work, H->coarse_lu, sizeof(double) * (size_t) nn * nn);
+            memcpy(H->U[level], H->F[level], sizeof(double) * nn);
+            gselim(work, H->U[level], nn);
+            free(work);
+         }
+         else { relax(H, level, H->prm.relax_coarse, H->F[level], H->U[level], nl > 1 || zero[level], 0); }
       }
       else
       {
-         relax(H, l, H->prm.relax_coarse, H->F[l], H->U[l], 1, 0);
+         const int type = cycle_param == 1 ? H->prm.relax_down : H->prm.relax_up;
+         for (int s = 0; s < H->prm.num_sweeps; s++)
+         {
+            relax_if(H, level, type, cycle_param, H->F[level], H->U[level], zero[level] && s == 0);
+            zero[level] = 0;
+         }
       }
-   }
-   for (int l = nl - 2; l >= 0; l--)
-   {
-      /* interpolation u_f += P u_c (:815-861), then post-relaxation */
-      or_matvec(1.0, &H->P[l], H->U[l + 1], 1.0, H->U[l], H->U[l]);
-      for (int s = 0; s < H->prm.num_sweeps; s++)
+      zero[level] = 0;
+      --counter[level];
+      if (counter[level] >= 0 && level != nl - 1)
       {
-         relax_if(H, l, H->prm.relax_up, 2, H->F[l], H->U[l], 0);
+         /* down (:730-807): residual, restriction, zero coarse guess */
+         or_matvec(-1.0, &H->A[level], H->U[level], 1.0, H->F[level], H->Vtmp);
+         matvecT(&H->P[level], H->Vtmp, H->F[level + 1]);
+         memset(H->U[level + 1], 0, sizeof(double) * H->A[level + 1].nr);
+         zero[level + 1] = 1;
+         ++level;
+         counter[level] = counter[level] > ct ? counter[level] : ct;
+         cycle_param = level == nl - 1 ? 3 : 1;
       }
+      else if (level != 0)
+      {
+         /* up (:808-860): u_f += P u_c */
+         or_matvec(1.0, &H->P[level - 1], H->U[level], 1.0, H->U[level - 1], H->U[level - 1]);
+         --level;
+         cycle_param = 2;
+         if (fcycle && fcycle_lev == level)
+         {
+            counter[level] = counter[level] > 1 ? counter[level] : 1;
+            fcycle_lev--;
+         }
+      }
+      else { break; }
    }
    memcpy(u, H->U[0], sizeof(double) * n0);
+   free(counter); free(zero);
    return 0;
 }
 

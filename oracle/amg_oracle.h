@@ -53,6 +53,8 @@ typedef struct
    int    cheby_variant;      /* 0 */
    int    cheby_eig_est;      /* 10 */
    int    relax_order;        /* 0 lexicographic, 1 C/F (C then F down, F then C up) */
+   int    cycle_type;         /* 1 V, 2 W (visits of each coarse level per visit of the finer) */
+   int    fcycle;             /* 0, or 1: F-cycle */
 } or_amg_params;
 
 typedef struct

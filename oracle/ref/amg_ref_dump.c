@@ -169,7 +169,7 @@ int main(int argc, char **argv)
    int pmx = 4, interp = 6, agg_nl = 0, agg_interp = 4, agg_pmx = 0, agg_p12 = 0, num_paths = 1;
    int relax = 18, relax_coarse = 9, coarse_th = 9, maxit = 100, solver = 1, kdim = 30;
    int max_levels = 25, dump_levels = 1, seed = 22775, cheby_order = 2, relax_order = 0;
-   int coarsen = 8, precond = 1, keep_t = 0, rhs_ones = 0;
+   int coarsen = 8, precond = 1, keep_t = 0, rhs_ones = 0, cycle_type = 1, fcycle = 0, num_sweeps = 1;
    int repeat = 1, threads = 0, want_digest = 0, matmat = 0, relax_down = -1, relax_up = -1;
    const char *jsonfile = NULL;
    double cheby_fraction = 0.3;
@@ -210,6 +210,9 @@ int main(int argc, char **argv)
       else if (ARG("-precond")) { precond = atoi(argv[++a]); }
       else if (ARG("-keepT")) { keep_t = atoi(argv[++a]); }
       else if (ARG("-relax_order")) { relax_order = atoi(argv[++a]); }
+      else if (ARG("-cycle_type")) { cycle_type = atoi(argv[++a]); }
+      else if (ARG("-fcycle")) { fcycle = atoi(argv[++a]); }
+      else if (ARG("-ns")) { num_sweeps = atoi(argv[++a]); }
       else if (ARG("-repeat")) { repeat = atoi(argv[++a]); }
       else if (ARG("-threads")) { threads = atoi(argv[++a]); }
       else if (ARG("-json")) { jsonfile = argv[++a]; }
@@ -349,8 +352,10 @@ int main(int argc, char **argv)
    HYPRE_BoomerAMGSetCycleRelaxType(amg, relax_coarse, 3);
    HYPRE_BoomerAMGSetRelaxWt(amg, relax_wt);
    HYPRE_BoomerAMGSetRelaxOrder(amg, relax_order);
-   HYPRE_BoomerAMGSetNumSweeps(amg, 1);
+   HYPRE_BoomerAMGSetNumSweeps(amg, num_sweeps);
    HYPRE_BoomerAMGSetCycleNumSweeps(amg, 1, 3);
+   HYPRE_BoomerAMGSetCycleType(amg, cycle_type);
+   HYPRE_BoomerAMGSetFCycle(amg, fcycle);
    HYPRE_BoomerAMGSetChebyOrder(amg, cheby_order);
    HYPRE_BoomerAMGSetChebyFraction(amg, cheby_fraction);
    HYPRE_BoomerAMGSetMaxCoarseSize(amg, coarse_th);

@@ -162,6 +162,19 @@ CASES = {
                                 coarse_th=9, solver=61, k=30, full=True),
     "aniso_40_cf8_w08_pcg": dict(gen="aniso", n=(40,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, rlx=8, w=0.8,
                                  relax_order=1, coarse_th=9, solver=1, full=True),
+    # W-cycles (cycle_type 2), F-cycles, two sweeps per relaxation
+    "lap7_16_w_pcg": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, rlx=18, cycle_type=2, coarse_th=9,
+                          solver=1, full=True),
+    "lap27_14_w_gs11_fgmres": dict(kind=27, n=(14, 14, 14), th=0.5, mxrs=1.0, Pmx=4, rlx=11, cycle_type=2,
+                                   coarse_th=9, solver=61, k=30, full=True),
+    "lap7_16_f_pcg": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, rlx=18, fcycle=1, coarse_th=9, solver=1,
+                          full=True),
+    "fv_12_w_hgs6_ns2_pcg": dict(gen="fv", n=(12,), seed=10, th=0.25, mxrs=0.9, Pmx=4, rlx=6, cycle_type=2, ns=2,
+                                 coarse_th=9, solver=1, full=True),
+    "lap27_16_agg4_f_cheby_pcg": dict(kind=27, n=(16, 16, 16), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=4,
+                                      rlx=16, cheby_order=2, fcycle=1, coarse_th=9, solver=1, full=True),
+    "lap7_14_w_cf18_amg": dict(kind=7, n=(14, 14, 14), th=0.25, mxrs=1.0, Pmx=4, rlx=18, cycle_type=2,
+                               relax_order=1, coarse_th=9, solver=0, precond=0, full=True),
     # edge cases: no strong couplings (coarsening stops at once, the single
     # level is above max_coarse_size and relaxes instead of a direct solve),
     # a level cap that leaves a large coarsest level, a matrix within
@@ -199,7 +212,7 @@ def dump_args(c, out):
         a = [DUMP, "-mat", mat]
     else:
         a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "relax_order", "w",
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "relax_order", "cycle_type", "fcycle", "ns", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]

@@ -75,6 +75,12 @@ def oracle_params(c):
         p["agg_p12_max_elmts"] = c["agg_P12_mx"]
     if "relax_order" in c:
         p["relax_order"] = c["relax_order"]
+    if "cycle_type" in c:
+        p["cycle_type"] = c["cycle_type"]
+    if "fcycle" in c:
+        p["fcycle"] = c["fcycle"]
+    if "ns" in c:
+        p["num_sweeps"] = c["ns"]
     if "max_levels" in c:
         p["max_levels"] = c["max_levels"]
     return p
@@ -96,6 +102,12 @@ def amg_params(c):
         p["AggP12MaxElmts"] = c["agg_P12_mx"]
     if "relax_order" in c:
         p["RelaxOrder"] = c["relax_order"]
+    if "cycle_type" in c:
+        p["CycleType"] = c["cycle_type"]
+    if "fcycle" in c:
+        p["FCycle"] = c["fcycle"]
+    if "ns" in c:
+        p["NumSweeps"] = c["ns"]
     if "max_levels" in c:
         p["MaxLevels"] = c["max_levels"]
     if "cheby_order" in c:
