@@ -129,7 +129,7 @@ def _declare(L):
         fn.restype = i32
     int_setters = ["MaxIter", "MaxCoarseSize", "MinCoarseSize", "MaxLevels", "CoarsenType", "AggNumLevels",
                    "NumPaths", "InterpType", "PMaxElmts", "AggInterpType", "AggPMaxElmts", "AggP12MaxElmts",
-                   "CycleType", "NumSweeps", "RelaxType", "RelaxOrder", "ChebyOrder", "ChebyScale", "ChebyVariant",
+                   "CycleType", "FCycle", "NumSweeps", "RelaxType", "RelaxOrder", "ChebyOrder", "ChebyScale", "ChebyVariant",
                    "ChebyEigEst", "PrintLevel", "Logging", "RAP2", "ModuleRAP2", "KeepTranspose"]
     real_setters = ["Tol", "StrongThreshold", "MaxRowSum", "TruncFactor", "AggTruncFactor", "RelaxWt",
                     "ChebyFraction"]

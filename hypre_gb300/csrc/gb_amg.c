@@ -1961,9 +1961,99 @@ static void relax_cf_d(gb_amg *amg, int l, int type, int cycle_param, const doub
    relax_points_d(amg, l, type, f, u, 0, -p0);
 }
 
+/* One relaxation in place on u, for the general cycle: the cycle part's C/F
+ * order when it applies, else the smoother of the V-cycle */
+static void relax_level_d(gb_amg *amg, int l, int type, int cycle_param, const double *f, double *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   if (amg->prm.relax_order == 1 && amg->num_levels > 1 && cycle_param < 3 && type != 16)
+   {
+      relax_cf_d(amg, l, type, cycle_param, f, u, u_zero);
+   }
+   else if (type == 11 || type == 12) { twostage_gs_d(amg, l, type == 11 ? 1 : 2, f, u, u_zero); }
+   else if (type == 16) { cheby_d(amg, l, f, u, u_zero); }
+   else if (hgs_type(type)) { hybrid_gs_d(amg, l, type, f, u, u_zero, 0); }
+   else if (u_zero) { relax_d(amg, l, type, f, u, u, 1); }
+   else
+   {
+      relax_d(amg, l, type, f, u, L->U2, 0);
+      cudaMemcpyAsync(u, L->U2, sizeof(double) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+   }
+}
+
+/* W- and F-cycles: the reference's level counters (hypre_BoomerAMGCycle
+ * src/parcsr_ls/par_cycle.c:225-866) choose the next level -- coarser while
+ * the level's counter stays >= 0, else finer -- with the per-level
+ * operations of the V-cycle: relaxation of the cycle part (down 1, up 2,
+ * coarsest 3), residual and restriction with a zero coarse guess on the way
+ * down, u_f += P u_c on the way up.  Host control only: the sequence is
+ * captured into the cycle's graph like the V-cycle's. */
+static void cycle_gen_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
+{
+   gb_amg_params *prm = &amg->prm;
+   cudaStream_t s = gb_stream();
+   const int nl = amg->num_levels, ct = prm->cycle_type;
+   const double *F[32];
+   double *U[32];
+   int counter[32], zero[32];
+   F[0] = f0; U[0] = u0;
+   for (int l = 1; l < nl; l++) { F[l] = amg->lev[l].F; U[l] = amg->lev[l].U; }
+   counter[0] = 1;
+   zero[0] = u0_zero;
+   for (int l = 1; l < nl; l++) { counter[l] = prm->fcycle ? 1 : ct; zero[l] = 0; }
+   int fl = nl - 2, level = 0, cp = nl == 1 ? 3 : 1;
+   for (;;)
+   {
+      gb_level *L = &amg->lev[level];
+      if (level == nl - 1)
+      {
+         if (amg->coarse_inv) { gb_dense_apply_d(amg->coarse_n, amg->coarse_inv, F[level], U[level], s); }
+         else { relax_level_d(amg, level, prm->relax_type[3], 3, F[level], U[level], zero[level]); }
+      }
+      else
+      {
+         for (int sw = 0; sw < prm->num_sweeps[cp]; sw++)
+         {
+            relax_level_d(amg, level, prm->relax_type[cp], cp, F[level], U[level], zero[level] && sw == 0);
+         }
+      }
+      zero[level] = 0;
+      --counter[level];
+      if (counter[level] >= 0 && level != nl - 1)
+      {
+         gb_spmv_d(gb_solve_desc(L->A, GB_PREC_F64), U[level], L->V, 2, -1.0, 1.0, F[level], NULL, 0.0, NULL, NULL,
+                   s);
+         gb_spmv_d(gb_solve_desc(L->R, GB_PREC_F64), L->V, (double *) F[level + 1], 0, 1.0, 0.0, NULL, NULL, 0.0,
+                   NULL, NULL, s);
+         cudaMemsetAsync(U[level + 1], 0, sizeof(double) * (size_t) amg->lev[level + 1].n, s);
+         zero[level + 1] = 1;
+         ++level;
+         if (counter[level] < ct) { counter[level] = ct; }
+         cp = level == nl - 1 ? 3 : 1;
+      }
+      else if (level != 0)
+      {
+         gb_level *Lf = &amg->lev[level - 1];
+         gb_spmv_d(gb_solve_desc(Lf->P, GB_PREC_F64), U[level], Lf->U2, 0, 1.0, 1.0, U[level - 1], NULL, 0.0, NULL,
+                   NULL, s);
+         cudaMemcpyAsync(U[level - 1], Lf->U2, sizeof(double) * (size_t) Lf->n, cudaMemcpyDeviceToDevice, s);
+         --level;
+         cp = 2;
+         if (prm->fcycle && fl == level)
+         {
+            if (counter[level] < 1) { counter[level] = 1; }
+            fl--;
+         }
+      }
+      else { break; }
+   }
+}
+
 static void cycle_d(gb_amg *amg, const double *f0, double *u0, int u0_zero)
 {
    gb_amg_params *prm = &amg->prm;
+   if (prm->cycle_type != 1 || prm->fcycle) { cycle_gen_d(amg, f0, u0, u0_zero); return; }
    cudaStream_t s = gb_stream();
    int nl = amg->num_levels;
    /* C/F relaxation order above the coarsest level (par_cycle.c:441-452) */
@@ -2117,9 +2207,91 @@ static void relax_cf_f(gb_amg *amg, int l, int type, int cycle_param, const floa
    relax_points_f(amg, l, type, f, u, 0, -p0);
 }
 
+static void relax_level_f(gb_amg *amg, int l, int type, int cycle_param, const float *f, float *u, int u_zero)
+{
+   gb_level *L = &amg->lev[l];
+   cudaStream_t s = gb_stream();
+   if (amg->prm.relax_order == 1 && amg->num_levels > 1 && cycle_param < 3 && type != 16)
+   {
+      relax_cf_f(amg, l, type, cycle_param, f, u, u_zero);
+   }
+   else if (type == 11 || type == 12) { twostage_gs_f(amg, l, type == 11 ? 1 : 2, f, u, u_zero); }
+   else if (type == 16) { cheby_f(amg, l, f, u, u_zero); }
+   else if (hgs_type(type)) { hybrid_gs_f(amg, l, type, f, u, u_zero, 0); }
+   else if (u_zero) { relax_f(amg, l, type, f, u, u, 1); }
+   else
+   {
+      relax_f(amg, l, type, f, u, L->U2f, 0);
+      cudaMemcpyAsync(u, L->U2f, sizeof(float) * (size_t) L->n, cudaMemcpyDeviceToDevice, s);
+   }
+}
+
+/* the FP32 form of cycle_gen_d, from a zero initial guess (f0d/u0d FP64) */
+static void cycle_gen_f(gb_amg *amg, const double *f0d, double *u0d)
+{
+   gb_amg_params *prm = &amg->prm;
+   cudaStream_t s = gb_stream();
+   const int nl = amg->num_levels, ct = prm->cycle_type;
+   float *F[32] = {0}, *U[32] = {0};
+   int counter[32], zero[32];
+   for (int l = 0; l < nl; l++) { F[l] = amg->lev[l].Ff; U[l] = amg->lev[l].Uf; }
+   gb_d2f(amg->lev[0].n, f0d, F[0], s);
+   counter[0] = 1;
+   zero[0] = 1;
+   for (int l = 1; l < nl; l++) { counter[l] = prm->fcycle ? 1 : ct; zero[l] = 0; }
+   int fl = nl - 2, level = 0, cp = nl == 1 ? 3 : 1;
+   for (;;)
+   {
+      gb_level *L = &amg->lev[level];
+      const int vp = (prm->cycle_prec == GB_PREC_F16 && level == 0) ? GB_PREC_F16 : GB_PREC_F32;
+      if (level == nl - 1)
+      {
+         if (amg->coarse_inv) { gb_dense_apply_f(amg->coarse_n, amg->coarse_inv, F[level], U[level], s); }
+         else { relax_level_f(amg, level, prm->relax_type[3], 3, F[level], U[level], zero[level]); }
+      }
+      else
+      {
+         for (int sw = 0; sw < prm->num_sweeps[cp]; sw++)
+         {
+            relax_level_f(amg, level, prm->relax_type[cp], cp, F[level], U[level], zero[level] && sw == 0);
+         }
+      }
+      zero[level] = 0;
+      --counter[level];
+      if (counter[level] >= 0 && level != nl - 1)
+      {
+         gb_spmv_f(gb_solve_desc(L->A, vp), U[level], L->Vf, 2, -1.f, 1.f, F[level], NULL, 0.f, NULL, NULL, s);
+         gb_spmv_f(gb_solve_desc(L->R, GB_PREC_F32), L->Vf, F[level + 1], 0, 1.f, 0.f, NULL, NULL, 0.f, NULL, NULL,
+                   s);
+         cudaMemsetAsync(U[level + 1], 0, sizeof(float) * (size_t) amg->lev[level + 1].n, s);
+         zero[level + 1] = 1;
+         ++level;
+         if (counter[level] < ct) { counter[level] = ct; }
+         cp = level == nl - 1 ? 3 : 1;
+      }
+      else if (level != 0)
+      {
+         gb_level *Lf = &amg->lev[level - 1];
+         gb_spmv_f(gb_solve_desc(Lf->P, GB_PREC_F32), U[level], Lf->U2f, 0, 1.f, 1.f, U[level - 1], NULL, 0.f, NULL,
+                   NULL, s);
+         cudaMemcpyAsync(U[level - 1], Lf->U2f, sizeof(float) * (size_t) Lf->n, cudaMemcpyDeviceToDevice, s);
+         --level;
+         cp = 2;
+         if (prm->fcycle && fl == level)
+         {
+            if (counter[level] < 1) { counter[level] = 1; }
+            fl--;
+         }
+      }
+      else { break; }
+   }
+   gb_f2d(amg->lev[0].n, U[0], u0d, s);
+}
+
 static void cycle_f(gb_amg *amg, const double *f0d, double *u0d)
 {
    gb_amg_params *prm = &amg->prm;
+   if (prm->cycle_type != 1 || prm->fcycle) { cycle_gen_f(amg, f0d, u0d); return; }
    cudaStream_t s = gb_stream();
    int nl = amg->num_levels;
    const int cf = prm->relax_order == 1 && nl > 1;
@@ -2401,8 +2573,21 @@ HYPRE_Int HYPRE_BoomerAMGSetCycleType(HYPRE_Solver solver, HYPRE_Int v)
 {
    gb_amg *a = amg_of(solver, 1);
    if (!a) { return gb_error_flag; }
-   if (v != 1) { gb_error(HYPRE_ERROR_GENERIC, "cycle_type: only V-cycles (1) are supported"); gb_error_in_arg(2); return gb_error_flag; }
+   if (v != 1 && v != 2)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "cycle_type: V (1) and W (2) cycles are supported");
+      gb_error_in_arg(2);
+      return gb_error_flag;
+   }
    a->prm.cycle_type = v;
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGSetFCycle(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   a->prm.fcycle = v != 0;
    return gb_error_flag;
 }
 

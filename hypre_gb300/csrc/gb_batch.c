@@ -211,9 +211,9 @@ HYPRE_Int HYPRE_GB300_BatchedPCGSetup(HYPRE_Solver solver, HYPRE_Solver amg_solv
          return gb_error_flag;
       }
    }
-   if (prm->relax_order != 0)
+   if (prm->relax_order != 0 || prm->cycle_type != 1 || prm->fcycle)
    {
-      gb_error(HYPRE_ERROR_GENERIC, "batched PCG: relax_order must be 0 (lexicographic)");
+      gb_error(HYPRE_ERROR_GENERIC, "batched PCG: V-cycles with relax_order 0 (lexicographic)");
       return gb_error_flag;
    }
    if (prm->agg_num_levels > 0)

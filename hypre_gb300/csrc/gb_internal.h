@@ -153,7 +153,8 @@ typedef struct
    double *level_relax_weight;   /* optional, per level */
    int    cheby_order, cheby_scale, cheby_variant, cheby_eig_est;
    double cheby_fraction;
-   int    cycle_type;
+   int    cycle_type;        /* 1 V, 2 W */
+   int    fcycle;            /* 1: F-cycle */
    double tol;
    int    max_iter;
    int    print_level, logging;

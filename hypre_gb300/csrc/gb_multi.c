@@ -120,7 +120,7 @@ static int multi_cycle_supported(gb_amg *amg)
    {
       if (p->relax_type[k] != 18 && p->relax_type[k] != 7) { return 0; }
    }
-   if (p->relax_order != 0 && amg->num_levels > 1) { return 0; }
+   if ((p->relax_order != 0 || p->cycle_type != 1 || p->fcycle) && amg->num_levels > 1) { return 0; }
    return amg->coarse_inv != NULL || amg->num_levels == 1;
 }
 
@@ -271,7 +271,7 @@ int gb_pcg_multi(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
       amg = (gb_amg *) k->precond_solver;
       if (!amg->setup_done || !multi_cycle_supported(amg))
       {
-         gb_error(HYPRE_ERROR_GENERIC, "multi-vector PCG: BoomerAMG needs setup, relax 18 or 7 in lexicographic order, direct coarsest");
+         gb_error(HYPRE_ERROR_GENERIC, "multi-vector PCG: BoomerAMG needs setup, V-cycles, relax 18 or 7 in lexicographic order, direct coarsest");
          return gb_error_flag;
       }
    }
