@@ -2519,7 +2519,6 @@ SETTER(HYPRE_BoomerAMGSetMinCoarseSize, min_coarse_size, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetStrongThreshold, strong_threshold, HYPRE_Real)
 SETTER(HYPRE_BoomerAMGSetMaxRowSum, max_row_sum, HYPRE_Real)
 SETTER(HYPRE_BoomerAMGSetAggNumLevels, agg_num_levels, HYPRE_Int)
-SETTER(HYPRE_BoomerAMGSetNumPaths, num_paths, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetTruncFactor, trunc_factor, HYPRE_Real)
 SETTER(HYPRE_BoomerAMGSetPMaxElmts, p_max_elmts, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetAggInterpType, agg_interp_type, HYPRE_Int)
@@ -2580,6 +2579,22 @@ HYPRE_Int HYPRE_BoomerAMGSetCycleType(HYPRE_Solver solver, HYPRE_Int v)
       return gb_error_flag;
    }
    a->prm.cycle_type = v;
+   return gb_error_flag;
+}
+
+/* second-order strength with one path (par_strength.c:2435-2526); the
+ * path-counting form for num_paths > 1 is not built */
+HYPRE_Int HYPRE_BoomerAMGSetNumPaths(HYPRE_Solver solver, HYPRE_Int v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (v != 1)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "num_paths: only 1 is supported");
+      gb_error_in_arg(2);
+      return gb_error_flag;
+   }
+   a->prm.num_paths = v;
    return gb_error_flag;
 }
 

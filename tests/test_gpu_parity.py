@@ -257,6 +257,11 @@ def test_unsupported_options_are_refused(gb, oracle_mod):
     for v in (3, 6, 14, 15, 16, 17, 18):
         L.HYPRE_ClearAllErrors()
         assert amg.set("InterpType", v) == 0, v
+    for name, bad, good in (("NumPaths", 2, 1), ("CycleType", 3, 2), ("RelaxOrder", 2, 1)):
+        L.HYPRE_ClearAllErrors()
+        assert amg.set(name, bad) & gb.HYPRE_ERROR_GENERIC, name
+        L.HYPRE_ClearAllErrors()
+        assert amg.set(name, good) == 0, name
     L.HYPRE_ClearAllErrors()
     amg.destroy()
     # aggressive interpolation types are checked at setup: the two-stage
