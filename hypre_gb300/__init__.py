@@ -129,10 +129,10 @@ def _declare(L):
         fn.restype = i32
     int_setters = ["MaxIter", "MaxCoarseSize", "MinCoarseSize", "MaxLevels", "CoarsenType", "AggNumLevels",
                    "NumPaths", "InterpType", "PMaxElmts", "AggInterpType", "AggPMaxElmts", "AggP12MaxElmts",
-                   "CycleType", "FCycle", "NumSweeps", "RelaxType", "RelaxOrder", "ChebyOrder", "ChebyScale", "ChebyVariant",
-                   "ChebyEigEst", "PrintLevel", "Logging", "RAP2", "ModuleRAP2", "KeepTranspose"]
-    real_setters = ["Tol", "StrongThreshold", "MaxRowSum", "TruncFactor", "AggTruncFactor", "RelaxWt",
-                    "ChebyFraction"]
+                   "CycleType", "FCycle", "NumSweeps", "RelaxType", "RelaxOrder", "ChebyOrder", "ChebyScale",
+                   "ChebyVariant", "ChebyEigEst", "PrintLevel", "Logging", "RAP2", "ModuleRAP2", "KeepTranspose"]
+    real_setters = ["Tol", "StrongThreshold", "MaxRowSum", "TruncFactor", "AggTruncFactor", "AggP12TruncFactor",
+                    "RelaxWt", "ChebyFraction"]
     for s in int_setters:
         fn = getattr(L, "HYPRE_BoomerAMGSet" + s)
         fn.argtypes = [vp, i32]

@@ -2525,6 +2525,7 @@ SETTER(HYPRE_BoomerAMGSetAggInterpType, agg_interp_type, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetAggTruncFactor, agg_trunc_factor, HYPRE_Real)
 SETTER(HYPRE_BoomerAMGSetAggPMaxElmts, agg_p_max_elmts, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetAggP12MaxElmts, agg_p12_max_elmts, HYPRE_Int)
+SETTER(HYPRE_BoomerAMGSetAggP12TruncFactor, agg_p12_trunc_factor, HYPRE_Real)
 SETTER(HYPRE_BoomerAMGSetChebyOrder, cheby_order, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetChebyFraction, cheby_fraction, HYPRE_Real)
 SETTER(HYPRE_BoomerAMGSetChebyScale, cheby_scale, HYPRE_Int)
