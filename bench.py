@@ -15,7 +15,9 @@ its setup phases and the host's waits on the stream during setup.
 Other workloads (`--workload`, one JSON line each): spgemm128 (the
 reference's SpGEMM benchmark, A*A), batch512, multi64, fv256, learned128 and
 mlp4m (the learned part's dense layers alone, TFLOP/s against the measured
-BF16 peak).
+BF16 peak).  The default run also runs spgemm128, multi64, batch512, fv256
+and mlp4m, each in its own process (default warm-up, two timed steps), and
+summarises their lines under `secondary` (`--no-secondary` skips them).
 
 Arms:
   default            GPU path (FP64 setup, FP32 or FP16-finest V-cycle inside
@@ -70,6 +72,8 @@ def parse():
     ap.add_argument("--arms", default="fp64_plain,fp32_cycle,fp16_finest",
                     help="comma-separated arms to time (profiling runs use fp32_cycle alone)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end IJ arm (profiling runs)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the secondary workloads the headline line summarises (profiling runs)")
     ap.add_argument("--spmv-only", action="store_true",
                     help="only the level-0 SpMV loop of the roofline measurement (for profiling)")
     ap.add_argument("--spmv-prec", type=int, default=0, choices=[0, 1, 2],
@@ -474,10 +478,41 @@ def gpu_arm(args):
         "parity": parity,
         "clocks": best["clocks"],
     }
+    if rank == 0 and world == 1 and n1 == 160 and not args.no_secondary:
+        result["secondary"] = run_secondary()
     if rank == 0:
         print(json.dumps(result))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+# the other workloads, each in its own process with the default warm-up and
+# two timed steps, summarised in the headline line: the reference's SpGEMM
+# benchmark (A*A nonzero counts and times against its saved MI250X numbers),
+# 64 right-hand sides, 512 batched systems, the FV diffusion configuration
+# in three cycle precisions and the learned part's dense layers
+SECONDARY = ("spgemm128", "multi64", "batch512", "fv256", "mlp4m")
+SECONDARY_DROP = ("config", "n_gpus", "scaling", "data", "higher_is_better", "tuning_ms", "problems", "peaks")
+
+
+def run_secondary():
+    out = {}
+    for w in SECONDARY:
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--workload", w, "--steps", "2",
+                                "--warmup", "3"], capture_output=True, text=True, timeout=900, cwd=ROOT)
+            lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[w] = {"error": "exit %d: %s" % (r.returncode, (r.stderr or r.stdout)[-300:])}
+                continue
+            d = json.loads(lines[-1])
+            out[w] = {k: v for k, v in d.items() if k not in SECONDARY_DROP}
+            out[w]["workload"] = d.get("config", {}).get("workload", w)
+        except Exception as e:  # recorded, never fatal for the headline line
+            out[w] = {"error": repr(e)[-300:]}
+        out[w]["wall_seconds_total"] = time.perf_counter() - t0
+    return out
 
 
 def _spmv_shape(L, A, prec):
