@@ -2691,8 +2691,31 @@ HYPRE_Int HYPRE_BoomerAMGSetLevelRelaxWt(HYPRE_Solver solver, HYPRE_Real v, HYPR
    return gb_error_flag;
 }
 
-HYPRE_Int HYPRE_BoomerAMGSetRAP2(HYPRE_Solver solver, HYPRE_Int v) { (void) v; amg_of(solver, 1); return gb_error_flag; }
-HYPRE_Int HYPRE_BoomerAMGSetModuleRAP2(HYPRE_Solver solver, HYPRE_Int v) { (void) v; amg_of(solver, 1); return gb_error_flag; }
+/* The coarse operator is the reference's host Galerkin product
+ * (hypre_BoomerAMGBuildCoarseOperatorKT, par_amg_setup.c:3055-3066) and the
+ * aggressive P1 P2 its hypre_ParMatmul; RAP2 (A P, then P^T (A P)) and the
+ * modularized products (ModuleRAP2) sum in other orders and are not built, so
+ * they are refused rather than ignored.  KeepTranspose changes nothing the
+ * results depend on (the restriction multiplies by a stored P^T whose rows
+ * are in the same order as the transposed product's sums). */
+static HYPRE_Int refuse_nonzero(HYPRE_Solver solver, HYPRE_Int v, const char *what)
+{
+   if (!amg_of(solver, 1)) { return gb_error_flag; }
+   if (v != 0)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, what);
+      gb_error_in_arg(2);
+   }
+   return gb_error_flag;
+}
+HYPRE_Int HYPRE_BoomerAMGSetRAP2(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return refuse_nonzero(solver, v, "rap2: only the Galerkin triple product (0) is supported");
+}
+HYPRE_Int HYPRE_BoomerAMGSetModuleRAP2(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return refuse_nonzero(solver, v, "module_rap2: only the host products (0) are supported");
+}
 HYPRE_Int HYPRE_BoomerAMGSetKeepTranspose(HYPRE_Solver solver, HYPRE_Int v) { (void) v; amg_of(solver, 1); return gb_error_flag; }
 
 HYPRE_Int HYPRE_GB300_BoomerAMGSetCyclePrecision(HYPRE_Solver solver, HYPRE_Int v)

@@ -180,6 +180,10 @@ CASES = {
     # a level cap that leaves a large coarsest level, a matrix within
     # max_coarse_size (direct solve only)
     "diag_2000_pcg": dict(gen="diag", n=(2000,), th=0.25, mxrs=0.9, Pmx=4, rlx=18, coarse_th=9, solver=1, full=True),
+    # the smallest systems: one unknown, and a 1-D pair (two 7-point cells)
+    "diag_1_pcg": dict(gen="diag", n=(1,), th=0.25, mxrs=0.9, Pmx=4, rlx=18, coarse_th=9, solver=1, full=True),
+    "lap7_2x1x1_fgmres": dict(kind=7, n=(2, 1, 1), th=0.25, mxrs=1.0, Pmx=4, rlx=18, coarse_th=9, solver=61, k=5,
+                              full=True),
     "lap27_12_ml2_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=18, coarse_th=9, max_levels=2,
                              solver=1, full=True),
     "lap27_12_ml2_hgs6_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=6, coarse_th=9, max_levels=2,

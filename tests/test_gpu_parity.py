@@ -257,7 +257,8 @@ def test_unsupported_options_are_refused(gb, oracle_mod):
     for v in (3, 6, 14, 15, 16, 17, 18):
         L.HYPRE_ClearAllErrors()
         assert amg.set("InterpType", v) == 0, v
-    for name, bad, good in (("NumPaths", 2, 1), ("CycleType", 3, 2), ("RelaxOrder", 2, 1)):
+    for name, bad, good in (("NumPaths", 2, 1), ("CycleType", 3, 2), ("RelaxOrder", 2, 1), ("RAP2", 1, 0),
+                            ("ModuleRAP2", 1, 0)):
         L.HYPRE_ClearAllErrors()
         assert amg.set(name, bad) & gb.HYPRE_ERROR_GENERIC, name
         L.HYPRE_ClearAllErrors()
