@@ -365,7 +365,7 @@ class Krylov:
     (HYPRE_BoomerAMGSolve / HYPRE_BoomerAMGSetup passed as function pointers,
     as in the reference's drivers)."""
 
-    def __init__(self, kind="pcg", tol=1e-8, maxit=100, kdim=30, amg=None, two_norm=1):
+    def __init__(self, kind="pcg", tol=1e-8, maxit=100, kdim=30, amg=None, two_norm=1, rel_change=0):
         L = lib()
         self.kind = kind
         self.h = C.c_void_p()
@@ -374,7 +374,7 @@ class Krylov:
             L.HYPRE_PCGSetTol(self.h, tol)
             L.HYPRE_PCGSetMaxIter(self.h, maxit)
             L.HYPRE_PCGSetTwoNorm(self.h, two_norm)
-            L.HYPRE_PCGSetRelChange(self.h, 0)
+            L.HYPRE_PCGSetRelChange(self.h, rel_change)
             L.HYPRE_PCGSetLogging(self.h, 1)
             if amg is not None:
                 L.HYPRE_PCGSetPrecond(self.h, fn_ptr("HYPRE_BoomerAMGSolve"), fn_ptr("HYPRE_BoomerAMGSetup"), amg.h)

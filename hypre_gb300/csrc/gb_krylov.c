@@ -166,8 +166,12 @@ static int pcg_solve(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
       gamma = h[0];
       i_prod = k->two_norm ? h[1] : gamma;
       hist_push(k, i, sqrt(i_prod / bi_prod));
+      /* the convergence tests of pcg.c:808-849: the basic test, then (on
+       * request) the recomputed residual and the relative change of x,
+       * alpha^2 <p,p> / <x,x> < eps */
       if (i_prod / bi_prod < eps)
       {
+         int tentative = 1;
          if (k->recompute_residual)
          {
             gb_spmv_d(Ad, x->d, k->r, 2, -1.0, 1.0, b->d, NULL, 0.0, NULL, NULL, st);
@@ -178,9 +182,14 @@ static int pcg_solve(gb_krylov *k, gb_parcsr *A, gb_parvec *b, gb_parvec *x)
                i_prod = gb_dot(n, k->r, k->s);
                gamma = i_prod;
             }
-            if (i_prod / bi_prod < eps) { converged = 1; break; }
+            if (i_prod / bi_prod >= eps) { tentative = 0; }
          }
-         else { converged = 1; break; }
+         if (tentative && k->rel_change && i_prod > 0.0)
+         {
+            const double pi_prod = gb_dot(n, k->p, k->p), xi_prod = gb_dot(n, x->d, x->d);
+            if (alpha * alpha * pi_prod / xi_prod >= eps) { tentative = 0; }
+         }
+         if (tentative) { converged = 1; break; }
       }
       /* p = s + beta p */
       double beta = gamma / gamma_old;

@@ -2519,8 +2519,9 @@ int or_amg_vcycle(or_hierarchy *H, const double *f, double *u)
 }
 
 /* ------------------------------------------------------------------------ */
-/* PCG, hypre_PCGSolve src/krylov/pcg.c:313-1015 (two_norm = 1, rel_change 0, */
-/* recompute_residual 0, as the reference's ij driver configures it)         */
+/* PCG, hypre_PCGSolve src/krylov/pcg.c:313-1015 (two_norm = 1,             */
+/* recompute_residual 0, as the reference's ij driver configures it; the     */
+/* relative-change test when the hierarchy's pcg_rel_change is set)          */
 /* ------------------------------------------------------------------------ */
 
 int or_pcg(const or_csr *A, or_hierarchy *H, const double *b, double *x,
@@ -2563,7 +2564,17 @@ int or_pcg(const or_csr *A, or_hierarchy *H, const double *b, double *x,
       gamma = or_dot(n, r, s);
       i_prod = or_dot(n, r, r);
       if (relres) { relres[i] = sqrt(i_prod / bi_prod); }
-      if (i_prod / bi_prod < eps) { conv = 1; break; }
+      if (i_prod / bi_prod < eps)
+      {
+         int tentative = 1;
+         if (H->prm.pcg_rel_change && i_prod > 0.0)
+         {
+            /* :836-843: x must also have changed little, alpha^2 <p,p> / <x,x> < eps */
+            const double pi_prod = or_dot(n, p, p), xi_prod = or_dot(n, x, x);
+            if (alpha * alpha * pi_prod / xi_prod >= eps) { tentative = 0; }
+         }
+         if (tentative) { conv = 1; break; }
+      }
       double beta = gamma / gamma_old;
       for (int k = 0; k < n; k++) { p[k] = s[k] + beta * p[k]; }
    }

@@ -55,6 +55,7 @@ typedef struct
    int    relax_order;        /* 0 lexicographic, 1 C/F (C then F down, F then C up) */
    int    cycle_type;         /* 1 V, 2 W (visits of each coarse level per visit of the finer) */
    int    fcycle;             /* 0, or 1: F-cycle */
+   int    pcg_rel_change;     /* PCG driven by this hierarchy: the relative-change test (pcg.c:836-843) */
 } or_amg_params;
 
 typedef struct

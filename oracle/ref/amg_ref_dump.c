@@ -170,6 +170,7 @@ int main(int argc, char **argv)
    int relax = 18, relax_coarse = 9, coarse_th = 9, maxit = 100, solver = 1, kdim = 30;
    int max_levels = 25, dump_levels = 1, seed = 22775, cheby_order = 2, relax_order = 0;
    int coarsen = 8, precond = 1, keep_t = 0, rhs_ones = 0, cycle_type = 1, fcycle = 0, num_sweeps = 1;
+   int rel_change = 0;
    int repeat = 1, threads = 0, want_digest = 0, matmat = 0, relax_down = -1, relax_up = -1;
    const char *jsonfile = NULL;
    double cheby_fraction = 0.3;
@@ -213,6 +214,7 @@ int main(int argc, char **argv)
       else if (ARG("-cycle_type")) { cycle_type = atoi(argv[++a]); }
       else if (ARG("-fcycle")) { fcycle = atoi(argv[++a]); }
       else if (ARG("-ns")) { num_sweeps = atoi(argv[++a]); }
+      else if (ARG("-rel_change")) { rel_change = atoi(argv[++a]); }
       else if (ARG("-repeat")) { repeat = atoi(argv[++a]); }
       else if (ARG("-threads")) { threads = atoi(argv[++a]); }
       else if (ARG("-json")) { jsonfile = argv[++a]; }
@@ -379,7 +381,7 @@ int main(int argc, char **argv)
       HYPRE_PCGSetMaxIter(ks, maxit);
       HYPRE_PCGSetTol(ks, tol);
       HYPRE_PCGSetTwoNorm(ks, 1);
-      HYPRE_PCGSetRelChange(ks, 0);
+      HYPRE_PCGSetRelChange(ks, rel_change);
       HYPRE_PCGSetPrintLevel(ks, 0);
       HYPRE_PCGSetLogging(ks, 1);
       HYPRE_PCGSetPrecond(ks, (HYPRE_PtrToSolverFcn) HYPRE_BoomerAMGSolve,

@@ -175,6 +175,11 @@ CASES = {
                                       rlx=16, cheby_order=2, fcycle=1, coarse_th=9, solver=1, full=True),
     "lap7_14_w_cf18_amg": dict(kind=7, n=(14, 14, 14), th=0.25, mxrs=1.0, Pmx=4, rlx=18, cycle_type=2,
                                relax_order=1, coarse_th=9, solver=0, precond=0, full=True),
+    # PCG's relative-change test (x must also stop changing)
+    "lap7_16_relchg_pcg": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, rlx=18, rel_change=1, coarse_th=9,
+                               solver=1, full=True),
+    "fv_12_relchg_pcg": dict(gen="fv", n=(12,), seed=11, th=0.25, mxrs=0.9, Pmx=4, rlx=18, rel_change=1,
+                             coarse_th=9, solver=1, full=True),
     # edge cases: no strong couplings (coarsening stops at once, the single
     # level is above max_coarse_size and relaxes instead of a direct solve),
     # a level cap that leaves a large coarsest level, a matrix within
@@ -216,7 +221,7 @@ def dump_args(c, out):
         a = [DUMP, "-mat", mat]
     else:
         a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "relax_order", "cycle_type", "fcycle", "ns", "w",
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "relax_order", "cycle_type", "fcycle", "ns", "rel_change", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]

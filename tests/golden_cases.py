@@ -81,6 +81,8 @@ def oracle_params(c):
         p["fcycle"] = c["fcycle"]
     if "ns" in c:
         p["num_sweeps"] = c["ns"]
+    if "rel_change" in c:
+        p["pcg_rel_change"] = c["rel_change"]
     if "max_levels" in c:
         p["max_levels"] = c["max_levels"]
     return p

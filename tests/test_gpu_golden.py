@@ -34,7 +34,7 @@ def test_gpu_matches_reference(gb, oracle_mod, name):
         gb.check(gb.lib().HYPRE_BoomerAMGSetup(amg.h, A.par, bv.par, xv.par), "setup")
     else:
         amg = gb.BoomerAMG(Tol=0.0, MaxIter=1, **G.amg_params(c))
-        k = gb.Krylov(kind, tol=1e-8, maxit=100, kdim=c.get("k", 30), amg=amg)
+        k = gb.Krylov(kind, tol=1e-8, maxit=100, kdim=c.get("k", 30), amg=amg, rel_change=c.get("rel_change", 0))
         k.setup(A, bv, xv)
     nl = amg.num_levels()
 
