@@ -1517,3 +1517,150 @@ HYPRE_Int HYPRE_IJVectorDestroy(HYPRE_IJVector v)
    free(v);
    return gb_error_flag;
 }
+
+/* ------------------------------------------------------------------------
+ * The rest of the reference's IJ interface for one process
+ * (HYPRE_IJ_mv.h:140-750): object types, row counts, constant values, the
+ * inner product of two IJ vectors, and the settings that only concern
+ * off-process entries, printing, threading or the memory location, which
+ * one process holding its data on the device accepts and ignores.
+ * ------------------------------------------------------------------------ */
+HYPRE_Int HYPRE_IJMatrixGetObjectType(HYPRE_IJMatrix m, HYPRE_Int *type)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!type) { gb_error_in_arg(2); return gb_error_flag; }
+   *type = m->object_type;
+   return gb_error_flag;
+}
+
+/* the assembled rows' lengths (IJMatrix_parcsr.c:449-495: the ParCSR's row
+ * pointers; rows outside the local range count 0) */
+HYPRE_Int HYPRE_IJMatrixGetRowCounts(HYPRE_IJMatrix m, HYPRE_Int nrows, HYPRE_BigInt *rows, HYPRE_Int *ncols)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (nrows < 0) { gb_error_in_arg(2); return gb_error_flag; }
+   if (nrows > 0 && !rows) { gb_error_in_arg(3); return gb_error_flag; }
+   if (nrows > 0 && !ncols) { gb_error_in_arg(4); return gb_error_flag; }
+   if (!m->assembled || !m->par) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not assembled"); return gb_error_flag; }
+   const int n = m->par->A.nr;
+   int *ptr = (int *) malloc(sizeof(int) * (size_t) (n + 1));
+   if (!ptr) { gb_error(HYPRE_ERROR_MEMORY, "row counts"); return gb_error_flag; }
+   cudaMemcpyAsync(ptr, m->par->A.i, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   for (int t = 0; t < nrows; t++)
+   {
+      const long long r = (long long) rows[t] - m->ilower;
+      ncols[t] = (r >= 0 && r < n) ? ptr[r + 1] - ptr[r] : 0;
+   }
+   free(ptr);
+   return gb_error_flag;
+}
+
+/* every stored entry of the assembled matrix takes the value
+ * (hypre_IJMatrixSetConstantValuesParCSR, IJMatrix_parcsr.c:1170-1198, which
+ * requires assembly); the value-dependent solve forms are rebuilt on use */
+HYPRE_Int HYPRE_IJMatrixSetConstantValues(HYPRE_IJMatrix m, HYPRE_Complex value)
+{
+   if (!check_ijm(m, 1)) { return gb_error_flag; }
+   if (!m->assembled || !m->par) { gb_error(HYPRE_ERROR_GENERIC, "IJ matrix not assembled"); return gb_error_flag; }
+   gb_parcsr *M = m->par;
+   gb_fill_d(M->A.nnz, M->A.v, value, gb_stream());
+   for (int p = 0; p < 3; p++) { solveform_free(&M->sf[p]); }
+   gb_dfree(M->diag);
+   M->diag = NULL;
+   free(M->row_vals);
+   M->row_vals = NULL;
+   free(M->row_cols);
+   M->row_cols = NULL;
+   /* the host copy of the rows that GetValues reads */
+   if (!ijm_host_ready(m) || !ijm_migrate(m)) { return gb_error_flag; }
+   for (int r = 0; r < m->nrows; r++)
+   {
+      for (int z = 0; z < m->row_len[r]; z++) { m->vals[m->row_off[r] + z] = value; }
+   }
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixSetMaxOffProcElmts(HYPRE_IJMatrix m, HYPRE_Int v)
+{
+   (void) v;
+   check_ijm(m, 1);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixSetPrintLevel(HYPRE_IJMatrix m, HYPRE_Int v)
+{
+   (void) v;
+   check_ijm(m, 1);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixSetOMPFlag(HYPRE_IJMatrix m, HYPRE_Int v)
+{
+   (void) v;
+   check_ijm(m, 1);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJMatrixMigrate(HYPRE_IJMatrix m, HYPRE_MemoryLocation loc)
+{
+   (void) loc;
+   check_ijm(m, 1);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorGetObjectType(HYPRE_IJVector v, HYPRE_Int *type)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (!type) { gb_error_in_arg(2); return gb_error_flag; }
+   *type = v->object_type;
+   return gb_error_flag;
+}
+
+/* every value of the vector (hypre_IJVectorSetConstantValuesPar) */
+HYPRE_Int HYPRE_IJVectorSetConstantValues(HYPRE_IJVector v, HYPRE_Complex value)
+{
+   if (!check_ijv(v, 1)) { return gb_error_flag; }
+   if (!v->initialized || !v->par) { gb_error(HYPRE_ERROR_GENERIC, "IJ vector not initialized"); return gb_error_flag; }
+   gb_fill_d(v->n, v->par->d, value, gb_stream());
+   v->h_valid = 0;
+   v->h_dirty = 0;
+   return gb_error_flag;
+}
+
+/* <x, y> of the two vectors' current values (hypre_IJVectorInnerProdPar) */
+HYPRE_Int HYPRE_IJVectorInnerProd(HYPRE_IJVector x, HYPRE_IJVector y, HYPRE_Real *prod)
+{
+   if (!check_ijv(x, 1)) { return gb_error_flag; }
+   if (!y || y->magic != GB_MAGIC_IJV) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!prod) { gb_error_in_arg(3); return gb_error_flag; }
+   if (!x->par || !y->par || x->n != y->n) { gb_error_in_arg(2); return gb_error_flag; }
+   if (x->h_dirty || y->h_dirty)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "IJ vector values put but not assembled");
+      return gb_error_flag;
+   }
+   *prod = gb_dot(x->n, x->par->d, y->par->d);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorSetMaxOffProcElmts(HYPRE_IJVector v, HYPRE_Int n)
+{
+   (void) n;
+   check_ijv(v, 1);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorSetPrintLevel(HYPRE_IJVector v, HYPRE_Int n)
+{
+   (void) n;
+   check_ijv(v, 1);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_IJVectorMigrate(HYPRE_IJVector v, HYPRE_MemoryLocation loc)
+{
+   (void) loc;
+   check_ijv(v, 1);
+   return gb_error_flag;
+}

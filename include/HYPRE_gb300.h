@@ -136,6 +136,24 @@ HYPRE_Int HYPRE_IJVectorSetObjectType(HYPRE_IJVector vector, HYPRE_Int type); /*
 HYPRE_Int HYPRE_IJVectorGetObject(HYPRE_IJVector vector, void **object);  /* :701 */
 HYPRE_Int HYPRE_IJVectorGetLocalRange(HYPRE_IJVector vector, HYPRE_BigInt *jlower,
                                       HYPRE_BigInt *jupper);               /* :692 */
+/* the rest of the IJ interface for one process: object types, row counts,
+ * constant values, the inner product of two IJ vectors; the off-process,
+ * print, thread and memory-location settings are accepted (one process, data
+ * on the device) */
+HYPRE_Int HYPRE_IJMatrixGetObjectType(HYPRE_IJMatrix matrix, HYPRE_Int *type); /* HYPRE_IJ_mv.h:274 */
+HYPRE_Int HYPRE_IJMatrixGetRowCounts(HYPRE_IJMatrix matrix, HYPRE_Int nrows, HYPRE_BigInt *rows,
+                                     HYPRE_Int *ncols); /* :209 */
+HYPRE_Int HYPRE_IJMatrixSetConstantValues(HYPRE_IJMatrix matrix, HYPRE_Complex value); /* :140 */
+HYPRE_Int HYPRE_IJMatrixSetMaxOffProcElmts(HYPRE_IJMatrix matrix, HYPRE_Int max_off_proc_elmts); /* :348 */
+HYPRE_Int HYPRE_IJMatrixSetPrintLevel(HYPRE_IJMatrix matrix, HYPRE_Int print_level); /* :382 */
+HYPRE_Int HYPRE_IJMatrixSetOMPFlag(HYPRE_IJMatrix matrix, HYPRE_Int omp_flag); /* :400 */
+HYPRE_Int HYPRE_IJMatrixMigrate(HYPRE_IJMatrix matrix, HYPRE_MemoryLocation memory_location); /* :466 */
+HYPRE_Int HYPRE_IJVectorGetObjectType(HYPRE_IJVector vector, HYPRE_Int *type); /* :686 */
+HYPRE_Int HYPRE_IJVectorSetConstantValues(HYPRE_IJVector vector, HYPRE_Complex value); /* :621 */
+HYPRE_Int HYPRE_IJVectorInnerProd(HYPRE_IJVector x, HYPRE_IJVector y, HYPRE_Real *prod); /* :743 */
+HYPRE_Int HYPRE_IJVectorSetMaxOffProcElmts(HYPRE_IJVector vector, HYPRE_Int max_off_proc_elmts); /* :582 */
+HYPRE_Int HYPRE_IJVectorSetPrintLevel(HYPRE_IJVector vector, HYPRE_Int print_level); /* :709 */
+HYPRE_Int HYPRE_IJVectorMigrate(HYPRE_IJVector vector, HYPRE_MemoryLocation memory_location); /* :750 */
 HYPRE_Int HYPRE_IJVectorRead(const char *filename, MPI_Comm comm, HYPRE_Int type,
                              HYPRE_IJVector *vector);                      /* :715 */
 HYPRE_Int HYPRE_IJVectorReadBinary(const char *filename, MPI_Comm comm, HYPRE_Int type,

@@ -315,3 +315,51 @@ def test_matrix_from_device_csr_matches_host_csr(gb):
     same(gb.parcsr_to_host(Ad), expected_csr(rows))
     L.HYPRE_GB300_ParCSRMatrixDestroy(Ad)
     L.HYPRE_GB300_ParCSRMatrixDestroy(Ah)
+
+
+def test_row_counts_constant_values_and_vector_calls(gb, oracle_mod):
+    """GetObjectType, GetRowCounts (rows outside the range count 0),
+    SetConstantValues on the assembled matrix (the product then uses the
+    constant; GetValues reads it back), and the IJ vector's constant values and
+    inner product."""
+    L = gb.lib()
+    L.HYPRE_IJMatrixGetRowCounts.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.HYPRE_IJMatrixSetConstantValues.argtypes = [C.c_void_p, C.c_double]
+    L.HYPRE_IJVectorSetConstantValues.argtypes = [C.c_void_p, C.c_double]
+    L.HYPRE_IJVectorInnerProd.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    L.HYPRE_ClearAllErrors()
+    I, J, V = oracle_mod.stencil(7, 6, 5, 4)
+    n = len(I) - 1
+    A = gb.IJMatrix(I, J, V)
+    t = C.c_int()
+    gb.check(L.HYPRE_IJMatrixGetObjectType(A.h, C.byref(t)))
+    assert t.value == gb.HYPRE_PARCSR
+    rows = np.array([0, 7, n - 1, n, -1], np.int32)
+    cnt = np.zeros(len(rows), np.int32)
+    gb.check(L.HYPRE_IJMatrixGetRowCounts(A.h, len(rows), rows.ctypes.data, cnt.ctypes.data))
+    lens = np.diff(I)
+    assert list(cnt) == [lens[0], lens[7], lens[n - 1], 0, 0]
+    gb.check(L.HYPRE_IJMatrixSetConstantValues(A.h, 0.5))
+    x = np.random.default_rng(3).standard_normal(n)
+    xv, yv = gb.IJVector(n, x), gb.IJVector(n, np.zeros(n))
+    gb.check(L.HYPRE_ParCSRMatrixMatvec(1.0, A.par, xv.par, 0.0, yv.par))
+    ref = np.array([0.5 * x[J[I[r]:I[r + 1]]].sum() for r in range(n)])
+    np.testing.assert_allclose(yv.values(), ref, rtol=1e-14, atol=1e-14)
+    ncols = np.array([2], np.int32)
+    r = np.array([3], np.int32)
+    cols = np.array(J[I[3]:I[3] + 2], np.int32)
+    vals = np.zeros(2)
+    gb.check(L.HYPRE_IJMatrixGetValues(A.h, 1, ncols.ctypes.data, r.ctypes.data, cols.ctypes.data,
+                                       vals.ctypes.data))
+    assert list(vals) == [0.5, 0.5]
+    gb.check(L.HYPRE_IJVectorGetObjectType(xv.h, C.byref(t)))
+    assert t.value == gb.HYPRE_PARCSR
+    gb.check(L.HYPRE_IJVectorSetConstantValues(yv.h, 2.0))
+    d = C.c_double()
+    gb.check(L.HYPRE_IJVectorInnerProd(xv.h, yv.h, C.byref(d)))
+    assert abs(d.value - 2.0 * x.sum()) <= 1e-12 * np.abs(x).sum() * 2
+    for f in (L.HYPRE_IJMatrixSetMaxOffProcElmts, L.HYPRE_IJMatrixSetPrintLevel, L.HYPRE_IJMatrixSetOMPFlag):
+        assert f(A.h, 1) == 0
+    for f in (L.HYPRE_IJVectorSetMaxOffProcElmts, L.HYPRE_IJVectorSetPrintLevel):
+        assert f(xv.h, 1) == 0
+    A.destroy(); xv.destroy(); yv.destroy()
