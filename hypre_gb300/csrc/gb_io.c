@@ -555,3 +555,214 @@ HYPRE_Int HYPRE_IJVectorPrintBinary(HYPRE_IJVector vector, const char *filename)
    if (w != 8 + (size_t) n) { gb_error(HYPRE_ERROR_GENERIC, "Could not write all entries"); }
    return gb_error_flag;
 }
+
+/* ------------------------------------------------------------------------
+ * ParVector text files of one process (hypre_ParVectorPrint / Read,
+ * src/parcsr_mv/par_vector.c:330-410, with hypre_SeqVectorPrint / Read
+ * src/seq_mv/vector.c:420-525): <name>.0 holds the size and then one value
+ * per line (%.14e); <name>.INFO.0 the global size and the row range [0, n).
+ * ------------------------------------------------------------------------ */
+HYPRE_Int HYPRE_ParVectorPrint(HYPRE_ParVector vector, const char *file_name)
+{
+   gb_parvec *v = (gb_parvec *) vector;
+   if (!v || v->magic != GB_MAGIC_VEC || !v->d) { gb_error_in_arg(1); return gb_error_flag; }
+   if (!file_name) { gb_error_in_arg(2); return gb_error_flag; }
+   const int n = v->n;
+   double *h = (double *) malloc(sizeof(double) * (size_t) (n > 0 ? n : 1));
+   if (!h) { gb_error(HYPRE_ERROR_MEMORY, "ParVectorPrint"); return gb_error_flag; }
+   cudaMemcpyAsync(h, v->d, sizeof(double) * (size_t) n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   char name[4096];
+   snprintf(name, sizeof(name), "%s.0", file_name);
+   FILE *f = fopen(name, "w");
+   if (!f) { free(h); gb_error(HYPRE_ERROR_GENERIC, "ParVectorPrint: cannot open the file"); return gb_error_flag; }
+   fprintf(f, "%d\n", n);
+   for (int i = 0; i < n; i++) { fprintf(f, "%.14e\n", h[i]); }
+   fclose(f);
+   free(h);
+   snprintf(name, sizeof(name), "%s.INFO.0", file_name);
+   f = fopen(name, "w");
+   if (!f) { gb_error(HYPRE_ERROR_GENERIC, "ParVectorPrint: cannot open the file"); return gb_error_flag; }
+   fprintf(f, "%d\n%d\n%d\n", n, 0, n);
+   fclose(f);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParVectorRead(MPI_Comm comm, const char *file_name, HYPRE_ParVector *vector)
+{
+   (void) comm;
+   if (!file_name) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!vector) { gb_error_in_arg(3); return gb_error_flag; }
+   *vector = NULL;
+   char name[4096];
+   snprintf(name, sizeof(name), "%s.INFO.0", file_name);
+   FILE *f = fopen(name, "r");
+   int gsize = 0, p0 = 0, p1 = 0;
+   if (!f || fscanf(f, "%d %d %d", &gsize, &p0, &p1) != 3)
+   {
+      if (f) { fclose(f); }
+      gb_error(HYPRE_ERROR_GENERIC, "ParVectorRead: cannot read the INFO file");
+      return gb_error_flag;
+   }
+   fclose(f);
+   snprintf(name, sizeof(name), "%s.0", file_name);
+   f = fopen(name, "r");
+   int n = 0;
+   if (!f || fscanf(f, "%d", &n) != 1 || n < 0 || n != p1 - p0 || n != gsize)
+   {
+      if (f) { fclose(f); }
+      gb_error(HYPRE_ERROR_GENERIC, "ParVectorRead: cannot read the vector file (one process)");
+      return gb_error_flag;
+   }
+   double *h = (double *) malloc(sizeof(double) * (size_t) (n > 0 ? n : 1));
+   if (!h) { fclose(f); gb_error(HYPRE_ERROR_MEMORY, "ParVectorRead"); return gb_error_flag; }
+   for (int i = 0; i < n; i++)
+   {
+      if (fscanf(f, "%le", &h[i]) != 1)
+      {
+         fclose(f); free(h);
+         gb_error(HYPRE_ERROR_GENERIC, "ParVectorRead: short vector file");
+         return gb_error_flag;
+      }
+   }
+   fclose(f);
+   HYPRE_ParVector v = NULL;
+   HYPRE_ParVectorCreate(comm, n, NULL, &v);
+   HYPRE_ParVectorInitialize(v);
+   gb_parvec *pv = (gb_parvec *) v;
+   if (pv && pv->d)
+   {
+      cudaMemcpyAsync(pv->d, h, sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, gb_stream());
+      gb_sync();
+   }
+   free(h);
+   *vector = v;
+   return gb_error_flag;
+}
+
+/* values at the given global indices (all values in order when indices is
+ * NULL), copied to the host (HYPRE_parcsr_vector.c, one process) */
+HYPRE_Int HYPRE_ParVectorGetValues(HYPRE_ParVector vector, HYPRE_Int num_values, HYPRE_BigInt *indices,
+                                   HYPRE_Complex *values)
+{
+   gb_parvec *v = (gb_parvec *) vector;
+   if (!v || v->magic != GB_MAGIC_VEC || !v->d) { gb_error_in_arg(1); return gb_error_flag; }
+   if (num_values < 0) { gb_error_in_arg(2); return gb_error_flag; }
+   if (num_values > 0 && !values) { gb_error_in_arg(4); return gb_error_flag; }
+   if (!indices)
+   {
+      if (num_values > v->n) { gb_error_in_arg(2); return gb_error_flag; }
+      cudaMemcpyAsync(values, v->d, sizeof(double) * (size_t) num_values, cudaMemcpyDeviceToHost, gb_stream());
+      gb_sync();
+      return gb_error_flag;
+   }
+   double *h = (double *) malloc(sizeof(double) * (size_t) (v->n > 0 ? v->n : 1));
+   if (!h) { gb_error(HYPRE_ERROR_MEMORY, "ParVectorGetValues"); return gb_error_flag; }
+   cudaMemcpyAsync(h, v->d, sizeof(double) * (size_t) v->n, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   for (int k = 0; k < num_values; k++)
+   {
+      if (indices[k] < 0 || indices[k] >= v->n) { gb_error_in_arg(3); continue; }
+      values[k] = h[indices[k]];
+   }
+   free(h);
+   return gb_error_flag;
+}
+
+/* ------------------------------------------------------------------------
+ * ParCSR text files of one process (hypre_ParCSRMatrixPrint / Read,
+ * src/parcsr_mv/par_csr_matrix.c:872-930, with hypre_CSRMatrixPrint
+ * src/seq_mv/csr_matrix.c:540-610): <name>.D.0 holds the row count, the row
+ * pointers, the column indices (both 1-based) and the values (%.14e), one
+ * per line; <name>.INFO.0 the global sizes, the number of off-process columns
+ * (0) and the row and column ranges.  No <name>.O.0 is written: one process
+ * has no off-process block.  Read accepts square matrices.
+ * ------------------------------------------------------------------------ */
+HYPRE_Int HYPRE_ParCSRMatrixPrint(HYPRE_ParCSRMatrix matrix, const char *file_name)
+{
+   gb_parcsr *A = (gb_parcsr *) matrix;
+   if (!A || A->magic != GB_MAGIC_MAT) { gb_error_in_arg(1); return gb_error_flag; }
+   if (!file_name) { gb_error_in_arg(2); return gb_error_flag; }
+   const int n = A->A.nr, nnz = A->A.nnz;
+   int *I = (int *) malloc(sizeof(int) * (size_t) (n + 1)), *J = (int *) malloc(sizeof(int) * (size_t) (nnz ? nnz : 1));
+   double *V = (double *) malloc(sizeof(double) * (size_t) (nnz ? nnz : 1));
+   if (!I || !J || !V) { free(I); free(J); free(V); gb_error(HYPRE_ERROR_MEMORY, "ParCSRMatrixPrint"); return gb_error_flag; }
+   cudaMemcpyAsync(I, A->A.i, sizeof(int) * (size_t) (n + 1), cudaMemcpyDeviceToHost, gb_stream());
+   cudaMemcpyAsync(J, A->A.j, sizeof(int) * (size_t) nnz, cudaMemcpyDeviceToHost, gb_stream());
+   cudaMemcpyAsync(V, A->A.v, sizeof(double) * (size_t) nnz, cudaMemcpyDeviceToHost, gb_stream());
+   gb_sync();
+   char name[4096];
+   snprintf(name, sizeof(name), "%s.D.0", file_name);
+   FILE *f = fopen(name, "w");
+   if (!f) { free(I); free(J); free(V); gb_error(HYPRE_ERROR_GENERIC, "ParCSRMatrixPrint: cannot open the file"); return gb_error_flag; }
+   fprintf(f, "%d\n", n);
+   for (int r = 0; r <= n; r++) { fprintf(f, "%d\n", I[r] + 1); }
+   for (int k = 0; k < nnz; k++) { fprintf(f, "%d\n", J[k] + 1); }
+   for (int k = 0; k < nnz; k++) { fprintf(f, "%.14e\n", V[k]); }
+   fclose(f);
+   free(I); free(J); free(V);
+   snprintf(name, sizeof(name), "%s.INFO.0", file_name);
+   f = fopen(name, "w");
+   if (!f) { gb_error(HYPRE_ERROR_GENERIC, "ParCSRMatrixPrint: cannot open the file"); return gb_error_flag; }
+   fprintf(f, "%d\n%d\n%d\n%d %d %d %d\n", n, A->A.nc, 0, 0, n, 0, A->A.nc);
+   fclose(f);
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_ParCSRMatrixRead(MPI_Comm comm, const char *file_name, HYPRE_ParCSRMatrix *matrix)
+{
+   (void) comm;
+   if (!file_name) { gb_error_in_arg(2); return gb_error_flag; }
+   if (!matrix) { gb_error_in_arg(3); return gb_error_flag; }
+   *matrix = NULL;
+   char name[4096];
+   snprintf(name, sizeof(name), "%s.INFO.0", file_name);
+   FILE *f = fopen(name, "r");
+   int gr = 0, gc = 0, noffd = 0, rs = 0, re = 0, cs = 0, ce = 0;
+   if (!f || fscanf(f, "%d %d %d %d %d %d %d", &gr, &gc, &noffd, &rs, &re, &cs, &ce) != 7)
+   {
+      if (f) { fclose(f); }
+      gb_error(HYPRE_ERROR_GENERIC, "ParCSRMatrixRead: cannot read the INFO file");
+      return gb_error_flag;
+   }
+   fclose(f);
+   if (noffd != 0 || gr != gc || rs != 0 || re != gr || cs != 0 || ce != gc)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "ParCSRMatrixRead: one process, square matrices");
+      return gb_error_flag;
+   }
+   snprintf(name, sizeof(name), "%s.D.0", file_name);
+   f = fopen(name, "r");
+   int n = -1;
+   if (!f || fscanf(f, "%d", &n) != 1 || n != gr)
+   {
+      if (f) { fclose(f); }
+      gb_error(HYPRE_ERROR_GENERIC, "ParCSRMatrixRead: cannot read the matrix file");
+      return gb_error_flag;
+   }
+   int *I = (int *) malloc(sizeof(int) * (size_t) (n + 1));
+   int ok = I != NULL;
+   for (int r = 0; ok && r <= n; r++) { ok = fscanf(f, "%d", &I[r]) == 1; if (ok) { I[r] -= 1; } }
+   const int nnz = ok ? I[n] : 0;
+   ok = ok && I[0] == 0 && nnz >= 0;
+   for (int r = 0; ok && r < n; r++) { ok = I[r + 1] >= I[r]; }
+   int *J = ok ? (int *) malloc(sizeof(int) * (size_t) (nnz ? nnz : 1)) : NULL;
+   double *V = ok ? (double *) malloc(sizeof(double) * (size_t) (nnz ? nnz : 1)) : NULL;
+   ok = ok && J && V;
+   for (int k = 0; ok && k < nnz; k++)
+   {
+      ok = fscanf(f, "%d", &J[k]) == 1;
+      if (ok) { J[k] -= 1; ok = J[k] >= 0 && J[k] < n; }
+   }
+   for (int k = 0; ok && k < nnz; k++) { ok = fscanf(f, "%le", &V[k]) == 1; }
+   fclose(f);
+   if (!ok)
+   {
+      free(I); free(J); free(V);
+      gb_error(HYPRE_ERROR_GENERIC, "ParCSRMatrixRead: malformed matrix file");
+      return gb_error_flag;
+   }
+   HYPRE_GB300_ParCSRMatrixCreateFromHostCSR(n, I, J, V, matrix);
+   free(I); free(J); free(V);
+   return gb_error_flag;
+}

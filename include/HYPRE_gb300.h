@@ -180,6 +180,17 @@ HYPRE_Int HYPRE_ParCSRMatrixMatvecT(HYPRE_Complex alpha, HYPRE_ParCSRMatrix A, H
 HYPRE_Int HYPRE_ParCSRMatrixMatmat(HYPRE_ParCSRMatrix A, HYPRE_ParCSRMatrix B,
                                    HYPRE_ParCSRMatrix *C);                 /* :305 */
 HYPRE_Int HYPRE_ParCSRMatrixDestroy(HYPRE_ParCSRMatrix matrix);           /* :75 */
+/* ParVector text files of one process (<name>.0 with the size and %.14e values,
+ * <name>.INFO.0 with the global size and row range) and values by index */
+HYPRE_Int HYPRE_ParVectorPrint(HYPRE_ParVector vector, const char *file_name); /* HYPRE_parcsr_mv.h:209 */
+HYPRE_Int HYPRE_ParVectorRead(MPI_Comm comm, const char *file_name, HYPRE_ParVector *vector); /* :201 */
+HYPRE_Int HYPRE_ParVectorGetValues(HYPRE_ParVector vector, HYPRE_Int num_values, HYPRE_BigInt *indices,
+                                   HYPRE_Complex *values); /* :331 */
+/* ParCSR text files of one process (<name>.D.0: row count, 1-based row
+ * pointers and columns, %.14e values; <name>.INFO.0: sizes and ranges; Read
+ * takes square matrices) */
+HYPRE_Int HYPRE_ParCSRMatrixPrint(HYPRE_ParCSRMatrix matrix, const char *file_name); /* HYPRE_parcsr_mv.h:95 */
+HYPRE_Int HYPRE_ParCSRMatrixRead(MPI_Comm comm, const char *file_name, HYPRE_ParCSRMatrix *matrix); /* :87 */
 HYPRE_Int HYPRE_ParVectorCreate(MPI_Comm comm, HYPRE_BigInt global_size, HYPRE_BigInt *partitioning,
                                 HYPRE_ParVector *vector);                  /* :179 */
 HYPRE_Int HYPRE_ParVectorDestroy(HYPRE_ParVector vector);                 /* :188 */

@@ -265,3 +265,65 @@ def test_read_errors(gb, tmp_path):
     assert err & ERR_GENERIC
     L.HYPRE_ClearAllErrors()
     assert not os.path.exists(missing + ".00000")
+
+
+def test_par_vector_print_read_and_get_values(gb, tmp_path):
+    """HYPRE_ParVectorPrint writes the reference's one-process files
+    (<name>.0: the size, then %.14e per line; <name>.INFO.0: global size and
+    row range), HYPRE_ParVectorRead reads them back, and
+    HYPRE_ParVectorGetValues returns values by index."""
+    import ctypes as C
+    L = gb.lib()
+    L.HYPRE_ParVectorPrint.argtypes = [C.c_void_p, C.c_char_p]
+    L.HYPRE_ParVectorRead.argtypes = [C.c_int, C.c_char_p, C.POINTER(C.c_void_p)]
+    L.HYPRE_ParVectorGetValues.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.HYPRE_ClearAllErrors()
+    n = 37
+    x = np.random.default_rng(5).standard_normal(n)
+    v = gb.IJVector(n, x)
+    name = str(tmp_path / "vec")
+    gb.check(L.HYPRE_ParVectorPrint(v.par, name.encode()))
+    lines = open(name + ".0").read().split()
+    assert int(lines[0]) == n and lines[1] == "%.14e" % x[0]
+    assert open(name + ".INFO.0").read().split() == [str(n), "0", str(n)]
+    w = C.c_void_p()
+    gb.check(L.HYPRE_ParVectorRead(0, name.encode(), C.byref(w)))
+    back = np.zeros(n)
+    gb.check(L.HYPRE_ParVectorGetValues(w, n, None, back.ctypes.data))
+    np.testing.assert_array_equal(back, np.array([float("%.14e" % t) for t in x]))
+    idx = np.array([3, 0, 36], np.int32)
+    got = np.zeros(3)
+    gb.check(L.HYPRE_ParVectorGetValues(v.par, 3, idx.ctypes.data, got.ctypes.data))
+    np.testing.assert_array_equal(got, x[idx])
+    L.HYPRE_ParVectorDestroy(w)
+    v.destroy()
+
+
+def test_parcsr_print_and_read(gb, oracle_mod, tmp_path):
+    """HYPRE_ParCSRMatrixPrint writes the reference's one-process files
+    (<name>.D.0: row count, 1-based row pointers and columns, %.14e values;
+    <name>.INFO.0: sizes and ranges) and HYPRE_ParCSRMatrixRead reads them
+    back to the same matrix."""
+    import ctypes as C
+    L = gb.lib()
+    L.HYPRE_ParCSRMatrixPrint.argtypes = [C.c_void_p, C.c_char_p]
+    L.HYPRE_ParCSRMatrixRead.argtypes = [C.c_int, C.c_char_p, C.POINTER(C.c_void_p)]
+    L.HYPRE_ClearAllErrors()
+    I, J, V = oracle_mod.stencil(27, 5, 4, 3)
+    V = V * (1.0 + 0.001 * np.arange(len(V)))
+    n = len(I) - 1
+    A = gb.IJMatrix(I, J, V)
+    name = str(tmp_path / "mat")
+    gb.check(L.HYPRE_ParCSRMatrixPrint(A.par, name.encode()))
+    d = open(name + ".D.0").read().split()
+    I2, J2, V2 = A.csr()
+    assert int(d[0]) == n and [int(t) for t in d[1:n + 2]] == list(I2 + 1)
+    assert open(name + ".INFO.0").read().split() == [str(n), str(n), "0", "0", str(n), "0", str(n)]
+    B = C.c_void_p()
+    gb.check(L.HYPRE_ParCSRMatrixRead(0, name.encode(), C.byref(B)))
+    I3, J3, V3 = gb.parcsr_to_host(B)
+    np.testing.assert_array_equal(I3, I2)
+    np.testing.assert_array_equal(J3, J2)
+    np.testing.assert_array_equal(V3, np.array([float("%.14e" % t) for t in V2]))
+    L.HYPRE_ParCSRMatrixDestroy(B)
+    A.destroy()
