@@ -2453,8 +2453,9 @@ HYPRE_Int HYPRE_BoomerAMGSolve(HYPRE_Solver solver, HYPRE_ParCSRMatrix A, HYPRE_
    gb_amg_params *prm = &a->prm;
    /* hypre_BoomerAMGSolve (par_amg_solve.c:150-342): the relative residual
     * ||b - A x|| / ||b|| (absolute when b = 0; 1 when tol = 0) before the
-    * loop and after every cycle; cycles while it is >= tol and fewer than
-    * max_iter ran; running into max_iter with tol > 0 is a convergence error */
+    * loop and after every cycle; cycles while it is >= tol (or fewer than
+    * min_iter ran) and fewer than max_iter ran; running into max_iter with
+    * tol > 0 is a convergence error */
    const int check = prm->tol > 0.0;
    double *r = a->r_work;
    double rel = 1.0, rhs = 0.0;
@@ -2467,7 +2468,7 @@ HYPRE_Int HYPRE_BoomerAMGSolve(HYPRE_Solver solver, HYPRE_ParCSRMatrix A, HYPRE_
    }
    int iter = 0;
    double *corr = prm->cycle_prec == GB_PREC_F64 ? NULL : (double *) gb_scratch(5, sizeof(double) * (size_t) n);
-   while (rel >= prm->tol && iter < prm->max_iter)
+   while ((rel >= prm->tol || iter < prm->min_iter) && iter < prm->max_iter)
    {
       if (!corr)
       {
@@ -2513,6 +2514,7 @@ int gb_amg_precond(HYPRE_Solver solver, const double *b, double *x)
    }
 
 SETTER(HYPRE_BoomerAMGSetTol, tol, HYPRE_Real)
+SETTER(HYPRE_BoomerAMGSetMinIter, min_iter, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetMaxIter, max_iter, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetMaxCoarseSize, max_coarse_size, HYPRE_Int)
 SETTER(HYPRE_BoomerAMGSetMinCoarseSize, min_coarse_size, HYPRE_Int)
@@ -2885,5 +2887,112 @@ HYPRE_Int HYPRE_GB300_BoomerAMGGetLevelL1(HYPRE_Solver solver, HYPRE_Int level, 
    if (level < 0 || level >= a->num_levels || !l1) { gb_error_in_arg(2); return gb_error_flag; }
    cudaMemcpyAsync(l1, a->lev[level].l1, sizeof(double) * (size_t) a->lev[level].n, cudaMemcpyDeviceToHost, gb_stream());
    gb_sync();
+   return gb_error_flag;
+}
+
+/* ------------------------------------------------------------------------
+ * Getters of the parameters above (HYPRE_parcsr_ls.h), and settings that
+ * have one supported value: anything else is refused, not ignored.
+ * Output-only settings (debug flag, sequential threshold of the multi-process
+ * coarse solve) are accepted.
+ * ------------------------------------------------------------------------ */
+#define GETTER(name, field, type)                                  \
+   HYPRE_Int name(HYPRE_Solver solver, type *v)                     \
+   {                                                                \
+      gb_amg *a = amg_of(solver, 1);                                \
+      if (!a) { return gb_error_flag; }                             \
+      if (!v) { gb_error_in_arg(2); return gb_error_flag; }         \
+      *v = (type) a->prm.field;                                     \
+      return gb_error_flag;                                         \
+   }
+GETTER(HYPRE_BoomerAMGGetMaxIter, max_iter, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetTol, tol, HYPRE_Real)
+GETTER(HYPRE_BoomerAMGGetCycleType, cycle_type, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetFCycle, fcycle, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetStrongThreshold, strong_threshold, HYPRE_Real)
+GETTER(HYPRE_BoomerAMGGetMaxRowSum, max_row_sum, HYPRE_Real)
+GETTER(HYPRE_BoomerAMGGetPMaxElmts, p_max_elmts, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetTruncFactor, trunc_factor, HYPRE_Real)
+GETTER(HYPRE_BoomerAMGGetMaxLevels, max_levels, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetMaxCoarseSize, max_coarse_size, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetMinCoarseSize, min_coarse_size, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetCoarsenType, coarsen_type, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetPrintLevel, print_level, HYPRE_Int)
+GETTER(HYPRE_BoomerAMGGetLogging, logging, HYPRE_Int)
+#undef GETTER
+
+/* k: 1 down, 2 up, 3 coarsest (HYPRE_parcsr_ls.h:821, :907) */
+HYPRE_Int HYPRE_BoomerAMGGetCycleNumSweeps(HYPRE_Solver solver, HYPRE_Int *num_sweeps, HYPRE_Int k)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (!num_sweeps) { gb_error_in_arg(2); return gb_error_flag; }
+   if (k < 1 || k > 3) { gb_error_in_arg(3); return gb_error_flag; }
+   *num_sweeps = a->prm.num_sweeps[k];
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGGetCycleRelaxType(HYPRE_Solver solver, HYPRE_Int *relax_type, HYPRE_Int k)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (!relax_type) { gb_error_in_arg(2); return gb_error_flag; }
+   if (k < 1 || k > 3) { gb_error_in_arg(3); return gb_error_flag; }
+   *relax_type = a->prm.relax_type[k];
+   return gb_error_flag;
+}
+
+HYPRE_Int HYPRE_BoomerAMGGetNumFunctions(HYPRE_Solver solver, HYPRE_Int *num_functions)
+{
+   if (!amg_of(solver, 1)) { return gb_error_flag; }
+   if (!num_functions) { gb_error_in_arg(2); return gb_error_flag; }
+   *num_functions = 1;
+   return gb_error_flag;
+}
+
+static HYPRE_Int only_value(HYPRE_Solver solver, HYPRE_Int v, HYPRE_Int ok, const char *what)
+{
+   if (!amg_of(solver, 1)) { return gb_error_flag; }
+   if (v != ok)
+   {
+      gb_error(HYPRE_ERROR_GENERIC, what);
+      gb_error_in_arg(2);
+   }
+   return gb_error_flag;
+}
+HYPRE_Int HYPRE_BoomerAMGSetNumFunctions(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return only_value(solver, v, 1, "num_functions: scalar problems (1) are supported");
+}
+HYPRE_Int HYPRE_BoomerAMGSetNodal(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return only_value(solver, v, 0, "nodal: only 0 is supported");
+}
+HYPRE_Int HYPRE_BoomerAMGSetMeasureType(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return only_value(solver, v, 0, "measure_type: only local measures (0) are supported");
+}
+HYPRE_Int HYPRE_BoomerAMGSetRedundant(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return only_value(solver, v, 0, "redundant: only 0 is supported");
+}
+HYPRE_Int HYPRE_BoomerAMGSetCoarsenCutFactor(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return only_value(solver, v, 0, "coarsen_cut_factor: only 0 is supported");
+}
+HYPRE_Int HYPRE_BoomerAMGSetConvergeType(HYPRE_Solver solver, HYPRE_Int v)
+{
+   return only_value(solver, v, 0, "converge_type: only the relative residual (0) is supported");
+}
+HYPRE_Int HYPRE_BoomerAMGSetDebugFlag(HYPRE_Solver solver, HYPRE_Int v)
+{
+   (void) v;
+   amg_of(solver, 1);
+   return gb_error_flag;
+}
+HYPRE_Int HYPRE_BoomerAMGSetSeqThreshold(HYPRE_Solver solver, HYPRE_Int v)
+{
+   (void) v;
+   amg_of(solver, 1);
    return gb_error_flag;
 }

@@ -157,6 +157,7 @@ typedef struct
    int    fcycle;            /* 1: F-cycle */
    double tol;
    int    max_iter;
+   int    min_iter;          /* BoomerAMG as the solver: cycles at least this many */
    int    print_level, logging;
    int    cycle_prec;        /* GB_PREC_F64 / F32 / F16 (finest values) */
    int    use_graph;

@@ -229,6 +229,35 @@ HYPRE_Int HYPRE_BoomerAMGSetAggTruncFactor(HYPRE_Solver solver, HYPRE_Real agg_t
 HYPRE_Int HYPRE_BoomerAMGSetAggPMaxElmts(HYPRE_Solver solver, HYPRE_Int agg_P_max_elmts); /* :577 */
 HYPRE_Int HYPRE_BoomerAMGSetAggP12TruncFactor(HYPRE_Solver solver, HYPRE_Real agg_P12_trunc_factor); /* :569 */
 HYPRE_Int HYPRE_BoomerAMGSetAggP12MaxElmts(HYPRE_Solver solver, HYPRE_Int agg_P12_max_elmts); /* :585 */
+/* getters of the stored parameters, and settings with one supported value
+ * (others are refused with HYPRE_ERROR_GENERIC); MinIter bounds the
+ * stand-alone solve's cycles from below */
+HYPRE_Int HYPRE_BoomerAMGSetMinIter(HYPRE_Solver solver, HYPRE_Int min_iter); /* :237 */
+HYPRE_Int HYPRE_BoomerAMGGetMaxIter(HYPRE_Solver solver, HYPRE_Int *max_iter); /* :232 */
+HYPRE_Int HYPRE_BoomerAMGGetTol(HYPRE_Solver solver, HYPRE_Real *tol); /* :222 */
+HYPRE_Int HYPRE_BoomerAMGGetCycleType(HYPRE_Solver solver, HYPRE_Int *cycle_type); /* :656 */
+HYPRE_Int HYPRE_BoomerAMGGetFCycle(HYPRE_Solver solver, HYPRE_Int *fcycle); /* :665 */
+HYPRE_Int HYPRE_BoomerAMGGetStrongThreshold(HYPRE_Solver solver, HYPRE_Real *strong_threshold); /* :289 */
+HYPRE_Int HYPRE_BoomerAMGGetMaxRowSum(HYPRE_Solver solver, HYPRE_Real *max_row_sum);
+HYPRE_Int HYPRE_BoomerAMGGetPMaxElmts(HYPRE_Solver solver, HYPRE_Int *P_max_elmts);
+HYPRE_Int HYPRE_BoomerAMGGetTruncFactor(HYPRE_Solver solver, HYPRE_Real *trunc_factor);
+HYPRE_Int HYPRE_BoomerAMGGetMaxLevels(HYPRE_Solver solver, HYPRE_Int *max_levels);
+HYPRE_Int HYPRE_BoomerAMGGetMaxCoarseSize(HYPRE_Solver solver, HYPRE_Int *max_coarse_size);
+HYPRE_Int HYPRE_BoomerAMGGetMinCoarseSize(HYPRE_Solver solver, HYPRE_Int *min_coarse_size);
+HYPRE_Int HYPRE_BoomerAMGGetCoarsenType(HYPRE_Solver solver, HYPRE_Int *coarsen_type);
+HYPRE_Int HYPRE_BoomerAMGGetPrintLevel(HYPRE_Solver solver, HYPRE_Int *print_level);
+HYPRE_Int HYPRE_BoomerAMGGetLogging(HYPRE_Solver solver, HYPRE_Int *logging);
+HYPRE_Int HYPRE_BoomerAMGGetCycleNumSweeps(HYPRE_Solver solver, HYPRE_Int *num_sweeps, HYPRE_Int k); /* :821 */
+HYPRE_Int HYPRE_BoomerAMGGetCycleRelaxType(HYPRE_Solver solver, HYPRE_Int *relax_type, HYPRE_Int k); /* :907 */
+HYPRE_Int HYPRE_BoomerAMGGetNumFunctions(HYPRE_Solver solver, HYPRE_Int *num_functions); /* :174 */
+HYPRE_Int HYPRE_BoomerAMGSetNumFunctions(HYPRE_Solver solver, HYPRE_Int num_functions); /* :171 */
+HYPRE_Int HYPRE_BoomerAMGSetNodal(HYPRE_Solver solver, HYPRE_Int nodal); /* :446 */
+HYPRE_Int HYPRE_BoomerAMGSetMeasureType(HYPRE_Solver solver, HYPRE_Int measure_type); /* :405 */
+HYPRE_Int HYPRE_BoomerAMGSetRedundant(HYPRE_Solver solver, HYPRE_Int redundant); /* :785 */
+HYPRE_Int HYPRE_BoomerAMGSetCoarsenCutFactor(HYPRE_Solver solver, HYPRE_Int coarsen_cut_factor); /* :274 */
+HYPRE_Int HYPRE_BoomerAMGSetConvergeType(HYPRE_Solver solver, HYPRE_Int type); /* :208 */
+HYPRE_Int HYPRE_BoomerAMGSetDebugFlag(HYPRE_Solver solver, HYPRE_Int debug_flag); /* :1521 */
+HYPRE_Int HYPRE_BoomerAMGSetSeqThreshold(HYPRE_Solver solver, HYPRE_Int seq_threshold); /* :775 */
 HYPRE_Int HYPRE_BoomerAMGSetCycleType(HYPRE_Solver solver, HYPRE_Int cycle_type); /* :653 */
 HYPRE_Int HYPRE_BoomerAMGSetFCycle(HYPRE_Solver solver, HYPRE_Int fcycle); /* :662 */
 HYPRE_Int HYPRE_BoomerAMGSetNumSweeps(HYPRE_Solver solver, HYPRE_Int num_sweeps); /* :806 */

@@ -280,3 +280,38 @@ def test_unsupported_options_are_refused(gb, oracle_mod):
         L.HYPRE_ClearAllErrors()
         amg.destroy()
     A.destroy(); b.destroy(); x.destroy()
+
+
+def test_getters_and_min_iter(gb, oracle_mod):
+    """The BoomerAMG getters return what the setters stored, single-value
+    settings refuse other values, and MinIter makes the stand-alone solve run
+    at least that many cycles (par_amg_solve.c: cycle while the residual is
+    above tol or fewer than min_iter cycles ran)."""
+    import ctypes as C
+    L = gb.lib()
+    L.HYPRE_ClearAllErrors()
+    amg = gb.BoomerAMG(StrongThreshold=0.3, MaxIter=20, Tol=0.5, PMaxElmts=3, MaxLevels=7)
+    i, d = C.c_int(), C.c_double()
+    for name, want in (("MaxIter", 20), ("PMaxElmts", 3), ("MaxLevels", 7), ("CycleType", 1)):
+        gb.check(getattr(L, "HYPRE_BoomerAMGGet" + name)(amg.h, C.byref(i)))
+        assert i.value == want, name
+    for name, want in (("Tol", 0.5), ("StrongThreshold", 0.3)):
+        gb.check(getattr(L, "HYPRE_BoomerAMGGet" + name)(amg.h, C.byref(d)))
+        assert d.value == want, name
+    gb.check(L.HYPRE_BoomerAMGGetCycleRelaxType(amg.h, C.byref(i), 1))
+    assert i.value == 18
+    for name, bad, good in (("NumFunctions", 2, 1), ("Nodal", 1, 0), ("MeasureType", 1, 0)):
+        L.HYPRE_ClearAllErrors()
+        assert getattr(L, "HYPRE_BoomerAMGSet" + name)(amg.h, bad) & gb.HYPRE_ERROR_GENERIC, name
+        L.HYPRE_ClearAllErrors()
+        assert getattr(L, "HYPRE_BoomerAMGSet" + name)(amg.h, good) == 0, name
+    I, J, V = oracle_mod.stencil(7, 8, 8, 8)
+    n = len(I) - 1
+    A = gb.IJMatrix(I, J, V)
+    b, x = gb.IJVector(n, np.ones(n)), gb.IJVector(n, np.zeros(n))
+    gb.check(L.HYPRE_BoomerAMGSetMinIter(amg.h, 5))
+    gb.check(L.HYPRE_BoomerAMGSetup(amg.h, A.par, b.par, x.par))
+    gb.check(L.HYPRE_BoomerAMGSolve(amg.h, A.par, b.par, x.par))
+    gb.check(L.HYPRE_BoomerAMGGetNumIterations(amg.h, C.byref(i)))
+    assert i.value == 5
+    amg.destroy(); A.destroy(); b.destroy(); x.destroy()
