@@ -791,10 +791,16 @@ def suite_arm(args):
             L.HYPRE_GB300_ParCSRMatrixDestroy(A)
             t = float(np.median(walls))
             byts = 2 * (12.0 * len(J) + 4.0 * (n + 1)) + 12.0 * nnz_c + 4.0 * (n + 1)
+            # scalar products of C = A*A: sum over the entries a_ik of nnz(A_k),
+            # i.e. sum over k of (entries in column k) x (entries in row k)
+            rowlen = np.diff(I).astype(np.int64)
+            colcnt = np.bincount(J, minlength=n).astype(np.int64)
+            nprod = int(np.dot(colcnt, rowlen))
             cases.append({"case": name, "rows": n, "nnz_A": len(J), "nnz_C": nnz_c, "nnz_reference": nnz_ref,
                           "nnz_equal": nnz_c == nnz_ref, "seconds": t, "device_seconds": float(np.median(devs)),
                           "mi250x_seconds": t_ref, "speedup_vs_mi250x": t_ref / t,
-                          "algorithmic_bytes": byts, "achieved_gbs": byts / t / 1e9, "frac": byts / t / 1e9 / peak})
+                          "algorithmic_bytes": byts, "achieved_gbs": byts / t / 1e9, "frac": byts / t / 1e9 / peak,
+                          "scalar_products": nprod, "gproducts_per_s": nprod / t / 1e9})
         top = cases[1]
         _line("SpGEMM C = A*A seconds, 27-point 128^3 (HYPRE_ParCSRMatrixMatmat)", top["seconds"], "s", args,
               {"workload": "spgemm_lap27_128", "operation": "C = A*A, ordered (reference column and summation order)",
