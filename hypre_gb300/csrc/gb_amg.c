@@ -1096,7 +1096,7 @@ done:
 /* aggressive level (par_amg_setup.c:1311-1358, :1778-1915): second-order
  * strength and PMIS on it, then multipass interpolation (agg_interp_type 4;
  * 8 and 9 in product form) or a two-stage P = P1 P2 (1: extended+i and
- * partial extended+i; 5, 6, 7: modified extended, extended+i, extended+e
+ * partial extended+i; 3: extended and partial extended; 5, 6, 7: modified extended, extended+i, extended+e
  * and the matching partial second stage).  Returns the number of coarse
  * points. */
 static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb_csr *P)
@@ -1191,13 +1191,14 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
       return nc;
    }
    /* P1 over the first coarsening (par_amg_setup.c:1778-1847): extended+i
-    * (agg_interp_type 1; turns CF -3 into -1), modified extended (5),
+    * (agg_interp_type 1) or extended (3), both turning CF -3 into -1;
+    * modified extended (5),
     * modified extended+i (6), modified extended+e (7) */
    const int at = prm->agg_interp_type;
    gb_csr P1;
-   if (at == 1)
+   if (at == 1 || at == 3)
    {
-      if (extpi_host(A, S, CF, f2c1, n, NULL, nc1, 1, &P1)) { return -1; }
+      if (extpi_host(A, S, CF, f2c1, n, NULL, nc1, at == 1, &P1)) { return -1; }
       gb_sf_to_f(n, CF, s);
    }
    else if (mm_interp(A, S, CF, f2c1, nc1, at == 5 ? 16 : at == 7 ? 18 : 17, &P1)) { return -1; }
@@ -1209,9 +1210,10 @@ static int agg_interp(gb_amg *amg, const gb_csr *A, const gb_csr *S, int *CF, gb
    int *f2c2 = (int *) gb_dmalloc(sizeof(int) * (size_t) (n + 1));
    int nc2 = number_points(n, CF, 1, 1, f2c2, NULL);
    gb_csr P2;
-   if (at == 1 || at == 6)
+   if (at == 1 || at == 3 || at == 6)
    {
-      if (extpi_host(A, S, CF, f2c2, nc1, c2f1, nc2, 1, &P2)) { return -1; }
+      /* partial extended+i, or partial extended for 3 (partial.c:1902) */
+      if (extpi_host(A, S, CF, f2c2, nc1, c2f1, nc2, at != 3, &P2)) { return -1; }
       gb_cf_clamp(n, CF, s);
    }
    else if (mm_partial_interp(A, S, CF, f2c2, nc2, at, &P2)) { return -1; }
@@ -1641,9 +1643,9 @@ static int amg_setup_inner(gb_amg *amg, gb_parcsr *A0)
    amg->lev[0].n = A0->A.nr;
    int level = 0;
    int maxl = prm->max_levels < 32 ? prm->max_levels : 32;
-   if (prm->agg_num_levels > 0 && !(prm->agg_interp_type == 1 || (prm->agg_interp_type >= 4 && prm->agg_interp_type <= 9)))
+   if (prm->agg_num_levels > 0 && !(prm->agg_interp_type == 1 || (prm->agg_interp_type >= 3 && prm->agg_interp_type <= 9)))
    {
-      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening: agg_interp_type 1 and 4-9 are supported");
+      gb_error(HYPRE_ERROR_GENERIC, "aggressive coarsening: agg_interp_type 1 and 3-9 are supported");
       return gb_error_flag;
    }
    while (1)

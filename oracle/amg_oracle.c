@@ -1581,7 +1581,23 @@ int or_mod_partial_interp(const or_csr *A, const or_csr *S, const int *CF, int v
  * or_extpi_interp) for the rows of the old C points only (CF == 1 identity,
  * CF == -2 interpolated); rows numbered by old coarse index, columns by new.
  * Afterwards CF values below -1 become -1 (:700). */
+static int partial_ext_interp(const or_csr *A, const or_csr *S, int *CF, int iterm, or_csr *P);
+
 int or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
+{
+   return partial_ext_interp(A, S, CF, 1, P);
+}
+
+/* Partial extended interpolation, hypre_BoomerAMGBuildPartialExtInterp
+ * src/parcsr_ls/partial.c:1902-2635: the same rows, pattern and weights as
+ * the partial extended+i interpolation without the i terms (a strong F
+ * neighbour's connection back to i takes no share of the distribution). */
+int or_partial_ext_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P)
+{
+   return partial_ext_interp(A, S, CF, 0, P);
+}
+
+static int partial_ext_interp(const or_csr *A, const or_csr *S, int *CF, int iterm, or_csr *P)
 {
    int n = A->nr;
    int *f2c = xmalloc(sizeof(int) * (n ? n : 1));
@@ -1659,7 +1675,7 @@ int or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P
                for (int jj1 = A->i[i1] + 1; jj1 < A->i[i1 + 1]; jj1++)
                {
                   int i2 = A->j[jj1];
-                  if ((pmark[i2] >= begin || i2 == i) && (sgn * A->v[jj1]) < 0) { sum += A->v[jj1]; }
+                  if ((pmark[i2] >= begin || (iterm && i2 == i)) && (sgn * A->v[jj1]) < 0) { sum += A->v[jj1]; }
                }
                if (sum != 0)
                {
@@ -1668,7 +1684,7 @@ int or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P
                   {
                      int i2 = A->j[jj1];
                      if (pmark[i2] >= begin && (sgn * A->v[jj1]) < 0) { Pv[pmark[i2]] += distribute * A->v[jj1]; }
-                     if (i2 == i && (sgn * A->v[jj1]) < 0) { diagonal += distribute * A->v[jj1]; }
+                     if (iterm && i2 == i && (sgn * A->v[jj1]) < 0) { diagonal += distribute * A->v[jj1]; }
                   }
                }
                else { diagonal += A->v[jj]; }
@@ -2291,7 +2307,7 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
       int nc;
       if (level < prm->agg_num_levels)
       {
-         /* par_amg_setup.c:1311-1358 and :1778-1915 (agg_interp_type 1, 4-9) */
+         /* par_amg_setup.c:1311-1358 and :1778-1915 (agg_interp_type 1, 3-9) */
          or_csr S2;
          or_strength2(&S, CF, prm->num_paths, &S2);
          int *CFN = xmalloc(sizeof(int) * (S2.nr ? S2.nr : 1));
@@ -2321,10 +2337,12 @@ int or_amg_setup(const or_csr *A0, const or_amg_params *prm, or_hierarchy *H)
             or_csr P1, P2;
             const int t = prm->agg_interp_type;
             if (t == 1) { or_extpi_interp(A, &S, CF, &P1); }
+            else if (t == 3) { or_ext_interp(A, &S, CF, &P1); }
             else { mod_interp(A, &S, CF, t == 5 ? 16 : t == 7 ? 18 : 17, &P1); }
             or_truncate(&P1, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
             or_correct_cf2(n, CF, CFN);
             if (t == 1 || t == 6) { or_partial_extpi_interp(A, &S, CF, &P2); }
+            else if (t == 3) { or_partial_ext_interp(A, &S, CF, &P2); }
             else { or_mod_partial_interp(A, &S, CF, t, &P2); }
             or_truncate(&P2, prm->agg_p12_trunc_factor, prm->agg_p12_max_elmts);
             or_matmul(&P1, &P2, &P);

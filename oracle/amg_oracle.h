@@ -107,6 +107,7 @@ void   or_correct_cf(int n, int *CF, const int *CFN);
 int    or_multipass_interp(const or_csr *A, const or_csr *S, int *CF, double trunc_factor, int max_elmts, or_csr *P);
 int    or_mod_multipass_interp(const or_csr *A, const or_csr *S, int *CF, int type, double trunc_factor,
                                int max_elmts, or_csr *P);
+int    or_partial_ext_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);
 int    or_mod_partial_interp(const or_csr *A, const or_csr *S, const int *CF, int variant, or_csr *P);
 int    or_mod_extpi_interp(const or_csr *A, const or_csr *S, const int *CF, or_csr *P);
 int    or_partial_extpi_interp(const or_csr *A, const or_csr *S, int *CF, or_csr *P);

@@ -142,6 +142,10 @@ CASES = {
                                   agg_P12_mx=4, rlx=18, coarse_th=9, solver=1, full=True),
     "lap7_20_agg1x2_pcg": dict(kind=7, n=(20, 20, 20), th=0.25, mxrs=1.0, Pmx=4, agg_nl=2, agg_interp=1, rlx=18,
                                coarse_th=9, solver=1, full=True),
+    "lap27_16_agg3_pcg": dict(kind=27, n=(16, 16, 16), th=0.5, mxrs=1.0, Pmx=4, agg_nl=1, agg_interp=3, rlx=18,
+                              coarse_th=9, solver=1, full=True),
+    "fv_14_agg3x2_p12_pcg": dict(gen="fv", n=(14,), seed=12, th=0.25, mxrs=0.9, Pmx=4, agg_nl=2, agg_interp=3,
+                                 agg_P12_mx=3, rlx=18, coarse_th=9, solver=1, full=True),
     "aniso_48_agg7_pcg": dict(gen="aniso", n=(48,), eps=0.001, th=0.25, mxrs=0.9, Pmx=4, agg_nl=1, agg_interp=7,
                               rlx=18, coarse_th=9, solver=1, full=True),
     # C/F relaxation (relax_order 1): C then F points on the way down, F then

@@ -266,12 +266,12 @@ def test_unsupported_options_are_refused(gb, oracle_mod):
     L.HYPRE_ClearAllErrors()
     amg.destroy()
     # aggressive interpolation types are checked at setup: the two-stage
-    # standard (2) and extended (3) ones are refused
+    # standard one (2) is refused
     I, J, V = oracle_mod.stencil(7, 8, 8, 8)
     n = len(I) - 1
     A = gb.IJMatrix(I, J, V)
     b, x = gb.IJVector(n, np.ones(n)), gb.IJVector(n, np.zeros(n))
-    for at, ok in ((2, False), (3, False), (8, True)):
+    for at, ok in ((2, False), (3, True), (8, True)):
         amg = gb.BoomerAMG(MaxRowSum=1.0, StrongThreshold=0.25, AggNumLevels=1, AggInterpType=at, Tol=0.0,
                            MaxIter=1)
         L.HYPRE_ClearAllErrors()
