@@ -132,7 +132,7 @@ def _declare(L):
                    "CycleType", "FCycle", "NumSweeps", "RelaxType", "RelaxOrder", "ChebyOrder", "ChebyScale",
                    "ChebyVariant", "ChebyEigEst", "PrintLevel", "Logging", "RAP2", "ModuleRAP2", "KeepTranspose"]
     real_setters = ["Tol", "StrongThreshold", "MaxRowSum", "TruncFactor", "AggTruncFactor", "AggP12TruncFactor",
-                    "RelaxWt", "ChebyFraction"]
+                    "RelaxWt", "OuterWt", "ChebyFraction"]
     for s in int_setters:
         fn = getattr(L, "HYPRE_BoomerAMGSet" + s)
         fn.argtypes = [vp, i32]

@@ -50,6 +50,7 @@ static void amg_defaults(gb_amg_params *p)
    p->cheby_scale = 1;
    p->cheby_eig_est = 10;
    p->cycle_type = 1;
+   p->outer_weight = 1.0;
    p->tol = 1.0e-6;
    p->max_iter = 20;
    p->cycle_prec = GB_PREC_F64;
@@ -1822,7 +1823,7 @@ static void hybrid_gs_d(gb_amg *amg, int l, int type, const double *f, double *u
    cudaStream_t s = gb_stream();
    const int n = L->n;
    if (u_zero) { gb_fill_d(n, u, 0.0, s); }
-   const double w = L->relax_w, omega = 1.0;
+   const double w = L->relax_w, omega = amg->prm.outer_weight;
    const int scaled = !(w == 1.0 && omega == 1.0);
    const int l1 = type == 8 || type == 13 || type == 14;
    const int skip = l1 ? scaled : 1;
@@ -1849,7 +1850,7 @@ static void hybrid_gs_f(gb_amg *amg, int l, int type, const float *f, float *u, 
    cudaStream_t s = gb_stream();
    const int n = L->n;
    if (u_zero) { gb_fill_f(n, u, 0.f, s); }
-   const double w = L->relax_w, omega = 1.0;
+   const double w = L->relax_w, omega = amg->prm.outer_weight;
    const int scaled = !(w == 1.0 && omega == 1.0);
    const int l1 = type == 8 || type == 13 || type == 14;
    const int skip = l1 ? scaled : 1;
@@ -2600,6 +2601,23 @@ HYPRE_Int HYPRE_BoomerAMGSetNumPaths(HYPRE_Solver solver, HYPRE_Int v)
       return gb_error_flag;
    }
    a->prm.num_paths = v;
+   return gb_error_flag;
+}
+
+/* outer weight omega of the hybrid Gauss-Seidel / SSOR smoothers on every
+ * level (par_amg.c:2611-2634); the CG-estimated weights (omega < 0) are not
+ * built */
+HYPRE_Int HYPRE_BoomerAMGSetOuterWt(HYPRE_Solver solver, HYPRE_Real v)
+{
+   gb_amg *a = amg_of(solver, 1);
+   if (!a) { return gb_error_flag; }
+   if (!(v > 0.0))
+   {
+      gb_error(HYPRE_ERROR_GENERIC, "outer_wt: positive weights are supported");
+      gb_error_in_arg(2);
+      return gb_error_flag;
+   }
+   a->prm.outer_weight = v;
    return gb_error_flag;
 }
 

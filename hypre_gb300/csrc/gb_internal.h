@@ -150,6 +150,7 @@ typedef struct
    int    num_sweeps[4];
    int    relax_order;       /* 0 lexicographic, 1 C/F (C then F down, F then C up) */
    double relax_weight;
+   double outer_weight;      /* omega of the hybrid Gauss-Seidel / SSOR smoothers (> 0) */
    double *level_relax_weight;   /* optional, per level */
    int    cheby_order, cheby_scale, cheby_variant, cheby_eig_est;
    double cheby_fraction;

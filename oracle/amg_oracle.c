@@ -69,6 +69,7 @@ void or_default_params(or_amg_params *p)
    p->cheby_scale = 1;
    p->cheby_eig_est = 10;
    p->cycle_type = 1;
+   p->outer_weight = 1.0;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -2223,7 +2224,7 @@ static void relax(or_hierarchy *H, int lvl, int type, const double *f, double *u
        * 13 forward, 14 backward, 8 symmetric (l1 norms; the diagonal term
        * stays in the sum unless weighted) */
       const int l1 = type == 8 || type == 13 || type == 14;
-      const double omega = 1.0;
+      const double omega = H->prm.outer_weight;   /* hypre_BoomerAMGSetOuterWt, par_amg.c:2611-2634 */
       const int skip = l1 ? !(w == 1.0 && omega == 1.0) : 1;
       relax_hybrid_gs(A, f, l1 ? H->l1[lvl] : NULL, w, omega, (type == 4 || type == 14) ? -1 : 1,
                       (type == 6 || type == 8) ? 2 : 1, skip, u, H->Ztmp, CF, pts);

@@ -56,6 +56,7 @@ typedef struct
    int    cycle_type;         /* 1 V, 2 W (visits of each coarse level per visit of the finer) */
    int    fcycle;             /* 0, or 1: F-cycle */
    int    pcg_rel_change;     /* PCG driven by this hierarchy: the relative-change test (pcg.c:836-843) */
+   double outer_weight;       /* 1.0: outer weight omega of the hybrid Gauss-Seidel / SSOR smoothers */
 } or_amg_params;
 
 typedef struct

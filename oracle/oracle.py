@@ -28,6 +28,7 @@ class Params(C.Structure):
         ("relax_weight", C.c_double), ("cheby_order", C.c_int), ("cheby_fraction", C.c_double),
         ("cheby_scale", C.c_int), ("cheby_variant", C.c_int), ("cheby_eig_est", C.c_int),
         ("relax_order", C.c_int), ("cycle_type", C.c_int), ("fcycle", C.c_int), ("pcg_rel_change", C.c_int),
+        ("outer_weight", C.c_double),
     ]
 
 

@@ -171,6 +171,7 @@ int main(int argc, char **argv)
    int max_levels = 25, dump_levels = 1, seed = 22775, cheby_order = 2, relax_order = 0;
    int coarsen = 8, precond = 1, keep_t = 0, rhs_ones = 0, cycle_type = 1, fcycle = 0, num_sweeps = 1;
    int rel_change = 0;
+   double outer_wt = 1.0;
    int repeat = 1, threads = 0, want_digest = 0, matmat = 0, relax_down = -1, relax_up = -1;
    const char *jsonfile = NULL;
    double cheby_fraction = 0.3;
@@ -215,6 +216,7 @@ int main(int argc, char **argv)
       else if (ARG("-fcycle")) { fcycle = atoi(argv[++a]); }
       else if (ARG("-ns")) { num_sweeps = atoi(argv[++a]); }
       else if (ARG("-rel_change")) { rel_change = atoi(argv[++a]); }
+      else if (ARG("-ow")) { outer_wt = atof(argv[++a]); }
       else if (ARG("-repeat")) { repeat = atoi(argv[++a]); }
       else if (ARG("-threads")) { threads = atoi(argv[++a]); }
       else if (ARG("-json")) { jsonfile = argv[++a]; }
@@ -353,6 +355,7 @@ int main(int argc, char **argv)
    if (relax_up >= 0) { HYPRE_BoomerAMGSetCycleRelaxType(amg, relax_up, 2); }
    HYPRE_BoomerAMGSetCycleRelaxType(amg, relax_coarse, 3);
    HYPRE_BoomerAMGSetRelaxWt(amg, relax_wt);
+   HYPRE_BoomerAMGSetOuterWt(amg, outer_wt);
    HYPRE_BoomerAMGSetRelaxOrder(amg, relax_order);
    HYPRE_BoomerAMGSetNumSweeps(amg, num_sweeps);
    HYPRE_BoomerAMGSetCycleNumSweeps(amg, 1, 3);

@@ -180,6 +180,11 @@ CASES = {
     "lap7_14_w_cf18_amg": dict(kind=7, n=(14, 14, 14), th=0.25, mxrs=1.0, Pmx=4, rlx=18, cycle_type=2,
                                relax_order=1, coarse_th=9, solver=0, precond=0, full=True),
     # PCG's relative-change test (x must also stop changing)
+    # SSOR / hybrid Gauss-Seidel with an outer weight (SetOuterWt)
+    "lap7_12_hgs6_ow09_pcg": dict(kind=7, n=(12, 12, 12), th=0.25, mxrs=1.0, Pmx=4, rlx=6, ow=0.9, coarse_th=9,
+                                  solver=1, full=True),
+    "lap27_12_hgs8_w08_ow12_pcg": dict(kind=27, n=(12, 12, 12), th=0.5, mxrs=1.0, Pmx=4, rlx=8, w=0.8, ow=1.2,
+                                       coarse_th=9, solver=1, full=True),
     "lap7_16_relchg_pcg": dict(kind=7, n=(16, 16, 16), th=0.25, mxrs=1.0, Pmx=4, rlx=18, rel_change=1, coarse_th=9,
                                solver=1, full=True),
     "fv_12_relchg_pcg": dict(gen="fv", n=(12,), seed=11, th=0.25, mxrs=0.9, Pmx=4, rlx=18, rel_change=1,
@@ -225,7 +230,7 @@ def dump_args(c, out):
         a = [DUMP, "-mat", mat]
     else:
         a = [DUMP, "-lap%d" % c["kind"]] + [str(v) for v in c["n"]]
-    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "relax_order", "cycle_type", "fcycle", "ns", "rel_change", "w",
+    for key in ("th", "mxrs", "Pmx", "tr", "interptype", "agg_nl", "agg_interp", "agg_Pmx", "agg_P12_mx", "max_levels", "precond", "rlx", "rlx_down", "rlx_up", "relax_order", "cycle_type", "fcycle", "ns", "rel_change", "ow", "w",
                 "coarse_th", "solver", "k", "cheby_order"):
         if key in c:
             a += ["-" + key, str(c[key])]

@@ -83,6 +83,8 @@ def oracle_params(c):
         p["num_sweeps"] = c["ns"]
     if "rel_change" in c:
         p["pcg_rel_change"] = c["rel_change"]
+    if "ow" in c:
+        p["outer_weight"] = c["ow"]
     if "max_levels" in c:
         p["max_levels"] = c["max_levels"]
     return p
@@ -110,6 +112,8 @@ def amg_params(c):
         p["FCycle"] = c["fcycle"]
     if "ns" in c:
         p["NumSweeps"] = c["ns"]
+    if "ow" in c:
+        p["OuterWt"] = c["ow"]
     if "max_levels" in c:
         p["MaxLevels"] = c["max_levels"]
     if "cheby_order" in c:
